@@ -1,0 +1,65 @@
+/*
+ * spx_oracle.h -- CPU restatement of SPECTRUM's test-particle stepping path (TEST ORACLE).
+ *
+ * This is test infrastructure, not product: only tests/, __graft_entry__.smoke() and the CPU
+ * baseline leg of bench.py may load it. It restates, in plain C, the per-trajectory algorithm of
+ * the reference (src/trajectory_base.cc, src/trajectory_parker.cc, src/trajectory_lorentz.cc,
+ * src/trajectory_focused.cc and the plugins they call), driven by the same plugin blobs and the
+ * same Philox random streams (oracle/spx_rng.h) as the CUDA library, so the CUDA results can be
+ * compared with it trajectory by trajectory. Its own parity with the reference is pinned by
+ * running the reference's sources through oracle/ref_glue (see tests/test_oracle_vs_reference.py).
+ */
+#ifndef SPX_ORACLE_H
+#define SPX_ORACLE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Final state of one trajectory; same fields as the reference harness output. */
+typedef struct {
+   uint32_t attempts;
+   uint32_t status;      /* reference TRAJ_* bits (src/trajectory_base.hh:45-57); 0x10000 = gave up */
+   uint64_t steps;
+   double t, pos[3], mom[3];
+   double t0, pos0[3], mom0[3];
+   double amp, logwgt;
+} spx_oracle_traj;
+
+typedef struct {
+   int traj_type;          /* 200 Lorentz, 205 Focused, 206 Parker, 207 Parker+source */
+   int time_flow;          /* 0 forward, 1 backward */
+   int rk;                 /* Butcher table number of common/rk_config.hh (0 or 25) */
+   int deriv_mode;         /* 0: the reference's compiled-in defaults; 1: analytic derivatives */
+   double steps_per_orbit; /* Lorentz orbit resolution (reference: 100, src/trajectory_lorentz.hh:26) */
+   int pa_scattering;      /* Focused: add the Euler pitch-angle scattering step */
+   int max_attempts;       /* retries of a discarded trajectory (src/simulation.cc:262-288) */
+} spx_oracle_opts;
+
+/*
+ * Run trajectories [first, first + n) of the problem in "spec" (format of
+ * oracle/ref_glue/harness.cc). traj_out may be NULL. counts/sums/n_events receive the
+ * distributions back to back in plugin order (sums has width 1, 3 or 9 doubles per bin);
+ * they are accumulated into, not cleared. Returns 0 or a negative error code; err gets a message.
+ */
+int spx_oracle_run(const uint8_t* spec, size_t spec_len, const spx_oracle_opts* opts, uint32_t first,
+                   uint32_t n, spx_oracle_traj* traj_out, int32_t* counts, double* sums, int64_t* n_events,
+                   char* err, size_t err_len);
+
+/* Sizes of the distributions of a spec: returns the number of distributions, fills up to
+ * "max" entries of n_bins[] and width[]. Negative on a malformed spec. */
+int spx_oracle_distro_sizes(const uint8_t* spec, size_t spec_len, int max, int64_t* n_bins, int* width);
+
+/* The four normals of one step block and four uniforms of one init block, for RNG cross-checks. */
+void spx_oracle_normals(uint64_t seed, uint32_t index, uint32_t traj, uint32_t problem, uint32_t attempt,
+                        double out[4]);
+void spx_oracle_uniforms(uint64_t seed, uint32_t index, uint32_t traj, uint32_t problem, uint32_t attempt,
+                         double out[4]);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,114 @@
+"""A simulation problem: configure-time physics choices plus a list of set-up plugins.
+
+The reference fixes the trajectory type, time flow and Runge-Kutta table at configure time
+(configure.ac:236-295) and receives every plugin as ``Add*(Prototype(), DataContainer)``. A
+``Problem`` records the same information in a form that can be handed to the C ABI
+(``spx_create`` + ``spx_add_plugin``) or serialised for the reference's own code (the oracle
+harness reads the byte format written by ``to_spec``).
+"""
+from __future__ import annotations
+
+import struct
+from dataclasses import dataclass, field
+
+from . import plugins as P
+from .datacontainer import DataContainer
+
+# trajectory types: the reference's configure.ac:236-244 numbering
+TRAJ_LORENTZ = 200
+TRAJ_FOCUSED = 205
+TRAJ_PARKER = 206
+TRAJ_PARKER_SOURCE = 207
+TRAJ_NAMES = {TRAJ_LORENTZ: "TrajectoryLorentz", TRAJ_FOCUSED: "TrajectoryFocused",
+              TRAJ_PARKER: "TrajectoryParker", TRAJ_PARKER_SOURCE: "TrajectoryParkerSource"}
+
+FORWARD = 0
+BACKWARD = 1
+
+
+@dataclass
+class PluginEntry:
+    plugin: P.Plugin
+    blob: bytes
+    n_records: int
+
+
+@dataclass
+class Problem:
+    traj: int = TRAJ_PARKER
+    time_flow: int = FORWARD
+    rk: int = 0
+    plugins: list[PluginEntry] = field(default_factory=list)
+    seed: int = 0x5EED0000
+    n_traj: int = 1000
+    problem_id: int = 0
+    #: options of the stepping kernel (see include/spx.h, SPX_OPT_*)
+    options: dict[int, float] = field(default_factory=dict)
+
+    def add(self, plugin: P.Plugin, container: DataContainer) -> "Problem":
+        self.plugins.append(PluginEntry(plugin, container.data(), container.size()))
+        return self
+
+    # reference-style method names
+    def AddBackground(self, proto, c):  # noqa: N802
+        return self._add_role(P.ROLE_BACKGROUND, proto, c)
+
+    def AddDiffusion(self, proto, c):  # noqa: N802
+        return self._add_role(P.ROLE_DIFFUSION, proto, c)
+
+    def AddSource(self, proto, c):  # noqa: N802
+        return self._add_role(P.ROLE_SOURCE, proto, c)
+
+    def AddBoundary(self, proto, c):  # noqa: N802
+        return self._add_role(P.ROLE_BOUNDARY, proto, c)
+
+    def AddInitial(self, proto, c):  # noqa: N802
+        return self._add_role(P.ROLE_INITIAL, proto, c)
+
+    def AddDistribution(self, proto, c):  # noqa: N802
+        return self._add_role(P.ROLE_DISTRIBUTION, proto, c)
+
+    def _add_role(self, role, proto, c):
+        if proto.role != role:
+            raise TypeError(f"{proto.name} is not a {P.ROLE_NAMES[role]} plugin")
+        return self.add(proto, c)
+
+    def replace(self, role: int, slot: int, plugin: P.Plugin, container: DataContainer) -> "Problem":
+        """Replace the ``slot``-th plugin of ``role`` (used to derive batched problems)."""
+        idx = [i for i, e in enumerate(self.plugins) if e.plugin.role == role]
+        self.plugins[idx[slot]] = PluginEntry(plugin, container.data(), container.size())
+        return self
+
+    def distributions(self) -> list[PluginEntry]:
+        return [e for e in self.plugins if e.plugin.role == P.ROLE_DISTRIBUTION]
+
+    def normals_per_step(self) -> int:
+        """Normal draws per step of the trajectory type (3 for Parker: src/trajectory_parker.cc:159-180)."""
+        if self.traj in (TRAJ_PARKER, TRAJ_PARKER_SOURCE):
+            return 3
+        return 1
+
+    def to_spec(self, max_attempts: int = 100) -> bytes:
+        """Serialise for the oracle harness (format documented in oracle/ref_glue/harness.cc)."""
+        out = bytearray(b"SPXS")
+        out += struct.pack("<IQIIIII", 1, self.seed, self.n_traj, self.problem_id,
+                           self.normals_per_step(), max_attempts, len(self.plugins))
+        for e in self.plugins:
+            name = e.plugin.name.encode()
+            out += struct.pack("<II", e.plugin.role, len(name)) + name
+            out += struct.pack("<II", e.n_records, len(e.blob)) + e.blob
+        return bytes(out)
+
+
+def distro_header(c: DataContainer, n_bins, minval, maxval, log_bins=(0, 0, 0), bin_outside=(0, 0, 0),
+                  unit_distro=1.0, unit_val=(1.0, 1.0, 1.0), keep_records=False, width=1) -> DataContainer:
+    """The DistributionTemplated part of a distribution container (src/distribution_templated.cc:92-108)."""
+    c.mi(n_bins).vec(minval).vec(maxval).mi(log_bins).mi(bin_outside)
+    if width == 1:
+        c.double(unit_distro)
+    elif width == 3:
+        c.vec(unit_distro if hasattr(unit_distro, "__len__") else (unit_distro,) * 3)
+    else:
+        c.mat([[unit_distro] * 3] * 3)
+    c.vec(unit_val).bool(keep_records)
+    return c

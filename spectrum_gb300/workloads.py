@@ -1,0 +1,264 @@
+"""The five benchmark workloads, set up the way a reference user would set them up.
+
+Each builder fills a ``Problem`` with ``Add*(Prototype(), DataContainer)`` calls in the order and
+with the parameter layout of the reference's own mains (benchmarks/main_test_full_diff.cc:37-244,
+runs/gcr_modulation_example.cc:76-332, benchmarks/main_test_dipole_periods.cc:42-72). Inputs are
+synthetic; seeds are fixed (``0x5eed0000 + workload number``; problem p of a batch uses
+problem id p).
+
+  1  pure spatial diffusion        Parker fwd, uniform B, kappa = 1, t = 1, 3-D position histogram
+  2  diffusive shock acceleration  Parker fwd, smooth planar shock s = 4, log-p histogram
+  3  dipole Lorentz orbits         Lorentz RK4, dipole, log-uniform E, L in [2,6], pitch band
+  4  GCR modulation                Parker bwd, Parker spiral, 32 energies, LIS-weighted spectrum
+  5  focused transport             Focused RK4 + pitch-angle scattering, 64 problems, (t, mu)
+
+Sizes default to the full workload; every builder takes ``n_traj`` (per problem) so tests can
+shrink them.
+"""
+from __future__ import annotations
+
+import math
+
+from . import units as U
+from .datacontainer import DataContainer
+from .plugins import (BackgroundDipole, BackgroundSmoothShock, BackgroundSolarWind, BackgroundUniform,
+                      BoundaryMomentumInject, BoundaryPlaneAbsorb, BoundarySphereAbsorb, BoundarySpherePass,
+                      BoundaryTimeExpire, DiffusionFullConstant, DiffusionIsotropicConstant,
+                      DiffusionRigidityMagneticFieldPowerLaw, DistributionMomentumUniform,
+                      DistributionPositionUniform, DistributionSpectrumKineticEnergyPowerLaw,
+                      DistributionTimeMu, DistributionTimeUniform, InitialMomentumLogEnergyPitchBand,
+                      InitialMomentumShell, InitialSpaceEquatorialBand, InitialSpaceFixed, InitialTimeFixed)
+from .problem import BACKWARD, FORWARD, TRAJ_FOCUSED, TRAJ_LORENTZ, TRAJ_PARKER, Problem, distro_header
+
+ONE_AU = U.ASTRONOMICAL_UNIT / U.unit_length
+SEED_BASE = 0x5EED0000
+
+
+def _boundary(c: DataContainer, max_crossings: int, actions) -> DataContainer:
+    """BoundaryBase header: int max_crossings, std::vector<int> actions (src/boundary_base.cc:138-141)."""
+    return c.int(max_crossings).ints(actions)
+
+
+# ------------------------------------------------------------------------------------------------
+# 1. pure spatial diffusion
+# ------------------------------------------------------------------------------------------------
+def diffusion_uniform(n_traj: int = 100_000, kappa: float = 1.0, t_end: float = 1.0, dt: float = 1.0e-3,
+                      n_bins: int = 100, half_width: float = 6.0) -> Problem:
+    """Parker forward, uniform B along z, U = 0, constant isotropic kappa.
+
+    dt is not an input of the reference: it is min(dt_physical, dt_adaptive) with the diffusive
+    bound 0.5 * dmax^2 / max(kappa) (src/trajectory_parker.cc:212-221). dmax0 is therefore chosen
+    as sqrt(2 * kappa * dt) so that the step is ``dt``.
+    """
+    pb = Problem(traj=TRAJ_PARKER, time_flow=FORWARD, rk=0, seed=SEED_BASE + 1, n_traj=n_traj)
+    dmax0 = math.sqrt(2.0 * kappa * dt)
+    c = DataContainer()
+    c.double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0.0, 0.0, 1.0)).double(dmax0)
+    pb.AddBackground(BackgroundUniform(), c)
+    pb.AddInitial(InitialTimeFixed(), DataContainer().double(0.0))
+    pb.AddInitial(InitialSpaceFixed(), DataContainer().vec((0, 0, 0)))
+    pb.AddInitial(InitialMomentumShell(), DataContainer().double(1.0))
+    pb.AddDiffusion(DiffusionFullConstant(), DataContainer().double(kappa).double(kappa))
+    pb.AddBoundary(BoundaryTimeExpire(), _boundary(DataContainer(), 1, [0]).double(t_end))
+    c = distro_header(DataContainer(), (n_bins,) * 3, (-half_width,) * 3, (half_width,) * 3)
+    c.double(1.0).double(0.0).int(1).int(0)        # val_hot, val_cold, val_time, val_coord
+    pb.AddDistribution(DistributionPositionUniform(), c)
+    return pb
+
+
+# ------------------------------------------------------------------------------------------------
+# 2. diffusive shock acceleration
+# ------------------------------------------------------------------------------------------------
+def shock_acceleration(n_traj: int = 10_000_000, s: float = 4.0, u1: float = 1.0, kappa: float = 1.0,
+                       width_frac: float = 1.0e-3, p_max: float = 1.0e3, x_escape: float = -10.0,
+                       x_downstream: float = 10.0, n_bins: int = 200, dmax_fraction: float = 0.1) -> Problem:
+    """Parker forward in a smooth planar shock; injection at the shock with p0 = 1.
+
+    The shock normal points upstream (-x): the flow u0 = (U1, 0, 0) enters from x < 0 and is
+    compressed by ``s`` behind the shock at x = 0 (src/background_shock.cc:58-80). The width is
+    ``width_frac`` of the diffusion length kappa/U1. Trajectories end at the momentum boundary
+    p_max (recorded), at the free-escape plane x = x_escape upstream, or at the downstream
+    escape plane x = x_downstream (both recorded with their own action so the spectrum can be
+    formed from the momentum reached). The recorded value is p at termination.
+    """
+    pb = Problem(traj=TRAJ_PARKER, time_flow=FORWARD, rk=0, seed=SEED_BASE + 2, n_traj=n_traj)
+    width = width_frac * kappa / u1
+    dmax0 = 0.05 * kappa / u1
+    c = DataContainer()
+    c.double(0.0).vec((0, 0, 0)).vec((u1, 0, 0)).vec((1.0, 0.0, 0.0)).double(dmax0)
+    c.vec((-1.0, 0.0, 0.0)).double(0.0).double(s)          # n_shock, v_shock, compression
+    c.double(width).double(dmax_fraction)                  # width_shock, dmax_fraction
+    pb.AddBackground(BackgroundSmoothShock(), c)
+    pb.AddInitial(InitialTimeFixed(), DataContainer().double(0.0))
+    pb.AddInitial(InitialSpaceFixed(), DataContainer().vec((0, 0, 0)))
+    pb.AddInitial(InitialMomentumShell(), DataContainer().double(1.0))
+    pb.AddDiffusion(DiffusionFullConstant(), DataContainer().double(kappa).double(kappa))
+    pb.AddBoundary(BoundaryTimeExpire(), _boundary(DataContainer(), 1, [-1]).double(1.0e6 * kappa / u1 ** 2))
+    pb.AddBoundary(BoundaryPlaneAbsorb(), _boundary(DataContainer(), 1, [0]).vec((x_escape, 0, 0)).vec((-1, 0, 0)))
+    pb.AddBoundary(BoundaryPlaneAbsorb(), _boundary(DataContainer(), 1, [0]).vec((x_downstream, 0, 0)).vec((1, 0, 0)))
+    pb.AddBoundary(BoundaryMomentumInject(), _boundary(DataContainer(), 1, [0]).double(p_max))
+    c = distro_header(DataContainer(), (n_bins, 0, 0), (1.0, 0, 0), (p_max * 1.0000001, 0, 0), log_bins=(1, 0, 0),
+                      bin_outside=(1, 0, 0))
+    c.double(1.0).double(0.0).int(1).int(0)                # val_hot, val_cold, val_time, val_coord
+    pb.AddDistribution(DistributionMomentumUniform(), c)
+    return pb
+
+
+# ------------------------------------------------------------------------------------------------
+# 3. Lorentz orbits in a dipole
+# ------------------------------------------------------------------------------------------------
+R_EARTH_CM = 6.37e8
+B_EARTH_G = 0.311
+
+
+def dipole_orbits(n_traj: int = 1_000_000, e1_mev: float = 1.0, e2_mev: float = 100.0, l1: float = 2.0,
+                  l2: float = 6.0, pitch_deg=(10.0, 170.0), steps_per_orbit: int = 32,
+                  n_drift_periods: float = 100.0, t_end: float | None = None) -> Problem:
+    """Full orbits in an Earth-like dipole (benchmarks/main_test_dipole_periods.cc:42-72).
+
+    The drift-period scale of the slowest particle (1 MeV at L = 2) sets the default time limit
+    of ``n_drift_periods`` periods; ``t_end`` overrides it (tests use a few gyroperiods).
+    """
+    pb = Problem(traj=TRAJ_LORENTZ, time_flow=FORWARD, rk=25, seed=SEED_BASE + 3, n_traj=n_traj)
+    r_e = R_EARTH_CM / U.unit_length
+    b_eq = B_EARTH_G / U.unit_magnetic
+    c = DataContainer()
+    c.double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0.0, 0.0, -b_eq)).double(0.1 * r_e)
+    c.double(r_e).double(0.1)                              # r_ref, dmax_fraction
+    pb.AddBackground(BackgroundDipole(), c)
+    pb.AddInitial(InitialTimeFixed(), DataContainer().double(0.0))
+    pb.AddInitial(InitialSpaceEquatorialBand(), DataContainer().vec((0, 0, 0)).double(r_e).double(l1).double(l2))
+    mu_lo = math.cos(math.radians(pitch_deg[1]))
+    mu_hi = math.cos(math.radians(pitch_deg[0]))
+    pb.AddInitial(InitialMomentumLogEnergyPitchBand(),
+                  DataContainer().double(e1_mev * U.MEV / U.unit_energy).double(e2_mev * U.MEV / U.unit_energy)
+                  .double(mu_lo).double(mu_hi))
+    if t_end is None:
+        # drift period (s) ~ 3600*1.05/(E_MeV * L * (1+0.43)) for equatorial pitch
+        # (benchmarks/main_test_dipole_periods.cc:129-130)
+        t_drift = 3600.0 * 1.05 / (e1_mev * l1 * 1.43) / U.unit_time
+        t_end = n_drift_periods * t_drift
+    pb.AddBoundary(BoundaryTimeExpire(), _boundary(DataContainer(), 1, [0]).double(t_end))
+    pb.AddBoundary(BoundarySphereAbsorb(), _boundary(DataContainer(), 1, [1]).vec((0, 0, 0)).double(r_e))
+    c = distro_header(DataContainer(), (64, 32, 0), (e1_mev * U.MEV / U.unit_energy * 0.5, -1.0, 0.0),
+                      (e2_mev * U.MEV / U.unit_energy * 2.0, 1.0, 1.0), log_bins=(1, 0, 0), bin_outside=(1, 1, 0))
+    c.double(1.0).double(0.0).int(1).int(1)
+    pb.AddDistribution(DistributionMomentumUniform(), c)
+    pb.options[SPX_OPT_STEPS_PER_ORBIT] = float(steps_per_orbit)
+    return pb
+
+
+# ------------------------------------------------------------------------------------------------
+# 4. GCR modulation in the Parker spiral (backward in time)
+# ------------------------------------------------------------------------------------------------
+def solarwind_params(c: DataContainer, dmax0: float = ONE_AU) -> DataContainer:
+    """BackgroundSolarWind container of runs/gcr_modulation_example.cc:40-78: 400 km/s radial wind,
+    |B| = 5 nT at 1 AU scaled from r_ref = 3 solar radii, 25-day rotation about +z."""
+    umag = 4.0e7 / U.unit_velocity
+    rs = 6.957e10 / U.unit_length
+    r_ref = 3.0 * rs
+    bmag_e = 5.0e-5 / U.unit_magnetic
+    bmag_ref = bmag_e * (ONE_AU / r_ref) ** 2
+    w0 = 2.0 * math.pi / (25.0 * 24.0 * 3600.0) * U.unit_time
+    c.double(0.0).vec((0, 0, 0)).vec((umag, 0, 0)).vec((bmag_ref, 0, 0)).double(dmax0)
+    c.vec((0.0, 0.0, w0)).double(r_ref).double(0.1)
+    return c
+
+
+BMAG_1AU = 5.0e-5 / U.unit_magnetic
+
+
+def modulation_energies(n: int = 32, e1_mev: float = 10.0, e2_mev: float = 1.0e4) -> list[float]:
+    return [e1_mev * (e2_mev / e1_mev) ** (i / (n - 1)) for i in range(n)] if n > 1 else [e1_mev]
+
+
+def gcr_modulation(n_traj: int = 1_000_000, energies_mev=None, lam0_au: float = 0.1, pow_law_r: float = 0.5,
+                   pow_law_b: float = -1.0, kap_rat: float = 0.02, r_inner_au: float = 0.05,
+                   r_outer_au: float = 100.0, t_max_years: float = 2.0, lis_gamma: float = -1.8) -> list[Problem]:
+    """One problem per energy: start at 1 AU, trace backward until the 100 AU outer boundary
+    (hot: weighted by the LIS J0 (T/T0)^gamma / p^2 * v, src/distribution_other.cc:553-602), the
+    0.05 AU inner boundary (cold) or the time limit.
+
+    kappa_par = (lam0 v / 3)(R/R0)^0.5 (B/B0)^pow_law_b, kappa_perp = kap_rat kappa_par
+    (src/diffusion_other.cc:804-809); the run example uses pow_law_b = -1.
+    """
+    if energies_mev is None:
+        energies_mev = modulation_energies()
+    out = []
+    t_max = t_max_years * 365.0 * 24.0 * 3600.0 / U.unit_time
+    r0_rig = 3.33e6 / (U.unit_energy / U.unit_charge)
+    unit_distro = 1.0 / (U.unit_length ** 2 * U.unit_time * 4.0 * math.pi * U.unit_energy)
+    for p_idx, e in enumerate(energies_mev):
+        pb = Problem(traj=TRAJ_PARKER, time_flow=BACKWARD, rk=0, seed=SEED_BASE + 4, n_traj=n_traj, problem_id=p_idx)
+        pb.AddBackground(BackgroundSolarWind(), solarwind_params(DataContainer()))
+        pb.AddInitial(InitialTimeFixed(), DataContainer().double(0.0))
+        pb.AddInitial(InitialSpaceFixed(), DataContainer().vec((ONE_AU, 0, 0)))
+        p0 = U.mev_to_mom(e)
+        pb.AddInitial(InitialMomentumShell(), DataContainer().double(p0))
+        pb.AddBoundary(BoundarySphereAbsorb(), _boundary(DataContainer(), 1, [1]).vec((0, 0, 0)).double(r_inner_au * ONE_AU))
+        pb.AddBoundary(BoundarySphereAbsorb(), _boundary(DataContainer(), 1, [0]).vec((0, 0, 0)).double(r_outer_au * ONE_AU))
+        pb.AddBoundary(BoundaryTimeExpire(), _boundary(DataContainer(), 1, [-1]).double(-t_max))
+        pb.AddDiffusion(DiffusionRigidityMagneticFieldPowerLaw(),
+                        DataContainer().double(lam0_au * ONE_AU).double(r0_rig).double(BMAG_1AU)
+                        .double(pow_law_r).double(pow_law_b).double(kap_rat))
+        t1 = U.EnrKin(U.mev_to_mom(energies_mev[0])) * 0.5
+        t2 = U.EnrKin(U.mev_to_mom(energies_mev[-1])) * 2.0
+        c = distro_header(DataContainer(), (len(energies_mev) * 4, 0, 0), (t1, 0, 0), (t2, 0, 0), log_bins=(1, 0, 0),
+                          unit_distro=unit_distro, unit_val=(U.unit_energy, 1.0, 1.0))
+        c.double(1.0 / unit_distro).double(1.0 * U.GEV / U.unit_energy).double(lis_gamma).double(0.0)
+        pb.AddDistribution(DistributionSpectrumKineticEnergyPowerLaw(), c)
+        out.append(pb)
+    return out
+
+
+# ------------------------------------------------------------------------------------------------
+# 5. focused transport with pitch-angle scattering
+# ------------------------------------------------------------------------------------------------
+def focused_transport(n_problems: int = 64, n_min: int = 1000, n_max: int = 1_000_000, lam_au=(0.01, 1.0),
+                      e_mev=(1.0, 100.0), t_max_hours: float = 48.0, n_t: int = 256, n_mu: int = 32,
+                      n_traj: int | None = None, seed_offset: int = 5) -> list[Problem]:
+    """64 problems in the Parker spiral: impulsive injection at 0.1 AU, isotropic, mono-energetic
+    per problem (log-uniform draw in [1, 100] MeV), mean free path log-uniform in [0.01, 1] AU,
+    trajectory count log-uniform in [1e3, 1e6]; an observer sphere at 1 AU records (t, mu) of
+    every crossing (256 x 32 bins). Pitch-angle scattering uses D_mumu = D0 (1 - mu^2)
+    (src/diffusion_other.cc:64-79) with D0 = v / lambda: then kappa_par =
+    (v^2/4) int (1-mu^2)^2 / D_mumu dmu = v^2 / (3 D0), so the parallel mean free path
+    3 kappa_par / v equals lambda.
+    The parameters of problem p come from a fixed-seed generator so the batch is reproducible.
+    """
+    import random
+    rnd = random.Random(SEED_BASE + seed_offset)
+    out = []
+    t_max = t_max_hours * 3600.0 / U.unit_time
+    for p_idx in range(n_problems):
+        count = int(round(math.exp(rnd.uniform(math.log(n_min), math.log(n_max)))))
+        lam = math.exp(rnd.uniform(math.log(lam_au[0]), math.log(lam_au[1]))) * ONE_AU
+        e = math.exp(rnd.uniform(math.log(e_mev[0]), math.log(e_mev[1])))
+        p0 = U.mev_to_mom(e)
+        v = U.Vel(p0)
+        d0 = v / lam
+        pb = Problem(traj=TRAJ_FOCUSED, time_flow=FORWARD, rk=25, seed=SEED_BASE + seed_offset,
+                     n_traj=n_traj if n_traj is not None else count, problem_id=p_idx)
+        pb.AddBackground(BackgroundSolarWind(), solarwind_params(DataContainer()))
+        pb.AddInitial(InitialTimeFixed(), DataContainer().double(0.0))
+        pb.AddInitial(InitialSpaceFixed(), DataContainer().vec((0.1 * ONE_AU, 0, 0)))
+        pb.AddInitial(InitialMomentumShell(), DataContainer().double(p0))
+        pb.AddDiffusion(DiffusionIsotropicConstant(), DataContainer().double(d0))
+        pb.AddBoundary(BoundaryTimeExpire(), _boundary(DataContainer(), 1, [-1]).double(t_max))
+        pb.AddBoundary(BoundarySphereAbsorb(), _boundary(DataContainer(), 1, [-1]).vec((0, 0, 0)).double(0.05 * ONE_AU))
+        pb.AddBoundary(BoundarySphereAbsorb(), _boundary(DataContainer(), 1, [-1]).vec((0, 0, 0)).double(5.0 * ONE_AU))
+        pb.AddBoundary(BoundarySpherePass(), _boundary(DataContainer(), -1, [0]).vec((0, 0, 0)).double(ONE_AU))
+        c = distro_header(DataContainer(), (n_t, n_mu, 0), (0.0, -1.0, 0.0), (t_max, 1.0, 1.0),
+                          unit_val=(U.unit_time, 1.0, 1.0))
+        c.double(1.0).double(0.0)
+        pb.AddDistribution(DistributionTimeMu(), c)
+        pb.options[SPX_OPT_PA_SCATTERING] = 1.0
+        out.append(pb)
+    return out
+
+
+# option numbers (include/spx.h)
+SPX_OPT_STEPS_PER_ORBIT = 1
+SPX_OPT_DERIV_MODE = 2
+SPX_OPT_PA_SCATTERING = 3
+SPX_OPT_RECORD_FINAL = 4

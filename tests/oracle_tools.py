@@ -1,0 +1,166 @@
+"""Test-side access to the oracles: the C restatement (oracle/_build/libspx_oracle.so) and, where
+the reference sources are present, the reference itself (oracle/_ref/ref_*).
+
+This module is test infrastructure. It is imported by tests/, by __graft_entry__.smoke() and by
+the CPU-baseline leg of bench.py, and by nothing in the product package.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import struct
+import subprocess
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+ORACLE_DIR = os.path.join(ROOT, "oracle")
+ORACLE_LIB = os.path.join(ORACLE_DIR, "_build", "libspx_oracle.so")
+REF_DIR = os.path.join(ORACLE_DIR, "_ref")
+
+TRAJ_DTYPE = np.dtype([("attempts", "<u4"), ("status", "<u4"), ("steps", "<u8"), ("t", "<f8"), ("pos", "<f8", 3),
+                       ("mom", "<f8", 3), ("t0", "<f8"), ("pos0", "<f8", 3), ("mom0", "<f8", 3), ("amp", "<f8"),
+                       ("logwgt", "<f8")])
+
+
+class _Opts(ctypes.Structure):
+    _fields_ = [("traj_type", ctypes.c_int), ("time_flow", ctypes.c_int), ("rk", ctypes.c_int),
+                ("deriv_mode", ctypes.c_int), ("steps_per_orbit", ctypes.c_double),
+                ("pa_scattering", ctypes.c_int), ("max_attempts", ctypes.c_int)]
+
+
+def build_oracle() -> str:
+    """Compile the C restatement (gcc only; a second or two)."""
+    subprocess.run(["make", "-s", "-C", ORACLE_DIR, "all"], check=True)
+    return ORACLE_LIB
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(ORACLE_LIB):
+            build_oracle()
+        _lib = ctypes.CDLL(ORACLE_LIB)
+        _lib.spx_oracle_run.restype = ctypes.c_int
+        _lib.spx_oracle_distro_sizes.restype = ctypes.c_int
+    return _lib
+
+
+def distro_sizes(spec: bytes):
+    nb = (ctypes.c_int64 * 8)()
+    w = (ctypes.c_int * 8)()
+    n = lib().spx_oracle_distro_sizes(spec, ctypes.c_size_t(len(spec)), 8, nb, w)
+    if n < 0:
+        raise ValueError("malformed spec")
+    return [(int(nb[i]), int(w[i])) for i in range(n)]
+
+
+class OracleResult:
+    def __init__(self, traj, distros):
+        self.traj = traj
+        #: list of (counts int32[n], sums float64[n, width], n_events)
+        self.distros = distros
+
+
+def run_oracle(problem, first: int = 0, n: int | None = None, deriv_mode: int = 0, steps_per_orbit: float | None = None,
+               pa_scattering: int | None = None, max_attempts: int = 100, record: bool = True) -> OracleResult:
+    """Run the C restatement on ``problem`` (a spectrum_gb300.problem.Problem)."""
+    from spectrum_gb300.workloads import SPX_OPT_PA_SCATTERING, SPX_OPT_STEPS_PER_ORBIT
+    spec = problem.to_spec()
+    n = problem.n_traj if n is None else n
+    if steps_per_orbit is None:
+        steps_per_orbit = problem.options.get(SPX_OPT_STEPS_PER_ORBIT, 100.0)
+    if pa_scattering is None:
+        pa_scattering = int(problem.options.get(SPX_OPT_PA_SCATTERING, 0))
+    opts = _Opts(problem.traj, problem.time_flow, problem.rk, deriv_mode, float(steps_per_orbit), pa_scattering,
+                 max_attempts)
+    sizes = distro_sizes(spec)
+    tot = sum(s for s, _ in sizes)
+    counts = np.zeros(max(tot, 1), dtype=np.int32)
+    sums = np.zeros(max(sum(s * w for s, w in sizes), 1), dtype=np.float64)
+    nev = np.zeros(max(len(sizes), 1), dtype=np.int64)
+    traj = np.zeros(n if record else 0, dtype=TRAJ_DTYPE)
+    err = ctypes.create_string_buffer(256)
+    rc = lib().spx_oracle_run(spec, ctypes.c_size_t(len(spec)), ctypes.byref(opts), ctypes.c_uint32(first),
+                              ctypes.c_uint32(n), traj.ctypes.data_as(ctypes.c_void_p) if record else None,
+                              counts.ctypes.data_as(ctypes.c_void_p), sums.ctypes.data_as(ctypes.c_void_p),
+                              nev.ctypes.data_as(ctypes.c_void_p), err, ctypes.c_size_t(256))
+    if rc != 0:
+        raise RuntimeError(f"oracle error {rc}: {err.value.decode()}")
+    distros = []
+    off = 0
+    soff = 0
+    for d, (nb, w) in enumerate(sizes):
+        distros.append((counts[off:off + nb].copy(), sums[soff:soff + nb * w].reshape(nb, w).copy(), int(nev[d])))
+        off += nb
+        soff += nb * w
+    return OracleResult(traj, distros)
+
+
+def oracle_normals(seed, index, traj, problem=0, attempt=0):
+    out = (ctypes.c_double * 4)()
+    lib().spx_oracle_normals(ctypes.c_uint64(seed), ctypes.c_uint32(index), ctypes.c_uint32(traj),
+                             ctypes.c_uint32(problem), ctypes.c_uint32(attempt), out)
+    return np.array(list(out))
+
+
+def oracle_uniforms(seed, index, traj, problem=0, attempt=0):
+    out = (ctypes.c_double * 4)()
+    lib().spx_oracle_uniforms(ctypes.c_uint64(seed), ctypes.c_uint32(index), ctypes.c_uint32(traj),
+                              ctypes.c_uint32(problem), ctypes.c_uint32(attempt), out)
+    return np.array(list(out))
+
+
+# -- the reference itself (only where oracle/_ref was built from the reference sources) --------
+REF_VARIANTS = {(206, 0, 0): "parker_fwd_rk0", (206, 1, 0): "parker_bwd_rk0", (207, 1, 0): "parkersrc_bwd_rk0",
+                (200, 0, 25): "lorentz_fwd_rk25", (205, 0, 25): "focused_fwd_rk25"}
+
+
+def ref_binary(problem) -> str | None:
+    v = REF_VARIANTS.get((problem.traj, problem.time_flow, problem.rk))
+    if v is None:
+        return None
+    path = os.path.join(REF_DIR, "ref_" + v)
+    return path if os.path.exists(path) else None
+
+
+def parse_ref_output(buf: bytes, sizes) -> OracleResult:
+    if buf[:4] != b"SPXR":
+        raise ValueError("bad reference output")
+    n, nd = struct.unpack_from("<II", buf, 4)
+    pos = 12
+    traj = np.frombuffer(buf, dtype=TRAJ_DTYPE, count=n, offset=pos).copy()
+    pos += n * TRAJ_DTYPE.itemsize
+    distros = []
+    for _ in range(nd):
+        nb, w = struct.unpack_from("<II", buf, pos)
+        pos += 8
+        counts = np.frombuffer(buf, dtype=np.int32, count=nb, offset=pos).copy()
+        pos += 4 * nb
+        sums = np.frombuffer(buf, dtype=np.float64, count=nb * w, offset=pos).reshape(nb, w).copy()
+        pos += 8 * nb * w
+        (nev,) = struct.unpack_from("<i", buf, pos)
+        pos += 4
+        distros.append((counts, sums, nev))
+    return OracleResult(traj, distros)
+
+
+def run_reference(problem, timeout: float = 600.0) -> OracleResult:
+    """Run the reference's own code (oracle/_ref) on ``problem``."""
+    exe = ref_binary(problem)
+    if exe is None:
+        raise FileNotFoundError("reference harness not built for this trajectory type")
+    with tempfile.TemporaryDirectory() as td:
+        spec_path = os.path.join(td, "spec.bin")
+        out_path = os.path.join(td, "out.bin")
+        with open(spec_path, "wb") as f:
+            f.write(problem.to_spec())
+        r = subprocess.run([exe, spec_path, out_path], capture_output=True, text=True, timeout=timeout)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference harness failed: {r.stderr[-2000:]}")
+        with open(out_path, "rb") as f:
+            return parse_ref_output(f.read(), None)
