@@ -1,0 +1,164 @@
+/*
+ * spx.h -- C ABI of spectrum_gb300, the GB300 (sm_103a) implementation of SPECTRUM's
+ * test-particle stepping path (the per-trajectory loop of the method of stochastic
+ * characteristics).
+ *
+ * The reference exposes this path as a C++ plugin surface: a user builds DataContainer
+ * parameter blobs and calls SimulationWorker::Add{Background,Diffusion,Source,Boundary,Initial,
+ * Distribution}, SetTasks, MainLoop and reads the distributions back (src/simulation.hh:93-138;
+ * each Add* clones a prototype and calls SetupObject, src/trajectory_base.cc:644-741). This ABI
+ * carries the same information across a plain-C boundary: plugins arrive as the reference's own
+ * DataContainer bytes (common/data_container.cc:139-224: per record one size byte then the
+ * payload), configure-time choices (configure.ac:236-295) arrive as spx_create arguments, and the
+ * MPI trajectory farm (src/simulation.cc:253-305, 743-767) is replaced by one device-resident
+ * launch. Nothing here allocates on behalf of the caller's buffers; blobs are copied at call
+ * time. All device work is ordered on the context's own CUDA stream.
+ *
+ * Reference exceptions map to return codes (below); per-trajectory failures (the reference's
+ * TRAJ_DISCARD, src/trajectory_base.cc:964-992) are retried with a new random stream, as
+ * src/simulation.cc:262-288 does, and counted in spx_stats instead of being returned.
+ */
+#ifndef SPX_H
+#define SPX_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- return codes ---------------------------------------------------------------------- */
+#define SPX_OK 0
+#define SPX_ERR_INVALID_ARG -1      /* null pointer, unknown enum value */
+#define SPX_ERR_UNKNOWN_PLUGIN -2   /* kind not known for this role / trajectory type */
+#define SPX_ERR_BAD_BLOB -3         /* blob shorter than the class's parameter list */
+#define SPX_ERR_INCOMPLETE -4       /* TrajectoryBase::IsSimmulationReady false (src/trajectory_base.cc:608-632) */
+#define SPX_ERR_CUDA -5             /* a CUDA runtime call failed */
+#define SPX_ERR_OUT_OF_MEMORY -6
+#define SPX_ERR_LIMIT -7            /* more than 4 boundaries per class or 4 distributions */
+#define SPX_ERR_STATE -8            /* call out of order (e.g. spx_run before spx_add_problem) */
+#define SPX_ERR_DEVICE -9           /* the kernel reported an error (e.g. action beyond the ActionTable) */
+#define SPX_ERR_NO_DEVICE -11       /* no CUDA device, or not an sm_103 device */
+#define SPX_ERR_IO -12              /* spx_dump / spx_restore file error */
+#define SPX_ERR_TOO_LARGE -13       /* size beyond a fixed capacity */
+
+/* ---- enumerations ---------------------------------------------------------------------- */
+/* trajectory types: the numbers of configure.ac:236-244 */
+#define SPX_TRAJ_LORENTZ 200
+#define SPX_TRAJ_FOCUSED 205
+#define SPX_TRAJ_PARKER 206
+#define SPX_TRAJ_PARKER_SOURCE 207
+/* time flow: configure.ac:263-280 */
+#define SPX_FORWARD 0
+#define SPX_BACKWARD 1
+/* arithmetic: plain FP64 drop-in, or FP32 bulk with float-float accumulation */
+#define SPX_FP64 0
+#define SPX_MIXED 1
+/* plugin roles */
+#define SPX_ROLE_BACKGROUND 0
+#define SPX_ROLE_DIFFUSION 1
+#define SPX_ROLE_SOURCE 2
+#define SPX_ROLE_BOUNDARY 3
+#define SPX_ROLE_INITIAL 4
+#define SPX_ROLE_DISTRIBUTION 5
+/* options (spx_set_option) */
+#define SPX_OPT_STEPS_PER_ORBIT 1   /* Lorentz orbit resolution; reference constant 100 (src/trajectory_lorentz.hh:26) */
+#define SPX_OPT_DERIV_MODE 2        /* 0: the reference's compiled-in derivative methods; 1: analytic */
+#define SPX_OPT_PA_SCATTERING 3     /* Focused: Euler pitch-angle scattering step (1) or none (0) */
+#define SPX_OPT_RECORD_FINAL 4      /* keep the final state of every trajectory (spx_get_records) */
+#define SPX_OPT_MAX_ATTEMPTS 5      /* retries of a discarded trajectory, default 100 */
+/* plugin kinds: see spectrum_gb300/plugins.py; e.g. background 1 uniform, 3 smooth shock,
+ * 4 dipole, 5 solar wind; diffusion 5 full constant, 8 rigidity/field power law; boundary
+ * 1 time expire, 10 plane absorb, 14 sphere absorb, 30 momentum inject; distribution 2 position
+ * uniform, 5 kinetic-energy power-law spectrum. */
+
+/* ---- types ----------------------------------------------------------------------------- */
+typedef struct spx_ctx* spx_ctx_t;
+
+typedef struct {
+   int block_size;      /* threads per block; 0 = autotuned */
+   int blocks_per_sm;   /* resident blocks per SM for the persistent launch; 0 = autotuned */
+   int steps_per_sync;  /* steps between lane refills of the work queue; 0 = autotuned */
+   int schedule;        /* 0 = one thread per trajectory (plain grid), 1 = persistent work queue */
+} spx_tuning;
+
+typedef struct {
+   double kernel_ms;        /* device time of the last spx_run (CUDA events on the context stream) */
+   int64_t trajectories;    /* trajectories finished in the last spx_run */
+   int64_t steps;           /* accepted steps in the last spx_run */
+   int64_t retries;         /* discarded attempts that were re-run with a new random stream */
+   int64_t given_up;        /* trajectories discarded max_attempts times */
+   int64_t events;          /* distribution events recorded */
+   int kernel_launches;     /* kernels launched by the last spx_run */
+   spx_tuning tuning;       /* the launch shape used */
+} spx_stats;
+
+typedef struct {
+   uint32_t attempts, status;   /* status: reference TRAJ_* bits (src/trajectory_base.hh:45-57) */
+   uint64_t steps;
+   double t, pos[3], mom[3];
+   double t0, pos0[3], mom0[3];
+   double amp, logwgt;
+} spx_traj_record;
+
+/* ---- calls ----------------------------------------------------------------------------- */
+/* Create a context on the current CUDA device. Replaces CreateSimulation
+ * (src/simulation.cc:899-907) plus the configure-time choice of TRAJ_TYPE, TRAJ_TIME_FLOW and
+ * RK_INTEGRATOR_TYPE (configure.ac:236-295; Runge-Kutta tables 0 and 25 are supported). */
+int spx_create(spx_ctx_t* ctx, int traj_kind, int time_flow, int rk_method, int precision);
+
+/* Set an SPX_OPT_* option (no reference counterpart: these are the reference's compile-time
+ * constants made run-time). */
+int spx_set_option(spx_ctx_t ctx, int option, double value);
+
+/* Add one plugin; replaces SimulationWorker::Add{Background,Diffusion,Source,Boundary,Initial,
+ * Distribution} (src/simulation.hh:105-123, src/trajectory_base.cc:644-741). blob/blob_len/
+ * n_records are exactly DataContainer::data()/length()/size(). */
+int spx_add_plugin(spx_ctx_t ctx, int role, int kind, const uint8_t* blob, size_t blob_len, size_t n_records);
+
+/* Add a problem of n_traj trajectories built from the plugins added so far, with optional
+ * per-problem replacements: override_blob is a sequence of records
+ * { u32 role, u32 slot, u32 kind, u32 n_records, u32 blob_len, u8 blob[blob_len] } replacing the
+ * slot-th plugin of that role. Replaces SetTasks(n_traj, batch_size) (src/simulation.cc:509); many
+ * problems (energies, mean free paths) run in one launch. */
+int spx_add_problem(spx_ctx_t ctx, int64_t n_traj, uint64_t seed, const uint8_t* override_blob, size_t override_len);
+
+/* Integrate every trajectory of every problem; replaces MainLoop (src/simulation.cc:818-835).
+ * Enqueues on the context stream and returns; tuning may be NULL (autotuned). Each call draws
+ * fresh trajectory ids, so repeated calls add new trajectories to the distributions. */
+int spx_run(spx_ctx_t ctx, const spx_tuning* tuning);
+
+/* Wait for the last spx_run and report its statistics (stats may be NULL). */
+int spx_sync(spx_ctx_t ctx, spx_stats* stats);
+
+/* Shape of a distribution: number of bins and doubles per bin (1, 3 or 9). */
+int spx_get_distribution_info(spx_ctx_t ctx, int problem, int distro, int64_t* n_bins, int* width);
+
+/* Copy one distribution to host memory: int32 counts[n_bins], double sums[n_bins*width] and the
+ * event count; any pointer may be NULL. Layout of DistributionTemplated (counts, distro,
+ * n_events; src/distribution_templated.cc:145-181), bins linearised by MultiIndex::LinIdx
+ * (common/multi_index.hh:138-141). */
+int spx_get_distribution(spx_ctx_t ctx, int problem, int distro, int32_t* counts, double* sums, int64_t* n_events);
+
+/* Final states of the trajectories of one problem (SPX_OPT_RECORD_FINAL must be set). Returns the
+ * number written (<= max_records) or an error code. */
+int64_t spx_get_records(spx_ctx_t ctx, int problem, spx_traj_record* out, int64_t max_records);
+
+/* Clear all distributions (DistributionTemplated::ResetDistribution). */
+int spx_reset_distributions(spx_ctx_t ctx);
+
+/* Write / read all distributions (the checkpoint of src/simulation.cc:592-594, 714-720). */
+int spx_dump(spx_ctx_t ctx, const char* path);
+int spx_restore(spx_ctx_t ctx, const char* path);
+
+const char* spx_strerror(int code);
+void spx_destroy(spx_ctx_t ctx);
+
+/* Library version string. */
+const char* spx_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -7,7 +7,9 @@
  *   - the k-th normal of a trajectory is component k % nps of the SPX_RNG_STEP block with
  *     index k / nps, where nps ("normals per step", <= 4) is fixed by the harness for the
  *     trajectory type (3 for Parker: dWx, dWy, dWz in src/trajectory_parker.cc:159-180);
- *   - the k-th uniform is component k % 4 of the SPX_RNG_INIT block with index k / 4.
+ *   - the k-th uniform is component k % 4 of the SPX_RNG_INIT block with index k / 4;
+ *   - normals drawn while the trajectory is set up (between spx_standin_begin and
+ *     spx_standin_steps) come from the SPX_RNG_INIT_NORMAL stream instead.
  * The harness selects the trajectory and attempt with spx_standin_begin() before SetStart(). */
 #include <cstdio>
 #include <cstdlib>
@@ -21,11 +23,12 @@
 struct spx_gsl_rng {
    uint64_t seed;
    uint32_t traj, problem, attempt;
-   uint64_t normal_idx, uniform_idx;
+   uint64_t normal_idx, uniform_idx, init_normal_idx;
    int nps;
+   int in_setup;
 };
 
-static spx_gsl_rng g_rng = {0, 0, 0, 0, 0, 0, 3};
+static spx_gsl_rng g_rng = {0, 0, 0, 0, 0, 0, 0, 3, 1};
 static const gsl_rng_type g_type = {"spx-philox4x32-10"};
 const gsl_rng_type* gsl_rng_default = &g_type;
 
@@ -45,9 +48,15 @@ double gsl_rng_uniform(const gsl_rng* r)
 double gsl_ran_ugaussian(const gsl_rng* r)
 {
    gsl_rng* s = const_cast<gsl_rng*>(r);
-   uint64_t k = s->normal_idx++;
    uint32_t b[4];
    double n[4];
+   if (s->in_setup) {
+      uint64_t j = s->init_normal_idx++;
+      spx_rng_block(s->seed, (uint32_t)(j / 4), s->traj, s->problem, SPX_RNG_INIT_NORMAL, s->attempt, b);
+      spx_normals4(b, n);
+      return n[j % 4];
+   }
+   uint64_t k = s->normal_idx++;
    spx_rng_block(s->seed, (uint32_t)(k / s->nps), s->traj, s->problem, SPX_RNG_STEP, s->attempt, b);
    spx_normals4(b, n);
    return n[k % s->nps];
@@ -77,6 +86,10 @@ void spx_standin_begin(uint32_t traj, uint32_t problem, uint32_t attempt)
    g_rng.attempt = attempt;
    g_rng.normal_idx = 0;
    g_rng.uniform_idx = 0;
+   g_rng.init_normal_idx = 0;
+   g_rng.in_setup = 1;
 }
+
+void spx_standin_steps(void) { g_rng.in_setup = 0; }
 
 uint64_t spx_standin_normals_drawn(void) { return g_rng.normal_idx; }

@@ -256,6 +256,7 @@ int main(int argc, char** argv)
             attempt++;
             try {
                traj->SetStart();
+               spx_standin_steps();
                traj->Integrate();
                done = true;
             }

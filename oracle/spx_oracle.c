@@ -649,7 +649,7 @@ typedef struct {
    const spx_oracle_opts* o;
    /* RNG */
    uint32_t traj_id, attempt;
-   uint64_t n_normal, n_uniform;
+   uint64_t n_normal, n_uniform, n_init_normal;
    /* state (Params, TrajectoryBase) */
    double t, dt, dt_physical, dt_adaptive, amp, wgt;
    v3 pos, mom, vel;
@@ -682,6 +682,16 @@ static double next_uniform(trj_t* T)
    uint32_t b[4];
    spx_rng_block(T->pb->seed, (uint32_t)(k / 4), T->traj_id, T->pb->problem, SPX_RNG_INIT, T->attempt, b);
    return spx_u01(b[k % 4]);
+}
+
+static double next_init_normal(trj_t* T)
+{
+   uint64_t k = T->n_init_normal++;
+   uint32_t b[4];
+   double n[4];
+   spx_rng_block(T->pb->seed, (uint32_t)(k / 4), T->traj_id, T->pb->problem, SPX_RNG_INIT_NORMAL, T->attempt, b);
+   spx_normals4(b, n);
+   return n[k % 4];
 }
 
 static int nps_of(const trj_t* T)
@@ -1427,7 +1437,7 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
       }
    }
    case IM_MAXWELL: {
-      double p_para = q->a[0] + q->a[1] * next_normal(T);
+      double p_para = q->a[0] + q->a[1] * next_init_normal(T);
       double p_perp = q->a[2] * sqrt(-2.0 * log(next_uniform(T)));
       if (tt == 200) {
          double phi = M_2PI_ * next_uniform(T);
@@ -1892,7 +1902,7 @@ static int set_start(trj_t* T)
    double c = c_code();
    T->status = 0;
    T->segments = 0;
-   T->n_normal = T->n_uniform = 0;
+   T->n_normal = T->n_uniform = T->n_init_normal = 0;
    T->t = sample_time(T);
    T->pos = sample_pos(T);
    T->mom = sample_mom(T, V(1.0, 1.0, 1.0));

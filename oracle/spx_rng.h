@@ -17,7 +17,9 @@
  *   counter = { index, trajectory id, problem id, (purpose << 24) | attempt }
  *   purpose SPX_RNG_STEP : index = step number; the block's four normals feed that step
  *   purpose SPX_RNG_INIT : index = k/4 for the k-th uniform drawn by the initial samplers
- *   purpose SPX_RNG_EXTRA: index = step number; spare normals for rejection loops
+ *   purpose SPX_RNG_EXTRA: index = step * 64 + k; spare normals for rejection loops
+ *   purpose SPX_RNG_INIT_NORMAL: index = j/4 for the j-th normal drawn while a trajectory is set
+ *                        up (before its first step)
  * The reference draws its noise through gsl_ran_ugaussian / gsl_rng_uniform
  * (common/random.hh:99-122); the stand-in in oracle/ref_glue maps those calls onto the same
  * layout so the reference and this restatement see identical random numbers.
@@ -35,6 +37,7 @@
 #define SPX_RNG_STEP 0u
 #define SPX_RNG_INIT 1u
 #define SPX_RNG_EXTRA 2u
+#define SPX_RNG_INIT_NORMAL 3u
 
 static inline void spx_philox_round(uint32_t c[4], const uint32_t k[2])
 {

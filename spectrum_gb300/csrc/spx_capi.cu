@@ -1,0 +1,560 @@
+// spx_capi.cu -- the C ABI of include/spx.h: contexts, plugin and problem set-up, launches on the
+// context's stream, statistics, distribution read-back and checkpoints.
+//
+// A context owns one CUDA stream and its device buffers: the problem descriptors in FP64 and FP32,
+// the run counters (the work-queue head among them), the distribution counts and sums, the event
+// counters and, when asked for, the per-trajectory final records. Problems are snapshots of the
+// plugins added before them plus per-problem replacements; all problems of a context share one
+// trajectory type, time flow, Runge-Kutta table and background class (these select the kernel).
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <memory>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/spx.h"
+#include "spx_launch.hh"
+#include "spx_parse.hh"
+
+static_assert(sizeof(spx_traj_record) == sizeof(spx::TrajRecord), "record layouts differ");
+
+namespace {
+
+struct PluginBlob {
+   int role, kind;
+   std::vector<uint8_t> blob;
+};
+
+struct ProblemHost {
+   spx::ProblemDesc pd;
+   int64_t n_traj;
+};
+
+}  // namespace
+
+struct spx_ctx {
+   int device = 0;
+   cudaStream_t stream = nullptr;
+   cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+   int traj = 0, flow = 0, rk = 0, precision = 0;
+   double steps_per_orbit = 100.0;
+   int deriv_mode = 0, pa_scattering = 0, record_final = 0, max_attempts = 100;
+   std::vector<PluginBlob> base;
+   std::vector<ProblemHost> problems;
+   int bg_kind = 0;
+   bool dirty = true;
+   int64_t run_index = 0;
+   int64_t total_traj = 0;
+   int64_t n_counts = 0, n_sums = 0;
+   // device buffers
+   spx::ProblemDesc* d_pd = nullptr;
+   void* d_pr = nullptr;
+   spx::RunCounters* d_ctr = nullptr;
+   int32_t* d_counts = nullptr;
+   double* d_sums = nullptr;
+   unsigned long long* d_nev = nullptr;
+   spx::TrajRecord* d_rec = nullptr;
+   int64_t rec_cap = 0;
+   bool launched = false;
+   spx_stats last{};
+   int sm_count = 0;
+};
+
+namespace {
+
+int cuda_err(cudaError_t e) { return e == cudaSuccess ? SPX_OK : (e == cudaErrorMemoryAllocation ? SPX_ERR_OUT_OF_MEMORY : SPX_ERR_CUDA); }
+
+#define SPX_CUDA(call)                              \
+   do {                                             \
+      cudaError_t e__ = (call);                     \
+      if (e__ != cudaSuccess) return cuda_err(e__); \
+   } while (0)
+
+void free_buffers(spx_ctx* c)
+{
+   cudaFree(c->d_pd);
+   cudaFree(c->d_pr);
+   cudaFree(c->d_ctr);
+   cudaFree(c->d_counts);
+   cudaFree(c->d_sums);
+   cudaFree(c->d_nev);
+   cudaFree(c->d_rec);
+   c->d_pd = nullptr;
+   c->d_pr = nullptr;
+   c->d_ctr = nullptr;
+   c->d_counts = nullptr;
+   c->d_sums = nullptr;
+   c->d_nev = nullptr;
+   c->d_rec = nullptr;
+   c->rec_cap = 0;
+}
+
+// Lay out the distributions of all problems, allocate and upload (called when problems changed).
+int upload(spx_ctx* c)
+{
+   int n = (int)c->problems.size();
+   int64_t off_c = 0, off_s = 0, first = 0;
+   for (int k = 0; k < n; k++) {
+      spx::ProblemDesc& pd = c->problems[k].pd;
+      pd.first = first;
+      pd.n_traj = c->problems[k].n_traj;
+      first += pd.n_traj;
+      for (int d = 0; d < pd.nd; d++) {
+         int64_t nb = (int64_t)pd.d[d].n_bins[0] * pd.d[d].n_bins[1] * pd.d[d].n_bins[2];
+         pd.d[d].offset_counts = off_c;
+         pd.d[d].offset_sums = off_s;
+         off_c += nb;
+         off_s += nb * pd.d[d].width;
+      }
+   }
+   c->total_traj = first;
+   bool resize = (off_c != c->n_counts) || (off_s != c->n_sums) || c->d_pd == nullptr;
+   if (resize) {
+      cudaFree(c->d_pd);
+      cudaFree(c->d_pr);
+      cudaFree(c->d_counts);
+      cudaFree(c->d_sums);
+      cudaFree(c->d_nev);
+      c->d_pd = nullptr;
+      c->d_pr = nullptr;
+      c->d_counts = nullptr;
+      c->d_sums = nullptr;
+      c->d_nev = nullptr;
+      SPX_CUDA(cudaMalloc(&c->d_pd, sizeof(spx::ProblemDesc) * n));
+      size_t rsz = c->precision == SPX_FP64 ? sizeof(spx::ProblemDescT<double>) : sizeof(spx::ProblemDescT<float>);
+      SPX_CUDA(cudaMalloc(&c->d_pr, rsz * n));
+      SPX_CUDA(cudaMalloc(&c->d_counts, sizeof(int32_t) * std::max<int64_t>(off_c, 1)));
+      SPX_CUDA(cudaMalloc(&c->d_sums, sizeof(double) * std::max<int64_t>(off_s, 1)));
+      SPX_CUDA(cudaMalloc(&c->d_nev, sizeof(unsigned long long) * n * spx::kMaxDistro));
+      SPX_CUDA(cudaMemsetAsync(c->d_counts, 0, sizeof(int32_t) * std::max<int64_t>(off_c, 1), c->stream));
+      SPX_CUDA(cudaMemsetAsync(c->d_sums, 0, sizeof(double) * std::max<int64_t>(off_s, 1), c->stream));
+      SPX_CUDA(cudaMemsetAsync(c->d_nev, 0, sizeof(unsigned long long) * n * spx::kMaxDistro, c->stream));
+      c->n_counts = off_c;
+      c->n_sums = off_s;
+   }
+   if (c->d_ctr == nullptr) SPX_CUDA(cudaMalloc(&c->d_ctr, sizeof(spx::RunCounters)));
+   std::vector<spx::ProblemDesc> hd(n);
+   for (int k = 0; k < n; k++) hd[k] = c->problems[k].pd;
+   SPX_CUDA(cudaMemcpyAsync(c->d_pd, hd.data(), sizeof(spx::ProblemDesc) * n, cudaMemcpyHostToDevice, c->stream));
+   if (c->precision == SPX_FP64) {
+      SPX_CUDA(cudaMemcpyAsync(c->d_pr, hd.data(), sizeof(spx::ProblemDesc) * n, cudaMemcpyHostToDevice, c->stream));
+   }
+   else {
+      std::vector<spx::ProblemDescT<float>> hf(n);
+      for (int k = 0; k < n; k++) spx::convert_problem(hd[k], hf[k]);
+      SPX_CUDA(cudaMemcpyAsync(c->d_pr, hf.data(), sizeof(spx::ProblemDescT<float>) * n, cudaMemcpyHostToDevice,
+                               c->stream));
+      SPX_CUDA(cudaStreamSynchronize(c->stream));  // hf is a host temporary
+   }
+   SPX_CUDA(cudaStreamSynchronize(c->stream));
+   if (c->record_final && c->rec_cap < c->total_traj) {
+      cudaFree(c->d_rec);
+      c->d_rec = nullptr;
+      SPX_CUDA(cudaMalloc(&c->d_rec, sizeof(spx::TrajRecord) * c->total_traj));
+      c->rec_cap = c->total_traj;
+   }
+   c->dirty = false;
+   return SPX_OK;
+}
+
+cudaError_t launch(spx_ctx* c, const spx::LaunchArgs& a)
+{
+   bool f64 = c->precision == SPX_FP64;
+   switch (c->traj) {
+   case SPX_TRAJ_PARKER:
+   case SPX_TRAJ_PARKER_SOURCE: return f64 ? spx::launch_parker_f64(c->bg_kind, a) : spx::launch_parker_f32(c->bg_kind, a);
+   case SPX_TRAJ_LORENTZ: return f64 ? spx::launch_lorentz_f64(c->bg_kind, a) : spx::launch_lorentz_f32(c->bg_kind, a);
+   case SPX_TRAJ_FOCUSED: return f64 ? spx::launch_focused_f64(c->bg_kind, a) : spx::launch_focused_f32(c->bg_kind, a);
+   default: return cudaErrorInvalidValue;
+   }
+}
+
+int occupancy(spx_ctx* c, int block)
+{
+   bool f64 = c->precision == SPX_FP64;
+   switch (c->traj) {
+   case SPX_TRAJ_PARKER:
+   case SPX_TRAJ_PARKER_SOURCE: return f64 ? spx::occupancy_parker_f64(c->bg_kind, block) : spx::occupancy_parker_f32(c->bg_kind, block);
+   case SPX_TRAJ_LORENTZ: return f64 ? spx::occupancy_lorentz_f64(c->bg_kind, block) : spx::occupancy_lorentz_f32(c->bg_kind, block);
+   case SPX_TRAJ_FOCUSED: return f64 ? spx::occupancy_focused_f64(c->bg_kind, block) : spx::occupancy_focused_f32(c->bg_kind, block);
+   default: return 0;
+   }
+}
+
+bool valid_ctx(spx_ctx* c) { return c != nullptr; }
+
+}  // namespace
+
+extern "C" {
+
+int spx_create(spx_ctx_t* out, int traj_kind, int time_flow, int rk_method, int precision)
+{
+   if (!out) return SPX_ERR_INVALID_ARG;
+   *out = nullptr;
+   if (traj_kind != SPX_TRAJ_PARKER && traj_kind != SPX_TRAJ_PARKER_SOURCE && traj_kind != SPX_TRAJ_LORENTZ &&
+       traj_kind != SPX_TRAJ_FOCUSED)
+      return SPX_ERR_INVALID_ARG;
+   if (time_flow != SPX_FORWARD && time_flow != SPX_BACKWARD) return SPX_ERR_INVALID_ARG;
+   if (precision != SPX_FP64 && precision != SPX_MIXED) return SPX_ERR_INVALID_ARG;
+   // Parker is an Euler-Maruyama scheme (RK table 0, src/trajectory_parker.cc:415-419); the RK
+   // trajectories take table 0 or the classic fourth-order table 25.
+   if ((traj_kind == SPX_TRAJ_PARKER || traj_kind == SPX_TRAJ_PARKER_SOURCE) && rk_method != 0) return SPX_ERR_INVALID_ARG;
+   if (rk_method != 0 && rk_method != 25) return SPX_ERR_INVALID_ARG;
+   int ndev = 0;
+   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
+      cudaGetLastError();
+      return SPX_ERR_NO_DEVICE;
+   }
+   auto c = std::make_unique<spx_ctx>();
+   if (cudaGetDevice(&c->device) != cudaSuccess) return SPX_ERR_NO_DEVICE;
+   cudaDeviceProp prop;
+   if (cudaGetDeviceProperties(&prop, c->device) != cudaSuccess) return SPX_ERR_NO_DEVICE;
+   if (prop.major != 10 || prop.minor != 3) return SPX_ERR_NO_DEVICE;  // built for sm_103a only
+   c->sm_count = prop.multiProcessorCount;
+   c->traj = traj_kind;
+   c->flow = time_flow;
+   c->rk = rk_method;
+   c->precision = precision;
+   if (precision == SPX_MIXED) c->deriv_mode = 1;
+   if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return SPX_ERR_CUDA;
+   if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) return SPX_ERR_CUDA;
+   *out = c.release();
+   return SPX_OK;
+}
+
+int spx_set_option(spx_ctx_t c, int option, double value)
+{
+   if (!valid_ctx(c)) return SPX_ERR_INVALID_ARG;
+   switch (option) {
+   case SPX_OPT_STEPS_PER_ORBIT:
+      if (!(value > 0.0)) return SPX_ERR_INVALID_ARG;
+      c->steps_per_orbit = value;
+      return SPX_OK;
+   case SPX_OPT_DERIV_MODE:
+      if (value != 0.0 && value != 1.0) return SPX_ERR_INVALID_ARG;
+      // the FP32 kernels compute analytic derivatives only
+      if (c->precision == SPX_MIXED && value == 0.0) return SPX_ERR_INVALID_ARG;
+      c->deriv_mode = (int)value;
+      return SPX_OK;
+   case SPX_OPT_PA_SCATTERING:
+      if (c->traj != SPX_TRAJ_FOCUSED && value != 0.0) return SPX_ERR_INVALID_ARG;
+      c->pa_scattering = value != 0.0;
+      return SPX_OK;
+   case SPX_OPT_RECORD_FINAL:
+      c->record_final = value != 0.0;
+      c->dirty = true;
+      return SPX_OK;
+   case SPX_OPT_MAX_ATTEMPTS:
+      if (!(value >= 1.0)) return SPX_ERR_INVALID_ARG;
+      c->max_attempts = (int)value;
+      return SPX_OK;
+   default: return SPX_ERR_INVALID_ARG;
+   }
+}
+
+int spx_add_plugin(spx_ctx_t c, int role, int kind, const uint8_t* blob, size_t blob_len, size_t n_records)
+{
+   if (!valid_ctx(c) || (blob_len && !blob) || role < 0 || role > SPX_ROLE_DISTRIBUTION) return SPX_ERR_INVALID_ARG;
+   (void)n_records;
+   // parse now so a malformed blob is reported where it is added
+   spx::ProblemDesc probe;
+   std::memset(&probe, 0, sizeof probe);
+   int rc = spx::parse_plugin(probe, c->traj, role, kind, blob, blob_len, -1);
+   if (rc != SPX_OK) return rc;
+   if (role == SPX_ROLE_SOURCE && c->traj != SPX_TRAJ_PARKER_SOURCE) return SPX_ERR_UNKNOWN_PLUGIN;
+   c->base.push_back(PluginBlob{role, kind, std::vector<uint8_t>(blob, blob + blob_len)});
+   return SPX_OK;
+}
+
+int spx_add_problem(spx_ctx_t c, int64_t n_traj, uint64_t seed, const uint8_t* ov, size_t ov_len)
+{
+   if (!valid_ctx(c) || n_traj <= 0 || n_traj > 0xffffffffLL || (ov_len && !ov)) return SPX_ERR_INVALID_ARG;
+   ProblemHost ph;
+   std::memset(&ph.pd, 0, sizeof ph.pd);
+   for (const auto& p : c->base) {
+      int rc = spx::parse_plugin(ph.pd, c->traj, p.role, p.kind, p.blob.data(), p.blob.size(), -1);
+      if (rc != SPX_OK) return rc;
+   }
+   size_t pos = 0;
+   while (pos < ov_len) {
+      uint32_t hdr[5];
+      if (pos + sizeof hdr > ov_len) return SPX_ERR_BAD_BLOB;
+      std::memcpy(hdr, ov + pos, sizeof hdr);
+      pos += sizeof hdr;
+      if (pos + hdr[4] > ov_len) return SPX_ERR_BAD_BLOB;
+      int role = (int)hdr[0], slot = (int)hdr[1], kind = (int)hdr[2];
+      bool slotted = role == SPX_ROLE_BOUNDARY || role == SPX_ROLE_DISTRIBUTION;
+      int rc = spx::parse_plugin(ph.pd, c->traj, role, kind, ov + pos, hdr[4], slotted ? slot : -1);
+      if (rc != SPX_OK) return rc;
+      pos += hdr[4];
+   }
+   int rc = spx::check_ready(ph.pd, c->traj);
+   if (rc != SPX_OK) return rc;
+   if (c->problems.empty()) c->bg_kind = ph.pd.bg.kind;
+   else if (ph.pd.bg.kind != c->bg_kind) return SPX_ERR_INVALID_ARG;  // one background class per context
+   if (c->problems.size() >= 65536) return SPX_ERR_LIMIT;
+   ph.pd.problem_id = (uint32_t)c->problems.size();
+   ph.pd.seed = seed;
+   ph.n_traj = n_traj;
+   c->problems.push_back(ph);
+   c->dirty = true;
+   return SPX_OK;
+}
+
+int spx_run(spx_ctx_t c, const spx_tuning* tuning)
+{
+   if (!valid_ctx(c)) return SPX_ERR_INVALID_ARG;
+   if (c->problems.empty()) return SPX_ERR_STATE;
+   SPX_CUDA(cudaSetDevice(c->device));
+   if (c->dirty) {
+      int rc = upload(c);
+      if (rc != SPX_OK) return rc;
+   }
+   spx_tuning tu{};
+   if (tuning) tu = *tuning;
+   if (tu.schedule != 0 && tu.schedule != 1) return SPX_ERR_INVALID_ARG;
+   if (tu.block_size <= 0) tu.block_size = 128;
+   if (tu.block_size % 32 || tu.block_size > 128) return SPX_ERR_INVALID_ARG;
+   if (!tuning) tu.schedule = c->precision == SPX_MIXED ? 1 : 0;
+   if (tu.steps_per_sync <= 0) tu.steps_per_sync = tu.schedule ? 16 : 1 << 30;
+   int occ = occupancy(c, tu.block_size);
+   if (occ <= 0) occ = 1;
+   if (tu.blocks_per_sm <= 0 || tu.blocks_per_sm > occ) tu.blocks_per_sm = occ;
+   spx::LaunchArgs a;
+   a.block = dim3(tu.block_size);
+   int64_t grid;
+   if (tu.schedule == 1) grid = (int64_t)c->sm_count * tu.blocks_per_sm;  // persistent: fill the GPU once
+   else grid = (c->total_traj + tu.block_size - 1) / tu.block_size;      // one thread per trajectory
+   grid = std::max<int64_t>(1, std::min<int64_t>(grid, 0x7fffffff));
+   a.grid = dim3((unsigned)grid);
+   a.stream = c->stream;
+   a.problems_r = c->d_pr;
+   a.problems_d = c->d_pd;
+   a.cfg.traj_kind = c->traj;
+   a.cfg.time_flow = c->flow;
+   a.cfg.rk = c->rk;
+   a.cfg.deriv_mode = c->deriv_mode;
+   a.cfg.pa_scattering = c->pa_scattering;
+   a.cfg.max_attempts = c->max_attempts;
+   a.cfg.steps_per_orbit = c->steps_per_orbit;
+   a.cfg.steps_per_orbit_f = (float)c->steps_per_orbit;
+   a.cfg.record_final = c->record_final;
+   a.cfg.n_problems = (int)c->problems.size();
+   a.cfg.steps_per_sync = tu.steps_per_sync;
+   a.cfg.total_traj = c->total_traj;
+   a.cfg.run_index = c->run_index;
+   a.ctr = c->d_ctr;
+   a.counts = c->d_counts;
+   a.sums = c->d_sums;
+   a.n_events = c->d_nev;
+   a.records = c->d_rec;
+   a.queue = tu.schedule;
+   if (c->record_final && c->d_rec == nullptr) return SPX_ERR_STATE;
+   SPX_CUDA(cudaMemsetAsync(c->d_ctr, 0, sizeof(spx::RunCounters), c->stream));
+   SPX_CUDA(cudaEventRecord(c->ev0, c->stream));
+   SPX_CUDA(launch(c, a));
+   SPX_CUDA(cudaEventRecord(c->ev1, c->stream));
+   // ids of the next run continue after this one's (new random streams)
+   for (const auto& p : c->problems)
+      if ((uint64_t)(c->run_index + 2) * (uint64_t)p.n_traj > 0xffffffffull) return SPX_ERR_LIMIT;
+   c->run_index++;
+   c->launched = true;
+   c->last = spx_stats{};
+   c->last.tuning = tu;
+   c->last.kernel_launches = 1;
+   return SPX_OK;
+}
+
+int spx_sync(spx_ctx_t c, spx_stats* stats)
+{
+   if (!valid_ctx(c)) return SPX_ERR_INVALID_ARG;
+   if (!c->launched) return SPX_ERR_STATE;
+   SPX_CUDA(cudaStreamSynchronize(c->stream));
+   spx::RunCounters h;
+   SPX_CUDA(cudaMemcpy(&h, c->d_ctr, sizeof h, cudaMemcpyDeviceToHost));
+   float ms = 0.0f;
+   SPX_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+   c->last.kernel_ms = ms;
+   c->last.trajectories = (int64_t)h.finished + (int64_t)h.given_up;
+   c->last.steps = (int64_t)h.steps;
+   c->last.retries = (int64_t)h.retries;
+   c->last.given_up = (int64_t)h.given_up;
+   if (stats) *stats = c->last;
+   if (h.error != 0) return SPX_ERR_DEVICE;
+   return SPX_OK;
+}
+
+int spx_get_distribution_info(spx_ctx_t c, int problem, int distro, int64_t* n_bins, int* width)
+{
+   if (!valid_ctx(c) || problem < 0 || problem >= (int)c->problems.size()) return SPX_ERR_INVALID_ARG;
+   const spx::ProblemDesc& pd = c->problems[problem].pd;
+   if (distro < 0 || distro >= pd.nd) return SPX_ERR_INVALID_ARG;
+   if (n_bins) *n_bins = (int64_t)pd.d[distro].n_bins[0] * pd.d[distro].n_bins[1] * pd.d[distro].n_bins[2];
+   if (width) *width = pd.d[distro].width;
+   return SPX_OK;
+}
+
+int spx_get_distribution(spx_ctx_t c, int problem, int distro, int32_t* counts, double* sums, int64_t* n_events)
+{
+   int64_t nb = 0;
+   int w = 0;
+   int rc = spx_get_distribution_info(c, problem, distro, &nb, &w);
+   if (rc != SPX_OK) return rc;
+   if (c->dirty || c->d_counts == nullptr) {
+      if (counts) std::memset(counts, 0, sizeof(int32_t) * nb);
+      if (sums) std::memset(sums, 0, sizeof(double) * nb * w);
+      if (n_events) *n_events = 0;
+      return SPX_OK;
+   }
+   SPX_CUDA(cudaStreamSynchronize(c->stream));
+   const spx::DistParams& d = c->problems[problem].pd.d[distro];
+   if (counts) SPX_CUDA(cudaMemcpy(counts, c->d_counts + d.offset_counts, sizeof(int32_t) * nb, cudaMemcpyDeviceToHost));
+   if (sums) SPX_CUDA(cudaMemcpy(sums, c->d_sums + d.offset_sums, sizeof(double) * nb * w, cudaMemcpyDeviceToHost));
+   if (n_events) {
+      unsigned long long ne = 0;
+      SPX_CUDA(cudaMemcpy(&ne, c->d_nev + (int64_t)problem * spx::kMaxDistro + distro, sizeof ne, cudaMemcpyDeviceToHost));
+      *n_events = (int64_t)ne;
+   }
+   return SPX_OK;
+}
+
+int64_t spx_get_records(spx_ctx_t c, int problem, spx_traj_record* out, int64_t max_records)
+{
+   if (!valid_ctx(c) || problem < 0 || problem >= (int)c->problems.size() || (!out && max_records > 0))
+      return SPX_ERR_INVALID_ARG;
+   if (!c->record_final || c->d_rec == nullptr || !c->launched) return SPX_ERR_STATE;
+   const spx::ProblemDesc& pd = c->problems[problem].pd;
+   int64_t n = std::min<int64_t>(max_records, c->problems[problem].n_traj);
+   if (n <= 0) return 0;
+   cudaError_t e = cudaStreamSynchronize(c->stream);
+   if (e == cudaSuccess) e = cudaMemcpy(out, c->d_rec + pd.first, sizeof(spx::TrajRecord) * n, cudaMemcpyDeviceToHost);
+   if (e != cudaSuccess) return cuda_err(e);
+   return n;
+}
+
+int spx_reset_distributions(spx_ctx_t c)
+{
+   if (!valid_ctx(c)) return SPX_ERR_INVALID_ARG;
+   if (c->d_counts == nullptr) return SPX_OK;
+   SPX_CUDA(cudaMemsetAsync(c->d_counts, 0, sizeof(int32_t) * std::max<int64_t>(c->n_counts, 1), c->stream));
+   SPX_CUDA(cudaMemsetAsync(c->d_sums, 0, sizeof(double) * std::max<int64_t>(c->n_sums, 1), c->stream));
+   SPX_CUDA(cudaMemsetAsync(c->d_nev, 0, sizeof(unsigned long long) * c->problems.size() * spx::kMaxDistro, c->stream));
+   SPX_CUDA(cudaStreamSynchronize(c->stream));
+   return SPX_OK;
+}
+
+// Checkpoint file: "SPXD" u32 version=1, u32 n_problems, i64 run_index, then per problem u32 nd and
+// per distribution u64 n_bins, u32 width, i32 counts[n_bins], f64 sums[n_bins*width], i64 n_events.
+int spx_dump(spx_ctx_t c, const char* path)
+{
+   if (!valid_ctx(c) || !path) return SPX_ERR_INVALID_ARG;
+   FILE* f = std::fopen(path, "wb");
+   if (!f) return SPX_ERR_IO;
+   uint32_t hdr[3] = {0x44585053u, 1u, (uint32_t)c->problems.size()};
+   bool ok = std::fwrite(hdr, sizeof hdr, 1, f) == 1 && std::fwrite(&c->run_index, 8, 1, f) == 1;
+   for (int p = 0; ok && p < (int)c->problems.size(); p++) {
+      const spx::ProblemDesc& pd = c->problems[p].pd;
+      uint32_t nd = (uint32_t)pd.nd;
+      ok = std::fwrite(&nd, 4, 1, f) == 1;
+      for (int d = 0; ok && d < pd.nd; d++) {
+         int64_t nb = 0;
+         int w = 0;
+         spx_get_distribution_info(c, p, d, &nb, &w);
+         std::vector<int32_t> counts(nb);
+         std::vector<double> sums(nb * w);
+         int64_t ne = 0;
+         if (spx_get_distribution(c, p, d, counts.data(), sums.data(), &ne) != SPX_OK) ok = false;
+         uint64_t nbu = (uint64_t)nb;
+         uint32_t wu = (uint32_t)w;
+         ok = ok && std::fwrite(&nbu, 8, 1, f) == 1 && std::fwrite(&wu, 4, 1, f) == 1 &&
+              std::fwrite(counts.data(), 4, nb, f) == (size_t)nb && std::fwrite(sums.data(), 8, nb * w, f) == (size_t)(nb * w) &&
+              std::fwrite(&ne, 8, 1, f) == 1;
+      }
+   }
+   ok = (std::fclose(f) == 0) && ok;
+   return ok ? SPX_OK : SPX_ERR_IO;
+}
+
+int spx_restore(spx_ctx_t c, const char* path)
+{
+   if (!valid_ctx(c) || !path) return SPX_ERR_INVALID_ARG;
+   if (c->problems.empty()) return SPX_ERR_STATE;
+   if (c->dirty) {
+      int rc = upload(c);
+      if (rc != SPX_OK) return rc;
+   }
+   FILE* f = std::fopen(path, "rb");
+   if (!f) return SPX_ERR_IO;
+   uint32_t hdr[3];
+   int64_t run_index = 0;
+   bool ok = std::fread(hdr, sizeof hdr, 1, f) == 1 && hdr[0] == 0x44585053u && hdr[1] == 1u &&
+             hdr[2] == c->problems.size() && std::fread(&run_index, 8, 1, f) == 1;
+   for (int p = 0; ok && p < (int)c->problems.size(); p++) {
+      const spx::ProblemDesc& pd = c->problems[p].pd;
+      uint32_t nd = 0;
+      ok = std::fread(&nd, 4, 1, f) == 1 && nd == (uint32_t)pd.nd;
+      for (int d = 0; ok && d < pd.nd; d++) {
+         uint64_t nb = 0;
+         uint32_t w = 0;
+         ok = std::fread(&nb, 8, 1, f) == 1 && std::fread(&w, 4, 1, f) == 1;
+         int64_t nbe = 0;
+         int we = 0;
+         spx_get_distribution_info(c, p, d, &nbe, &we);
+         ok = ok && (int64_t)nb == nbe && (int)w == we;
+         if (!ok) break;
+         std::vector<int32_t> counts(nb);
+         std::vector<double> sums(nb * w);
+         int64_t ne = 0;
+         ok = std::fread(counts.data(), 4, nb, f) == nb && std::fread(sums.data(), 8, nb * w, f) == nb * w &&
+              std::fread(&ne, 8, 1, f) == 1;
+         if (!ok) break;
+         const spx::DistParams& dp = pd.d[d];
+         unsigned long long neu = (unsigned long long)ne;
+         ok = cudaMemcpy(c->d_counts + dp.offset_counts, counts.data(), 4 * nb, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(c->d_sums + dp.offset_sums, sums.data(), 8 * nb * w, cudaMemcpyHostToDevice) == cudaSuccess &&
+              cudaMemcpy(c->d_nev + (int64_t)p * spx::kMaxDistro + d, &neu, 8, cudaMemcpyHostToDevice) == cudaSuccess;
+      }
+   }
+   std::fclose(f);
+   if (!ok) return SPX_ERR_IO;
+   c->run_index = run_index;  // trajectories after a restore continue with new ids
+   return SPX_OK;
+}
+
+const char* spx_strerror(int code)
+{
+   switch (code) {
+   case SPX_OK: return "success";
+   case SPX_ERR_INVALID_ARG: return "invalid argument";
+   case SPX_ERR_UNKNOWN_PLUGIN: return "unknown plugin kind for this role or trajectory type";
+   case SPX_ERR_BAD_BLOB: return "malformed parameter blob";
+   case SPX_ERR_INCOMPLETE: return "simulation not ready: background, time/space/momentum initial conditions, a time boundary (and a diffusion model for Parker) are required";
+   case SPX_ERR_CUDA: return "CUDA runtime error";
+   case SPX_ERR_OUT_OF_MEMORY: return "out of device memory";
+   case SPX_ERR_LIMIT: return "capacity exceeded (4 boundaries per class, 4 distributions, 2^32 trajectory ids)";
+   case SPX_ERR_STATE: return "call out of order";
+   case SPX_ERR_DEVICE: return "the kernel reported an error (distribution action out of range)";
+   case SPX_ERR_NO_DEVICE: return "no sm_103 CUDA device";
+   case SPX_ERR_IO: return "checkpoint file error";
+   case SPX_ERR_TOO_LARGE: return "size beyond a fixed capacity";
+   default: return "unknown error";
+   }
+}
+
+void spx_destroy(spx_ctx_t c)
+{
+   if (!c) return;
+   if (c->stream) cudaStreamSynchronize(c->stream);
+   free_buffers(c);
+   if (c->ev0) cudaEventDestroy(c->ev0);
+   if (c->ev1) cudaEventDestroy(c->ev1);
+   if (c->stream) cudaStreamDestroy(c->stream);
+   delete c;
+}
+
+const char* spx_version(void) { return "spectrum_gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"

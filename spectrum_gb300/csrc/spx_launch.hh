@@ -1,0 +1,35 @@
+// spx_launch.hh -- host entry points of the stepping kernels, one translation unit per trajectory
+// family and arithmetic so they compile in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "spx_params.hh"
+
+namespace spx {
+
+struct LaunchArgs {
+   dim3 grid, block;
+   cudaStream_t stream;
+   const void* problems_r;          // ProblemDescT<R>* for the launch arithmetic
+   const ProblemDesc* problems_d;   // FP64 descriptors (set-up and events)
+   RunConfig cfg;
+   RunCounters* ctr;
+   int32_t* counts;
+   double* sums;
+   unsigned long long* n_events;
+   TrajRecord* records;
+   int queue;                       // 1: persistent work-queue schedule
+};
+
+#define SPX_DECLARE_FAMILY(fam)                                  \
+   cudaError_t launch_##fam##_f64(int bg, const LaunchArgs& a);  \
+   cudaError_t launch_##fam##_f32(int bg, const LaunchArgs& a);  \
+   int occupancy_##fam##_f64(int bg, int block);                 \
+   int occupancy_##fam##_f32(int bg, int block);
+SPX_DECLARE_FAMILY(parker)
+SPX_DECLARE_FAMILY(lorentz)
+SPX_DECLARE_FAMILY(focused)
+#undef SPX_DECLARE_FAMILY
+
+}  // namespace spx

@@ -1,0 +1,165 @@
+// spx_params.hh -- plain-old-data plugin descriptors, filled on the host from the reference's
+// DataContainer blobs and read by the stepping kernels from device memory.
+//
+// One ProblemDescT<R> holds everything a trajectory of one problem needs: background, diffusion,
+// source, boundaries, initial conditions and distribution layouts. The descriptors are templates
+// over the real type R: the host parses into ProblemDescT<double> and derives a
+// ProblemDescT<float> copy, so the FP32 kernel reads no FP64 data in its step loop (on GB300 the
+// FP64 pipe, which also converts double to float, runs at a small fraction of the FP32 rate).
+// Kinds are the numbers of include/spx.h; lengths are code units of the reference
+// (common/specie.hh:30-82).
+#pragma once
+
+#include <cstdint>
+
+namespace spx {
+
+constexpr int kMaxBnd = 4;     // boundaries per class (time, space, momentum)
+constexpr int kMaxDistro = 4;  // distributions per problem
+
+enum TrajKind : int { kLorentz = 200, kFocused = 205, kParker = 206, kParkerSource = 207 };
+
+enum BgKind : int { kBgUniform = 1, kBgShock = 2, kBgSmoothShock = 3, kBgDipole = 4, kBgSolarWind = 5 };
+
+enum DiffKind : int {
+   kDfIsotropic = 1, kDfQLT, kDfPara, kDfPerp, kDfFull, kDfFlowMomentum, kDfKinEnergyRadial, kDfRigidityB,
+   kDfStrauss2013, kDfPotgieter2015, kDfEmpiricalSOQLT
+};
+
+enum BndKind : int {
+   kBtTimeExpire = 1, kBtTimePass, kBtTimeRecurrent,
+   kBtPlaneAbsorb = 10, kBtPlaneReflect, kBtPlanePass, kBtBoxReflect, kBtSphereAbsorb, kBtSphereReflect,
+   kBtRankineAbsorb, kBtCylinderAbsorb, kBtRegionAbsorb, kBtSpherePass,
+   kBtMomentumInject = 30, kBtMomentumPass, kBtMomentumSlab, kBtMomentumShell, kBtMirror
+};
+
+enum IniKind : int {
+   kItFixed = 1, kItInterval,
+   kIsFixed = 10, kIsLine, kIsCircle, kIsBox, kIsSphere, kIsSphereSector, kIsRankine,
+   kImFixed = 30, kImBeam, kImRing, kImShell, kImThickShell, kImMaxwell,
+   kImLogEnergyPitchBand = 40, kIsEquatorialBand = 41
+};
+
+enum DistKind : int {
+   kDsTimeUniform = 1, kDsPositionUniform, kDsMomentumUniform, kDsPositionMomentumUniform, kDsSpectrumPowerLaw,
+   kDsSpectrumBentPowerLaw, kDsCumulative1, kDsCumulative2, kDsDivergenceFlow, kDsTimeMu = 20
+};
+
+template <class R>
+struct BgParamsT {
+   int kind;
+   R t0, dmax0;
+   R r0[3], u0[3], B0[3];
+   R n_shock[3], u1[3], B1[3], E0[3], E1[3];
+   R v_shock, compression, width, dmax_fraction;
+   R M[3];                    // dipole moment B0 r_ref^3
+   R eprime[3][3];            // solar wind rotation frame (rows)
+   R w0, r_ref, ur0, A;       // A = Br0 r_ref^2
+};
+
+template <class R>
+struct DiffParamsT {
+   int kind, i0, i1;
+   R a[10];
+};
+
+template <class R>
+struct SrcParamsT {
+   int kind;                  // 0 none, 2 momentum injection
+   R p_inj, rate;
+};
+
+template <class R>
+struct BndParamsT {
+   int kind, cls;             // cls: 0 time, 1 space, 2 momentum
+   int reflect, recurrent;
+   int max_crossings, n_actions;
+   int actions[kMaxDistro];
+   int region_ind;
+   R timemark, timemark_lo;   // timemark_lo: the part of the double timemark a float cannot hold
+   R momentum, radius, z_nose, r1, r2, region_val;
+   R origin[3], norm[3], corner0[3], corner1[3], normals[3][3], axis[3], fa[3][3];
+   R slab_r0[3], slab_r1[3], slab_n[3];
+};
+
+template <class R>
+struct IniParamsT {
+   int kind, n_int, flag;
+   R a[8];
+   R v0[3], v1[3], v2[3];
+};
+
+template <class R>
+struct DistParamsT {
+   int kind, width, dims, n_actions;
+   int n_bins[3], log_bins[3], bin_outside[3];
+   R limits0[3], bin_size[3];
+   R val_hot, val_cold;
+   int val_time, val_coord, pos_idx, mom_idx;
+   R J0, T0, pow_law, T_b, pow_law_comb, bend, A0;
+   int64_t offset_counts;     // into the context's counts array
+   int64_t offset_sums;       // into the context's sums array (doubles)
+};
+
+template <class R>
+struct ProblemDescT {
+   BgParamsT<R> bg;
+   DiffParamsT<R> df;
+   SrcParamsT<R> src;
+   IniParamsT<R> it, is, im;
+   BndParamsT<R> bt[kMaxBnd], bs[kMaxBnd], bm[kMaxBnd];
+   DistParamsT<R> d[kMaxDistro];
+   int nbt, nbs, nbm, nd;
+   int has_diff;
+   uint32_t problem_id;
+   uint64_t seed;
+   int64_t n_traj;            // trajectories of this problem in one run
+   int64_t first;             // index of its first trajectory in the launch's global order
+   int64_t id_base;           // trajectory id of its first trajectory in this run (ids continue across runs)
+};
+
+using ProblemDesc = ProblemDescT<double>;
+using BgParams = BgParamsT<double>;
+using DiffParams = DiffParamsT<double>;
+using BndParams = BndParamsT<double>;
+using IniParams = IniParamsT<double>;
+using DistParams = DistParamsT<double>;
+
+// Per-trajectory final state, the same fields as the reference harness writes.
+struct TrajRecord {
+   uint32_t attempts, status;
+   uint64_t steps;
+   double t, pos[3], mom[3];
+   double t0, pos0[3], mom0[3];
+   double amp, logwgt;
+};
+
+// Kernel-wide settings (one per launch).
+struct RunConfig {
+   int traj_kind, time_flow, rk, deriv_mode, pa_scattering, max_attempts;
+   double steps_per_orbit;
+   float steps_per_orbit_f;
+   int record_final;
+   int n_problems;
+   int steps_per_sync;
+   int64_t total_traj;
+   int64_t run_index;         // trajectory ids of run r are r * n_traj + local (new streams per run)
+};
+
+// Device-side counters of one run (scratch memory, zeroed before each launch).
+struct RunCounters {
+   unsigned long long next_traj;     // work-queue head
+   unsigned long long finished;
+   unsigned long long steps;
+   unsigned long long retries;
+   unsigned long long given_up;
+   unsigned long long events;
+   unsigned int error;               // first device-side error code (0 = none)
+   unsigned int pad;
+};
+
+// Host-side conversion of the double descriptors to another real type.
+template <class R>
+void convert_problem(const ProblemDesc& s, ProblemDescT<R>& d);
+
+}  // namespace spx

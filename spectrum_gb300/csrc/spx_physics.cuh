@@ -1,0 +1,636 @@
+// spx_physics.cuh -- field evaluators, diffusion models and boundary tests, as device functions
+// over the real type R. Each function names the reference code whose arithmetic it carries out.
+#pragma once
+
+#include "spx_device.cuh"
+#include "spx_params.hh"
+
+namespace spx {
+
+// ---- unit system and proton kinematics (common/specie.hh:30-82, common/physics.hh:246-510) --
+template <class R> struct Units;
+template <> struct Units<double> {
+   static constexpr double c = 2.99792458e+10 / (0.1 * 2.99792458e+10);
+};
+template <> struct Units<float> {
+   static constexpr float c = (float)(2.99792458e+10 / (0.1 * 2.99792458e+10));
+};
+template <class R> __device__ __forceinline__ R c_code() { return Units<R>::c; }
+template <class R> __device__ __forceinline__ R enr_tot(R p) { R c = c_code<R>(); return m_sqrt(p * p + c * c) * c; }
+template <class R> __device__ __forceinline__ R enr_kin(R p) { R c = c_code<R>(); return enr_tot(p) - c * c; }
+template <class R> __device__ __forceinline__ R vel_of(R p) { R c = c_code<R>(); return p * (c * c) / enr_tot(p); }
+template <class R> __device__ __forceinline__ R mom_of(R e) { R c = c_code<R>(); return m_sqrt(e * (e + R(2) * (c * c))) / c; }
+template <class R> __device__ __forceinline__ R rigidity(R p) { return p * c_code<R>(); }
+template <class R> __device__ __forceinline__ R larmor(R p, R b) { return p * c_code<R>() / b; }
+template <class R> __device__ __forceinline__ R rel_factor(R v) { R r = v / c_code<R>(); return R(1) / m_sqrt(R(1) - r * r); }
+template <class R> __device__ __forceinline__ R cyclotron(R v, R b) { return b / (rel_factor(v) * c_code<R>()); }
+template <class R> __device__ __forceinline__ V3<R> vel_cart(V3<R> mom) { R m = norm(mom); return (vel_of(m) / m) * mom; }
+
+// ---- spatial data (common/spatial_data.hh:55-135) ----------------------------------------------
+constexpr unsigned kU = 0x1, kB = 0x2, kE = 0x4, kAll = 0x7, kGradU = 0x10, kGradB = 0x20, kDUdt = 0x100;
+
+template <class R>
+struct SD {
+   V3<R> U, B, E, bhat, gradBmag, dUdt, region;
+   M3<R> gradU, gradB;
+   R Bmag, dmax;
+   R dr[3];
+};
+
+template <class R> __device__ __forceinline__ R sd_divU(const SD<R>& s) { return trace(s.gradU); }
+template <class R> __device__ __forceinline__ V3<R> sd_curlB(const SD<R>& s)
+{
+   return {s.gradB.m[1][2] - s.gradB.m[2][1], s.gradB.m[2][0] - s.gradB.m[0][2], s.gradB.m[0][1] - s.gradB.m[1][0]};
+}
+// divbhat and bhat.grad(bhat), common/spatial_data.hh:288-330
+template <class R> __device__ __forceinline__ R sd_divbhat(const SD<R>& s)
+{
+   return (trace(s.gradB) - dot(s.gradBmag, s.bhat)) / s.Bmag;
+}
+template <class R> __device__ __forceinline__ V3<R> sd_b_gradbhat(const SD<R>& s)
+{
+   V3<R> r;
+   R o[3];
+#pragma unroll
+   for (int j = 0; j < 3; j++) {
+      R acc = R(0);
+#pragma unroll
+      for (int i = 0; i < 3; i++) acc += s.bhat[i] * ((s.gradB.m[i][j] - s.gradBmag[i] * s.bhat[j]) / s.Bmag);
+      o[j] = acc;
+   }
+   r = {o[0], o[1], o[2]};
+   return r;
+}
+
+template <class R> __device__ __forceinline__ void zero(M3<R>& a)
+{
+#pragma unroll
+   for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) a.m[i][j] = R(0);
+}
+
+// ---- backgrounds -------------------------------------------------------------------------------
+// Smooth transition of SMOOTH_SHOCK_ORDER 4 (src/background_smooth_shock.cc:46-105)
+template <class R> __device__ __forceinline__ R shock_tr(R x) { return R(0.5) * (R(1) + m_tanh(R(8) * x)); }
+template <class R> __device__ __forceinline__ R shock_trd(R x) { R th = m_tanh(R(8) * x); return R(0.5) * R(8) * (R(1) - th * th); }
+
+template <class R> __device__ __forceinline__ V3<R> eframe_to(const BgParamsT<R>& g, V3<R> a)
+{
+   return {a.x * g.eprime[0][0] + a.y * g.eprime[0][1] + a.z * g.eprime[0][2],
+           a.x * g.eprime[1][0] + a.y * g.eprime[1][1] + a.z * g.eprime[1][2],
+           a.x * g.eprime[2][0] + a.y * g.eprime[2][1] + a.z * g.eprime[2][2]};
+}
+template <class R> __device__ __forceinline__ V3<R> eframe_from(const BgParamsT<R>& g, V3<R> a)
+{
+   return {a.x * g.eprime[0][0] + a.y * g.eprime[1][0] + a.z * g.eprime[2][0],
+           a.x * g.eprime[0][1] + a.y * g.eprime[1][1] + a.z * g.eprime[2][1],
+           a.x * g.eprime[0][2] + a.y * g.eprime[1][2] + a.z * g.eprime[2][2]};
+}
+
+// EvaluateBackground of the analytic backgrounds: U, B, E by mask, region; *ds is the smooth-shock
+// coordinate (used by the derivatives).
+template <int BG, class R>
+__device__ __forceinline__ void eval_bg(const BgParamsT<R>& g, R t, V3<R> pos, unsigned mask, SD<R>& s, R& ds)
+{
+   if (BG == kBgUniform) {  // src/background_uniform.cc:63-72
+      if (mask & kU) s.U = ld3(g.u0);
+      if (mask & kB) s.B = ld3(g.B0);
+      if (mask & kE) s.E = ld3(g.E0);
+      s.region = mk(R(1), R(1), R(1));
+   }
+   else if (BG == kBgShock) {  // src/background_shock.cc:86-104
+      if (dot(pos - ld3(g.r0), ld3(g.n_shock)) - g.v_shock * t > R(0)) {
+         if (mask & kU) s.U = ld3(g.u0);
+         if (mask & kB) s.B = ld3(g.B0);
+         if (mask & kE) s.E = ld3(g.E0);
+         s.region = mk(R(1), R(1), R(1));
+      }
+      else {
+         if (mask & kU) s.U = ld3(g.u1);
+         if (mask & kB) s.B = ld3(g.B1);
+         if (mask & kE) s.E = ld3(g.E1);
+         s.region = mk(R(2), R(2), R(2));
+      }
+   }
+   else if (BG == kBgSmoothShock) {  // src/background_smooth_shock.cc:124-140
+      ds = (dot(pos - ld3(g.r0), ld3(g.n_shock)) - g.v_shock * t) / g.width;
+      R a1 = shock_tr(ds), a2 = R(1) - a1;
+      if ((mask & kU) || (mask & kE)) s.U = a1 * ld3(g.u0) + a2 * ld3(g.u1);
+      if (mask & kB) s.B = a1 * ld3(g.B0) + a2 * ld3(g.B1);
+      if (mask & kE) s.E = (R(-1) / c_code<R>()) * cross(s.U, s.B);
+      R rg = R(1) * a1 + R(2) * a2;
+      s.region = mk(rg, rg, rg);
+   }
+   else if (BG == kBgDipole) {  // src/background_dipole.cc:64-80
+      if (mask & kU) s.U = mk(R(0), R(0), R(0));
+      if (mask & kB) {
+         V3<R> pp = pos - ld3(g.r0), M = ld3(g.M);
+         R r2 = norm(pp);
+         R r5 = r2 * r2 * r2;
+         r2 *= r2;
+         r5 *= r2;
+         s.B = (R(3) * dot(pp, M) * pp - r2 * M) / r5;
+      }
+      if (mask & kE) s.E = mk(R(0), R(0), R(0));
+      s.region = mk(R(1), R(1), R(1));
+   }
+   else if (BG == kBgSolarWind) {  // src/background_solarwind.cc:111-255, switches at their defaults
+      V3<R> pp = eframe_to(g, pos - ld3(g.r0));
+      R r = norm(pp), r_mns = r - g.r_ref, costheta = pp.z / r, ur = g.ur0;
+      s.region = mk(r < R(117.0 * 1.495978707E+13 / 1.0e10) ? R(1) : R(-1), R(-1), s.region.z);
+      if (mask & kU) s.U = eframe_from(g, ur * unit(pp));
+      if (mask & kB) {
+         R sintheta = m_sqrt(m_max(R(1) - costheta * costheta, R(0)));
+         R sr = m_sqrt(pp.x * pp.x + pp.y * pp.y), cosphi, sinphi;
+         if (sr < r * Lim<R>::tiny) { cosphi = R(0); sinphi = R(0); }
+         else { cosphi = pp.x / sr; sinphi = pp.y / sr; }
+         R q = g.r_ref / r;
+         R Br = g.B0[0] * (q * q);
+         R Bp = -Br * sintheta * r_mns * g.w0 / ur;
+         s.B = eframe_from(g, mk(Br * sintheta * cosphi - Bp * sinphi, Br * sintheta * sinphi + Bp * cosphi, Br * costheta));
+      }
+      if (mask & kE) s.E = (R(-1) / c_code<R>()) * cross(s.U, s.B);
+   }
+}
+
+// EvaluateDmax (src/background_base.cc:378-382 and overrides). The smooth shock uses the shock
+// distance at the evaluated point (the reference uses the previous evaluation's value because
+// EvaluateDmax runs before EvaluateBackground in GetFields, src/background_base.cc:434-442).
+template <int BG, class R>
+__device__ __forceinline__ R eval_dmax(const BgParamsT<R>& g, R t, V3<R> pos)
+{
+   if (BG == kBgSmoothShock) {
+      R ds = (dot(pos - ld3(g.r0), ld3(g.n_shock)) - g.v_shock * t) / g.width;
+      return m_min(g.dmax_fraction * g.width * m_max(R(1), m_abs(ds)), g.dmax0);
+   }
+   if (BG == kBgDipole || BG == kBgSolarWind) return m_min(g.dmax_fraction * norm(pos - ld3(g.r0)), g.dmax0);
+   return g.dmax0;
+}
+
+// Analytic gradients of the Parker spiral. With x the position in the rotation frame, r = |x|,
+// A = Br0 r_ref^2, k = A w0 / ur and w = (x2, -x1, 0):
+//   B = A x / r^3 + k f(r) w,  f = (r - r_ref) / r^3,  f' = (3 r_ref - 2 r) / r^4,
+//   d_i B_j = A (delta_ij / r^3 - 3 x_i x_j / r^5) + k (f' x_i w_j / r + f dw_j/dx_i),
+//   d_i U_j = ur (delta_ij / r - x_i x_j / r^3),   div U = 2 ur / r.
+// (The reference's SOLARWIND_DERIVATIVE_METHOD 0 branch is not buildable as shipped.)
+template <class R>
+__device__ __forceinline__ void solarwind_grad(const BgParamsT<R>& g, V3<R> pos, SD<R>& s, bool need_gradB)
+{
+   V3<R> x = eframe_to(g, pos - ld3(g.r0));
+   R r = norm(x), ir = R(1) / r, ir2 = ir * ir, ir3 = ir2 * ir;
+   R xs[3] = {x.x, x.y, x.z};
+   M3<R> gu, gb;
+#pragma unroll
+   for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) gu.m[i][j] = g.ur0 * ((i == j ? ir : R(0)) - xs[i] * xs[j] * ir3);
+   // rotate to the global frame: grad = E^T grad' E (E rows = eprime)
+   M3<R> G;
+#pragma unroll
+   for (int i = 0; i < 3; i++)
+#pragma unroll
+      for (int j = 0; j < 3; j++) {
+         R acc = R(0);
+#pragma unroll
+         for (int a = 0; a < 3; a++)
+#pragma unroll
+            for (int b = 0; b < 3; b++) acc += g.eprime[a][i] * gu.m[a][b] * g.eprime[b][j];
+         G.m[i][j] = acc;
+      }
+   s.gradU = G;
+   if (need_gradB) {
+      R k = g.A * g.w0 / g.ur0;
+      R f = (r - g.r_ref) * ir3, fp = (R(3) * g.r_ref - R(2) * r) * ir2 * ir2;
+      R w[3] = {x.y, -x.x, R(0)};
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+         for (int j = 0; j < 3; j++)
+            gb.m[i][j] = g.A * ((i == j ? ir3 : R(0)) - R(3) * xs[i] * xs[j] * ir3 * ir2) + k * (fp * xs[i] * w[j] * ir);
+      gb.m[0][1] -= k * f;
+      gb.m[1][0] += k * f;
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+         for (int j = 0; j < 3; j++) {
+            R acc = R(0);
+#pragma unroll
+            for (int a = 0; a < 3; a++)
+#pragma unroll
+               for (int b = 0; b < 3; b++) acc += g.eprime[a][i] * gb.m[a][b] * g.eprime[b][j];
+            G.m[i][j] = acc;
+         }
+      s.gradB = G;
+      s.gradBmag = mv(s.gradB, s.bhat);
+   }
+   s.dUdt = mk(R(0), R(0), R(0));
+}
+
+// BackgroundBase::NumericalDerivatives restricted to U and B (src/background_base.cc:228-312):
+// central differences along the field-aligned basis with step r_g = min(r_L, dmax), rotated back
+// to the global frame, then the time derivative of U with step 1/w_g.
+template <int BG, class R>
+__device__ __noinline__ void numerical_derivs(const BgParamsT<R>& g, R t, V3<R> pos, R p, SD<R>& s, unsigned mask)
+{
+   unsigned m1 = mask >> 4, m2 = m1 >> 4;
+   if (m1 & kAll) {
+      R r_g = m_min(larmor(p, s.Bmag), s.dmax);
+      V3<R> fa[3];
+      fa[2] = s.bhat;
+      fa[0] = second_unit(s.bhat);
+      fa[1] = cross(fa[2], fa[0]);
+      M3<R> gu, gbv;
+      R gbm[3];
+#pragma unroll
+      for (int xyz = 0; xyz < 3; xyz++) {
+         SD<R> f, b;
+         R dr = r_g, ds = R(0);
+         V3<R> pt = pos + dr * fa[xyz];
+         eval_bg<BG>(g, t, pt, m1, f, ds);
+         dr *= R(2);
+         pt = pt - dr * fa[xyz];
+         eval_bg<BG>(g, t, pt, m1, b, ds);
+         if (m1 & kU) { gu.m[xyz][0] = (f.U.x - b.U.x) / dr; gu.m[xyz][1] = (f.U.y - b.U.y) / dr; gu.m[xyz][2] = (f.U.z - b.U.z) / dr; }
+         if (m1 & kB) {
+            gbv.m[xyz][0] = (f.B.x - b.B.x) / dr; gbv.m[xyz][1] = (f.B.y - b.B.y) / dr; gbv.m[xyz][2] = (f.B.z - b.B.z) / dr;
+            gbm[xyz] = (norm(f.B) - norm(b.B)) / dr;
+         }
+         s.dr[xyz] = dr;
+      }
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+         for (int j = 0; j < 3; j++) {
+            if (m1 & kU) s.gradU.m[i][j] = fa[0][i] * gu.m[0][j] + fa[1][i] * gu.m[1][j] + fa[2][i] * gu.m[2][j];
+            if (m1 & kB) s.gradB.m[i][j] = fa[0][i] * gbv.m[0][j] + fa[1][i] * gbv.m[1][j] + fa[2][i] * gbv.m[2][j];
+         }
+      if (m1 & kB) {
+         s.gradBmag = mk(fa[0].x * gbm[0] + fa[1].x * gbm[1] + fa[2].x * gbm[2],
+                         fa[0].y * gbm[0] + fa[1].y * gbm[1] + fa[2].y * gbm[2],
+                         fa[0].z * gbm[0] + fa[1].z * gbm[1] + fa[2].z * gbm[2]);
+      }
+   }
+   if (m2 & kAll) {
+      R v = vel_of(p);
+      R w_g = m_min(cyclotron(v, s.Bmag), v / s.dmax);
+      R dt = R(1) / w_g, ds = R(0);
+      SD<R> f, b;
+      eval_bg<BG>(g, t + dt, pos, m2, f, ds);
+      dt *= R(2);
+      eval_bg<BG>(g, t + dt * R(0.5) - dt, pos, m2, b, ds);
+      if (m2 & kU) s.dUdt = (f.U - b.U) / dt;
+   }
+}
+
+// BackgroundBase::GetFields (src/background_base.cc:425-456). Returns false on a field error
+// (|B| below the reference's sp_tiny).
+template <int BG, class R>
+__device__ __forceinline__ bool get_fields(const BgParamsT<R>& g, int deriv_mode, R t, V3<R> pos, R p, unsigned mask,
+                                           SD<R>& s)
+{
+   R ds = R(0);
+   s.dmax = eval_dmax<BG>(g, t, pos);
+   eval_bg<BG>(g, t, pos, mask, s, ds);
+   if (mask & kB) {
+      s.Bmag = norm(s.B);
+      if (!(s.Bmag >= Lim<R>::tiny)) return false;
+      s.bhat = s.B / s.Bmag;
+   }
+   s.dr[0] = s.dr[1] = s.dr[2] = R(0.0001) * g.dmax0;  // incr_dmax_ratio * dmax0 (src/background_base.cc:349)
+   if (!(mask & (kGradU | kGradB | kDUdt))) return true;
+   if (BG == kBgUniform || BG == kBgShock) {
+      zero(s.gradU);
+      zero(s.gradB);
+      s.gradBmag = mk(R(0), R(0), R(0));
+      s.dUdt = mk(R(0), R(0), R(0));
+   }
+   else if (BG == kBgSmoothShock) {  // src/background_smooth_shock.cc:149-183
+      R tr = shock_trd(ds);
+      R fac = tr / g.width;
+      V3<R> du = ld3(g.u0) - ld3(g.u1), db = ld3(g.B0) - ld3(g.B1), n = ld3(g.n_shock);
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+         for (int b = 0; b < 3; b++) {
+            s.gradU.m[a][b] = n[a] * du[b] * fac;
+            s.gradB.m[a][b] = n[a] * db[b] * fac;
+         }
+      s.gradBmag = mv(s.gradB, s.bhat);
+      s.dUdt = (tr * g.v_shock / g.width) * (ld3(g.u1) - ld3(g.u0));
+   }
+   else if (BG == kBgDipole) {  // src/background_dipole.cc:86-115
+      V3<R> pp = pos - ld3(g.r0), M = ld3(g.M);
+      R r2 = norm(pp);
+      R r5 = r2 * r2 * r2;
+      r2 *= r2;
+      r5 *= r2;
+      R mr = dot(M, pp);
+      zero(s.gradU);
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+         for (int b = 0; b < 3; b++)
+            s.gradB.m[a][b] = R(3) * (M[a] * pp[b] + pp[a] * M[b] + mr * ((a == b ? R(1) : R(0)) - R(5) * pp[a] * pp[b] / r2)) / r5;
+      s.gradBmag = mv(s.gradB, s.bhat);
+      s.dUdt = mk(R(0), R(0), R(0));
+   }
+   else if (BG == kBgSolarWind) {
+      if (deriv_mode == 1) solarwind_grad(g, pos, s, (mask & kGradB) != 0);
+      else numerical_derivs<BG>(g, t, pos, p, s, mask);
+   }
+   return true;
+}
+
+// ---- diffusion ---------------------------------------------------------------------------------
+// The reference evaluates one component per DiffusionBase::GetComponent call
+// (src/diffusion_base.cc:105-121); every model computes K_perp and K_para from the same inputs,
+// so both are formed here in one evaluation (the values are those of the two calls). Components a
+// model does not set stay zero, as Kappa is zeroed in DiffusionBase::SetupDiffusion
+// (src/diffusion_base.cc:80-81).
+template <class R>
+struct Kap {
+   R perp, para;
+};
+
+template <class R>
+__device__ Kap<R> kappa_pp(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const SD<R>& s)
+{
+   Kap<R> K{R(0), R(0)};
+   switch (d.kind) {
+   case kDfPara: K.para = d.a[0]; break;                      // src/diffusion_other.cc:381-385
+   case kDfPerp: K.perp = d.a[0]; break;                      // :459-463
+   case kDfFull: K.perp = d.a[0]; K.para = d.a[1]; break;     // :538-543
+   case kDfFlowMomentum:                                      // :622-627
+      K.para = d.a[0] * m_pow(norm(s.U) / d.a[1], d.a[2]) * m_pow(p / d.a[3], d.a[4]);
+      K.perp = d.a[5] * K.para;
+      break;
+   case kDfKinEnergyRadial: {                                 // :713-723
+      R r = norm(pos);
+      R kap_mom = d.a[0] * m_pow(enr_kin(p) / d.a[1], d.a[3]);
+      if (d.i0 == 0 || r < d.a[2]) K.para = kap_mom * m_pow(r / d.a[2], d.a[4]);
+      else if (r < d.a[2] + d.a[7]) { R q = norm(s.U) / d.a[6]; K.para = kap_mom * (q * q); }
+      else K.para = kap_mom * d.a[9];
+      K.perp = d.a[5] * K.para;
+      break;
+   }
+   case kDfRigidityB:                                         // :804-809
+      K.para = (d.a[0] * vmag / R(3)) * m_pow(rigidity(p) / d.a[1], d.a[3]) * m_pow(s.Bmag / d.a[2], d.a[4]);
+      K.perp = d.a[5] * K.para;
+      break;
+   case kDfStrauss2013:
+   case kDfPotgieter2015: {                                   // :886-904, 968-986
+      R lism = (d.i0 < 0) ? R(0) : (s.region[d.i0] > R(0) ? R(0) : R(1));
+      R lk = lism * d.a[1] + (R(1) - lism) * d.a[0];
+      R B0_eff = lism * s.Bmag + (R(1) - lism) * d.a[3];
+      R rig = rigidity(p);
+      if (d.kind == kDfStrauss2013)
+         K.para = (lk * vmag / R(3)) * (rig < d.a[2] ? m_cbrt(rig / d.a[2]) : rig / d.a[2]) * (B0_eff / s.Bmag);
+      else {
+         R q = rig / d.a[2];
+         K.para = lk * (vmag / c_code<R>()) * (rig < d.a[2] ? R(1) : m_sqrt(q * q * q)) * (B0_eff / s.Bmag);
+      }
+      K.perp = (lism * d.a[5] + (R(1) - lism) * d.a[4]) * K.para;
+      break;
+   }
+   case kDfEmpiricalSOQLT: {                                  // :1049-1072
+      R q = rigidity(p) / d.a[2];
+      R c = m_cos(R(0.5) * s.region[d.i1 < 0 ? 0 : (d.i1 > 2 ? 2 : d.i1)]);
+      R damp = R(1) + d.a[6] * (c * c);
+      K.para = ((d.a[0] * vmag / R(3)) * m_cbrt(q * (R(1) + (q * q) * (q * q))) * (d.a[3] / s.Bmag)) / damp;
+      R bmix = (d.i0 < 0) ? R(1) : (s.region[d.i0] < R(0) ? R(0) : R(1));
+      R lam = (norm(pos) < d.a[5]) ? d.a[1] * (bmix + (R(1) - bmix) * d.a[4]) : d.a[1];
+      K.perp = ((lam * vmag / R(3)) * m_cbrt(q * (R(1) + q * q)) * (d.a[3] / s.Bmag)) / damp;
+      break;
+   }
+   default: break;
+   }
+   return K;
+}
+
+// Pitch-angle component D_mumu (Kappa[2]) of the pitch-angle models.
+template <class R>
+__device__ __forceinline__ R kappa_mumu(const DiffParamsT<R>& d, R vmag, R Omega, R mu)
+{
+   R st2 = R(1) - mu * mu;
+   if (d.kind == kDfIsotropic) return d.a[0] * st2;  // src/diffusion_other.cc:64-68
+   if (d.kind == kDfQLT)                              // src/diffusion_other.cc:145-149
+      return R(0.25) * R(3.141592653589793238462643383279502884) * d.a[4] * m_abs(Omega) * st2 *
+             m_pow(vmag * d.a[3] * m_abs(mu / Omega), d.a[4]) * d.a[0];
+   return R(0);
+}
+
+// d D_mumu / d mu: analytic for the isotropic model (src/diffusion_other.cc:76-79), else the
+// one-sided difference of DiffusionBase::GetMuDerivative (src/diffusion_base.cc:226-255).
+template <class R>
+__device__ __forceinline__ R kappa_mumu_dmu(const DiffParamsT<R>& d, R vmag, R Omega, R mu, R dmumu)
+{
+   if (d.kind == kDfIsotropic) return R(-2) * d.a[0] * mu;
+   if (d.kind != kDfQLT) return R(0);
+   R dmu = Lim<R>::small * (mu + Lim<R>::small < R(1) ? R(1) : R(-1));
+   return (kappa_mumu(d, vmag, Omega, mu + dmu) - dmumu) / dmu;
+}
+
+// Spatial gradients of K_perp and K_para: the analytic GetDirectionalDerivative overrides
+// (src/diffusion_other.cc:395-398, 473-476, 553-556, 637-642, 732-742, 818-823), else the
+// base-class central difference with the field moved along its gradient
+// (src/diffusion_base.cc:131-174).
+template <class R>
+__device__ void kappa_grad(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const SD<R>& s, Kap<R> K, V3<R>& gperp,
+                           V3<R>& gpara)
+{
+   switch (d.kind) {
+   case kDfPara: case kDfPerp: case kDfFull:
+      gperp = mk(R(0), R(0), R(0));
+      gpara = gperp;
+      return;
+   case kDfFlowMomentum: {
+      R un2 = norm2(s.U);
+      V3<R> gl = mk(dot(row(s.gradU, 0), s.U), dot(row(s.gradU, 1), s.U), dot(row(s.gradU, 2), s.U));
+      gperp = (K.perp * d.a[2] / un2) * gl;
+      gpara = (K.para * d.a[2] / un2) * gl;
+      return;
+   }
+   case kDfKinEnergyRadial: {
+      R r = norm(pos);
+      V3<R> gl;
+      if (d.i0 == 0 || r < d.a[2]) gl = (d.a[4] / (r * r)) * pos;
+      else if (r < d.a[2] + d.a[7]) {
+         R un2 = norm2(s.U);
+         gl = (R(2) / un2) * mk(dot(row(s.gradU, 0), s.U), dot(row(s.gradU, 1), s.U), dot(row(s.gradU, 2), s.U));
+      }
+      else gl = mk(R(0), R(0), R(0));
+      gperp = K.perp * gl;
+      gpara = K.para * gl;
+      return;
+   }
+   case kDfRigidityB: {
+      V3<R> gl = (d.a[4] / s.Bmag) * s.gradBmag;
+      gperp = K.perp * gl;
+      gpara = K.para * gl;
+      return;
+   }
+   default: {
+      R gpe[3], gpa[3];
+#pragma unroll 1
+      for (int xyz = 0; xyz < 3; xyz++) {
+         SD<R> s2 = s;
+         R dr = R(0.5) * s.dr[xyz];
+         R e[3] = {R(0), R(0), R(0)};
+         e[xyz] = dr;
+         s2.B = s.B + dr * row(s.gradB, xyz);
+         s2.Bmag = s.Bmag + s.gradBmag[xyz] * dr;
+         Kap<R> kf = kappa_pp(d, pos + mk(e[0], e[1], e[2]), p, vmag, s2);
+         s2.B = s2.B - (R(2) * dr) * row(s.gradB, xyz);
+         s2.Bmag = s2.Bmag - s.gradBmag[xyz] * (R(2) * dr);
+         e[xyz] = dr - R(2) * dr;
+         Kap<R> kb = kappa_pp(d, pos + mk(e[0], e[1], e[2]), p, vmag, s2);
+         gpe[xyz] = (kf.perp - kb.perp) / (R(2) * dr);
+         gpa[xyz] = (kf.para - kb.para) / (R(2) * dr);
+      }
+      gperp = mk(gpe[0], gpe[1], gpe[2]);
+      gpara = mk(gpa[0], gpa[1], gpa[2]);
+      return;
+   }
+   }
+}
+
+// ---- boundaries ---------------------------------------------------------------------------------
+// Transient state of one boundary (src/boundary_base.hh): delta, delta_old, crossings left,
+// crossed flag; TERMINAL is crossings_left == 1 (src/boundary_base.cc:150-151, 187-188).
+template <class R>
+struct BndState {
+   R delta, delta_old;
+   int crossings_left;
+   int crossed;
+};
+
+// Outward normal of a reflecting spatial boundary at "pos" (the _normal of EvaluateBoundary).
+template <class R>
+__device__ V3<R> bnd_normal(const BndParamsT<R>& b, V3<R> pos)
+{
+   switch (b.kind) {
+   case kBtPlaneAbsorb: case kBtPlaneReflect: case kBtPlanePass: return ld3(b.norm);
+   case kBtBoxReflect: {
+      R best = -Lim<R>::large;
+      V3<R> nrm = mk(R(0), R(0), R(0));
+      for (int s = 0; s < 3; s++) {
+         V3<R> n = ld3(b.normals[s]);
+         R d1 = -dot(pos - ld3(b.corner0), n);
+         if (d1 > best) { best = d1; nrm = R(-1) * n; }
+         R d2 = dot(pos - ld3(b.corner1), n);
+         if (d2 > best) { best = d2; nrm = n; }
+      }
+      return nrm;
+   }
+   case kBtSphereAbsorb: case kBtSphereReflect: case kBtSpherePass: return unit(pos - ld3(b.origin));
+   case kBtCylinderAbsorb: {
+      V3<R> fa[3] = {ld3(b.fa[0]), ld3(b.fa[1]), ld3(b.fa[2])};
+      V3<R> pr = to_basis(pos - ld3(b.origin), fa);
+      pr.z = R(0);
+      return from_basis(unit(pr), fa);
+   }
+   default: return mk(R(0), R(0), R(0));
+   }
+}
+
+// EvaluateBoundary of every boundary class (src/boundary_time.cc, src/boundary_space.cc,
+// src/boundary_momentum.cc). For time boundaries the delta is formed from the accumulated time.
+template <class R, class A>
+__device__ __forceinline__ void eval_bnd(const BndParamsT<R>& b, BndState<R>& st, const A& t, V3<R> pos, V3<R> mom,
+                                         V3<R> bhat, V3<R> region, int traj)
+{
+   switch (b.kind) {
+   case kBtTimeExpire: case kBtTimePass: st.delta = (R)acc_diff(t, b.timemark, b.timemark_lo); break;
+   case kBtTimeRecurrent: {
+      R k = (R)((b.max_crossings - st.crossings_left) + 1);
+      st.delta = (R)acc_diff(t, k * b.timemark, k * b.timemark_lo);
+      break;
+   }
+   case kBtPlaneAbsorb: case kBtPlaneReflect: case kBtPlanePass:
+      st.delta = dot(pos - ld3(b.origin), ld3(b.norm));
+      break;
+   case kBtBoxReflect: {
+      st.delta = -Lim<R>::large;
+#pragma unroll
+      for (int s = 0; s < 3; s++) {
+         V3<R> n = ld3(b.normals[s]);
+         R d1 = -dot(pos - ld3(b.corner0), n);
+         if (d1 > st.delta) st.delta = d1;
+         R d2 = dot(pos - ld3(b.corner1), n);
+         if (d2 > st.delta) st.delta = d2;
+      }
+      break;
+   }
+   case kBtSphereAbsorb: case kBtSphereReflect: case kBtSpherePass: {
+      st.delta = norm(pos - ld3(b.origin)) - b.radius;
+      break;
+   }
+   case kBtRankineAbsorb: {
+      V3<R> pr = pos - ld3(b.origin);
+      R z = dot(pr, ld3(b.axis)), r = norm(pr);
+      st.delta = r - b.z_nose * m_sqrt(R(2) / (R(1) + z / r));
+      break;
+   }
+   case kBtCylinderAbsorb: {
+      V3<R> fa[3] = {ld3(b.fa[0]), ld3(b.fa[1]), ld3(b.fa[2])};
+      V3<R> pr = to_basis(pos - ld3(b.origin), fa);
+      st.delta = m_sqrt(pr.x * pr.x + pr.y * pr.y) - b.radius;
+      break;
+   }
+   case kBtRegionAbsorb: st.delta = region[b.region_ind] - b.region_val; break;
+   case kBtMomentumInject: case kBtMomentumPass: case kBtMomentumSlab: case kBtMomentumShell:
+      st.delta = (traj == kLorentz ? norm(mom) : mom.x) - b.momentum;
+      if (b.kind == kBtMomentumSlab && st.delta * st.delta_old < R(0)) {
+         if (dot(pos - ld3(b.slab_r0), ld3(b.slab_n)) * dot(pos - ld3(b.slab_r1), ld3(b.slab_n)) > R(0)) st.delta_old = st.delta;
+      }
+      if (b.kind == kBtMomentumShell && st.delta * st.delta_old < R(0)) {
+         R rd = norm(pos - ld3(b.slab_r0));
+         if (rd < b.r1 || rd > b.r2) st.delta_old = st.delta;
+      }
+      break;
+   case kBtMirror: st.delta = (traj == kFocused) ? mom.x * mom.y : dot(mom, bhat); break;
+   }
+}
+
+// BoundaryBase::ResetBoundary (src/boundary_base.cc:138-162)
+template <class R, class A>
+__device__ __forceinline__ void reset_bnd(const BndParamsT<R>& b, BndState<R>& st, R scale, const A& t, V3<R> pos,
+                                          V3<R> mom, V3<R> bhat, V3<R> region, int traj)
+{
+   st.crossings_left = b.max_crossings;
+   st.delta_old = R(0);
+   eval_bnd(b, st, t, pos, mom, bhat, region, traj);
+   st.delta_old = st.delta;
+   if (st.delta_old == R(0)) st.delta_old = -Lim<R>::tiny * m_abs(scale);
+   st.crossed = 0;
+}
+
+// BoundaryBase::ComputeBoundary (src/boundary_base.cc:105-127)
+template <class R, class A>
+__device__ __forceinline__ void compute_bnd(const BndParamsT<R>& b, BndState<R>& st, const A& t, V3<R> pos, V3<R> mom,
+                                            V3<R> bhat, V3<R> region, int traj)
+{
+   eval_bnd(b, st, t, pos, mom, bhat, region, traj);
+   if (st.delta * st.delta_old <= R(0)) {
+      st.crossed = 1;
+      if (st.delta * st.delta_old == R(0)) st.delta = -st.delta_old;
+   }
+   else st.crossed = 0;
+}
+
+// BoundaryBase::RecordBoundary (src/boundary_base.cc:168-191)
+template <class R, class A>
+__device__ __forceinline__ void record_bnd(const BndParamsT<R>& b, BndState<R>& st, const A& t, V3<R> pos, V3<R> mom,
+                                           V3<R> bhat, V3<R> region, int traj)
+{
+   if (st.crossed) {
+      st.crossings_left--;
+      if (b.recurrent) eval_bnd(b, st, t, pos, mom, bhat, region, traj);
+      else st.delta_old = st.delta;
+      st.crossed = 0;
+   }
+   else st.delta_old = st.delta;
+}
+
+}  // namespace spx

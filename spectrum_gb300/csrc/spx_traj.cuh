@@ -1,0 +1,907 @@
+// spx_traj.cuh -- the per-trajectory stepping loop on the device: SetStart, the Parker
+// Euler-Maruyama advance, the Runge-Kutta advance of Lorentz and focused trajectories (with the
+// Euler pitch-angle scattering step), boundary handling, distribution events, and the kernel
+// that schedules trajectories onto lanes.
+//
+// One lane integrates one trajectory. The state a lane carries from step to step is only time,
+// position, momentum, weights, the time-step memory and the boundary deltas; the fields are
+// evaluated at the start of every step (the reference evaluates them at the end of the previous
+// step, src/trajectory_parker.cc:300, which gives the same values). The plain schedule gives
+// lane k the trajectories k, k + stride, ...; the queue schedule refills finished lanes from a
+// global work-queue counter, one atomic per warp and refill, lanes ranked with __ballot_sync/__popc.
+#pragma once
+
+#include "spx_physics.cuh"
+
+namespace spx {
+
+constexpr uint32_t TRAJ_FINISH = 0x0010u, TRAJ_TIME_CROSSED = 0x0020u, TRAJ_SPATIAL_CROSSED = 0x0040u,
+                   TRAJ_MOMENTUM_CROSSED = 0x0080u, TRAJ_DISCARD = 0x0100u, TRAJ_GAVE_UP = 0x10000u;
+constexpr uint32_t kMaxTrajSteps = 10000000u;  // src/trajectory_base.hh:38
+constexpr int kMaxBndTotal = 3 * kMaxBnd;
+
+constexpr unsigned kErrAction = 1u;  // RunCounters::error: an action beyond the ActionTable
+
+// Lane state carried across steps.
+template <class R, class A>
+struct Lane {
+   int prob;
+   uint32_t traj_id, attempt, steps, status;
+   A t;
+   AV3<A> pos, mom;  // mom: Parker (p,-,-), Focused (p, mu, -), Lorentz (px, py, pz)
+   R amp, wgt, dt, dt_adapt, src_del_old;
+};
+
+// Initial point of the trajectory (needed only by events and records).
+struct Start {
+   double t0;
+   V3<double> pos0, mom0, bhat0;
+};
+
+struct Sinks {
+   int32_t* counts;
+   double* sums;
+   unsigned long long* n_events;  // [problem * kMaxDistro + distro]
+   RunCounters* ctr;
+};
+
+template <class R, class A>
+__device__ __forceinline__ V3<R> lane_mom(const Lane<R, A>& L) { return val3<R>(L.mom); }
+
+__device__ __forceinline__ double neg(double a) { return -a; }
+__device__ __forceinline__ FF neg(FF a) { return {-a.hi, -a.lo}; }
+
+template <int TT>
+__device__ __forceinline__ constexpr unsigned traj_mask()
+{
+   return TT == kLorentz ? (kE | kB)                                 // src/trajectory_lorentz.cc:36
+        : TT == kFocused ? (kAll | kGradB | kGradU | kDUdt)           // src/trajectory_focused.cc:40
+                         : (kU | kB | kGradU | kGradB);               // src/trajectory_parker.cc:204
+}
+
+// Momentum magnitude passed to the field evaluators (ConvertMomentum()[0]).
+template <int TT, class R>
+__device__ __forceinline__ R field_p(V3<R> mom) { return TT == kLorentz ? norm(mom) : mom.x; }
+
+// ---- random numbers for set-up -----------------------------------------------------------
+struct InitRng {
+   uint64_t seed;
+   uint32_t traj, problem, attempt, n_uniform, n_normal;
+   __device__ double uniform()
+   {
+      uint32_t k = n_uniform++;
+      uint4 b = rng_block(seed, k >> 2, traj, problem, kRngInit, attempt);
+      uint32_t x = (k & 3) == 0 ? b.x : ((k & 3) == 1 ? b.y : ((k & 3) == 2 ? b.z : b.w));
+      return u01d(x);
+   }
+   __device__ double normal()
+   {
+      uint32_t j = n_normal++;
+      double n[4];
+      normals4<double>(rng_block(seed, j >> 2, traj, problem, kRngInitNormal, attempt), n);
+      return n[j & 3];
+   }
+};
+
+// ---- initial conditions (src/initial_*.cc), sampled in FP64 once per trajectory ------------
+static __device__ __noinline__ double sample_time(InitRng& rng, const ProblemDesc& P, int64_t local)
+{
+   const IniParams& q = P.it;
+   if (q.kind == kItInterval) {
+      if (q.n_int <= 0) return q.a[0] + (q.a[1] - q.a[0]) * rng.uniform();
+      // trajectory k takes the k-th element of the sequence (the reference steps a per-process counter)
+      return q.a[0] + ((double)local + 0.5) * ((q.a[1] - q.a[0]) / (double)q.n_int);
+   }
+   return q.a[0];
+}
+
+static __device__ __noinline__ V3<double> sample_pos(InitRng& rng, const ProblemDesc& P, int64_t local)
+{
+   const IniParams& q = P.is;
+   const double two_pi = 6.283185307179586476925286766559;
+   V3<double> v0 = ld3(q.v0), v1 = ld3(q.v1), v2 = ld3(q.v2);
+   switch (q.kind) {
+   case kIsLine:
+      if (q.n_int <= 0) return v0 + rng.uniform() * (v1 - v0);
+      return v0 + ((double)local + 0.5) * ((v1 - v0) / (double)q.n_int);
+   case kIsBox: {
+      double x = q.v0[0] + (q.v1[0] - q.v0[0]) * rng.uniform();
+      double y = q.v0[1] + (q.v1[1] - q.v0[1]) * rng.uniform();
+      double z = q.v0[2] + (q.v1[2] - q.v0[2]) * rng.uniform();
+      return mk(x, y, z);
+   }
+   case kIsCircle: {
+      double phi = two_pi * rng.uniform();
+      return (v0 + cos(phi) * v1) + sin(phi) * v2;
+   }
+   case kIsSphere:
+   case kIsSphereSector: {
+      double ct, st, phi;
+      if (q.kind == kIsSphere) {
+         ct = -1.0 + 2.0 * rng.uniform();
+         st = sqrt(1.0 - ct * ct);
+         phi = two_pi * rng.uniform();
+      }
+      else {
+         ct = q.a[5] + (q.a[6] - q.a[5]) * rng.uniform();
+         st = sqrt(1.0 - ct * ct);
+         phi = q.a[3] + (q.a[4] - q.a[3]) * rng.uniform();
+      }
+      return v0 + mk(q.a[0] * st * cos(phi), q.a[0] * st * sin(phi), q.a[0] * ct);
+   }
+   case kIsRankine: {
+      double ct = q.a[2] + (1.0 - q.a[2]) * rng.uniform();
+      double r = q.a[0] * sqrt(2.0 / (1.0 + ct)), z = r * ct, s = sqrt(r * r - z * z);
+      double phi = two_pi * rng.uniform();
+      return v0 + mk(s * cos(phi), s * sin(phi), z);
+   }
+   case kIsEquatorialBand: {
+      double Lv = q.a[1] + (q.a[2] - q.a[1]) * rng.uniform();
+      double phi = two_pi * rng.uniform();
+      return v0 + mk(Lv * q.a[0] * cos(phi), Lv * q.a[0] * sin(phi), 0.0);
+   }
+   default: return v0;
+   }
+}
+
+// GetMomSample(axis) (src/initial_base.cc:133-143) with the samplers of
+// src/initial_momentum.cc; the result is in the trajectory's native momentum coordinates.
+static __device__ __noinline__ V3<double> sample_mom(InitRng& rng, const ProblemDesc& P, int traj, V3<double> axis_in)
+{
+   const IniParams& q = P.im;
+   V3<double> axis = unit(axis_in);
+   const double two_pi = 6.283185307179586476925286766559;
+   switch (q.kind) {
+   case kImFixed: return ld3(q.v0);
+   case kImBeam:
+      if (traj == kLorentz) return q.a[0] * axis;
+      return mk(q.a[0], 0.0, 0.0);
+   case kImRing:
+      if (traj == kLorentz) {
+         double phi = two_pi * rng.uniform();
+         V3<double> e1 = second_unit(axis), e2 = cross(axis, e1);
+         return (q.a[0] * q.a[2]) * axis + (q.a[0] * q.a[3]) * (cos(phi) * e1 + sin(phi) * e2);
+      }
+      return mk(q.a[0], q.a[2], 0.0);
+   case kImShell:
+   case kImThickShell: {
+      double p = q.a[0];
+      if (q.kind == kImThickShell) {
+         if (q.flag) p = pow(10.0, q.a[0] + (q.a[1] - q.a[0]) * rng.uniform());
+         else p = q.a[0] + (q.a[1] - q.a[0]) * rng.uniform();
+      }
+      if (traj == kParker || traj == kParkerSource) return mk(p, 0.0, 0.0);
+      if (traj == kFocused) { double mu = -1.0 + 2.0 * rng.uniform(); return mk(p, mu, 0.0); }
+      double mu = -1.0 + 2.0 * rng.uniform(), st = sqrt(1.0 - mu * mu), phi = two_pi * rng.uniform();
+      return mk(p * st * cos(phi), p * st * sin(phi), p * mu);
+   }
+   case kImMaxwell: {
+      double p_para = q.a[0] + q.a[1] * rng.normal();
+      double p_perp = q.a[2] * sqrt(-2.0 * log(rng.uniform()));
+      if (traj == kLorentz) {
+         double phi = two_pi * rng.uniform();
+         V3<double> e1 = second_unit(axis), e2 = cross(axis, e1);
+         return p_para * axis + p_perp * (cos(phi) * e1 + sin(phi) * e2);
+      }
+      double p = sqrt(p_para * p_para + p_perp * p_perp);
+      if (traj == kFocused) return mk(p, p_para / p, 0.0);
+      return mk(p, 0.0, 0.0);
+   }
+   case kImLogEnergyPitchBand: {
+      double le1 = log(q.a[0]), le2 = log(q.a[1]);
+      double e = exp(le1 + (le2 - le1) * rng.uniform());
+      double mu = q.a[2] + (q.a[3] - q.a[2]) * rng.uniform();
+      double p = mom_of<double>(e);
+      if (traj == kLorentz) {
+         double psi = two_pi * rng.uniform(), st = sqrt(1.0 - mu * mu);
+         V3<double> e1 = second_unit(axis), e2 = cross(axis, e1);
+         return (p * mu) * axis + (p * st) * (cos(psi) * e1 + sin(psi) * e2);
+      }
+      if (traj == kFocused) return mk(p, mu, 0.0);
+      return mk(p, 0.0, 0.0);
+   }
+   }
+   return mk(0.0, 0.0, 0.0);
+}
+
+// ---- distribution events (DistributionBase::ProcessTrajectory, src/distribution_base.cc:174-194;
+// DistributionTemplated::AddEvent, src/distribution_templated.cc:145-181), in FP64 ----------
+// The event's "second point" is the current state; its spatial data are the fields of the
+// step's start point, as in the reference (HandleBoundaries runs before CommonFields).
+struct EventPoint {
+   double t;
+   V3<double> pos, mom, bhat;
+   double divU, amp, wgt;
+};
+
+static __device__ __noinline__ void process_event(int traj, const EventPoint& e, const Start& s0, const ProblemDesc& P,
+                                           int prob, int di, int action, const Sinks& S)
+{
+   const DistParams& d = P.d[di];
+   if (action >= d.n_actions) {
+      atomicCAS(&S.ctr->error, 0u, kErrAction);
+      return;
+   }
+   V3<double> value = mk(0.0, 0.0, 0.0);
+   double w[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+   switch (d.kind) {
+   case kDsTimeUniform: value.x = d.val_time == 0 ? s0.t0 : e.t; break;
+   case kDsPositionUniform:
+      value = d.val_time == 0 ? s0.pos0 : e.pos;
+      if (d.val_coord == 1) {  // Metric<SphericalRTP>::PosToCurv, common/coordinates.hh:124-135
+         double r = norm(value), phi = atan2(value.y, value.x);
+         if (phi < 0.0) phi += 6.283185307179586476925286766559;
+         value = mk(r, acos(value.z / r), phi);
+      }
+      break;
+   case kDsMomentumUniform: {
+      V3<double> m = d.val_time == 0 ? s0.mom0 : e.mom;
+      V3<double> bh = d.val_time == 0 ? s0.bhat0 : e.bhat;
+      if (d.val_coord == 0 || traj != kLorentz) value = m;
+      else { double mm = norm(m); value = mk(mm, dot(m, bh) / mm, 0.0); }
+      break;
+   }
+   case kDsPositionMomentumUniform: {
+      V3<double> p = d.val_time == 0 ? s0.pos0 : e.pos, m = d.val_time == 0 ? s0.mom0 : e.mom;
+      value.x = d.pos_idx == 3 ? norm(p) : p[d.pos_idx];
+      value.y = m[d.mom_idx];
+      break;
+   }
+   case kDsSpectrumPowerLaw: case kDsSpectrumBentPowerLaw:
+      value.x = enr_kin<double>(traj == kLorentz ? norm(s0.mom0) : s0.mom0.x);
+      break;
+   case kDsCumulative1: case kDsCumulative2: value.x = e.t; break;
+   case kDsDivergenceFlow: value = s0.mom0; break;
+   case kDsTimeMu:
+      value.x = e.t;
+      value.y = traj == kLorentz ? dot(e.mom, e.bhat) / norm(e.mom) : e.mom.y;
+      break;
+   }
+   switch (d.kind) {
+   case kDsTimeUniform: case kDsPositionUniform: case kDsMomentumUniform: case kDsPositionMomentumUniform: case kDsTimeMu:
+      w[0] = action == 0 ? d.val_hot : d.val_cold;
+      break;
+   case kDsSpectrumPowerLaw: case kDsSpectrumBentPowerLaw:
+      if (action == 0) {  // DISTRO_KINETIC_ENERGY_POWER_LAW_TYPE 0, src/distribution_other.cc:567-591
+         double m2 = traj == kLorentz ? norm(e.mom) : e.mom.x;
+         double ke = enr_kin<double>(m2), v = vel_of<double>(m2);
+         w[0] = d.J0 * v * pow(ke / d.T0, d.pow_law) / (m2 * m2);
+         if (d.kind == kDsSpectrumBentPowerLaw) w[0] /= pow(1.0 + pow(ke / d.T_b, d.pow_law_comb), d.bend);
+      }
+      else w[0] = d.val_cold;
+      break;
+   case kDsCumulative1: { V3<double> dp = e.pos - s0.pos0; w[0] = dp.x; w[1] = dp.y; w[2] = dp.z; break; }
+   case kDsCumulative2: {
+      V3<double> dp = e.pos - s0.pos0;
+      for (int i = 0; i < 3; i++)
+         for (int j = 0; j < 3; j++) w[3 * i + j] = dp[i] * dp[j];
+      break;
+   }
+   case kDsDivergenceFlow: w[0] = action == 0 ? d.A0 * pow(fabs(e.divU), d.pow_law) : d.val_cold; break;
+   }
+   int bin[3] = {0, 0, 0};
+   for (int k = 0; k < 3; k++) {
+      if (!(d.dims & (1 << k))) continue;
+      double val = (d.log_bins[k] ? log10(value[k]) : value[k]) - d.limits0[k];
+      if (!(val >= 0.0)) {
+         if (d.bin_outside[k] && val < 0.0) { bin[k] = 0; continue; }
+         return;
+      }
+      double q = val / d.bin_size[k];
+      if (q >= (double)d.n_bins[k]) {
+         if (d.bin_outside[k]) { bin[k] = d.n_bins[k] - 1; continue; }
+         return;
+      }
+      bin[k] = (int)q;
+   }
+   int64_t lin = (int64_t)d.n_bins[2] * ((int64_t)d.n_bins[1] * bin[0] + bin[1]) + bin[2];
+   double ew = exp(e.wgt);
+   for (int k = 0; k < d.width; k++) atomicAdd(&S.sums[d.offset_sums + lin * d.width + k], w[k] * ew + e.amp);
+   atomicAdd(&S.counts[d.offset_counts + lin], 1);
+   atomicAdd(&S.n_events[(int64_t)prob * kMaxDistro + di], 1ull);
+}
+
+template <class R, class A>
+__device__ __forceinline__ EventPoint event_point(const Lane<R, A>& L, const SD<R>& sp)
+{
+   EventPoint e;
+   e.t = acc_dbl(L.t);
+   e.pos = mk(acc_dbl(L.pos.x), acc_dbl(L.pos.y), acc_dbl(L.pos.z));
+   e.mom = mk(acc_dbl(L.mom.x), acc_dbl(L.mom.y), acc_dbl(L.mom.z));
+   e.bhat = mk((double)sp.bhat.x, (double)sp.bhat.y, (double)sp.bhat.z);
+   e.divU = (double)sd_divU(sp);
+   e.amp = (double)L.amp;
+   e.wgt = (double)L.wgt;
+   return e;
+}
+
+template <int TT, class R, class A>
+__device__ __forceinline__ void distro_events(const Lane<R, A>& L, const SD<R>& sp, const Start& s0,
+                                              const ProblemDesc& Pd, int bnd_global, const Sinks& S)
+{
+   const BndParams& b = bnd_global < kMaxBnd ? Pd.bt[bnd_global]
+                      : (bnd_global < 2 * kMaxBnd ? Pd.bs[bnd_global - kMaxBnd] : Pd.bm[bnd_global - 2 * kMaxBnd]);
+   EventPoint e = event_point(L, sp);
+   for (int di = 0; di < Pd.nd; di++) {
+      int action = di < b.n_actions ? b.actions[di] : -1;
+      if (action >= 0) process_event(TT, e, s0, Pd, L.prob, di, action, S);
+   }
+}
+
+// Boundary slots: 0..3 time, 4..7 space, 8..11 momentum.
+template <class R>
+__device__ __forceinline__ const BndParamsT<R>& bnd_param(const ProblemDescT<R>& P, int k)
+{
+   return k < kMaxBnd ? P.bt[k] : (k < 2 * kMaxBnd ? P.bs[k - kMaxBnd] : P.bm[k - 2 * kMaxBnd]);
+}
+template <class R>
+__device__ __forceinline__ bool bnd_used(const ProblemDescT<R>& P, int k)
+{
+   return k < kMaxBnd ? k < P.nbt : (k < 2 * kMaxBnd ? k - kMaxBnd < P.nbs : k - 2 * kMaxBnd < P.nbm);
+}
+
+// ---- HandleBoundaries (src/trajectory_base.cc:413-535) ---------------------------------------
+template <int TT, class R, class A>
+__device__ void handle_boundaries(Lane<R, A>& L, BndState<R>* bs, const SD<R>& sp, const Start& s0,
+                                  const ProblemDescT<R>& P, const ProblemDesc& Pd, const Sinks& S)
+{
+   V3<R> pos = val3<R>(L.pos), mom = lane_mom(L);
+   unsigned crossed = 0;
+#pragma unroll 1
+   for (int k = 0; k < kMaxBndTotal; k++) {
+      if (!bnd_used(P, k)) continue;
+      compute_bnd(bnd_param(P, k), bs[k], L.t, pos, mom, sp.bhat, sp.region, TT);
+      if (bs[k].crossed) crossed |= 1u << k;
+   }
+   if (crossed) {
+      // momentum boundaries
+      int active = -1;
+      for (int k = 2 * kMaxBnd; k < 3 * kMaxBnd; k++) {
+         if (!(crossed & (1u << k))) continue;
+         active = k;
+         if (!bnd_param(P, k).reflect && bs[k].crossings_left == 1) L.status |= TRAJ_MOMENTUM_CROSSED | TRAJ_FINISH;
+      }
+      if (active >= 0) distro_events<TT>(L, sp, s0, Pd, active, S);
+      // spatial boundaries
+      active = -1;
+      for (int k = kMaxBnd; k < 2 * kMaxBnd; k++) {
+         if (!(crossed & (1u << k))) continue;
+         active = k;
+         const BndParamsT<R>& b = bnd_param(P, k);
+         if (b.reflect) {
+            // src/trajectory_base.cc:462-483: mirror the position, reverse the momentum
+            V3<R> shift = (R(2) * bs[k].delta) * bnd_normal(b, pos);
+            add3(L.pos, R(-1) * shift);
+            if (TT != kParker && TT != kParkerSource) {
+               L.mom.x = neg(L.mom.x); L.mom.y = neg(L.mom.y); L.mom.z = neg(L.mom.z);
+            }
+            pos = val3<R>(L.pos);
+            mom = lane_mom(L);
+            compute_bnd(b, bs[k], L.t, pos, mom, sp.bhat, sp.region, TT);
+            bs[k].crossings_left--;
+         }
+         else if (bs[k].crossings_left == 1) L.status |= TRAJ_SPATIAL_CROSSED | TRAJ_FINISH;
+      }
+      if (active >= 0) distro_events<TT>(L, sp, s0, Pd, active, S);
+      // time boundaries
+      active = -1;
+      for (int k = 0; k < kMaxBnd; k++) {
+         if (!(crossed & (1u << k))) continue;
+         active = k;
+         if (bs[k].crossings_left == 1) L.status |= TRAJ_TIME_CROSSED | TRAJ_FINISH;
+      }
+      if (active >= 0) distro_events<TT>(L, sp, s0, Pd, active, S);
+   }
+#pragma unroll 1
+   for (int k = 0; k < kMaxBndTotal; k++)
+      if (bnd_used(P, k)) record_bnd(bnd_param(P, k), bs[k], L.t, pos, mom, sp.bhat, sp.region, TT);
+}
+
+// SpaceTerminateCheck (src/trajectory_base.cc:188-237); true if the trajectory ended mid-step
+template <int TT, class R, class A>
+__device__ bool space_terminate(Lane<R, A>& L, BndState<R>* bs, const SD<R>& sp, const Start& s0,
+                                const ProblemDescT<R>& P, const ProblemDesc& Pd, const Sinks& S)
+{
+   V3<R> pos = val3<R>(L.pos), mom = lane_mom(L);
+   for (int k = kMaxBnd; k < kMaxBnd + P.nbs; k++) {
+      compute_bnd(bnd_param(P, k), bs[k], L.t, pos, mom, sp.bhat, sp.region, TT);
+      if (bs[k].crossed && bs[k].crossings_left == 1) {
+         L.status |= TRAJ_SPATIAL_CROSSED | TRAJ_FINISH;
+         distro_events<TT>(L, sp, s0, Pd, k, S);
+         L.steps++;
+         return true;
+      }
+   }
+   return false;
+}
+
+// TimeBoundaryProximityCheck (src/trajectory_base.cc:151-179)
+template <class R>
+__device__ __forceinline__ R time_proximity(R dt, R dmax, const BndState<R>* bs, int nbt, bool fwd)
+{
+   R c = c_code<R>();
+   R dn = fwd ? -Lim<R>::large * dmax / c : Lim<R>::large * dmax / c;
+   for (int b = 0; b < nbt; b++) {
+      R delta = bs[b].delta;
+      if (fwd) { if (delta <= R(0) && delta > dn) dn = delta; }
+      else { if (delta >= R(0) && delta < dn) dn = delta; }
+   }
+   if (fwd) { if (dt >= -dn) dt = m_max(-(R(1) + Lim<R>::little) * dn, Lim<R>::small * dmax / c); }
+   else { if (dt >= dn) dt = m_max((R(1) + Lim<R>::little) * dn, Lim<R>::small * dmax / c); }
+   return dt;
+}
+
+// ---- Parker (src/trajectory_parker.cc:83-306) ----------------------------------------------
+template <int BG, class R>
+__device__ __noinline__ bool parker_divk_fd(const ProblemDescT<R>& P, int deriv_mode, R t, V3<R> pos, R p, R vmag,
+                                            const SD<R>& sp, V3<R>& divK)
+{
+   // TRAJ_PARKER_DIVK_METHOD 0 (src/trajectory_parker.cc:87-119): central differences of the tensor
+   R delta = m_min(larmor(p, sp.Bmag), sp.dmax);
+   R dk[3] = {R(0), R(0), R(0)};
+#pragma unroll 1
+   for (int j = 0; j < 3; j++) {
+      SD<R> sf, sb;
+      R pt[3] = {pos.x, pos.y, pos.z};
+      pt[j] = pt[j] + delta;
+      if (!get_fields<BG>(P.bg, deriv_mode, t, mk(pt[0], pt[1], pt[2]), p, kU | kB, sf)) return false;
+      Kap<R> kf = kappa_pp(P.df, mk(pt[0], pt[1], pt[2]), p, vmag, sf);
+      pt[j] -= R(2) * delta;
+      if (!get_fields<BG>(P.bg, deriv_mode, t, mk(pt[0], pt[1], pt[2]), p, kU | kB, sb)) return false;
+      Kap<R> kb = kappa_pp(P.df, mk(pt[0], pt[1], pt[2]), p, vmag, sb);
+      for (int i = 0; i < 3; i++) {
+         R f = kf.perp * (i == j ? R(1) : R(0)) + (kf.para - kf.perp) * sf.bhat[j] * sf.bhat[i];
+         R b = kb.perp * (i == j ? R(1) : R(0)) + (kb.para - kb.perp) * sb.bhat[j] * sb.bhat[i];
+         dk[i] += R(0.5) * (f - b) / delta;
+      }
+   }
+   divK = mk(dk[0], dk[1], dk[2]);
+   return true;
+}
+
+template <int BG, class R, class A>
+__device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndState<R>* bs, const Start& s0,
+                                               const ProblemDescT<R>& P, const ProblemDesc& Pd, const RunConfig& cfg,
+                                               const Sinks& S)
+{
+   constexpr bool kFP64 = sizeof(R) == sizeof(double);
+   const bool fwd = cfg.time_flow == 0;
+   const int deriv_mode = kFP64 ? cfg.deriv_mode : 1;
+   V3<R> pos = val3<R>(L.pos);
+   R p = (R)acc_val(L.mom.x);
+   R t = (R)acc_val(L.t);
+   SD<R> sp;
+   if (!get_fields<BG>(P.bg, deriv_mode, t, pos, p, traj_mask<kParker>(), sp)) { L.status |= TRAJ_DISCARD; return; }
+   R vmag = vel_of(p);
+   // DiffusionCoeff (src/trajectory_parker.cc:83-153)
+   Kap<R> K = kappa_pp(P.df, pos, p, vmag, sp);
+   V3<R> divK;
+   if (kFP64 && deriv_mode == 0) {
+      if (!parker_divk_fd<BG>(P, deriv_mode, t, pos, p, vmag, sp, divK)) { L.status |= TRAJ_DISCARD; return; }
+   }
+   else {
+      // TRAJ_PARKER_DIVK_METHOD 1 (src/trajectory_parker.cc:120-140)
+      V3<R> gpe, gpa;
+      kappa_grad(P.df, pos, p, vmag, sp, K, gpe, gpa);
+      V3<R> t1 = gpa - gpe;
+      divK = (gpe + dot(sp.bhat, t1) * sp.bhat) + (K.para - K.perp) * (sd_divbhat(sp) * sp.bhat + sd_b_gradbhat(sp));
+   }
+   V3<R> slope = fwd ? sp.U + divK : sp.U - divK;
+   R divU = sd_divU(sp);
+   R slope_p = -p * divU / R(3);
+   R sa = R(0);
+   if (P.src.kind == 2) {
+      // TrajectoryParkerSource::Slopes / SourceMomentumInjection::EvaluateSource
+      // (src/trajectory_parker_source.cc:58-66, src/source_other.cc:113-119); dt is the previous step's
+      R del = p - P.src.p_inj;
+      if (del * L.src_del_old < R(0)) sa = P.src.rate / L.dt;
+      L.src_del_old = del;
+   }
+   // PhysicalStep (src/trajectory_parker.cc:212-221)
+   R dtp = R(0.5) * sp.dmax / norm(slope);
+   dtp = m_min(dtp, R(0.5) * (sp.dmax * sp.dmax) / m_max(K.perp, K.para));
+   dtp = m_min(dtp, R(0.5) * R(3) * R(0.01) / m_abs(divU));
+   L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bs, P.nbt, fwd);
+   // EulerDiffSlopes (src/trajectory_parker.cc:159-180)
+   V3<R> fa[3];
+   fa[2] = sp.bhat;
+   fa[0] = second_unit(sp.bhat);
+   fa[1] = cross(fa[2], fa[0]);
+   R n[4];
+   normals4<R>(rng_block(P.seed, L.steps, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
+   R sdt = m_sqrt(L.dt);
+   R dWx = sdt * n[0], dWy = sdt * n[1], dWz = sdt * n[2];
+   R sperp = m_sqrt(R(2) * K.perp), spara = m_sqrt(R(2) * K.para);
+   V3<R> dr = from_basis(mk(sperp * dWx, sperp * dWy, spara * dWz), fa);
+   // RKStep with the Euler table, then the stochastic displacement
+   R dts = L.dt * R(1);
+   if (fwd) {
+      acc_add(L.t, L.dt);
+      if constexpr (kFP64) {
+         acc_add(L.pos.x, dts * slope.x); acc_add(L.pos.y, dts * slope.y); acc_add(L.pos.z, dts * slope.z);
+         acc_add(L.mom.x, dts * slope_p);
+         acc_add(L.pos.x, dr.x); acc_add(L.pos.y, dr.y); acc_add(L.pos.z, dr.z);
+      }
+      else {
+         add3(L.pos, dts * slope + dr);
+         acc_add(L.mom.x, dts * slope_p);
+      }
+   }
+   else {
+      acc_add(L.t, -L.dt);
+      if constexpr (kFP64) {
+         acc_add(L.pos.x, -(dts * slope.x)); acc_add(L.pos.y, -(dts * slope.y)); acc_add(L.pos.z, -(dts * slope.z));
+         acc_add(L.mom.x, -(dts * slope_p));
+         acc_add(L.pos.x, dr.x); acc_add(L.pos.y, dr.y); acc_add(L.pos.z, dr.z);
+      }
+      else {
+         add3(L.pos, dr - dts * slope);
+         acc_add(L.mom.x, -(dts * slope_p));
+      }
+   }
+   if (sa != R(0)) L.amp += dts * sa * m_exp(L.wgt);
+   handle_boundaries<kParker>(L, bs, sp, s0, P, Pd, S);
+   // the end point's dmax for the time-step check of Integrate
+   L.steps++;
+   if (!(L.status & TRAJ_FINISH)) {
+      R dmax_end = eval_dmax<BG>(P.bg, (R)acc_val(L.t), val3<R>(L.pos));
+      if (!(L.dt >= Lim<R>::tiny * dmax_end / c_code<R>())) L.status |= TRAJ_DISCARD;
+   }
+}
+
+// ---- Runge-Kutta advance for Lorentz and Focused (src/trajectory_base.cc:315-406, 545-579) ----
+template <class R> __device__ __forceinline__ R rk_a(int s) { return s == 0 ? R(0) : (s == 3 ? R(1) : R(0.5)); }
+template <class R> __device__ __forceinline__ R rk_b(int s, int l)
+{
+   return (s == 1 && l == 0) ? R(0.5) : ((s == 2 && l == 1) ? R(0.5) : ((s == 3 && l == 2) ? R(1) : R(0)));
+}
+template <class R> __device__ __forceinline__ R rk_v(int l) { return (l == 0 || l == 3) ? R(1.0 / 6.0) : R(1.0 / 3.0); }
+
+template <int TT, class R>
+__device__ __forceinline__ V3<R> vel_load(V3<R> mom)
+{
+   if (TT == kFocused) { R v = vel_of(mom.x); return (v / mom.x) * mom; }  // Vel<SphericalRMP>
+   return vel_cart(mom);
+}
+
+// TrajectoryFocused::DriftCoeff (src/trajectory_focused.cc:62-80)
+template <class R>
+__device__ __forceinline__ V3<R> focused_drift(const SD<R>& s, V3<R> mom, V3<R> vel)
+{
+   R ct2 = mom.y * mom.y, st2 = R(1) - ct2;
+   V3<R> dv = (R(0.5) * st2) * (cross(s.bhat, s.gradBmag) / s.Bmag);
+   V3<R> cur = (R(0.5) * st2 * dot(s.B, sd_curlB(s))) * s.bhat + ct2 * cross(s.bhat, vm(s.B, s.gradB));
+   dv = dv + cur / (s.Bmag * s.Bmag);
+   dv = (larmor(mom.x, s.Bmag) * vel.x) * dv;
+   return dv + (s.U + (vel.x * mom.y) * s.bhat);
+}
+
+template <int TT, class R>
+__device__ __forceinline__ void rk_slopes(const SD<R>& s, V3<R> mom, V3<R> vel, V3<R>& sp, V3<R>& sm, V3<R>& drift)
+{
+   if (TT == kLorentz) {  // src/trajectory_lorentz.cc:67-71
+      sp = vel;
+      sm = s.E + cross(vel, s.B) / c_code<R>();
+   }
+   else {  // src/trajectory_focused.cc:100-128
+      drift = focused_drift(s, mom, vel);
+      sp = drift;
+      R st2 = R(1) - mom.y * mom.y, bbgu = R(0);
+#pragma unroll
+      for (int i = 0; i < 3; i++)
+#pragma unroll
+         for (int j = 0; j < 3; j++) bbgu += s.bhat[i] * s.bhat[j] * s.gradU.m[i][j];
+      V3<R> cd = s.dUdt + vm(s.U, s.gradU);
+      R bcd = R(2) * dot(s.bhat, cd) / vel.x;
+      R divU = sd_divU(s);
+      sm.x = R(0.5) * mom.x * ((R(3) * st2 - R(2)) * bbgu - st2 * divU - mom.y * bcd);
+      sm.y = R(0.5) * st2 * (vel.x * sd_divbhat(s) - bcd + mom.y * (divU - R(3) * bbgu));
+      sm.z = R(0);
+   }
+}
+
+template <class A, class R>
+__device__ __forceinline__ void clamp_mu(AV3<A>& mom)
+{
+   // TrajectoryFocused::MomentumCorrection (src/trajectory_focused.cc:146-156)
+   R mu = (R)acc_val(mom.y);
+   if (mu > R(1)) acc_setf(mom.y, R(1));
+   else if (mu < R(-1)) acc_setf(mom.y, R(-1));
+}
+
+template <int TT, int BG, class R, class A, int STAGES>
+__device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndState<R>* bs, const Start& s0, const ProblemDescT<R>& P,
+                                           const ProblemDesc& Pd, const RunConfig& cfg, const Sinks& S)
+{
+   constexpr bool kFP64 = sizeof(R) == sizeof(double);
+   const bool fwd = cfg.time_flow == 0;
+   const int deriv_mode = kFP64 ? cfg.deriv_mode : 1;
+   const bool scatt = (TT == kFocused) && cfg.pa_scattering;
+   SD<R> sp;
+   V3<R> mom = lane_mom(L);
+   if (!get_fields<BG>(P.bg, deriv_mode, (R)acc_val(L.t), val3<R>(L.pos), field_p<TT>(mom), traj_mask<TT>(), sp)) {
+      L.status |= TRAJ_DISCARD;
+      return;
+   }
+   V3<R> vel = vel_load<TT>(mom);
+   V3<R> drift = mk(R(0), R(0), R(0));
+   if (scatt) {
+      // Euler pitch-angle scattering, composed after TrajectoryGuidingScatt::Advance
+      // (src/trajectory_guiding_scatt.cc:61-110, 255-300): coefficients, the mu-CFL, then the step
+      R vmag = vel_of(mom.x);
+      R Omega = cyclotron(vmag, sp.Bmag);
+      R Dmumu = kappa_mumu(P.df, vmag, Omega, mom.y);
+      R Vmu = kappa_mumu_dmu(P.df, vmag, Omega, mom.y, Dmumu);
+      drift = focused_drift(sp, mom, vel);
+      R dtp = R(0.5) * sp.dmax / (norm(drift) + R(0.5) * vel.x);
+      const R dth = R(2.0 * 3.141592653589793238462643383279502884 / 180.0);
+      R amu = m_abs(mom.y);
+      R dmumax = m_sqrt(R(1) - amu) * dth + R(0.5) * amu * (dth * dth);
+      dtp = m_min(dtp, R(0.5) * (dmumax * dmumax) / Dmumu);
+      dtp = m_min(dtp, R(0.5) * dmumax / m_abs(Vmu));
+      L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bs, P.nbt, fwd);
+      R n[4];
+      normals4<R>(rng_block(P.seed, L.steps, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
+      R sq = m_sqrt(R(2) * Dmumu * L.dt);
+      R mu_new = mom.y + Vmu * L.dt + sq * n[0];
+      int k = 1, blk = 0;
+      while (m_abs(mu_new) > R(1) && blk < 64) {
+         if (k == 4) {
+            normals4<R>(rng_block(P.seed, L.steps * 64u + (uint32_t)blk, L.traj_id, P.problem_id, kRngExtra, L.attempt), n);
+            blk++;
+            k = 0;
+         }
+         mu_new = mom.y + Vmu * L.dt + sq * n[k++];
+      }
+      if (m_abs(mu_new) > R(1)) mu_new = mu_new > R(0) ? R(1) : R(-1);
+      acc_setf(L.mom.y, mu_new);
+      mom = lane_mom(L);
+      vel = vel_load<TT>(mom);
+   }
+   const A t_loc = L.t;
+   const AV3<A> pos_loc = L.pos, mom_loc = L.mom;
+   V3<R> slp[STAGES], slm[STAGES];
+   rk_slopes<TT>(sp, mom, vel, slp[0], slm[0], drift);
+   if (!scatt) {
+      R dtp;
+      if (TT == kLorentz) {  // src/trajectory_lorentz.cc:51-59
+         R vn = norm(vel);
+         R Om = m_max(cyclotron(vn, sp.Bmag), Lim<R>::tiny);
+         R spo = kFP64 ? (R)cfg.steps_per_orbit : (R)cfg.steps_per_orbit_f;
+         dtp = R(6.283185307179586476925286766559005768) / Om / spo;
+         dtp = m_min(dtp, R(0.1) * sp.dmax / vn);
+      }
+      else {  // src/trajectory_focused.cc:87-91
+         dtp = R(0.5) * sp.dmax / (norm(drift) + R(0.5) * vel.x);
+      }
+      L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bs, P.nbt, fwd);
+   }
+   // RKSlopes
+#pragma unroll
+   for (int is = 1; is < STAGES; is++) {
+#pragma unroll
+      for (int il = 0; il < is; il++) {
+         R ds = L.dt * rk_b<R>(is, il);
+         R dta = rk_a<R>(is) * L.dt;
+         if (fwd) { acc_add(L.t, dta); add3(L.pos, ds * slp[il]); add3(L.mom, ds * slm[il]); }
+         else { acc_add(L.t, -dta); add3(L.pos, R(-1) * (ds * slp[il])); add3(L.mom, R(-1) * (ds * slm[il])); }
+      }
+      if (space_terminate<TT>(L, bs, sp, s0, P, Pd, S)) return;
+      V3<R> ms = lane_mom(L);
+      if (!get_fields<BG>(P.bg, deriv_mode, (R)acc_val(L.t), val3<R>(L.pos), field_p<TT>(ms), traj_mask<TT>(), sp)) {
+         L.status |= TRAJ_DISCARD;
+         return;
+      }
+      if (TT == kFocused) { clamp_mu<A, R>(L.mom); ms = lane_mom(L); }
+      V3<R> vs = vel_cart(ms);  // src/trajectory_base.cc:344 uses the Cartesian velocity for every type
+      V3<R> dummy;
+      rk_slopes<TT>(sp, ms, vs, slp[is], slm[is], dummy);
+      L.t = t_loc;
+      L.pos = pos_loc;
+      L.mom = mom_loc;
+   }
+   // RKStep
+   if (fwd) acc_add(L.t, L.dt); else acc_add(L.t, -L.dt);
+   if constexpr (kFP64) {
+#pragma unroll
+      for (int il = 0; il < STAGES; il++) {
+         R w = L.dt * (STAGES == 1 ? R(1) : rk_v<R>(il));
+         if (fwd) { add3(L.pos, w * slp[il]); add3(L.mom, w * slm[il]); }
+         else { add3(L.pos, R(-1) * (w * slp[il])); add3(L.mom, R(-1) * (w * slm[il])); }
+      }
+   }
+   else {
+      V3<R> dp = mk(R(0), R(0), R(0)), dm = mk(R(0), R(0), R(0));
+#pragma unroll
+      for (int il = 0; il < STAGES; il++) {
+         R w = STAGES == 1 ? R(1) : rk_v<R>(il);
+         dp = dp + w * slp[il];
+         dm = dm + w * slm[il];
+      }
+      R sdt = fwd ? L.dt : -L.dt;
+      add3(L.pos, sdt * dp);
+      add3(L.mom, sdt * dm);
+   }
+   handle_boundaries<TT>(L, bs, sp, s0, P, Pd, S);
+   if (!(L.status & TRAJ_FINISH) && TT == kFocused) clamp_mu<A, R>(L.mom);
+   L.steps++;
+   if (!(L.status & TRAJ_FINISH)) {
+      R dmax_end = eval_dmax<BG>(P.bg, (R)acc_val(L.t), val3<R>(L.pos));
+      if (!(L.dt >= Lim<R>::tiny * dmax_end / c_code<R>())) L.status |= TRAJ_DISCARD;
+   }
+}
+
+// ---- SetStart (src/trajectory_base.cc:867-939 and overrides) -------------------------------
+template <int TT, int BG, class R, class A>
+__device__ __noinline__ void set_start(Lane<R, A>& L, BndState<R>* bs, Start& s0, const ProblemDescT<R>& P,
+                                       const ProblemDesc& Pd, const RunConfig& cfg, int64_t local)
+{
+   constexpr bool kFP64 = sizeof(R) == sizeof(double);
+   const int deriv_mode = kFP64 ? cfg.deriv_mode : 1;
+   L.status = 0;
+   L.steps = 0;
+   L.amp = R(0);
+   L.wgt = R(0);
+   L.dt = R(0);
+   InitRng rng{Pd.seed, L.traj_id, Pd.problem_id, L.attempt, 0u, 0u};
+   double t = sample_time(rng, Pd, local);
+   V3<double> pos = sample_pos(rng, Pd, local);
+   V3<double> mom = sample_mom(rng, Pd, TT, mk(1.0, 1.0, 1.0));
+   acc_set(L.t, t);
+   acc_set(L.pos.x, pos.x); acc_set(L.pos.y, pos.y); acc_set(L.pos.z, pos.z);
+   SD<R> sp;
+   V3<R> pr = val3<R>(L.pos);
+   R pm = TT == kLorentz ? (R)norm(mom) : (R)mom.x;
+   if (!get_fields<BG>(P.bg, deriv_mode, (R)t, pr, pm, traj_mask<TT>(), sp)) { L.status |= TRAJ_DISCARD; return; }
+   V3<double> bh = mk((double)sp.bhat.x, (double)sp.bhat.y, (double)sp.bhat.z);
+   mom = sample_mom(rng, Pd, TT, bh);
+   acc_set(L.mom.x, mom.x); acc_set(L.mom.y, mom.y); acc_set(L.mom.z, mom.z);
+   s0.t0 = t;
+   s0.pos0 = pos;
+   s0.mom0 = mom;
+   s0.bhat0 = bh;
+   R c = c_code<R>();
+   L.dt_adapt = Lim<R>::large * sp.dmax / c;
+   V3<R> mr = lane_mom(L);
+   for (int k = 0; k < kMaxBndTotal; k++) {
+      if (!bnd_used(P, k)) continue;
+      R scale = k < kMaxBnd ? sp.dmax / c : (k < 2 * kMaxBnd ? sp.dmax : norm(mr));
+      reset_bnd(bnd_param(P, k), bs[k], scale, L.t, pr, mr, sp.bhat, sp.region, TT);
+   }
+   // TrajectoryParkerSource::SetStart (src/trajectory_parker_source.cc:43-50)
+   if (P.src.kind == 2) L.src_del_old = mr.x - P.src.p_inj;
+}
+
+// ---- the kernel --------------------------------------------------------------------------------
+template <class R>
+__device__ __forceinline__ int find_problem(const ProblemDescT<R>* P, int n, int64_t g)
+{
+   int lo = 0, hi = n - 1;
+   while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (P[mid].first <= g) lo = mid;
+      else hi = mid - 1;
+   }
+   return lo;
+}
+
+template <class R, class A>
+__device__ __noinline__ void write_record(const Lane<R, A>& L, const Start& s0, TrajRecord* rec, int64_t g)
+{
+   TrajRecord r;
+   r.attempts = L.attempt + 1;
+   r.status = L.status;
+   r.steps = L.steps;
+   r.t = acc_dbl(L.t);
+   r.pos[0] = acc_dbl(L.pos.x); r.pos[1] = acc_dbl(L.pos.y); r.pos[2] = acc_dbl(L.pos.z);
+   r.mom[0] = acc_dbl(L.mom.x); r.mom[1] = acc_dbl(L.mom.y); r.mom[2] = acc_dbl(L.mom.z);
+   r.t0 = s0.t0;
+   r.pos0[0] = s0.pos0.x; r.pos0[1] = s0.pos0.y; r.pos0[2] = s0.pos0.z;
+   r.mom0[0] = s0.mom0.x; r.mom0[1] = s0.mom0.y; r.mom0[2] = s0.mom0.z;
+   r.amp = (double)L.amp;
+   r.logwgt = (double)L.wgt;
+   rec[g] = r;
+}
+
+// Start trajectory g on the lane.
+template <int TT, int BG, class R, class A>
+__device__ __forceinline__ void start_lane(Lane<R, A>& L, BndState<R>* bs, Start& s0, const ProblemDescT<R>* P,
+                                           const ProblemDesc* Pd, const RunConfig& cfg, int64_t g, uint32_t attempt)
+{
+   L.prob = find_problem(P, cfg.n_problems, g);
+   int64_t local = g - P[L.prob].first;
+   L.traj_id = (uint32_t)(cfg.run_index * P[L.prob].n_traj + local);
+   L.attempt = attempt;
+   set_start<TT, BG>(L, bs, s0, P[L.prob], Pd[L.prob], cfg, local);
+}
+
+template <int TT, int BG, class R>
+__global__ void __launch_bounds__(128) step_kernel(const ProblemDescT<R>* __restrict__ P, const ProblemDesc* __restrict__ Pd,
+                                                   RunConfig cfg, RunCounters* ctr, int32_t* counts, double* sums,
+                                                   unsigned long long* n_events, TrajRecord* rec, int queue)
+{
+   using A = typename AccOf<R>::type;
+   Sinks S{counts, sums, n_events, ctr};
+   Lane<R, A> L;
+   BndState<R> bs[kMaxBndTotal];
+   Start s0;
+   int64_t g = -1;
+   bool active = false;
+   unsigned long long my_steps = 0, my_retries = 0, my_given_up = 0, my_done = 0;
+   const int64_t total = cfg.total_traj;
+   const int64_t stride = (int64_t)gridDim.x * blockDim.x;
+   if (!queue) {
+      g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+      if (g < total) { start_lane<TT, BG>(L, bs, s0, P, Pd, cfg, g, 0u); active = true; }
+   }
+   const int K = cfg.steps_per_sync > 0 ? cfg.steps_per_sync : 1;
+   while (true) {
+      if (queue) {
+         // refill idle lanes from the work queue: one atomic per warp
+         unsigned idle = __ballot_sync(0xffffffffu, !active);
+         if (idle) {
+            int lane = threadIdx.x & 31;
+            int leader = __ffs(idle) - 1;
+            unsigned long long base = 0;
+            if (lane == leader) base = atomicAdd(&ctr->next_traj, (unsigned long long)__popc(idle));
+            base = __shfl_sync(0xffffffffu, base, leader);
+            if (!active) {
+               int64_t mine = (int64_t)base + __popc(idle & ((1u << lane) - 1u));
+               if (mine < total) { g = mine; start_lane<TT, BG>(L, bs, s0, P, Pd, cfg, g, 0u); active = true; }
+            }
+         }
+         if (!__any_sync(0xffffffffu, active)) break;
+      }
+      else if (!active) break;
+      for (int k = 0; k < K && active; k++) {
+         bool done = false;
+         if (L.status & TRAJ_DISCARD) {
+            // discarded attempt: redo the trajectory with a fresh random stream (src/simulation.cc:262-288)
+            if (L.attempt + 1 >= (uint32_t)cfg.max_attempts) {
+               L.status |= TRAJ_GAVE_UP;
+               my_given_up++;
+               done = true;
+            }
+            else {
+               my_retries++;
+               start_lane<TT, BG>(L, bs, s0, P, Pd, cfg, g, L.attempt + 1);
+               continue;
+            }
+         }
+         else {
+            const ProblemDescT<R>& Pp = P[L.prob];
+            if (TT == kParker) parker_advance<BG>(L, bs, s0, Pp, Pd[L.prob], cfg, S);
+            else if (cfg.rk == 25) rk_advance<TT, BG, R, A, 4>(L, bs, s0, Pp, Pd[L.prob], cfg, S);
+            else rk_advance<TT, BG, R, A, 1>(L, bs, s0, Pp, Pd[L.prob], cfg, S);
+            // Integrate's safety limits (src/trajectory_base.cc:964-992)
+            if (L.steps > kMaxTrajSteps || !isfinite(L.dt) || L.dt == R(0)) L.status |= TRAJ_DISCARD;
+            done = (L.status & TRAJ_FINISH) && !(L.status & TRAJ_DISCARD);
+         }
+         if (done) {
+            my_steps += L.steps;
+            my_done++;
+            if (cfg.record_final) write_record(L, s0, rec, g);
+            active = false;
+            if (!queue) {
+               g += stride;
+               if (g < total) { start_lane<TT, BG>(L, bs, s0, P, Pd, cfg, g, 0u); active = true; }
+            }
+         }
+      }
+   }
+   // warp-aggregated counters
+   for (int o = 16; o > 0; o >>= 1) {
+      my_steps += __shfl_down_sync(0xffffffffu, my_steps, o);
+      my_retries += __shfl_down_sync(0xffffffffu, my_retries, o);
+      my_given_up += __shfl_down_sync(0xffffffffu, my_given_up, o);
+      my_done += __shfl_down_sync(0xffffffffu, my_done, o);
+   }
+   if ((threadIdx.x & 31) == 0) {
+      atomicAdd(&ctr->steps, my_steps);
+      if (my_retries) atomicAdd(&ctr->retries, my_retries);
+      if (my_given_up) atomicAdd(&ctr->given_up, my_given_up);
+      atomicAdd(&ctr->finished, my_done);
+   }
+}
+
+}  // namespace spx

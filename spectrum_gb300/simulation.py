@@ -1,0 +1,164 @@
+"""SimulationGPU: the reference's simulation interface on top of the C ABI.
+
+The method names and argument meanings are those of SimulationWorker (src/simulation.hh:93-138):
+Add{Background,Diffusion,Source,Boundary,Initial,Distribution}(prototype, container), SetTasks,
+MainLoop, PrintDistro1D, RestoreDistro, DistroFileName, GetTrajectoryName. Instead of an MPI farm
+the trajectories run in one device launch; SetTasks may be called several times to batch many
+problems, each optionally replacing plugins of the base set (``AddProblem``).
+
+``run_problems`` runs a list of ``Problem`` objects (spectrum_gb300.problem) that share their
+plugin structure as one batched launch.
+"""
+from __future__ import annotations
+
+import struct
+
+import numpy as np
+
+from . import capi
+from . import plugins as P
+from .datacontainer import DataContainer
+from .problem import TRAJ_NAMES, Problem
+from .workloads import SPX_OPT_DERIV_MODE, SPX_OPT_PA_SCATTERING, SPX_OPT_RECORD_FINAL, SPX_OPT_STEPS_PER_ORBIT
+
+
+class SimulationGPU:
+    def __init__(self, traj: int, time_flow: int = 0, rk: int = 0, precision: int = capi.SPX_FP64,
+                 options: dict[int, float] | None = None):
+        self.traj = traj
+        self.ctx = capi.Context(traj, time_flow, rk, precision)
+        self.precision = precision
+        for k, v in (options or {}).items():
+            self.ctx.set_option(k, v)
+        self._distro_names: list[str] = []
+        self._file_prefix = ""
+        self.stats: capi.Stats | None = None
+
+    # -- plugin set-up (src/simulation.hh:105-123) ----------------------------------------------
+    def _add(self, role: int, proto: P.Plugin, container: DataContainer) -> None:
+        if proto.role != role:
+            raise TypeError(f"{proto.name} is not a {P.ROLE_NAMES[role]} plugin")
+        self.ctx.add_plugin(role, proto.kind, container.data(), container.size())
+        if role == P.ROLE_DISTRIBUTION:
+            self._distro_names.append(proto.name)
+
+    def AddBackground(self, proto, container, fname_pattern_in: str = ""):  # noqa: N802
+        self._add(P.ROLE_BACKGROUND, proto, container)
+
+    def AddDiffusion(self, proto, container):  # noqa: N802
+        self._add(P.ROLE_DIFFUSION, proto, container)
+
+    def AddSource(self, proto, container):  # noqa: N802
+        self._add(P.ROLE_SOURCE, proto, container)
+
+    def AddBoundary(self, proto, container):  # noqa: N802
+        self._add(P.ROLE_BOUNDARY, proto, container)
+
+    def AddInitial(self, proto, container):  # noqa: N802
+        self._add(P.ROLE_INITIAL, proto, container)
+
+    def AddDistribution(self, proto, container):  # noqa: N802
+        self._add(P.ROLE_DISTRIBUTION, proto, container)
+
+    # -- tasks and the main loop -----------------------------------------------------------------
+    def SetTasks(self, n_traj: int, batch_size: int = 0, max_traj_per_worker: int = 0, seed: int = 0x5EED0000):  # noqa: N802
+        """One problem of n_traj trajectories (batch sizes belong to the MPI farm and are ignored)."""
+        return self.ctx.add_problem(n_traj, seed)
+
+    def AddProblem(self, n_traj: int, seed: int, overrides=()):  # noqa: N802
+        """A further problem: ``overrides`` is a list of (role, slot, prototype, DataContainer)."""
+        blob = bytearray()
+        for role, slot, proto, c in overrides:
+            data = c.data()
+            blob += struct.pack("<5I", role, slot, proto.kind, c.size(), len(data)) + data
+        return self.ctx.add_problem(n_traj, seed, bytes(blob))
+
+    def MainLoop(self, tuning: capi.Tuning | None = None) -> capi.Stats:  # noqa: N802
+        self.ctx.run(tuning)
+        self.stats = self.ctx.sync()
+        return self.stats
+
+    def GetTrajectoryName(self) -> str:  # noqa: N802
+        return TRAJ_NAMES.get(self.traj, "Trajectory")
+
+    def DistroFileName(self, file_name: str) -> None:  # noqa: N802
+        self._file_prefix = file_name
+
+    def RestoreDistro(self, distro: int = 0) -> None:  # noqa: N802
+        self.ctx.restore(self._file_prefix + "distros.spx")
+
+    def DumpDistro(self) -> None:  # noqa: N802
+        self.ctx.dump(self._file_prefix + "distros.spx")
+
+    def distribution(self, distro: int, problem: int = 0):
+        return self.ctx.distribution(problem, distro)
+
+    def PrintDistro1D(self, distro: int, ijk: int, file_name: str, phys_units: bool = False, problem: int = 0) -> None:  # noqa: N802
+        """Write bin index, count and mean weight per bin along axis ``ijk`` (summed over the others),
+        the columns of DistributionTemplated::Print1D (src/distribution_templated.cc:546-590) in
+        code units."""
+        counts, sums, _ = self.distribution(distro, problem)
+        nb, _ = self.ctx.distribution_info(problem, distro)
+        with open(file_name, "w") as f:
+            for i, (c, s) in enumerate(zip(counts, sums[:, 0])):
+                f.write(f"{i:8d} {c:12d} {s / c if c else 0.0:20.12e}\n")
+
+    def close(self) -> None:
+        self.ctx.close()
+
+
+def _diff_overrides(base: Problem, other: Problem) -> bytes:
+    if [(e.plugin.role, e.plugin.kind) for e in base.plugins] != [(e.plugin.role, e.plugin.kind) for e in other.plugins]:
+        raise ValueError("batched problems must share their plugin structure")
+    out = bytearray()
+    slots: dict[int, int] = {}
+    for eb, eo in zip(base.plugins, other.plugins):
+        role = eb.plugin.role
+        slot = slots.get(role, 0)
+        slots[role] = slot + 1
+        if eb.blob != eo.blob:
+            if role == P.ROLE_BOUNDARY:
+                raise ValueError("boundaries of batched problems must agree (replace them by slot via AddProblem)")
+            out += struct.pack("<5I", role, slot, eo.plugin.kind, eo.n_records, len(eo.blob)) + eo.blob
+    return bytes(out)
+
+
+def open_problems(problems: list[Problem] | Problem, precision: int = capi.SPX_FP64, record: bool = False,
+                  deriv_mode: int | None = None) -> SimulationGPU:
+    """Set up one context for ``problems`` (one problem or a batch with a shared structure)."""
+    if isinstance(problems, Problem):
+        problems = [problems]
+    base = problems[0]
+    opts = dict(base.options)
+    if deriv_mode is not None:
+        opts[SPX_OPT_DERIV_MODE] = deriv_mode
+    elif precision == capi.SPX_MIXED:
+        opts[SPX_OPT_DERIV_MODE] = 1
+    if record:
+        opts[SPX_OPT_RECORD_FINAL] = 1
+    sim = SimulationGPU(base.traj, base.time_flow, base.rk, precision, opts)
+    for e in base.plugins:
+        sim.ctx.add_plugin(e.plugin.role, e.plugin.kind, e.blob, e.n_records)
+    for p in problems:
+        sim.ctx.add_problem(p.n_traj, p.seed, _diff_overrides(base, p))
+    return sim
+
+
+class RunResult:
+    def __init__(self, sim: SimulationGPU, stats: capi.Stats, n_problems: int, n_distros: int, records=None):
+        self.stats = stats
+        self.distros = [[sim.ctx.distribution(k, d) for d in range(n_distros)] for k in range(n_problems)]
+        self.records = records
+
+
+def run_problems(problems: list[Problem] | Problem, precision: int = capi.SPX_FP64, record: bool = False,
+                 deriv_mode: int | None = None, tuning: capi.Tuning | None = None) -> RunResult:
+    if isinstance(problems, Problem):
+        problems = [problems]
+    sim = open_problems(problems, precision, record, deriv_mode)
+    try:
+        stats = sim.MainLoop(tuning)
+        recs = [sim.ctx.records(k, p.n_traj) for k, p in enumerate(problems)] if record else None
+        return RunResult(sim, stats, len(problems), len(problems[0].distributions()), recs)
+    finally:
+        sim.close()
