@@ -1,0 +1,348 @@
+"""Benchmark of the test-particle stepping path on one GB300 (or N GPUs as independent shards).
+
+Workload (one step = one launch over the whole batch): backward-time GCR modulation in the
+Parker-spiral solar wind, 32 log-spaced energies 10 MeV - 10 GeV, ``--per-energy`` trajectories
+each, LIS-weighted spectrum at the 100 AU boundary (spectrum_gb300.workloads.gcr_modulation).
+
+Reported (one JSON line on rank 0):
+  value       trajectories/s of the batched FP32 stepper (persistent work queue, float-float
+              accumulation), device time of the K timed launches, descriptors already on the GPU
+  fp64        the plain FP64 drop-in (one thread per trajectory) on step 0's identical Philox keys,
+              its trajectories/s, and the per-bin error of the FP32 spectrum against it
+  e2e         the same metric through the C ABI from host blobs to host histograms per step
+  roofline    FP32 work of the dominant kernel per launch over its event-timed duration
+  cpu_baseline the CPU restatement of the reference algorithm on this host's cores
+
+``--impl reference`` times the reference algorithm on the host cores instead (the CPU
+restatement in oracle/; the reference's own sources cannot be built where they are absent).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import multiprocessing as mp
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "SDE trajectories/s at <=1% bin error: batched FP32 vs plain FP64 GPU, 1 GB300"
+UNIT = "trajectories/s"
+WORKLOAD = "gcr_modulation_parker_spiral_32E"
+# FP32 operations per accepted step of the FP32 Parker solar-wind kernel (executed
+# FP32 instructions from ncu per launch divided by the launch's steps, FMA counted as 2)
+FP32_FLOP_PER_STEP = float(os.environ.get("SPX_FP32_FLOP_PER_STEP", "0")) or None
+
+
+def rank_info():
+    r = int(os.environ.get("RANK", "0"))
+    w = int(os.environ.get("WORLD_SIZE", "1"))
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    return r, w, lr
+
+
+def problems(per_energy: int, seed_offset: int = 0):
+    from spectrum_gb300 import workloads
+    pbs = workloads.gcr_modulation(n_traj=per_energy)
+    for p in pbs:
+        p.seed += seed_offset
+    return pbs
+
+
+# ---------------------------------------------------------------------------------------------
+# CPU leg (the oracle restatement of the reference algorithm) -- test infrastructure
+# ---------------------------------------------------------------------------------------------
+def _cpu_worker(args):
+    spec_idx, first, n, per_energy = args
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_tools
+    pbs = problems(per_energy)
+    t0 = time.perf_counter()
+    res = oracle_tools.run_oracle(pbs[spec_idx], first=first, n=n, deriv_mode=0, record=True)
+    dt = time.perf_counter() - t0
+    return int(len(res.traj)), int(res.traj["steps"].sum()), dt
+
+
+def cpu_sample(seconds: float = 20.0, per_energy: int = 1000):
+    """Time the reference algorithm (C restatement, the reference's own derivative methods) on all
+    host cores, one process per core, on a bounded sample of the same workload: the energies in
+    turn, trajectories 0.. of each, until about ``seconds`` of wall time is spent."""
+    cores = os.cpu_count() or 1
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import oracle_tools
+    oracle_tools.lib()  # build/load before forking workers
+    ctx = mp.get_context("spawn")
+    tasks = []
+    n_per_task = 2
+    k = 0
+    for rnd in range(100000):
+        for e in range(32):
+            tasks.append((e, rnd * n_per_task, n_per_task, per_energy))
+            k += 1
+    done_traj = done_steps = 0
+    t0 = time.perf_counter()
+    with ctx.Pool(cores) as pool:
+        it = pool.imap_unordered(_cpu_worker, tasks, chunksize=1)
+        for ntraj, nsteps, _ in it:
+            done_traj += ntraj
+            done_steps += nsteps
+            if time.perf_counter() - t0 > seconds:
+                pool.terminate()
+                break
+    wall = time.perf_counter() - t0
+    return {"value": done_traj / wall, "unit": UNIT, "cores": cores, "kind": "port",
+            "sample": f"{done_traj} trajectories ({done_steps} steps) of the 32-energy batch, round-robin over "
+                      f"energies, {wall:.1f} s wall on {cores} processes",
+            "steps_per_s": done_steps / wall}
+
+
+# ---------------------------------------------------------------------------------------------
+# GPU helpers
+# ---------------------------------------------------------------------------------------------
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, gpu_index: int, path: str):
+        self.path = path
+        self.proc = None
+        self.gpu = gpu_index
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.f = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                          "-lms", "200"], stdout=self.f, stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            self.proc.wait()
+            self.f.close()
+
+    def summary(self):
+        try:
+            rows = [l.split(",") for l in open(self.path) if l.strip()]
+        except Exception:
+            return None
+        if not rows:
+            return None
+        sm = [float(r[1]) for r in rows if r[1].strip().replace(".", "").isdigit()]
+        mx = max(float(r[2]) for r in rows)
+        reasons = set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            for i, n in enumerate(names):
+                if r[5 + i].strip().lower() == "active":
+                    reasons.add(n)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(rows)}
+
+
+def flush_l2(torch, dev):
+    # 256 MiB > the 129 MB L2
+    buf = flush_l2.buf if hasattr(flush_l2, "buf") else None
+    if buf is None:
+        buf = flush_l2.buf = torch.empty(64 * 1024 * 1024, dtype=torch.float32, device=dev)
+    buf.zero_()
+    torch.cuda.synchronize(dev)
+
+
+def per_bin_error(a, b, min_count):
+    """Relative per-bin differences of counts and weighted sums of two runs (a against b)."""
+    worst_c = worst_s = 0.0
+    nb = 0
+    for (ca, sa, _), (cb, sb, _) in zip(a, b):
+        m = cb >= min_count
+        if not m.any():
+            continue
+        nb += int(m.sum())
+        worst_c = max(worst_c, float((abs(ca[m].astype(float) - cb[m]) / cb[m]).max()))
+        ref = sb[m, 0]
+        ok = ref != 0
+        if ok.any():
+            worst_s = max(worst_s, float((abs(sa[m, 0][ok] - ref[ok]) / abs(ref[ok])).max()))
+    return worst_c, worst_s, nb
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="spectrum_gb300", choices=["spectrum_gb300", "reference"])
+    ap.add_argument("--per-energy", type=int, default=int(os.environ.get("SPX_BENCH_PER_ENERGY", "16000")))
+    ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--no-fp64", action="store_true")
+    args = ap.parse_args()
+    rank, world, local = rank_info()
+    cfg = {"workload": WORKLOAD, "energies": 32, "per_energy": args.per_energy,
+           "trajectories_per_step": 32 * args.per_energy * world, "time_flow": "backward", "background": "solar wind",
+           "diffusion": "kappa_par = lam v/3 (R/1GV)^0.5 (B/5nT)^-1, kappa_perp = 0.02 kappa_par",
+           "boundaries": "0.05 AU absorb (cold), 100 AU absorb (LIS-weighted), 1 yr", "l2": "flushed between steps"}
+
+    if args.impl == "reference":
+        if rank != 0:
+            return
+        # warm-up: the oracle library build and a short run
+        cpu_sample(1.0, args.per_energy)
+        vals = []
+        for _ in range(args.steps):
+            vals.append(cpu_sample(max(5.0, args.cpu_seconds / max(args.steps, 1)), args.per_energy))
+        v = sum(x["value"] for x in vals) / len(vals)
+        line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
+                "steps": args.steps, "warmup": 1, "ms_per_step": 1e3 / v * cfg["trajectories_per_step"],
+                "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+                "data": "synthetic (seeded Philox streams)", "config": cfg,
+                "cpu_baseline": {"value": v, "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
+                                 "sample": vals[0]["sample"]},
+                "e2e": {"value": v, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+        print(json.dumps(line), flush=True)
+        return
+
+    import numpy as np
+    import torch
+    from spectrum_gb300 import capi
+    from spectrum_gb300.simulation import open_problems
+
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    seed_offset = 7919 * rank
+    pbs = problems(args.per_energy, seed_offset)
+    n_step = 32 * args.per_energy
+
+    # ---- batched FP32 stepper: value ---------------------------------------------------------
+    sim = open_problems(pbs, precision=capi.SPX_MIXED)
+    tun = capi.Tuning(0, 0, 0, 1)
+    for _ in range(args.warmup):
+        sim.MainLoop(tun)
+    sim.ctx.reset_distributions()
+    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
+    clocks = Clocks(local, os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv"))
+    kms = []
+    steps_done = 0
+    traj_done = 0
+    # the timed region: K launches, each preceded by an L2 flush, device time from CUDA events
+    if world > 1:
+        torch.distributed.barrier()
+    torch.cuda.synchronize(dev)
+    t_wall0 = time.perf_counter()
+    with clocks:
+        first_distros = None
+        for k in range(args.steps):
+            flush_l2(torch, dev)
+            st = sim.MainLoop(tun)
+            kms.append(st.kernel_ms)
+            steps_done += st.steps
+            traj_done += st.trajectories
+            if k == 0:
+                first_distros = [sim.ctx.distribution(p, 0) for p in range(len(pbs))]
+                sim.ctx.reset_distributions()
+    torch.cuda.synchronize(dev)
+    wall = time.perf_counter() - t_wall0
+    tuning = {"block_size": st.tuning.block_size, "blocks_per_sm": st.tuning.blocks_per_sm,
+              "steps_per_sync": st.tuning.steps_per_sync, "schedule": "persistent work queue"}
+    sim.close()
+    t_dev = sum(kms) / 1e3
+    t_max = t_dev
+    if world > 1:
+        tt = torch.tensor([t_dev], device=dev)
+        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
+        t_max = float(tt.item())
+    value = traj_done * world / t_max
+    steps_rate = steps_done * world / t_max
+
+    # ---- plain FP64 drop-in on step 0's keys: comparison and per-bin error -------------------
+    fp64 = None
+    if not args.no_fp64:
+        # Every fourth energy at the full per-energy count (so each spectrum bin holds >= 1e4 events);
+        # fresh contexts with the same problem list draw identical Philox streams.
+        sub = pbs[::4]
+        sim64 = open_problems(sub, precision=capi.SPX_FP64, deriv_mode=1)
+        flush_l2(torch, dev)
+        st64 = sim64.MainLoop(capi.Tuning(0, 0, 1, 0))
+        d64 = [[sim64.ctx.distribution(p, d) for d in range(2)] for p in range(len(sub))]
+        sim64.close()
+        sim32 = open_problems(sub, precision=capi.SPX_MIXED)
+        flush_l2(torch, dev)
+        st32 = sim32.MainLoop(tun)
+        d32 = [[sim32.ctx.distribution(p, d) for d in range(2)] for p in range(len(sub))]
+        sim32.close()
+        # counts of every histogram (the criterion: bins with an FP64 count >= 1e4)
+        ec, _, nbins = per_bin_error([x for r in d32 for x in r], [x for r in d64 for x in r], 10000)
+        # the LIS-weighted spectrum (one bin per energy)
+        _, es, nbs = per_bin_error([r[0] for r in d32], [r[0] for r in d64], 10000)
+        fp64 = {"value": st64.trajectories / (st64.kernel_ms / 1e3), "unit": UNIT, "kernel_ms": st64.kernel_ms,
+                "trajectories": st64.trajectories, "energies": "every 4th of the 32",
+                "steps_per_s": st64.steps / (st64.kernel_ms / 1e3), "schedule": "one thread per trajectory",
+                "derivatives": "analytic (the FP32 kernel's formulation)",
+                "bin_error": ec, "bins_compared": nbins, "bin_error_ok": bool(nbins > 0 and ec <= 0.01),
+                "weighted_spectrum_error": es, "weighted_bins_compared": nbs,
+                "ratio_fp32_batched_over_fp64_plain": (st32.trajectories / (st32.kernel_ms / 1e3)) /
+                                                      (st64.trajectories / (st64.kernel_ms / 1e3))}
+
+    # ---- end to end through the C ABI --------------------------------------------------------
+    e2e_times = []
+    h2d = d2h = 0
+    for k in range(max(1, min(args.steps, 2))):
+        flush_l2(torch, dev)
+        t0 = time.perf_counter()
+        s = open_problems(pbs, precision=capi.SPX_MIXED)
+        st_e = s.MainLoop(tun)
+        outs = [s.ctx.distribution(p, 0) for p in range(len(pbs))]
+        s.close()
+        e2e_times.append(time.perf_counter() - t0)
+        d2h = sum(c.nbytes + x.nbytes + 8 for c, x, _ in outs) + 64
+        h2d = len(pbs) * (6800 * 2)  # FP64 and FP32 descriptors per problem (sizeof ProblemDescT)
+    e2e_val = st_e.trajectories * world / statistics.mean(e2e_times)
+
+    # ---- roofline of the dominant kernel -------------------------------------------------------
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except Exception:
+        pass
+    sm_max = peaks.get("sm_max_mhz", 2070.0)
+    props = torch.cuda.get_device_properties(dev)
+    fp32_peak = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, FFMA pipe
+    roof = {"bound": "fp32", "unit": "TFLOP/s", "peak": fp32_peak,
+            "peak_source": "nominal FP32 FMA pipe: SMs x 128 lanes x 2 x sm_max_mhz of MEASURED_PEAKS.json "
+                           "(the file has no FP32 figure; HBM and tensor peaks do not bound this kernel)",
+            "traffic": None}
+    flop_step = FP32_FLOP_PER_STEP
+    if flop_step:
+        ach = steps_rate / world * flop_step / 1e12
+        roof.update({"achieved": ach, "frac": ach / fp32_peak, "flop_per_step": flop_step})
+    else:
+        roof.update({"achieved": None, "frac": None})
+
+    clk = clocks.summary()
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32 (float-float accumulation)",
+            "data": "synthetic (seeded Philox streams)", "config": cfg, "steps_per_s": steps_rate,
+            "wall_s": wall, "tuning": tuning, "gpu_launches": args.steps, "fp64_plain": fp64,
+            "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "roofline": roof, "clocks": clk}
+    if rank == 0:
+        line["cpu_baseline"] = cpu_sample(args.cpu_seconds, args.per_energy) if args.cpu_seconds > 0 else None
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -694,23 +694,6 @@ static double next_init_normal(trj_t* T)
    return n[k % 4];
 }
 
-static int nps_of(const trj_t* T)
-{
-   int tt = T->o->traj_type;
-   return (tt == 206 || tt == 207) ? 3 : 1;
-}
-
-static double next_normal(trj_t* T)
-{
-   uint64_t k = T->n_normal++;
-   uint32_t b[4];
-   double n[4];
-   int nps = nps_of(T);
-   spx_rng_block(T->pb->seed, (uint32_t)(k / nps), T->traj_id, T->pb->problem, SPX_RNG_STEP, T->attempt, b);
-   spx_normals4(b, n);
-   return n[k % nps];
-}
-
 /* ------------------------------------------------------------------------------------------ */
 /* backgrounds                                                                                */
 /* ------------------------------------------------------------------------------------------ */
@@ -1314,11 +1297,16 @@ static void process_trajectory(trj_t* T, int di, int action)
       double val;
       if (!(d->dims & (1 << ijk))) continue;
       val = (d->log_bins[ijk] ? log10(value.x[ijk]) : value.x[ijk]) - d->limits0[ijk];
-      if (val < 0.0) {
-         if (d->bin_outside[ijk]) { bin[ijk] = 0; continue; }  /* D2 */
-         return;
+      if (val != val) return;
+      /* a "left" outlier is dropped unless bin_outside; the bin is then still val / bin_size,
+       * which is how a negative bin width (max < min) bins correctly */
+      if (val < 0.0 && !d->bin_outside[ijk]) return;
+      {
+         double q = val / d->bin_size[ijk];
+         if (q >= (double)d->n_bins[ijk]) bin[ijk] = d->n_bins[ijk];
+         else if (q <= -1.0) bin[ijk] = 0; /* D2 */
+         else bin[ijk] = (int)q;
       }
-      bin[ijk] = (int)(val / d->bin_size[ijk]);
       if (bin[ijk] >= d->n_bins[ijk]) {
          if (d->bin_outside[ijk]) bin[ijk] = d->n_bins[ijk] - 1;
          else return;

@@ -14,7 +14,7 @@ import sys
 
 PKG = os.path.dirname(os.path.abspath(__file__))
 CSRC = os.path.join(PKG, "csrc")
-OUT = os.path.join(PKG, "_lib")
+OUT = os.path.join(PKG, os.environ.get("SPX_LIB_DIR", "_lib"))
 OBJ = os.path.join(OUT, "obj")
 LIB = os.path.join(OUT, "libspx.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
@@ -44,7 +44,10 @@ def _compile(src: str, nvcc: str, extra: list[str]) -> tuple[str, int, str]:
     if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(path), _newest_header()):
         return obj, 0, ""
     lang = ["-x", "cu"] if src.endswith(".cu") else ["-x", "c++"]
-    cmd = [nvcc, *lang, *ARCH, *CFLAGS, *extra, "-c", path, "-o", obj]
+    # The FP32 kernels use the hardware approximations of division, square root, log, exp, sin,
+    # cos and pow (relative errors of a few 1e-7); the FP64 kernels keep IEEE arithmetic.
+    fast = ["-use_fast_math"] if src.endswith("_f32.cu") else []
+    cmd = [nvcc, *lang, *ARCH, *CFLAGS, *fast, *extra, "-c", path, "-o", obj]
     r = subprocess.run(cmd, capture_output=True, text=True)
     return obj, r.returncode, r.stdout + r.stderr
 
@@ -52,7 +55,7 @@ def _compile(src: str, nvcc: str, extra: list[str]) -> tuple[str, int, str]:
 def build(verbose: bool = False, extra: list[str] | None = None, jobs: int | None = None) -> str:
     nvcc = _nvcc()
     os.makedirs(OBJ, exist_ok=True)
-    extra = extra or []
+    extra = (extra or []) + os.environ.get("SPX_NVCC_FLAGS", "").split()
     srcs = sources()
     jobs = jobs or min(len(srcs), max(1, os.cpu_count() or 1))
     with cf.ThreadPoolExecutor(max_workers=jobs) as ex:

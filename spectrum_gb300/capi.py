@@ -10,7 +10,7 @@ import os
 import numpy as np
 
 _HERE = os.path.dirname(os.path.abspath(__file__))
-LIB_PATH = os.path.join(_HERE, "_lib", "libspx.so")
+LIB_PATH = os.environ.get("SPX_LIB", os.path.join(_HERE, "_lib", "libspx.so"))
 
 SPX_OK = 0
 SPX_FP64 = 0

@@ -28,26 +28,32 @@ template <class R> __device__ __forceinline__ V3<R> vel_cart(V3<R> mom) { R m = 
 
 // ---- spatial data (common/spatial_data.hh:55-135) ----------------------------------------------
 constexpr unsigned kU = 0x1, kB = 0x2, kE = 0x4, kAll = 0x7, kGradU = 0x10, kGradB = 0x20, kDUdt = 0x100;
+// Mask bit of this implementation: the caller needs only div U, div b, b.grad(b) and grad|B|, not
+// the gradient matrices (Parker transport).
+constexpr unsigned kDerivedOnly = 0x4000;
 
 template <class R>
 struct SD {
-   V3<R> U, B, E, bhat, gradBmag, dUdt, region;
+   V3<R> U, B, E, bhat, gradBmag, dUdt, region, bgradb;
    M3<R> gradU, gradB;
-   R Bmag, dmax;
+   R Bmag, dmax, divU, divbhat;
    R dr[3];
 };
 
-template <class R> __device__ __forceinline__ R sd_divU(const SD<R>& s) { return trace(s.gradU); }
+template <class R> __device__ __forceinline__ R sd_divU(const SD<R>& s) { return s.divU; }
 template <class R> __device__ __forceinline__ V3<R> sd_curlB(const SD<R>& s)
 {
    return {s.gradB.m[1][2] - s.gradB.m[2][1], s.gradB.m[2][0] - s.gradB.m[0][2], s.gradB.m[0][1] - s.gradB.m[1][0]};
 }
-// divbhat and bhat.grad(bhat), common/spatial_data.hh:288-330
-template <class R> __device__ __forceinline__ R sd_divbhat(const SD<R>& s)
+template <class R> __device__ __forceinline__ R sd_divbhat(const SD<R>& s) { return s.divbhat; }
+template <class R> __device__ __forceinline__ V3<R> sd_b_gradbhat(const SD<R>& s) { return s.bgradb; }
+
+// div U, divbhat and bhat.grad(bhat) from the gradient matrices (common/spatial_data.hh:213-330)
+template <class R> __device__ __forceinline__ R mat_divbhat(const SD<R>& s)
 {
    return (trace(s.gradB) - dot(s.gradBmag, s.bhat)) / s.Bmag;
 }
-template <class R> __device__ __forceinline__ V3<R> sd_b_gradbhat(const SD<R>& s)
+template <class R> __device__ __forceinline__ V3<R> mat_b_gradbhat(const SD<R>& s)
 {
    V3<R> r;
    R o[3];
@@ -86,6 +92,13 @@ template <class R> __device__ __forceinline__ V3<R> eframe_from(const BgParamsT<
    return {a.x * g.eprime[0][0] + a.y * g.eprime[1][0] + a.z * g.eprime[2][0],
            a.x * g.eprime[0][1] + a.y * g.eprime[1][1] + a.z * g.eprime[2][1],
            a.x * g.eprime[0][2] + a.y * g.eprime[1][2] + a.z * g.eprime[2][2]};
+}
+
+template <class R> __device__ __forceinline__ void derive_from_matrices(SD<R>& s)
+{
+   s.divU = trace(s.gradU);
+   s.divbhat = mat_divbhat(s);
+   s.bgradb = mat_b_gradbhat(s);
 }
 
 // EvaluateBackground of the analytic backgrounds: U, B, E by mask, region; *ds is the smooth-shock
@@ -168,63 +181,61 @@ __device__ __forceinline__ R eval_dmax(const BgParamsT<R>& g, R t, V3<R> pos)
    return g.dmax0;
 }
 
-// Analytic gradients of the Parker spiral. With x the position in the rotation frame, r = |x|,
-// A = Br0 r_ref^2, k = A w0 / ur and w = (x2, -x1, 0):
-//   B = A x / r^3 + k f(r) w,  f = (r - r_ref) / r^3,  f' = (3 r_ref - 2 r) / r^4,
-//   d_i B_j = A (delta_ij / r^3 - 3 x_i x_j / r^5) + k (f' x_i w_j / r + f dw_j/dx_i),
-//   d_i U_j = ur (delta_ij / r - x_i x_j / r^3),   div U = 2 ur / r.
-// (The reference's SOLARWIND_DERIVATIVE_METHOD 0 branch is not buildable as shipped.)
+// The Parker spiral and its derivatives in closed form in the global frame (analytic mode). With
+// x = pos - r0, r = |x|, O = the rotation axis (eprime[2]), A = Br0 r_ref^2, k = A w0 / ur,
+// f = (r - r_ref) / r^3, f' = (3 r_ref - 2 r) / r^4 and w = x cross O:
+//   U = ur x / r,   B = A x / r^3 + k f w   (the field of src/background_solarwind.cc:111-249
+//   without the angles: Br = A / r^2 along x/r, B_phi phi = k f w),
+//   d_i U_j = ur (delta_ij / r - x_i x_j / r^3),  div U = 2 ur / r,
+//   d_i B_j = A (delta_ij / r^3 - 3 x_i x_j / r^5) + k (f' x_i w_j / r + f eps_jil O_l),  div B = 0,
+//   grad|B| = (grad B) b = A (b / r^3 - 3 (x.b) x / r^5) + k (f' (w.b) x / r + f O x b),
+//   b^T grad B = A (b / r^3 - 3 (x.b) x / r^5) + k (f' (x.b) w / r + f b x O).
 template <class R>
-__device__ __forceinline__ void solarwind_grad(const BgParamsT<R>& g, V3<R> pos, SD<R>& s, bool need_gradB)
+__device__ __forceinline__ bool solarwind_closed(const BgParamsT<R>& g, V3<R> pos, unsigned mask, SD<R>& s)
 {
-   V3<R> x = eframe_to(g, pos - ld3(g.r0));
-   R r = norm(x), ir = R(1) / r, ir2 = ir * ir, ir3 = ir2 * ir;
+   V3<R> x = pos - ld3(g.r0), O = mk(g.eprime[2][0], g.eprime[2][1], g.eprime[2][2]);
+   R r2 = norm2(x), r = m_sqrt(r2), ir = R(1) / r, ir2 = ir * ir, ir3 = ir2 * ir;
+   s.dmax = m_min(g.dmax_fraction * r, g.dmax0);
+   s.region = mk(r < R(117.0 * 1.495978707E+13 / 1.0e10) ? R(1) : R(-1), R(-1), s.region.z);
+   R k = g.A * g.w0 / g.ur0;
+   R f = (r - g.r_ref) * ir3;
+   V3<R> w = cross(x, O);
+   s.U = (g.ur0 * ir) * x;
+   s.B = (g.A * ir3) * x + (k * f) * w;
+   if (mask & kE) s.E = (R(-1) / c_code<R>()) * cross(s.U, s.B);
+   s.Bmag = norm(s.B);
+   if (!(s.Bmag >= Lim<R>::tiny)) return false;
+   R iB = R(1) / s.Bmag;
+   s.bhat = iB * s.B;
+   if (!(mask & (kGradU | kGradB | kDUdt))) return true;
+   R fp = (R(3) * g.r_ref - R(2) * r) * ir2 * ir2;
+   R xb = dot(x, s.bhat), wb = dot(w, s.bhat);
+   R a3 = g.A * ir3, a5 = R(3) * g.A * ir3 * ir2 * xb;
+   s.gradBmag = (a3 * s.bhat - a5 * x) + ((k * fp * wb * ir) * x + (k * f) * cross(O, s.bhat));
+   V3<R> bgB = (a3 * s.bhat - a5 * x) + ((k * fp * xb * ir) * w + (k * f) * cross(s.bhat, O));
+   R bgm = dot(s.bhat, s.gradBmag);
+   s.divU = R(2) * g.ur0 * ir;
+   s.divbhat = -bgm * iB;
+   s.bgradb = iB * (bgB - bgm * s.bhat);
+   s.dUdt = mk(R(0), R(0), R(0));
    R xs[3] = {x.x, x.y, x.z};
-   M3<R> gu, gb;
 #pragma unroll
    for (int i = 0; i < 3; i++)
 #pragma unroll
-      for (int j = 0; j < 3; j++) gu.m[i][j] = g.ur0 * ((i == j ? ir : R(0)) - xs[i] * xs[j] * ir3);
-   // rotate to the global frame: grad = E^T grad' E (E rows = eprime)
-   M3<R> G;
-#pragma unroll
-   for (int i = 0; i < 3; i++)
-#pragma unroll
-      for (int j = 0; j < 3; j++) {
-         R acc = R(0);
-#pragma unroll
-         for (int a = 0; a < 3; a++)
-#pragma unroll
-            for (int b = 0; b < 3; b++) acc += g.eprime[a][i] * gu.m[a][b] * g.eprime[b][j];
-         G.m[i][j] = acc;
-      }
-   s.gradU = G;
-   if (need_gradB) {
-      R k = g.A * g.w0 / g.ur0;
-      R f = (r - g.r_ref) * ir3, fp = (R(3) * g.r_ref - R(2) * r) * ir2 * ir2;
-      R w[3] = {x.y, -x.x, R(0)};
+      for (int j = 0; j < 3; j++) s.gradU.m[i][j] = g.ur0 * ((i == j ? ir : R(0)) - xs[i] * xs[j] * ir3);
+   if (!(mask & kDerivedOnly)) {
+      R ws[3] = {w.x, w.y, w.z}, Os[3] = {O.x, O.y, O.z};
 #pragma unroll
       for (int i = 0; i < 3; i++)
 #pragma unroll
          for (int j = 0; j < 3; j++)
-            gb.m[i][j] = g.A * ((i == j ? ir3 : R(0)) - R(3) * xs[i] * xs[j] * ir3 * ir2) + k * (fp * xs[i] * w[j] * ir);
-      gb.m[0][1] -= k * f;
-      gb.m[1][0] += k * f;
-#pragma unroll
-      for (int i = 0; i < 3; i++)
-#pragma unroll
-         for (int j = 0; j < 3; j++) {
-            R acc = R(0);
-#pragma unroll
-            for (int a = 0; a < 3; a++)
-#pragma unroll
-               for (int b = 0; b < 3; b++) acc += g.eprime[a][i] * gb.m[a][b] * g.eprime[b][j];
-            G.m[i][j] = acc;
-         }
-      s.gradB = G;
-      s.gradBmag = mv(s.gradB, s.bhat);
+            s.gradB.m[i][j] = g.A * ((i == j ? ir3 : R(0)) - R(3) * xs[i] * xs[j] * ir3 * ir2) + k * (fp * xs[i] * ws[j] * ir);
+      // f eps_jil O_l
+      s.gradB.m[0][1] -= k * f * Os[2]; s.gradB.m[1][0] += k * f * Os[2];
+      s.gradB.m[0][2] += k * f * Os[1]; s.gradB.m[2][0] -= k * f * Os[1];
+      s.gradB.m[1][2] -= k * f * Os[0]; s.gradB.m[2][1] += k * f * Os[0];
    }
-   s.dUdt = mk(R(0), R(0), R(0));
+   return true;
 }
 
 // BackgroundBase::NumericalDerivatives restricted to U and B (src/background_base.cc:228-312):
@@ -289,6 +300,10 @@ template <int BG, class R>
 __device__ __forceinline__ bool get_fields(const BgParamsT<R>& g, int deriv_mode, R t, V3<R> pos, R p, unsigned mask,
                                            SD<R>& s)
 {
+   if (BG == kBgSolarWind && deriv_mode == 1) {
+      s.dr[0] = s.dr[1] = s.dr[2] = R(0.0001) * g.dmax0;
+      return solarwind_closed(g, pos, mask, s);
+   }
    R ds = R(0);
    s.dmax = eval_dmax<BG>(g, t, pos);
    eval_bg<BG>(g, t, pos, mask, s, ds);
@@ -304,6 +319,10 @@ __device__ __forceinline__ bool get_fields(const BgParamsT<R>& g, int deriv_mode
       zero(s.gradB);
       s.gradBmag = mk(R(0), R(0), R(0));
       s.dUdt = mk(R(0), R(0), R(0));
+      s.divU = R(0);
+      s.divbhat = R(0);
+      s.bgradb = mk(R(0), R(0), R(0));
+      return true;
    }
    else if (BG == kBgSmoothShock) {  // src/background_smooth_shock.cc:149-183
       R tr = shock_trd(ds);
@@ -336,9 +355,9 @@ __device__ __forceinline__ bool get_fields(const BgParamsT<R>& g, int deriv_mode
       s.dUdt = mk(R(0), R(0), R(0));
    }
    else if (BG == kBgSolarWind) {
-      if (deriv_mode == 1) solarwind_grad(g, pos, s, (mask & kGradB) != 0);
-      else numerical_derivs<BG>(g, t, pos, p, s, mask);
+      numerical_derivs<BG>(g, t, pos, p, s, mask);
    }
+   derive_from_matrices(s);
    return true;
 }
 
@@ -429,6 +448,14 @@ __device__ __forceinline__ R kappa_mumu_dmu(const DiffParamsT<R>& d, R vmag, R O
    if (d.kind != kDfQLT) return R(0);
    R dmu = Lim<R>::small * (mu + Lim<R>::small < R(1) ? R(1) : R(-1));
    return (kappa_mumu(d, vmag, Omega, mu + dmu) - dmumu) / dmu;
+}
+
+// Models whose gradient needs no field-gradient matrix (only grad|B| or grad U . U).
+template <class R>
+__device__ __forceinline__ bool kappa_grad_is_analytic(const DiffParamsT<R>& d)
+{
+   return d.kind == kDfPara || d.kind == kDfPerp || d.kind == kDfFull || d.kind == kDfFlowMomentum ||
+          d.kind == kDfKinEnergyRadial || d.kind == kDfRigidityB;
 }
 
 // Spatial gradients of K_perp and K_para: the analytic GetDirectionalDerivative overrides

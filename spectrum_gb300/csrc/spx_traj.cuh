@@ -283,16 +283,17 @@ static __device__ __noinline__ void process_event(int traj, const EventPoint& e,
    for (int k = 0; k < 3; k++) {
       if (!(d.dims & (1 << k))) continue;
       double val = (d.log_bins[k] ? log10(value[k]) : value[k]) - d.limits0[k];
-      if (!(val >= 0.0)) {
-         if (d.bin_outside[k] && val < 0.0) { bin[k] = 0; continue; }
-         return;
-      }
+      if (val != val) return;
+      // a "left" outlier is dropped unless bin_outside; the bin is then still val / bin_size, which
+      // is how a negative bin width (max < min, e.g. backward exit times) bins correctly
+      if (val < 0.0 && !d.bin_outside[k]) return;
       double q = val / d.bin_size[k];
       if (q >= (double)d.n_bins[k]) {
          if (d.bin_outside[k]) { bin[k] = d.n_bins[k] - 1; continue; }
          return;
       }
-      bin[k] = (int)q;
+      // the reference indexes before the array for q <= -1 (bin_outside set); bin 0 here
+      bin[k] = q <= -1.0 ? 0 : (int)q;
    }
    int64_t lin = (int64_t)d.n_bins[2] * ((int64_t)d.n_bins[1] * bin[0] + bin[1]) + bin[2];
    double ew = exp(e.wgt);
@@ -315,12 +316,18 @@ __device__ __forceinline__ EventPoint event_point(const Lane<R, A>& L, const SD<
    return e;
 }
 
+// Boundaries are held compactly: j < nbt time, then nbs spatial, then nbm momentum boundaries.
+template <class R>
+__device__ __forceinline__ const BndParamsT<R>& bnd_param(const ProblemDescT<R>& P, int j)
+{
+   return j < P.nbt ? P.bt[j] : (j < P.nbt + P.nbs ? P.bs[j - P.nbt] : P.bm[j - P.nbt - P.nbs]);
+}
+
 template <int TT, class R, class A>
 __device__ __forceinline__ void distro_events(const Lane<R, A>& L, const SD<R>& sp, const Start& s0,
-                                              const ProblemDesc& Pd, int bnd_global, const Sinks& S)
+                                              const ProblemDesc& Pd, int j, const Sinks& S)
 {
-   const BndParams& b = bnd_global < kMaxBnd ? Pd.bt[bnd_global]
-                      : (bnd_global < 2 * kMaxBnd ? Pd.bs[bnd_global - kMaxBnd] : Pd.bm[bnd_global - 2 * kMaxBnd]);
+   const BndParams& b = bnd_param(Pd, j);
    EventPoint e = event_point(L, sp);
    for (int di = 0; di < Pd.nd; di++) {
       int action = di < b.n_actions ? b.actions[di] : -1;
@@ -328,73 +335,63 @@ __device__ __forceinline__ void distro_events(const Lane<R, A>& L, const SD<R>& 
    }
 }
 
-// Boundary slots: 0..3 time, 4..7 space, 8..11 momentum.
-template <class R>
-__device__ __forceinline__ const BndParamsT<R>& bnd_param(const ProblemDescT<R>& P, int k)
-{
-   return k < kMaxBnd ? P.bt[k] : (k < 2 * kMaxBnd ? P.bs[k - kMaxBnd] : P.bm[k - 2 * kMaxBnd]);
-}
-template <class R>
-__device__ __forceinline__ bool bnd_used(const ProblemDescT<R>& P, int k)
-{
-   return k < kMaxBnd ? k < P.nbt : (k < 2 * kMaxBnd ? k - kMaxBnd < P.nbs : k - 2 * kMaxBnd < P.nbm);
-}
-
 // ---- HandleBoundaries (src/trajectory_base.cc:413-535) ---------------------------------------
+// ComputeAllBoundaries, the momentum/space/time handlers with their distribution events, and
+// UpdateAllBoundaries. A boundary that was not crossed is recorded right after it is computed
+// (RecordBoundary only copies delta to delta_old for it); crossed ones after their events.
 template <int TT, class R, class A>
 __device__ void handle_boundaries(Lane<R, A>& L, BndState<R>* bs, const SD<R>& sp, const Start& s0,
                                   const ProblemDescT<R>& P, const ProblemDesc& Pd, const Sinks& S)
 {
    V3<R> pos = val3<R>(L.pos), mom = lane_mom(L);
+   const int nb = P.nbt + P.nbs + P.nbm;
    unsigned crossed = 0;
-#pragma unroll 1
-   for (int k = 0; k < kMaxBndTotal; k++) {
-      if (!bnd_used(P, k)) continue;
-      compute_bnd(bnd_param(P, k), bs[k], L.t, pos, mom, sp.bhat, sp.region, TT);
-      if (bs[k].crossed) crossed |= 1u << k;
+   for (int j = 0; j < nb; j++) {
+      compute_bnd(bnd_param(P, j), bs[j], L.t, pos, mom, sp.bhat, sp.region, TT);
+      if (bs[j].crossed) crossed |= 1u << j;
+      else bs[j].delta_old = bs[j].delta;
    }
-   if (crossed) {
-      // momentum boundaries
-      int active = -1;
-      for (int k = 2 * kMaxBnd; k < 3 * kMaxBnd; k++) {
-         if (!(crossed & (1u << k))) continue;
-         active = k;
-         if (!bnd_param(P, k).reflect && bs[k].crossings_left == 1) L.status |= TRAJ_MOMENTUM_CROSSED | TRAJ_FINISH;
-      }
-      if (active >= 0) distro_events<TT>(L, sp, s0, Pd, active, S);
-      // spatial boundaries
-      active = -1;
-      for (int k = kMaxBnd; k < 2 * kMaxBnd; k++) {
-         if (!(crossed & (1u << k))) continue;
-         active = k;
-         const BndParamsT<R>& b = bnd_param(P, k);
-         if (b.reflect) {
-            // src/trajectory_base.cc:462-483: mirror the position, reverse the momentum
-            V3<R> shift = (R(2) * bs[k].delta) * bnd_normal(b, pos);
-            add3(L.pos, R(-1) * shift);
-            if (TT != kParker && TT != kParkerSource) {
-               L.mom.x = neg(L.mom.x); L.mom.y = neg(L.mom.y); L.mom.z = neg(L.mom.z);
-            }
-            pos = val3<R>(L.pos);
-            mom = lane_mom(L);
-            compute_bnd(b, bs[k], L.t, pos, mom, sp.bhat, sp.region, TT);
-            bs[k].crossings_left--;
+   if (!crossed) return;
+   const int s_lo = P.nbt, m_lo = P.nbt + P.nbs;
+   // momentum boundaries
+   int active = -1;
+   for (int j = m_lo; j < nb; j++) {
+      if (!(crossed & (1u << j))) continue;
+      active = j;
+      if (!bnd_param(P, j).reflect && bs[j].crossings_left == 1) L.status |= TRAJ_MOMENTUM_CROSSED | TRAJ_FINISH;
+   }
+   if (active >= 0) distro_events<TT>(L, sp, s0, Pd, active, S);
+   // spatial boundaries
+   active = -1;
+   for (int j = s_lo; j < m_lo; j++) {
+      if (!(crossed & (1u << j))) continue;
+      active = j;
+      const BndParamsT<R>& b = bnd_param(P, j);
+      if (b.reflect) {
+         // src/trajectory_base.cc:462-483: mirror the position, reverse the momentum
+         V3<R> shift = (R(2) * bs[j].delta) * bnd_normal(b, pos);
+         add3(L.pos, R(-1) * shift);
+         if (TT != kParker && TT != kParkerSource) {
+            L.mom.x = neg(L.mom.x); L.mom.y = neg(L.mom.y); L.mom.z = neg(L.mom.z);
          }
-         else if (bs[k].crossings_left == 1) L.status |= TRAJ_SPATIAL_CROSSED | TRAJ_FINISH;
+         pos = val3<R>(L.pos);
+         mom = lane_mom(L);
+         compute_bnd(b, bs[j], L.t, pos, mom, sp.bhat, sp.region, TT);
+         bs[j].crossings_left--;
       }
-      if (active >= 0) distro_events<TT>(L, sp, s0, Pd, active, S);
-      // time boundaries
-      active = -1;
-      for (int k = 0; k < kMaxBnd; k++) {
-         if (!(crossed & (1u << k))) continue;
-         active = k;
-         if (bs[k].crossings_left == 1) L.status |= TRAJ_TIME_CROSSED | TRAJ_FINISH;
-      }
-      if (active >= 0) distro_events<TT>(L, sp, s0, Pd, active, S);
+      else if (bs[j].crossings_left == 1) L.status |= TRAJ_SPATIAL_CROSSED | TRAJ_FINISH;
    }
-#pragma unroll 1
-   for (int k = 0; k < kMaxBndTotal; k++)
-      if (bnd_used(P, k)) record_bnd(bnd_param(P, k), bs[k], L.t, pos, mom, sp.bhat, sp.region, TT);
+   if (active >= 0) distro_events<TT>(L, sp, s0, Pd, active, S);
+   // time boundaries
+   active = -1;
+   for (int j = 0; j < s_lo; j++) {
+      if (!(crossed & (1u << j))) continue;
+      active = j;
+      if (bs[j].crossings_left == 1) L.status |= TRAJ_TIME_CROSSED | TRAJ_FINISH;
+   }
+   if (active >= 0) distro_events<TT>(L, sp, s0, Pd, active, S);
+   for (int j = 0; j < nb; j++)
+      if (crossed & (1u << j)) record_bnd(bnd_param(P, j), bs[j], L.t, pos, mom, sp.bhat, sp.region, TT);
 }
 
 // SpaceTerminateCheck (src/trajectory_base.cc:188-237); true if the trajectory ended mid-step
@@ -403,11 +400,11 @@ __device__ bool space_terminate(Lane<R, A>& L, BndState<R>* bs, const SD<R>& sp,
                                 const ProblemDescT<R>& P, const ProblemDesc& Pd, const Sinks& S)
 {
    V3<R> pos = val3<R>(L.pos), mom = lane_mom(L);
-   for (int k = kMaxBnd; k < kMaxBnd + P.nbs; k++) {
-      compute_bnd(bnd_param(P, k), bs[k], L.t, pos, mom, sp.bhat, sp.region, TT);
-      if (bs[k].crossed && bs[k].crossings_left == 1) {
+   for (int j = P.nbt; j < P.nbt + P.nbs; j++) {
+      compute_bnd(bnd_param(P, j), bs[j], L.t, pos, mom, sp.bhat, sp.region, TT);
+      if (bs[j].crossed && bs[j].crossings_left == 1) {
          L.status |= TRAJ_SPATIAL_CROSSED | TRAJ_FINISH;
-         distro_events<TT>(L, sp, s0, Pd, k, S);
+         distro_events<TT>(L, sp, s0, Pd, j, S);
          L.steps++;
          return true;
       }
@@ -471,7 +468,8 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndState<R>* bs, c
    R p = (R)acc_val(L.mom.x);
    R t = (R)acc_val(L.t);
    SD<R> sp;
-   if (!get_fields<BG>(P.bg, deriv_mode, t, pos, p, traj_mask<kParker>(), sp)) { L.status |= TRAJ_DISCARD; return; }
+   const unsigned mask = traj_mask<kParker>() | (kappa_grad_is_analytic(P.df) ? kDerivedOnly : 0u);
+   if (!get_fields<BG>(P.bg, deriv_mode, t, pos, p, mask, sp)) { L.status |= TRAJ_DISCARD; return; }
    R vmag = vel_of(p);
    // DiffusionCoeff (src/trajectory_parker.cc:83-153)
    Kap<R> K = kappa_pp(P.df, pos, p, vmag, sp);
@@ -503,15 +501,16 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndState<R>* bs, c
    dtp = m_min(dtp, R(0.5) * R(3) * R(0.01) / m_abs(divU));
    L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bs, P.nbt, fwd);
    // EulerDiffSlopes (src/trajectory_parker.cc:159-180)
+   R n[4];
+   normals4<R>(rng_block(P.seed, L.steps, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
+   R sdt = m_sqrt(L.dt);
+   R sperp = m_sqrt(R(2) * K.perp), spara = m_sqrt(R(2) * K.para);
+   // the reference's field-aligned basis (GetSecondUnitVec): n0, n1 across, n2 along the field
    V3<R> fa[3];
    fa[2] = sp.bhat;
    fa[0] = second_unit(sp.bhat);
    fa[1] = cross(fa[2], fa[0]);
-   R n[4];
-   normals4<R>(rng_block(P.seed, L.steps, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
-   R sdt = m_sqrt(L.dt);
    R dWx = sdt * n[0], dWy = sdt * n[1], dWz = sdt * n[2];
-   R sperp = m_sqrt(R(2) * K.perp), spara = m_sqrt(R(2) * K.para);
    V3<R> dr = from_basis(mk(sperp * dWx, sperp * dWy, spara * dWz), fa);
    // RKStep with the Euler table, then the stochastic displacement
    R dts = L.dt * R(1);
@@ -763,10 +762,9 @@ __device__ __noinline__ void set_start(Lane<R, A>& L, BndState<R>* bs, Start& s0
    R c = c_code<R>();
    L.dt_adapt = Lim<R>::large * sp.dmax / c;
    V3<R> mr = lane_mom(L);
-   for (int k = 0; k < kMaxBndTotal; k++) {
-      if (!bnd_used(P, k)) continue;
-      R scale = k < kMaxBnd ? sp.dmax / c : (k < 2 * kMaxBnd ? sp.dmax : norm(mr));
-      reset_bnd(bnd_param(P, k), bs[k], scale, L.t, pr, mr, sp.bhat, sp.region, TT);
+   for (int j = 0; j < P.nbt + P.nbs + P.nbm; j++) {
+      R scale = j < P.nbt ? sp.dmax / c : (j < P.nbt + P.nbs ? sp.dmax : norm(mr));
+      reset_bnd(bnd_param(P, j), bs[j], scale, L.t, pr, mr, sp.bhat, sp.region, TT);
    }
    // TrajectoryParkerSource::SetStart (src/trajectory_parker_source.cc:43-50)
    if (P.src.kind == 2) L.src_del_old = mr.x - P.src.p_inj;
@@ -815,8 +813,16 @@ __device__ __forceinline__ void start_lane(Lane<R, A>& L, BndState<R>* bs, Start
    set_start<TT, BG>(L, bs, s0, P[L.prob], Pd[L.prob], cfg, local);
 }
 
+// Resident blocks of 128 threads per SM the register allocation is sized for.
+#ifndef SPX_MIN_BLOCKS_F32
+#define SPX_MIN_BLOCKS_F32 1
+#endif
+#ifndef SPX_MIN_BLOCKS_F64
+#define SPX_MIN_BLOCKS_F64 1
+#endif
+
 template <int TT, int BG, class R>
-__global__ void __launch_bounds__(128) step_kernel(const ProblemDescT<R>* __restrict__ P, const ProblemDesc* __restrict__ Pd,
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? SPX_MIN_BLOCKS_F32 : SPX_MIN_BLOCKS_F64) step_kernel(const ProblemDescT<R>* __restrict__ P, const ProblemDesc* __restrict__ Pd,
                                                    RunConfig cfg, RunCounters* ctr, int32_t* counts, double* sums,
                                                    unsigned long long* n_events, TrajRecord* rec, int queue)
 {

@@ -174,7 +174,7 @@ def modulation_energies(n: int = 32, e1_mev: float = 10.0, e2_mev: float = 1.0e4
 
 def gcr_modulation(n_traj: int = 1_000_000, energies_mev=None, lam0_au: float = 0.1, pow_law_r: float = 0.5,
                    pow_law_b: float = -1.0, kap_rat: float = 0.02, r_inner_au: float = 0.05,
-                   r_outer_au: float = 100.0, t_max_years: float = 2.0, lis_gamma: float = -1.8) -> list[Problem]:
+                   r_outer_au: float = 100.0, t_max_years: float = 1.0, lis_gamma: float = -1.8) -> list[Problem]:
     """One problem per energy: start at 1 AU, trace backward until the 100 AU outer boundary
     (hot: weighted by the LIS J0 (T/T0)^gamma / p^2 * v, src/distribution_other.cc:553-602), the
     0.05 AU inner boundary (cold) or the time limit.
@@ -195,9 +195,10 @@ def gcr_modulation(n_traj: int = 1_000_000, energies_mev=None, lam0_au: float = 
         pb.AddInitial(InitialSpaceFixed(), DataContainer().vec((ONE_AU, 0, 0)))
         p0 = U.mev_to_mom(e)
         pb.AddInitial(InitialMomentumShell(), DataContainer().double(p0))
-        pb.AddBoundary(BoundarySphereAbsorb(), _boundary(DataContainer(), 1, [1]).vec((0, 0, 0)).double(r_inner_au * ONE_AU))
-        pb.AddBoundary(BoundarySphereAbsorb(), _boundary(DataContainer(), 1, [0]).vec((0, 0, 0)).double(r_outer_au * ONE_AU))
-        pb.AddBoundary(BoundaryTimeExpire(), _boundary(DataContainer(), 1, [-1]).double(-t_max))
+        # actions per distribution: (spectrum, exit time); the inner boundary is "cold" for the spectrum
+        pb.AddBoundary(BoundarySphereAbsorb(), _boundary(DataContainer(), 1, [1, -1]).vec((0, 0, 0)).double(r_inner_au * ONE_AU))
+        pb.AddBoundary(BoundarySphereAbsorb(), _boundary(DataContainer(), 1, [0, 0]).vec((0, 0, 0)).double(r_outer_au * ONE_AU))
+        pb.AddBoundary(BoundaryTimeExpire(), _boundary(DataContainer(), 1, [-1, -1]).double(-t_max))
         pb.AddDiffusion(DiffusionRigidityMagneticFieldPowerLaw(),
                         DataContainer().double(lam0_au * ONE_AU).double(r0_rig).double(BMAG_1AU)
                         .double(pow_law_r).double(pow_law_b).double(kap_rat))
@@ -207,6 +208,12 @@ def gcr_modulation(n_traj: int = 1_000_000, energies_mev=None, lam0_au: float = 
                           unit_distro=unit_distro, unit_val=(U.unit_energy, 1.0, 1.0))
         c.double(1.0 / unit_distro).double(1.0 * U.GEV / U.unit_energy).double(lis_gamma).double(0.0)
         pb.AddDistribution(DistributionSpectrumKineticEnergyPowerLaw(), c)
+        # exit-time histogram of the run example (runs/gcr_modulation_example.cc:280-330): bins from 0
+        # to the (negative) time limit, outliers into the end bins
+        c = distro_header(DataContainer(), (32, 0, 0), (0.0, 0, 0), (-t_max, 0, 0), bin_outside=(1, 0, 0),
+                          unit_val=(U.unit_time, 1.0, 1.0))
+        c.double(1.0).double(0.0).int(1)
+        pb.AddDistribution(DistributionTimeUniform(), c)
         out.append(pb)
     return out
 
