@@ -2028,3 +2028,8 @@ void spx_oracle_uniforms(uint64_t seed, uint32_t index, uint32_t traj, uint32_t 
    spx_rng_block(seed, index, traj, problem, SPX_RNG_INIT, attempt, b);
    for (i = 0; i < 4; i++) out[i] = spx_u01(b[i]);
 }
+
+void spx_oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4])
+{
+   spx_philox4x32_10(ctr, key, out);
+}

@@ -58,6 +58,8 @@ void spx_oracle_normals(uint64_t seed, uint32_t index, uint32_t traj, uint32_t p
                         double out[4]);
 void spx_oracle_uniforms(uint64_t seed, uint32_t index, uint32_t traj, uint32_t problem, uint32_t attempt,
                          double out[4]);
+/* Philox4x32-10 of one counter under one key (for the generator's known-answer tests). */
+void spx_oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 
 #ifdef __cplusplus
 }

@@ -4,7 +4,7 @@
  * This header is part of the ORACLE: it is used by the CPU restatement in oracle/spx_oracle.c
  * and by the GSL stand-in that lets the reference's own sources run with the same random
  * numbers (oracle/ref_glue). Nothing in the product library includes it; the CUDA kernels
- * carry their own implementation (spectrum_gb300/csrc/spx_rng.cuh) and the tests check the two
+ * carry their own implementation (spectrum_gb300/csrc/spx_device.cuh) and the tests check the two
  * against each other.
  *
  * Generator: Philox4x32-10, the published counter-based generator of Salmon, Moraes, Dror and

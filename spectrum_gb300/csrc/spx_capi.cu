@@ -172,16 +172,28 @@ cudaError_t launch(spx_ctx* c, const spx::LaunchArgs& a)
    }
 }
 
-int occupancy(spx_ctx* c, int block)
+int occupancy(spx_ctx* c, int block, int slots)
 {
    bool f64 = c->precision == SPX_FP64;
+   int bg = c->bg_kind;
    switch (c->traj) {
    case SPX_TRAJ_PARKER:
-   case SPX_TRAJ_PARKER_SOURCE: return f64 ? spx::occupancy_parker_f64(c->bg_kind, block) : spx::occupancy_parker_f32(c->bg_kind, block);
-   case SPX_TRAJ_LORENTZ: return f64 ? spx::occupancy_lorentz_f64(c->bg_kind, block) : spx::occupancy_lorentz_f32(c->bg_kind, block);
-   case SPX_TRAJ_FOCUSED: return f64 ? spx::occupancy_focused_f64(c->bg_kind, block) : spx::occupancy_focused_f32(c->bg_kind, block);
+   case SPX_TRAJ_PARKER_SOURCE:
+      return f64 ? spx::occupancy_parker_f64(bg, block, slots) : spx::occupancy_parker_f32(bg, block, slots);
+   case SPX_TRAJ_LORENTZ:
+      return f64 ? spx::occupancy_lorentz_f64(bg, block, slots) : spx::occupancy_lorentz_f32(bg, block, slots);
+   case SPX_TRAJ_FOCUSED:
+      return f64 ? spx::occupancy_focused_f64(bg, block, slots) : spx::occupancy_focused_f32(bg, block, slots);
    default: return 0;
    }
+}
+
+// Boundary states a lane holds: the largest boundary count of the context's problems.
+int bnd_slots(const spx_ctx* c)
+{
+   int n = 1;
+   for (const auto& p : c->problems) n = std::max(n, p.pd.nbt + p.pd.nbs + p.pd.nbm);
+   return n;
 }
 
 bool valid_ctx(spx_ctx* c) { return c != nullptr; }
@@ -320,7 +332,8 @@ int spx_run(spx_ctx_t c, const spx_tuning* tuning)
    if (tu.block_size % 32 || tu.block_size > 128) return SPX_ERR_INVALID_ARG;
    if (!tuning) tu.schedule = c->precision == SPX_MIXED ? 1 : 0;
    if (tu.steps_per_sync <= 0) tu.steps_per_sync = tu.schedule ? 16 : 1 << 30;
-   int occ = occupancy(c, tu.block_size);
+   const int slots = bnd_slots(c);
+   int occ = occupancy(c, tu.block_size, slots);
    if (occ <= 0) occ = 1;
    if (tu.blocks_per_sm <= 0 || tu.blocks_per_sm > occ) tu.blocks_per_sm = occ;
    spx::LaunchArgs a;
@@ -352,6 +365,7 @@ int spx_run(spx_ctx_t c, const spx_tuning* tuning)
    a.n_events = c->d_nev;
    a.records = c->d_rec;
    a.queue = tu.schedule;
+   a.bnd_slots = slots;
    if (c->record_final && c->d_rec == nullptr) return SPX_ERR_STATE;
    SPX_CUDA(cudaMemsetAsync(c->d_ctr, 0, sizeof(spx::RunCounters), c->stream));
    SPX_CUDA(cudaEventRecord(c->ev0, c->stream));

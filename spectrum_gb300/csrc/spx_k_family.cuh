@@ -1,0 +1,69 @@
+// spx_k_family.cuh -- launch and occupancy entry points of the stepping kernel for one
+// trajectory family in one arithmetic, switching over the background classes. Each spx_k_*.cu
+// instantiates it once, so the six families compile in parallel.
+#pragma once
+
+#include "spx_launch.hh"
+#include "spx_traj.cuh"
+
+namespace spx {
+
+template <int TT, class R>
+struct FamilyTU {
+   // dynamic shared memory: the boundary states of every lane of a block
+   static size_t smem(int slots, int block) { return (size_t)(slots > 0 ? slots : 1) * block * sizeof(BndState<R>); }
+
+   template <int BG>
+   static cudaError_t go(const LaunchArgs& a)
+   {
+      const auto* P = static_cast<const ProblemDescT<R>*>(a.problems_r);
+      step_kernel<TT, BG, R><<<a.grid, a.block, smem(a.bnd_slots, a.block.x), a.stream>>>(
+          P, a.problems_d, a.cfg, a.ctr, a.counts, a.sums, a.n_events, a.records, a.queue);
+      return cudaGetLastError();
+   }
+
+   template <int BG>
+   static int occ(int block, int slots)
+   {
+      int n = 0;
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<TT, BG, R>, block, smem(slots, block)) !=
+          cudaSuccess)
+         n = 0;
+      return n;
+   }
+
+   static cudaError_t launch(int bg, const LaunchArgs& a)
+   {
+      switch (bg) {
+      case kBgUniform: return go<kBgUniform>(a);
+      case kBgShock: return go<kBgShock>(a);
+      case kBgSmoothShock: return go<kBgSmoothShock>(a);
+      case kBgDipole: return go<kBgDipole>(a);
+      case kBgSolarWind: return go<kBgSolarWind>(a);
+      default: return cudaErrorInvalidValue;
+      }
+   }
+
+   static int occupancy(int bg, int block, int slots)
+   {
+      switch (bg) {
+      case kBgUniform: return occ<kBgUniform>(block, slots);
+      case kBgShock: return occ<kBgShock>(block, slots);
+      case kBgSmoothShock: return occ<kBgSmoothShock>(block, slots);
+      case kBgDipole: return occ<kBgDipole>(block, slots);
+      case kBgSolarWind: return occ<kBgSolarWind>(block, slots);
+      default: return 0;
+      }
+   }
+};
+
+}  // namespace spx
+
+#define SPX_FAMILY_TU(fam, prec, TT, R)                                                                    \
+   namespace spx {                                                                                          \
+   cudaError_t launch_##fam##_##prec(int bg, const LaunchArgs& a) { return FamilyTU<TT, R>::launch(bg, a); } \
+   int occupancy_##fam##_##prec(int bg, int block, int slots)                                               \
+   {                                                                                                        \
+      return FamilyTU<TT, R>::occupancy(bg, block, slots);                                                  \
+   }                                                                                                        \
+   }

@@ -20,13 +20,14 @@ struct LaunchArgs {
    unsigned long long* n_events;
    TrajRecord* records;
    int queue;                       // 1: persistent work-queue schedule
+   int bnd_slots;                   // boundary states per lane (the largest problem's count)
 };
 
 #define SPX_DECLARE_FAMILY(fam)                                  \
    cudaError_t launch_##fam##_f64(int bg, const LaunchArgs& a);  \
    cudaError_t launch_##fam##_f32(int bg, const LaunchArgs& a);  \
-   int occupancy_##fam##_f64(int bg, int block);                 \
-   int occupancy_##fam##_f32(int bg, int block);
+   int occupancy_##fam##_f64(int bg, int block, int slots);      \
+   int occupancy_##fam##_f32(int bg, int block, int slots);
 SPX_DECLARE_FAMILY(parker)
 SPX_DECLARE_FAMILY(lorentz)
 SPX_DECLARE_FAMILY(focused)

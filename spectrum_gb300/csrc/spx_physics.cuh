@@ -372,8 +372,17 @@ struct Kap {
    R perp, para;
 };
 
+// The field values the coefficient models read: |B|, U and the region indicators. Passed by value
+// so the coefficient evaluation never takes the address of the lane's field record.
 template <class R>
-__device__ Kap<R> kappa_pp(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const SD<R>& s)
+struct KapIn {
+   R Bmag;
+   V3<R> U, region;
+};
+template <class R> __device__ __forceinline__ KapIn<R> kap_in(const SD<R>& s) { return {s.Bmag, s.U, s.region}; }
+
+template <class R>
+__device__ __forceinline__ Kap<R> kappa_pp(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const KapIn<R>& s)
 {
    Kap<R> K{R(0), R(0)};
    switch (d.kind) {
@@ -462,8 +471,15 @@ __device__ __forceinline__ bool kappa_grad_is_analytic(const DiffParamsT<R>& d)
 // (src/diffusion_other.cc:395-398, 473-476, 553-556, 637-642, 732-742, 818-823), else the
 // base-class central difference with the field moved along its gradient
 // (src/diffusion_base.cc:131-174).
+// Out-of-line evaluation for the difference quotients of the gradient (six calls a step).
 template <class R>
-__device__ void kappa_grad(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const SD<R>& s, Kap<R> K, V3<R>& gperp,
+__device__ __noinline__ Kap<R> kappa_pp_call(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, KapIn<R> s)
+{
+   return kappa_pp(d, pos, p, vmag, s);
+}
+
+template <class R>
+__device__ __forceinline__ void kappa_grad(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const SD<R>& s, Kap<R> K, V3<R>& gperp,
                            V3<R>& gpara)
 {
    switch (d.kind) {
@@ -499,19 +515,17 @@ __device__ void kappa_grad(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, cons
    }
    default: {
       R gpe[3], gpa[3];
-#pragma unroll 1
+      KapIn<R> q = kap_in(s);
+#pragma unroll
       for (int xyz = 0; xyz < 3; xyz++) {
-         SD<R> s2 = s;
          R dr = R(0.5) * s.dr[xyz];
          R e[3] = {R(0), R(0), R(0)};
          e[xyz] = dr;
-         s2.B = s.B + dr * row(s.gradB, xyz);
-         s2.Bmag = s.Bmag + s.gradBmag[xyz] * dr;
-         Kap<R> kf = kappa_pp(d, pos + mk(e[0], e[1], e[2]), p, vmag, s2);
-         s2.B = s2.B - (R(2) * dr) * row(s.gradB, xyz);
-         s2.Bmag = s2.Bmag - s.gradBmag[xyz] * (R(2) * dr);
+         q.Bmag = s.Bmag + s.gradBmag[xyz] * dr;
+         Kap<R> kf = kappa_pp_call(d, pos + mk(e[0], e[1], e[2]), p, vmag, q);
+         q.Bmag = q.Bmag - s.gradBmag[xyz] * (R(2) * dr);
          e[xyz] = dr - R(2) * dr;
-         Kap<R> kb = kappa_pp(d, pos + mk(e[0], e[1], e[2]), p, vmag, s2);
+         Kap<R> kb = kappa_pp_call(d, pos + mk(e[0], e[1], e[2]), p, vmag, q);
          gpe[xyz] = (kf.perp - kb.perp) / (R(2) * dr);
          gpa[xyz] = (kf.para - kb.para) / (R(2) * dr);
       }
@@ -526,10 +540,20 @@ __device__ void kappa_grad(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, cons
 // Transient state of one boundary (src/boundary_base.hh): delta, delta_old, crossings left,
 // crossed flag; TERMINAL is crossings_left == 1 (src/boundary_base.cc:150-151, 187-188).
 template <class R>
-struct BndState {
+struct alignas(sizeof(R) == 4 ? 16 : 8) BndState {
    R delta, delta_old;
    int crossings_left;
    int crossed;
+};
+
+// The boundary states of one lane, held in dynamic shared memory: state j of the block's lanes
+// is one contiguous row, so a warp reads or writes a row with conflict-free vector accesses.
+template <class R>
+struct BndView {
+   BndState<R>* p;  // this lane's state 0
+   int stride;      // lanes per block
+   __device__ __forceinline__ BndState<R> ld(int j) const { return p[j * stride]; }
+   __device__ __forceinline__ void st(int j, const BndState<R>& b) const { p[j * stride] = b; }
 };
 
 // Outward normal of a reflecting spatial boundary at "pos" (the _normal of EvaluateBoundary).

@@ -335,30 +335,22 @@ __device__ __forceinline__ void distro_events(const Lane<R, A>& L, const SD<R>& 
    }
 }
 
-// ---- HandleBoundaries (src/trajectory_base.cc:413-535) ---------------------------------------
-// ComputeAllBoundaries, the momentum/space/time handlers with their distribution events, and
-// UpdateAllBoundaries. A boundary that was not crossed is recorded right after it is computed
-// (RecordBoundary only copies delta to delta_old for it); crossed ones after their events.
+// The crossed part of HandleBoundaries: momentum, then spatial, then time boundaries, each class
+// with the distribution events of its last crossed boundary, then RecordBoundary of the crossed.
 template <int TT, class R, class A>
-__device__ void handle_boundaries(Lane<R, A>& L, BndState<R>* bs, const SD<R>& sp, const Start& s0,
-                                  const ProblemDescT<R>& P, const ProblemDesc& Pd, const Sinks& S)
+__device__ __forceinline__ void handle_crossings(Lane<R, A>& L, BndView<R> bv, const SD<R>& sp, const Start& s0,
+                                                 const ProblemDescT<R>& P, const ProblemDesc& Pd, const Sinks& S,
+                                                 unsigned crossed)
 {
    V3<R> pos = val3<R>(L.pos), mom = lane_mom(L);
    const int nb = P.nbt + P.nbs + P.nbm;
-   unsigned crossed = 0;
-   for (int j = 0; j < nb; j++) {
-      compute_bnd(bnd_param(P, j), bs[j], L.t, pos, mom, sp.bhat, sp.region, TT);
-      if (bs[j].crossed) crossed |= 1u << j;
-      else bs[j].delta_old = bs[j].delta;
-   }
-   if (!crossed) return;
    const int s_lo = P.nbt, m_lo = P.nbt + P.nbs;
    // momentum boundaries
    int active = -1;
    for (int j = m_lo; j < nb; j++) {
       if (!(crossed & (1u << j))) continue;
       active = j;
-      if (!bnd_param(P, j).reflect && bs[j].crossings_left == 1) L.status |= TRAJ_MOMENTUM_CROSSED | TRAJ_FINISH;
+      if (!bnd_param(P, j).reflect && bv.ld(j).crossings_left == 1) L.status |= TRAJ_MOMENTUM_CROSSED | TRAJ_FINISH;
    }
    if (active >= 0) distro_events<TT>(L, sp, s0, Pd, active, S);
    // spatial boundaries
@@ -367,19 +359,21 @@ __device__ void handle_boundaries(Lane<R, A>& L, BndState<R>* bs, const SD<R>& s
       if (!(crossed & (1u << j))) continue;
       active = j;
       const BndParamsT<R>& b = bnd_param(P, j);
+      BndState<R> st = bv.ld(j);
       if (b.reflect) {
          // src/trajectory_base.cc:462-483: mirror the position, reverse the momentum
-         V3<R> shift = (R(2) * bs[j].delta) * bnd_normal(b, pos);
+         V3<R> shift = (R(2) * st.delta) * bnd_normal(b, pos);
          add3(L.pos, R(-1) * shift);
          if (TT != kParker && TT != kParkerSource) {
             L.mom.x = neg(L.mom.x); L.mom.y = neg(L.mom.y); L.mom.z = neg(L.mom.z);
          }
          pos = val3<R>(L.pos);
          mom = lane_mom(L);
-         compute_bnd(b, bs[j], L.t, pos, mom, sp.bhat, sp.region, TT);
-         bs[j].crossings_left--;
+         compute_bnd(b, st, L.t, pos, mom, sp.bhat, sp.region, TT);
+         st.crossings_left--;
+         bv.st(j, st);
       }
-      else if (bs[j].crossings_left == 1) L.status |= TRAJ_SPATIAL_CROSSED | TRAJ_FINISH;
+      else if (st.crossings_left == 1) L.status |= TRAJ_SPATIAL_CROSSED | TRAJ_FINISH;
    }
    if (active >= 0) distro_events<TT>(L, sp, s0, Pd, active, S);
    // time boundaries
@@ -387,22 +381,50 @@ __device__ void handle_boundaries(Lane<R, A>& L, BndState<R>* bs, const SD<R>& s
    for (int j = 0; j < s_lo; j++) {
       if (!(crossed & (1u << j))) continue;
       active = j;
-      if (bs[j].crossings_left == 1) L.status |= TRAJ_TIME_CROSSED | TRAJ_FINISH;
+      if (bv.ld(j).crossings_left == 1) L.status |= TRAJ_TIME_CROSSED | TRAJ_FINISH;
    }
    if (active >= 0) distro_events<TT>(L, sp, s0, Pd, active, S);
    for (int j = 0; j < nb; j++)
-      if (crossed & (1u << j)) record_bnd(bnd_param(P, j), bs[j], L.t, pos, mom, sp.bhat, sp.region, TT);
+      if (crossed & (1u << j)) {
+         BndState<R> st = bv.ld(j);
+         record_bnd(bnd_param(P, j), st, L.t, pos, mom, sp.bhat, sp.region, TT);
+         bv.st(j, st);
+      }
+}
+
+// ---- HandleBoundaries (src/trajectory_base.cc:413-535) ---------------------------------------
+// ComputeAllBoundaries, the momentum/space/time handlers with their distribution events, and
+// UpdateAllBoundaries. A boundary that was not crossed is recorded right after it is computed
+// (RecordBoundary only copies delta to delta_old for it); crossed ones after their events.
+template <int TT, class R, class A>
+__device__ __forceinline__ void handle_boundaries(Lane<R, A>& L, BndView<R> bv, const SD<R>& sp, const Start& s0,
+                                                  const ProblemDescT<R>& P, const ProblemDesc& Pd, const Sinks& S)
+{
+   V3<R> pos = val3<R>(L.pos), mom = lane_mom(L);
+   const int nb = P.nbt + P.nbs + P.nbm;
+   unsigned crossed = 0;
+   for (int j = 0; j < nb; j++) {
+      BndState<R> b = bv.ld(j);
+      compute_bnd(bnd_param(P, j), b, L.t, pos, mom, sp.bhat, sp.region, TT);
+      if (b.crossed) crossed |= 1u << j;
+      else b.delta_old = b.delta;
+      bv.st(j, b);
+   }
+   if (!crossed) return;
+   handle_crossings<TT>(L, bv, sp, s0, P, Pd, S, crossed);
 }
 
 // SpaceTerminateCheck (src/trajectory_base.cc:188-237); true if the trajectory ended mid-step
 template <int TT, class R, class A>
-__device__ bool space_terminate(Lane<R, A>& L, BndState<R>* bs, const SD<R>& sp, const Start& s0,
-                                const ProblemDescT<R>& P, const ProblemDesc& Pd, const Sinks& S)
+__device__ __forceinline__ bool space_terminate(Lane<R, A>& L, BndView<R> bv, const SD<R>& sp, const Start& s0,
+                                                const ProblemDescT<R>& P, const ProblemDesc& Pd, const Sinks& S)
 {
    V3<R> pos = val3<R>(L.pos), mom = lane_mom(L);
    for (int j = P.nbt; j < P.nbt + P.nbs; j++) {
-      compute_bnd(bnd_param(P, j), bs[j], L.t, pos, mom, sp.bhat, sp.region, TT);
-      if (bs[j].crossed && bs[j].crossings_left == 1) {
+      BndState<R> b = bv.ld(j);
+      compute_bnd(bnd_param(P, j), b, L.t, pos, mom, sp.bhat, sp.region, TT);
+      bv.st(j, b);
+      if (b.crossed && b.crossings_left == 1) {
          L.status |= TRAJ_SPATIAL_CROSSED | TRAJ_FINISH;
          distro_events<TT>(L, sp, s0, Pd, j, S);
          L.steps++;
@@ -414,12 +436,12 @@ __device__ bool space_terminate(Lane<R, A>& L, BndState<R>* bs, const SD<R>& sp,
 
 // TimeBoundaryProximityCheck (src/trajectory_base.cc:151-179)
 template <class R>
-__device__ __forceinline__ R time_proximity(R dt, R dmax, const BndState<R>* bs, int nbt, bool fwd)
+__device__ __forceinline__ R time_proximity(R dt, R dmax, BndView<R> bv, int nbt, bool fwd)
 {
    R c = c_code<R>();
    R dn = fwd ? -Lim<R>::large * dmax / c : Lim<R>::large * dmax / c;
    for (int b = 0; b < nbt; b++) {
-      R delta = bs[b].delta;
+      R delta = bv.ld(b).delta;
       if (fwd) { if (delta <= R(0) && delta > dn) dn = delta; }
       else { if (delta >= R(0) && delta < dn) dn = delta; }
    }
@@ -442,10 +464,10 @@ __device__ __noinline__ bool parker_divk_fd(const ProblemDescT<R>& P, int deriv_
       R pt[3] = {pos.x, pos.y, pos.z};
       pt[j] = pt[j] + delta;
       if (!get_fields<BG>(P.bg, deriv_mode, t, mk(pt[0], pt[1], pt[2]), p, kU | kB, sf)) return false;
-      Kap<R> kf = kappa_pp(P.df, mk(pt[0], pt[1], pt[2]), p, vmag, sf);
+      Kap<R> kf = kappa_pp(P.df, mk(pt[0], pt[1], pt[2]), p, vmag, kap_in(sf));
       pt[j] -= R(2) * delta;
       if (!get_fields<BG>(P.bg, deriv_mode, t, mk(pt[0], pt[1], pt[2]), p, kU | kB, sb)) return false;
-      Kap<R> kb = kappa_pp(P.df, mk(pt[0], pt[1], pt[2]), p, vmag, sb);
+      Kap<R> kb = kappa_pp(P.df, mk(pt[0], pt[1], pt[2]), p, vmag, kap_in(sb));
       for (int i = 0; i < 3; i++) {
          R f = kf.perp * (i == j ? R(1) : R(0)) + (kf.para - kf.perp) * sf.bhat[j] * sf.bhat[i];
          R b = kb.perp * (i == j ? R(1) : R(0)) + (kb.para - kb.perp) * sb.bhat[j] * sb.bhat[i];
@@ -457,7 +479,7 @@ __device__ __noinline__ bool parker_divk_fd(const ProblemDescT<R>& P, int deriv_
 }
 
 template <int BG, class R, class A>
-__device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndState<R>* bs, const Start& s0,
+__device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, const Start& s0,
                                                const ProblemDescT<R>& P, const ProblemDesc& Pd, const RunConfig& cfg,
                                                const Sinks& S)
 {
@@ -472,7 +494,7 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndState<R>* bs, c
    if (!get_fields<BG>(P.bg, deriv_mode, t, pos, p, mask, sp)) { L.status |= TRAJ_DISCARD; return; }
    R vmag = vel_of(p);
    // DiffusionCoeff (src/trajectory_parker.cc:83-153)
-   Kap<R> K = kappa_pp(P.df, pos, p, vmag, sp);
+   Kap<R> K = kappa_pp(P.df, pos, p, vmag, kap_in(sp));
    V3<R> divK;
    if (kFP64 && deriv_mode == 0) {
       if (!parker_divk_fd<BG>(P, deriv_mode, t, pos, p, vmag, sp, divK)) { L.status |= TRAJ_DISCARD; return; }
@@ -499,7 +521,7 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndState<R>* bs, c
    R dtp = R(0.5) * sp.dmax / norm(slope);
    dtp = m_min(dtp, R(0.5) * (sp.dmax * sp.dmax) / m_max(K.perp, K.para));
    dtp = m_min(dtp, R(0.5) * R(3) * R(0.01) / m_abs(divU));
-   L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bs, P.nbt, fwd);
+   L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bv, P.nbt, fwd);
    // EulerDiffSlopes (src/trajectory_parker.cc:159-180)
    R n[4];
    normals4<R>(rng_block(P.seed, L.steps, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
@@ -539,7 +561,7 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndState<R>* bs, c
       }
    }
    if (sa != R(0)) L.amp += dts * sa * m_exp(L.wgt);
-   handle_boundaries<kParker>(L, bs, sp, s0, P, Pd, S);
+   handle_boundaries<kParker>(L, bv, sp, s0, P, Pd, S);
    // the end point's dmax for the time-step check of Integrate
    L.steps++;
    if (!(L.status & TRAJ_FINISH)) {
@@ -609,7 +631,7 @@ __device__ __forceinline__ void clamp_mu(AV3<A>& mom)
 }
 
 template <int TT, int BG, class R, class A, int STAGES>
-__device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndState<R>* bs, const Start& s0, const ProblemDescT<R>& P,
+__device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const Start& s0, const ProblemDescT<R>& P,
                                            const ProblemDesc& Pd, const RunConfig& cfg, const Sinks& S)
 {
    constexpr bool kFP64 = sizeof(R) == sizeof(double);
@@ -638,7 +660,7 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndState<R>* bs, const
       R dmumax = m_sqrt(R(1) - amu) * dth + R(0.5) * amu * (dth * dth);
       dtp = m_min(dtp, R(0.5) * (dmumax * dmumax) / Dmumu);
       dtp = m_min(dtp, R(0.5) * dmumax / m_abs(Vmu));
-      L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bs, P.nbt, fwd);
+      L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bv, P.nbt, fwd);
       R n[4];
       normals4<R>(rng_block(P.seed, L.steps, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
       R sq = m_sqrt(R(2) * Dmumu * L.dt);
@@ -673,7 +695,7 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndState<R>* bs, const
       else {  // src/trajectory_focused.cc:87-91
          dtp = R(0.5) * sp.dmax / (norm(drift) + R(0.5) * vel.x);
       }
-      L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bs, P.nbt, fwd);
+      L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bv, P.nbt, fwd);
    }
    // RKSlopes
 #pragma unroll
@@ -685,7 +707,7 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndState<R>* bs, const
          if (fwd) { acc_add(L.t, dta); add3(L.pos, ds * slp[il]); add3(L.mom, ds * slm[il]); }
          else { acc_add(L.t, -dta); add3(L.pos, R(-1) * (ds * slp[il])); add3(L.mom, R(-1) * (ds * slm[il])); }
       }
-      if (space_terminate<TT>(L, bs, sp, s0, P, Pd, S)) return;
+      if (space_terminate<TT>(L, bv, sp, s0, P, Pd, S)) return;
       V3<R> ms = lane_mom(L);
       if (!get_fields<BG>(P.bg, deriv_mode, (R)acc_val(L.t), val3<R>(L.pos), field_p<TT>(ms), traj_mask<TT>(), sp)) {
          L.status |= TRAJ_DISCARD;
@@ -721,7 +743,7 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndState<R>* bs, const
       add3(L.pos, sdt * dp);
       add3(L.mom, sdt * dm);
    }
-   handle_boundaries<TT>(L, bs, sp, s0, P, Pd, S);
+   handle_boundaries<TT>(L, bv, sp, s0, P, Pd, S);
    if (!(L.status & TRAJ_FINISH) && TT == kFocused) clamp_mu<A, R>(L.mom);
    L.steps++;
    if (!(L.status & TRAJ_FINISH)) {
@@ -731,8 +753,9 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndState<R>* bs, const
 }
 
 // ---- SetStart (src/trajectory_base.cc:867-939 and overrides) -------------------------------
+// Works on a lane record of its own (see start_lane) and writes the boundary states of the lane.
 template <int TT, int BG, class R, class A>
-__device__ __noinline__ void set_start(Lane<R, A>& L, BndState<R>* bs, Start& s0, const ProblemDescT<R>& P,
+__device__ __noinline__ void set_start(Lane<R, A>& L, BndView<R> bv, Start& s0, const ProblemDescT<R>& P,
                                        const ProblemDesc& Pd, const RunConfig& cfg, int64_t local)
 {
    constexpr bool kFP64 = sizeof(R) == sizeof(double);
@@ -742,12 +765,15 @@ __device__ __noinline__ void set_start(Lane<R, A>& L, BndState<R>* bs, Start& s0
    L.amp = R(0);
    L.wgt = R(0);
    L.dt = R(0);
+   L.dt_adapt = R(0);
+   L.src_del_old = R(0);
    InitRng rng{Pd.seed, L.traj_id, Pd.problem_id, L.attempt, 0u, 0u};
    double t = sample_time(rng, Pd, local);
    V3<double> pos = sample_pos(rng, Pd, local);
    V3<double> mom = sample_mom(rng, Pd, TT, mk(1.0, 1.0, 1.0));
    acc_set(L.t, t);
    acc_set(L.pos.x, pos.x); acc_set(L.pos.y, pos.y); acc_set(L.pos.z, pos.z);
+   acc_set(L.mom.x, mom.x); acc_set(L.mom.y, mom.y); acc_set(L.mom.z, mom.z);
    SD<R> sp;
    V3<R> pr = val3<R>(L.pos);
    R pm = TT == kLorentz ? (R)norm(mom) : (R)mom.x;
@@ -764,7 +790,9 @@ __device__ __noinline__ void set_start(Lane<R, A>& L, BndState<R>* bs, Start& s0
    V3<R> mr = lane_mom(L);
    for (int j = 0; j < P.nbt + P.nbs + P.nbm; j++) {
       R scale = j < P.nbt ? sp.dmax / c : (j < P.nbt + P.nbs ? sp.dmax : norm(mr));
-      reset_bnd(bnd_param(P, j), bs[j], scale, L.t, pr, mr, sp.bhat, sp.region, TT);
+      BndState<R> st;
+      reset_bnd(bnd_param(P, j), st, scale, L.t, pr, mr, sp.bhat, sp.region, TT);
+      bv.st(j, st);
    }
    // TrajectoryParkerSource::SetStart (src/trajectory_parker_source.cc:43-50)
    if (P.src.kind == 2) L.src_del_old = mr.x - P.src.p_inj;
@@ -783,8 +811,9 @@ __device__ __forceinline__ int find_problem(const ProblemDescT<R>* P, int n, int
    return lo;
 }
 
+// Takes the lane state by value so that the caller's copy stays in registers.
 template <class R, class A>
-__device__ __noinline__ void write_record(const Lane<R, A>& L, const Start& s0, TrajRecord* rec, int64_t g)
+__device__ __noinline__ void write_record(const Lane<R, A> L, const Start& s0, TrajRecord* rec, int64_t g)
 {
    TrajRecord r;
    r.attempts = L.attempt + 1;
@@ -801,44 +830,58 @@ __device__ __noinline__ void write_record(const Lane<R, A>& L, const Start& s0, 
    rec[g] = r;
 }
 
-// Start trajectory g on the lane.
+// Start (or restart, with a new attempt number) trajectory g on the lane. SetStart fills a
+// separate record that is then copied member by member: the lane state proper is never passed by
+// address to an out-of-line call, so it lives in registers for the whole kernel.
 template <int TT, int BG, class R, class A>
-__device__ __forceinline__ void start_lane(Lane<R, A>& L, BndState<R>* bs, Start& s0, const ProblemDescT<R>* P,
+__device__ __forceinline__ void start_lane(Lane<R, A>& L, BndView<R> bv, Start& s0, const ProblemDescT<R>* P,
                                            const ProblemDesc* Pd, const RunConfig& cfg, int64_t g, uint32_t attempt)
 {
-   L.prob = find_problem(P, cfg.n_problems, g);
-   int64_t local = g - P[L.prob].first;
-   L.traj_id = (uint32_t)(cfg.run_index * P[L.prob].n_traj + local);
-   L.attempt = attempt;
-   set_start<TT, BG>(L, bs, s0, P[L.prob], Pd[L.prob], cfg, local);
+   Lane<R, A> n;
+   n.prob = find_problem(P, cfg.n_problems, g);
+   int64_t local = g - P[n.prob].first;
+   n.traj_id = (uint32_t)(cfg.run_index * P[n.prob].n_traj + local);
+   n.attempt = attempt;
+   set_start<TT, BG>(n, bv, s0, P[n.prob], Pd[n.prob], cfg, local);
+   L.prob = n.prob; L.traj_id = n.traj_id; L.attempt = n.attempt; L.steps = n.steps; L.status = n.status;
+   L.t = n.t;
+   L.pos.x = n.pos.x; L.pos.y = n.pos.y; L.pos.z = n.pos.z;
+   L.mom.x = n.mom.x; L.mom.y = n.mom.y; L.mom.z = n.mom.z;
+   L.amp = n.amp; L.wgt = n.wgt; L.dt = n.dt; L.dt_adapt = n.dt_adapt; L.src_del_old = n.src_del_old;
 }
 
 // Resident blocks of 128 threads per SM the register allocation is sized for.
 #ifndef SPX_MIN_BLOCKS_F32
-#define SPX_MIN_BLOCKS_F32 1
+#define SPX_MIN_BLOCKS_F32 4
 #endif
 #ifndef SPX_MIN_BLOCKS_F64
 #define SPX_MIN_BLOCKS_F64 1
 #endif
 
+// One lane per thread. Dynamic shared memory holds the lanes' boundary states
+// (boundaries per lane x blockDim.x x sizeof(BndState<R>)).
 template <int TT, int BG, class R>
-__global__ void __launch_bounds__(128, sizeof(R) == 4 ? SPX_MIN_BLOCKS_F32 : SPX_MIN_BLOCKS_F64) step_kernel(const ProblemDescT<R>* __restrict__ P, const ProblemDesc* __restrict__ Pd,
-                                                   RunConfig cfg, RunCounters* ctr, int32_t* counts, double* sums,
-                                                   unsigned long long* n_events, TrajRecord* rec, int queue)
+__global__ void __launch_bounds__(128, sizeof(R) == 4 ? SPX_MIN_BLOCKS_F32 : SPX_MIN_BLOCKS_F64)
+step_kernel(const ProblemDescT<R>* __restrict__ P, const ProblemDesc* __restrict__ Pd, RunConfig cfg,
+            RunCounters* ctr, int32_t* counts, double* sums, unsigned long long* n_events, TrajRecord* rec, int queue)
 {
    using A = typename AccOf<R>::type;
+   extern __shared__ __align__(16) unsigned char spx_smem[];
+   const BndView<R> bv{reinterpret_cast<BndState<R>*>(spx_smem) + threadIdx.x, (int)blockDim.x};
    Sinks S{counts, sums, n_events, ctr};
    Lane<R, A> L;
-   BndState<R> bs[kMaxBndTotal];
    Start s0;
    int64_t g = -1;
-   bool active = false;
-   unsigned long long my_steps = 0, my_retries = 0, my_given_up = 0, my_done = 0;
+   bool active = false;  // the lane holds trajectory g
+   bool fresh = false;   // trajectory g is to be (re)started with attempt number "attempt"
+   uint32_t attempt = 0;
+   unsigned long long my_steps = 0;
+   unsigned my_retries = 0, my_given_up = 0, my_done = 0;
    const int64_t total = cfg.total_traj;
    const int64_t stride = (int64_t)gridDim.x * blockDim.x;
    if (!queue) {
       g = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-      if (g < total) { start_lane<TT, BG>(L, bs, s0, P, Pd, cfg, g, 0u); active = true; }
+      if (g < total) { active = true; fresh = true; }
    }
    const int K = cfg.steps_per_sync > 0 ? cfg.steps_per_sync : 1;
    while (true) {
@@ -853,13 +896,18 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? SPX_MIN_BLOCKS_F32 : SPX
             base = __shfl_sync(0xffffffffu, base, leader);
             if (!active) {
                int64_t mine = (int64_t)base + __popc(idle & ((1u << lane) - 1u));
-               if (mine < total) { g = mine; start_lane<TT, BG>(L, bs, s0, P, Pd, cfg, g, 0u); active = true; }
+               if (mine < total) { g = mine; active = true; fresh = true; attempt = 0; }
             }
          }
          if (!__any_sync(0xffffffffu, active)) break;
       }
       else if (!active) break;
       for (int k = 0; k < K && active; k++) {
+         if (fresh) {
+            start_lane<TT, BG>(L, bv, s0, P, Pd, cfg, g, attempt);
+            fresh = false;
+            continue;
+         }
          bool done = false;
          if (L.status & TRAJ_DISCARD) {
             // discarded attempt: redo the trajectory with a fresh random stream (src/simulation.cc:262-288)
@@ -870,15 +918,16 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? SPX_MIN_BLOCKS_F32 : SPX
             }
             else {
                my_retries++;
-               start_lane<TT, BG>(L, bs, s0, P, Pd, cfg, g, L.attempt + 1);
+               attempt = L.attempt + 1;
+               fresh = true;
                continue;
             }
          }
          else {
             const ProblemDescT<R>& Pp = P[L.prob];
-            if (TT == kParker) parker_advance<BG>(L, bs, s0, Pp, Pd[L.prob], cfg, S);
-            else if (cfg.rk == 25) rk_advance<TT, BG, R, A, 4>(L, bs, s0, Pp, Pd[L.prob], cfg, S);
-            else rk_advance<TT, BG, R, A, 1>(L, bs, s0, Pp, Pd[L.prob], cfg, S);
+            if (TT == kParker) parker_advance<BG>(L, bv, s0, Pp, Pd[L.prob], cfg, S);
+            else if (cfg.rk == 25) rk_advance<TT, BG, R, A, 4>(L, bv, s0, Pp, Pd[L.prob], cfg, S);
+            else rk_advance<TT, BG, R, A, 1>(L, bv, s0, Pp, Pd[L.prob], cfg, S);
             // Integrate's safety limits (src/trajectory_base.cc:964-992)
             if (L.steps > kMaxTrajSteps || !isfinite(L.dt) || L.dt == R(0)) L.status |= TRAJ_DISCARD;
             done = (L.status & TRAJ_FINISH) && !(L.status & TRAJ_DISCARD);
@@ -890,7 +939,7 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? SPX_MIN_BLOCKS_F32 : SPX
             active = false;
             if (!queue) {
                g += stride;
-               if (g < total) { start_lane<TT, BG>(L, bs, s0, P, Pd, cfg, g, 0u); active = true; }
+               if (g < total) { active = true; fresh = true; attempt = 0; }
             }
          }
       }
@@ -904,9 +953,9 @@ __global__ void __launch_bounds__(128, sizeof(R) == 4 ? SPX_MIN_BLOCKS_F32 : SPX
    }
    if ((threadIdx.x & 31) == 0) {
       atomicAdd(&ctr->steps, my_steps);
-      if (my_retries) atomicAdd(&ctr->retries, my_retries);
-      if (my_given_up) atomicAdd(&ctr->given_up, my_given_up);
-      atomicAdd(&ctr->finished, my_done);
+      if (my_retries) atomicAdd(&ctr->retries, (unsigned long long)my_retries);
+      if (my_given_up) atomicAdd(&ctr->given_up, (unsigned long long)my_given_up);
+      atomicAdd(&ctr->finished, (unsigned long long)my_done);
    }
 }
 

@@ -1,0 +1,121 @@
+"""Generate the golden fixtures of this directory from the reference's own code.
+
+Each fixture holds one problem spec (the exact bytes the reference harness and the oracle read),
+the options the comparison needs, and the reference's output for it: per-trajectory final states
+and the distributions (stored sparse). The outputs come from oracle/_ref/ref_* -- the reference's
+trajectory, background, diffusion, boundary, initial and distribution sources compiled
+unchanged with the Philox stand-in for GSL (oracle/Makefile, target "ref"). The reference
+sources must be present to run this script; the fixtures it writes are then used everywhere,
+including where the sources are not.
+
+    python tests/golden/make_golden.py          # rewrites tests/golden/*.npz
+"""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+from spectrum_gb300 import workloads  # noqa: E402
+from spectrum_gb300.workloads import SPX_OPT_PA_SCATTERING, SPX_OPT_STEPS_PER_ORBIT  # noqa: E402
+
+
+def _dipole_reference_classes(n_traj: int):
+    """The dipole workload's background and boundaries with initial conditions the reference
+    itself provides (a fixed point at L = 4 on the equator, an isotropic 10 MeV shell)."""
+    from spectrum_gb300 import units as U
+    from spectrum_gb300.datacontainer import DataContainer as DC
+    from spectrum_gb300.plugins import InitialMomentumShell, InitialSpaceFixed, InitialTimeFixed
+    from spectrum_gb300.problem import Problem
+    src = workloads.dipole_orbits(n_traj=n_traj, t_end=0.5 / U.unit_time)
+    pb = Problem(traj=src.traj, time_flow=src.time_flow, rk=src.rk, seed=src.seed, n_traj=n_traj)
+    r_e = workloads.R_EARTH_CM / U.unit_length
+    for e in src.plugins:
+        name = type(e.plugin).__name__
+        if name.startswith("Initial"):
+            continue
+        pb.plugins.append(e)
+    pb.AddInitial(InitialTimeFixed(), DC().double(0.0))
+    pb.AddInitial(InitialSpaceFixed(), DC().vec((4.0 * r_e, 0.0, 0.0)))
+    pb.AddInitial(InitialMomentumShell(), DC().double(U.mev_to_mom(10.0)))
+    return pb
+
+
+def _focused_reference_classes(n_traj: int):
+    """Focused transport in the Parker spiral without scattering, recorded with the reference's
+    own distribution and boundary classes (time-of-exit histogram at the 1 AU absorber)."""
+    from spectrum_gb300 import units as U
+    from spectrum_gb300.datacontainer import DataContainer as DC
+    from spectrum_gb300.plugins import (BackgroundSolarWind, BoundarySphereAbsorb, BoundaryTimeExpire,
+                                        DiffusionIsotropicConstant, DistributionTimeUniform, InitialMomentumShell,
+                                        InitialSpaceFixed, InitialTimeFixed)
+    from spectrum_gb300.problem import FORWARD, TRAJ_FOCUSED, Problem, distro_header
+    au = workloads.ONE_AU
+    t_max = 3600.0 / U.unit_time
+    pb = Problem(traj=TRAJ_FOCUSED, time_flow=FORWARD, rk=25, seed=workloads.SEED_BASE + 5, n_traj=n_traj)
+    pb.AddBackground(BackgroundSolarWind(), workloads.solarwind_params(DC()))
+    pb.AddInitial(InitialTimeFixed(), DC().double(0.0))
+    pb.AddInitial(InitialSpaceFixed(), DC().vec((0.1 * au, 0, 0)))
+    pb.AddInitial(InitialMomentumShell(), DC().double(U.mev_to_mom(10.0)))
+    pb.AddDiffusion(DiffusionIsotropicConstant(), DC().double(1.0e-3))
+    pb.AddBoundary(BoundaryTimeExpire(), workloads._boundary(DC(), 1, [-1]).double(t_max))
+    pb.AddBoundary(BoundarySphereAbsorb(), workloads._boundary(DC(), 1, [0]).vec((0, 0, 0)).double(0.05 * au))
+    pb.AddBoundary(BoundarySphereAbsorb(), workloads._boundary(DC(), 1, [0]).vec((0, 0, 0)).double(1.0 * au))
+    c = distro_header(DC(), (32, 0, 0), (0.0, 0, 0), (t_max, 0, 0), bin_outside=(1, 0, 0),
+                      unit_val=(U.unit_time, 1.0, 1.0))
+    c.double(1.0).double(0.0).int(1)
+    pb.AddDistribution(DistributionTimeUniform(), c)
+    return pb
+
+
+def cases():
+    """(name, problem) pairs, each small enough for the oracle to finish in seconds."""
+    out = []
+    out.append(("parker_fwd_uniform", workloads.diffusion_uniform(n_traj=200)))
+    dsa = workloads.shock_acceleration(n_traj=12, x_escape=-2.0, x_downstream=2.0, p_max=20.0)
+    out.append(("parker_fwd_smoothshock", dsa))
+    for k, pb in enumerate(workloads.gcr_modulation(n_traj=6, energies_mev=[30.0, 3000.0], t_max_years=0.05)):
+        out.append((f"parker_bwd_solarwind_{k}", pb))
+    out.append(("lorentz_fwd_dipole", _dipole_reference_classes(6)))
+    out.append(("focused_fwd_solarwind", _focused_reference_classes(6)))
+    return out
+
+
+def sparse(distros):
+    out = {}
+    for d, (counts, sums, nev) in enumerate(distros):
+        nz = np.nonzero(counts)[0]
+        out[f"d{d}_n_bins"] = np.int64(len(counts))
+        out[f"d{d}_width"] = np.int64(sums.shape[1])
+        out[f"d{d}_idx"] = nz.astype(np.int64)
+        out[f"d{d}_counts"] = counts[nz].astype(np.int32)
+        out[f"d{d}_sums"] = sums[nz].astype(np.float64)
+        out[f"d{d}_n_events"] = np.int64(nev)
+    out["n_distros"] = np.int64(len(distros))
+    return out
+
+
+def main():
+    import oracle_tools as ot
+    for name, pb in cases():
+        ref = ot.run_reference(pb)
+        fx = {"spec": np.frombuffer(pb.to_spec(), dtype=np.uint8), "traj": ref.traj,
+              "traj_kind": np.int64(pb.traj), "time_flow": np.int64(pb.time_flow), "rk": np.int64(pb.rk),
+              "steps_per_orbit": np.float64(pb.options.get(SPX_OPT_STEPS_PER_ORBIT, 100.0)),
+              "pa_scattering": np.int64(pb.options.get(SPX_OPT_PA_SCATTERING, 0)),
+              "n_traj": np.int64(pb.n_traj)}
+        fx.update(sparse(ref.distros))
+        path = os.path.join(HERE, name + ".npz")
+        np.savez_compressed(path, **fx)
+        print(f"{name}: {len(ref.traj)} trajectories, {int(ref.traj['steps'].sum())} steps, "
+              f"{os.path.getsize(path)} bytes")
+
+
+if __name__ == "__main__":
+    main()

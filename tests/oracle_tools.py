@@ -70,14 +70,21 @@ def run_oracle(problem, first: int = 0, n: int | None = None, deriv_mode: int = 
                pa_scattering: int | None = None, max_attempts: int = 100, record: bool = True) -> OracleResult:
     """Run the C restatement on ``problem`` (a spectrum_gb300.problem.Problem)."""
     from spectrum_gb300.workloads import SPX_OPT_PA_SCATTERING, SPX_OPT_STEPS_PER_ORBIT
-    spec = problem.to_spec()
-    n = problem.n_traj if n is None else n
     if steps_per_orbit is None:
         steps_per_orbit = problem.options.get(SPX_OPT_STEPS_PER_ORBIT, 100.0)
     if pa_scattering is None:
         pa_scattering = int(problem.options.get(SPX_OPT_PA_SCATTERING, 0))
-    opts = _Opts(problem.traj, problem.time_flow, problem.rk, deriv_mode, float(steps_per_orbit), pa_scattering,
-                 max_attempts)
+    return run_oracle_spec(problem.to_spec(), problem.traj, problem.time_flow, problem.rk,
+                           problem.n_traj if n is None else n, first=first, deriv_mode=deriv_mode,
+                           steps_per_orbit=steps_per_orbit, pa_scattering=pa_scattering, max_attempts=max_attempts,
+                           record=record)
+
+
+def run_oracle_spec(spec: bytes, traj_kind: int, time_flow: int, rk: int, n: int, first: int = 0, deriv_mode: int = 0,
+                    steps_per_orbit: float = 100.0, pa_scattering: int = 0, max_attempts: int = 100,
+                    record: bool = True) -> OracleResult:
+    """Run the C restatement on a problem spec (the bytes Problem.to_spec() makes)."""
+    opts = _Opts(traj_kind, time_flow, rk, deriv_mode, float(steps_per_orbit), int(pa_scattering), max_attempts)
     sizes = distro_sizes(spec)
     tot = sum(s for s, _ in sizes)
     counts = np.zeros(max(tot, 1), dtype=np.int32)
@@ -99,6 +106,42 @@ def run_oracle(problem, first: int = 0, n: int | None = None, deriv_mode: int = 
         off += nb
         soff += nb * w
     return OracleResult(traj, distros)
+
+
+def philox(ctr, key):
+    """Philox4x32-10 of one counter (4 words) under one key (2 words), from the oracle library."""
+    out = (ctypes.c_uint32 * 4)()
+    lib().spx_oracle_philox((ctypes.c_uint32 * 4)(*ctr), (ctypes.c_uint32 * 2)(*key), out)
+    return [int(x) for x in out]
+
+
+# -- golden fixtures (tests/golden, written by tests/golden/make_golden.py) ----------------------
+GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def golden_names():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz"))
+
+
+def load_golden(name: str):
+    """(fixture dict, OracleResult of the reference's output) for one fixture."""
+    fx = dict(np.load(os.path.join(GOLDEN_DIR, name + ".npz")))
+    distros = []
+    for d in range(int(fx["n_distros"])):
+        nb, w = int(fx[f"d{d}_n_bins"]), int(fx[f"d{d}_width"])
+        counts = np.zeros(nb, dtype=np.int32)
+        sums = np.zeros((nb, w), dtype=np.float64)
+        idx = fx[f"d{d}_idx"]
+        counts[idx] = fx[f"d{d}_counts"]
+        sums[idx] = fx[f"d{d}_sums"]
+        distros.append((counts, sums, int(fx[f"d{d}_n_events"])))
+    return fx, OracleResult(fx["traj"], distros)
+
+
+def run_oracle_golden(fx, deriv_mode: int = 0) -> OracleResult:
+    return run_oracle_spec(fx["spec"].tobytes(), int(fx["traj_kind"]), int(fx["time_flow"]), int(fx["rk"]),
+                           int(fx["n_traj"]), deriv_mode=deriv_mode, steps_per_orbit=float(fx["steps_per_orbit"]),
+                           pa_scattering=int(fx["pa_scattering"]))
 
 
 def oracle_normals(seed, index, traj, problem=0, attempt=0):
