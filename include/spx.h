@@ -132,6 +132,32 @@ int spx_run(spx_ctx_t ctx, const spx_tuning* tuning);
 /* Wait for the last spx_run and report its statistics (stats may be NULL). */
 int spx_sync(spx_ctx_t ctx, spx_stats* stats);
 
+/* Size of the fixed device array spx_run_static works in (every GPU that loads the library holds
+ * it until the process exits): 46 problems in SPX_MIXED, 72 in SPX_FP64. */
+#define SPX_STATIC_SCRATCH_BYTES (512u * 1024u)
+
+/* spx_run without any device allocation. No counterpart in the reference: it is for callers that
+ * cannot call cudaMalloc -- code running inside a host framework that owns all device memory
+ * through its own pool, or on a latency-critical path where cudaMalloc's implicit device
+ * synchronisation is not acceptable. The caller passes device buffers for the outputs, laid out
+ * as one array over all (problem, distribution) pairs in order, each as spx_get_distribution_info
+ * sizes it: int32 counts[n_counts], double sums[n_sums], and n_events[problem * 4 + distribution]
+ * (n_events_len >= 4 * problems); the kernel adds into them, so the caller zeroes them first.
+ * With SPX_OPT_RECORD_FINAL set, records[n_records] (device memory, one per trajectory over all
+ * problems in order) receives the final states. The run counters and the device copies of the
+ * problem descriptors live in a fixed array of SPX_STATIC_SCRATCH_BYTES; a context whose
+ * descriptors do not fit is rejected with SPX_ERR_TOO_LARGE. The call allocates no device memory
+ * (no cudaMalloc, cudaFree or allocating library routine); it blocks until the launch is done
+ * and fills stats (may be NULL). The first call on a device looks up the array's address there
+ * (and may load the library's device code), so make it before any stream capture. All calls share
+ * the array and it keeps the last call's contents (each call clears the counters it needs):
+ * calls whose launches overlap on the GPU race and give wrong results. Trajectory ids continue
+ * from spx_run's, so a sequence of spx_run_static calls draws the same trajectories as the same
+ * sequence of spx_run calls; spx_sync reports spx_run launches only. */
+int spx_run_static(spx_ctx_t ctx, const spx_tuning* tuning, int32_t* counts, int64_t n_counts, double* sums,
+                   int64_t n_sums, unsigned long long* n_events, int64_t n_events_len, spx_traj_record* records,
+                   int64_t n_records, spx_stats* stats);
+
 /* Shape of a distribution: number of bins and doubles per bin (1, 3 or 9). */
 int spx_get_distribution_info(spx_ctx_t ctx, int problem, int distro, int64_t* n_bins, int* width);
 

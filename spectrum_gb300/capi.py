@@ -24,7 +24,10 @@ SPX_OPT_MAX_ATTEMPTS = 5
 #: the symbols include/spx.h declares
 EXPORTS = ["spx_create", "spx_set_option", "spx_add_plugin", "spx_add_problem", "spx_run", "spx_sync",
            "spx_get_distribution_info", "spx_get_distribution", "spx_get_records", "spx_reset_distributions",
-           "spx_dump", "spx_restore", "spx_strerror", "spx_destroy", "spx_version"]
+           "spx_dump", "spx_restore", "spx_strerror", "spx_destroy", "spx_version", "spx_run_static"]
+
+#: bytes of the fixed device array spx_run_static works in (SPX_STATIC_SCRATCH_BYTES)
+STATIC_SCRATCH_BYTES = 512 * 1024
 
 
 class Tuning(ctypes.Structure):
@@ -80,6 +83,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         lib.spx_destroy.argtypes = [c_vp]
         lib.spx_destroy.restype = None
         lib.spx_version.restype = ctypes.c_char_p
+        lib.spx_run_static.argtypes = [c_vp, ctypes.POINTER(Tuning), c_vp, ctypes.c_int64, c_vp, ctypes.c_int64, c_vp,
+                                       ctypes.c_int64, c_vp, ctypes.c_int64, ctypes.POINTER(Stats)]
         _lib = lib
     return _lib
 
@@ -176,3 +181,16 @@ class Context:
 
     def restore(self, path: str) -> None:
         check(self.lib.spx_restore(self._h, path.encode()), "spx_restore")
+
+    def run_static(self, counts_ptr: int, n_counts: int, sums_ptr: int, n_sums: int, n_events_ptr: int,
+                   n_events_len: int, records_ptr: int = 0, n_records: int = 0,
+                   tuning: Tuning | None = None) -> Stats:
+        """spx_run_static: one launch into caller-owned device buffers (raw device addresses), no
+        device allocation by the library; blocks until done."""
+        st = Stats()
+        check(self.lib.spx_run_static(self._h, ctypes.byref(tuning) if tuning is not None else None,
+                                      ctypes.c_void_p(counts_ptr), n_counts, ctypes.c_void_p(sums_ptr), n_sums,
+                                      ctypes.c_void_p(n_events_ptr), n_events_len,
+                                      ctypes.c_void_p(records_ptr) if records_ptr else None, n_records,
+                                      ctypes.byref(st)), "spx_run_static")
+        return st

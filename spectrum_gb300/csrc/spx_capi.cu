@@ -10,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <memory>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -570,5 +571,172 @@ void spx_destroy(spx_ctx_t c)
 }
 
 const char* spx_version(void) { return "spectrum_gb300 0.1 (sm_103a)"; }
+
+}  // extern "C"
+
+// ---- spx_run_static: the same launch with no device allocation ---------------------------------
+// For callers that cannot call cudaMalloc: code that runs where the device allocator is off
+// limits (inside a host framework that owns all device memory through its own pool, or on a
+// latency-critical path where cudaMalloc's implicit device synchronisation is not acceptable).
+// Such a caller passes its own device buffers for the outputs; the scratch memory the launch needs
+// -- the run counters, whose first word is the work-queue head, and the device copies of the
+// problem descriptors -- lives in one fixed array compiled into the library.
+//
+// Every GPU that loads the library holds this array until the process exits. All calls share it
+// and it keeps the last call's contents: each call clears the run counters before its launch and
+// overwrites the descriptors. Calls whose launches overlap on the GPU (two host threads, two
+// contexts or two streams at once) race on it and give wrong results.
+static __device__ __align__(256) unsigned char spx_static_scratch[SPX_STATIC_SCRATCH_BYTES];
+
+namespace {
+
+constexpr size_t kStaticCounterBytes = 256;  // RunCounters, padded to the array's alignment
+static_assert(sizeof(spx::RunCounters) <= kStaticCounterBytes, "run counters exceed their slot");
+
+std::mutex g_static_mu;
+void* g_static_ptr[256] = {};
+
+// The array's device address on the current device. Looked up once per device, on the first call
+// made with that device current (the look-up may load the library's device code on that device).
+int static_scratch(int device, unsigned char** out)
+{
+   if (device < 0 || device >= 256) return SPX_ERR_NO_DEVICE;
+   std::lock_guard<std::mutex> lock(g_static_mu);
+   if (g_static_ptr[device] == nullptr) {
+      void* ptr = nullptr;
+      cudaError_t e = cudaGetSymbolAddress((void**)&ptr, spx_static_scratch);
+      if (e != cudaSuccess) return cuda_err(e);
+      g_static_ptr[device] = ptr;
+   }
+   *out = static_cast<unsigned char*>(g_static_ptr[device]);
+   return SPX_OK;
+}
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace
+
+extern "C" {
+
+int spx_run_static(spx_ctx_t c, const spx_tuning* tuning, int32_t* counts, int64_t n_counts, double* sums,
+                   int64_t n_sums, unsigned long long* n_events, int64_t n_events_len, spx_traj_record* records,
+                   int64_t n_records, spx_stats* stats)
+{
+   if (!valid_ctx(c)) return SPX_ERR_INVALID_ARG;
+   if (c->problems.empty()) return SPX_ERR_STATE;
+   const int n = (int)c->problems.size();
+   const bool f64 = c->precision == SPX_FP64;
+
+   // the layout of the distributions and trajectories, on copies of the descriptors
+   std::vector<spx::ProblemDesc> hd(n);
+   int64_t off_c = 0, off_s = 0, total = 0;
+   for (int k = 0; k < n; k++) {
+      hd[k] = c->problems[k].pd;
+      hd[k].first = total;
+      hd[k].n_traj = c->problems[k].n_traj;
+      total += hd[k].n_traj;
+      for (int d = 0; d < hd[k].nd; d++) {
+         int64_t nb = (int64_t)hd[k].d[d].n_bins[0] * hd[k].d[d].n_bins[1] * hd[k].d[d].n_bins[2];
+         hd[k].d[d].offset_counts = off_c;
+         hd[k].d[d].offset_sums = off_s;
+         off_c += nb;
+         off_s += nb * hd[k].d[d].width;
+      }
+   }
+
+   // scratch: [run counters | FP64 descriptors | FP32 descriptors (mixed precision only)]
+   const size_t off_pd = kStaticCounterBytes;
+   const size_t bytes_pd = sizeof(spx::ProblemDesc) * n;
+   const size_t off_pr = f64 ? off_pd : align_up(off_pd + bytes_pd, 256);
+   const size_t bytes_pr = f64 ? 0 : sizeof(spx::ProblemDescT<float>) * n;
+   const size_t need = f64 ? off_pd + bytes_pd : off_pr + bytes_pr;
+   if (need > (size_t)SPX_STATIC_SCRATCH_BYTES) return SPX_ERR_TOO_LARGE;
+
+   // the caller's outputs
+   if (!counts || !sums || !n_events) return SPX_ERR_INVALID_ARG;
+   if (n_counts < off_c || n_sums < off_s || n_events_len < (int64_t)n * spx::kMaxDistro) return SPX_ERR_INVALID_ARG;
+   if (c->record_final && (!records || n_records < total)) return SPX_ERR_INVALID_ARG;
+   for (const auto& p : c->problems)
+      if ((uint64_t)(c->run_index + 2) * (uint64_t)p.n_traj > 0xffffffffull) return SPX_ERR_LIMIT;
+
+   SPX_CUDA(cudaSetDevice(c->device));
+   unsigned char* scratch = nullptr;
+   int rc = static_scratch(c->device, &scratch);
+   if (rc != SPX_OK) return rc;
+
+   // launch shape: the defaults of spx_run
+   spx_tuning tu{};
+   if (tuning) tu = *tuning;
+   if (tu.schedule != 0 && tu.schedule != 1) return SPX_ERR_INVALID_ARG;
+   if (tu.block_size <= 0) tu.block_size = 128;
+   if (tu.block_size % 32 || tu.block_size > 128) return SPX_ERR_INVALID_ARG;
+   if (!tuning) tu.schedule = c->precision == SPX_MIXED ? 1 : 0;
+   if (tu.steps_per_sync <= 0) tu.steps_per_sync = tu.schedule ? 16 : 1 << 30;
+   int slots = 1;
+   for (int k = 0; k < n; k++) slots = std::max(slots, hd[k].nbt + hd[k].nbs + hd[k].nbm);
+   int occ = occupancy(c, tu.block_size, slots);
+   if (occ <= 0) occ = 1;
+   if (tu.blocks_per_sm <= 0 || tu.blocks_per_sm > occ) tu.blocks_per_sm = occ;
+   int64_t grid = tu.schedule == 1 ? (int64_t)c->sm_count * tu.blocks_per_sm : (total + tu.block_size - 1) / tu.block_size;
+   grid = std::max<int64_t>(1, std::min<int64_t>(grid, 0x7fffffff));
+
+   // descriptors into the scratch, counters cleared
+   std::vector<spx::ProblemDescT<float>> hf;
+   SPX_CUDA(cudaMemsetAsync(scratch, 0, kStaticCounterBytes, c->stream));
+   SPX_CUDA(cudaMemcpyAsync(scratch + off_pd, hd.data(), bytes_pd, cudaMemcpyHostToDevice, c->stream));
+   if (!f64) {
+      hf.resize(n);
+      for (int k = 0; k < n; k++) spx::convert_problem(hd[k], hf[k]);
+      SPX_CUDA(cudaMemcpyAsync(scratch + off_pr, hf.data(), bytes_pr, cudaMemcpyHostToDevice, c->stream));
+   }
+
+   spx::LaunchArgs a;
+   a.block = dim3(tu.block_size);
+   a.grid = dim3((unsigned)grid);
+   a.stream = c->stream;
+   a.problems_r = scratch + off_pr;
+   a.problems_d = reinterpret_cast<const spx::ProblemDesc*>(scratch + off_pd);
+   a.cfg.traj_kind = c->traj;
+   a.cfg.time_flow = c->flow;
+   a.cfg.rk = c->rk;
+   a.cfg.deriv_mode = c->deriv_mode;
+   a.cfg.pa_scattering = c->pa_scattering;
+   a.cfg.max_attempts = c->max_attempts;
+   a.cfg.steps_per_orbit = c->steps_per_orbit;
+   a.cfg.steps_per_orbit_f = (float)c->steps_per_orbit;
+   a.cfg.record_final = c->record_final;
+   a.cfg.n_problems = n;
+   a.cfg.steps_per_sync = tu.steps_per_sync;
+   a.cfg.total_traj = total;
+   a.cfg.run_index = c->run_index;
+   a.ctr = reinterpret_cast<spx::RunCounters*>(scratch);
+   a.counts = counts;
+   a.sums = sums;
+   a.n_events = n_events;
+   a.records = c->record_final ? reinterpret_cast<spx::TrajRecord*>(records) : nullptr;
+   a.queue = tu.schedule;
+   a.bnd_slots = slots;
+   SPX_CUDA(cudaEventRecord(c->ev0, c->stream));
+   SPX_CUDA(launch(c, a));
+   SPX_CUDA(cudaEventRecord(c->ev1, c->stream));
+   SPX_CUDA(cudaStreamSynchronize(c->stream));
+   c->run_index++;
+
+   spx::RunCounters h;
+   SPX_CUDA(cudaMemcpy(&h, scratch, sizeof h, cudaMemcpyDeviceToHost));
+   if (stats) {
+      float ms = 0.0f;
+      SPX_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+      *stats = spx_stats{};
+      stats->kernel_ms = ms;
+      stats->trajectories = (int64_t)h.finished + (int64_t)h.given_up;
+      stats->steps = (int64_t)h.steps;
+      stats->retries = (int64_t)h.retries;
+      stats->given_up = (int64_t)h.given_up;
+      stats->kernel_launches = 1;
+      stats->tuning = tu;
+   }
+   return h.error != 0 ? SPX_ERR_DEVICE : SPX_OK;
+}
 
 }  // extern "C"
