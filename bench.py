@@ -181,7 +181,9 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="spectrum_gb300", choices=["spectrum_gb300", "reference"])
-    ap.add_argument("--per-energy", type=int, default=int(os.environ.get("SPX_BENCH_PER_ENERGY", "16000")))
+    ap.add_argument("--per-energy", type=int, default=int(os.environ.get("SPX_BENCH_PER_ENERGY", "100000")))
+    ap.add_argument("--fp64-per-energy", type=int, default=16000,
+                    help="trajectories per energy of the FP64 comparison (every fourth energy)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-fp64", action="store_true")
     args = ap.parse_args()
@@ -268,9 +270,10 @@ def main():
     # ---- plain FP64 drop-in on step 0's keys: comparison and per-bin error -------------------
     fp64 = None
     if not args.no_fp64:
-        # Every fourth energy at the full per-energy count (so each spectrum bin holds >= 1e4 events);
-        # fresh contexts with the same problem list draw identical Philox streams.
-        sub = pbs[::4]
+        # Every fourth energy, at a per-energy count that keeps the FP64 leg to about a minute (each
+        # spectrum bin still holds >= 1e4 events); fresh contexts with the same problem list draw
+        # identical Philox streams.
+        sub = problems(min(args.per_energy, args.fp64_per_energy), seed_offset)[::4]
         sim64 = open_problems(sub, precision=capi.SPX_FP64, deriv_mode=1)
         flush_l2(torch, dev)
         st64 = sim64.MainLoop(capi.Tuning(0, 0, 1, 0))
@@ -287,6 +290,7 @@ def main():
         _, es, nbs = per_bin_error([r[0] for r in d32], [r[0] for r in d64], 10000)
         fp64 = {"value": st64.trajectories / (st64.kernel_ms / 1e3), "unit": UNIT, "kernel_ms": st64.kernel_ms,
                 "trajectories": st64.trajectories, "energies": "every 4th of the 32",
+                "per_energy": min(args.per_energy, args.fp64_per_energy),
                 "steps_per_s": st64.steps / (st64.kernel_ms / 1e3), "schedule": "one thread per trajectory",
                 "derivatives": "analytic (the FP32 kernel's formulation)",
                 "bin_error": ec, "bins_compared": nbins, "bin_error_ok": bool(nbins > 0 and ec <= 0.01),

@@ -1,0 +1,102 @@
+"""Host-side logic on the CPU: the DataContainer byte layout, problem specs, the plugin catalogue,
+and the C-ABI library (it loads and exports every symbol include/spx.h declares; nothing is
+launched, so no GPU is needed)."""
+import ctypes
+import os
+import re
+import struct
+
+import numpy as np
+import pytest
+
+import oracle_tools as ot
+from spectrum_gb300 import capi, plugins, units, workloads
+from spectrum_gb300.datacontainer import DataContainer
+from spectrum_gb300.problem import Problem
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def test_datacontainer_records():
+    """[1-byte size][payload] per record (common/data_container.cc:139-224)."""
+    c = DataContainer().double(1.5).int(-3).bool(True).vec((1.0, 2.0, 3.0)).mi((4, 5, 6))
+    blob = c.data()
+    assert c.size() == 5
+    assert c.length() == len(blob)
+    expect = (bytes([8]) + struct.pack("<d", 1.5) + bytes([4]) + struct.pack("<i", -3) + bytes([1, 1]) +
+              bytes([24]) + struct.pack("<3d", 1, 2, 3) + bytes([12]) + struct.pack("<3i", 4, 5, 6))
+    assert blob == expect
+
+
+def test_datacontainer_record_limit():
+    with pytest.raises(ValueError):
+        DataContainer()._add(b"x" * 256)
+
+
+def test_units_code_system():
+    """Code units of common/specie.hh: c = 10 in code velocity; kinetic energy round trip."""
+    p = units.mev_to_mom(100.0)
+    assert abs(units.EnrKin(p) * units.unit_energy / units.MEV - 100.0) < 1e-9
+    assert units.Vel(p) < 10.0
+
+
+def test_problem_spec_sizes_match_oracle():
+    pbs = workloads.gcr_modulation(n_traj=10, energies_mev=[100.0, 200.0, 300.0])
+    sizes = ot.distro_sizes(pbs[0].to_spec())
+    assert sizes == [(3 * 4, 1), (32, 1)]  # spectrum: 4 bins per energy; exit times: 32 bins
+    pb = workloads.diffusion_uniform(n_traj=10)
+    assert ot.distro_sizes(pb.to_spec()) == [(100 ** 3, 1)]
+
+
+def test_plugin_roles_enforced():
+    pb = Problem(traj=206, time_flow=0, rk=0, seed=1, n_traj=1)
+    with pytest.raises(TypeError):
+        pb.AddBackground(plugins.BoundaryTimeExpire(), DataContainer())
+
+
+def test_workload_shapes():
+    pbs = workloads.gcr_modulation(n_traj=7)
+    assert len(pbs) == 32
+    e = workloads.modulation_energies()
+    assert abs(e[0] - 10.0) < 1e-12 and abs(e[-1] - 1.0e4) < 1e-9
+    assert [p.problem_id for p in pbs] == list(range(32))
+    foc = workloads.focused_transport(n_problems=64)
+    counts = [p.n_traj for p in foc]
+    assert min(counts) >= 1000 and max(counts) <= 1_000_000
+
+
+def _declared_symbols():
+    hdr = open(os.path.join(ROOT, "include", "spx.h")).read()
+    return sorted(set(re.findall(r"^\s*(?:int|int64_t|void|const char\*)\s+(spx_\w+)\s*\(", hdr, re.M)))
+
+
+def test_header_and_binding_agree():
+    assert _declared_symbols() == sorted(capi.EXPORTS)
+
+
+def test_library_exports_every_declared_symbol(built_lib):
+    lib = ctypes.CDLL(built_lib)
+    for name in _declared_symbols():
+        assert hasattr(lib, name), name
+    lib.spx_strerror.restype = ctypes.c_char_p
+    assert lib.spx_strerror(0) == b"success"
+    lib.spx_version.restype = ctypes.c_char_p
+    assert b"sm_103a" in lib.spx_version()
+
+
+def test_library_refuses_without_a_device(built_lib):
+    """No CPU fallback: on a machine without an sm_103 device, contexts are refused."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = ctypes.CDLL(built_lib)
+    lib.spx_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    h = ctypes.c_void_p()
+    rc = lib.spx_create(ctypes.byref(h), 206, 0, 0, 0)
+    assert rc < 0 and not h.value
+
+
+def test_record_dtype_matches_oracle():
+    assert capi.RECORD_DTYPE == ot.TRAJ_DTYPE
+    assert capi.RECORD_DTYPE.itemsize == 144
+    assert np.dtype(capi.RECORD_DTYPE).names[0] == "attempts"
