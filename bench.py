@@ -37,6 +37,9 @@ WORKLOAD = "gcr_modulation_parker_spiral_32E"
 # FP32 operations per accepted step of the FP32 Parker solar-wind kernel (executed
 # FP32 instructions from ncu per launch divided by the launch's steps, FMA counted as 2)
 FP32_FLOP_PER_STEP = float(os.environ.get("SPX_FP32_FLOP_PER_STEP", "0")) or None
+# run indices reserved per rank under torchrun: rank r integrates trajectory ids of runs
+# r*RUNS_PER_RANK ... (disjoint shards of one job)
+RUNS_PER_RANK = 256
 
 
 def rank_info():
@@ -214,7 +217,7 @@ def main():
 
     import numpy as np
     import torch
-    from spectrum_gb300 import capi
+    from spectrum_gb300 import capi, shard
     from spectrum_gb300.simulation import open_problems
 
     dev = torch.device("cuda", local)
@@ -222,12 +225,14 @@ def main():
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
-    seed_offset = 7919 * rank
-    pbs = problems(args.per_energy, seed_offset)
+    # ranks take disjoint trajectory-id ranges of one job (spectrum_gb300.shard)
+    pbs = problems(args.per_energy)
     n_step = 32 * args.per_energy
 
     # ---- batched FP32 stepper: value ---------------------------------------------------------
     sim = open_problems(pbs, precision=capi.SPX_MIXED)
+    if world > 1:
+        shard.assign(sim, rank, RUNS_PER_RANK)
     tun = capi.Tuning(0, 0, 0, 1)
     for _ in range(args.warmup):
         sim.MainLoop(tun)
@@ -259,11 +264,7 @@ def main():
               "steps_per_sync": st.tuning.steps_per_sync, "schedule": "persistent work queue"}
     sim.close()
     t_dev = sum(kms) / 1e3
-    t_max = t_dev
-    if world > 1:
-        tt = torch.tensor([t_dev], device=dev)
-        torch.distributed.all_reduce(tt, op=torch.distributed.ReduceOp.MAX)
-        t_max = float(tt.item())
+    t_max = shard.max_over_ranks(t_dev) if world > 1 else t_dev
     value = traj_done * world / t_max
     steps_rate = steps_done * world / t_max
 
@@ -273,7 +274,7 @@ def main():
         # Every fourth energy, at a per-energy count that keeps the FP64 leg to about a minute (each
         # spectrum bin still holds >= 1e4 events); fresh contexts with the same problem list draw
         # identical Philox streams.
-        sub = problems(min(args.per_energy, args.fp64_per_energy), seed_offset)[::4]
+        sub = problems(min(args.per_energy, args.fp64_per_energy))[::4]
         sim64 = open_problems(sub, precision=capi.SPX_FP64, deriv_mode=1)
         flush_l2(torch, dev)
         st64 = sim64.MainLoop(capi.Tuning(0, 0, 1, 0))
@@ -305,6 +306,8 @@ def main():
         flush_l2(torch, dev)
         t0 = time.perf_counter()
         s = open_problems(pbs, precision=capi.SPX_MIXED)
+        if world > 1:
+            s.ctx.set_option(capi.SPX_OPT_RUN_INDEX, shard.first_run_index(rank, RUNS_PER_RANK) + RUNS_PER_RANK // 2 + k)
         st_e = s.MainLoop(tun)
         outs = [s.ctx.distribution(p, 0) for p in range(len(pbs))]
         s.close()

@@ -68,6 +68,8 @@ extern "C" {
 #define SPX_OPT_PA_SCATTERING 3     /* Focused: Euler pitch-angle scattering step (1) or none (0) */
 #define SPX_OPT_RECORD_FINAL 4      /* keep the final state of every trajectory (spx_get_records) */
 #define SPX_OPT_MAX_ATTEMPTS 5      /* retries of a discarded trajectory, default 100 */
+#define SPX_OPT_RUN_INDEX 6         /* index of the next run: problem p's trajectory ids start at index * n_traj(p);
+                                       each run advances it by one (set per rank to shard one job over GPUs) */
 /* plugin kinds: see spectrum_gb300/plugins.py; e.g. background 1 uniform, 3 smooth shock,
  * 4 dipole, 5 solar wind; diffusion 5 full constant, 8 rigidity/field power law; boundary
  * 1 time expire, 10 plane absorb, 14 sphere absorb, 30 momentum inject; distribution 2 position

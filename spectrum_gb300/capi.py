@@ -20,6 +20,7 @@ SPX_OPT_DERIV_MODE = 2
 SPX_OPT_PA_SCATTERING = 3
 SPX_OPT_RECORD_FINAL = 4
 SPX_OPT_MAX_ATTEMPTS = 5
+SPX_OPT_RUN_INDEX = 6
 
 #: the symbols include/spx.h declares
 EXPORTS = ["spx_create", "spx_set_option", "spx_add_plugin", "spx_add_problem", "spx_run", "spx_sync",

@@ -264,6 +264,11 @@ int spx_set_option(spx_ctx_t c, int option, double value)
       if (!(value >= 1.0)) return SPX_ERR_INVALID_ARG;
       c->max_attempts = (int)value;
       return SPX_OK;
+   case SPX_OPT_RUN_INDEX:
+      // shards of one job: rank r starting at index r draws trajectory ids disjoint from the others'
+      if (!(value >= 0.0) || value != (double)(int64_t)value || value > 4294967295.0) return SPX_ERR_INVALID_ARG;
+      c->run_index = (int64_t)value;
+      return SPX_OK;
    default: return SPX_ERR_INVALID_ARG;
    }
 }
