@@ -1,0 +1,290 @@
+// spx_simulation.hh -- C++ host mirror of the reference's simulation interface on top of the C ABI
+// of spx.h (header only).
+//
+// A reference application builds DataContainer parameter blobs and hands them, with a prototype
+// object, to SimulationWorker::Add{Background,Diffusion,Source,Boundary,Initial,Distribution}, then
+// calls SetTasks and MainLoop and prints or restores distributions (src/simulation.hh:93-138). This
+// header gives the same calls the same names and arguments:
+//   - spx::DataContainer writes the reference's record layout (one size byte, then the payload;
+//     common/data_container.cc:139-224), with Insert for double, int, bool, GeoVector, MultiIndex,
+//     GeoMatrix and std::vector;
+//   - one empty prototype type per plugin class (BackgroundSolarWind(), BoundaryTimeExpire(), ...),
+//     carrying the class's role and kind;
+//   - spx::SimulationGPU, whose methods forward to spx_add_plugin / spx_add_problem / spx_run /
+//     spx_get_distribution.
+// An application changes its includes and the CreateSimulation call; everything between stays.
+#ifndef SPX_SIMULATION_HH
+#define SPX_SIMULATION_HH
+
+#include <cmath>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "spx.h"
+
+namespace spx {
+
+// ---- code units of the reference (common/specie.hh:30-82, common/physical_constants.hh) ------------
+namespace units {
+constexpr double speed_of_light = 2.99792458e10;   // cm/s
+constexpr double mass_proton = 1.67262192596e-24;  // g
+constexpr double electron_charge = 4.8032044e-10;  // Fr
+constexpr double electron_volt = 1.602176634e-12;  // erg
+constexpr double astronomical_unit = 1.495978707e13;  // cm
+constexpr double unit_length = 1.0e10;
+constexpr double unit_velocity = 0.1 * speed_of_light;
+constexpr double unit_mass = mass_proton;
+constexpr double unit_charge = electron_charge;
+constexpr double unit_momentum = unit_mass * unit_velocity;
+constexpr double unit_energy = unit_mass * unit_velocity * unit_velocity;
+constexpr double unit_time = unit_length / unit_velocity;
+constexpr double unit_magnetic = unit_momentum / (unit_charge * unit_time);
+constexpr double c_code = speed_of_light / unit_velocity;
+// proton kinematics in code units (common/physics.hh:274-316)
+inline double EnrTot(double p) { return std::sqrt(p * p + c_code * c_code) * c_code; }
+inline double EnrKin(double p) { return EnrTot(p) - c_code * c_code; }
+inline double Mom(double enr_kin) { return std::sqrt(enr_kin * (enr_kin + 2.0 * c_code * c_code)) / c_code; }
+inline double Vel(double p) { return p * c_code * c_code / EnrTot(p); }
+inline double MeVToMom(double e_mev) { return Mom(e_mev * (1.0e6 * electron_volt) / unit_energy); }
+}  // namespace units
+
+// ---- parameter containers ------------------------------------------------------------------------
+struct GeoVector {
+   double x[3];
+   GeoVector(double a = 0.0, double b = 0.0, double c = 0.0) : x{a, b, c} {}
+   double& operator[](int i) { return x[i]; }
+   double operator[](int i) const { return x[i]; }
+};
+
+struct MultiIndex {
+   int i[3];
+   MultiIndex(int a = 0, int b = 0, int c = 0) : i{a, b, c} {}
+};
+
+struct GeoMatrix {
+   GeoVector row[3];
+};
+
+const GeoVector gv_zeros(0.0, 0.0, 0.0);
+const GeoVector gv_ones(1.0, 1.0, 1.0);
+const GeoVector gv_nz(0.0, 0.0, 1.0);
+
+// The reference's positional parameter blob: per Insert one record of [size byte][payload].
+class DataContainer {
+   std::vector<uint8_t> bytes_;
+   size_t records_ = 0;
+
+   void put(const void* p, size_t n)
+   {
+      if (n > 255) throw std::length_error("a DataContainer record holds at most 255 bytes");
+      bytes_.push_back((uint8_t)n);
+      const uint8_t* b = static_cast<const uint8_t*>(p);
+      bytes_.insert(bytes_.end(), b, b + n);
+      records_++;
+   }
+
+public:
+   void Clear(void) { bytes_.clear(); records_ = 0; }
+   void Insert(double v) { put(&v, sizeof v); }
+   void Insert(int v) { put(&v, sizeof v); }
+   void Insert(bool v) { uint8_t b = v ? 1 : 0; put(&b, 1); }
+   void Insert(const GeoVector& v) { put(v.x, sizeof v.x); }
+   void Insert(const MultiIndex& v) { put(v.i, sizeof v.i); }
+   void Insert(const GeoMatrix& m)
+   {
+      double a[9];
+      for (int r = 0; r < 3; r++)
+         for (int c = 0; c < 3; c++) a[3 * r + c] = m.row[r][c];
+      put(a, sizeof a);
+   }
+   template <typename T>
+   void Insert(const std::vector<T>& v) { put(v.data(), v.size() * sizeof(T)); }
+   const uint8_t* data(void) const { return bytes_.data(); }
+   size_t length(void) const { return bytes_.size(); }
+   size_t size(void) const { return records_; }
+};
+
+// ---- plugin prototypes ---------------------------------------------------------------------------
+struct BackgroundBase { int kind; };
+struct DiffusionBase { int kind; };
+struct SourceBase { int kind; };
+struct BoundaryBase { int kind; };
+struct InitialBase { int kind; };
+struct DistributionBase { int kind; };
+
+#define SPX_PROTOTYPE(name, base, k) \
+   struct name : base {              \
+      name() : base{k} {}            \
+   };
+SPX_PROTOTYPE(BackgroundUniform, BackgroundBase, 1)
+SPX_PROTOTYPE(BackgroundShock, BackgroundBase, 2)
+SPX_PROTOTYPE(BackgroundSmoothShock, BackgroundBase, 3)
+SPX_PROTOTYPE(BackgroundDipole, BackgroundBase, 4)
+SPX_PROTOTYPE(BackgroundSolarWind, BackgroundBase, 5)
+SPX_PROTOTYPE(DiffusionIsotropicConstant, DiffusionBase, 1)
+SPX_PROTOTYPE(DiffusionQLTConstant, DiffusionBase, 2)
+SPX_PROTOTYPE(DiffusionParaConstant, DiffusionBase, 3)
+SPX_PROTOTYPE(DiffusionPerpConstant, DiffusionBase, 4)
+SPX_PROTOTYPE(DiffusionFullConstant, DiffusionBase, 5)
+SPX_PROTOTYPE(DiffusionFlowMomentumPowerLaw, DiffusionBase, 6)
+SPX_PROTOTYPE(DiffusionKineticEnergyRadialDistancePowerLaw, DiffusionBase, 7)
+SPX_PROTOTYPE(DiffusionRigidityMagneticFieldPowerLaw, DiffusionBase, 8)
+SPX_PROTOTYPE(DiffusionStraussEtAl2013, DiffusionBase, 9)
+SPX_PROTOTYPE(DiffusionPotgieterEtAl2015, DiffusionBase, 10)
+SPX_PROTOTYPE(DiffusionEmpiricalSOQLTandUNLT, DiffusionBase, 11)
+SPX_PROTOTYPE(SourceConstant, SourceBase, 1)
+SPX_PROTOTYPE(SourceMomentumInjection, SourceBase, 2)
+SPX_PROTOTYPE(BoundaryTimeExpire, BoundaryBase, 1)
+SPX_PROTOTYPE(BoundaryTimePass, BoundaryBase, 2)
+SPX_PROTOTYPE(BoundaryTimeRecurrent, BoundaryBase, 3)
+SPX_PROTOTYPE(BoundaryPlaneAbsorb, BoundaryBase, 10)
+SPX_PROTOTYPE(BoundaryPlaneReflect, BoundaryBase, 11)
+SPX_PROTOTYPE(BoundaryPlanePass, BoundaryBase, 12)
+SPX_PROTOTYPE(BoundaryBoxReflect, BoundaryBase, 13)
+SPX_PROTOTYPE(BoundarySphereAbsorb, BoundaryBase, 14)
+SPX_PROTOTYPE(BoundarySphereReflect, BoundaryBase, 15)
+SPX_PROTOTYPE(BoundaryRankineAbsorb, BoundaryBase, 16)
+SPX_PROTOTYPE(BoundaryCylinderAbsorb, BoundaryBase, 17)
+SPX_PROTOTYPE(BoundaryRegionAbsorb, BoundaryBase, 18)
+SPX_PROTOTYPE(BoundarySpherePass, BoundaryBase, 19)  // extension: no reference class
+SPX_PROTOTYPE(BoundaryMomentumInject, BoundaryBase, 30)
+SPX_PROTOTYPE(BoundaryMomentumPass, BoundaryBase, 31)
+SPX_PROTOTYPE(BoundaryMomentumInjectRestrictSlab, BoundaryBase, 32)
+SPX_PROTOTYPE(BoundaryMomentumInjectRestrictShell, BoundaryBase, 33)
+SPX_PROTOTYPE(BoundaryMirror, BoundaryBase, 34)
+SPX_PROTOTYPE(InitialTimeFixed, InitialBase, 1)
+SPX_PROTOTYPE(InitialTimeInterval, InitialBase, 2)
+SPX_PROTOTYPE(InitialSpaceFixed, InitialBase, 10)
+SPX_PROTOTYPE(InitialSpaceLine, InitialBase, 11)
+SPX_PROTOTYPE(InitialSpaceCircle, InitialBase, 12)
+SPX_PROTOTYPE(InitialSpaceBox, InitialBase, 13)
+SPX_PROTOTYPE(InitialSpaceSphere, InitialBase, 14)
+SPX_PROTOTYPE(InitialSpaceSphereSector, InitialBase, 15)
+SPX_PROTOTYPE(InitialSpaceRankineHalfBody, InitialBase, 16)
+SPX_PROTOTYPE(InitialMomentumFixed, InitialBase, 30)
+SPX_PROTOTYPE(InitialMomentumBeam, InitialBase, 31)
+SPX_PROTOTYPE(InitialMomentumRing, InitialBase, 32)
+SPX_PROTOTYPE(InitialMomentumShell, InitialBase, 33)
+SPX_PROTOTYPE(InitialMomentumThickShell, InitialBase, 34)
+SPX_PROTOTYPE(InitialMomentumMaxwell, InitialBase, 35)
+SPX_PROTOTYPE(InitialMomentumLogEnergyPitchBand, InitialBase, 40)  // extension: no reference class
+SPX_PROTOTYPE(InitialSpaceEquatorialBand, InitialBase, 41)  // extension: no reference class
+SPX_PROTOTYPE(DistributionTimeUniform, DistributionBase, 1)
+SPX_PROTOTYPE(DistributionPositionUniform, DistributionBase, 2)
+SPX_PROTOTYPE(DistributionMomentumUniform, DistributionBase, 3)
+SPX_PROTOTYPE(DistributionPositionMomentumUniform, DistributionBase, 4)
+SPX_PROTOTYPE(DistributionSpectrumKineticEnergyPowerLaw, DistributionBase, 5)
+SPX_PROTOTYPE(DistributionSpectrumKineticEnergyBentPowerLaw, DistributionBase, 6)
+SPX_PROTOTYPE(DistributionPositionCumulativeOrder1, DistributionBase, 7)
+SPX_PROTOTYPE(DistributionPositionCumulativeOrder2, DistributionBase, 8)
+SPX_PROTOTYPE(DistributionDivergenceFlowPowerLaw, DistributionBase, 9)
+SPX_PROTOTYPE(DistributionTimeMu, DistributionBase, 20)  // extension: no reference class
+#undef SPX_PROTOTYPE
+
+// ---- the simulation object -----------------------------------------------------------------------
+class SimulationGPU {
+   spx_ctx_t ctx_ = nullptr;
+   int traj_;
+   uint64_t seed_;
+   std::string prefix_;
+   std::vector<std::string> distro_names_;
+
+   void check(int rc, const char* what) const
+   {
+      if (rc < 0) throw std::runtime_error(std::string(what) + ": " + spx_strerror(rc));
+   }
+   void add(int role, int kind, const DataContainer& c, const char* what)
+   {
+      check(spx_add_plugin(ctx_, role, kind, c.data(), c.length(), c.size()), what);
+   }
+
+public:
+   // traj_kind, time_flow and rk are the reference's configure-time TRAJ_TYPE, TRAJ_TIME_FLOW and
+   // RK_INTEGRATOR_TYPE (configure.ac:236-295); precision is SPX_FP64 or SPX_MIXED.
+   SimulationGPU(int traj_kind, int time_flow, int rk, int precision, uint64_t seed = 0x5EED0000u)
+      : traj_(traj_kind), seed_(seed)
+   {
+      check(spx_create(&ctx_, traj_kind, time_flow, rk, precision), "spx_create");
+   }
+   ~SimulationGPU() { if (ctx_) spx_destroy(ctx_); }
+   SimulationGPU(const SimulationGPU&) = delete;
+   SimulationGPU& operator=(const SimulationGPU&) = delete;
+
+   spx_ctx_t context(void) const { return ctx_; }
+   void SetOption(int option, double value) { check(spx_set_option(ctx_, option, value), "spx_set_option"); }
+
+   // src/simulation.hh:105-123
+   void AddBackground(const BackgroundBase& p, const DataContainer& c, const std::string& = "")
+   { add(SPX_ROLE_BACKGROUND, p.kind, c, "AddBackground"); }
+   void AddDiffusion(const DiffusionBase& p, const DataContainer& c) { add(SPX_ROLE_DIFFUSION, p.kind, c, "AddDiffusion"); }
+   void AddSource(const SourceBase& p, const DataContainer& c) { add(SPX_ROLE_SOURCE, p.kind, c, "AddSource"); }
+   void AddBoundary(const BoundaryBase& p, const DataContainer& c) { add(SPX_ROLE_BOUNDARY, p.kind, c, "AddBoundary"); }
+   void AddInitial(const InitialBase& p, const DataContainer& c) { add(SPX_ROLE_INITIAL, p.kind, c, "AddInitial"); }
+   void AddDistribution(const DistributionBase& p, const DataContainer& c)
+   {
+      add(SPX_ROLE_DISTRIBUTION, p.kind, c, "AddDistribution");
+      distro_names_.push_back(std::to_string(p.kind));
+   }
+
+   // src/simulation.hh:96-97: one problem of n_traj trajectories (the batch sizes of the MPI farm
+   // have no meaning on the device and are ignored). Returns the problem index.
+   int SetTasks(int n_traj, int = 0, int = 0)
+   {
+      check(spx_add_problem(ctx_, n_traj, seed_, nullptr, 0), "SetTasks");
+      return n_problems_++;
+   }
+
+   std::string GetTrajectoryName(void) const
+   {
+      switch (traj_) {
+      case SPX_TRAJ_LORENTZ: return "TrajectoryLorentz";
+      case SPX_TRAJ_FOCUSED: return "TrajectoryFocused";
+      case SPX_TRAJ_PARKER: return "TrajectoryParker";
+      case SPX_TRAJ_PARKER_SOURCE: return "TrajectoryParkerSource";
+      default: return "Trajectory";
+      }
+   }
+
+   void DistroFileName(const std::string& file_name) { prefix_ = file_name; }
+
+   // src/simulation.cc:818-835: every trajectory of every problem, then wait.
+   spx_stats MainLoop(void)
+   {
+      check(spx_run(ctx_, nullptr), "spx_run");
+      spx_stats st;
+      check(spx_sync(ctx_, &st), "spx_sync");
+      return st;
+   }
+
+   void RestoreDistro(int = 0) { check(spx_restore(ctx_, (prefix_ + "distros.spx").c_str()), "RestoreDistro"); }
+   void DumpDistro(void) { check(spx_dump(ctx_, (prefix_ + "distros.spx").c_str()), "DumpDistro"); }
+
+   // Bin index, count and mean weight per bin of one distribution of one problem (the columns of
+   // DistributionTemplated::Print1D, src/distribution_templated.cc:546-590, in code units).
+   void PrintDistro1D(int distro, int /*ijk*/, const std::string& file_name, bool /*phys_units*/, int problem = 0) const
+   {
+      int64_t nb = 0;
+      int w = 0;
+      check(spx_get_distribution_info(ctx_, problem, distro, &nb, &w), "PrintDistro1D");
+      std::vector<int32_t> counts(nb);
+      std::vector<double> sums(nb * w);
+      int64_t nev = 0;
+      check(spx_get_distribution(ctx_, problem, distro, counts.data(), sums.data(), &nev), "PrintDistro1D");
+      FILE* f = std::fopen(file_name.c_str(), "w");
+      if (!f) throw std::runtime_error("cannot open " + file_name);
+      for (int64_t i = 0; i < nb; i++)
+         std::fprintf(f, "%8lld %12d %20.12e\n", (long long)i, counts[i], counts[i] ? sums[i * w] / counts[i] : 0.0);
+      std::fclose(f);
+   }
+
+private:
+   int n_problems_ = 0;
+};
+
+}  // namespace spx
+
+#endif

@@ -79,20 +79,22 @@ def test_focused_fp64_matches_oracle(built_lib, scattering):
 
 
 def test_pitch_angle_isotropisation(built_lib):
-    """Pure pitch-angle scattering with D_mumu = D0 (1 - mu^2) relaxes a beam to isotropy:
-    <mu> decays as exp(-2 D0 t) (benchmarks/benchmark_explained.txt:34-39)."""
+    """Pure pitch-angle scattering with D_mumu = D0 (1 - mu^2) relaxes a ring of pitch cosine mu0
+    to isotropy: <mu> decays as mu0 exp(-2 D0 t) (benchmarks/benchmark_explained.txt:34-39). The
+    ring sampler gives focused trajectories (p0, cos theta0, 0) (src/initial_momentum.cc:203-217)."""
     from spectrum_gb300.datacontainer import DataContainer as DC
     from spectrum_gb300.plugins import (BackgroundUniform, BoundaryTimeExpire, DiffusionIsotropicConstant,
-                                        DistributionTimeUniform, InitialMomentumBeam, InitialSpaceFixed,
+                                        DistributionTimeUniform, InitialMomentumRing, InitialSpaceFixed,
                                         InitialTimeFixed)
     from spectrum_gb300.problem import FORWARD, TRAJ_FOCUSED, Problem, distro_header
     d0 = 1.0
     t_end = 0.25
+    theta0 = 0.3
     pb = Problem(traj=TRAJ_FOCUSED, time_flow=FORWARD, rk=25, seed=77, n_traj=40_000)
     pb.AddBackground(BackgroundUniform(), DC().double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0, 0, 1.0)).double(1.0e3))
     pb.AddInitial(InitialTimeFixed(), DC().double(0.0))
     pb.AddInitial(InitialSpaceFixed(), DC().vec((0, 0, 0)))
-    pb.AddInitial(InitialMomentumBeam(), DC().double(1.0))
+    pb.AddInitial(InitialMomentumRing(), DC().double(1.0).double(theta0))
     pb.AddDiffusion(DiffusionIsotropicConstant(), DC().double(d0))
     pb.AddBoundary(BoundaryTimeExpire(), workloads._boundary(DC(), 1, [0]).double(t_end))
     c = distro_header(DC(), (4, 0, 0), (0.0, 0, 0), (1.0, 0, 0))
@@ -103,7 +105,7 @@ def test_pitch_angle_isotropisation(built_lib):
         rec = run_problems(pb, precision=prec, record=True).records[0]
         mu = rec["mom"][:, 1]
         t = rec["t"].mean()
-        expect = math.exp(-2.0 * d0 * t)
+        expect = math.cos(theta0) * math.exp(-2.0 * d0 * t)
         sigma = mu.std() / math.sqrt(len(mu))
         assert abs(mu.mean() - expect) < 4.0 * sigma + 0.01, (prec, mu.mean(), expect)
         assert np.all(np.abs(mu) <= 1.0)
@@ -126,16 +128,47 @@ def test_shock_acceleration_index(built_lib):
     assert abs(slope - (3.0 - 4.0)) < 0.12, slope
 
 
-def test_batched_problems_equal_separate_runs(built_lib):
-    """A batch of problems in one launch gives each problem exactly what its own launch gives
-    (trajectory ids and problem ids key the random streams)."""
-    pbs = workloads.gcr_modulation(n_traj=128, energies_mev=[50.0, 500.0, 5000.0], t_max_years=0.1)
+def test_batched_problems_match_oracle(built_lib):
+    """A batch of problems with different diffusion coefficients in one launch: every problem's
+    trajectories equal the oracle's for that problem (its problem id keys its random streams)."""
+    pbs = []
+    for k, kappa in enumerate((0.5, 1.0, 2.0)):
+        pb = workloads.diffusion_uniform(n_traj=200, kappa=kappa, t_end=0.2)
+        pb.problem_id = k
+        pbs.append(pb)
     batch = run_problems(pbs, precision=capi.SPX_FP64, record=True)
     for k, pb in enumerate(pbs):
-        alone = run_problems(pb, precision=capi.SPX_FP64, record=True)
-        a, b = batch.records[k], alone.records[0]
-        assert np.array_equal(a["steps"], b["steps"])
-        assert np.array_equal(a["pos"], b["pos"])
-        ca, _, na = batch.distros[k][0]
-        cb, _, nb = alone.distros[0][0]
-        assert na == nb and np.array_equal(ca, cb)
+        ref = ot.run_oracle(pb)
+        rec = batch.records[k]
+        assert np.array_equal(rec["steps"], ref.traj["steps"])
+        assert np.allclose(rec["pos"], ref.traj["pos"], rtol=1e-12, atol=1e-14)
+        counts, _, nev = batch.distros[k][0]
+        rc, _, rn = ref.distros[0]
+        assert nev == rn and np.array_equal(counts, rc)
+
+
+def test_cpp_application_equals_python_path(built_lib, tmp_path):
+    """A reference-style C++ application on include/spx_simulation.hh gives, trajectory set for
+    trajectory set, the spectrum the Python host path gives."""
+    import os
+    import shutil
+    import subprocess
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    exe = str(tmp_path / "gcr_modulation")
+    lib_dir = os.path.dirname(built_lib)
+    subprocess.run([gxx, "-std=c++17", "-O2", "-I", os.path.join(root, "include"),
+                    os.path.join(root, "spectrum_gb300", "examples", "gcr_modulation.cc"), "-L", lib_dir, "-lspx",
+                    f"-Wl,-rpath,{lib_dir}", "-o", exe], check=True)
+    n_e, n, years = 3, 2000, 0.2
+    out = subprocess.run([exe, str(n_e), str(n), str(years), str(capi.SPX_MIXED), str(tmp_path / "x_")], check=True,
+                         capture_output=True, text=True).stdout.split("\n")
+    rows = [line.split() for line in out if line.strip()]
+    pbs = workloads.gcr_modulation(n_traj=n, energies_mev=workloads.modulation_energies(n_e), t_max_years=years)
+    res = run_problems(pbs, precision=capi.SPX_MIXED)
+    for k in range(n_e):
+        counts, sums, _ = res.distros[k][0]
+        assert int(rows[k][2]) == int(counts.sum()), k
+        assert math.isclose(float(rows[k][3]), float(sums[:, 0].sum()), rel_tol=1e-9), k

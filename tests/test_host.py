@@ -100,3 +100,32 @@ def test_record_dtype_matches_oracle():
     assert capi.RECORD_DTYPE == ot.TRAJ_DTYPE
     assert capi.RECORD_DTYPE.itemsize == 144
     assert np.dtype(capi.RECORD_DTYPE).names[0] == "attempts"
+
+
+def _build_example(built_lib, tmp_path):
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    exe = str(tmp_path / "gcr_modulation")
+    lib_dir = os.path.dirname(built_lib)
+    subprocess.run([gxx, "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+                    os.path.join(ROOT, "spectrum_gb300", "examples", "gcr_modulation.cc"), "-L", lib_dir, "-lspx",
+                    f"-Wl,-rpath,{lib_dir}", "-o", exe], check=True)
+    return exe
+
+
+def test_cpp_host_mirror_blobs_equal_python(built_lib, tmp_path):
+    """The C++ host mirror (include/spx_simulation.hh) writes the same parameter bytes as the
+    Python builder for the modulation set-up of the example application."""
+    import subprocess
+    exe = _build_example(built_lib, tmp_path)
+    out = subprocess.run([exe, "--dump"], check=True, capture_output=True, text=True).stdout.split("\n")
+    cpp = [tuple(line.split()) for line in out if line.strip()]
+    pb = workloads.gcr_modulation(n_traj=1, energies_mev=workloads.modulation_energies(4))[0]
+    py = [(str(e.plugin.role), str(e.plugin.kind), str(e.n_records), e.blob.hex()) for e in pb.plugins]
+    assert sorted(cpp) == sorted(py)
+    # the same order within each role (slots are positional)
+    for role in range(6):
+        assert [x for x in cpp if x[0] == str(role)] == [x for x in py if x[0] == str(role)]
