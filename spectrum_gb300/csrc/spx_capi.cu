@@ -176,15 +176,15 @@ cudaError_t launch(spx_ctx* c, const spx::LaunchArgs& a)
 int occupancy(spx_ctx* c, int block, int slots)
 {
    bool f64 = c->precision == SPX_FP64;
-   int bg = c->bg_kind;
+   int bg = c->bg_kind, dm = c->deriv_mode;
    switch (c->traj) {
    case SPX_TRAJ_PARKER:
    case SPX_TRAJ_PARKER_SOURCE:
-      return f64 ? spx::occupancy_parker_f64(bg, block, slots) : spx::occupancy_parker_f32(bg, block, slots);
+      return f64 ? spx::occupancy_parker_f64(bg, block, slots, dm) : spx::occupancy_parker_f32(bg, block, slots, dm);
    case SPX_TRAJ_LORENTZ:
-      return f64 ? spx::occupancy_lorentz_f64(bg, block, slots) : spx::occupancy_lorentz_f32(bg, block, slots);
+      return f64 ? spx::occupancy_lorentz_f64(bg, block, slots, dm) : spx::occupancy_lorentz_f32(bg, block, slots, dm);
    case SPX_TRAJ_FOCUSED:
-      return f64 ? spx::occupancy_focused_f64(bg, block, slots) : spx::occupancy_focused_f32(bg, block, slots);
+      return f64 ? spx::occupancy_focused_f64(bg, block, slots, dm) : spx::occupancy_focused_f32(bg, block, slots, dm);
    default: return 0;
    }
 }

@@ -13,23 +13,42 @@ struct FamilyTU {
    // dynamic shared memory: the boundary states of every lane of a block
    static size_t smem(int slots, int block) { return (size_t)(slots > 0 ? slots : 1) * block * sizeof(BndState<R>); }
 
-   template <int BG>
-   static cudaError_t go(const LaunchArgs& a)
+   template <int BG, int DM>
+   static cudaError_t go_dm(const LaunchArgs& a)
    {
       const auto* P = static_cast<const ProblemDescT<R>*>(a.problems_r);
-      step_kernel<TT, BG, R><<<a.grid, a.block, smem(a.bnd_slots, a.block.x), a.stream>>>(
+      step_kernel<TT, BG, R, DM><<<a.grid, a.block, smem(a.bnd_slots, a.block.x), a.stream>>>(
           P, a.problems_d, a.cfg, a.ctr, a.counts, a.sums, a.n_events, a.records, a.queue);
       return cudaGetLastError();
    }
 
+   // FP64 kernels exist for both derivative methods; the FP32 kernels are analytic only.
    template <int BG>
-   static int occ(int block, int slots)
+   static cudaError_t go(const LaunchArgs& a)
+   {
+      if constexpr (sizeof(R) == sizeof(double)) {
+         if (a.cfg.deriv_mode == 0) return go_dm<BG, 0>(a);
+      }
+      return go_dm<BG, 1>(a);
+   }
+
+   template <int BG, int DM>
+   static int occ_dm(int block, int slots)
    {
       int n = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<TT, BG, R>, block, smem(slots, block)) !=
+      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<TT, BG, R, DM>, block, smem(slots, block)) !=
           cudaSuccess)
          n = 0;
       return n;
+   }
+
+   template <int BG>
+   static int occ(int block, int slots, int deriv_mode)
+   {
+      if constexpr (sizeof(R) == sizeof(double)) {
+         if (deriv_mode == 0) return occ_dm<BG, 0>(block, slots);
+      }
+      return occ_dm<BG, 1>(block, slots);
    }
 
    static cudaError_t launch(int bg, const LaunchArgs& a)
@@ -44,14 +63,14 @@ struct FamilyTU {
       }
    }
 
-   static int occupancy(int bg, int block, int slots)
+   static int occupancy(int bg, int block, int slots, int deriv_mode)
    {
       switch (bg) {
-      case kBgUniform: return occ<kBgUniform>(block, slots);
-      case kBgShock: return occ<kBgShock>(block, slots);
-      case kBgSmoothShock: return occ<kBgSmoothShock>(block, slots);
-      case kBgDipole: return occ<kBgDipole>(block, slots);
-      case kBgSolarWind: return occ<kBgSolarWind>(block, slots);
+      case kBgUniform: return occ<kBgUniform>(block, slots, deriv_mode);
+      case kBgShock: return occ<kBgShock>(block, slots, deriv_mode);
+      case kBgSmoothShock: return occ<kBgSmoothShock>(block, slots, deriv_mode);
+      case kBgDipole: return occ<kBgDipole>(block, slots, deriv_mode);
+      case kBgSolarWind: return occ<kBgSolarWind>(block, slots, deriv_mode);
       default: return 0;
       }
    }
@@ -62,8 +81,8 @@ struct FamilyTU {
 #define SPX_FAMILY_TU(fam, prec, TT, R)                                                                    \
    namespace spx {                                                                                          \
    cudaError_t launch_##fam##_##prec(int bg, const LaunchArgs& a) { return FamilyTU<TT, R>::launch(bg, a); } \
-   int occupancy_##fam##_##prec(int bg, int block, int slots)                                               \
+   int occupancy_##fam##_##prec(int bg, int block, int slots, int deriv_mode)                               \
    {                                                                                                        \
-      return FamilyTU<TT, R>::occupancy(bg, block, slots);                                                  \
+      return FamilyTU<TT, R>::occupancy(bg, block, slots, deriv_mode);                                      \
    }                                                                                                        \
    }

@@ -26,8 +26,8 @@ struct LaunchArgs {
 #define SPX_DECLARE_FAMILY(fam)                                  \
    cudaError_t launch_##fam##_f64(int bg, const LaunchArgs& a);  \
    cudaError_t launch_##fam##_f32(int bg, const LaunchArgs& a);  \
-   int occupancy_##fam##_f64(int bg, int block, int slots);      \
-   int occupancy_##fam##_f32(int bg, int block, int slots);
+   int occupancy_##fam##_f64(int bg, int block, int slots, int deriv_mode); \
+   int occupancy_##fam##_f32(int bg, int block, int slots, int deriv_mode);
 SPX_DECLARE_FAMILY(parker)
 SPX_DECLARE_FAMILY(lorentz)
 SPX_DECLARE_FAMILY(focused)

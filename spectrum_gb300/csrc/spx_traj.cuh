@@ -860,12 +860,16 @@ __device__ __forceinline__ void start_lane(Lane<R, A>& L, BndView<R> bv, Start& 
 
 // One lane per thread. Dynamic shared memory holds the lanes' boundary states
 // (boundaries per lane x blockDim.x x sizeof(BndState<R>)).
-template <int TT, int BG, class R>
+// DM is the field-derivative method (SPX_OPT_DERIV_MODE) fixed per instantiation, so the analytic
+// kernels carry no finite-difference code (whose out-of-line calls would pin the field record to
+// the stack).
+template <int TT, int BG, class R, int DM>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? SPX_MIN_BLOCKS_F32 : SPX_MIN_BLOCKS_F64)
 step_kernel(const ProblemDescT<R>* __restrict__ P, const ProblemDesc* __restrict__ Pd, RunConfig cfg,
             RunCounters* ctr, int32_t* counts, double* sums, unsigned long long* n_events, TrajRecord* rec, int queue)
 {
    using A = typename AccOf<R>::type;
+   cfg.deriv_mode = DM;
    extern __shared__ __align__(16) unsigned char spx_smem[];
    const BndView<R> bv{reinterpret_cast<BndState<R>*>(spx_smem) + threadIdx.x, (int)blockDim.x};
    Sinks S{counts, sums, n_events, ctr};
