@@ -34,9 +34,13 @@ sys.path.insert(0, ROOT)
 METRIC = "SDE trajectories/s at <=1% bin error: batched FP32 vs plain FP64 GPU, 1 GB300"
 UNIT = "trajectories/s"
 WORKLOAD = "gcr_modulation_parker_spiral_32E"
-# FP32 operations per accepted step of the FP32 Parker solar-wind kernel (executed
-# FP32 instructions from ncu per launch divided by the launch's steps, FMA counted as 2)
-FP32_FLOP_PER_STEP = float(os.environ.get("SPX_FP32_FLOP_PER_STEP", "0")) or None
+# Per-step work of the FP32 Parker solar-wind kernel, from one ncu capture of a 128,000-trajectory
+# batch of this workload (profiles/step_kernel_parker_solarwind_f32_gcr4k.md): executed FP32
+# operations (FFMA x 2 + FADD + FMUL) and thread instructions per accepted step, and DRAM bytes
+# per trajectory (10.6 MB over 128,000 trajectories; the kernel reads no field data from HBM).
+FP32_FLOP_PER_STEP = float(os.environ.get("SPX_FP32_FLOP_PER_STEP", "439"))
+THREAD_INST_PER_STEP = 812.0
+DRAM_BYTES_PER_TRAJ = 10.635e6 / 128000
 # run indices reserved per rank under torchrun: rank r integrates trajectory ids of runs
 # r*RUNS_PER_RANK ... (disjoint shards of one job)
 RUNS_PER_RANK = 256
@@ -71,37 +75,70 @@ def _cpu_worker(args):
     return int(len(res.traj)), int(res.traj["steps"].sum()), dt
 
 
-def cpu_sample(seconds: float = 20.0, per_energy: int = 1000):
-    """Time the reference algorithm (C restatement, the reference's own derivative methods) on all
-    host cores, one process per core, on a bounded sample of the same workload: the energies in
-    turn, trajectories 0.. of each, until about ``seconds`` of wall time is spent."""
-    cores = os.cpu_count() or 1
-    sys.path.insert(0, os.path.join(ROOT, "tests"))
-    import oracle_tools
-    oracle_tools.lib()  # build/load before forking workers
-    ctx = mp.get_context("spawn")
-    tasks = []
-    n_per_task = 2
-    k = 0
-    for rnd in range(100000):
-        for e in range(32):
-            tasks.append((e, rnd * n_per_task, n_per_task, per_energy))
-            k += 1
-    done_traj = done_steps = 0
-    t0 = time.perf_counter()
-    with ctx.Pool(cores) as pool:
-        it = pool.imap_unordered(_cpu_worker, tasks, chunksize=1)
-        for ntraj, nsteps, _ in it:
+class CpuLeg:
+    """The reference algorithm (the C restatement with the reference's own derivative methods) on
+    all host cores: one spawned process per core, tasks of two trajectories taken round-robin over
+    the 32 energies (trajectories 0, 1, 2, ... of each). A sample keeps every core busy for about
+    the requested wall time, then drains the tasks in flight, so the rate counts all work done in
+    the measured wall time."""
+
+    def __init__(self, per_energy: int):
+        self.cores = os.cpu_count() or 1
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        import oracle_tools
+        oracle_tools.lib()  # build/load before starting workers
+        self.pool = mp.get_context("spawn").Pool(self.cores)
+        self.per_energy = per_energy
+        self.k = 0
+        self.n_per_task = 2
+
+    def _task(self):
+        e, rnd = self.k % 32, self.k // 32
+        self.k += 1
+        return (e, rnd * self.n_per_task, self.n_per_task, self.per_energy)
+
+    def sample(self, seconds: float):
+        done_traj = done_steps = 0
+        t0 = time.perf_counter()
+        pending = []
+        while True:
+            now = time.perf_counter()
+            still = []
+            for r in pending:
+                if r.ready():
+                    ntraj, nsteps, _ = r.get()
+                    done_traj += ntraj
+                    done_steps += nsteps
+                else:
+                    still.append(r)
+            pending = still
+            if now - t0 >= seconds:
+                break
+            while len(pending) < 2 * self.cores:
+                pending.append(self.pool.apply_async(_cpu_worker, (self._task(),)))
+            time.sleep(0.005)
+        for r in pending:
+            ntraj, nsteps, _ = r.get()
             done_traj += ntraj
             done_steps += nsteps
-            if time.perf_counter() - t0 > seconds:
-                pool.terminate()
-                break
-    wall = time.perf_counter() - t0
-    return {"value": done_traj / wall, "unit": UNIT, "cores": cores, "kind": "port",
-            "sample": f"{done_traj} trajectories ({done_steps} steps) of the 32-energy batch, round-robin over "
-                      f"energies, {wall:.1f} s wall on {cores} processes",
-            "steps_per_s": done_steps / wall}
+        wall = time.perf_counter() - t0
+        return {"value": done_traj / wall, "unit": UNIT, "cores": self.cores, "kind": "port",
+                "sample": f"{done_traj} trajectories ({done_steps} steps) of the 32-energy batch, round-robin over "
+                          f"energies, {wall:.1f} s wall on {self.cores} processes",
+                "steps_per_s": done_steps / wall}
+
+    def close(self):
+        self.pool.terminate()
+        self.pool.join()
+
+
+def cpu_sample(seconds: float = 20.0, per_energy: int = 1000):
+    leg = CpuLeg(per_energy)
+    try:
+        leg.sample(min(2.0, seconds))  # workers start and load the oracle
+        return leg.sample(seconds)
+    finally:
+        leg.close()
 
 
 # ---------------------------------------------------------------------------------------------
@@ -199,14 +236,16 @@ def main():
     if args.impl == "reference":
         if rank != 0:
             return
-        # warm-up: the oracle library build and a short run
-        cpu_sample(1.0, args.per_energy)
-        vals = []
-        for _ in range(args.steps):
-            vals.append(cpu_sample(max(5.0, args.cpu_seconds / max(args.steps, 1)), args.per_energy))
+        leg = CpuLeg(args.per_energy)
+        try:
+            for _ in range(args.warmup):  # workers start, load the oracle, reach steady state
+                leg.sample(1.0)
+            vals = [leg.sample(max(5.0, args.cpu_seconds / max(args.steps, 1))) for _ in range(args.steps)]
+        finally:
+            leg.close()
         v = sum(x["value"] for x in vals) / len(vals)
         line = {"impl": "reference", "metric": METRIC, "value": v, "unit": UNIT, "n_gpus": args.gpus,
-                "steps": args.steps, "warmup": 1, "ms_per_step": 1e3 / v * cfg["trajectories_per_step"],
+                "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 / v * cfg["trajectories_per_step"],
                 "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
                 "data": "synthetic (seeded Philox streams)", "config": cfg,
                 "cpu_baseline": {"value": v, "unit": UNIT, "cores": vals[0]["cores"], "kind": "port",
@@ -329,12 +368,16 @@ def main():
             "peak_source": "nominal FP32 FMA pipe: SMs x 128 lanes x 2 x sm_max_mhz of MEASURED_PEAKS.json "
                            "(the file has no FP32 figure; HBM and tensor peaks do not bound this kernel)",
             "traffic": None}
-    flop_step = FP32_FLOP_PER_STEP
-    if flop_step:
-        ach = steps_rate / world * flop_step / 1e12
-        roof.update({"achieved": ach, "frac": ach / fp32_peak, "flop_per_step": flop_step})
-    else:
-        roof.update({"achieved": None, "frac": None})
+    ach = steps_rate / world * FP32_FLOP_PER_STEP / 1e12
+    roof.update({"achieved": ach, "frac": ach / fp32_peak, "flop_per_step": FP32_FLOP_PER_STEP,
+                 "traffic": DRAM_BYTES_PER_TRAJ * traj_done / max(args.steps, 1) / world,
+                 "traffic_unit": "bytes per launch (ncu, scaled by trajectories)"})
+    # the binding resource: instruction issue (4 schedulers per SM, one warp instruction per cycle)
+    issue_peak = props.multi_processor_count * 4 * sm_max * 1e6
+    roof["issue"] = {"thread_inst_per_step": THREAD_INST_PER_STEP,
+                     "warp_inst_per_s_at_full_simt": steps_rate / world * THREAD_INST_PER_STEP / 32.0,
+                     "peak_warp_inst_per_s": issue_peak,
+                     "frac_at_full_simt": steps_rate / world * THREAD_INST_PER_STEP / 32.0 / issue_peak}
 
     clk = clocks.summary()
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,

@@ -450,6 +450,20 @@ __device__ __forceinline__ R time_proximity(R dt, R dmax, BndView<R> bv, int nbt
    return dt;
 }
 
+// Integrate's time-step check (src/trajectory_base.cc:979-983) of the previous step: dt against the
+// dmax of the point where that step ended. That point is where this step starts, so the dmax of
+// this step's field evaluation is the same number the reference compares with; a failed check
+// discards the attempt before anything else of this step happens.
+template <class R, class A>
+__device__ __forceinline__ bool prev_step_ok(Lane<R, A>& L, R dmax)
+{
+   if (L.steps > 0 && !(L.dt >= Lim<R>::tiny * dmax / c_code<R>())) {
+      L.status |= TRAJ_DISCARD;
+      return false;
+   }
+   return true;
+}
+
 // ---- Parker (src/trajectory_parker.cc:83-306) ----------------------------------------------
 template <int BG, class R>
 __device__ __noinline__ bool parker_divk_fd(const ProblemDescT<R>& P, int deriv_mode, R t, V3<R> pos, R p, R vmag,
@@ -492,6 +506,7 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, con
    SD<R> sp;
    const unsigned mask = traj_mask<kParker>() | (kappa_grad_is_analytic(P.df) ? kDerivedOnly : 0u);
    if (!get_fields<BG>(P.bg, deriv_mode, t, pos, p, mask, sp)) { L.status |= TRAJ_DISCARD; return; }
+   if (!prev_step_ok(L, sp.dmax)) return;
    R vmag = vel_of(p);
    // DiffusionCoeff (src/trajectory_parker.cc:83-153)
    Kap<R> K = kappa_pp(P.df, pos, p, vmag, kap_in(sp));
@@ -562,12 +577,7 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, con
    }
    if (sa != R(0)) L.amp += dts * sa * m_exp(L.wgt);
    handle_boundaries<kParker>(L, bv, sp, s0, P, Pd, S);
-   // the end point's dmax for the time-step check of Integrate
    L.steps++;
-   if (!(L.status & TRAJ_FINISH)) {
-      R dmax_end = eval_dmax<BG>(P.bg, (R)acc_val(L.t), val3<R>(L.pos));
-      if (!(L.dt >= Lim<R>::tiny * dmax_end / c_code<R>())) L.status |= TRAJ_DISCARD;
-   }
 }
 
 // ---- Runge-Kutta advance for Lorentz and Focused (src/trajectory_base.cc:315-406, 545-579) ----
@@ -644,6 +654,7 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
       L.status |= TRAJ_DISCARD;
       return;
    }
+   if (!prev_step_ok(L, sp.dmax)) return;
    V3<R> vel = vel_load<TT>(mom);
    V3<R> drift = mk(R(0), R(0), R(0));
    if (scatt) {
@@ -746,10 +757,6 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
    handle_boundaries<TT>(L, bv, sp, s0, P, Pd, S);
    if (!(L.status & TRAJ_FINISH) && TT == kFocused) clamp_mu<A, R>(L.mom);
    L.steps++;
-   if (!(L.status & TRAJ_FINISH)) {
-      R dmax_end = eval_dmax<BG>(P.bg, (R)acc_val(L.t), val3<R>(L.pos));
-      if (!(L.dt >= Lim<R>::tiny * dmax_end / c_code<R>())) L.status |= TRAJ_DISCARD;
-   }
 }
 
 // ---- SetStart (src/trajectory_base.cc:867-939 and overrides) -------------------------------
