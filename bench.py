@@ -272,7 +272,8 @@ def main():
     sim = open_problems(pbs, precision=capi.SPX_MIXED)
     if world > 1:
         shard.assign(sim, rank, RUNS_PER_RANK)
-    tun = capi.Tuning(0, 0, 0, 1)
+    # the launch shape: the project's autotuner, timed on a sample of this batch (set-up, untimed)
+    tun = sim.ctx.autotune(0)
     for _ in range(args.warmup):
         sim.MainLoop(tun)
     sim.ctx.reset_distributions()
@@ -300,7 +301,9 @@ def main():
     torch.cuda.synchronize(dev)
     wall = time.perf_counter() - t_wall0
     tuning = {"block_size": st.tuning.block_size, "blocks_per_sm": st.tuning.blocks_per_sm,
-              "steps_per_sync": st.tuning.steps_per_sync, "schedule": "persistent work queue"}
+              "steps_per_sync": st.tuning.steps_per_sync,
+              "schedule": "persistent work queue" if st.tuning.schedule == 1 else "one thread per trajectory",
+              "chosen_by": "spx_autotune"}
     sim.close()
     t_dev = sum(kms) / 1e3
     t_max = shard.max_over_ranks(t_dev) if world > 1 else t_dev

@@ -134,6 +134,13 @@ int spx_run(spx_ctx_t ctx, const spx_tuning* tuning);
 /* Wait for the last spx_run and report its statistics (stats may be NULL). */
 int spx_sync(spx_ctx_t ctx, spx_stats* stats);
 
+/* Choose the launch shape (block size, refill interval, schedule) by timing candidates on a sample
+ * of the context's problems: about sample_traj trajectories (0: two per resident lane), each
+ * stopped after 2048 steps, on separate buffers and random streams. spx_run with a NULL tuning
+ * then uses the fastest; best (may be NULL) receives it. No reference counterpart: the
+ * reference's MPI farm has no launch shape to tune. */
+int spx_autotune(spx_ctx_t ctx, int64_t sample_traj, spx_tuning* best);
+
 /* Size of the fixed device array spx_run_static works in (every GPU that loads the library holds
  * it until the process exits): 46 problems in SPX_MIXED, 72 in SPX_FP64. */
 #define SPX_STATIC_SCRATCH_BYTES (512u * 1024u)

@@ -25,7 +25,8 @@ SPX_OPT_RUN_INDEX = 6
 #: the symbols include/spx.h declares
 EXPORTS = ["spx_create", "spx_set_option", "spx_add_plugin", "spx_add_problem", "spx_run", "spx_sync",
            "spx_get_distribution_info", "spx_get_distribution", "spx_get_records", "spx_reset_distributions",
-           "spx_dump", "spx_restore", "spx_strerror", "spx_destroy", "spx_version", "spx_run_static"]
+           "spx_dump", "spx_restore", "spx_strerror", "spx_destroy", "spx_version", "spx_run_static",
+           "spx_autotune"]
 
 #: bytes of the fixed device array spx_run_static works in (SPX_STATIC_SCRATCH_BYTES)
 STATIC_SCRATCH_BYTES = 512 * 1024
@@ -84,6 +85,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         lib.spx_destroy.argtypes = [c_vp]
         lib.spx_destroy.restype = None
         lib.spx_version.restype = ctypes.c_char_p
+        lib.spx_autotune.argtypes = [c_vp, ctypes.c_int64, ctypes.POINTER(Tuning)]
         lib.spx_run_static.argtypes = [c_vp, ctypes.POINTER(Tuning), c_vp, ctypes.c_int64, c_vp, ctypes.c_int64, c_vp,
                                        ctypes.c_int64, c_vp, ctypes.c_int64, ctypes.POINTER(Stats)]
         _lib = lib
@@ -145,6 +147,13 @@ class Context:
 
     def run(self, tuning: Tuning | None = None) -> None:
         check(self.lib.spx_run(self._h, ctypes.byref(tuning) if tuning is not None else None), "spx_run")
+
+    def autotune(self, sample_traj: int = 0) -> Tuning:
+        """spx_autotune: time candidate launch shapes on a sample; later runs without a tuning use
+        the fastest."""
+        t = Tuning()
+        check(self.lib.spx_autotune(self._h, int(sample_traj), ctypes.byref(t)), "spx_autotune")
+        return t
 
     def sync(self) -> Stats:
         st = Stats()

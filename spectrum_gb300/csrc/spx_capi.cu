@@ -62,6 +62,16 @@ struct spx_ctx {
    bool launched = false;
    spx_stats last{};
    int sm_count = 0;
+   // spx_run replays one captured graph (counter reset, timing events, the step kernel); only the
+   // kernel's arguments change between runs (the run index), so they are updated in place
+   cudaGraph_t graph = nullptr;
+   cudaGraphExec_t gexec = nullptr;
+   cudaGraphNode_t gkernel = nullptr;
+   cudaKernelNodeParams gparams{};
+   unsigned char gkey[160] = {};
+   // launch shape chosen by spx_autotune (used by spx_run when it gets no tuning)
+   bool has_tuned = false;
+   spx_tuning tuned{};
 };
 
 namespace {
@@ -199,6 +209,106 @@ int bnd_slots(const spx_ctx* c)
 
 bool valid_ctx(spx_ctx* c) { return c != nullptr; }
 
+// What a captured graph depends on: launch shape, the run configuration apart from the run
+// index, and the device buffers. A different key means a new capture.
+struct GraphKey {
+   unsigned grid, block, slots;
+   int queue;
+   spx::RunConfig cfg;
+   const void* ptr[7];
+};
+static_assert(sizeof(GraphKey) <= sizeof(spx_ctx::gkey), "graph key does not fit");
+
+void graph_key(const spx::LaunchArgs& a, unsigned char* out)
+{
+   GraphKey k;
+   std::memset(&k, 0, sizeof k);
+   k.grid = a.grid.x;
+   k.block = a.block.x;
+   k.slots = (unsigned)a.bnd_slots;
+   k.queue = a.queue;
+   k.cfg = a.cfg;
+   k.cfg.run_index = 0;
+   const void* p[7] = {a.problems_r, a.problems_d, a.ctr, a.counts, a.sums, a.n_events, a.records};
+   std::memcpy(k.ptr, p, sizeof p);
+   std::memset(out, 0, sizeof(spx_ctx::gkey));
+   std::memcpy(out, &k, sizeof k);
+}
+
+void drop_graph(spx_ctx* c)
+{
+   if (c->gexec) cudaGraphExecDestroy(c->gexec);
+   if (c->graph) cudaGraphDestroy(c->graph);
+   c->gexec = nullptr;
+   c->graph = nullptr;
+   c->gkernel = nullptr;
+}
+
+// Capture [clear the run counters, start event, step kernel, stop event] on the context stream.
+int capture_graph(spx_ctx* c, const spx::LaunchArgs& a)
+{
+   drop_graph(c);
+   SPX_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+   cudaError_t e = cudaMemsetAsync(c->d_ctr, 0, sizeof(spx::RunCounters), c->stream);
+   if (e == cudaSuccess) e = cudaEventRecord(c->ev0, c->stream);
+   if (e == cudaSuccess) e = launch(c, a);
+   if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->stream);
+   cudaGraph_t g = nullptr;
+   cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
+   if (e == cudaSuccess) e = e2;
+   if (e != cudaSuccess) {
+      if (g) cudaGraphDestroy(g);
+      cudaGetLastError();
+      return cuda_err(e);
+   }
+   size_t n = 0;
+   SPX_CUDA(cudaGraphGetNodes(g, nullptr, &n));
+   std::vector<cudaGraphNode_t> nodes(n);
+   SPX_CUDA(cudaGraphGetNodes(g, nodes.data(), &n));
+   for (cudaGraphNode_t node : nodes) {
+      cudaGraphNodeType t;
+      SPX_CUDA(cudaGraphNodeGetType(node, &t));
+      if (t == cudaGraphNodeTypeKernel) {
+         c->gkernel = node;
+         SPX_CUDA(cudaGraphKernelNodeGetParams(node, &c->gparams));
+      }
+   }
+   c->graph = g;
+   if (c->gkernel == nullptr) return SPX_ERR_CUDA;
+   SPX_CUDA(cudaGraphInstantiate(&c->gexec, g, 0));
+   graph_key(a, c->gkey);
+   return SPX_OK;
+}
+
+// One run: replay the captured graph with this run's kernel arguments.
+int run_graph(spx_ctx* c, const spx::LaunchArgs& a)
+{
+   unsigned char key[sizeof(spx_ctx::gkey)];
+   graph_key(a, key);
+   if (c->gexec == nullptr || std::memcmp(key, c->gkey, sizeof key) != 0) {
+      int rc = capture_graph(c, a);
+      if (rc != SPX_OK) return rc;
+   }
+   // the step kernel's parameter list: (problems_r, problems_d, cfg, ctr, counts, sums, n_events,
+   // records, queue)
+   const void* pr = a.problems_r;
+   const spx::ProblemDesc* pd = a.problems_d;
+   spx::RunConfig cfg = a.cfg;
+   spx::RunCounters* ctr = a.ctr;
+   int32_t* counts = a.counts;
+   double* sums = a.sums;
+   unsigned long long* nev = a.n_events;
+   spx::TrajRecord* rec = a.records;
+   int queue = a.queue;
+   void* args[9] = {&pr, &pd, &cfg, &ctr, &counts, &sums, &nev, &rec, &queue};
+   cudaKernelNodeParams p = c->gparams;
+   p.kernelParams = args;
+   p.extra = nullptr;
+   SPX_CUDA(cudaGraphExecKernelNodeSetParams(c->gexec, c->gkernel, &p));
+   SPX_CUDA(cudaGraphLaunch(c->gexec, c->stream));
+   return SPX_OK;
+}
+
 }  // namespace
 
 extern "C" {
@@ -333,10 +443,19 @@ int spx_run(spx_ctx_t c, const spx_tuning* tuning)
    }
    spx_tuning tu{};
    if (tuning) tu = *tuning;
+   else if (c->has_tuned) tu = c->tuned;  // chosen by spx_autotune
+   else {
+      // untuned defaults: the FP64 drop-in keeps one thread per trajectory; the FP32 stepper takes
+      // the persistent queue with the shape that measured fastest on the modulation batch
+      tu.schedule = c->precision == SPX_MIXED ? 1 : 0;
+      if (tu.schedule) {
+         tu.block_size = 64;
+         tu.steps_per_sync = 8;
+      }
+   }
    if (tu.schedule != 0 && tu.schedule != 1) return SPX_ERR_INVALID_ARG;
    if (tu.block_size <= 0) tu.block_size = 128;
    if (tu.block_size % 32 || tu.block_size > 128) return SPX_ERR_INVALID_ARG;
-   if (!tuning) tu.schedule = c->precision == SPX_MIXED ? 1 : 0;
    if (tu.steps_per_sync <= 0) tu.steps_per_sync = tu.schedule ? 16 : 1 << 30;
    const int slots = bnd_slots(c);
    int occ = occupancy(c, tu.block_size, slots);
@@ -363,6 +482,7 @@ int spx_run(spx_ctx_t c, const spx_tuning* tuning)
    a.cfg.record_final = c->record_final;
    a.cfg.n_problems = (int)c->problems.size();
    a.cfg.steps_per_sync = tu.steps_per_sync;
+   a.cfg.step_cap = 0;
    a.cfg.total_traj = c->total_traj;
    a.cfg.run_index = c->run_index;
    a.ctr = c->d_ctr;
@@ -373,10 +493,8 @@ int spx_run(spx_ctx_t c, const spx_tuning* tuning)
    a.queue = tu.schedule;
    a.bnd_slots = slots;
    if (c->record_final && c->d_rec == nullptr) return SPX_ERR_STATE;
-   SPX_CUDA(cudaMemsetAsync(c->d_ctr, 0, sizeof(spx::RunCounters), c->stream));
-   SPX_CUDA(cudaEventRecord(c->ev0, c->stream));
-   SPX_CUDA(launch(c, a));
-   SPX_CUDA(cudaEventRecord(c->ev1, c->stream));
+   int grc = run_graph(c, a);
+   if (grc != SPX_OK) return grc;
    // ids of the next run continue after this one's (new random streams)
    for (const auto& p : c->problems)
       if ((uint64_t)(c->run_index + 2) * (uint64_t)p.n_traj > 0xffffffffull) return SPX_ERR_LIMIT;
@@ -385,6 +503,127 @@ int spx_run(spx_ctx_t c, const spx_tuning* tuning)
    c->last = spx_stats{};
    c->last.tuning = tu;
    c->last.kernel_launches = 1;
+   return SPX_OK;
+}
+
+// The autotuner: time candidate launch shapes on a sample of the context's problems (each problem
+// keeps its share of trajectories, every trajectory stops after a fixed number of steps) and keep
+// the fastest by accepted steps per second. The sample runs on buffers of its own with other
+// random streams, so the context's distributions and trajectory ids are untouched.
+int spx_autotune(spx_ctx_t c, int64_t sample_traj, spx_tuning* best)
+{
+   if (!valid_ctx(c)) return SPX_ERR_INVALID_ARG;
+   if (c->problems.empty()) return SPX_ERR_STATE;
+   SPX_CUDA(cudaSetDevice(c->device));
+   const int n = (int)c->problems.size();
+   const bool f64 = c->precision == SPX_FP64;
+   const int slots = bnd_slots(c);
+   if (sample_traj <= 0) sample_traj = (int64_t)c->sm_count * 4 * 128 * 2;  // about two per resident lane
+   int64_t total = 0;
+   for (const auto& p : c->problems) total += p.n_traj;
+   std::vector<spx::ProblemDesc> hd(n);
+   int64_t off_c = 0, off_s = 0, first = 0;
+   for (int k = 0; k < n; k++) {
+      hd[k] = c->problems[k].pd;
+      int64_t nk = std::max<int64_t>(1, (int64_t)((double)c->problems[k].n_traj * sample_traj / std::max<int64_t>(total, 1)));
+      hd[k].n_traj = nk;
+      hd[k].first = first;
+      hd[k].seed ^= 0x9E3779B97F4A7C15ull;
+      first += nk;
+      for (int d = 0; d < hd[k].nd; d++) {
+         int64_t nb = (int64_t)hd[k].d[d].n_bins[0] * hd[k].d[d].n_bins[1] * hd[k].d[d].n_bins[2];
+         hd[k].d[d].offset_counts = off_c;
+         hd[k].d[d].offset_sums = off_s;
+         off_c += nb;
+         off_s += nb * hd[k].d[d].width;
+      }
+   }
+   struct DevBuf {
+      void* p = nullptr;
+      ~DevBuf() { cudaFree(p); }
+   } b_pd, b_pr, b_ctr, b_counts, b_sums, b_nev;
+   SPX_CUDA(cudaMalloc(&b_pd.p, sizeof(spx::ProblemDesc) * n));
+   SPX_CUDA(cudaMalloc(&b_pr.p, f64 ? sizeof(spx::ProblemDesc) * n : sizeof(spx::ProblemDescT<float>) * n));
+   SPX_CUDA(cudaMalloc(&b_ctr.p, sizeof(spx::RunCounters)));
+   SPX_CUDA(cudaMalloc(&b_counts.p, sizeof(int32_t) * std::max<int64_t>(off_c, 1)));
+   SPX_CUDA(cudaMalloc(&b_sums.p, sizeof(double) * std::max<int64_t>(off_s, 1)));
+   SPX_CUDA(cudaMalloc(&b_nev.p, sizeof(unsigned long long) * n * spx::kMaxDistro));
+   SPX_CUDA(cudaMemcpy(b_pd.p, hd.data(), sizeof(spx::ProblemDesc) * n, cudaMemcpyHostToDevice));
+   if (f64) SPX_CUDA(cudaMemcpy(b_pr.p, hd.data(), sizeof(spx::ProblemDesc) * n, cudaMemcpyHostToDevice));
+   else {
+      std::vector<spx::ProblemDescT<float>> hf(n);
+      for (int k = 0; k < n; k++) spx::convert_problem(hd[k], hf[k]);
+      SPX_CUDA(cudaMemcpy(b_pr.p, hf.data(), sizeof(spx::ProblemDescT<float>) * n, cudaMemcpyHostToDevice));
+   }
+
+   // candidates: the persistent work queue at three block sizes and four refill intervals (two of
+   // each for FP64, whose samples take longer); the plain grid as well for FP64, the drop-in's
+   // own schedule
+   std::vector<spx_tuning> cands;
+   if (f64) {
+      for (int bs : {128, 64})
+         for (int sps : {4, 16}) cands.push_back(spx_tuning{bs, 0, sps, 1});
+      cands.push_back(spx_tuning{128, 0, 1 << 30, 0});
+      cands.push_back(spx_tuning{64, 0, 1 << 30, 0});
+   }
+   else {
+      for (int bs : {128, 64, 32})
+         for (int sps : {2, 4, 8, 16}) cands.push_back(spx_tuning{bs, 0, sps, 1});
+   }
+   double best_rate = -1.0;
+   spx_tuning best_tu = cands[0];
+   for (spx_tuning tu : cands) {
+      int occ = occupancy(c, tu.block_size, slots);
+      if (occ <= 0) continue;
+      tu.blocks_per_sm = occ;
+      int64_t grid = tu.schedule == 1 ? (int64_t)c->sm_count * occ : (first + tu.block_size - 1) / tu.block_size;
+      spx::LaunchArgs a;
+      a.block = dim3(tu.block_size);
+      a.grid = dim3((unsigned)std::max<int64_t>(1, std::min<int64_t>(grid, 0x7fffffff)));
+      a.stream = c->stream;
+      a.problems_r = b_pr.p;
+      a.problems_d = static_cast<const spx::ProblemDesc*>(b_pd.p);
+      a.cfg.traj_kind = c->traj;
+      a.cfg.time_flow = c->flow;
+      a.cfg.rk = c->rk;
+      a.cfg.deriv_mode = c->deriv_mode;
+      a.cfg.pa_scattering = c->pa_scattering;
+      a.cfg.max_attempts = c->max_attempts;
+      a.cfg.steps_per_orbit = c->steps_per_orbit;
+      a.cfg.steps_per_orbit_f = (float)c->steps_per_orbit;
+      a.cfg.record_final = 0;
+      a.cfg.n_problems = n;
+      a.cfg.steps_per_sync = tu.steps_per_sync;
+      a.cfg.step_cap = 2048;
+      a.cfg.total_traj = first;
+      a.cfg.run_index = 0;
+      a.ctr = static_cast<spx::RunCounters*>(b_ctr.p);
+      a.counts = static_cast<int32_t*>(b_counts.p);
+      a.sums = static_cast<double*>(b_sums.p);
+      a.n_events = static_cast<unsigned long long*>(b_nev.p);
+      a.records = nullptr;
+      a.queue = tu.schedule;
+      a.bnd_slots = slots;
+      SPX_CUDA(cudaMemsetAsync(b_ctr.p, 0, sizeof(spx::RunCounters), c->stream));
+      SPX_CUDA(cudaEventRecord(c->ev0, c->stream));
+      SPX_CUDA(launch(c, a));
+      SPX_CUDA(cudaEventRecord(c->ev1, c->stream));
+      SPX_CUDA(cudaStreamSynchronize(c->stream));
+      float ms = 0.0f;
+      SPX_CUDA(cudaEventElapsedTime(&ms, c->ev0, c->ev1));
+      spx::RunCounters h;
+      SPX_CUDA(cudaMemcpy(&h, b_ctr.p, sizeof h, cudaMemcpyDeviceToHost));
+      double rate = ms > 0.0f ? (double)h.steps / ms : 0.0;
+      if (rate > best_rate) {
+         best_rate = rate;
+         best_tu = tu;
+      }
+   }
+   if (best_rate <= 0.0) return SPX_ERR_CUDA;
+   c->tuned = best_tu;
+   c->has_tuned = true;
+   c->launched = false;  // the timing events now describe a sample, not an spx_run
+   if (best) *best = best_tu;
    return SPX_OK;
 }
 
@@ -568,6 +807,7 @@ void spx_destroy(spx_ctx_t c)
 {
    if (!c) return;
    if (c->stream) cudaStreamSynchronize(c->stream);
+   drop_graph(c);
    free_buffers(c);
    if (c->ev0) cudaEventDestroy(c->ev0);
    if (c->ev1) cudaEventDestroy(c->ev1);
@@ -712,6 +952,7 @@ int spx_run_static(spx_ctx_t c, const spx_tuning* tuning, int32_t* counts, int64
    a.cfg.record_final = c->record_final;
    a.cfg.n_problems = n;
    a.cfg.steps_per_sync = tu.steps_per_sync;
+   a.cfg.step_cap = 0;
    a.cfg.total_traj = total;
    a.cfg.run_index = c->run_index;
    a.ctr = reinterpret_cast<spx::RunCounters*>(scratch);

@@ -172,3 +172,31 @@ def test_cpp_application_equals_python_path(built_lib, tmp_path):
         counts, sums, _ = res.distros[k][0]
         assert int(rows[k][2]) == int(counts.sum()), k
         assert math.isclose(float(rows[k][3]), float(sums[:, 0].sum()), rel_tol=1e-9), k
+
+
+@pytest.mark.parametrize("precision", [capi.SPX_MIXED, capi.SPX_FP64])
+def test_autotune_changes_speed_not_results(built_lib, precision):
+    """spx_autotune picks a launch shape from timed samples; runs with it give the same
+    trajectories as runs with the default shape (results do not depend on the schedule)."""
+    from spectrum_gb300.simulation import open_problems
+    pbs = workloads.gcr_modulation(n_traj=400, energies_mev=[100.0, 1000.0], t_max_years=0.1)
+    a = open_problems(pbs, precision=precision, record=True, deriv_mode=1)
+    b = open_problems(pbs, precision=precision, record=True, deriv_mode=1)
+    try:
+        st_a = a.MainLoop()
+        tuned = b.ctx.autotune(20000)
+        assert tuned.block_size in (64, 128) and tuned.schedule in (0, 1)
+        st_b = b.MainLoop()
+        assert (st_b.tuning.block_size, st_b.tuning.steps_per_sync, st_b.tuning.schedule) == \
+               (tuned.block_size, tuned.steps_per_sync, tuned.schedule)
+        assert st_a.trajectories == st_b.trajectories and st_a.steps == st_b.steps
+        for k, p in enumerate(pbs):
+            ra, rb = a.ctx.records(k, p.n_traj), b.ctx.records(k, p.n_traj)
+            for f in ("steps", "status", "t", "pos", "mom"):
+                assert np.array_equal(ra[f], rb[f]), (k, f)
+            ca, _, na = a.ctx.distribution(k, 0)
+            cb, _, nb = b.ctx.distribution(k, 0)
+            assert na == nb and np.array_equal(ca, cb)
+    finally:
+        a.close()
+        b.close()
