@@ -68,3 +68,39 @@ def test_diffusion_uniform_gaussian_spread(built_lib):
         t = gpu.records[0]["t"].mean()
         sigma = 2.0 * t * np.sqrt(2.0 / len(x))  # std of the sample second moment of N(0, 2t)
         assert np.all(np.abs(var - 2.0 * t) < 4.0 * sigma), (var, t)
+
+
+def _within_3sigma(a, b, min_count=20):
+    """Per-bin agreement of two histograms within 3 sigma of Poisson noise (bins with enough counts
+    in either)."""
+    a = np.asarray(a, dtype=float)
+    b = np.asarray(b, dtype=float)
+    m = (a + b) >= min_count
+    sig = np.sqrt(a[m] + b[m])
+    return m.sum(), np.abs(a[m] - b[m]) <= 3.0 * sig
+
+
+def test_fp32_position_histogram_within_3sigma_of_oracle(built_lib):
+    """The FP32 stepper's 3-D position histogram, reduced to each axis, against the oracle's
+    (FP64, the reference's algorithm) on the same trajectories: populated bins within 3 sigma."""
+    pb = workloads.diffusion_uniform(n_traj=20_000, t_end=0.5)
+    gpu = run_problems(pb, precision=capi.SPX_MIXED)
+    ref = ot.run_oracle(pb, record=False)
+    g3 = gpu.distros[0][0][0].reshape(100, 100, 100)
+    r3 = ref.distros[0][0].reshape(100, 100, 100)
+    for axis in range(3):
+        other = tuple(i for i in range(3) if i != axis)
+        n, ok = _within_3sigma(g3.sum(axis=other), r3.sum(axis=other))
+        assert n > 20 and ok.mean() >= 0.99, (axis, n, ok.mean())
+
+
+def test_fp32_modulation_spectrum_within_3sigma_of_oracle(built_lib):
+    """LIS-weighted modulation counts and exit-time histogram of the FP32 stepper against the oracle
+    (FP64, analytic field derivatives), per bin within 3 sigma."""
+    pbs = workloads.gcr_modulation(n_traj=300, energies_mev=[200.0, 2000.0], t_max_years=0.2)
+    gpu = run_problems(pbs, precision=capi.SPX_MIXED)
+    for k, pb in enumerate(pbs):
+        ref = ot.run_oracle(pb, deriv_mode=1, record=False)
+        for d in range(2):
+            n, ok = _within_3sigma(gpu.distros[k][d][0], ref.distros[d][0], min_count=10)
+            assert n >= 1 and ok.all(), (k, d, gpu.distros[k][d][0], ref.distros[d][0])
