@@ -248,11 +248,14 @@ void drop_graph(spx_ctx* c)
 int capture_graph(spx_ctx* c, const spx::LaunchArgs& a)
 {
    drop_graph(c);
+   cudaGetLastError();  // a launch check below must not report an earlier call's error
    SPX_CUDA(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
    cudaError_t e = cudaMemsetAsync(c->d_ctr, 0, sizeof(spx::RunCounters), c->stream);
-   if (e == cudaSuccess) e = cudaEventRecord(c->ev0, c->stream);
+   // inside a capture a plain event record only orders streams; the timing events must become
+   // event-record nodes of the graph
+   if (e == cudaSuccess) e = cudaEventRecordWithFlags(c->ev0, c->stream, cudaEventRecordExternal);
    if (e == cudaSuccess) e = launch(c, a);
-   if (e == cudaSuccess) e = cudaEventRecord(c->ev1, c->stream);
+   if (e == cudaSuccess) e = cudaEventRecordWithFlags(c->ev1, c->stream, cudaEventRecordExternal);
    cudaGraph_t g = nullptr;
    cudaError_t e2 = cudaStreamEndCapture(c->stream, &g);
    if (e == cudaSuccess) e = e2;
