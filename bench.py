@@ -215,6 +215,80 @@ def per_bin_error(a, b, min_count):
     return worst_c, worst_s, nb
 
 
+# Throughput of the other workload families, for the per-family figures of the design doc. Each entry:
+# builder of the problem list (FP32 run), its description, and the share of it the FP64 plain
+# kernel runs for the ratio.
+def _other_workloads():
+    from spectrum_gb300 import units as U
+    from spectrum_gb300 import workloads as W
+    return {
+        "diffusion": (lambda: [W.diffusion_uniform(n_traj=1_000_000)],
+                      "Parker fwd, uniform B, kappa = 1, t = 1 (1,000 steps each): 1e6 trajectories "
+                      "(10x the named 1e5, so one launch lasts long enough to time)", 0.1),
+        "shock": (lambda: [W.shock_acceleration(n_traj=200_000, x_downstream=40.0, p_max=1.0e3)],
+                  "Parker fwd, smooth shock s = 4, width 1e-3: 2e5 of the named 1e7 trajectories", 0.05),
+        "dipole": (lambda: [W.dipole_orbits(n_traj=1_000_000, t_end=1.0 / U.unit_time)],
+                   "Lorentz RK4 in the dipole, 1e6 protons 1-100 MeV, L 2-6, 32 steps per gyro-orbit, for 1 s "
+                   "of flight (100 drift periods take ~3e8 steps for the slowest trajectory)", 0.01),
+        "focused": (lambda: W.focused_transport(n_problems=64, n_traj=20_000, t_max_hours=0.5),
+                    "Focused RK4 + pitch-angle scattering, 64 problems (mean free paths 0.01-1 AU, 1-100 MeV) of "
+                    "2e4 trajectories each, 0.5 h of the named 48 h", 0.05),
+    }
+
+
+OTHER_WORKLOADS = ("diffusion", "shock", "dipole", "focused")
+
+
+def bench_other(args, rank, world, local):
+    """One line per run: FP32 batched trajectories/s and steps/s of another workload family, and the
+    plain FP64 kernel on a share of the same trajectories."""
+    import torch
+    from spectrum_gb300 import capi
+    from spectrum_gb300.simulation import open_problems
+    dev = torch.device("cuda", local)
+    torch.cuda.set_device(dev)
+    build, desc, share = _other_workloads()[args.workload]
+    pbs = build()
+    sim = open_problems(pbs, precision=capi.SPX_MIXED)
+    tun = sim.ctx.autotune(0)
+    for _ in range(args.warmup):
+        sim.MainLoop(tun)
+    kms, traj, steps = [], 0, 0
+    for _ in range(args.steps):
+        flush_l2(torch, dev)
+        st = sim.MainLoop(tun)
+        kms.append(st.kernel_ms)
+        traj += st.trajectories
+        steps += st.steps
+    sim.close()
+    t = sum(kms) / 1e3
+    line = {"metric": f"SDE trajectories/s, {args.workload} workload, batched FP32, 1 GB300",
+            "value": traj / t, "unit": UNIT, "steps_per_s": steps / t, "n_gpus": 1, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": t / args.steps * 1e3, "higher_is_better": True,
+            "dtype": "f32 (float-float accumulation)", "data": "synthetic (seeded Philox streams)",
+            "config": {"workload": args.workload, "description": desc, "problems": len(pbs),
+                       "trajectories_per_step": sum(p.n_traj for p in pbs), "l2": "flushed between steps"},
+            "tuning": {"block_size": tun.block_size, "steps_per_sync": tun.steps_per_sync, "schedule": tun.schedule}}
+    if not args.no_fp64:
+        sub = build()
+        for p in sub:
+            p.n_traj = max(1, int(p.n_traj * share))
+        s64 = open_problems(sub, precision=capi.SPX_FP64, deriv_mode=1)
+        flush_l2(torch, dev)
+        st64 = s64.MainLoop(capi.Tuning(0, 0, 1, 0))
+        s64.close()
+        s32 = open_problems(sub, precision=capi.SPX_MIXED)
+        flush_l2(torch, dev)
+        st32 = s32.MainLoop(tun)
+        s32.close()
+        line["fp64_plain"] = {"trajectories": st64.trajectories, "value": st64.trajectories / st64.kernel_ms * 1e3,
+                              "steps_per_s": st64.steps / st64.kernel_ms * 1e3,
+                              "ratio_fp32_batched_over_fp64_plain": (st32.trajectories / st32.kernel_ms) /
+                                                                    (st64.trajectories / st64.kernel_ms)}
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -226,8 +300,13 @@ def main():
                     help="trajectories per energy of the FP64 comparison (every fourth energy)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--workload", default="gcr", choices=["gcr"] + sorted(OTHER_WORKLOADS),
+                    help="gcr: the headline modulation batch; the others print throughput lines for the "
+                         "other workload families (shortened where the full configuration takes hours)")
     args = ap.parse_args()
     rank, world, local = rank_info()
+    if args.workload != "gcr":
+        return bench_other(args, rank, world, local)
     cfg = {"workload": WORKLOAD, "energies": 32, "per_energy": args.per_energy,
            "trajectories_per_step": 32 * args.per_energy * world, "time_flow": "backward", "background": "solar wind",
            "diffusion": "kappa_par = lam v/3 (R/1GV)^0.5 (B/5nT)^-1, kappa_perp = 0.02 kappa_par",
