@@ -6,7 +6,9 @@
  *   D1 BackgroundSmoothShock::EvaluateDmax (src/background_smooth_shock.cc:193-197) uses the
  *      shock distance of the *previous* field evaluation of the object (it runs before
  *      EvaluateBackground in BackgroundBase::GetFields, src/background_base.cc:434-442); here it
- *      is the distance at the current point.
+ *      is the distance at the current point. With opts->reference_quirks the reference's
+ *      behaviour is reproduced instead (the object's distance persists across the trajectories of
+ *      a run; it starts at 0), so the restatement can be compared with the reference bit for bit.
  *   D2 DistributionTemplated::AddEvent (src/distribution_templated.cc:145-181) computes a
  *      negative bin for left outliers beyond one bin width when bin_outside is set; here such
  *      events go to bin 0, which is what the code intends.
@@ -669,6 +671,9 @@ typedef struct {
    double Dmumu, Vmu;
    /* SourceMomentumInjection state (del_mom_old, src/source_other.cc:113-119) */
    double src_del_old;
+   /* BackgroundSmoothShock::ds_shock of the last field evaluation; like the reference's background
+      object it lives on across the trajectories of a run (used with reference_quirks, D1) */
+   double bg_ds_prev;
    /* distributions */
    int32_t* counts;
    double* sums;
@@ -899,8 +904,12 @@ static int get_fields(trj_t* T, double t, v3 pos, v3 mom_pmu, unsigned mask, spd
    double ds = 0.0;
    int i;
    s->mask = mask;
-   s->dmax = eval_dmax(g, t, pos);
+   if (g->kind == BG_SMOOTHSHOCK && T->o->reference_quirks)  /* D1 as the reference has it */
+      s->dmax = fmin(g->dmax_fraction * g->width * fmax(1.0, fabs(T->bg_ds_prev)), g->dmax0);
+   else
+      s->dmax = eval_dmax(g, t, pos);
    eval_bg(g, t, pos, mask, s, &ds);
+   if (g->kind == BG_SMOOTHSHOCK) T->bg_ds_prev = ds;
    if (mask & BG_B) {
       s->Bmag = vnorm(s->B);
       if (s->Bmag < SP_TINY) return 1;

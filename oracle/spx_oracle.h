@@ -37,6 +37,9 @@ typedef struct {
    double steps_per_orbit; /* Lorentz orbit resolution (reference: 100, src/trajectory_lorentz.hh:26) */
    int pa_scattering;      /* Focused: add the Euler pitch-angle scattering step */
    int max_attempts;       /* retries of a discarded trajectory (src/simulation.cc:262-288) */
+   int reference_quirks;   /* 1: reproduce deviation D1 as the reference has it (the smooth shock's dmax
+                              from the previous field evaluation), to compare with the reference's own
+                              output; 0: the corrected behaviour the CUDA kernels share */
 } spx_oracle_opts;
 
 /*

@@ -27,7 +27,7 @@ TRAJ_DTYPE = np.dtype([("attempts", "<u4"), ("status", "<u4"), ("steps", "<u8"),
 class _Opts(ctypes.Structure):
     _fields_ = [("traj_type", ctypes.c_int), ("time_flow", ctypes.c_int), ("rk", ctypes.c_int),
                 ("deriv_mode", ctypes.c_int), ("steps_per_orbit", ctypes.c_double),
-                ("pa_scattering", ctypes.c_int), ("max_attempts", ctypes.c_int)]
+                ("pa_scattering", ctypes.c_int), ("max_attempts", ctypes.c_int), ("reference_quirks", ctypes.c_int)]
 
 
 def build_oracle() -> str:
@@ -67,7 +67,8 @@ class OracleResult:
 
 
 def run_oracle(problem, first: int = 0, n: int | None = None, deriv_mode: int = 0, steps_per_orbit: float | None = None,
-               pa_scattering: int | None = None, max_attempts: int = 100, record: bool = True) -> OracleResult:
+               pa_scattering: int | None = None, max_attempts: int = 100, record: bool = True,
+               reference_quirks: int = 0) -> OracleResult:
     """Run the C restatement on ``problem`` (a spectrum_gb300.problem.Problem)."""
     from spectrum_gb300.workloads import SPX_OPT_PA_SCATTERING, SPX_OPT_STEPS_PER_ORBIT
     if steps_per_orbit is None:
@@ -77,14 +78,16 @@ def run_oracle(problem, first: int = 0, n: int | None = None, deriv_mode: int = 
     return run_oracle_spec(problem.to_spec(), problem.traj, problem.time_flow, problem.rk,
                            problem.n_traj if n is None else n, first=first, deriv_mode=deriv_mode,
                            steps_per_orbit=steps_per_orbit, pa_scattering=pa_scattering, max_attempts=max_attempts,
-                           record=record)
+                           record=record, reference_quirks=reference_quirks)
 
 
 def run_oracle_spec(spec: bytes, traj_kind: int, time_flow: int, rk: int, n: int, first: int = 0, deriv_mode: int = 0,
                     steps_per_orbit: float = 100.0, pa_scattering: int = 0, max_attempts: int = 100,
-                    record: bool = True) -> OracleResult:
-    """Run the C restatement on a problem spec (the bytes Problem.to_spec() makes)."""
-    opts = _Opts(traj_kind, time_flow, rk, deriv_mode, float(steps_per_orbit), int(pa_scattering), max_attempts)
+                    record: bool = True, reference_quirks: int = 0) -> OracleResult:
+    """Run the C restatement on a problem spec (the bytes Problem.to_spec() makes). With
+    reference_quirks=1 the listed deviation D1 is reproduced as the reference has it."""
+    opts = _Opts(traj_kind, time_flow, rk, deriv_mode, float(steps_per_orbit), int(pa_scattering), max_attempts,
+                 int(reference_quirks))
     sizes = distro_sizes(spec)
     tot = sum(s for s, _ in sizes)
     counts = np.zeros(max(tot, 1), dtype=np.int32)
@@ -138,10 +141,10 @@ def load_golden(name: str):
     return fx, OracleResult(fx["traj"], distros)
 
 
-def run_oracle_golden(fx, deriv_mode: int = 0) -> OracleResult:
+def run_oracle_golden(fx, deriv_mode: int = 0, reference_quirks: int = 0) -> OracleResult:
     return run_oracle_spec(fx["spec"].tobytes(), int(fx["traj_kind"]), int(fx["time_flow"]), int(fx["rk"]),
                            int(fx["n_traj"]), deriv_mode=deriv_mode, steps_per_orbit=float(fx["steps_per_orbit"]),
-                           pa_scattering=int(fx["pa_scattering"]))
+                           pa_scattering=int(fx["pa_scattering"]), reference_quirks=reference_quirks)
 
 
 def oracle_normals(seed, index, traj, problem=0, attempt=0):

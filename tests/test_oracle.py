@@ -61,31 +61,28 @@ def _assert_same(a: ot.OracleResult, b: ot.OracleResult):
         assert np.array_equal(sa, sb)
 
 
-# The smooth shock's spatial step limit is one of the oracle's listed deviations (D1 in
-# oracle/spx_oracle.c): the reference evaluates it from the shock distance of the previous field
-# evaluation, the oracle from the current one, so paths part after the first steps near the shock.
-DEVIATING = {"parker_fwd_smoothshock"}
-
-
-@pytest.mark.parametrize("name", [n for n in ot.golden_names() if n not in DEVIATING])
+@pytest.mark.parametrize("name", ot.golden_names())
 def test_oracle_matches_golden(name):
     """Bit-exact: every trajectory's attempts, status, steps, final and initial state and
-    weights, and every distribution bin, equal the reference's output for the same spec."""
+    weights, and every distribution bin, equal the reference's output for the same spec. The
+    oracle runs with its listed deviations reproduced as the reference has them (only D1, the
+    smooth shock's step limit, applies to these fixtures)."""
     fx, ref = ot.load_golden(name)
-    got = ot.run_oracle_golden(fx)
+    got = ot.run_oracle_golden(fx, reference_quirks=1)
     _assert_same(got, ref)
 
 
-def test_oracle_smoothshock_golden_up_to_d1():
-    """Same initial states and the same outcome (boundary class) per trajectory; the paths differ
-    through deviation D1 only."""
+def test_oracle_smoothshock_deviation_d1():
+    """Without the quirk the smooth shock's step limit uses the current shock distance (D1, the
+    behaviour the CUDA kernels share): the same initial states and outcomes per trajectory, paths
+    that part after the first steps near the shock."""
     fx, ref = ot.load_golden("parker_fwd_smoothshock")
     got = ot.run_oracle_golden(fx)
     for f in ("attempts", "t0", "pos0", "mom0"):
         assert np.array_equal(got.traj[f], ref.traj[f]), f
     assert np.array_equal(got.traj["status"] & OUTCOME, ref.traj["status"] & OUTCOME)
-    # the escape side (upstream or downstream plane) agrees trajectory by trajectory
     assert np.array_equal(np.sign(got.traj["pos"][:, 0]), np.sign(ref.traj["pos"][:, 0]))
+    assert not np.array_equal(got.traj["steps"], ref.traj["steps"])
 
 
 def test_golden_fixtures_cover_every_trajectory_family():
@@ -121,3 +118,12 @@ def test_oracle_first_offset_is_a_slice():
     part = ot.run_oracle(pb, first=25, n=15)
     for f in full.traj.dtype.names:
         assert np.array_equal(full.traj[f][25:], part.traj[f]), f
+
+
+@needs_ref
+def test_oracle_matches_reference_live_smoothshock():
+    """A shock set-up the fixtures do not hold (compression 3, other seed), run by the reference and
+    by the oracle with D1 reproduced: bit for bit."""
+    pb = workloads.shock_acceleration(n_traj=6, s=3.0, x_escape=-1.5, x_downstream=1.5, p_max=8.0)
+    pb.seed = 4242
+    _assert_same(ot.run_oracle(pb, reference_quirks=1), ot.run_reference(pb))
