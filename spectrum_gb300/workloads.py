@@ -228,8 +228,8 @@ def focused_transport(n_problems: int = 64, n_min: int = 1000, n_max: int = 1_00
     per problem (log-uniform draw in [1, 100] MeV), mean free path log-uniform in [0.01, 1] AU,
     trajectory count log-uniform in [1e3, 1e6]; an observer sphere at 1 AU records (t, mu) of
     every crossing (256 x 32 bins). Pitch-angle scattering uses D_mumu = D0 (1 - mu^2)
-    (src/diffusion_other.cc:64-79) with D0 = v / lambda: then kappa_par =
-    (v^2/4) int (1-mu^2)^2 / D_mumu dmu = v^2 / (3 D0), so the parallel mean free path
+    (src/diffusion_other.cc:64-79) with D0 = v / (2 lambda): then kappa_par =
+    (v^2/8) int (1-mu^2)^2 / D_mumu dmu = v^2 / (6 D0), so the parallel mean free path
     3 kappa_par / v equals lambda.
     The parameters of problem p come from a fixed-seed generator so the batch is reproducible.
     """
@@ -243,7 +243,7 @@ def focused_transport(n_problems: int = 64, n_min: int = 1000, n_max: int = 1_00
         e = math.exp(rnd.uniform(math.log(e_mev[0]), math.log(e_mev[1])))
         p0 = U.mev_to_mom(e)
         v = U.Vel(p0)
-        d0 = v / lam
+        d0 = v / (2.0 * lam)
         pb = Problem(traj=TRAJ_FOCUSED, time_flow=FORWARD, rk=25, seed=SEED_BASE + seed_offset,
                      n_traj=n_traj if n_traj is not None else count, problem_id=p_idx)
         pb.AddBackground(BackgroundSolarWind(), solarwind_params(DataContainer()))

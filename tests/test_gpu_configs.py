@@ -200,3 +200,65 @@ def test_autotune_changes_speed_not_results(built_lib, precision):
     finally:
         a.close()
         b.close()
+
+
+def test_pitch_angle_scattering_parallel_diffusion(built_lib):
+    """Focused transport with isotropic scattering D_mumu = D0 (1 - mu^2) in a uniform field: the
+    spread along the field is that of a diffusion with kappa_par = v^2 / (6 D0)
+    (benchmarks/main_test_pa_scatt.cc:252; the standard (v^2/8) int (1-mu^2)^2 / D_mumu dmu),
+    including the ballistic start, <z^2> = 2 kappa (t - tau (1 - exp(-t / tau))), tau = 1 / (2 D0)."""
+    from spectrum_gb300.datacontainer import DataContainer as DC
+    from spectrum_gb300.plugins import (BackgroundUniform, BoundaryTimeExpire, DiffusionIsotropicConstant,
+                                        DistributionTimeUniform, InitialMomentumShell, InitialSpaceFixed,
+                                        InitialTimeFixed)
+    from spectrum_gb300.problem import FORWARD, TRAJ_FOCUSED, Problem, distro_header
+    d0, t_end, p0 = 1.0, 20.0, 1.0
+    pb = Problem(traj=TRAJ_FOCUSED, time_flow=FORWARD, rk=25, seed=91, n_traj=20_000)
+    pb.AddBackground(BackgroundUniform(), DC().double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0, 0, 1.0)).double(1.0e3))
+    pb.AddInitial(InitialTimeFixed(), DC().double(0.0))
+    pb.AddInitial(InitialSpaceFixed(), DC().vec((0, 0, 0)))
+    pb.AddInitial(InitialMomentumShell(), DC().double(p0))
+    pb.AddDiffusion(DiffusionIsotropicConstant(), DC().double(d0))
+    pb.AddBoundary(BoundaryTimeExpire(), workloads._boundary(DC(), 1, [0]).double(t_end))
+    c = distro_header(DC(), (4, 0, 0), (0.0, 0, 0), (t_end * 1.01, 0, 0))
+    c.double(1.0).double(0.0).int(1)
+    pb.AddDistribution(DistributionTimeUniform(), c)
+    pb.options[workloads.SPX_OPT_PA_SCATTERING] = 1.0
+    v = units.Vel(p0)
+    kappa = v * v / (6.0 * d0)
+    tau = 1.0 / (2.0 * d0)
+    for prec in (capi.SPX_MIXED, capi.SPX_FP64):
+        rec = run_problems(pb, precision=prec, record=True).records[0]
+        t = rec["t"].mean()
+        z2 = (rec["pos"][:, 2] ** 2).mean()
+        expect = 2.0 * kappa * (t - tau * (1.0 - math.exp(-t / tau)))
+        assert abs(z2 / expect - 1.0) < 0.05, (prec, z2, expect)
+
+
+def test_dipole_drift_period(built_lib):
+    """10 MeV protons at L = 4 with 90 degree pitch drift westward around the dipole with the period
+    3600 s * 1.05 / (E_MeV L (1 + 0.43 sin theta_eq)) of the reference's benchmark
+    (benchmarks/main_test_dipole_periods.cc:129): after a quarter period the azimuth, averaged over
+    gyrophases, has turned by -pi/2 to within a few percent; |p| is conserved."""
+    from spectrum_gb300.datacontainer import DataContainer as DC
+    from spectrum_gb300.plugins import InitialMomentumRing, InitialSpaceFixed, InitialTimeFixed
+    from spectrum_gb300.problem import Problem
+    e_mev, L = 10.0, 4.0
+    t_drift = 3600.0 * 1.05 / (e_mev * L * 1.43) / units.unit_time
+    src = workloads.dipole_orbits(n_traj=4000, t_end=0.25 * t_drift)
+    r_e = workloads.R_EARTH_CM / units.unit_length
+    pb = Problem(traj=src.traj, time_flow=src.time_flow, rk=src.rk, seed=17, n_traj=4000)
+    for e in src.plugins:
+        if not type(e.plugin).__name__.startswith("Initial"):
+            pb.plugins.append(e)
+    pb.AddInitial(InitialTimeFixed(), DC().double(0.0))
+    pb.AddInitial(InitialSpaceFixed(), DC().vec((L * r_e, 0.0, 0.0)))
+    pb.AddInitial(InitialMomentumRing(), DC().double(units.mev_to_mom(e_mev)).double(0.5 * math.pi))
+    pb.options.update(src.options)
+    for prec in (capi.SPX_MIXED, capi.SPX_FP64):
+        rec = run_problems(pb, precision=prec, record=True).records[0]
+        phi = np.arctan2(rec["pos"][:, 1], rec["pos"][:, 0])
+        frac = phi.mean() / (-0.5 * math.pi * rec["t"].mean() / (0.25 * t_drift))
+        assert abs(frac - 1.0) < 0.05, (prec, phi.mean(), frac)
+        p = np.linalg.norm(rec["mom"], axis=1)
+        assert np.max(np.abs(p / np.linalg.norm(rec["mom0"], axis=1) - 1.0)) < 1e-4
