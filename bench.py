@@ -225,8 +225,9 @@ def _other_workloads():
         "diffusion": (lambda: [W.diffusion_uniform(n_traj=1_000_000)],
                       "Parker fwd, uniform B, kappa = 1, t = 1 (1,000 steps each): 1e6 trajectories "
                       "(10x the named 1e5, so one launch lasts long enough to time)", 0.1),
-        "shock": (lambda: [W.shock_acceleration(n_traj=200_000, x_downstream=40.0, p_max=1.0e3)],
-                  "Parker fwd, smooth shock s = 4, width 1e-3: 2e5 of the named 1e7 trajectories", 0.05),
+        "shock": (lambda: [W.shock_acceleration(n_traj=100_000, x_downstream=40.0, p_max=1.0e2)],
+                  "Parker fwd, smooth shock s = 4, width 1e-3, momentum boundary 1e2 p0: 1e5 of the named 1e7 "
+                  "trajectories (each makes ~1e5-1e6 steps in the shock layer)", 0.01),
         "dipole": (lambda: [W.dipole_orbits(n_traj=1_000_000, t_end=1.0 / U.unit_time)],
                    "Lorentz RK4 in the dipole, 1e6 protons 1-100 MeV, L 2-6, 32 steps per gyro-orbit, for 1 s "
                    "of flight (100 drift periods take ~3e8 steps for the slowest trajectory)", 0.01),
