@@ -119,7 +119,7 @@ int spx_set_option(spx_ctx_t ctx, int option, double value);
  * n_records are exactly DataContainer::data()/length()/size(). */
 int spx_add_plugin(spx_ctx_t ctx, int role, int kind, const uint8_t* blob, size_t blob_len, size_t n_records);
 
-/* Add a problem of n_traj trajectories built from the plugins added so far, with optional
+/* Add a problem of n_traj trajectories (0 allowed: an empty member of a batch) built from the plugins added so far, with optional
  * per-problem replacements: override_blob is a sequence of records
  * { u32 role, u32 slot, u32 kind, u32 n_records, u32 blob_len, u8 blob[blob_len] } replacing the
  * slot-th plugin of that role. Replaces SetTasks(n_traj, batch_size) (src/simulation.cc:509); many

@@ -402,7 +402,7 @@ int spx_add_plugin(spx_ctx_t c, int role, int kind, const uint8_t* blob, size_t 
 
 int spx_add_problem(spx_ctx_t c, int64_t n_traj, uint64_t seed, const uint8_t* ov, size_t ov_len)
 {
-   if (!valid_ctx(c) || n_traj <= 0 || n_traj > 0xffffffffLL || (ov_len && !ov)) return SPX_ERR_INVALID_ARG;
+   if (!valid_ctx(c) || n_traj < 0 || n_traj > 0xffffffffLL || (ov_len && !ov)) return SPX_ERR_INVALID_ARG;
    ProblemHost ph;
    std::memset(&ph.pd, 0, sizeof ph.pd);
    for (const auto& p : c->base) {
@@ -496,12 +496,12 @@ int spx_run(spx_ctx_t c, const spx_tuning* tuning)
    a.queue = tu.schedule;
    a.bnd_slots = slots;
    if (c->record_final && c->d_rec == nullptr) return SPX_ERR_STATE;
+   // trajectory ids of this run, run_index * n_traj ... (run_index + 1) * n_traj - 1, must fit 32 bits
+   for (const auto& p : c->problems)
+      if ((uint64_t)(c->run_index + 1) * (uint64_t)p.n_traj > 0x100000000ull) return SPX_ERR_LIMIT;
    int grc = run_graph(c, a);
    if (grc != SPX_OK) return grc;
-   // ids of the next run continue after this one's (new random streams)
-   for (const auto& p : c->problems)
-      if ((uint64_t)(c->run_index + 2) * (uint64_t)p.n_traj > 0xffffffffull) return SPX_ERR_LIMIT;
-   c->run_index++;
+   c->run_index++;  // the next run draws the ids after these (new random streams)
    c->launched = true;
    c->last = spx_stats{};
    c->last.tuning = tu;
@@ -905,7 +905,7 @@ int spx_run_static(spx_ctx_t c, const spx_tuning* tuning, int32_t* counts, int64
    if (n_counts < off_c || n_sums < off_s || n_events_len < (int64_t)n * spx::kMaxDistro) return SPX_ERR_INVALID_ARG;
    if (c->record_final && (!records || n_records < total)) return SPX_ERR_INVALID_ARG;
    for (const auto& p : c->problems)
-      if ((uint64_t)(c->run_index + 2) * (uint64_t)p.n_traj > 0xffffffffull) return SPX_ERR_LIMIT;
+      if ((uint64_t)(c->run_index + 1) * (uint64_t)p.n_traj > 0x100000000ull) return SPX_ERR_LIMIT;
 
    SPX_CUDA(cudaSetDevice(c->device));
    unsigned char* scratch = nullptr;

@@ -262,3 +262,43 @@ def test_dipole_drift_period(built_lib):
         assert abs(frac - 1.0) < 0.05, (prec, phi.mean(), frac)
         p = np.linalg.norm(rec["mom"], axis=1)
         assert np.max(np.abs(p / np.linalg.norm(rec["mom0"], axis=1) - 1.0)) < 1e-4
+
+
+@pytest.mark.parametrize("precision", [capi.SPX_MIXED, capi.SPX_FP64])
+def test_ragged_batch_with_empty_problem(built_lib, precision):
+    """Problems of 0, 1 and 1,000 trajectories in one launch: the empty problem records nothing, the
+    others equal their own launches (FP64: trajectory by trajectory against the oracle)."""
+    pbs = []
+    for k, n in enumerate((0, 1, 1000)):
+        pb = workloads.diffusion_uniform(n_traj=n, t_end=0.1)
+        pb.problem_id = k
+        pbs.append(pb)
+    res = run_problems(pbs, precision=precision, record=True)
+    assert res.stats.trajectories == 1001
+    counts0, _, nev0 = res.distros[0][0]
+    assert nev0 == 0 and counts0.sum() == 0 and len(res.records[0]) == 0
+    for k in (1, 2):
+        counts, _, nev = res.distros[k][0]
+        assert nev == pbs[k].n_traj and counts.sum() == pbs[k].n_traj
+        if precision == capi.SPX_FP64:
+            ref = ot.run_oracle(pbs[k])
+            assert np.array_equal(res.records[k]["steps"], ref.traj["steps"])
+            assert np.allclose(res.records[k]["pos"], ref.traj["pos"], rtol=1e-12, atol=1e-14)
+
+
+def test_run_refuses_trajectory_ids_beyond_32_bits(built_lib):
+    """Trajectory ids are 32-bit Philox counter words: a run whose ids would pass 2^32 is refused
+    before anything is launched, and the context stays usable."""
+    from spectrum_gb300.simulation import open_problems
+    pb = workloads.diffusion_uniform(n_traj=1000, t_end=0.05)
+    sim = open_problems(pb, precision=capi.SPX_FP64)
+    try:
+        sim.ctx.set_option(capi.SPX_OPT_RUN_INDEX, 4_294_967)  # ids up to 4,294,968,000 > 2^32
+        with pytest.raises(capi.SpxError) as e:
+            sim.ctx.run()
+        assert e.value.code == -7  # SPX_ERR_LIMIT
+        sim.ctx.set_option(capi.SPX_OPT_RUN_INDEX, 4_294_966)  # the last run that fits
+        st = sim.MainLoop()
+        assert st.trajectories == 1000
+    finally:
+        sim.close()
