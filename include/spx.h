@@ -36,7 +36,7 @@ extern "C" {
 #define SPX_ERR_INCOMPLETE -4       /* TrajectoryBase::IsSimmulationReady false (src/trajectory_base.cc:608-632) */
 #define SPX_ERR_CUDA -5             /* a CUDA runtime call failed */
 #define SPX_ERR_OUT_OF_MEMORY -6
-#define SPX_ERR_LIMIT -7            /* more than 4 boundaries per class or 4 distributions */
+#define SPX_ERR_LIMIT -7            /* more than 4 boundaries per class or 4 distributions, or trajectory ids beyond 2^32 */
 #define SPX_ERR_STATE -8            /* call out of order (e.g. spx_run before spx_add_problem) */
 #define SPX_ERR_DEVICE -9           /* the kernel reported an error (e.g. action beyond the ActionTable) */
 #define SPX_ERR_NO_DEVICE -11       /* no CUDA device, or not an sm_103 device */
