@@ -34,13 +34,13 @@ sys.path.insert(0, ROOT)
 METRIC = "SDE trajectories/s at <=1% bin error: batched FP32 vs plain FP64 GPU, 1 GB300"
 UNIT = "trajectories/s"
 WORKLOAD = "gcr_modulation_parker_spiral_32E"
-# Per-step work of the FP32 Parker solar-wind kernel, from one ncu capture of a 128,000-trajectory
-# batch of this workload (profiles/step_kernel_parker_solarwind_f32_gcr4k.md): executed FP32
+# Per-step work of the FP32 Parker solar-wind kernel, from one ncu capture of a 64,000-trajectory
+# batch of this workload (profiles/step_kernel_parker_solarwind_f32_gcr2k.md): executed FP32
 # operations (FFMA x 2 + FADD + FMUL) and thread instructions per accepted step, and DRAM bytes
-# per trajectory (10.6 MB over 128,000 trajectories; the kernel reads no field data from HBM).
-FP32_FLOP_PER_STEP = float(os.environ.get("SPX_FP32_FLOP_PER_STEP", "439"))
+# per trajectory (2.84 MB over 64,000 trajectories; the kernel reads no field data from HBM).
+FP32_FLOP_PER_STEP = float(os.environ.get("SPX_FP32_FLOP_PER_STEP", "421"))
 THREAD_INST_PER_STEP = 812.0
-DRAM_BYTES_PER_TRAJ = 10.635e6 / 128000
+DRAM_BYTES_PER_TRAJ = 2.835e6 / 64000
 # run indices reserved per rank under torchrun: rank r integrates trajectory ids of runs
 # r*RUNS_PER_RANK ... (disjoint shards of one job)
 RUNS_PER_RANK = 256
