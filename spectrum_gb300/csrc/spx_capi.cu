@@ -644,6 +644,7 @@ int spx_sync(spx_ctx_t c, spx_stats* stats)
    c->last.steps = (int64_t)h.steps;
    c->last.retries = (int64_t)h.retries;
    c->last.given_up = (int64_t)h.given_up;
+   c->last.events = (int64_t)h.events;
    if (stats) *stats = c->last;
    if (h.error != 0) return SPX_ERR_DEVICE;
    return SPX_OK;
@@ -982,6 +983,7 @@ int spx_run_static(spx_ctx_t c, const spx_tuning* tuning, int32_t* counts, int64
       stats->steps = (int64_t)h.steps;
       stats->retries = (int64_t)h.retries;
       stats->given_up = (int64_t)h.given_up;
+      stats->events = (int64_t)h.events;
       stats->kernel_launches = 1;
       stats->tuning = tu;
    }

@@ -300,6 +300,7 @@ static __device__ __noinline__ void process_event(int traj, const EventPoint& e,
    for (int k = 0; k < d.width; k++) atomicAdd(&S.sums[d.offset_sums + lin * d.width + k], w[k] * ew + e.amp);
    atomicAdd(&S.counts[d.offset_counts + lin], 1);
    atomicAdd(&S.n_events[(int64_t)prob * kMaxDistro + di], 1ull);
+   atomicAdd(&S.ctr->events, 1ull);  // the run's total, for spx_stats
 }
 
 template <class R, class A>

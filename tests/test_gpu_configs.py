@@ -275,6 +275,7 @@ def test_ragged_batch_with_empty_problem(built_lib, precision):
         pbs.append(pb)
     res = run_problems(pbs, precision=precision, record=True)
     assert res.stats.trajectories == 1001
+    assert res.stats.events == 1001  # one distribution event per trajectory (the time boundary)
     counts0, _, nev0 = res.distros[0][0]
     assert nev0 == 0 and counts0.sum() == 0 and len(res.records[0]) == 0
     for k in (1, 2):

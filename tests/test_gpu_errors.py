@@ -1,0 +1,63 @@
+"""The C ABI's error returns, the counterparts of the reference's set-up exceptions
+(common/params.hh:52-90, src/trajectory_base.cc:608-632): each bad set-up is refused with its code,
+nothing is launched, and the context stays usable. Needs a device only because contexts do."""
+import pytest
+
+from spectrum_gb300 import capi, workloads
+from spectrum_gb300.problem import TRAJ_PARKER
+
+pytestmark = pytest.mark.gpu
+
+
+def _ctx_with(pb, skip_role=None, blob_edit=None, kind_edit=None):
+    ctx = capi.Context(pb.traj, pb.time_flow, pb.rk, capi.SPX_FP64)
+    for e in pb.plugins:
+        if e.plugin.role == skip_role:
+            continue
+        blob, kind = e.blob, e.plugin.kind
+        if blob_edit and e.plugin.role == blob_edit[0]:
+            blob = blob_edit[1](blob)
+        if kind_edit and e.plugin.role == kind_edit[0]:
+            kind = kind_edit[1]
+        ctx.add_plugin(e.plugin.role, kind, blob, e.n_records)
+    return ctx
+
+
+def _code(fn):
+    with pytest.raises(capi.SpxError) as e:
+        fn()
+    return e.value.code
+
+
+def test_bad_set_ups_are_refused(built_lib):
+    pb = workloads.diffusion_uniform(n_traj=10, t_end=0.01)
+    # Parker is an Euler-Maruyama scheme: RK table 25 is refused
+    assert _code(lambda: capi.Context(TRAJ_PARKER, 0, 25, capi.SPX_FP64)) == -1
+    # unknown background class
+    ctx = _ctx_with(pb, kind_edit=(0, 99))
+    assert _code(lambda: ctx.add_problem(10, 1)) == -2
+    ctx.close()
+    # parameter blob shorter than the class's list
+    ctx = _ctx_with(pb, blob_edit=(0, lambda b: b[: len(b) // 2]))
+    assert _code(lambda: ctx.add_problem(10, 1)) == -3
+    ctx.close()
+    # no time boundary: TrajectoryBase::IsSimmulationReady is false
+    ctx = _ctx_with(pb, skip_role=3)
+    assert _code(lambda: ctx.add_problem(10, 1)) == -4
+    ctx.close()
+    # a run before any problem
+    ctx = _ctx_with(pb)
+    assert _code(lambda: ctx.run()) == -8
+    # the context is still usable
+    ctx.add_problem(10, 1)
+    ctx.run()
+    st = ctx.sync()
+    assert st.trajectories == 10
+    ctx.close()
+
+
+def test_negative_trajectory_count_is_refused(built_lib):
+    pb = workloads.diffusion_uniform(n_traj=10, t_end=0.01)
+    ctx = _ctx_with(pb)
+    assert _code(lambda: ctx.add_problem(-1, 1)) == -1
+    ctx.close()
