@@ -231,13 +231,17 @@ def _other_workloads():
         "dipole": (lambda: [W.dipole_orbits(n_traj=1_000_000, t_end=1.0 / U.unit_time)],
                    "Lorentz RK4 in the dipole, 1e6 protons 1-100 MeV, L 2-6, 32 steps per gyro-orbit, for 1 s "
                    "of flight (100 drift periods take ~3e8 steps for the slowest trajectory)", 0.01),
+        "grid": (lambda: W.gcr_modulation_grid(n_traj=100_000, n_nodes=256),
+                 "Parker bwd, the Parker spiral sampled on a 256^3 block over +-6 AU (BackgroundServerCartesian, "
+                 "first-order interpolation; 537 MB of FP32 node data, above the 126 MB L2), 8 energies 30 MeV-3 GeV "
+                 "x 1e5 trajectories, boundaries at 0.3 and 5 AU, 0.2 yr", 0.01),
         "focused": (lambda: W.focused_transport(n_problems=64, n_traj=20_000, t_max_hours=0.5),
                     "Focused RK4 + pitch-angle scattering, 64 problems (mean free paths 0.01-1 AU, 1-100 MeV) of "
                     "2e4 trajectories each, 0.5 h of the named 48 h", 0.05),
     }
 
 
-OTHER_WORKLOADS = ("diffusion", "shock", "dipole", "focused")
+OTHER_WORKLOADS = ("diffusion", "shock", "dipole", "focused", "grid")
 
 
 def bench_other(args, rank, world, local):

@@ -126,6 +126,16 @@ int spx_add_plugin(spx_ctx_t ctx, int role, int kind, const uint8_t* blob, size_
  * problems (energies, mean free paths) run in one launch. */
 int spx_add_problem(spx_ctx_t ctx, int64_t n_traj, uint64_t seed, const uint8_t* override_blob, size_t override_len);
 
+/* The data of a gridded background (kind 6, BackgroundServerCartesian with first-order
+ * interpolation, src/server_cartesian.cc:206-840): one uniform block of n[0] x n[1] x n[2] nodes,
+ * node (i, j, k) at cent_min + (i, j, k) * zone_length, six doubles per node (U, then B, in code
+ * units), x fastest. Replaces the data files the reference's server reads (the fname_pattern of
+ * AddBackground, src/simulation.hh:111) and its MPI block server: the block is copied to device
+ * memory now (this call allocates), shared by all problems of the context. Points whose 8-node
+ * stencil leaves the block are field errors (the trajectory is discarded and retried). */
+int spx_set_background_grid(spx_ctx_t ctx, const int64_t n[3], const double cent_min[3], const double zone_length[3],
+                            const double* values);
+
 /* Integrate every trajectory of every problem; replaces MainLoop (src/simulation.cc:818-835).
  * Enqueues on the context stream and returns; tuning may be NULL (autotuned). Each call draws
  * fresh trajectory ids, so repeated calls add new trajectories to the distributions. */

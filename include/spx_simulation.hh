@@ -125,6 +125,7 @@ SPX_PROTOTYPE(BackgroundShock, BackgroundBase, 2)
 SPX_PROTOTYPE(BackgroundSmoothShock, BackgroundBase, 3)
 SPX_PROTOTYPE(BackgroundDipole, BackgroundBase, 4)
 SPX_PROTOTYPE(BackgroundSolarWind, BackgroundBase, 5)
+SPX_PROTOTYPE(BackgroundServerCartesian, BackgroundBase, 6)
 SPX_PROTOTYPE(DiffusionIsotropicConstant, DiffusionBase, 1)
 SPX_PROTOTYPE(DiffusionQLTConstant, DiffusionBase, 2)
 SPX_PROTOTYPE(DiffusionParaConstant, DiffusionBase, 3)
@@ -220,6 +221,12 @@ public:
    // src/simulation.hh:105-123
    void AddBackground(const BackgroundBase& p, const DataContainer& c, const std::string& = "")
    { add(SPX_ROLE_BACKGROUND, p.kind, c, "AddBackground"); }
+   // The block of a BackgroundServerCartesian background (six values per node: U, B; x fastest),
+   // in place of the data files the reference's server reads.
+   void SetBackgroundGrid(const int64_t n[3], const double cent_min[3], const double zone_length[3], const double* values)
+   {
+      check(spx_set_background_grid(ctx_, n, cent_min, zone_length, values), "SetBackgroundGrid");
+   }
    void AddDiffusion(const DiffusionBase& p, const DataContainer& c) { add(SPX_ROLE_DIFFUSION, p.kind, c, "AddDiffusion"); }
    void AddSource(const SourceBase& p, const DataContainer& c) { add(SPX_ROLE_SOURCE, p.kind, c, "AddSource"); }
    void AddBoundary(const BoundaryBase& p, const DataContainer& c) { add(SPX_ROLE_BOUNDARY, p.kind, c, "AddBoundary"); }

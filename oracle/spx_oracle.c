@@ -201,7 +201,7 @@ static int rd_ints(rd_t* r, int* out, int max)
 #define MAXB 8
 #define MAXD 4
 
-enum { BG_UNIFORM = 1, BG_SHOCK, BG_SMOOTHSHOCK, BG_DIPOLE, BG_SOLARWIND };
+enum { BG_UNIFORM = 1, BG_SHOCK, BG_SMOOTHSHOCK, BG_DIPOLE, BG_SOLARWIND, BG_GRID };
 typedef struct {
    int kind;
    double t0, dmax0;
@@ -539,6 +539,7 @@ static int kind_of(uint32_t role, const char* nm, size_t nl)
    if (role == 0) {
       K("BackgroundUniform", BG_UNIFORM) K("BackgroundShock", BG_SHOCK) K("BackgroundSmoothShock", BG_SMOOTHSHOCK)
       K("BackgroundDipole", BG_DIPOLE) K("BackgroundSolarWind", BG_SOLARWIND)
+      K("BackgroundServerCartesian", BG_GRID)
    }
    else if (role == 1) {
       K("DiffusionIsotropicConstant", DF_ISO) K("DiffusionQLTConstant", DF_QLT) K("DiffusionParaConstant", DF_PARA)
@@ -897,6 +898,97 @@ static void numerical_derivs(const bg_t* g, double t, v3 pos, v3 mom_pmu, spdata
    }
 }
 
+/* ------------------------------------------------------------------------------------------ */
+/* gridded background: BackgroundServerCartesian, first-order interpolation, one uniform block  */
+/* ------------------------------------------------------------------------------------------ */
+static struct {
+   int n[3];
+   v3 cent, zone;
+   double zone_min;
+   double* v; /* 8 per node: U, B, |B|, unused */
+} g_grid;
+
+void spx_oracle_set_grid(const int64_t n[3], const double cent_min[3], const double zone_length[3],
+                         const double* values)
+{
+   int64_t i, nodes = n[0] * n[1] * n[2];
+   int k, q;
+   free(g_grid.v);
+   g_grid.v = (double*)calloc((size_t)nodes * 8, sizeof(double));
+   for (k = 0; k < 3; k++) {
+      g_grid.n[k] = (int)n[k];
+      g_grid.cent.x[k] = cent_min[k];
+      g_grid.zone.x[k] = zone_length[k];
+   }
+   g_grid.zone_min = fmin(zone_length[0], fmin(zone_length[1], zone_length[2]));
+   for (i = 0; i < nodes; i++) {
+      const double* v = values + 6 * i;
+      double* o = g_grid.v + 8 * i;
+      for (q = 0; q < 6; q++) o[q] = v[q];
+      o[6] = sqrt(v[3] * v[3] + v[4] * v[4] + v[5] * v[5]);  /* src/server_cartesian.cc:566-569 */
+   }
+}
+
+/* GetZoneOffset (src/block_base.cc:194-203), InteriorInterpolationStencil
+ * (src/server_cartesian.cc:206-268), GetVariablesInterp1 (:551-666), GetVariables' dmax cap (:687)
+ * and GetGradientsInterp1 (:724-823) for a point inside the block. Nonzero outside. */
+static int grid_fields(double dmax0, v3 pos, unsigned mask, spdata* s)
+{
+   double lo[3], hi[3], w[8], der[24], var[6] = {0, 0, 0, 0, 0, 0}, grads[6][3], gbm[3] = {0, 0, 0};
+   int z[3], k, c, q, u;
+   int64_t nx = g_grid.n[0], nxy = nx * g_grid.n[1];
+   if (!g_grid.v) return 1;
+   for (k = 0; k < 3; k++) {
+      double o = (pos.x[k] - g_grid.cent.x[k]) / g_grid.zone.x[k];
+      if (!(o >= 0.0 && o < (double)(g_grid.n[k] - 1))) return 1;
+      z[k] = (int)o;
+      lo[k] = o - z[k];
+      hi[k] = 1.0 - lo[k];
+   }
+   for (c = 0; c < 8; c++) {
+      int ci = c & 1, cj = (c >> 1) & 1, ck = (c >> 2) & 1;
+      double fx = ci ? lo[0] : hi[0], fy = cj ? lo[1] : hi[1], fz = ck ? lo[2] : hi[2];
+      w[c] = fx * fy * fz;
+      der[3 * c + 0] = (ci ? fy * fz : -fy * fz) / g_grid.zone.x[0];
+      der[3 * c + 1] = (cj ? fx * fz : -fx * fz) / g_grid.zone.x[1];
+      der[3 * c + 2] = (ck ? fx * fy : -fx * fy) / g_grid.zone.x[2];
+   }
+   for (q = 0; q < 6; q++) grads[q][0] = grads[q][1] = grads[q][2] = 0.0;
+   s->Bmag = 0.0;
+   for (c = 0; c < 8; c++) {
+      int ci = c & 1, cj = (c >> 1) & 1, ck = (c >> 2) & 1;
+      const double* v = g_grid.v + 8 * ((z[2] + ck) * nxy + (int64_t)(z[1] + cj) * nx + (z[0] + ci));
+      for (q = 0; q < 6; q++) var[q] += w[c] * v[q];
+      s->Bmag += w[c] * v[6];
+      for (q = 0; q < 6; q++)
+         for (u = 0; u < 3; u++) grads[q][u] += der[3 * c + u] * v[q];
+      for (u = 0; u < 3; u++) gbm[u] += der[3 * c + u] * v[6];
+   }
+   s->dmax = fmin(dmax0, g_grid.zone_min);
+   for (k = 0; k < 3; k++) {
+      s->U.x[k] = var[k];
+      s->B.x[k] = var[3 + k];
+   }
+   {
+      v3 x = vcross(s->U, s->B);
+      for (k = 0; k < 3; k++) s->E.x[k] = -(x.x[k] / c_code());
+   }
+   s->region = V(0.0, 0.0, 0.0);
+   if (s->Bmag < SP_TINY) return 1;
+   s->bhat = vdiv(s->B, s->Bmag);
+   for (u = 0; u < 3; u++)
+      for (k = 0; k < 3; k++) {
+         s->gradU.m[u][k] = grads[k][u];
+         s->gradB.m[u][k] = grads[3 + k][u];
+      }
+   for (u = 0; u < 3; u++) s->gradBmag.x[u] = gbm[u];
+   s->dUdt = V(0, 0, 0);
+   s->dBdt = V(0, 0, 0);
+   s->dBmagdt = 0.0;
+   (void)mask;
+   return 0;
+}
+
 /* BackgroundBase::GetFields (src/background_base.cc:425-456). Returns nonzero on a field error. */
 static int get_fields(trj_t* T, double t, v3 pos, v3 mom_pmu, unsigned mask, spdata* s)
 {
@@ -904,6 +996,10 @@ static int get_fields(trj_t* T, double t, v3 pos, v3 mom_pmu, unsigned mask, spd
    double ds = 0.0;
    int i;
    s->mask = mask;
+   if (g->kind == BG_GRID) {
+      for (i = 0; i < 3; i++) s->dr[i] = 0.0001 * g->dmax0;
+      return grid_fields(g->dmax0, pos, mask, s);
+   }
    if (g->kind == BG_SMOOTHSHOCK && T->o->reference_quirks)  /* D1 as the reference has it */
       s->dmax = fmin(g->dmax_fraction * g->width * fmax(1.0, fabs(T->bg_ds_prev)), g->dmax0);
    else

@@ -61,6 +61,11 @@ void spx_oracle_normals(uint64_t seed, uint32_t index, uint32_t traj, uint32_t p
                         double out[4]);
 void spx_oracle_uniforms(uint64_t seed, uint32_t index, uint32_t traj, uint32_t problem, uint32_t attempt,
                          double out[4]);
+/* The block of a gridded background (BackgroundServerCartesian): n[0] x n[1] x n[2] nodes at
+ * cent_min + (i, j, k) * zone_length, six values per node (U, B), x fastest. One grid at a time. */
+void spx_oracle_set_grid(const int64_t n[3], const double cent_min[3], const double zone_length[3],
+                         const double* values);
+
 /* Philox4x32-10 of one counter under one key (for the generator's known-answer tests). */
 void spx_oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 

@@ -26,7 +26,7 @@ SPX_OPT_RUN_INDEX = 6
 EXPORTS = ["spx_create", "spx_set_option", "spx_add_plugin", "spx_add_problem", "spx_run", "spx_sync",
            "spx_get_distribution_info", "spx_get_distribution", "spx_get_records", "spx_reset_distributions",
            "spx_dump", "spx_restore", "spx_strerror", "spx_destroy", "spx_version", "spx_run_static",
-           "spx_autotune"]
+           "spx_autotune", "spx_set_background_grid"]
 
 #: bytes of the fixed device array spx_run_static works in (SPX_STATIC_SCRATCH_BYTES)
 STATIC_SCRATCH_BYTES = 512 * 1024
@@ -86,6 +86,7 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         lib.spx_destroy.restype = None
         lib.spx_version.restype = ctypes.c_char_p
         lib.spx_autotune.argtypes = [c_vp, ctypes.c_int64, ctypes.POINTER(Tuning)]
+        lib.spx_set_background_grid.argtypes = [c_vp, c_vp, c_vp, c_vp, c_vp]
         lib.spx_run_static.argtypes = [c_vp, ctypes.POINTER(Tuning), c_vp, ctypes.c_int64, c_vp, ctypes.c_int64, c_vp,
                                        ctypes.c_int64, c_vp, ctypes.c_int64, ctypes.POINTER(Stats)]
         _lib = lib
@@ -154,6 +155,17 @@ class Context:
         t = Tuning()
         check(self.lib.spx_autotune(self._h, int(sample_traj), ctypes.byref(t)), "spx_autotune")
         return t
+
+    def set_background_grid(self, n, cent_min, zone_length, values) -> None:
+        """spx_set_background_grid: the block of a gridded background (values (n2, n1, n0, 6): U, B)."""
+        nn = np.ascontiguousarray(np.asarray(n, dtype=np.int64))
+        cm = np.ascontiguousarray(np.asarray(cent_min, dtype=np.float64))
+        zl = np.ascontiguousarray(np.asarray(zone_length, dtype=np.float64))
+        v = np.ascontiguousarray(np.asarray(values, dtype=np.float64))
+        if v.size != 6 * int(np.prod(nn)):
+            raise ValueError("values must hold 6 numbers per node")
+        check(self.lib.spx_set_background_grid(self._h, nn.ctypes.data, cm.ctypes.data, zl.ctypes.data, v.ctypes.data),
+              "spx_set_background_grid")
 
     def sync(self) -> Stats:
         st = Stats()

@@ -7,6 +7,7 @@
 // plugins added before them plus per-problem replacements; all problems of a context share one
 // trajectory type, time flow, Runge-Kutta table and background class (these select the kernel).
 #include <algorithm>
+#include <cmath>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -72,6 +73,12 @@ struct spx_ctx {
    // launch shape chosen by spx_autotune (used by spx_run when it gets no tuning)
    bool has_tuned = false;
    spx_tuning tuned{};
+   // the gridded background (spx_set_background_grid): geometry and the node values on the device
+   bool has_grid = false;
+   int grid_n[3] = {0, 0, 0};
+   double grid_cent[3] = {0, 0, 0}, grid_zone[3] = {0, 0, 0};
+   double* d_grid64 = nullptr;
+   float* d_grid32 = nullptr;
 };
 
 namespace {
@@ -102,6 +109,27 @@ void free_buffers(spx_ctx* c)
    c->d_rec = nullptr;
    c->rec_cap = 0;
 }
+
+// Geometry and device address of the context's grid in a descriptor copy (gridded backgrounds).
+void apply_grid(const spx_ctx* c, spx::ProblemDesc& pd)
+{
+   if (pd.bg.kind != spx::kBgGrid) return;
+   for (int k = 0; k < 3; k++) {
+      pd.bg.cent_min[k] = c->grid_cent[k];
+      pd.bg.zone[k] = c->grid_zone[k];
+      pd.bg.grid_n[k] = c->grid_n[k];
+   }
+   pd.bg.zone_min = std::min(c->grid_zone[0], std::min(c->grid_zone[1], c->grid_zone[2]));
+   pd.bg.grid = c->d_grid64;
+}
+
+void apply_grid(const spx_ctx* c, spx::ProblemDescT<float>& pd)
+{
+   if (pd.bg.kind == spx::kBgGrid) pd.bg.grid = c->d_grid32;
+}
+
+// A gridded background needs its grid before anything runs.
+bool grid_missing(const spx_ctx* c) { return c->bg_kind == spx::kBgGrid && !c->has_grid; }
 
 // Lay out the distributions of all problems, allocate and upload (called when problems changed).
 int upload(spx_ctx* c)
@@ -147,15 +175,22 @@ int upload(spx_ctx* c)
       c->n_sums = off_s;
    }
    if (c->d_ctr == nullptr) SPX_CUDA(cudaMalloc(&c->d_ctr, sizeof(spx::RunCounters)));
+   if (grid_missing(c)) return SPX_ERR_STATE;
    std::vector<spx::ProblemDesc> hd(n);
-   for (int k = 0; k < n; k++) hd[k] = c->problems[k].pd;
+   for (int k = 0; k < n; k++) {
+      hd[k] = c->problems[k].pd;
+      apply_grid(c, hd[k]);
+   }
    SPX_CUDA(cudaMemcpyAsync(c->d_pd, hd.data(), sizeof(spx::ProblemDesc) * n, cudaMemcpyHostToDevice, c->stream));
    if (c->precision == SPX_FP64) {
       SPX_CUDA(cudaMemcpyAsync(c->d_pr, hd.data(), sizeof(spx::ProblemDesc) * n, cudaMemcpyHostToDevice, c->stream));
    }
    else {
       std::vector<spx::ProblemDescT<float>> hf(n);
-      for (int k = 0; k < n; k++) spx::convert_problem(hd[k], hf[k]);
+      for (int k = 0; k < n; k++) {
+         spx::convert_problem(hd[k], hf[k]);
+         apply_grid(c, hf[k]);
+      }
       SPX_CUDA(cudaMemcpyAsync(c->d_pr, hf.data(), sizeof(spx::ProblemDescT<float>) * n, cudaMemcpyHostToDevice,
                                c->stream));
       SPX_CUDA(cudaStreamSynchronize(c->stream));  // hf is a host temporary
@@ -173,28 +208,35 @@ int upload(spx_ctx* c)
 
 cudaError_t launch(spx_ctx* c, const spx::LaunchArgs& a)
 {
-   bool f64 = c->precision == SPX_FP64;
+   const bool f64 = c->precision == SPX_FP64, fd = f64 && c->deriv_mode == 0;
+   const int bg = c->bg_kind;
    switch (c->traj) {
    case SPX_TRAJ_PARKER:
-   case SPX_TRAJ_PARKER_SOURCE: return f64 ? spx::launch_parker_f64(c->bg_kind, a) : spx::launch_parker_f32(c->bg_kind, a);
-   case SPX_TRAJ_LORENTZ: return f64 ? spx::launch_lorentz_f64(c->bg_kind, a) : spx::launch_lorentz_f32(c->bg_kind, a);
-   case SPX_TRAJ_FOCUSED: return f64 ? spx::launch_focused_f64(c->bg_kind, a) : spx::launch_focused_f32(c->bg_kind, a);
+   case SPX_TRAJ_PARKER_SOURCE:
+      return fd ? spx::launch_parker_f64fd(bg, a) : f64 ? spx::launch_parker_f64(bg, a) : spx::launch_parker_f32(bg, a);
+   case SPX_TRAJ_LORENTZ:
+      return fd ? spx::launch_lorentz_f64fd(bg, a) : f64 ? spx::launch_lorentz_f64(bg, a) : spx::launch_lorentz_f32(bg, a);
+   case SPX_TRAJ_FOCUSED:
+      return fd ? spx::launch_focused_f64fd(bg, a) : f64 ? spx::launch_focused_f64(bg, a) : spx::launch_focused_f32(bg, a);
    default: return cudaErrorInvalidValue;
    }
 }
 
 int occupancy(spx_ctx* c, int block, int slots)
 {
-   bool f64 = c->precision == SPX_FP64;
-   int bg = c->bg_kind, dm = c->deriv_mode;
+   const bool f64 = c->precision == SPX_FP64, fd = f64 && c->deriv_mode == 0;
+   const int bg = c->bg_kind;
    switch (c->traj) {
    case SPX_TRAJ_PARKER:
    case SPX_TRAJ_PARKER_SOURCE:
-      return f64 ? spx::occupancy_parker_f64(bg, block, slots, dm) : spx::occupancy_parker_f32(bg, block, slots, dm);
+      return fd ? spx::occupancy_parker_f64fd(bg, block, slots)
+                : f64 ? spx::occupancy_parker_f64(bg, block, slots) : spx::occupancy_parker_f32(bg, block, slots);
    case SPX_TRAJ_LORENTZ:
-      return f64 ? spx::occupancy_lorentz_f64(bg, block, slots, dm) : spx::occupancy_lorentz_f32(bg, block, slots, dm);
+      return fd ? spx::occupancy_lorentz_f64fd(bg, block, slots)
+                : f64 ? spx::occupancy_lorentz_f64(bg, block, slots) : spx::occupancy_lorentz_f32(bg, block, slots);
    case SPX_TRAJ_FOCUSED:
-      return f64 ? spx::occupancy_focused_f64(bg, block, slots, dm) : spx::occupancy_focused_f32(bg, block, slots, dm);
+      return fd ? spx::occupancy_focused_f64fd(bg, block, slots)
+                : f64 ? spx::occupancy_focused_f64(bg, block, slots) : spx::occupancy_focused_f32(bg, block, slots);
    default: return 0;
    }
 }
@@ -208,6 +250,7 @@ int bnd_slots(const spx_ctx* c)
 }
 
 bool valid_ctx(spx_ctx* c) { return c != nullptr; }
+
 
 // What a captured graph depends on: launch shape, the run configuration apart from the run
 // index, and the device buffers. A different key means a new capture.
@@ -435,6 +478,55 @@ int spx_add_problem(spx_ctx_t c, int64_t n_traj, uint64_t seed, const uint8_t* o
    return SPX_OK;
 }
 
+// BackgroundServerCartesian's data: one uniform block of n[0] x n[1] x n[2] nodes, node (i, j, k) at
+// cent_min + (i, j, k) * zone_length, six values per node (U then B, code units), x fastest. The
+// values are copied to device memory now, in the context's arithmetic, with |B| of every node
+// appended (the magnitude the reference interpolates, src/server_cartesian.cc:566-569).
+int spx_set_background_grid(spx_ctx_t c, const int64_t n[3], const double cent_min[3], const double zone_length[3],
+                            const double* values)
+{
+   if (!valid_ctx(c) || !n || !cent_min || !zone_length || !values) return SPX_ERR_INVALID_ARG;
+   int64_t nodes = 1;
+   for (int k = 0; k < 3; k++) {
+      if (n[k] < 2 || n[k] > 1000000 || !(zone_length[k] > 0.0) || !std::isfinite(cent_min[k])) return SPX_ERR_INVALID_ARG;
+      nodes *= n[k];
+   }
+   if (nodes > ((int64_t)1 << 31)) return SPX_ERR_TOO_LARGE;
+   SPX_CUDA(cudaSetDevice(c->device));
+   SPX_CUDA(cudaStreamSynchronize(c->stream));
+   cudaFree(c->d_grid64);
+   cudaFree(c->d_grid32);
+   c->d_grid64 = nullptr;
+   c->d_grid32 = nullptr;
+   c->has_grid = false;
+   const size_t count = (size_t)nodes * spx::kGridStride;
+   std::vector<double> h(count, 0.0);
+   for (int64_t i = 0; i < nodes; i++) {
+      const double* v = values + 6 * i;
+      double* o = h.data() + spx::kGridStride * i;
+      for (int q = 0; q < 6; q++) o[q] = v[q];
+      const double bx2 = v[3] * v[3], by2 = v[4] * v[4], bz2 = v[5] * v[5];
+      o[6] = std::sqrt(bx2 + by2 + bz2);
+   }
+   if (c->precision == SPX_FP64) {
+      SPX_CUDA(cudaMalloc(&c->d_grid64, sizeof(double) * count));
+      SPX_CUDA(cudaMemcpy(c->d_grid64, h.data(), sizeof(double) * count, cudaMemcpyHostToDevice));
+   }
+   else {
+      std::vector<float> f(h.begin(), h.end());
+      SPX_CUDA(cudaMalloc(&c->d_grid32, sizeof(float) * count));
+      SPX_CUDA(cudaMemcpy(c->d_grid32, f.data(), sizeof(float) * count, cudaMemcpyHostToDevice));
+   }
+   for (int k = 0; k < 3; k++) {
+      c->grid_n[k] = (int)n[k];
+      c->grid_cent[k] = cent_min[k];
+      c->grid_zone[k] = zone_length[k];
+   }
+   c->has_grid = true;
+   c->dirty = true;
+   return SPX_OK;
+}
+
 int spx_run(spx_ctx_t c, const spx_tuning* tuning)
 {
    if (!valid_ctx(c)) return SPX_ERR_INVALID_ARG;
@@ -516,7 +608,7 @@ int spx_run(spx_ctx_t c, const spx_tuning* tuning)
 int spx_autotune(spx_ctx_t c, int64_t sample_traj, spx_tuning* best)
 {
    if (!valid_ctx(c)) return SPX_ERR_INVALID_ARG;
-   if (c->problems.empty()) return SPX_ERR_STATE;
+   if (c->problems.empty() || grid_missing(c)) return SPX_ERR_STATE;
    SPX_CUDA(cudaSetDevice(c->device));
    const int n = (int)c->problems.size();
    const bool f64 = c->precision == SPX_FP64;
@@ -528,6 +620,7 @@ int spx_autotune(spx_ctx_t c, int64_t sample_traj, spx_tuning* best)
    int64_t off_c = 0, off_s = 0, first = 0;
    for (int k = 0; k < n; k++) {
       hd[k] = c->problems[k].pd;
+      apply_grid(c, hd[k]);
       int64_t nk = std::max<int64_t>(1, (int64_t)((double)c->problems[k].n_traj * sample_traj / std::max<int64_t>(total, 1)));
       hd[k].n_traj = nk;
       hd[k].first = first;
@@ -555,7 +648,10 @@ int spx_autotune(spx_ctx_t c, int64_t sample_traj, spx_tuning* best)
    if (f64) SPX_CUDA(cudaMemcpy(b_pr.p, hd.data(), sizeof(spx::ProblemDesc) * n, cudaMemcpyHostToDevice));
    else {
       std::vector<spx::ProblemDescT<float>> hf(n);
-      for (int k = 0; k < n; k++) spx::convert_problem(hd[k], hf[k]);
+      for (int k = 0; k < n; k++) {
+         spx::convert_problem(hd[k], hf[k]);
+         apply_grid(c, hf[k]);
+      }
       SPX_CUDA(cudaMemcpy(b_pr.p, hf.data(), sizeof(spx::ProblemDescT<float>) * n, cudaMemcpyHostToDevice));
    }
 
@@ -813,6 +909,8 @@ void spx_destroy(spx_ctx_t c)
    if (c->stream) cudaStreamSynchronize(c->stream);
    drop_graph(c);
    free_buffers(c);
+   cudaFree(c->d_grid64);
+   cudaFree(c->d_grid32);
    if (c->ev0) cudaEventDestroy(c->ev0);
    if (c->ev1) cudaEventDestroy(c->ev1);
    if (c->stream) cudaStreamDestroy(c->stream);
@@ -872,7 +970,7 @@ int spx_run_static(spx_ctx_t c, const spx_tuning* tuning, int32_t* counts, int64
                    int64_t n_records, spx_stats* stats)
 {
    if (!valid_ctx(c)) return SPX_ERR_INVALID_ARG;
-   if (c->problems.empty()) return SPX_ERR_STATE;
+   if (c->problems.empty() || grid_missing(c)) return SPX_ERR_STATE;
    const int n = (int)c->problems.size();
    const bool f64 = c->precision == SPX_FP64;
 
@@ -881,6 +979,7 @@ int spx_run_static(spx_ctx_t c, const spx_tuning* tuning, int32_t* counts, int64
    int64_t off_c = 0, off_s = 0, total = 0;
    for (int k = 0; k < n; k++) {
       hd[k] = c->problems[k].pd;
+      apply_grid(c, hd[k]);
       hd[k].first = total;
       hd[k].n_traj = c->problems[k].n_traj;
       total += hd[k].n_traj;
@@ -935,7 +1034,10 @@ int spx_run_static(spx_ctx_t c, const spx_tuning* tuning, int32_t* counts, int64
    SPX_CUDA(cudaMemcpyAsync(scratch + off_pd, hd.data(), bytes_pd, cudaMemcpyHostToDevice, c->stream));
    if (!f64) {
       hf.resize(n);
-      for (int k = 0; k < n; k++) spx::convert_problem(hd[k], hf[k]);
+      for (int k = 0; k < n; k++) {
+         spx::convert_problem(hd[k], hf[k]);
+         apply_grid(c, hf[k]);
+      }
       SPX_CUDA(cudaMemcpyAsync(scratch + off_pr, hf.data(), bytes_pr, cudaMemcpyHostToDevice, c->stream));
    }
 

@@ -1,4 +1,5 @@
-// spx_k_lorentz_f64.cu -- the lorentz stepping kernels in double arithmetic, one per background.
+// spx_k_lorentz_f64.cu -- the lorentz stepping kernels in double arithmetic with analytic field
+// derivatives, one per background.
 #include "spx_k_family.cuh"
 
-SPX_FAMILY_TU(lorentz, f64, kLorentz, double)
+SPX_FAMILY_TU(lorentz, f64, kLorentz, double, 1)

@@ -1,5 +1,5 @@
 // spx_launch.hh -- host entry points of the stepping kernels, one translation unit per trajectory
-// family and arithmetic so they compile in parallel.
+// family, arithmetic and (FP64) field-derivative method so they compile in parallel.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -23,11 +23,13 @@ struct LaunchArgs {
    int bnd_slots;                   // boundary states per lane (the largest problem's count)
 };
 
-#define SPX_DECLARE_FAMILY(fam)                                  \
-   cudaError_t launch_##fam##_f64(int bg, const LaunchArgs& a);  \
-   cudaError_t launch_##fam##_f32(int bg, const LaunchArgs& a);  \
-   int occupancy_##fam##_f64(int bg, int block, int slots, int deriv_mode); \
-   int occupancy_##fam##_f32(int bg, int block, int slots, int deriv_mode);
+#define SPX_DECLARE_FAMILY(fam)                                        \
+   cudaError_t launch_##fam##_f64(int bg, const LaunchArgs& a);        \
+   cudaError_t launch_##fam##_f64fd(int bg, const LaunchArgs& a);      \
+   cudaError_t launch_##fam##_f32(int bg, const LaunchArgs& a);        \
+   int occupancy_##fam##_f64(int bg, int block, int slots);            \
+   int occupancy_##fam##_f64fd(int bg, int block, int slots);          \
+   int occupancy_##fam##_f32(int bg, int block, int slots);
 SPX_DECLARE_FAMILY(parker)
 SPX_DECLARE_FAMILY(lorentz)
 SPX_DECLARE_FAMILY(focused)

@@ -19,7 +19,7 @@ constexpr int kMaxDistro = 4;  // distributions per problem
 
 enum TrajKind : int { kLorentz = 200, kFocused = 205, kParker = 206, kParkerSource = 207 };
 
-enum BgKind : int { kBgUniform = 1, kBgShock = 2, kBgSmoothShock = 3, kBgDipole = 4, kBgSolarWind = 5 };
+enum BgKind : int { kBgUniform = 1, kBgShock = 2, kBgSmoothShock = 3, kBgDipole = 4, kBgSolarWind = 5, kBgGrid = 6 };
 
 enum DiffKind : int {
    kDfIsotropic = 1, kDfQLT, kDfPara, kDfPerp, kDfFull, kDfFlowMomentum, kDfKinEnergyRadial, kDfRigidityB,
@@ -55,7 +55,15 @@ struct BgParamsT {
    R M[3];                    // dipole moment B0 r_ref^3
    R eprime[3][3];            // solar wind rotation frame (rows)
    R w0, r_ref, ur0, A;       // A = Br0 r_ref^2
+   // uniform Cartesian grid (BackgroundServerCartesian): node (i, j, k) sits at
+   // cent_min + (i, j, k) * zone; kGridStride values per node, x fastest
+   R cent_min[3], zone[3], zone_min;
+   int grid_n[3];
+   const R* grid;             // device address of the node values (set when the context uploads)
 };
+
+// Values per grid node: U (3), B (3), |B| (the magnitude at the node), one pad (32 B per node in FP32)
+constexpr int kGridStride = 8;
 
 template <class R>
 struct DiffParamsT {

@@ -137,6 +137,8 @@ int parse_background(Reader& r, int kind, BgParams& g)
       g.A = g.B0[0] * g.r_ref * g.r_ref;
       break;
    }
+   case kBgGrid:  // BackgroundServerCartesian: the base parameters only; the grid comes separately
+      break;
    default:
       return SPX_ERR_UNKNOWN_PLUGIN;
    }
@@ -488,6 +490,9 @@ void convert_problem(const ProblemDesc& s, ProblemDescT<R>& d)
    b.dmax_fraction = (R)a.dmax_fraction;
    cp(a.M, b.M); cp(a.eprime, b.eprime);
    b.w0 = (R)a.w0; b.r_ref = (R)a.r_ref; b.ur0 = (R)a.ur0; b.A = (R)a.A;
+   cp(a.cent_min, b.cent_min); cp(a.zone, b.zone); b.zone_min = (R)a.zone_min;
+   for (int k = 0; k < 3; k++) b.grid_n[k] = a.grid_n[k];
+   b.grid = nullptr;  // the context points it at its own copy of the grid in this arithmetic
 
    d.df.kind = s.df.kind; d.df.i0 = s.df.i0; d.df.i1 = s.df.i1; cp(s.df.a, d.df.a);
    d.src.kind = s.src.kind; d.src.p_inj = (R)s.src.p_inj; d.src.rate = (R)s.src.rate;

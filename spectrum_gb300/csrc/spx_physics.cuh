@@ -178,6 +178,7 @@ __device__ __forceinline__ R eval_dmax(const BgParamsT<R>& g, R t, V3<R> pos)
       return m_min(g.dmax_fraction * g.width * m_max(R(1), m_abs(ds)), g.dmax0);
    }
    if (BG == kBgDipole || BG == kBgSolarWind) return m_min(g.dmax_fraction * norm(pos - ld3(g.r0)), g.dmax0);
+   if (BG == kBgGrid) return m_min(g.dmax0, g.zone_min);
    return g.dmax0;
 }
 
@@ -235,6 +236,98 @@ __device__ __forceinline__ bool solarwind_closed(const BgParamsT<R>& g, V3<R> po
       s.gradB.m[0][2] += k * f * Os[1]; s.gradB.m[2][0] -= k * f * Os[1];
       s.gradB.m[1][2] -= k * f * Os[0]; s.gradB.m[2][1] += k * f * Os[0];
    }
+   return true;
+}
+
+// ---- gridded background ------------------------------------------------------------------------
+// BackgroundServerCartesian with first-order interpolation, on one uniform block held in device
+// memory: zone and offset as BlockBase::GetZoneOffset (src/block_base.cc:194-203), the 8-node
+// stencil of ServerCartesianFront::InteriorInterpolationStencil (src/server_cartesian.cc:206-268),
+// the variables of GetVariablesInterp1 (:551-666: U and B interpolated, |B| interpolated from the
+// node magnitudes, E = -U x B / c, no region variable), dmax capped by the zone length
+// (:687), and the gradients of GetGradientsInterp1 (:724-823) from the stencil's derivative
+// weights. A node is 32 B in FP32 (two 16-byte loads), 64 B in FP64. A point whose stencil would
+// leave the block is a field error.
+__device__ __forceinline__ void load_node(const float* p, float* v)
+{
+   const float4 a = __ldg(reinterpret_cast<const float4*>(p)), b = __ldg(reinterpret_cast<const float4*>(p) + 1);
+   v[0] = a.x; v[1] = a.y; v[2] = a.z; v[3] = a.w; v[4] = b.x; v[5] = b.y; v[6] = b.z;
+}
+__device__ __forceinline__ void load_node(const double* p, double* v)
+{
+   const double2* q = reinterpret_cast<const double2*>(p);
+   const double2 a = __ldg(q), b = __ldg(q + 1), c = __ldg(q + 2), d = __ldg(q + 3);
+   v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y; v[6] = d.x;
+}
+
+template <class R>
+__device__ __forceinline__ bool grid_fields(const BgParamsT<R>& g, V3<R> pos, unsigned mask, SD<R>& s)
+{
+   R lo[3], hi[3];
+   int z[3];
+#pragma unroll
+   for (int k = 0; k < 3; k++) {
+      const R o = (pos[k] - g.cent_min[k]) / g.zone[k];
+      if (!(o >= R(0) && o < (R)(g.grid_n[k] - 1))) return false;
+      z[k] = (int)o;
+      lo[k] = o - (R)z[k];
+      hi[k] = R(1) - lo[k];
+   }
+   const int64_t nx = g.grid_n[0], nxy = nx * (int64_t)g.grid_n[1];
+   const R* base = g.grid + ((int64_t)z[2] * nxy + (int64_t)z[1] * nx + z[0]) * kGridStride;
+   const bool grads = (mask & (kGradU | kGradB | kDUdt)) != 0;
+   R var[6] = {R(0), R(0), R(0), R(0), R(0), R(0)}, bmag = R(0);
+   R gr[6][3], gbm[3] = {R(0), R(0), R(0)};
+#pragma unroll
+   for (int q = 0; q < 6; q++) gr[q][0] = gr[q][1] = gr[q][2] = R(0);
+#pragma unroll
+   for (int c = 0; c < 8; c++) {
+      const int ci = c & 1, cj = (c >> 1) & 1, ck = (c >> 2) & 1;
+      const R fx = ci ? lo[0] : hi[0], fy = cj ? lo[1] : hi[1], fz = ck ? lo[2] : hi[2];
+      R v[7];
+      load_node(base + ((int64_t)ck * nxy + (int64_t)cj * nx + ci) * kGridStride, v);
+      const R w = fx * fy * fz;
+#pragma unroll
+      for (int q = 0; q < 6; q++) var[q] += w * v[q];
+      bmag += w * v[6];
+      if (grads) {
+         const R d0 = (ci ? fy * fz : -fy * fz) / g.zone[0];
+         const R d1 = (cj ? fx * fz : -fx * fz) / g.zone[1];
+         const R d2 = (ck ? fx * fy : -fx * fy) / g.zone[2];
+#pragma unroll
+         for (int q = 0; q < 6; q++) {
+            gr[q][0] += d0 * v[q];
+            gr[q][1] += d1 * v[q];
+            gr[q][2] += d2 * v[q];
+         }
+         gbm[0] += d0 * v[6];
+         gbm[1] += d1 * v[6];
+         gbm[2] += d2 * v[6];
+      }
+   }
+   s.dmax = m_min(g.dmax0, g.zone_min);
+   s.U = mk(var[0], var[1], var[2]);
+   s.B = mk(var[3], var[4], var[5]);
+   if (mask & kE) {
+      const V3<R> x = cross(s.U, s.B);
+      const R c = c_code<R>();
+      s.E = mk(-(x.x / c), -(x.y / c), -(x.z / c));
+   }
+   s.region = mk(R(0), R(0), R(0));
+   s.Bmag = bmag;
+   if (!(s.Bmag >= Lim<R>::tiny)) return false;
+   s.bhat = s.B / s.Bmag;
+   if (!grads) return true;
+#pragma unroll
+   for (int u = 0; u < 3; u++)
+#pragma unroll
+      for (int x = 0; x < 3; x++) {
+         s.gradU.m[u][x] = gr[x][u];
+         s.gradB.m[u][x] = gr[3 + x][u];
+      }
+   s.gradBmag = mk(gbm[0], gbm[1], gbm[2]);
+   s.dUdt = mk(R(0), R(0), R(0));
+   derive_from_matrices(s);
    return true;
 }
 
@@ -303,6 +396,10 @@ __device__ __forceinline__ bool get_fields(const BgParamsT<R>& g, int deriv_mode
    if (BG == kBgSolarWind && deriv_mode == 1) {
       s.dr[0] = s.dr[1] = s.dr[2] = R(0.0001) * g.dmax0;
       return solarwind_closed(g, pos, mask, s);
+   }
+   if (BG == kBgGrid) {
+      s.dr[0] = s.dr[1] = s.dr[2] = R(0.0001) * g.dmax0;
+      return grid_fields(g, pos, mask, s);
    }
    R ds = R(0);
    s.dmax = eval_dmax<BG>(g, t, pos);

@@ -78,6 +78,13 @@ class BackgroundDipole(Plugin): pass  # src/background_dipole.cc:48-125
 class BackgroundSolarWind(Plugin): pass  # src/background_solarwind.cc:58-314
 
 
+@_plugin(ROLE_BACKGROUND, 6)
+class BackgroundServerCartesian(Plugin):
+    """The base parameters only (src/background_base.cc:342-346); the grid itself comes with
+    Problem.grid / spx_set_background_grid (src/background_server_cartesian.cc, first-order
+    interpolation of src/server_cartesian.cc:206-840 on one block)."""
+
+
 # -- diffusion (src/diffusion_other.hh) --------------------------------------------------------
 @_plugin(ROLE_DIFFUSION, 1)
 class DiffusionIsotropicConstant(Plugin): pass  # src/diffusion_other.cc:64-79

@@ -34,6 +34,27 @@ class PluginEntry:
 
 
 @dataclass
+class Grid:
+    """One uniform Cartesian block: node (i, j, k) at cent_min + (i, j, k) * zone_length; values
+    of shape (n[2], n[1], n[0], 6) holding U then B at each node (code units)."""
+    n: tuple
+    cent_min: tuple
+    zone_length: tuple
+    values: "object"
+
+    @classmethod
+    def sample(cls, n, cent_min, zone_length, fields) -> "Grid":
+        """Sample fields(x, y, z) -> (U, B) (arrays of shape (..., 3)) at the nodes."""
+        import numpy as np
+        ax = [cent_min[k] + zone_length[k] * np.arange(n[k]) for k in range(3)]
+        z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+        u, b = fields(x, y, z)
+        values = np.concatenate([u, b], axis=-1).astype(np.float64)
+        return cls(tuple(int(v) for v in n), tuple(float(v) for v in cent_min), tuple(float(v) for v in zone_length),
+                   np.ascontiguousarray(values))
+
+
+@dataclass
 class Problem:
     traj: int = TRAJ_PARKER
     time_flow: int = FORWARD
@@ -44,6 +65,8 @@ class Problem:
     problem_id: int = 0
     #: options of the stepping kernel (see include/spx.h, SPX_OPT_*)
     options: dict[int, float] = field(default_factory=dict)
+    #: the block of a gridded background (BackgroundServerCartesian): a Grid, or None
+    grid: "Grid | None" = None
 
     def add(self, plugin: P.Plugin, container: DataContainer) -> "Problem":
         self.plugins.append(PluginEntry(plugin, container.data(), container.size()))

@@ -45,6 +45,11 @@ class SimulationGPU:
     def AddBackground(self, proto, container, fname_pattern_in: str = ""):  # noqa: N802
         self._add(P.ROLE_BACKGROUND, proto, container)
 
+    def SetBackgroundGrid(self, grid) -> None:  # noqa: N802
+        """The block of a BackgroundServerCartesian background (a problem.Grid); takes the place of
+        the data files the reference's server reads."""
+        self.ctx.set_background_grid(grid.n, grid.cent_min, grid.zone_length, grid.values)
+
     def AddDiffusion(self, proto, container):  # noqa: N802
         self._add(P.ROLE_DIFFUSION, proto, container)
 
@@ -137,6 +142,9 @@ def open_problems(problems: list[Problem] | Problem, precision: int = capi.SPX_F
     if record:
         opts[SPX_OPT_RECORD_FINAL] = 1
     sim = SimulationGPU(base.traj, base.time_flow, base.rk, precision, opts)
+    if base.grid is not None:
+        g = base.grid
+        sim.ctx.set_background_grid(g.n, g.cent_min, g.zone_length, g.values)
     for e in base.plugins:
         sim.ctx.add_plugin(e.plugin.role, e.plugin.kind, e.blob, e.n_records)
     for p in problems:

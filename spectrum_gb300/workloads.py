@@ -219,6 +219,54 @@ def gcr_modulation(n_traj: int = 1_000_000, energies_mev=None, lam0_au: float = 
 
 
 # ------------------------------------------------------------------------------------------------
+# 4b. the same modulation on a gridded background
+# ------------------------------------------------------------------------------------------------
+def parker_spiral_fields(x, y, z, dmax0: float = ONE_AU):
+    """U and B of the Parker spiral of solarwind_params at points (x, y, z) (numpy arrays): the
+    closed form U = ur r/|r|, B = A r/|r|^3 + k (|r| - r_ref)/|r|^3 (r x z), A = Br0 r_ref^2, k = A w0 / ur
+    (the field of src/background_solarwind.cc:111-249 in the global frame)."""
+    import numpy as np
+    umag = 4.0e7 / U.unit_velocity
+    rs = 6.957e10 / U.unit_length
+    r_ref = 3.0 * rs
+    bmag_ref = (5.0e-5 / U.unit_magnetic) * (ONE_AU / r_ref) ** 2
+    w0 = 2.0 * math.pi / (25.0 * 24.0 * 3600.0) * U.unit_time
+    a = bmag_ref * r_ref * r_ref
+    k = a * w0 / umag
+    r = np.sqrt(x * x + y * y + z * z)
+    pos = np.stack([x, y, z], axis=-1)
+    w = np.stack([y, -x, np.zeros_like(x)], axis=-1)  # r x z
+    u = (umag / r)[..., None] * pos
+    f = (r - r_ref) / r ** 3
+    b = (a / r ** 3)[..., None] * pos + (k * f)[..., None] * w
+    return u, b
+
+
+def gcr_modulation_grid(n_traj: int = 100_000, n_nodes: int = 256, half_width_au: float = 6.0,
+                        energies_mev=None, r_inner_au: float = 0.3, r_outer_au: float = 5.0,
+                        t_max_years: float = 0.2, **kw) -> list[Problem]:
+    """The modulation problems with the Parker spiral sampled on a uniform n^3 grid over
+    [-half_width, half_width]^3 AU (BackgroundServerCartesian, first-order interpolation). An even
+    node count keeps the nodes off the origin. Boundaries shrink to fit the block: outer sphere
+    r_outer_au (hot), inner sphere r_inner_au (cold, a few zones from the origin)."""
+    from .plugins import BackgroundServerCartesian
+    from .problem import Grid
+    if energies_mev is None:
+        energies_mev = modulation_energies(8, 30.0, 3.0e3)
+    h = half_width_au * ONE_AU
+    zone = 2.0 * h / (n_nodes - 1)
+    grid = Grid.sample((n_nodes,) * 3, (-h,) * 3, (zone,) * 3, parker_spiral_fields)
+    pbs = gcr_modulation(n_traj=n_traj, energies_mev=energies_mev, r_inner_au=r_inner_au, r_outer_au=r_outer_au,
+                         t_max_years=t_max_years, **kw)
+    for pb in pbs:
+        c = DataContainer()
+        c.double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0, 0, 0)).double(ONE_AU)
+        pb.plugins[0] = type(pb.plugins[0])(BackgroundServerCartesian(), c.data(), c.size())
+        pb.grid = grid
+    return pbs
+
+
+# ------------------------------------------------------------------------------------------------
 # 5. focused transport with pitch-angle scattering
 # ------------------------------------------------------------------------------------------------
 def focused_transport(n_problems: int = 64, n_min: int = 1000, n_max: int = 1_000_000, lam_au=(0.01, 1.0),

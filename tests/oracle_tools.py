@@ -75,6 +75,8 @@ def run_oracle(problem, first: int = 0, n: int | None = None, deriv_mode: int = 
         steps_per_orbit = problem.options.get(SPX_OPT_STEPS_PER_ORBIT, 100.0)
     if pa_scattering is None:
         pa_scattering = int(problem.options.get(SPX_OPT_PA_SCATTERING, 0))
+    if getattr(problem, "grid", None) is not None:
+        set_grid(problem.grid)
     return run_oracle_spec(problem.to_spec(), problem.traj, problem.time_flow, problem.rk,
                            problem.n_traj if n is None else n, first=first, deriv_mode=deriv_mode,
                            steps_per_orbit=steps_per_orbit, pa_scattering=pa_scattering, max_attempts=max_attempts,
@@ -109,6 +111,16 @@ def run_oracle_spec(spec: bytes, traj_kind: int, time_flow: int, rk: int, n: int
         off += nb
         soff += nb * w
     return OracleResult(traj, distros)
+
+
+def set_grid(grid) -> None:
+    """Hand a problem.Grid to the oracle (one grid at a time)."""
+    n = np.ascontiguousarray(np.asarray(grid.n, dtype=np.int64))
+    cm = np.ascontiguousarray(np.asarray(grid.cent_min, dtype=np.float64))
+    zl = np.ascontiguousarray(np.asarray(grid.zone_length, dtype=np.float64))
+    v = np.ascontiguousarray(np.asarray(grid.values, dtype=np.float64))
+    lib().spx_oracle_set_grid(n.ctypes.data_as(ctypes.c_void_p), cm.ctypes.data_as(ctypes.c_void_p),
+                              zl.ctypes.data_as(ctypes.c_void_p), v.ctypes.data_as(ctypes.c_void_p))
 
 
 def philox(ctr, key):

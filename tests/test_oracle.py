@@ -127,3 +127,25 @@ def test_oracle_matches_reference_live_smoothshock():
     pb = workloads.shock_acceleration(n_traj=6, s=3.0, x_escape=-1.5, x_downstream=1.5, p_max=8.0)
     pb.seed = 4242
     _assert_same(ot.run_oracle(pb, reference_quirks=1), ot.run_reference(pb))
+
+
+def test_oracle_grid_of_a_uniform_field_equals_uniform_background():
+    """A block holding B = (0, 0, 1) at every node gives the trajectories of BackgroundUniform:
+    the interpolation weights sum to one, so only rounding separates them."""
+    from spectrum_gb300.plugins import BackgroundServerCartesian
+    from spectrum_gb300.problem import Grid
+    pb = workloads.diffusion_uniform(n_traj=50, t_end=0.05)
+    ref = ot.run_oracle(pb)
+    n = 8
+    grid = Grid.sample((n,) * 3, (-5.0,) * 3, (10.0 / (n - 1),) * 3,
+                       lambda x, y, z: (np.zeros(x.shape + (3,)),
+                                        np.stack([np.zeros_like(x), np.zeros_like(x), np.ones_like(x)], axis=-1)))
+    blob_entry = pb.plugins[0]
+    from spectrum_gb300.datacontainer import DataContainer
+    c = DataContainer()  # the base parameters of diffusion_uniform's background (dmax0 = sqrt(2 kappa dt))
+    c.double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0, 0, 1.0)).double(float(np.sqrt(2.0e-3)))
+    pb.plugins[0] = type(blob_entry)(BackgroundServerCartesian(), c.data(), c.size())
+    pb.grid = grid
+    got = ot.run_oracle(pb)
+    assert np.array_equal(got.traj["steps"], ref.traj["steps"])
+    assert np.allclose(got.traj["pos"], ref.traj["pos"], rtol=1e-12, atol=1e-13)
