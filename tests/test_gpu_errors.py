@@ -33,10 +33,8 @@ def test_bad_set_ups_are_refused(built_lib):
     pb = workloads.diffusion_uniform(n_traj=10, t_end=0.01)
     # Parker is an Euler-Maruyama scheme: RK table 25 is refused
     assert _code(lambda: capi.Context(TRAJ_PARKER, 0, 25, capi.SPX_FP64)) == -1
-    # unknown background class
-    ctx = _ctx_with(pb, kind_edit=(0, 99))
-    assert _code(lambda: ctx.add_problem(10, 1)) == -2
-    ctx.close()
+    # unknown background class: refused when the plugin is added
+    assert _code(lambda: _ctx_with(pb, kind_edit=(0, 99))) == -2
     # parameter blob shorter than the class's list
     ctx = _ctx_with(pb, blob_edit=(0, lambda b: b[: len(b) // 2]))
     assert _code(lambda: ctx.add_problem(10, 1)) == -3
