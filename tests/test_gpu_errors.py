@@ -35,10 +35,8 @@ def test_bad_set_ups_are_refused(built_lib):
     assert _code(lambda: capi.Context(TRAJ_PARKER, 0, 25, capi.SPX_FP64)) == -1
     # unknown background class: refused when the plugin is added
     assert _code(lambda: _ctx_with(pb, kind_edit=(0, 99))) == -2
-    # parameter blob shorter than the class's list
-    ctx = _ctx_with(pb, blob_edit=(0, lambda b: b[: len(b) // 2]))
-    assert _code(lambda: ctx.add_problem(10, 1)) == -3
-    ctx.close()
+    # parameter blob shorter than the class's list: refused when the plugin is added
+    assert _code(lambda: _ctx_with(pb, blob_edit=(0, lambda b: b[: len(b) // 2]))) == -3
     # no time boundary: TrajectoryBase::IsSimmulationReady is false
     ctx = _ctx_with(pb, skip_role=3)
     assert _code(lambda: ctx.add_problem(10, 1)) == -4
