@@ -20,10 +20,13 @@ def _within_3sigma(a, b, min_count=20):
     return m.sum(), np.abs(a[m] - b[m]) <= 3.0 * np.sqrt(a[m] + b[m])
 
 
-def test_grid_fp64_matches_oracle(built_lib):
+@pytest.mark.parametrize("deriv_mode", [1, 0])
+def test_grid_fp64_matches_oracle(built_lib, deriv_mode):
+    """Trajectory by trajectory, with the analytic divergence of the diffusion tensor (1) and with
+    the reference's finite-difference one (0, TRAJ_PARKER_DIVK_METHOD 0)."""
     pbs = workloads.gcr_modulation_grid(n_traj=64, n_nodes=48, energies_mev=[300.0], t_max_years=0.05)
-    gpu = run_problems(pbs, precision=capi.SPX_FP64, record=True)
-    ref = ot.run_oracle(pbs[0], deriv_mode=1)
+    gpu = run_problems(pbs, precision=capi.SPX_FP64, record=True, deriv_mode=deriv_mode)
+    ref = ot.run_oracle(pbs[0], deriv_mode=deriv_mode)
     rec = gpu.records[0]
     agree = rec["steps"] == ref.traj["steps"]
     assert agree.mean() >= 0.9, agree.mean()
