@@ -131,10 +131,8 @@ int spx_add_problem(spx_ctx_t ctx, int64_t n_traj, uint64_t seed, const uint8_t*
  * node (i, j, k) at cent_min + (i, j, k) * zone_length, six doubles per node (U, then B, in code
  * units), x fastest. Replaces the data files the reference's server reads (the fname_pattern of
  * AddBackground, src/simulation.hh:111) and its MPI block server: the block is copied to device
- * memory now (this call allocates), shared by all problems of the context. The device copy is
- * stored cell by cell, each cell with its 8 corner nodes, so it takes 8 x 8 reals per cell (4.3 GB
- * for 256^3 nodes in SPX_MIXED, twice that in SPX_FP64; beyond 64 GB: SPX_ERR_TOO_LARGE). Points
- * whose 8-node stencil leaves the block are field errors (the trajectory is discarded and retried). */
+ * memory now (this call allocates), shared by all problems of the context. Points whose 8-node
+ * stencil leaves the block are field errors (the trajectory is discarded and retried). */
 int spx_set_background_grid(spx_ctx_t ctx, const int64_t n[3], const double cent_min[3], const double zone_length[3],
                             const double* values);
 

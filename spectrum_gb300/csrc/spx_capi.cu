@@ -12,7 +12,6 @@
 #include <cstring>
 #include <memory>
 #include <mutex>
-#include <new>
 #include <string>
 #include <vector>
 
@@ -492,9 +491,7 @@ int spx_set_background_grid(spx_ctx_t c, const int64_t n[3], const double cent_m
       if (n[k] < 2 || n[k] > 1000000 || !(zone_length[k] > 0.0) || !std::isfinite(cent_min[k])) return SPX_ERR_INVALID_ARG;
       nodes *= n[k];
    }
-   // the device copy holds every cell's 8 corner nodes: 8 x 8 values per cell
-   const size_t real_size = c->precision == SPX_FP64 ? sizeof(double) : sizeof(float);
-   if ((double)(n[0] - 1) * (n[1] - 1) * (n[2] - 1) * 64.0 * real_size > 64.0 * (1ull << 30)) return SPX_ERR_TOO_LARGE;
+   if (nodes > ((int64_t)1 << 31)) return SPX_ERR_TOO_LARGE;
    SPX_CUDA(cudaSetDevice(c->device));
    SPX_CUDA(cudaStreamSynchronize(c->stream));
    cudaFree(c->d_grid64);
@@ -502,51 +499,23 @@ int spx_set_background_grid(spx_ctx_t c, const int64_t n[3], const double cent_m
    c->d_grid64 = nullptr;
    c->d_grid32 = nullptr;
    c->has_grid = false;
-   try {
-      // node values with |B| appended (the magnitude the reference interpolates)
-      std::vector<double> node((size_t)nodes * spx::kGridStride, 0.0);
-      for (int64_t i = 0; i < nodes; i++) {
-         const double* v = values + 6 * i;
-         double* o = node.data() + spx::kGridStride * i;
-         for (int q = 0; q < 6; q++) o[q] = v[q];
-         const double bx2 = v[3] * v[3], by2 = v[4] * v[4], bz2 = v[5] * v[5];
-         o[6] = std::sqrt(bx2 + by2 + bz2);
-      }
-      // cell-major copy: cell (i, j, k) holds its 8 corner nodes, corner (ci, cj, ck) at 4 ck + 2 cj + ci,
-      // so one stencil is one contiguous 8-node span (256 B in FP32)
-      const int64_t cx = n[0] - 1, cy = n[1] - 1, cz = n[2] - 1, cells = cx * cy * cz;
-      const size_t count = (size_t)cells * 8 * spx::kGridStride;
-      auto fill = [&](auto* out) {
-         for (int64_t k = 0; k < cz; k++)
-            for (int64_t j = 0; j < cy; j++)
-               for (int64_t i = 0; i < cx; i++) {
-                  auto* cell = out + ((k * cy + j) * cx + i) * 8 * spx::kGridStride;
-                  for (int corner = 0; corner < 8; corner++) {
-                     const int64_t ni = i + (corner & 1), nj = j + ((corner >> 1) & 1), nk = k + ((corner >> 2) & 1);
-                     const double* src = node.data() + ((nk * n[1] + nj) * n[0] + ni) * spx::kGridStride;
-                     for (int q = 0; q < spx::kGridStride; q++) cell[corner * spx::kGridStride + q] = src[q];
-                  }
-               }
-      };
-      if (c->precision == SPX_FP64) {
-         std::vector<double> h(count);
-         fill(h.data());
-         SPX_CUDA(cudaMalloc(&c->d_grid64, sizeof(double) * count));
-         SPX_CUDA(cudaMemcpy(c->d_grid64, h.data(), sizeof(double) * count, cudaMemcpyHostToDevice));
-      }
-      else {
-         std::vector<float> h(count);
-         fill(h.data());
-         SPX_CUDA(cudaMalloc(&c->d_grid32, sizeof(float) * count));
-         SPX_CUDA(cudaMemcpy(c->d_grid32, h.data(), sizeof(float) * count, cudaMemcpyHostToDevice));
-      }
+   const size_t count = (size_t)nodes * spx::kGridStride;
+   std::vector<double> h(count, 0.0);
+   for (int64_t i = 0; i < nodes; i++) {
+      const double* v = values + 6 * i;
+      double* o = h.data() + spx::kGridStride * i;
+      for (int q = 0; q < 6; q++) o[q] = v[q];
+      const double bx2 = v[3] * v[3], by2 = v[4] * v[4], bz2 = v[5] * v[5];
+      o[6] = std::sqrt(bx2 + by2 + bz2);
    }
-   catch (const std::bad_alloc&) {
-      cudaFree(c->d_grid64);
-      cudaFree(c->d_grid32);
-      c->d_grid64 = nullptr;
-      c->d_grid32 = nullptr;
-      return SPX_ERR_OUT_OF_MEMORY;
+   if (c->precision == SPX_FP64) {
+      SPX_CUDA(cudaMalloc(&c->d_grid64, sizeof(double) * count));
+      SPX_CUDA(cudaMemcpy(c->d_grid64, h.data(), sizeof(double) * count, cudaMemcpyHostToDevice));
+   }
+   else {
+      std::vector<float> f(h.begin(), h.end());
+      SPX_CUDA(cudaMalloc(&c->d_grid32, sizeof(float) * count));
+      SPX_CUDA(cudaMemcpy(c->d_grid32, f.data(), sizeof(float) * count, cudaMemcpyHostToDevice));
    }
    for (int k = 0; k < 3; k++) {
       c->grid_n[k] = (int)n[k];

@@ -246,9 +246,8 @@ __device__ __forceinline__ bool solarwind_closed(const BgParamsT<R>& g, V3<R> po
 // the variables of GetVariablesInterp1 (:551-666: U and B interpolated, |B| interpolated from the
 // node magnitudes, E = -U x B / c, no region variable), dmax capped by the zone length
 // (:687), and the gradients of GetGradientsInterp1 (:724-823) from the stencil's derivative
-// weights. A node is 32 B in FP32 (two 16-byte loads), 64 B in FP64; the block is stored cell by
-// cell with each cell's 8 corner nodes contiguous, so a stencil is one 256 B span in FP32 (8x the
-// node data, traded for locality). A point whose stencil would leave the block is a field error.
+// weights. A node is 32 B in FP32 (two 16-byte loads), 64 B in FP64. A point whose stencil would
+// leave the block is a field error.
 __device__ __forceinline__ void load_node(const float* p, float* v)
 {
    const float4 a = __ldg(reinterpret_cast<const float4*>(p)), b = __ldg(reinterpret_cast<const float4*>(p) + 1);
@@ -274,9 +273,8 @@ __device__ __forceinline__ bool grid_fields(const BgParamsT<R>& g, V3<R> pos, un
       lo[k] = o - (R)z[k];
       hi[k] = R(1) - lo[k];
    }
-   // cell-major block: the cell's 8 corner nodes are contiguous (corner 4 ck + 2 cj + ci)
-   const int64_t cx = g.grid_n[0] - 1, cxy = cx * (int64_t)(g.grid_n[1] - 1);
-   const R* base = g.grid + ((int64_t)z[2] * cxy + (int64_t)z[1] * cx + z[0]) * (8 * kGridStride);
+   const int64_t nx = g.grid_n[0], nxy = nx * (int64_t)g.grid_n[1];
+   const R* base = g.grid + ((int64_t)z[2] * nxy + (int64_t)z[1] * nx + z[0]) * kGridStride;
    const bool grads = (mask & (kGradU | kGradB | kDUdt)) != 0;
    R var[6] = {R(0), R(0), R(0), R(0), R(0), R(0)}, bmag = R(0);
    R gr[6][3], gbm[3] = {R(0), R(0), R(0)};
@@ -287,7 +285,7 @@ __device__ __forceinline__ bool grid_fields(const BgParamsT<R>& g, V3<R> pos, un
       const int ci = c & 1, cj = (c >> 1) & 1, ck = (c >> 2) & 1;
       const R fx = ci ? lo[0] : hi[0], fy = cj ? lo[1] : hi[1], fz = ck ? lo[2] : hi[2];
       R v[7];
-      load_node(base + c * kGridStride, v);
+      load_node(base + ((int64_t)ck * nxy + (int64_t)cj * nx + ci) * kGridStride, v);
       const R w = fx * fy * fz;
 #pragma unroll
       for (int q = 0; q < 6; q++) var[q] += w * v[q];
