@@ -42,6 +42,7 @@ extern "C" {
 #define SPX_ERR_NO_DEVICE -11       /* no CUDA device, or not an sm_103 device */
 #define SPX_ERR_IO -12              /* spx_dump / spx_restore file error */
 #define SPX_ERR_TOO_LARGE -13       /* size beyond a fixed capacity */
+#define SPX_ERR_MISMATCH -14        /* a dump file of another distribution class or parameter set */
 
 /* ---- enumerations ---------------------------------------------------------------------- */
 /* trajectory types: the numbers of configure.ac:236-244 */
@@ -196,6 +197,19 @@ int spx_reset_distributions(spx_ctx_t ctx);
 /* Write / read all distributions (the checkpoint of src/simulation.cc:592-594, 714-720). */
 int spx_dump(spx_ctx_t ctx, const char* path);
 int spx_restore(spx_ctx_t ctx, const char* path);
+
+/* One distribution in the reference's own dump-file layout, so that files pass both ways between
+ * this library and the reference's post-processing and restart:
+ * spx_dump_distribution replaces DistributionTemplated::Dump (src/distribution_templated.cc:394-425),
+ * which the reference calls as distro_file_name + index + ".out" (src/simulation.cc:590-594, 790-793);
+ * spx_restore_distribution replaces DistributionTemplated::Restore (src/distribution_templated.cc:433-466),
+ * called for the distributions flagged by SimulationMaster::RestoreDistro (src/simulation.cc:714-720).
+ * The file's class name and parameter container must equal the distribution's: SPX_ERR_MISMATCH
+ * otherwise (the reference returns without restoring), SPX_ERR_IO for a missing or short file.
+ * Distribution records (keep_records) are not kept on the device: dumps carry empty record arrays
+ * and a restore reads past any. */
+int spx_dump_distribution(spx_ctx_t ctx, int problem, int distro, const char* path);
+int spx_restore_distribution(spx_ctx_t ctx, int problem, int distro, const char* path);
 
 const char* spx_strerror(int code);
 void spx_destroy(spx_ctx_t ctx);

@@ -18,6 +18,8 @@
  *                   f64 t0, f64 pos0[3], f64 mom0[3], f64 amp, f64 logwgt
  *   per distribution: u32 n_bins, u32 width, i32 counts[n_bins], f64 sums[n_bins*width],
  *                     i32 n_events
+ * With a third argument, each distribution is also written by its own Dump() to
+ * <dump_prefix><index>.out.
  */
 #include <chrono>
 #include <cstdio>
@@ -200,7 +202,7 @@ void PutVec(FILE* f, const GeoVector& v)
 int main(int argc, char** argv)
 {
    if (argc < 3) {
-      std::fprintf(stderr, "usage: %s spec.bin out.bin\n", argv[0]);
+      std::fprintf(stderr, "usage: %s spec.bin out.bin [dump_prefix]\n", argv[0]);
       return 2;
    }
    Reader rd;
@@ -291,6 +293,9 @@ int main(int argc, char** argv)
          Put<int32_t>(out, distros[d]->NEvents());
       }
       std::fclose(out);
+      // the reference's own dump files, named as its simulation names them (src/simulation.cc:790-793)
+      if (argc > 3)
+         for (size_t d = 0; d < distros.size(); d++) distros[d]->Dump(std::string(argv[3]) + std::to_string(d) + ".out");
       std::fprintf(stderr, "harness: %u trajectories, %llu steps, %.3f s\n", n_traj,
                    (unsigned long long)total_steps, secs);
    }

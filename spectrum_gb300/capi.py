@@ -21,12 +21,14 @@ SPX_OPT_PA_SCATTERING = 3
 SPX_OPT_RECORD_FINAL = 4
 SPX_OPT_MAX_ATTEMPTS = 5
 SPX_OPT_RUN_INDEX = 6
+SPX_ERR_IO = -12
+SPX_ERR_MISMATCH = -14
 
 #: the symbols include/spx.h declares
 EXPORTS = ["spx_create", "spx_set_option", "spx_add_plugin", "spx_add_problem", "spx_run", "spx_sync",
            "spx_get_distribution_info", "spx_get_distribution", "spx_get_records", "spx_reset_distributions",
            "spx_dump", "spx_restore", "spx_strerror", "spx_destroy", "spx_version", "spx_run_static",
-           "spx_autotune", "spx_set_background_grid"]
+           "spx_autotune", "spx_set_background_grid", "spx_dump_distribution", "spx_restore_distribution"]
 
 #: bytes of the fixed device array spx_run_static works in (SPX_STATIC_SCRATCH_BYTES)
 STATIC_SCRATCH_BYTES = 512 * 1024
@@ -80,6 +82,8 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         lib.spx_reset_distributions.argtypes = [c_vp]
         lib.spx_dump.argtypes = [c_vp, ctypes.c_char_p]
         lib.spx_restore.argtypes = [c_vp, ctypes.c_char_p]
+        lib.spx_dump_distribution.argtypes = [c_vp, c_int, c_int, ctypes.c_char_p]
+        lib.spx_restore_distribution.argtypes = [c_vp, c_int, c_int, ctypes.c_char_p]
         lib.spx_strerror.argtypes = [c_int]
         lib.spx_strerror.restype = ctypes.c_char_p
         lib.spx_destroy.argtypes = [c_vp]
@@ -203,6 +207,14 @@ class Context:
 
     def restore(self, path: str) -> None:
         check(self.lib.spx_restore(self._h, path.encode()), "spx_restore")
+
+    def dump_distribution(self, problem: int, distro: int, path: str) -> None:
+        """One distribution in the reference's dump-file layout (DistributionTemplated::Dump)."""
+        check(self.lib.spx_dump_distribution(self._h, problem, distro, path.encode()), "spx_dump_distribution")
+
+    def restore_distribution(self, problem: int, distro: int, path: str) -> None:
+        """One distribution from a reference dump file (DistributionTemplated::Restore)."""
+        check(self.lib.spx_restore_distribution(self._h, problem, distro, path.encode()), "spx_restore_distribution")
 
     def run_static(self, counts_ptr: int, n_counts: int, sums_ptr: int, n_sums: int, n_events_ptr: int,
                    n_events_len: int, records_ptr: int = 0, n_records: int = 0,

@@ -8,6 +8,7 @@
 // trajectory type, time flow, Runge-Kutta table and background class (these select the kernel).
 #include <algorithm>
 #include <cmath>
+#include <cstdint>
 #include <cstdio>
 #include <cstring>
 #include <memory>
@@ -27,12 +28,15 @@ namespace {
 
 struct PluginBlob {
    int role, kind;
+   uint32_t n_records;
    std::vector<uint8_t> blob;
 };
 
 struct ProblemHost {
    spx::ProblemDesc pd;
    int64_t n_traj;
+   // the parameter blob of each distribution slot: the container a reference dump file carries
+   PluginBlob dist[spx::kMaxDistro];
 };
 
 }  // namespace
@@ -357,6 +361,35 @@ int run_graph(spx_ctx* c, const spx::LaunchArgs& a)
 
 }  // namespace
 
+namespace {
+
+// The class names the reference gives its distribution classes (src/distribution_other.hh:72-573):
+// the first field of a DistributionTemplated dump file, and what a restore checks it against.
+const char* distro_class_name(int kind)
+{
+   switch (kind) {
+   case spx::kDsTimeUniform: return "DistributionTimeUniform";
+   case spx::kDsPositionUniform: return "DistributionPositionUniform";
+   case spx::kDsMomentumUniform: return "DistributionMomentumUniform";
+   case spx::kDsPositionMomentumUniform: return "DistributionPositionMomentumUniform";
+   case spx::kDsSpectrumPowerLaw: return "DistributionSpectrumKineticEnergyPowerLaw";
+   case spx::kDsSpectrumBentPowerLaw: return "DistributionSpectrumKineticEnergyBentPowerLaw";
+   case spx::kDsCumulative1: return "DistributionPositionCumulativeOrder1";
+   case spx::kDsCumulative2: return "DistributionPositionCumulativeOrder2";
+   case spx::kDsDivergenceFlow: return "DistributionDivergenceFlowPowerLaw";
+   case spx::kDsTimeMu: return "DistributionTimeMu";  // a class of this library only
+   default: return nullptr;
+   }
+}
+
+template <class T>
+bool put(FILE* f, const T* v, size_t n) { return n == 0 || std::fwrite(v, sizeof(T), n, f) == n; }
+
+template <class T>
+bool get(FILE* f, T* v, size_t n) { return n == 0 || std::fread(v, sizeof(T), n, f) == n; }
+
+}  // namespace
+
 extern "C" {
 
 int spx_create(spx_ctx_t* out, int traj_kind, int time_flow, int rk_method, int precision)
@@ -432,14 +465,14 @@ int spx_set_option(spx_ctx_t c, int option, double value)
 int spx_add_plugin(spx_ctx_t c, int role, int kind, const uint8_t* blob, size_t blob_len, size_t n_records)
 {
    if (!valid_ctx(c) || (blob_len && !blob) || role < 0 || role > SPX_ROLE_DISTRIBUTION) return SPX_ERR_INVALID_ARG;
-   (void)n_records;
+   if (n_records > 0xffffffffu) return SPX_ERR_INVALID_ARG;
    // parse now so a malformed blob is reported where it is added
    spx::ProblemDesc probe;
    std::memset(&probe, 0, sizeof probe);
    int rc = spx::parse_plugin(probe, c->traj, role, kind, blob, blob_len, -1);
    if (rc != SPX_OK) return rc;
    if (role == SPX_ROLE_SOURCE && c->traj != SPX_TRAJ_PARKER_SOURCE) return SPX_ERR_UNKNOWN_PLUGIN;
-   c->base.push_back(PluginBlob{role, kind, std::vector<uint8_t>(blob, blob + blob_len)});
+   c->base.push_back(PluginBlob{role, kind, (uint32_t)n_records, std::vector<uint8_t>(blob, blob + blob_len)});
    return SPX_OK;
 }
 
@@ -451,6 +484,7 @@ int spx_add_problem(spx_ctx_t c, int64_t n_traj, uint64_t seed, const uint8_t* o
    for (const auto& p : c->base) {
       int rc = spx::parse_plugin(ph.pd, c->traj, p.role, p.kind, p.blob.data(), p.blob.size(), -1);
       if (rc != SPX_OK) return rc;
+      if (p.role == SPX_ROLE_DISTRIBUTION) ph.dist[ph.pd.nd - 1] = p;
    }
    size_t pos = 0;
    while (pos < ov_len) {
@@ -463,6 +497,7 @@ int spx_add_problem(spx_ctx_t c, int64_t n_traj, uint64_t seed, const uint8_t* o
       bool slotted = role == SPX_ROLE_BOUNDARY || role == SPX_ROLE_DISTRIBUTION;
       int rc = spx::parse_plugin(ph.pd, c->traj, role, kind, ov + pos, hdr[4], slotted ? slot : -1);
       if (rc != SPX_OK) return rc;
+      if (role == SPX_ROLE_DISTRIBUTION) ph.dist[slot] = PluginBlob{role, kind, hdr[3], std::vector<uint8_t>(ov + pos, ov + pos + hdr[4])};
       pos += hdr[4];
    }
    int rc = spx::check_ready(ph.pd, c->traj);
@@ -883,6 +918,96 @@ int spx_restore(spx_ctx_t c, const char* path)
    return SPX_OK;
 }
 
+// One distribution in the file layout of DistributionTemplated::Dump (src/distribution_templated.cc:
+// 394-425), native little-endian: u32 name length, the class name, one byte of Specie (a class of
+// static members only, so sizeof is 1 and the byte is 0), u32 records and u32 bytes of the parameter
+// container and its bytes, i32 n_events, i32 counts[bins], the per-bin sums (1, 3 or 9 doubles), then
+// u32 0 and u32 0 for the two empty record arrays (records are not kept on the device).
+int spx_dump_distribution(spx_ctx_t c, int problem, int distro, const char* path)
+{
+   int64_t nb = 0;
+   int w = 0;
+   if (!path) return SPX_ERR_INVALID_ARG;
+   int rc = spx_get_distribution_info(c, problem, distro, &nb, &w);
+   if (rc != SPX_OK) return rc;
+   const PluginBlob& pb = c->problems[problem].dist[distro];
+   const char* name = distro_class_name(pb.kind);
+   if (!name) return SPX_ERR_INVALID_ARG;
+   std::vector<int32_t> counts(nb);
+   std::vector<double> sums(nb * w);
+   int64_t ne = 0;
+   rc = spx_get_distribution(c, problem, distro, counts.data(), sums.data(), &ne);
+   if (rc != SPX_OK) return rc;
+   if (ne > INT32_MAX) return SPX_ERR_LIMIT;  // the file's event count is an int
+   FILE* f = std::fopen(path, "wb");
+   if (!f) return SPX_ERR_IO;
+   const uint32_t name_len = (uint32_t)std::strlen(name), n_rec = pb.n_records, blob_len = (uint32_t)pb.blob.size();
+   const uint8_t specie = 0;
+   const int32_t ne32 = (int32_t)ne;
+   const uint32_t no_records[2] = {0, 0};
+   bool ok = put(f, &name_len, 1) && put(f, name, name_len) && put(f, &specie, 1) && put(f, &n_rec, 1) &&
+             put(f, &blob_len, 1) && put(f, pb.blob.data(), blob_len) && put(f, &ne32, 1) &&
+             put(f, counts.data(), (size_t)nb) && put(f, sums.data(), (size_t)(nb * w)) && put(f, no_records, 2);
+   ok = (std::fclose(f) == 0) && ok;
+   return ok ? SPX_OK : SPX_ERR_IO;
+}
+
+// DistributionTemplated::Restore (src/distribution_templated.cc:433-466) for a distribution whose binning
+// is already fixed by its problem: the file's class name and parameter container must equal this
+// distribution's (else SPX_ERR_MISMATCH, where the reference returns without restoring); its counts,
+// sums and event count replace the device histogram. Record arrays in the file are read past.
+int spx_restore_distribution(spx_ctx_t c, int problem, int distro, const char* path)
+{
+   int64_t nb = 0;
+   int w = 0;
+   if (!path) return SPX_ERR_INVALID_ARG;
+   int rc = spx_get_distribution_info(c, problem, distro, &nb, &w);
+   if (rc != SPX_OK) return rc;
+   const PluginBlob& pb = c->problems[problem].dist[distro];
+   const char* name = distro_class_name(pb.kind);
+   if (!name) return SPX_ERR_INVALID_ARG;
+   if (c->dirty) {
+      rc = upload(c);
+      if (rc != SPX_OK) return rc;
+   }
+   FILE* f = std::fopen(path, "rb");
+   if (!f) return SPX_ERR_IO;
+   rc = SPX_OK;
+   uint32_t name_len = 0, n_rec = 0, blob_len = 0, n_values = 0, n_weights = 0;
+   uint8_t specie = 0;
+   int32_t ne = 0;
+   std::string file_name;
+   std::vector<uint8_t> blob;
+   std::vector<int32_t> counts(nb);
+   std::vector<double> sums(nb * w);
+   if (!get(f, &name_len, 1) || name_len > 4096) rc = SPX_ERR_IO;
+   if (rc == SPX_OK) {
+      file_name.resize(name_len);
+      if (!get(f, file_name.data(), name_len)) rc = SPX_ERR_IO;
+      else if (file_name != name) rc = SPX_ERR_MISMATCH;
+   }
+   if (rc == SPX_OK && !(get(f, &specie, 1) && get(f, &n_rec, 1) && get(f, &blob_len, 1))) rc = SPX_ERR_IO;
+   if (rc == SPX_OK && blob_len != pb.blob.size()) rc = SPX_ERR_MISMATCH;
+   if (rc == SPX_OK) {
+      blob.resize(blob_len);
+      if (!get(f, blob.data(), blob_len)) rc = SPX_ERR_IO;
+      else if (blob != pb.blob || n_rec != pb.n_records) rc = SPX_ERR_MISMATCH;
+   }
+   if (rc == SPX_OK && !(get(f, &ne, 1) && ne >= 0 && get(f, counts.data(), (size_t)nb) &&
+                         get(f, sums.data(), (size_t)(nb * w)) && get(f, &n_values, 1) &&
+                         std::fseek(f, (long)n_values * 24, SEEK_CUR) == 0 && get(f, &n_weights, 1)))
+      rc = SPX_ERR_IO;
+   std::fclose(f);
+   if (rc != SPX_OK) return rc;
+   const spx::DistParams& dp = c->problems[problem].pd.d[distro];
+   const unsigned long long neu = (unsigned long long)ne;
+   SPX_CUDA(cudaStreamSynchronize(c->stream));
+   SPX_CUDA(cudaMemcpy(c->d_counts + dp.offset_counts, counts.data(), sizeof(int32_t) * nb, cudaMemcpyHostToDevice));
+   SPX_CUDA(cudaMemcpy(c->d_sums + dp.offset_sums, sums.data(), sizeof(double) * nb * w, cudaMemcpyHostToDevice));
+   SPX_CUDA(cudaMemcpy(c->d_nev + (int64_t)problem * spx::kMaxDistro + distro, &neu, sizeof neu, cudaMemcpyHostToDevice));
+   return SPX_OK;
+}
+
 const char* spx_strerror(int code)
 {
    switch (code) {
@@ -899,6 +1024,7 @@ const char* spx_strerror(int code)
    case SPX_ERR_NO_DEVICE: return "no sm_103 CUDA device";
    case SPX_ERR_IO: return "checkpoint file error";
    case SPX_ERR_TOO_LARGE: return "size beyond a fixed capacity";
+   case SPX_ERR_MISMATCH: return "dump file written for another distribution class or parameter set";
    default: return "unknown error";
    }
 }

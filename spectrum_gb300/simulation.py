@@ -32,6 +32,8 @@ class SimulationGPU:
             self.ctx.set_option(k, v)
         self._distro_names: list[str] = []
         self._file_prefix = ""
+        self._restore: set[int] = set()
+        self._n_problems = 0
         self.stats: capi.Stats | None = None
 
     # -- plugin set-up (src/simulation.hh:105-123) ----------------------------------------------
@@ -68,7 +70,8 @@ class SimulationGPU:
     # -- tasks and the main loop -----------------------------------------------------------------
     def SetTasks(self, n_traj: int, batch_size: int = 0, max_traj_per_worker: int = 0, seed: int = 0x5EED0000):  # noqa: N802
         """One problem of n_traj trajectories (batch sizes belong to the MPI farm and are ignored)."""
-        return self.ctx.add_problem(n_traj, seed)
+        self.ctx.add_problem(n_traj, seed)
+        self._n_problems += 1
 
     def AddProblem(self, n_traj: int, seed: int, overrides=()):  # noqa: N802
         """A further problem: ``overrides`` is a list of (role, slot, prototype, DataContainer)."""
@@ -76,24 +79,49 @@ class SimulationGPU:
         for role, slot, proto, c in overrides:
             data = c.data()
             blob += struct.pack("<5I", role, slot, proto.kind, c.size(), len(data)) + data
-        return self.ctx.add_problem(n_traj, seed, bytes(blob))
+        self.ctx.add_problem(n_traj, seed, bytes(blob))
+        self._n_problems += 1
 
     def MainLoop(self, tuning: capi.Tuning | None = None) -> capi.Stats:  # noqa: N802
+        """Restore the distributions flagged by RestoreDistro, run every problem's trajectories, and,
+        when DistroFileName gave a file name, dump every distribution (src/simulation.cc:705-793).
+        Distributions accumulate over MainLoop calls (reset them with ctx.reset_distributions)."""
+        for d in sorted(self._restore):
+            for p in range(self._n_problems):
+                try:
+                    self.ctx.restore_distribution(p, d, self.distro_path(d, p))
+                except capi.SpxError as e:
+                    # DistributionTemplated::Restore returns quietly on a missing file or another class
+                    if e.code not in (capi.SPX_ERR_IO, capi.SPX_ERR_MISMATCH):
+                        raise
         self.ctx.run(tuning)
         self.stats = self.ctx.sync()
+        if self._file_prefix:
+            self.DumpDistro()
         return self.stats
 
     def GetTrajectoryName(self) -> str:  # noqa: N802
         return TRAJ_NAMES.get(self.traj, "Trajectory")
 
     def DistroFileName(self, file_name: str) -> None:  # noqa: N802
+        """Prefix of the dump files: distribution d of the first problem is <prefix><d>.out, the
+        reference's name (src/simulation.cc:790-793); of problem p > 0, <prefix><d>_problem<p>.out."""
         self._file_prefix = file_name
 
-    def RestoreDistro(self, distro: int = 0) -> None:  # noqa: N802
-        self.ctx.restore(self._file_prefix + "distros.spx")
+    def distro_path(self, distro: int, problem: int = 0) -> str:
+        suffix = "" if problem == 0 else f"_problem{problem}"
+        return f"{self._file_prefix}{distro}{suffix}.out"
+
+    def RestoreDistro(self, distro: int) -> None:  # noqa: N802
+        """Flag distribution ``distro`` to be restored from its dump file when MainLoop starts
+        (SimulationMaster::RestoreDistro, src/simulation.cc:714-720)."""
+        self._restore.add(distro)
 
     def DumpDistro(self) -> None:  # noqa: N802
-        self.ctx.dump(self._file_prefix + "distros.spx")
+        """Every distribution of every problem in the reference's dump-file layout."""
+        for p in range(self._n_problems):
+            for d in range(len(self._distro_names)):
+                self.ctx.dump_distribution(p, d, self.distro_path(d, p))
 
     def distribution(self, distro: int, problem: int = 0):
         return self.ctx.distribution(problem, distro)
@@ -147,8 +175,12 @@ def open_problems(problems: list[Problem] | Problem, precision: int = capi.SPX_F
         sim.ctx.set_background_grid(g.n, g.cent_min, g.zone_length, g.values)
     for e in base.plugins:
         sim.ctx.add_plugin(e.plugin.role, e.plugin.kind, e.blob, e.n_records)
+    for e in base.plugins:
+        if e.plugin.role == P.ROLE_DISTRIBUTION:
+            sim._distro_names.append(e.plugin.name)
     for p in problems:
         sim.ctx.add_problem(p.n_traj, p.seed, _diff_overrides(base, p))
+        sim._n_problems += 1
     return sim
 
 

@@ -9,6 +9,10 @@ sources must be present to run this script; the fixtures it writes are then used
 including where the sources are not.
 
     python tests/golden/make_golden.py          # rewrites tests/golden/*.npz
+    python tests/golden/make_golden.py --dumps  # rewrites tests/golden/*.distro<d>.out
+
+The second form keeps the reference's own distribution dump files (DistributionTemplated::Dump)
+of the fixtures whose distributions have at most DUMP_MAX_BINS bins: the pins of the dump format.
 """
 from __future__ import annotations
 
@@ -101,7 +105,31 @@ def sparse(distros):
     return out
 
 
+DUMP_MAX_BINS = 4096
+
+
+def write_dumps():
+    import tempfile
+
+    import oracle_tools as ot
+    for name, pb in cases():
+        with tempfile.TemporaryDirectory() as td:
+            ref = ot.run_reference(pb, dump_prefix=os.path.join(td, "distro"))
+            for d, (counts, _, _) in enumerate(ref.distros):
+                if len(counts) > DUMP_MAX_BINS:
+                    continue
+                with open(os.path.join(td, f"distro{d}.out"), "rb") as f:
+                    data = f.read()
+                path = os.path.join(HERE, f"{name}.distro{d}.out")
+                with open(path, "wb") as f:
+                    f.write(data)
+                print(f"{name}.distro{d}.out: {len(data)} bytes")
+
+
 def main():
+    if "--dumps" in sys.argv[1:]:
+        write_dumps()
+        return
     import oracle_tools as ot
     for name, pb in cases():
         ref = ot.run_reference(pb)

@@ -207,8 +207,9 @@ def parse_ref_output(buf: bytes, sizes) -> OracleResult:
     return OracleResult(traj, distros)
 
 
-def run_reference(problem, timeout: float = 600.0) -> OracleResult:
-    """Run the reference's own code (oracle/_ref) on ``problem``."""
+def run_reference(problem, timeout: float = 600.0, dump_prefix: str | None = None) -> OracleResult:
+    """Run the reference's own code (oracle/_ref) on ``problem``. With ``dump_prefix``, the
+    reference's DistributionTemplated::Dump also writes each distribution to <prefix><index>.out."""
     exe = ref_binary(problem)
     if exe is None:
         raise FileNotFoundError("reference harness not built for this trajectory type")
@@ -217,7 +218,8 @@ def run_reference(problem, timeout: float = 600.0) -> OracleResult:
         out_path = os.path.join(td, "out.bin")
         with open(spec_path, "wb") as f:
             f.write(problem.to_spec())
-        r = subprocess.run([exe, spec_path, out_path], capture_output=True, text=True, timeout=timeout)
+        cmd = [exe, spec_path, out_path] + ([dump_prefix] if dump_prefix else [])
+        r = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout)
         if r.returncode != 0:
             raise RuntimeError(f"reference harness failed: {r.stderr[-2000:]}")
         with open(out_path, "rb") as f:
