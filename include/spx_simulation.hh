@@ -256,19 +256,42 @@ public:
       }
    }
 
+   // Prefix of the dump files: distribution d of the first problem is <prefix><d>.out, the reference's
+   // name (src/simulation.cc:790-793); of problem p > 0, <prefix><d>_problem<p>.out.
    void DistroFileName(const std::string& file_name) { prefix_ = file_name; }
+   std::string DistroPath(int distro, int problem = 0) const
+   {
+      return prefix_ + std::to_string(distro) + (problem ? "_problem" + std::to_string(problem) : std::string()) + ".out";
+   }
 
-   // src/simulation.cc:818-835: every trajectory of every problem, then wait.
+   // src/simulation.cc:705-793: restore the flagged distributions, every trajectory of every problem,
+   // wait, and dump every distribution when a file name was given.
    spx_stats MainLoop(void)
    {
+      for (int d : restore_)
+         for (int p = 0; p < n_problems_; p++) {
+            int rc = spx_restore_distribution(ctx_, p, d, DistroPath(d, p).c_str());
+            // DistributionTemplated::Restore returns quietly on a missing file or another class
+            if (rc != SPX_OK && rc != SPX_ERR_IO && rc != SPX_ERR_MISMATCH) check(rc, "RestoreDistro");
+         }
       check(spx_run(ctx_, nullptr), "spx_run");
       spx_stats st;
       check(spx_sync(ctx_, &st), "spx_sync");
+      if (!prefix_.empty()) DumpDistro();
       return st;
    }
 
-   void RestoreDistro(int = 0) { check(spx_restore(ctx_, (prefix_ + "distros.spx").c_str()), "RestoreDistro"); }
-   void DumpDistro(void) { check(spx_dump(ctx_, (prefix_ + "distros.spx").c_str()), "DumpDistro"); }
+   // SimulationMaster::RestoreDistro (src/simulation.cc:714-720): restore distribution d from its dump
+   // file when MainLoop starts.
+   void RestoreDistro(int distro) { restore_.push_back(distro); }
+
+   // Every distribution of every problem in the reference's dump-file layout (DistributionTemplated::Dump).
+   void DumpDistro(void)
+   {
+      for (int p = 0; p < n_problems_; p++)
+         for (int d = 0; d < (int)distro_names_.size(); d++)
+            check(spx_dump_distribution(ctx_, p, d, DistroPath(d, p).c_str()), "DumpDistro");
+   }
 
    // Bin index, count and mean weight per bin of one distribution of one problem (the columns of
    // DistributionTemplated::Print1D, src/distribution_templated.cc:546-590, in code units).
@@ -290,6 +313,7 @@ public:
 
 private:
    int n_problems_ = 0;
+   std::vector<int> restore_;
 };
 
 }  // namespace spx

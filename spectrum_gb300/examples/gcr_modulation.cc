@@ -4,7 +4,7 @@
 // the reference's own modulation run (runs/gcr_modulation_example.cc:76-332); only the includes
 // and the simulation object differ.
 //
-//   build: g++ -std=c++17 -O2 -I include spectrum_gb300/examples/gcr_modulation.cc
+//   build: g++ -std=c++17 -O2 -ffp-contract=off -I include spectrum_gb300/examples/gcr_modulation.cc
 //              -L spectrum_gb300/_lib -lspx -Wl,-rpath,$PWD/spectrum_gb300/_lib -o gcr_modulation
 //   run:   ./gcr_modulation <n_energies> <trajectories per energy> <years> <precision 0|1> <out prefix>
 // Prints one line per energy: problem, kinetic energy (MeV), counts in the spectrum, weighted sum.

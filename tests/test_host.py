@@ -110,7 +110,9 @@ def _build_example(built_lib, tmp_path):
         pytest.skip("no g++")
     exe = str(tmp_path / "gcr_modulation")
     lib_dir = os.path.dirname(built_lib)
-    subprocess.run([gxx, "-std=c++17", "-O2", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+    # no fused multiply-add contraction (gcc's default on aarch64): the blobs' doubles must round as
+    # Python's do, operation by operation
+    subprocess.run([gxx, "-std=c++17", "-O2", "-ffp-contract=off", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
                     os.path.join(ROOT, "spectrum_gb300", "examples", "gcr_modulation.cc"), "-L", lib_dir, "-lspx",
                     f"-Wl,-rpath,{lib_dir}", "-o", exe], check=True)
     return exe
