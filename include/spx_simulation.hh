@@ -249,6 +249,8 @@ public:
    {
       switch (traj_) {
       case SPX_TRAJ_LORENTZ: return "TrajectoryLorentz";
+      case SPX_TRAJ_GUIDING: return "TrajectoryGuiding";
+      case SPX_TRAJ_GUIDING_SCATT: return "TrajectoryGuidingScatt";
       case SPX_TRAJ_FOCUSED: return "TrajectoryFocused";
       case SPX_TRAJ_PARKER: return "TrajectoryParker";
       case SPX_TRAJ_PARKER_SOURCE: return "TrajectoryParkerSource";

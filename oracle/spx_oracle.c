@@ -668,8 +668,10 @@ typedef struct {
    /* Parker */
    v3 drift_vel, divK, dr_perp;
    double Kperp, Kpara;
-   /* Focused */
+   /* Focused, GuidingScatt */
    double Dmumu, Vmu;
+   /* Guiding: the modified fields E*, B* of the last drift evaluation */
+   v3 e_star, b_star;
    /* SourceMomentumInjection state (del_mom_old, src/source_other.cc:113-119) */
    double src_del_old;
    /* BackgroundSmoothShock::ds_shock of the last field evaluation; like the reference's background
@@ -1044,7 +1046,7 @@ static int get_fields(trj_t* T, double t, v3 pos, v3 mom_pmu, unsigned mask, spd
       for (a = 0; a < 3; a++)
          for (b = 0; b < 3; b++) {
             double unit = (a == b) ? 1.0 : 0.0;
-            s->gradB.m[a][b] = 3.0 * (g->M.x[a] * pp.x[b] + pp.x[a] * g->M.x[b] + mdotr * (unit - 5.0 * pp.x[a] * pp.x[b] / r2)) / r5;
+            s->gradB.m[a][b] = 3.0 * (g->M.x[a] * pp.x[b] + pp.x[a] * g->M.x[b] + mdotr * (unit - 5.0 * (pp.x[a] * pp.x[b]) / r2)) / r5;
          }
       s->gradBmag = mvmul(&s->gradB, s->bhat);
       s->dUdt = V(0, 0, 0); s->dBdt = V(0, 0, 0); s->dBmagdt = 0.0;
@@ -1266,7 +1268,7 @@ static void eval_bnd(trj_t* T, bnd_t* b, double t, v3 pos, v3 mom, v3 bhat, v3 r
    }
    case BT_REGION: b->delta = region.x[b->region_ind] - b->region_val; b->normal = V(0, 0, 0); break;
    case BT_MOM_INJ: case BT_MOM_PASS: case BT_MOM_SLAB: case BT_MOM_SHELL:
-      if (tt == 200) b->delta = vnorm(mom) - b->momentum;
+      if (tt == 200 || tt == 201 || tt == 202) b->delta = vnorm(mom) - b->momentum;
       else b->delta = mom.x[0] - b->momentum;
       if (b->kind == BT_MOM_SLAB && b->delta * b->delta_old < 0.0) {
          if (vdot(vsub(pos, b->slab_r0), b->slab_n) * vdot(vsub(pos, b->slab_r1), b->slab_n) > 0.0) b->delta_old = b->delta;
@@ -1278,6 +1280,7 @@ static void eval_bnd(trj_t* T, bnd_t* b, double t, v3 pos, v3 mom, v3 bhat, v3 r
       break;
    case BT_MIRROR:
       if (tt == 205) b->delta = mom.x[0] * mom.x[1];
+      else if (tt == 201 || tt == 202) b->delta = mom.x[2];  /* the parallel component */
       else b->delta = vdot(mom, bhat);
       break;
    }
@@ -1351,8 +1354,9 @@ static void process_trajectory(trj_t* T, int di, int action)
    case DS_MOM: {
       v3 m = (d->val_time == 0) ? T->mom0 : T->mom;
       v3 bh = (d->val_time == 0) ? s1->bhat : s2->bhat;
-      if (d->val_coord == 0 || tt != 200) value = m;
-      else { value.x[0] = vnorm(m); value.x[1] = vdot(m, bh) / value.x[0]; value.x[2] = 0.0; }
+      if (d->val_coord == 0 || (tt != 200 && tt != 201 && tt != 202)) value = m;
+      else if (tt == 200) { value.x[0] = vnorm(m); value.x[1] = vdot(m, bh) / value.x[0]; value.x[2] = 0.0; }
+      else { value.x[0] = vnorm(m); value.x[1] = m.x[2] / value.x[0]; value.x[2] = 0.0; }
       break;
    }
    case DS_POSMOM: {
@@ -1361,12 +1365,12 @@ static void process_trajectory(trj_t* T, int di, int action)
       value.x[1] = m.x[d->mom_idx];
       break;
    }
-   case DS_SPEC: case DS_SPECBENT: value.x[0] = enr_kin(tt == 200 ? vnorm(T->mom0) : T->mom0.x[0]); break;
+   case DS_SPEC: case DS_SPECBENT: value.x[0] = enr_kin((tt >= 200 && tt <= 202) ? vnorm(T->mom0) : T->mom0.x[0]); break;
    case DS_CUM1: case DS_CUM2: value.x[0] = T->t; break;
    case DS_DIVFLOW: value = T->mom0; break;
    case DS_TIMEMU:
       value.x[0] = T->t;
-      value.x[1] = (tt == 200) ? vdot(T->mom, s2->bhat) / vnorm(T->mom) : T->mom.x[1];
+      value.x[1] = (tt == 200) ? vdot(T->mom, s2->bhat) / vnorm(T->mom) : (tt == 201 || tt == 202) ? T->mom.x[2] / vnorm(T->mom) : T->mom.x[1];
       break;
    }
    /* EvaluateWeight */
@@ -1376,7 +1380,7 @@ static void process_trajectory(trj_t* T, int di, int action)
       break;
    case DS_SPEC: case DS_SPECBENT:
       if (action == 0) {
-         double m2 = (tt == 200) ? vnorm(T->mom) : T->mom.x[0];
+         double m2 = (tt >= 200 && tt <= 202) ? vnorm(T->mom) : T->mom.x[0];
          double ke = enr_kin(m2), v = vel_of(m2);
          w[0] = d->J0 * v * pow(ke / d->T0, d->pow_law) / (m2 * m2);
          if (d->kind == DS_SPECBENT) w[0] /= pow(1.0 + pow(ke / d->T_b, d->pow_law_comb), d->bend);
@@ -1504,6 +1508,7 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
    case IM_FIXED: return q->v0;
    case IM_BEAM:
       if (tt == 200) return vscale(q->a[0], axis);
+      if (tt == 201 || tt == 202) return V(0.0, 0.0, q->a[0]);
       return V(q->a[0], 0.0, 0.0);
    case IM_RING:
       if (tt == 200) {
@@ -1512,6 +1517,7 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
          v3 m = vscale(q->a[0] * q->a[2], axis);
          return vadd(m, vscale(q->a[0] * q->a[3], vadd(vscale(cos(phi), e1), vscale(sin(phi), e2))));
       }
+      if (tt == 201 || tt == 202) return V(q->a[0] * q->a[3], 0.0, q->a[0] * q->a[2]);
       return V(q->a[0], q->a[2], 0.0);
    case IM_SHELL: case IM_THICK: {
       double p = q->a[0];
@@ -1523,6 +1529,10 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
       if (tt == 205) {
          double mu = -1.0 + 2.0 * next_uniform(T);
          return V(p, mu, 0.0);
+      }
+      if (tt == 201 || tt == 202) {
+         double mu = -1.0 + 2.0 * next_uniform(T), st = sqrt(1.0 - mu * mu);
+         return V(p * st, 0.0, p * mu);
       }
       {
          double mu = -1.0 + 2.0 * next_uniform(T), st = sqrt(1.0 - mu * mu), phi = M_2PI_ * next_uniform(T);
@@ -1537,6 +1547,7 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
          v3 e1 = second_unit(axis), e2 = vcross(axis, e1);
          return vadd(vscale(p_para, axis), vscale(p_perp, vadd(vscale(cos(phi), e1), vscale(sin(phi), e2))));
       }
+      if (tt == 201 || tt == 202) return V(p_perp, 0.0, p_para);
       {
          double p = sqrt(p_para * p_para + p_perp * p_perp);
          if (tt == 205) return V(p, p_para / p, 0.0);
@@ -1554,6 +1565,7 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
          return vadd(vscale(p * mu, axis), vscale(p * st, vadd(vscale(cos(psi), e1), vscale(sin(psi), e2))));
       }
       if (tt == 205) return V(p, mu, 0.0);
+      if (tt == 201 || tt == 202) return V(p * sqrt(1.0 - mu * mu), 0.0, p * mu);
       return V(p, 0.0, 0.0);
    }
    }
@@ -1564,6 +1576,7 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
 /* trajectory machinery                                                                       */
 /* ------------------------------------------------------------------------------------------ */
 static int is_parker(const trj_t* T) { return T->o->traj_type == 206 || T->o->traj_type == 207; }
+static int is_guiding(const trj_t* T) { return T->o->traj_type == 201 || T->o->traj_type == 202; }
 static int fwd(const trj_t* T) { return T->o->time_flow == 0; }
 
 /* ConvertMomentum: Parker/Focused native (p, mu, -); Lorentz (|p|, p.b/|p|, 0)
@@ -1574,6 +1587,8 @@ static v3 convert_mom(const trj_t* T)
       double m = vnorm(T->mom);
       return V(m, vdot(T->mom, T->sp.bhat) / m, 0.0);
    }
+   /* Guiding: (p_perp, -, p_para) -> (p, mu, 0), src/trajectory_guiding.hh:113-116 */
+   if (is_guiding(T)) return V(sqrt(T->mom.x[0] * T->mom.x[0] + T->mom.x[2] * T->mom.x[2]), T->mom.x[2] / vnorm(T->mom), 0.0);
    return T->mom;
 }
 
@@ -1582,6 +1597,8 @@ static unsigned traj_mask(const trj_t* T)
    switch (T->o->traj_type) {
    case 200: return BG_E | BG_B;                                  /* src/trajectory_lorentz.cc:36 */
    case 205: return BG_ALL | BG_gradB | BG_gradU | BG_dUdt;       /* src/trajectory_focused.cc:40 */
+   /* src/trajectory_guiding.cc:51-52 adds dB/dt, which is zero for every static background */
+   case 201: case 202: return BG_ALL | BG_gradB;
    default: return BG_U | BG_B | BG_gradU | BG_gradB;             /* src/trajectory_parker.cc:204 */
    }
 }
@@ -1692,6 +1709,19 @@ static void time_proximity(trj_t* T)
 static void store(trj_t* T) { T->segments++; }
 
 /* HandleBoundaries, src/trajectory_base.cc:413-535 */
+/* ReverseMomentum: the base negates the vector (src/trajectory_base.cc:139-142), Focused its mu
+ * (src/trajectory_focused.hh:141-144), Guiding its parallel component (src/trajectory_guiding.hh:123-126),
+ * Parker does nothing (src/trajectory_parker.hh:129-131) */
+static void reverse_momentum(trj_t* T)
+{
+   switch (T->o->traj_type) {
+   case 205: T->mom.x[1] = -T->mom.x[1]; break;
+   case 201: case 202: T->mom.x[2] = -T->mom.x[2]; break;
+   case 206: case 207: break;
+   default: T->mom = vscale(-1.0, T->mom);
+   }
+}
+
 static void handle_boundaries(trj_t* T)
 {
    int b;
@@ -1714,7 +1744,7 @@ static void handle_boundaries(trj_t* T)
          T->bactive_s = b;
          if (bd->reflect) {
             T->pos = vsub(T->pos, vscale(2.0 * bd->delta, bd->normal));
-            if (!is_parker(T)) T->mom = vscale(-1.0, T->mom);
+            reverse_momentum(T);
             compute_bnd(T, bd, T->t, T->pos, T->mom, T->sp.bhat, T->sp.region);
             bd->crossings_left--;
          }
@@ -1806,9 +1836,38 @@ static void focused_momentum_correction(trj_t* T)
    else if (T->mom.x[1] < -1.0) T->mom.x[1] = -1.0;
 }
 
+/* TrajectoryGuiding::ModifiedFields and DriftCoeff (src/trajectory_guiding.cc:60-96). The fields are
+ * static, so dB/dt and dBmag/dt are zero; dbhat/dt = (dB/dt - dBmag/dt bhat) / Bmag is formed from
+ * those zeros all the same, so that signed zeros propagate as in the reference. */
+static void guiding_drift(trj_t* T)
+{
+   const spdata* s = &T->sp;
+   double c = c_code();
+   double rL = larmor(T->mom.x[0], s->Bmag), rR = larmor(T->mom.x[2], s->Bmag);
+   v3 dbhatdt = vdiv(vsub(V(0.0, 0.0, 0.0), vscale(0.0, s->bhat)), s->Bmag);
+   v3 curlbhat = vdiv(vsub(sd_curlB(s), vcross(s->gradBmag, s->bhat)), s->Bmag);
+   v3 e_star = vsub(vsub(s->E, vdiv(vscale(rR * s->Bmag, dbhatdt), c)), vdiv(vscale(rL * T->vel.x[0], s->gradBmag), 2.0 * c));
+   v3 b_star = vadd(s->B, vscale(rR * s->Bmag, curlbhat));
+   T->e_star = e_star;
+   T->b_star = b_star;
+   T->drift_vel = vdiv(vadd(vscale(T->vel.x[2], b_star), vscale(c, vcross(e_star, s->bhat))), vdot(b_star, s->bhat));
+}
+
+/* TrajectoryGuiding::Slopes with PPERP_METHOD 1 (src/trajectory_guiding.cc:104-117) */
+static void guiding_slopes(trj_t* T, v3* sp, v3* sm)
+{
+   const spdata* s = &T->sp;
+   guiding_drift(T);
+   *sp = T->drift_vel;
+   sm->x[0] = 0.5 * T->mom.x[0] / s->Bmag * (0.0 + vdot(T->drift_vel, s->gradBmag));
+   sm->x[1] = 0.0;
+   sm->x[2] = p_charge * vdot(T->e_star, T->b_star) / vdot(T->b_star, s->bhat);
+}
+
 static void slopes_rk(trj_t* T, v3* sp, v3* sm)
 {
    if (T->o->traj_type == 200) lorentz_slopes(T, sp, sm);
+   else if (is_guiding(T)) guiding_slopes(T, sp, sm);
    else focused_slopes(T, sp, sm);
 }
 
@@ -1821,6 +1880,10 @@ static void physical_step_rk(trj_t* T)
       T->dt_physical = M_2PI_ / Om / T->o->steps_per_orbit;
       T->dt_physical = fmin(T->dt_physical, 0.1 * T->sp.dmax / vn);
    }
+   else if (is_guiding(T)) {
+      /* src/trajectory_guiding.cc:81-86 */
+      T->dt_physical = 0.5 * T->sp.dmax / (vnorm(T->drift_vel) + 0.5 * vnorm(T->vel));
+   }
    else {
       /* src/trajectory_focused.cc:87-91 */
       T->dt_physical = 0.5 * T->sp.dmax / (vnorm(T->drift_vel) + 0.5 * T->vel.x[0]);
@@ -1831,18 +1894,39 @@ static void physical_step_rk(trj_t* T)
 static void pa_coeffs(trj_t* T)
 {
    dstate st;
+   v3 m = convert_mom(T);
    memset(&st, 0, sizeof st);
-   T->Dmumu = get_component(T, 2, T->t, T->pos, T->mom, &T->sp, &st);
-   T->Vmu = mu_derivative(T, 2, T->t, T->pos, T->mom, &T->sp, &st);
+   T->Dmumu = get_component(T, 2, T->t, T->pos, m, &T->sp, &st);
+   T->Vmu = mu_derivative(T, 2, T->t, T->pos, m, &T->sp, &st);
 }
 
 static void pa_physical_step(trj_t* T)
 {
    const double dthetamax = 2.0 * M_PI_ / 180.0;
-   double amu = fabs(T->mom.x[1]);
+   double amu = is_guiding(T) ? fabs(T->mom.x[2] / vnorm(T->mom)) : fabs(T->mom.x[1]);
    double dmumax = sqrt(1.0 - amu) * dthetamax + 0.5 * amu * (dthetamax * dthetamax);
    T->dt_physical = fmin(T->dt_physical, 0.5 * (dmumax * dmumax) / T->Dmumu);
    T->dt_physical = fmin(T->dt_physical, 0.5 * dmumax / fabs(T->Vmu));
+}
+
+/* TrajectoryGuidingScatt::EulerPitchAngleScatt (src/trajectory_guiding_scatt.cc:61-84). The k-th normal of
+ * a trajectory is the first of the SPX_RNG_STEP block with index k, redraws included (one normal per
+ * block). */
+static void guiding_pa_scatter(trj_t* T)
+{
+   v3 mc = convert_mom(T);
+   double mu_new, n[4];
+   uint32_t b[4];
+   int tries = 0;
+   do {
+      spx_rng_block(T->pb->seed, (uint32_t)T->n_normal++, T->traj_id, T->pb->problem, SPX_RNG_STEP, T->attempt, b);
+      spx_normals4(b, n);
+      mu_new = mc.x[1] + T->Vmu * T->dt + sqrt(2.0 * T->Dmumu * T->dt) * n[0];
+   } while (fabs(mu_new) > 1.0 && ++tries < 256);
+   if (fabs(mu_new) > 1.0) mu_new = (mu_new > 0.0) ? 1.0 : -1.0;
+   T->mom.x[0] = mc.x[0] * sqrt(1.0 - mu_new * mu_new);
+   T->mom.x[2] = mc.x[0] * mu_new;
+   T->vel = vel_cart(T->mom);
 }
 
 static void pa_scatter(trj_t* T, uint32_t step)
@@ -1873,16 +1957,19 @@ static int rk_advance(trj_t* T)
    const rk_t* R = (T->o->rk == 25) ? &RK4 : &RK0;
    v3 slp[4], slm[4];
    int is, il;
-   int scatt = (T->o->traj_type == 205 && T->o->pa_scattering);
+   int scatt = (T->o->traj_type == 205 && T->o->pa_scattering) || T->o->traj_type == 202;
    set_vel_load(T);
    if (scatt) {
+      /* TrajectoryGuidingScatt::Advance (src/trajectory_guiding_scatt.cc:277-310) */
       pa_coeffs(T);
-      focused_drift(T);
+      if (is_guiding(T)) guiding_drift(T);
+      else focused_drift(T);
       physical_step_rk(T);
       pa_physical_step(T);
       T->dt = fmin(T->dt_physical, T->dt_adaptive);
       time_proximity(T);
-      pa_scatter(T, (uint32_t)T->segments);
+      if (is_guiding(T)) guiding_pa_scatter(T);
+      else pa_scatter(T, (uint32_t)T->segments);
       set_vel_load(T);
    }
    T->local_t = T->t; T->local_pos = T->pos; T->local_mom = T->mom; T->local_amp = T->amp; T->local_wgt = T->wgt;
@@ -2072,8 +2159,8 @@ int spx_oracle_run(const uint8_t* spec, size_t spec_len, const spx_oracle_opts* 
       free(pb); free(T);
       return -4;
    }
-   if ((opts->traj_type == 206 || opts->traj_type == 207) && !pb->has_diff) {
-      snprintf(err, err_len, "Parker trajectories need a diffusion model");
+   if ((opts->traj_type == 206 || opts->traj_type == 207 || opts->traj_type == 202) && !pb->has_diff) {
+      snprintf(err, err_len, "Parker and GuidingScatt trajectories need a diffusion model");
       free(pb); free(T);
       return -4;
    }

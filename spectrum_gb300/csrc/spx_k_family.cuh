@@ -13,22 +13,31 @@ struct FamilyTU {
    // dynamic shared memory: the boundary states of every lane of a block
    static size_t smem(int slots, int block) { return (size_t)(slots > 0 ? slots : 1) * block * sizeof(BndState<R>); }
 
+   // the guiding-centre family runs on static backgrounds only (no kernels for the moving shocks)
+   template <int BG>
+   static constexpr bool kBuilt = !(TT == kGuiding && (BG == kBgShock || BG == kBgSmoothShock));
+
    template <int BG>
    static cudaError_t go(const LaunchArgs& a)
    {
-      const auto* P = static_cast<const ProblemDescT<R>*>(a.problems_r);
-      step_kernel<TT, BG, R, DM><<<a.grid, a.block, smem(a.bnd_slots, a.block.x), a.stream>>>(
-          P, a.problems_d, a.cfg, a.ctr, a.counts, a.sums, a.n_events, a.records, a.queue);
-      return cudaGetLastError();
+      if constexpr (kBuilt<BG>) {
+         const auto* P = static_cast<const ProblemDescT<R>*>(a.problems_r);
+         step_kernel<TT, BG, R, DM><<<a.grid, a.block, smem(a.bnd_slots, a.block.x), a.stream>>>(
+             P, a.problems_d, a.cfg, a.ctr, a.counts, a.sums, a.n_events, a.records, a.queue);
+         return cudaGetLastError();
+      }
+      else return cudaErrorInvalidValue;
    }
 
    template <int BG>
    static int occ(int block, int slots)
    {
       int n = 0;
-      if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<TT, BG, R, DM>, block, smem(slots, block)) !=
-          cudaSuccess)
-         n = 0;
+      if constexpr (kBuilt<BG>) {
+         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<TT, BG, R, DM>, block, smem(slots, block)) !=
+             cudaSuccess)
+            n = 0;
+      }
       return n;
    }
 

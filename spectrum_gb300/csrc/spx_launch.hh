@@ -33,6 +33,7 @@ struct LaunchArgs {
 SPX_DECLARE_FAMILY(parker)
 SPX_DECLARE_FAMILY(lorentz)
 SPX_DECLARE_FAMILY(focused)
+SPX_DECLARE_FAMILY(guiding)
 #undef SPX_DECLARE_FAMILY
 
 }  // namespace spx

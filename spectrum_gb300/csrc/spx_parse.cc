@@ -442,6 +442,13 @@ int parse_plugin(ProblemDesc& pd, int traj, int role, int kind, const uint8_t* b
    }
 }
 
+bool background_allowed(int traj, int bg_kind)
+{
+   // the guiding-centre drift needs dB/dt, which the moving shocks have and the device does not evaluate
+   if ((traj == kGuiding || traj == kGuidingScatt) && (bg_kind == kBgShock || bg_kind == kBgSmoothShock)) return false;
+   return true;
+}
+
 int check_ready(const ProblemDesc& pd, int traj)
 {
    // TrajectoryBase::IsSimmulationReady (src/trajectory_base.cc:608-632) and the Parker override
@@ -449,6 +456,9 @@ int check_ready(const ProblemDesc& pd, int traj)
    if (pd.bg.kind == 0 || pd.it.kind == 0 || pd.is.kind == 0 || pd.im.kind == 0 || pd.nbt == 0)
       return SPX_ERR_INCOMPLETE;
    if ((traj == kParker || traj == kParkerSource) && !pd.has_diff) return SPX_ERR_INCOMPLETE;
+   // TrajectoryGuidingScatt::IsSimmulationReady (src/trajectory_guiding_scatt.cc:43-52)
+   if (traj == kGuidingScatt && !pd.has_diff) return SPX_ERR_INCOMPLETE;
+   if (!background_allowed(traj, pd.bg.kind)) return SPX_ERR_UNKNOWN_PLUGIN;
    if (traj == kParkerSource && pd.src.kind == 0) return SPX_ERR_INCOMPLETE;
    for (int k = 0; k < pd.nbt; k++)
       for (int a = 0; a < pd.bt[k].n_actions && a < pd.nd; a++)

@@ -12,6 +12,10 @@ namespace spx {
 // boundary's class) or distribution instead of appending. Returns an SPX_* code.
 int parse_plugin(ProblemDesc& pd, int traj, int role, int kind, const uint8_t* blob, size_t len, int slot);
 
+// Whether trajectory type traj can run on background class bg_kind (the guiding-centre types need
+// static fields).
+bool background_allowed(int traj, int bg_kind);
+
 // The reference's readiness check plus action-index validation. Returns an SPX_* code.
 int check_ready(const ProblemDesc& pd, int traj);
 

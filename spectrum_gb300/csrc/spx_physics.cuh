@@ -447,7 +447,7 @@ __device__ __forceinline__ bool get_fields(const BgParamsT<R>& g, int deriv_mode
       for (int a = 0; a < 3; a++)
 #pragma unroll
          for (int b = 0; b < 3; b++)
-            s.gradB.m[a][b] = R(3) * (M[a] * pp[b] + pp[a] * M[b] + mr * ((a == b ? R(1) : R(0)) - R(5) * pp[a] * pp[b] / r2)) / r5;
+            s.gradB.m[a][b] = R(3) * (M[a] * pp[b] + pp[a] * M[b] + mr * ((a == b ? R(1) : R(0)) - R(5) * (pp[a] * pp[b]) / r2)) / r5;
       s.gradBmag = mv(s.gradB, s.bhat);
       s.dUdt = mk(R(0), R(0), R(0));
    }

@@ -27,8 +27,9 @@ template <class R, class A>
 struct Lane {
    int prob;
    uint32_t traj_id, attempt, steps, status;
+   uint32_t nrm;     // GuidingScatt: normals drawn so far (the k-th is the first of step block k)
    A t;
-   AV3<A> pos, mom;  // mom: Parker (p,-,-), Focused (p, mu, -), Lorentz (px, py, pz)
+   AV3<A> pos, mom;  // mom: Parker (p,-,-), Focused (p, mu, -), Lorentz (px, py, pz), Guiding (p_perp, -, p_para)
    R amp, wgt, dt, dt_adapt, src_del_old;
 };
 
@@ -56,12 +57,13 @@ __device__ __forceinline__ constexpr unsigned traj_mask()
 {
    return TT == kLorentz ? (kE | kB)                                 // src/trajectory_lorentz.cc:36
         : TT == kFocused ? (kAll | kGradB | kGradU | kDUdt)           // src/trajectory_focused.cc:40
+        : TT == kGuiding ? (kAll | kGradB)  // src/trajectory_guiding.cc:51-52; dB/dt is zero for the static backgrounds
                          : (kU | kB | kGradU | kGradB);               // src/trajectory_parker.cc:204
 }
 
 // Momentum magnitude passed to the field evaluators (ConvertMomentum()[0]).
 template <int TT, class R>
-__device__ __forceinline__ R field_p(V3<R> mom) { return TT == kLorentz ? norm(mom) : mom.x; }
+__device__ __forceinline__ R field_p(V3<R> mom) { return (TT == kLorentz || TT == kGuiding) ? norm(mom) : mom.x; }
 
 // ---- random numbers for set-up -----------------------------------------------------------
 struct InitRng {
@@ -155,6 +157,7 @@ static __device__ __noinline__ V3<double> sample_mom(InitRng& rng, const Problem
    case kImFixed: return ld3(q.v0);
    case kImBeam:
       if (traj == kLorentz) return q.a[0] * axis;
+      if (traj == kGuiding) return mk(0.0, 0.0, q.a[0]);
       return mk(q.a[0], 0.0, 0.0);
    case kImRing:
       if (traj == kLorentz) {
@@ -162,6 +165,7 @@ static __device__ __noinline__ V3<double> sample_mom(InitRng& rng, const Problem
          V3<double> e1 = second_unit(axis), e2 = cross(axis, e1);
          return (q.a[0] * q.a[2]) * axis + (q.a[0] * q.a[3]) * (cos(phi) * e1 + sin(phi) * e2);
       }
+      if (traj == kGuiding) return mk(q.a[0] * q.a[3], 0.0, q.a[0] * q.a[2]);
       return mk(q.a[0], q.a[2], 0.0);
    case kImShell:
    case kImThickShell: {
@@ -172,6 +176,7 @@ static __device__ __noinline__ V3<double> sample_mom(InitRng& rng, const Problem
       }
       if (traj == kParker || traj == kParkerSource) return mk(p, 0.0, 0.0);
       if (traj == kFocused) { double mu = -1.0 + 2.0 * rng.uniform(); return mk(p, mu, 0.0); }
+      if (traj == kGuiding) { double mu = -1.0 + 2.0 * rng.uniform(), st = sqrt(1.0 - mu * mu); return mk(p * st, 0.0, p * mu); }
       double mu = -1.0 + 2.0 * rng.uniform(), st = sqrt(1.0 - mu * mu), phi = two_pi * rng.uniform();
       return mk(p * st * cos(phi), p * st * sin(phi), p * mu);
    }
@@ -183,6 +188,7 @@ static __device__ __noinline__ V3<double> sample_mom(InitRng& rng, const Problem
          V3<double> e1 = second_unit(axis), e2 = cross(axis, e1);
          return p_para * axis + p_perp * (cos(phi) * e1 + sin(phi) * e2);
       }
+      if (traj == kGuiding) return mk(p_perp, 0.0, p_para);
       double p = sqrt(p_para * p_para + p_perp * p_perp);
       if (traj == kFocused) return mk(p, p_para / p, 0.0);
       return mk(p, 0.0, 0.0);
@@ -198,6 +204,7 @@ static __device__ __noinline__ V3<double> sample_mom(InitRng& rng, const Problem
          return (p * mu) * axis + (p * st) * (cos(psi) * e1 + sin(psi) * e2);
       }
       if (traj == kFocused) return mk(p, mu, 0.0);
+      if (traj == kGuiding) return mk(p * sqrt(1.0 - mu * mu), 0.0, p * mu);
       return mk(p, 0.0, 0.0);
    }
    }
@@ -237,8 +244,9 @@ static __device__ __noinline__ void process_event(int traj, const EventPoint& e,
    case kDsMomentumUniform: {
       V3<double> m = d.val_time == 0 ? s0.mom0 : e.mom;
       V3<double> bh = d.val_time == 0 ? s0.bhat0 : e.bhat;
-      if (d.val_coord == 0 || traj != kLorentz) value = m;
-      else { double mm = norm(m); value = mk(mm, dot(m, bh) / mm, 0.0); }
+      if (d.val_coord == 0 || (traj != kLorentz && traj != kGuiding)) value = m;
+      else if (traj == kLorentz) { double mm = norm(m); value = mk(mm, dot(m, bh) / mm, 0.0); }
+      else { double mm = norm(m); value = mk(mm, m.z / mm, 0.0); }
       break;
    }
    case kDsPositionMomentumUniform: {
@@ -248,13 +256,13 @@ static __device__ __noinline__ void process_event(int traj, const EventPoint& e,
       break;
    }
    case kDsSpectrumPowerLaw: case kDsSpectrumBentPowerLaw:
-      value.x = enr_kin<double>(traj == kLorentz ? norm(s0.mom0) : s0.mom0.x);
+      value.x = enr_kin<double>((traj == kLorentz || traj == kGuiding) ? norm(s0.mom0) : s0.mom0.x);
       break;
    case kDsCumulative1: case kDsCumulative2: value.x = e.t; break;
    case kDsDivergenceFlow: value = s0.mom0; break;
    case kDsTimeMu:
       value.x = e.t;
-      value.y = traj == kLorentz ? dot(e.mom, e.bhat) / norm(e.mom) : e.mom.y;
+      value.y = traj == kLorentz ? dot(e.mom, e.bhat) / norm(e.mom) : traj == kGuiding ? e.mom.z / norm(e.mom) : e.mom.y;
       break;
    }
    switch (d.kind) {
@@ -263,7 +271,7 @@ static __device__ __noinline__ void process_event(int traj, const EventPoint& e,
       break;
    case kDsSpectrumPowerLaw: case kDsSpectrumBentPowerLaw:
       if (action == 0) {  // DISTRO_KINETIC_ENERGY_POWER_LAW_TYPE 0, src/distribution_other.cc:567-591
-         double m2 = traj == kLorentz ? norm(e.mom) : e.mom.x;
+         double m2 = (traj == kLorentz || traj == kGuiding) ? norm(e.mom) : e.mom.x;
          double ke = enr_kin<double>(m2), v = vel_of<double>(m2);
          w[0] = d.J0 * v * pow(ke / d.T0, d.pow_law) / (m2 * m2);
          if (d.kind == kDsSpectrumBentPowerLaw) w[0] /= pow(1.0 + pow(ke / d.T_b, d.pow_law_comb), d.bend);
@@ -365,9 +373,12 @@ __device__ __forceinline__ void handle_crossings(Lane<R, A>& L, BndView<R> bv, c
          // src/trajectory_base.cc:462-483: mirror the position, reverse the momentum
          V3<R> shift = (R(2) * st.delta) * bnd_normal(b, pos);
          add3(L.pos, R(-1) * shift);
-         if (TT != kParker && TT != kParkerSource) {
-            L.mom.x = neg(L.mom.x); L.mom.y = neg(L.mom.y); L.mom.z = neg(L.mom.z);
-         }
+         // ReverseMomentum: the base negates the vector (src/trajectory_base.cc:139-142), Focused its
+         // mu (src/trajectory_focused.hh:141-144), Guiding its parallel component
+         // (src/trajectory_guiding.hh:123-126), Parker nothing
+         if (TT == kLorentz) { L.mom.x = neg(L.mom.x); L.mom.y = neg(L.mom.y); L.mom.z = neg(L.mom.z); }
+         else if (TT == kFocused) L.mom.y = neg(L.mom.y);
+         else if (TT == kGuiding) L.mom.z = neg(L.mom.z);
          pos = val3<R>(L.pos);
          mom = lane_mom(L);
          compute_bnd(b, st, L.t, pos, mom, sp.bhat, sp.region, TT);
@@ -608,12 +619,39 @@ __device__ __forceinline__ V3<R> focused_drift(const SD<R>& s, V3<R> mom, V3<R> 
    return dv + (s.U + (vel.x * mom.y) * s.bhat);
 }
 
+// TrajectoryGuiding::ModifiedFields and DriftCoeff (src/trajectory_guiding.cc:60-96) and the momentum
+// slopes of Slopes with PPERP_METHOD 1 (:104-117). The backgrounds are static, so dB/dt and dBmag/dt are
+// zero; dbhat/dt = (dB/dt - dBmag/dt bhat) / Bmag is still formed from those zeros so that signed zeros
+// propagate as in the reference.
+template <class R>
+__device__ __forceinline__ V3<R> guiding_drift(const SD<R>& s, V3<R> mom, V3<R> vel, R& dp_perp, R& dp_para)
+{
+   const R c = c_code<R>();
+   const R rL = larmor(mom.x, s.Bmag), rR = larmor(mom.z, s.Bmag);
+   const V3<R> zero3 = mk(R(0), R(0), R(0));
+   V3<R> dbhatdt = (zero3 - R(0) * s.bhat) / s.Bmag;
+   V3<R> curlbhat = (sd_curlB(s) - cross(s.gradBmag, s.bhat)) / s.Bmag;
+   V3<R> e_star = (s.E - ((rR * s.Bmag) * dbhatdt) / c) - ((rL * vel.x) * s.gradBmag) / (R(2) * c);
+   V3<R> b_star = s.B + (rR * s.Bmag) * curlbhat;
+   R bsb = dot(b_star, s.bhat);
+   V3<R> drift = (vel.z * b_star + c * cross(e_star, s.bhat)) / bsb;
+   dp_perp = R(0.5) * mom.x / s.Bmag * (R(0) + dot(drift, s.gradBmag));
+   dp_para = dot(e_star, b_star) / bsb;  // the proton's charge is 1 in code units
+   return drift;
+}
+
 template <int TT, class R>
 __device__ __forceinline__ void rk_slopes(const SD<R>& s, V3<R> mom, V3<R> vel, V3<R>& sp, V3<R>& sm, V3<R>& drift)
 {
    if (TT == kLorentz) {  // src/trajectory_lorentz.cc:67-71
       sp = vel;
       sm = s.E + cross(vel, s.B) / c_code<R>();
+   }
+   else if (TT == kGuiding) {
+      R dpp, dpl;
+      drift = guiding_drift(s, mom, vel, dpp, dpl);
+      sp = drift;
+      sm = mk(dpp, R(0), dpl);
    }
    else {  // src/trajectory_focused.cc:100-128
       drift = focused_drift(s, mom, vel);
@@ -648,7 +686,7 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
    constexpr bool kFP64 = sizeof(R) == sizeof(double);
    const bool fwd = cfg.time_flow == 0;
    const int deriv_mode = kFP64 ? cfg.deriv_mode : 1;
-   const bool scatt = (TT == kFocused) && cfg.pa_scattering;
+   const bool scatt = (TT == kFocused || TT == kGuiding) && cfg.pa_scattering;
    SD<R> sp;
    V3<R> mom = lane_mom(L);
    if (!get_fields<BG>(P.bg, deriv_mode, (R)acc_val(L.t), val3<R>(L.pos), field_p<TT>(mom), traj_mask<TT>(), sp)) {
@@ -659,35 +697,61 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
    V3<R> vel = vel_load<TT>(mom);
    V3<R> drift = mk(R(0), R(0), R(0));
    if (scatt) {
-      // Euler pitch-angle scattering, composed after TrajectoryGuidingScatt::Advance
-      // (src/trajectory_guiding_scatt.cc:61-110, 255-300): coefficients, the mu-CFL, then the step
-      R vmag = vel_of(mom.x);
+      // TrajectoryGuidingScatt::Advance (src/trajectory_guiding_scatt.cc:277-310): coefficients, the
+      // mu-CFL, then the Euler pitch-angle step (:61-84); Focused composes the same step
+      R pmag, mu;
+      if (TT == kGuiding) { pmag = m_sqrt(mom.x * mom.x + mom.z * mom.z); mu = mom.z / norm(mom); }  // ConvertMomentum
+      else { pmag = mom.x; mu = mom.y; }
+      R vmag = vel_of(pmag);
       R Omega = cyclotron(vmag, sp.Bmag);
-      R Dmumu = kappa_mumu(P.df, vmag, Omega, mom.y);
-      R Vmu = kappa_mumu_dmu(P.df, vmag, Omega, mom.y, Dmumu);
-      drift = focused_drift(sp, mom, vel);
-      R dtp = R(0.5) * sp.dmax / (norm(drift) + R(0.5) * vel.x);
+      R Dmumu = kappa_mumu(P.df, vmag, Omega, mu);
+      R Vmu = kappa_mumu_dmu(P.df, vmag, Omega, mu, Dmumu);
+      R dtp;
+      if (TT == kGuiding) {
+         R d1, d2;
+         drift = guiding_drift(sp, mom, vel, d1, d2);
+         dtp = R(0.5) * sp.dmax / (norm(drift) + R(0.5) * norm(vel));
+      }
+      else {
+         drift = focused_drift(sp, mom, vel);
+         dtp = R(0.5) * sp.dmax / (norm(drift) + R(0.5) * vel.x);
+      }
       const R dth = R(2.0 * 3.141592653589793238462643383279502884 / 180.0);
-      R amu = m_abs(mom.y);
+      R amu = m_abs(mu);
       R dmumax = m_sqrt(R(1) - amu) * dth + R(0.5) * amu * (dth * dth);
       dtp = m_min(dtp, R(0.5) * (dmumax * dmumax) / Dmumu);
       dtp = m_min(dtp, R(0.5) * dmumax / m_abs(Vmu));
       L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bv, P.nbt, fwd);
       R n[4];
-      normals4<R>(rng_block(P.seed, L.steps, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
       R sq = m_sqrt(R(2) * Dmumu * L.dt);
-      R mu_new = mom.y + Vmu * L.dt + sq * n[0];
-      int k = 1, blk = 0;
-      while (m_abs(mu_new) > R(1) && blk < 64) {
-         if (k == 4) {
-            normals4<R>(rng_block(P.seed, L.steps * 64u + (uint32_t)blk, L.traj_id, P.problem_id, kRngExtra, L.attempt), n);
-            blk++;
-            k = 0;
+      R mu_new;
+      if (TT == kGuiding) {
+         // the k-th normal of the trajectory, redraws included, is the first of step block k
+         int tries = 0;
+         do {
+            normals4<R>(rng_block(P.seed, L.nrm++, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
+            mu_new = mu + Vmu * L.dt + sq * n[0];
+         } while (m_abs(mu_new) > R(1) && ++tries < 256);
+      }
+      else {
+         normals4<R>(rng_block(P.seed, L.steps, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
+         mu_new = mu + Vmu * L.dt + sq * n[0];
+         int k = 1, blk = 0;
+         while (m_abs(mu_new) > R(1) && blk < 64) {
+            if (k == 4) {
+               normals4<R>(rng_block(P.seed, L.steps * 64u + (uint32_t)blk, L.traj_id, P.problem_id, kRngExtra, L.attempt), n);
+               blk++;
+               k = 0;
+            }
+            mu_new = mu + Vmu * L.dt + sq * n[k++];
          }
-         mu_new = mom.y + Vmu * L.dt + sq * n[k++];
       }
       if (m_abs(mu_new) > R(1)) mu_new = mu_new > R(0) ? R(1) : R(-1);
-      acc_setf(L.mom.y, mu_new);
+      if (TT == kGuiding) {
+         acc_setf(L.mom.x, pmag * m_sqrt(R(1) - mu_new * mu_new));
+         acc_setf(L.mom.z, pmag * mu_new);
+      }
+      else acc_setf(L.mom.y, mu_new);
       mom = lane_mom(L);
       vel = vel_load<TT>(mom);
    }
@@ -703,6 +767,9 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
          R spo = kFP64 ? (R)cfg.steps_per_orbit : (R)cfg.steps_per_orbit_f;
          dtp = R(6.283185307179586476925286766559005768) / Om / spo;
          dtp = m_min(dtp, R(0.1) * sp.dmax / vn);
+      }
+      else if (TT == kGuiding) {  // src/trajectory_guiding.cc:81-86
+         dtp = R(0.5) * sp.dmax / (norm(drift) + R(0.5) * norm(vel));
       }
       else {  // src/trajectory_focused.cc:87-91
          dtp = R(0.5) * sp.dmax / (norm(drift) + R(0.5) * vel.x);
@@ -770,6 +837,7 @@ __device__ __noinline__ void set_start(Lane<R, A>& L, BndView<R> bv, Start& s0, 
    const int deriv_mode = kFP64 ? cfg.deriv_mode : 1;
    L.status = 0;
    L.steps = 0;
+   L.nrm = 0;
    L.amp = R(0);
    L.wgt = R(0);
    L.dt = R(0);
@@ -784,7 +852,7 @@ __device__ __noinline__ void set_start(Lane<R, A>& L, BndView<R> bv, Start& s0, 
    acc_set(L.mom.x, mom.x); acc_set(L.mom.y, mom.y); acc_set(L.mom.z, mom.z);
    SD<R> sp;
    V3<R> pr = val3<R>(L.pos);
-   R pm = TT == kLorentz ? (R)norm(mom) : (R)mom.x;
+   R pm = (TT == kLorentz || TT == kGuiding) ? (R)norm(mom) : (R)mom.x;
    if (!get_fields<BG>(P.bg, deriv_mode, (R)t, pr, pm, traj_mask<TT>(), sp)) { L.status |= TRAJ_DISCARD; return; }
    V3<double> bh = mk((double)sp.bhat.x, (double)sp.bhat.y, (double)sp.bhat.z);
    mom = sample_mom(rng, Pd, TT, bh);
@@ -851,7 +919,7 @@ __device__ __forceinline__ void start_lane(Lane<R, A>& L, BndView<R> bv, Start& 
    n.traj_id = (uint32_t)(cfg.run_index * P[n.prob].n_traj + local);
    n.attempt = attempt;
    set_start<TT, BG>(n, bv, s0, P[n.prob], Pd[n.prob], cfg, local);
-   L.prob = n.prob; L.traj_id = n.traj_id; L.attempt = n.attempt; L.steps = n.steps; L.status = n.status;
+   L.prob = n.prob; L.traj_id = n.traj_id; L.attempt = n.attempt; L.steps = n.steps; L.status = n.status; L.nrm = n.nrm;
    L.t = n.t;
    L.pos.x = n.pos.x; L.pos.y = n.pos.y; L.pos.z = n.pos.z;
    L.mom.x = n.mom.x; L.mom.y = n.mom.y; L.mom.z = n.mom.z;

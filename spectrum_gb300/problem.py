@@ -16,10 +16,13 @@ from .datacontainer import DataContainer
 
 # trajectory types: the reference's configure.ac:236-244 numbering
 TRAJ_LORENTZ = 200
+TRAJ_GUIDING = 201
+TRAJ_GUIDING_SCATT = 202
 TRAJ_FOCUSED = 205
 TRAJ_PARKER = 206
 TRAJ_PARKER_SOURCE = 207
-TRAJ_NAMES = {TRAJ_LORENTZ: "TrajectoryLorentz", TRAJ_FOCUSED: "TrajectoryFocused",
+TRAJ_NAMES = {TRAJ_LORENTZ: "TrajectoryLorentz", TRAJ_GUIDING: "TrajectoryGuiding",
+              TRAJ_GUIDING_SCATT: "TrajectoryGuidingScatt", TRAJ_FOCUSED: "TrajectoryFocused",
               TRAJ_PARKER: "TrajectoryParker", TRAJ_PARKER_SOURCE: "TrajectoryParkerSource"}
 
 FORWARD = 0
@@ -106,7 +109,8 @@ class Problem:
         return [e for e in self.plugins if e.plugin.role == P.ROLE_DISTRIBUTION]
 
     def normals_per_step(self) -> int:
-        """Normal draws per step of the trajectory type (3 for Parker: src/trajectory_parker.cc:159-180)."""
+        """Normal draws per step of the trajectory type (3 for Parker: src/trajectory_parker.cc:159-180;
+        1 for GuidingScatt, whose k-th normal, redraws included, is the first of block k)."""
         if self.traj in (TRAJ_PARKER, TRAJ_PARKER_SOURCE):
             return 3
         return 1

@@ -9,6 +9,7 @@ sources must be present to run this script; the fixtures it writes are then used
 including where the sources are not.
 
     python tests/golden/make_golden.py          # rewrites tests/golden/*.npz
+    python tests/golden/make_golden.py NAME...  # rewrites the named fixtures only
     python tests/golden/make_golden.py --dumps  # rewrites tests/golden/*.distro<d>.out
 
 The second form keeps the reference's own distribution dump files (DistributionTemplated::Dump)
@@ -78,6 +79,62 @@ def _focused_reference_classes(n_traj: int):
     return pb
 
 
+def _guiding_dipole(n_traj: int):
+    """Guiding-centre orbits (TrajectoryGuiding) in the dipole: 10 MeV protons from L = 4 on the
+    equator, 60 s (most of a drift period). The momentum distribution at the time boundary is
+    binned in (|p|, mu) and every mirror point is an event of a time histogram (BoundaryMirror)."""
+    from spectrum_gb300 import units as U
+    from spectrum_gb300.datacontainer import DataContainer as DC
+    from spectrum_gb300.plugins import (BackgroundDipole, BoundaryMirror, BoundarySphereAbsorb, BoundaryTimeExpire,
+                                        DistributionMomentumUniform, DistributionTimeUniform, InitialMomentumShell,
+                                        InitialSpaceFixed, InitialTimeFixed)
+    from spectrum_gb300.problem import FORWARD, TRAJ_GUIDING, Problem, distro_header
+    r_e = workloads.R_EARTH_CM / U.unit_length
+    b_eq = workloads.B_EARTH_G / U.unit_magnetic
+    t_end = 60.0 / U.unit_time
+    p0 = U.mev_to_mom(10.0)
+    pb = Problem(traj=TRAJ_GUIDING, time_flow=FORWARD, rk=25, seed=workloads.SEED_BASE + 7, n_traj=n_traj)
+    c = DC().double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0.0, 0.0, -b_eq)).double(0.1 * r_e)
+    pb.AddBackground(BackgroundDipole(), c.double(r_e).double(0.1))
+    pb.AddInitial(InitialTimeFixed(), DC().double(0.0))
+    pb.AddInitial(InitialSpaceFixed(), DC().vec((4.0 * r_e, 0.0, 0.0)))
+    pb.AddInitial(InitialMomentumShell(), DC().double(p0))
+    pb.AddBoundary(BoundaryTimeExpire(), workloads._boundary(DC(), 1, [0, -1]).double(t_end))
+    pb.AddBoundary(BoundarySphereAbsorb(), workloads._boundary(DC(), 1, [-1, -1]).vec((0, 0, 0)).double(r_e))
+    pb.AddBoundary(BoundaryMirror(), workloads._boundary(DC(), -1, [-1, 0]))
+    c = distro_header(DC(), (16, 20, 0), (0.5 * p0, -1.0, 0.0), (1.5 * p0, 1.0, 1.0))
+    pb.AddDistribution(DistributionMomentumUniform(), c.double(1.0).double(0.0).int(1).int(1))
+    c = distro_header(DC(), (60, 0, 0), (0.0, 0, 0), (t_end, 0, 0))
+    pb.AddDistribution(DistributionTimeUniform(), c.double(1.0).double(0.0).int(1))
+    return pb
+
+
+def _slab_between_mirrors(traj: int, n_traj: int, d0: float = 0.0):
+    """A uniform field along x between two reflecting planes at x = -1 and x = +1 (code units):
+    10 MeV protons from the origin, isotropic, 5 time units (several crossings of the slab). The
+    pitch-angle cosine at the time boundary is binned. With ``d0`` the pitch angle scatters with
+    D_mumu = d0 (1 - mu^2) (DiffusionIsotropicConstant)."""
+    from spectrum_gb300 import units as U
+    from spectrum_gb300.datacontainer import DataContainer as DC
+    from spectrum_gb300.plugins import (BackgroundUniform, BoundaryPlaneReflect, BoundaryTimeExpire,
+                                        DiffusionIsotropicConstant, DistributionMomentumUniform, InitialMomentumShell,
+                                        InitialSpaceFixed, InitialTimeFixed)
+    from spectrum_gb300.problem import FORWARD, Problem, distro_header
+    pb = Problem(traj=traj, time_flow=FORWARD, rk=25, seed=workloads.SEED_BASE + 8, n_traj=n_traj)
+    pb.AddBackground(BackgroundUniform(), DC().double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((1.0, 0.0, 0.0)).double(0.1))
+    pb.AddInitial(InitialTimeFixed(), DC().double(0.0))
+    pb.AddInitial(InitialSpaceFixed(), DC().vec((0.0, 0.0, 0.0)))
+    pb.AddInitial(InitialMomentumShell(), DC().double(U.mev_to_mom(10.0)))
+    if d0 > 0.0:
+        pb.AddDiffusion(DiffusionIsotropicConstant(), DC().double(d0))
+    pb.AddBoundary(BoundaryTimeExpire(), workloads._boundary(DC(), 1, [0]).double(5.0))
+    pb.AddBoundary(BoundaryPlaneReflect(), workloads._boundary(DC(), -1, [-1]).vec((1.0, 0, 0)).vec((1.0, 0, 0)))
+    pb.AddBoundary(BoundaryPlaneReflect(), workloads._boundary(DC(), -1, [-1]).vec((-1.0, 0, 0)).vec((-1.0, 0, 0)))
+    c = distro_header(DC(), (0, 20, 0), (0.0, -1.0, 0.0), (1.0, 1.0, 1.0))
+    pb.AddDistribution(DistributionMomentumUniform(), c.double(1.0).double(0.0).int(1).int(1))
+    return pb
+
+
 def cases():
     """(name, problem) pairs, each small enough for the oracle to finish in seconds."""
     out = []
@@ -88,6 +145,10 @@ def cases():
         out.append((f"parker_bwd_solarwind_{k}", pb))
     out.append(("lorentz_fwd_dipole", _dipole_reference_classes(6)))
     out.append(("focused_fwd_solarwind", _focused_reference_classes(6)))
+    from spectrum_gb300.problem import TRAJ_FOCUSED, TRAJ_GUIDING_SCATT
+    out.append(("focused_fwd_slab_reflect", _slab_between_mirrors(TRAJ_FOCUSED, 8)))
+    out.append(("guiding_fwd_dipole", _guiding_dipole(6)))
+    out.append(("guidingscatt_fwd_slab_reflect", _slab_between_mirrors(TRAJ_GUIDING_SCATT, 8, d0=0.5)))
     return out
 
 
@@ -127,11 +188,14 @@ def write_dumps():
 
 
 def main():
-    if "--dumps" in sys.argv[1:]:
+    args = sys.argv[1:]
+    if "--dumps" in args:
         write_dumps()
         return
     import oracle_tools as ot
     for name, pb in cases():
+        if args and name not in args:
+            continue
         ref = ot.run_reference(pb)
         fx = {"spec": np.frombuffer(pb.to_spec(), dtype=np.uint8), "traj": ref.traj,
               "traj_kind": np.int64(pb.traj), "time_flow": np.int64(pb.time_flow), "rk": np.int64(pb.rk),
