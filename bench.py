@@ -235,13 +235,16 @@ def _other_workloads():
                  "Parker bwd, the Parker spiral sampled on a 256^3 block over +-6 AU (BackgroundServerCartesian, "
                  "first-order interpolation; 537 MB of FP32 node data, above the 126 MB L2), 8 energies 30 MeV-3 GeV "
                  "x 1e5 trajectories, boundaries at 0.3 and 5 AU, 0.2 yr", 0.01),
+        "guiding": (lambda: [W.guiding_dipole(n_traj=1_000_000, t_end_s=60.0)],
+                    "Guiding centre RK4 in the dipole, 1e6 protons 1-100 MeV, L 2-6, pitch 10-170 deg, 60 s of "
+                    "bounce and drift, mirror points recorded", 0.01),
         "focused": (lambda: W.focused_transport(n_problems=64, n_traj=20_000, t_max_hours=0.5),
                     "Focused RK4 + pitch-angle scattering, 64 problems (mean free paths 0.01-1 AU, 1-100 MeV) of "
                     "2e4 trajectories each, 0.5 h of the named 48 h", 0.05),
     }
 
 
-OTHER_WORKLOADS = ("diffusion", "shock", "dipole", "focused", "grid")
+OTHER_WORKLOADS = ("diffusion", "shock", "dipole", "focused", "grid", "guiding")
 
 
 def bench_other(args, rank, world, local):

@@ -22,13 +22,13 @@ import math
 from . import units as U
 from .datacontainer import DataContainer
 from .plugins import (BackgroundDipole, BackgroundSmoothShock, BackgroundSolarWind, BackgroundUniform,
-                      BoundaryMomentumInject, BoundaryPlaneAbsorb, BoundarySphereAbsorb, BoundarySpherePass,
+                      BoundaryMirror, BoundaryMomentumInject, BoundaryPlaneAbsorb, BoundarySphereAbsorb, BoundarySpherePass,
                       BoundaryTimeExpire, DiffusionFullConstant, DiffusionIsotropicConstant,
                       DiffusionRigidityMagneticFieldPowerLaw, DistributionMomentumUniform,
                       DistributionPositionUniform, DistributionSpectrumKineticEnergyPowerLaw,
                       DistributionTimeMu, DistributionTimeUniform, InitialMomentumLogEnergyPitchBand,
                       InitialMomentumShell, InitialSpaceEquatorialBand, InitialSpaceFixed, InitialTimeFixed)
-from .problem import BACKWARD, FORWARD, TRAJ_FOCUSED, TRAJ_LORENTZ, TRAJ_PARKER, Problem, distro_header
+from .problem import BACKWARD, FORWARD, TRAJ_FOCUSED, TRAJ_GUIDING, TRAJ_LORENTZ, TRAJ_PARKER, Problem, distro_header
 
 ONE_AU = U.ASTRONOMICAL_UNIT / U.unit_length
 SEED_BASE = 0x5EED0000
@@ -145,6 +145,37 @@ def dipole_orbits(n_traj: int = 1_000_000, e1_mev: float = 1.0, e2_mev: float = 
     c.double(1.0).double(0.0).int(1).int(1)
     pb.AddDistribution(DistributionMomentumUniform(), c)
     pb.options[SPX_OPT_STEPS_PER_ORBIT] = float(steps_per_orbit)
+    return pb
+
+
+def guiding_dipole(n_traj: int = 1_000_000, e1_mev: float = 1.0, e2_mev: float = 100.0, l1: float = 2.0,
+                   l2: float = 6.0, pitch_deg=(10.0, 170.0), t_end_s: float = 60.0) -> Problem:
+    """Trapped protons as guiding centres (TrajectoryGuiding) in the Earth-like dipole of
+    ``dipole_orbits``: the same energies, L shells and pitch angles, followed for ``t_end_s``
+    seconds of bounce and drift motion. The (|p|, mu) distribution at the time boundary is binned,
+    and every mirror point (BoundaryMirror) is an event of a time histogram."""
+    pb = Problem(traj=TRAJ_GUIDING, time_flow=FORWARD, rk=25, seed=SEED_BASE + 9, n_traj=n_traj)
+    r_e = R_EARTH_CM / U.unit_length
+    b_eq = B_EARTH_G / U.unit_magnetic
+    t_end = t_end_s / U.unit_time
+    c = DataContainer()
+    c.double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0.0, 0.0, -b_eq)).double(0.1 * r_e)
+    c.double(r_e).double(0.1)
+    pb.AddBackground(BackgroundDipole(), c)
+    pb.AddInitial(InitialTimeFixed(), DataContainer().double(0.0))
+    pb.AddInitial(InitialSpaceEquatorialBand(), DataContainer().vec((0, 0, 0)).double(r_e).double(l1).double(l2))
+    mu_lo = math.cos(math.radians(pitch_deg[1]))
+    mu_hi = math.cos(math.radians(pitch_deg[0]))
+    e1, e2 = e1_mev * U.MEV / U.unit_energy, e2_mev * U.MEV / U.unit_energy
+    pb.AddInitial(InitialMomentumLogEnergyPitchBand(), DataContainer().double(e1).double(e2).double(mu_lo).double(mu_hi))
+    pb.AddBoundary(BoundaryTimeExpire(), _boundary(DataContainer(), 1, [0, -1]).double(t_end))
+    pb.AddBoundary(BoundarySphereAbsorb(), _boundary(DataContainer(), 1, [-1, -1]).vec((0, 0, 0)).double(r_e))
+    pb.AddBoundary(BoundaryMirror(), _boundary(DataContainer(), -1, [-1, 0]))
+    c = distro_header(DataContainer(), (64, 32, 0), (0.5 * e1, -1.0, 0.0), (2.0 * e2, 1.0, 1.0), log_bins=(1, 0, 0),
+                      bin_outside=(1, 1, 0))
+    pb.AddDistribution(DistributionMomentumUniform(), c.double(1.0).double(0.0).int(1).int(1))
+    c = distro_header(DataContainer(), (60, 0, 0), (0.0, 0, 0), (t_end, 0, 0))
+    pb.AddDistribution(DistributionTimeUniform(), c.double(1.0).double(0.0).int(1))
     return pb
 
 
