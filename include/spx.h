@@ -49,6 +49,8 @@ extern "C" {
 #define SPX_TRAJ_LORENTZ 200
 #define SPX_TRAJ_GUIDING 201        /* guiding centre, static backgrounds (uniform, dipole, solar wind, grid) */
 #define SPX_TRAJ_GUIDING_SCATT 202  /* guiding centre with Euler pitch-angle scattering; needs a diffusion model */
+#define SPX_TRAJ_GUIDING_DIFF 203   /* guiding centre with Euler perpendicular diffusion; needs a diffusion model */
+#define SPX_TRAJ_GUIDING_DIFF_SCATT 204  /* both stochastic steps; needs a diffusion model */
 #define SPX_TRAJ_FOCUSED 205
 #define SPX_TRAJ_PARKER 206
 #define SPX_TRAJ_PARKER_SOURCE 207

@@ -251,6 +251,8 @@ public:
       case SPX_TRAJ_LORENTZ: return "TrajectoryLorentz";
       case SPX_TRAJ_GUIDING: return "TrajectoryGuiding";
       case SPX_TRAJ_GUIDING_SCATT: return "TrajectoryGuidingScatt";
+      case SPX_TRAJ_GUIDING_DIFF: return "TrajectoryGuidingDiff";
+      case SPX_TRAJ_GUIDING_DIFF_SCATT: return "TrajectoryGuidingDiffScatt";
       case SPX_TRAJ_FOCUSED: return "TrajectoryFocused";
       case SPX_TRAJ_PARKER: return "TrajectoryParker";
       case SPX_TRAJ_PARKER_SOURCE: return "TrajectoryParkerSource";

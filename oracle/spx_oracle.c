@@ -216,6 +216,8 @@ typedef struct {
    double w0, r_ref, ur0;
 } bg_t;
 
+/* the guiding-centre types: Guiding, GuidingScatt, GuidingDiff, GuidingDiffScatt (configure.ac:239-242) */
+#define IS_GC(tt) ((tt) >= 201 && (tt) <= 204)
 enum { DF_ISO = 1, DF_QLT, DF_PARA, DF_PERP, DF_FULL, DF_FLOWMOM, DF_KINRAD, DF_RIGB, DF_STRAUSS, DF_POTGIETER, DF_EMPIRICAL };
 typedef struct {
    int kind;
@@ -672,6 +674,8 @@ typedef struct {
    double Dmumu, Vmu;
    /* Guiding: the modified fields E*, B* of the last drift evaluation */
    v3 e_star, b_star;
+   /* GuidingDiff: field-aligned frame, perpendicular drift and displacement of the step */
+   v3 fa[3], v_perp;
    /* SourceMomentumInjection state (del_mom_old, src/source_other.cc:113-119) */
    double src_del_old;
    /* BackgroundSmoothShock::ds_shock of the last field evaluation; like the reference's background
@@ -1268,7 +1272,7 @@ static void eval_bnd(trj_t* T, bnd_t* b, double t, v3 pos, v3 mom, v3 bhat, v3 r
    }
    case BT_REGION: b->delta = region.x[b->region_ind] - b->region_val; b->normal = V(0, 0, 0); break;
    case BT_MOM_INJ: case BT_MOM_PASS: case BT_MOM_SLAB: case BT_MOM_SHELL:
-      if (tt == 200 || tt == 201 || tt == 202) b->delta = vnorm(mom) - b->momentum;
+      if (tt == 200 || IS_GC(tt)) b->delta = vnorm(mom) - b->momentum;
       else b->delta = mom.x[0] - b->momentum;
       if (b->kind == BT_MOM_SLAB && b->delta * b->delta_old < 0.0) {
          if (vdot(vsub(pos, b->slab_r0), b->slab_n) * vdot(vsub(pos, b->slab_r1), b->slab_n) > 0.0) b->delta_old = b->delta;
@@ -1280,7 +1284,7 @@ static void eval_bnd(trj_t* T, bnd_t* b, double t, v3 pos, v3 mom, v3 bhat, v3 r
       break;
    case BT_MIRROR:
       if (tt == 205) b->delta = mom.x[0] * mom.x[1];
-      else if (tt == 201 || tt == 202) b->delta = mom.x[2];  /* the parallel component */
+      else if (IS_GC(tt)) b->delta = mom.x[2];  /* the parallel component */
       else b->delta = vdot(mom, bhat);
       break;
    }
@@ -1354,7 +1358,7 @@ static void process_trajectory(trj_t* T, int di, int action)
    case DS_MOM: {
       v3 m = (d->val_time == 0) ? T->mom0 : T->mom;
       v3 bh = (d->val_time == 0) ? s1->bhat : s2->bhat;
-      if (d->val_coord == 0 || (tt != 200 && tt != 201 && tt != 202)) value = m;
+      if (d->val_coord == 0 || (tt != 200 && !IS_GC(tt))) value = m;
       else if (tt == 200) { value.x[0] = vnorm(m); value.x[1] = vdot(m, bh) / value.x[0]; value.x[2] = 0.0; }
       else { value.x[0] = vnorm(m); value.x[1] = m.x[2] / value.x[0]; value.x[2] = 0.0; }
       break;
@@ -1365,12 +1369,12 @@ static void process_trajectory(trj_t* T, int di, int action)
       value.x[1] = m.x[d->mom_idx];
       break;
    }
-   case DS_SPEC: case DS_SPECBENT: value.x[0] = enr_kin((tt >= 200 && tt <= 202) ? vnorm(T->mom0) : T->mom0.x[0]); break;
+   case DS_SPEC: case DS_SPECBENT: value.x[0] = enr_kin((tt >= 200 && tt <= 204) ? vnorm(T->mom0) : T->mom0.x[0]); break;
    case DS_CUM1: case DS_CUM2: value.x[0] = T->t; break;
    case DS_DIVFLOW: value = T->mom0; break;
    case DS_TIMEMU:
       value.x[0] = T->t;
-      value.x[1] = (tt == 200) ? vdot(T->mom, s2->bhat) / vnorm(T->mom) : (tt == 201 || tt == 202) ? T->mom.x[2] / vnorm(T->mom) : T->mom.x[1];
+      value.x[1] = (tt == 200) ? vdot(T->mom, s2->bhat) / vnorm(T->mom) : IS_GC(tt) ? T->mom.x[2] / vnorm(T->mom) : T->mom.x[1];
       break;
    }
    /* EvaluateWeight */
@@ -1380,7 +1384,7 @@ static void process_trajectory(trj_t* T, int di, int action)
       break;
    case DS_SPEC: case DS_SPECBENT:
       if (action == 0) {
-         double m2 = (tt >= 200 && tt <= 202) ? vnorm(T->mom) : T->mom.x[0];
+         double m2 = (tt >= 200 && tt <= 204) ? vnorm(T->mom) : T->mom.x[0];
          double ke = enr_kin(m2), v = vel_of(m2);
          w[0] = d->J0 * v * pow(ke / d->T0, d->pow_law) / (m2 * m2);
          if (d->kind == DS_SPECBENT) w[0] /= pow(1.0 + pow(ke / d->T_b, d->pow_law_comb), d->bend);
@@ -1508,7 +1512,7 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
    case IM_FIXED: return q->v0;
    case IM_BEAM:
       if (tt == 200) return vscale(q->a[0], axis);
-      if (tt == 201 || tt == 202) return V(0.0, 0.0, q->a[0]);
+      if (IS_GC(tt)) return V(0.0, 0.0, q->a[0]);
       return V(q->a[0], 0.0, 0.0);
    case IM_RING:
       if (tt == 200) {
@@ -1517,7 +1521,7 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
          v3 m = vscale(q->a[0] * q->a[2], axis);
          return vadd(m, vscale(q->a[0] * q->a[3], vadd(vscale(cos(phi), e1), vscale(sin(phi), e2))));
       }
-      if (tt == 201 || tt == 202) return V(q->a[0] * q->a[3], 0.0, q->a[0] * q->a[2]);
+      if (IS_GC(tt)) return V(q->a[0] * q->a[3], 0.0, q->a[0] * q->a[2]);
       return V(q->a[0], q->a[2], 0.0);
    case IM_SHELL: case IM_THICK: {
       double p = q->a[0];
@@ -1530,7 +1534,7 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
          double mu = -1.0 + 2.0 * next_uniform(T);
          return V(p, mu, 0.0);
       }
-      if (tt == 201 || tt == 202) {
+      if (IS_GC(tt)) {
          double mu = -1.0 + 2.0 * next_uniform(T), st = sqrt(1.0 - mu * mu);
          return V(p * st, 0.0, p * mu);
       }
@@ -1547,7 +1551,7 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
          v3 e1 = second_unit(axis), e2 = vcross(axis, e1);
          return vadd(vscale(p_para, axis), vscale(p_perp, vadd(vscale(cos(phi), e1), vscale(sin(phi), e2))));
       }
-      if (tt == 201 || tt == 202) return V(p_perp, 0.0, p_para);
+      if (IS_GC(tt)) return V(p_perp, 0.0, p_para);
       {
          double p = sqrt(p_para * p_para + p_perp * p_perp);
          if (tt == 205) return V(p, p_para / p, 0.0);
@@ -1565,7 +1569,7 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
          return vadd(vscale(p * mu, axis), vscale(p * st, vadd(vscale(cos(psi), e1), vscale(sin(psi), e2))));
       }
       if (tt == 205) return V(p, mu, 0.0);
-      if (tt == 201 || tt == 202) return V(p * sqrt(1.0 - mu * mu), 0.0, p * mu);
+      if (IS_GC(tt)) return V(p * sqrt(1.0 - mu * mu), 0.0, p * mu);
       return V(p, 0.0, 0.0);
    }
    }
@@ -1576,7 +1580,8 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
 /* trajectory machinery                                                                       */
 /* ------------------------------------------------------------------------------------------ */
 static int is_parker(const trj_t* T) { return T->o->traj_type == 206 || T->o->traj_type == 207; }
-static int is_guiding(const trj_t* T) { return T->o->traj_type == 201 || T->o->traj_type == 202; }
+static int is_guiding(const trj_t* T) { return IS_GC(T->o->traj_type); }
+static int is_guiding_diff(const trj_t* T) { return T->o->traj_type == 203 || T->o->traj_type == 204; }
 static int fwd(const trj_t* T) { return T->o->time_flow == 0; }
 
 /* ConvertMomentum: Parker/Focused native (p, mu, -); Lorentz (|p|, p.b/|p|, 0)
@@ -1598,7 +1603,7 @@ static unsigned traj_mask(const trj_t* T)
    case 200: return BG_E | BG_B;                                  /* src/trajectory_lorentz.cc:36 */
    case 205: return BG_ALL | BG_gradB | BG_gradU | BG_dUdt;       /* src/trajectory_focused.cc:40 */
    /* src/trajectory_guiding.cc:51-52 adds dB/dt, which is zero for every static background */
-   case 201: case 202: return BG_ALL | BG_gradB;
+   case 201: case 202: case 203: case 204: return BG_ALL | BG_gradB;
    default: return BG_U | BG_B | BG_gradU | BG_gradB;             /* src/trajectory_parker.cc:204 */
    }
 }
@@ -1716,7 +1721,7 @@ static void reverse_momentum(trj_t* T)
 {
    switch (T->o->traj_type) {
    case 205: T->mom.x[1] = -T->mom.x[1]; break;
-   case 201: case 202: T->mom.x[2] = -T->mom.x[2]; break;
+   case 201: case 202: case 203: case 204: T->mom.x[2] = -T->mom.x[2]; break;
    case 206: case 207: break;
    default: T->mom = vscale(-1.0, T->mom);
    }
@@ -1864,10 +1869,61 @@ static void guiding_slopes(trj_t* T, v3* sp, v3* sm)
    sm->x[2] = p_charge * vdot(T->e_star, T->b_star) / vdot(T->b_star, s->bhat);
 }
 
+/* TrajectoryGuidingDiff::DiffusionCoeff (src/trajectory_guiding_diff.cc:61-86): the field-aligned frame,
+ * D_perp (component 0) and the perpendicular part of its gradient, V_perp */
+static void guiding_diff_coeff(trj_t* T)
+{
+   dstate st;
+   v3 g, fa[3], m = convert_mom(T);
+   int i;
+   memset(&st, 0, sizeof st);
+   fa[2] = T->sp.bhat;
+   fa[0] = second_unit(T->sp.bhat);
+   fa[1] = vcross(fa[2], fa[0]);
+   for (i = 0; i < 3; i++) T->fa[i] = fa[i];
+   T->Kperp = get_component(T, 0, T->t, T->pos, m, &T->sp, &st);
+   for (i = 0; i < 3; i++) g.x[i] = dir_derivative(T, 0, i, T->t, T->pos, m, &T->sp, &st);
+   T->v_perp = from_basis(V(vdot(g, fa[0]), vdot(g, fa[1]), 0.0), fa);
+}
+
+/* TrajectoryGuidingDiff::EulerPerpDiffSlopes (src/trajectory_guiding_diff.cc:92-107), STOCHASTIC_METHOD_PERP 0:
+ * two normals (the next of the trajectory's count, as for the pitch-angle step) */
+static void guiding_perp_step(trj_t* T)
+{
+   dstate st;
+   v3 m = convert_mom(T);
+   double n[4], n1, n2, dwx, dwy, d;
+   uint32_t b[4];
+   memset(&st, 0, sizeof st);
+   spx_rng_block(T->pb->seed, (uint32_t)T->n_normal++, T->traj_id, T->pb->problem, SPX_RNG_STEP, T->attempt, b);
+   spx_normals4(b, n);
+   n1 = n[0];
+   spx_rng_block(T->pb->seed, (uint32_t)T->n_normal++, T->traj_id, T->pb->problem, SPX_RNG_STEP, T->attempt, b);
+   spx_normals4(b, n);
+   n2 = n[0];
+   dwx = sqrt(T->dt) * n1;
+   dwy = sqrt(T->dt) * n2;
+   d = get_component(T, 0, T->t, T->pos, m, &T->sp, &st);
+   T->Kperp = d;
+   {
+      v3 fa[3];
+      int i;
+      for (i = 0; i < 3; i++) fa[i] = T->fa[i];
+      T->dr_perp = from_basis(V(sqrt(2.0 * d) * dwx, sqrt(2.0 * d) * dwy, 0.0), fa);
+   }
+}
+
 static void slopes_rk(trj_t* T, v3* sp, v3* sm)
 {
    if (T->o->traj_type == 200) lorentz_slopes(T, sp, sm);
-   else if (is_guiding(T)) guiding_slopes(T, sp, sm);
+   else if (is_guiding(T)) {
+      guiding_slopes(T, sp, sm);
+      if (is_guiding_diff(T)) {
+         /* TrajectoryGuidingDiff::Slopes (src/trajectory_guiding_diff.cc:327-336) */
+         guiding_diff_coeff(T);
+         *sp = fwd(T) ? vadd(*sp, T->v_perp) : vsub(*sp, T->v_perp);
+      }
+   }
    else focused_slopes(T, sp, sm);
 }
 
@@ -1879,6 +1935,12 @@ static void physical_step_rk(trj_t* T)
       double Om = fmax(cyclotron(vn, T->sp.Bmag), SP_TINY);
       T->dt_physical = M_2PI_ / Om / T->o->steps_per_orbit;
       T->dt_physical = fmin(T->dt_physical, 0.1 * T->sp.dmax / vn);
+   }
+   else if (is_guiding_diff(T)) {
+      /* TrajectoryGuidingDiff::PhysicalStep (src/trajectory_guiding_diff.cc:343-351) */
+      v3 dv = fwd(T) ? vadd(T->drift_vel, T->v_perp) : vsub(T->drift_vel, T->v_perp);
+      T->dt_physical = 0.5 * T->sp.dmax / (vnorm(dv) + 0.5 * vnorm(T->vel));
+      T->dt_physical = fmin(T->dt_physical, 0.5 * (T->sp.dmax * T->sp.dmax) / T->Kperp);
    }
    else if (is_guiding(T)) {
       /* src/trajectory_guiding.cc:81-86 */
@@ -1957,10 +2019,13 @@ static int rk_advance(trj_t* T)
    const rk_t* R = (T->o->rk == 25) ? &RK4 : &RK0;
    v3 slp[4], slm[4];
    int is, il;
-   int scatt = (T->o->traj_type == 205 && T->o->pa_scattering) || T->o->traj_type == 202;
+   int scatt = (T->o->traj_type == 205 && T->o->pa_scattering) || T->o->traj_type == 202 || T->o->traj_type == 204;
+   int perp = is_guiding_diff(T);
    set_vel_load(T);
    if (scatt) {
-      /* TrajectoryGuidingScatt::Advance (src/trajectory_guiding_scatt.cc:277-310) */
+      /* TrajectoryGuidingScatt::Advance (src/trajectory_guiding_scatt.cc:277-310) and
+       * TrajectoryGuidingDiffScatt::Advance (src/trajectory_guiding_diff_scatt.cc:84-145) */
+      if (perp) guiding_diff_coeff(T);
       pa_coeffs(T);
       if (is_guiding(T)) guiding_drift(T);
       else focused_drift(T);
@@ -1979,6 +2044,7 @@ static int rk_advance(trj_t* T)
       T->dt = fmin(T->dt_physical, T->dt_adaptive);
       time_proximity(T);
    }
+   if (perp) guiding_perp_step(T);
    /* RKSlopes */
    for (is = 1; is < R->stages; is++) {
       for (il = 0; il < is; il++) {
@@ -2014,6 +2080,7 @@ static int rk_advance(trj_t* T)
       }
    }
    T->vel = vel_cart(T->mom);
+   if (perp) T->pos = vadd(T->pos, T->dr_perp);
    handle_boundaries(T);
    if (!(T->status & TRAJ_FINISH)) {
       if (common_fields(T)) return 1;
@@ -2159,8 +2226,9 @@ int spx_oracle_run(const uint8_t* spec, size_t spec_len, const spx_oracle_opts* 
       free(pb); free(T);
       return -4;
    }
-   if ((opts->traj_type == 206 || opts->traj_type == 207 || opts->traj_type == 202) && !pb->has_diff) {
-      snprintf(err, err_len, "Parker and GuidingScatt trajectories need a diffusion model");
+   if ((opts->traj_type == 206 || opts->traj_type == 207 || (opts->traj_type >= 202 && opts->traj_type <= 204)) &&
+       !pb->has_diff) {
+      snprintf(err, err_len, "Parker, GuidingScatt, GuidingDiff and GuidingDiffScatt trajectories need a diffusion model");
       free(pb); free(T);
       return -4;
    }

@@ -224,6 +224,8 @@ cudaError_t launch(spx_ctx* c, const spx::LaunchArgs& a)
       return fd ? spx::launch_focused_f64fd(bg, a) : f64 ? spx::launch_focused_f64(bg, a) : spx::launch_focused_f32(bg, a);
    case SPX_TRAJ_GUIDING:
    case SPX_TRAJ_GUIDING_SCATT:
+   case SPX_TRAJ_GUIDING_DIFF:
+   case SPX_TRAJ_GUIDING_DIFF_SCATT:
       return fd ? spx::launch_guiding_f64fd(bg, a) : f64 ? spx::launch_guiding_f64(bg, a) : spx::launch_guiding_f32(bg, a);
    default: return cudaErrorInvalidValue;
    }
@@ -246,6 +248,8 @@ int occupancy(spx_ctx* c, int block, int slots)
                 : f64 ? spx::occupancy_focused_f64(bg, block, slots) : spx::occupancy_focused_f32(bg, block, slots);
    case SPX_TRAJ_GUIDING:
    case SPX_TRAJ_GUIDING_SCATT:
+   case SPX_TRAJ_GUIDING_DIFF:
+   case SPX_TRAJ_GUIDING_DIFF_SCATT:
       return fd ? spx::occupancy_guiding_f64fd(bg, block, slots)
                 : f64 ? spx::occupancy_guiding_f64(bg, block, slots) : spx::occupancy_guiding_f32(bg, block, slots);
    default: return 0;
@@ -404,7 +408,7 @@ int spx_create(spx_ctx_t* out, int traj_kind, int time_flow, int rk_method, int 
    if (!out) return SPX_ERR_INVALID_ARG;
    *out = nullptr;
    if (traj_kind != SPX_TRAJ_PARKER && traj_kind != SPX_TRAJ_PARKER_SOURCE && traj_kind != SPX_TRAJ_LORENTZ &&
-       traj_kind != SPX_TRAJ_FOCUSED && traj_kind != SPX_TRAJ_GUIDING && traj_kind != SPX_TRAJ_GUIDING_SCATT)
+       traj_kind != SPX_TRAJ_FOCUSED && (traj_kind < SPX_TRAJ_GUIDING || traj_kind > SPX_TRAJ_GUIDING_DIFF_SCATT))
       return SPX_ERR_INVALID_ARG;
    if (time_flow != SPX_FORWARD && time_flow != SPX_BACKWARD) return SPX_ERR_INVALID_ARG;
    if (precision != SPX_FP64 && precision != SPX_MIXED) return SPX_ERR_INVALID_ARG;
@@ -429,7 +433,7 @@ int spx_create(spx_ctx_t* out, int traj_kind, int time_flow, int rk_method, int 
    c->precision = precision;
    if (precision == SPX_MIXED) c->deriv_mode = 1;
    // TrajectoryGuidingScatt is the guiding-centre stepper with its pitch-angle step always on
-   if (traj_kind == SPX_TRAJ_GUIDING_SCATT) c->pa_scattering = 1;
+   if (traj_kind == SPX_TRAJ_GUIDING_SCATT || traj_kind == SPX_TRAJ_GUIDING_DIFF_SCATT) c->pa_scattering = 1;
    if (cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) return SPX_ERR_CUDA;
    if (cudaEventCreate(&c->ev0) != cudaSuccess || cudaEventCreate(&c->ev1) != cudaSuccess) return SPX_ERR_CUDA;
    *out = c.release();
@@ -452,7 +456,8 @@ int spx_set_option(spx_ctx_t c, int option, double value)
       return SPX_OK;
    case SPX_OPT_PA_SCATTERING:
       // an option of the focused stepper only; GuidingScatt scatters by its type
-      if (c->traj == SPX_TRAJ_GUIDING_SCATT) return value != 0.0 ? SPX_OK : SPX_ERR_INVALID_ARG;
+      if (c->traj == SPX_TRAJ_GUIDING_SCATT || c->traj == SPX_TRAJ_GUIDING_DIFF_SCATT)
+         return value != 0.0 ? SPX_OK : SPX_ERR_INVALID_ARG;
       if (c->traj != SPX_TRAJ_FOCUSED && value != 0.0) return SPX_ERR_INVALID_ARG;
       c->pa_scattering = value != 0.0;
       return SPX_OK;

@@ -17,9 +17,14 @@ namespace spx {
 constexpr int kMaxBnd = 4;     // boundaries per class (time, space, momentum)
 constexpr int kMaxDistro = 4;  // distributions per problem
 
-// kGuiding covers TrajectoryGuiding (201) and, with RunConfig::pa_scattering, TrajectoryGuidingScatt
-// (202): one kernel family, as the reference derives the second from the first.
-enum TrajKind : int { kLorentz = 200, kGuiding = 201, kGuidingScatt = 202, kFocused = 205, kParker = 206, kParkerSource = 207 };
+// kGuiding is the kernel family of all four guiding-centre types: TrajectoryGuiding (201), with
+// RunConfig::pa_scattering TrajectoryGuidingScatt (202), and with RunConfig::traj_kind 203/204 the
+// perpendicular-diffusion types TrajectoryGuidingDiff and TrajectoryGuidingDiffScatt, as the reference
+// derives the last three from the first.
+enum TrajKind : int {
+   kLorentz = 200, kGuiding = 201, kGuidingScatt = 202, kGuidingDiff = 203, kGuidingDiffScatt = 204, kFocused = 205,
+   kParker = 206, kParkerSource = 207
+};
 
 enum BgKind : int { kBgUniform = 1, kBgShock = 2, kBgSmoothShock = 3, kBgDipole = 4, kBgSolarWind = 5, kBgGrid = 6 };
 

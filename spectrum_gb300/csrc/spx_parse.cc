@@ -445,7 +445,7 @@ int parse_plugin(ProblemDesc& pd, int traj, int role, int kind, const uint8_t* b
 bool background_allowed(int traj, int bg_kind)
 {
    // the guiding-centre drift needs dB/dt, which the moving shocks have and the device does not evaluate
-   if ((traj == kGuiding || traj == kGuidingScatt) && (bg_kind == kBgShock || bg_kind == kBgSmoothShock)) return false;
+   if (traj >= kGuiding && traj <= kGuidingDiffScatt && (bg_kind == kBgShock || bg_kind == kBgSmoothShock)) return false;
    return true;
 }
 
@@ -456,8 +456,9 @@ int check_ready(const ProblemDesc& pd, int traj)
    if (pd.bg.kind == 0 || pd.it.kind == 0 || pd.is.kind == 0 || pd.im.kind == 0 || pd.nbt == 0)
       return SPX_ERR_INCOMPLETE;
    if ((traj == kParker || traj == kParkerSource) && !pd.has_diff) return SPX_ERR_INCOMPLETE;
-   // TrajectoryGuidingScatt::IsSimmulationReady (src/trajectory_guiding_scatt.cc:43-52)
-   if (traj == kGuidingScatt && !pd.has_diff) return SPX_ERR_INCOMPLETE;
+   // TrajectoryGuidingScatt / GuidingDiff::IsSimmulationReady (src/trajectory_guiding_scatt.cc:43-52,
+   // src/trajectory_guiding_diff.cc:43-52)
+   if ((traj == kGuidingScatt || traj == kGuidingDiff || traj == kGuidingDiffScatt) && !pd.has_diff) return SPX_ERR_INCOMPLETE;
    if (!background_allowed(traj, pd.bg.kind)) return SPX_ERR_UNKNOWN_PLUGIN;
    if (traj == kParkerSource && pd.src.kind == 0) return SPX_ERR_INCOMPLETE;
    for (int k = 0; k < pd.nbt; k++)

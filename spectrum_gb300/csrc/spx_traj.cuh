@@ -640,6 +640,24 @@ __device__ __forceinline__ V3<R> guiding_drift(const SD<R>& s, V3<R> mom, V3<R> 
    return drift;
 }
 
+// TrajectoryGuidingDiff::DiffusionCoeff (src/trajectory_guiding_diff.cc:61-86): the field-aligned frame,
+// D_perp (diffusion component 0) and the perpendicular part of its gradient, V_perp.
+template <class R>
+__device__ __forceinline__ V3<R> guiding_vperp(const DiffParamsT<R>& df, const SD<R>& s, V3<R> pos, V3<R> mom, R& d_perp,
+                                               V3<R> (&fa)[3])
+{
+   const R p = m_sqrt(mom.x * mom.x + mom.z * mom.z);  // ConvertMomentum()[0]
+   const R vmag = vel_of(p);
+   Kap<R> K = kappa_pp(df, pos, p, vmag, kap_in(s));
+   V3<R> gpe, gpa;
+   kappa_grad(df, pos, p, vmag, s, K, gpe, gpa);
+   fa[2] = s.bhat;
+   fa[0] = second_unit(s.bhat);
+   fa[1] = cross(fa[2], fa[0]);
+   d_perp = K.perp;
+   return from_basis(mk(dot(gpe, fa[0]), dot(gpe, fa[1]), R(0)), fa);
+}
+
 template <int TT, class R>
 __device__ __forceinline__ void rk_slopes(const SD<R>& s, V3<R> mom, V3<R> vel, V3<R>& sp, V3<R>& sm, V3<R>& drift)
 {
@@ -687,12 +705,18 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
    const bool fwd = cfg.time_flow == 0;
    const int deriv_mode = kFP64 ? cfg.deriv_mode : 1;
    const bool scatt = (TT == kFocused || TT == kGuiding) && cfg.pa_scattering;
+   // TrajectoryGuidingDiff / GuidingDiffScatt: perpendicular diffusion on top of the guiding-centre step
+   const bool gc_perp = TT == kGuiding && (cfg.traj_kind == kGuidingDiff || cfg.traj_kind == kGuidingDiffScatt);
    SD<R> sp;
    V3<R> mom = lane_mom(L);
    if (!get_fields<BG>(P.bg, deriv_mode, (R)acc_val(L.t), val3<R>(L.pos), field_p<TT>(mom), traj_mask<TT>(), sp)) {
       L.status |= TRAJ_DISCARD;
       return;
    }
+   // the guiding-centre mask has no grad U, which the diffusion models then see as zero, as in the reference
+   if (gc_perp) zero(sp.gradU);
+   R d_perp = R(0);
+   V3<R> fa[3];
    if (!prev_step_ok(L, sp.dmax)) return;
    V3<R> vel = vel_load<TT>(mom);
    V3<R> drift = mk(R(0), R(0), R(0));
@@ -710,7 +734,15 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
       if (TT == kGuiding) {
          R d1, d2;
          drift = guiding_drift(sp, mom, vel, d1, d2);
-         dtp = R(0.5) * sp.dmax / (norm(drift) + R(0.5) * norm(vel));
+         if (gc_perp) {
+            // TrajectoryGuidingDiffScatt::Advance: DiffusionCoeff, DriftCoeff, then GuidingDiff::PhysicalStep
+            // (src/trajectory_guiding_diff.cc:343-351) before the pitch-angle limits
+            V3<R> vp = guiding_vperp(P.df, sp, val3<R>(L.pos), mom, d_perp, fa);
+            V3<R> dv = fwd ? drift + vp : drift - vp;
+            dtp = R(0.5) * sp.dmax / (norm(dv) + R(0.5) * norm(vel));
+            dtp = m_min(dtp, R(0.5) * (sp.dmax * sp.dmax) / d_perp);
+         }
+         else dtp = R(0.5) * sp.dmax / (norm(drift) + R(0.5) * norm(vel));
       }
       else {
          drift = focused_drift(sp, mom, vel);
@@ -759,6 +791,11 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
    const AV3<A> pos_loc = L.pos, mom_loc = L.mom;
    V3<R> slp[STAGES], slm[STAGES];
    rk_slopes<TT>(sp, mom, vel, slp[0], slm[0], drift);
+   V3<R> vperp = mk(R(0), R(0), R(0));
+   if (gc_perp) {  // TrajectoryGuidingDiff::Slopes (src/trajectory_guiding_diff.cc:327-336)
+      vperp = guiding_vperp(P.df, sp, val3<R>(L.pos), mom, d_perp, fa);
+      slp[0] = fwd ? slp[0] + vperp : slp[0] - vperp;
+   }
    if (!scatt) {
       R dtp;
       if (TT == kLorentz) {  // src/trajectory_lorentz.cc:51-59
@@ -768,6 +805,11 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
          dtp = R(6.283185307179586476925286766559005768) / Om / spo;
          dtp = m_min(dtp, R(0.1) * sp.dmax / vn);
       }
+      else if (TT == kGuiding && gc_perp) {  // src/trajectory_guiding_diff.cc:343-351
+         V3<R> dv = fwd ? drift + vperp : drift - vperp;
+         dtp = R(0.5) * sp.dmax / (norm(dv) + R(0.5) * norm(vel));
+         dtp = m_min(dtp, R(0.5) * (sp.dmax * sp.dmax) / d_perp);
+      }
       else if (TT == kGuiding) {  // src/trajectory_guiding.cc:81-86
          dtp = R(0.5) * sp.dmax / (norm(drift) + R(0.5) * norm(vel));
       }
@@ -775,6 +817,17 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
          dtp = R(0.5) * sp.dmax / (norm(drift) + R(0.5) * vel.x);
       }
       L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bv, P.nbt, fwd);
+   }
+   V3<R> dr_perp = mk(R(0), R(0), R(0));
+   if (gc_perp) {
+      // EulerPerpDiffSlopes (src/trajectory_guiding_diff.cc:92-107): the next two normals of the trajectory
+      R n[4];
+      normals4<R>(rng_block(P.seed, L.nrm++, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
+      const R dwx = m_sqrt(L.dt) * n[0];
+      normals4<R>(rng_block(P.seed, L.nrm++, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
+      const R dwy = m_sqrt(L.dt) * n[0];
+      const R sq = m_sqrt(R(2) * d_perp);
+      dr_perp = from_basis(mk(sq * dwx, sq * dwy, R(0)), fa);
    }
    // RKSlopes
 #pragma unroll
@@ -796,6 +849,13 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
       V3<R> vs = vel_cart(ms);  // src/trajectory_base.cc:344 uses the Cartesian velocity for every type
       V3<R> dummy;
       rk_slopes<TT>(sp, ms, vs, slp[is], slm[is], dummy);
+      if (gc_perp) {
+         zero(sp.gradU);
+         R dstage;
+         V3<R> fstage[3];
+         V3<R> vp = guiding_vperp(P.df, sp, val3<R>(L.pos), ms, dstage, fstage);
+         slp[is] = fwd ? slp[is] + vp : slp[is] - vp;
+      }
       L.t = t_loc;
       L.pos = pos_loc;
       L.mom = mom_loc;
@@ -821,6 +881,10 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
       R sdt = fwd ? L.dt : -L.dt;
       add3(L.pos, sdt * dp);
       add3(L.mom, sdt * dm);
+   }
+   if (gc_perp) {  // Advance: _pos += dr_perp after RKStep (src/trajectory_guiding_diff.cc:373)
+      if constexpr (kFP64) { acc_add(L.pos.x, dr_perp.x); acc_add(L.pos.y, dr_perp.y); acc_add(L.pos.z, dr_perp.z); }
+      else add3(L.pos, dr_perp);
    }
    handle_boundaries<TT>(L, bv, sp, s0, P, Pd, S);
    if (!(L.status & TRAJ_FINISH) && TT == kFocused) clamp_mu<A, R>(L.mom);

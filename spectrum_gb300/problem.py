@@ -18,11 +18,14 @@ from .datacontainer import DataContainer
 TRAJ_LORENTZ = 200
 TRAJ_GUIDING = 201
 TRAJ_GUIDING_SCATT = 202
+TRAJ_GUIDING_DIFF = 203
+TRAJ_GUIDING_DIFF_SCATT = 204
 TRAJ_FOCUSED = 205
 TRAJ_PARKER = 206
 TRAJ_PARKER_SOURCE = 207
 TRAJ_NAMES = {TRAJ_LORENTZ: "TrajectoryLorentz", TRAJ_GUIDING: "TrajectoryGuiding",
-              TRAJ_GUIDING_SCATT: "TrajectoryGuidingScatt", TRAJ_FOCUSED: "TrajectoryFocused",
+              TRAJ_GUIDING_SCATT: "TrajectoryGuidingScatt", TRAJ_GUIDING_DIFF: "TrajectoryGuidingDiff",
+              TRAJ_GUIDING_DIFF_SCATT: "TrajectoryGuidingDiffScatt", TRAJ_FOCUSED: "TrajectoryFocused",
               TRAJ_PARKER: "TrajectoryParker", TRAJ_PARKER_SOURCE: "TrajectoryParkerSource"}
 
 FORWARD = 0

@@ -135,6 +135,44 @@ def _slab_between_mirrors(traj: int, n_traj: int, d0: float = 0.0):
     return pb
 
 
+def _guiding_perp(traj: int, n_traj: int, dipole: bool):
+    """Guiding centres with perpendicular diffusion (TrajectoryGuidingDiff, or GuidingDiffScatt).
+    In a uniform field along x with constant D_perp = 0.05 the positions spread across the field
+    (binned in y); in the dipole a rigidity and |B| power law (kappa_perp = 0.01 kappa_par ~ 1/B)
+    adds the perpendicular drift of its gradient."""
+    from spectrum_gb300 import units as U
+    from spectrum_gb300.datacontainer import DataContainer as DC
+    from spectrum_gb300.plugins import (BackgroundDipole, BackgroundUniform, BoundarySphereAbsorb, BoundaryTimeExpire,
+                                        DiffusionPerpConstant, DiffusionRigidityMagneticFieldPowerLaw,
+                                        DistributionPositionUniform, InitialMomentumShell, InitialSpaceFixed,
+                                        InitialTimeFixed)
+    from spectrum_gb300.problem import FORWARD, Problem, distro_header
+    p0 = U.mev_to_mom(10.0)
+    pb = Problem(traj=traj, time_flow=FORWARD, rk=25, seed=workloads.SEED_BASE + 10, n_traj=n_traj)
+    pb.AddInitial(InitialTimeFixed(), DC().double(0.0))
+    pb.AddInitial(InitialMomentumShell(), DC().double(p0))
+    if dipole:
+        r_e = workloads.R_EARTH_CM / U.unit_length
+        b_eq = workloads.B_EARTH_G / U.unit_magnetic
+        c = DC().double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0.0, 0.0, -b_eq)).double(0.1 * r_e)
+        pb.AddBackground(BackgroundDipole(), c.double(r_e).double(0.1))
+        pb.AddInitial(InitialSpaceFixed(), DC().vec((4.0 * r_e, 0.0, 0.0)))
+        pb.AddDiffusion(DiffusionRigidityMagneticFieldPowerLaw(),
+                        DC().double(0.2).double(U.Rigidity(p0)).double(b_eq / 64.0).double(0.5).double(-1.0).double(0.01))
+        t_end = 30.0 / U.unit_time
+        pb.AddBoundary(BoundaryTimeExpire(), workloads._boundary(DC(), 1, [0]).double(t_end))
+        pb.AddBoundary(BoundarySphereAbsorb(), workloads._boundary(DC(), 1, [-1]).vec((0, 0, 0)).double(r_e))
+        c = distro_header(DC(), (0, 0, 20), (0, 0, -2.0 * r_e), (1, 1, 2.0 * r_e))
+    else:
+        pb.AddBackground(BackgroundUniform(), DC().double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((1.0, 0.0, 0.0)).double(0.1))
+        pb.AddInitial(InitialSpaceFixed(), DC().vec((0.0, 0.0, 0.0)))
+        pb.AddDiffusion(DiffusionPerpConstant(), DC().double(0.05))
+        pb.AddBoundary(BoundaryTimeExpire(), workloads._boundary(DC(), 1, [0]).double(2.0))
+        c = distro_header(DC(), (0, 20, 0), (0, -1.0, 0), (1, 1.0, 1))
+    pb.AddDistribution(DistributionPositionUniform(), c.double(1.0).double(0.0).int(1).int(0))
+    return pb
+
+
 def cases():
     """(name, problem) pairs, each small enough for the oracle to finish in seconds."""
     out = []
@@ -149,6 +187,10 @@ def cases():
     out.append(("focused_fwd_slab_reflect", _slab_between_mirrors(TRAJ_FOCUSED, 8)))
     out.append(("guiding_fwd_dipole", _guiding_dipole(6)))
     out.append(("guidingscatt_fwd_slab_reflect", _slab_between_mirrors(TRAJ_GUIDING_SCATT, 8, d0=0.5)))
+    from spectrum_gb300.problem import TRAJ_GUIDING_DIFF, TRAJ_GUIDING_DIFF_SCATT
+    out.append(("guidingdiff_fwd_uniform", _guiding_perp(TRAJ_GUIDING_DIFF, 8, dipole=False)))
+    out.append(("guidingdiff_fwd_dipole", _guiding_perp(TRAJ_GUIDING_DIFF, 6, dipole=True)))
+    out.append(("guidingdiffscatt_fwd_uniform", _guiding_perp(TRAJ_GUIDING_DIFF_SCATT, 8, dipole=False)))
     return out
 
 

@@ -176,7 +176,8 @@ def oracle_uniforms(seed, index, traj, problem=0, attempt=0):
 # -- the reference itself (only where oracle/_ref was built from the reference sources) --------
 REF_VARIANTS = {(206, 0, 0): "parker_fwd_rk0", (206, 1, 0): "parker_bwd_rk0", (207, 1, 0): "parkersrc_bwd_rk0",
                 (200, 0, 25): "lorentz_fwd_rk25", (205, 0, 25): "focused_fwd_rk25",
-                (201, 0, 25): "guiding_fwd_rk25", (202, 0, 25): "guidingscatt_fwd_rk25"}
+                (201, 0, 25): "guiding_fwd_rk25", (202, 0, 25): "guidingscatt_fwd_rk25",
+                (203, 0, 25): "guidingdiff_fwd_rk25", (204, 0, 25): "guidingdiffscatt_fwd_rk25"}
 
 
 def ref_binary(problem) -> str | None:

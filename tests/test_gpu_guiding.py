@@ -4,7 +4,8 @@ and the reflection of focused trajectories (ReverseMomentum negates mu only).
 - FP64 kernels against the oracle trajectory by trajectory, on the problems of the golden fixtures
   (whose oracle runs are pinned bit-exact to the reference's own code) with more trajectories.
 - FP32 against FP64.
-- Known answers: an equatorial proton in a dipole drifts at the gradient-drift rate
+- Known answers: constant perpendicular diffusion across a uniform field spreads the guiding
+  centres as <y^2 + z^2> = 4 D_perp t; an equatorial proton in a dipole drifts at the gradient-drift rate
   omega = 1.5 r_L v / r^2 and keeps its radius; in the dipole the magnetic moment p_perp^2 / B
   and |p| are conserved along the orbit (PPERP_METHOD 1 integrates dp_perp/dt = p_perp/(2B) dB/dt);
   pure pitch-angle scattering relaxes <mu> as mu0 exp(-2 D0 t).
@@ -27,7 +28,8 @@ pytestmark = pytest.mark.gpu
 sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
 import make_golden  # noqa: E402
 
-from spectrum_gb300.problem import TRAJ_FOCUSED, TRAJ_GUIDING, TRAJ_GUIDING_SCATT  # noqa: E402
+from spectrum_gb300.problem import (TRAJ_FOCUSED, TRAJ_GUIDING, TRAJ_GUIDING_DIFF, TRAJ_GUIDING_DIFF_SCATT,  # noqa: E402
+                                    TRAJ_GUIDING_SCATT)
 
 
 def _agree(rec, ref, tol):
@@ -42,6 +44,9 @@ def _agree(rec, ref, tol):
     ("guiding_dipole", lambda: make_golden._guiding_dipole(128)),
     ("guidingscatt_slab", lambda: make_golden._slab_between_mirrors(TRAJ_GUIDING_SCATT, 256, d0=0.5)),
     ("focused_slab_reflect", lambda: make_golden._slab_between_mirrors(TRAJ_FOCUSED, 256)),
+    ("guidingdiff_uniform", lambda: make_golden._guiding_perp(TRAJ_GUIDING_DIFF, 256, dipole=False)),
+    ("guidingdiff_dipole", lambda: make_golden._guiding_perp(TRAJ_GUIDING_DIFF, 64, dipole=True)),
+    ("guidingdiffscatt_uniform", lambda: make_golden._guiding_perp(TRAJ_GUIDING_DIFF_SCATT, 256, dipole=False)),
 ])
 def test_fp64_matches_oracle(built_lib, name, problem):
     pb = problem()
@@ -178,3 +183,15 @@ def test_guiding_scatt_needs_diffusion(built_lib):
         assert e.value.code == -4
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("precision", [capi.SPX_FP64, capi.SPX_MIXED])
+def test_perpendicular_spread(built_lib, precision):
+    pb = make_golden._guiding_perp(TRAJ_GUIDING_DIFF, 20_000, dipole=False)  # D_perp = 0.05, B along x, t = 2
+    rec = run_problems(pb, precision=precision, record=True).records[0]
+    r2 = rec["pos"][:, 1] ** 2 + rec["pos"][:, 2] ** 2
+    expect = 4.0 * 0.05 * rec["t"].mean()
+    sigma = r2.std() / math.sqrt(len(r2))
+    assert abs(r2.mean() - expect) < 4.0 * sigma, (r2.mean(), expect, sigma)
+    np.testing.assert_allclose(np.linalg.norm(rec["mom"], axis=1), np.linalg.norm(rec["mom0"], axis=1), rtol=1e-4)
+

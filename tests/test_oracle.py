@@ -87,7 +87,7 @@ def test_oracle_smoothshock_deviation_d1():
 
 def test_golden_fixtures_cover_every_trajectory_family():
     kinds = {int(ot.load_golden(n)[0]["traj_kind"]) for n in ot.golden_names()}
-    assert {200, 201, 202, 205, 206} <= kinds
+    assert {200, 201, 202, 203, 204, 205, 206} <= kinds
 
 
 needs_ref = pytest.mark.skipif(not os.path.exists(os.path.join(ot.REF_DIR, "ref_parker_bwd_rk0")),
