@@ -138,8 +138,9 @@ def _slab_between_mirrors(traj: int, n_traj: int, d0: float = 0.0):
 def _guiding_perp(traj: int, n_traj: int, dipole: bool):
     """Guiding centres with perpendicular diffusion (TrajectoryGuidingDiff, or GuidingDiffScatt).
     In a uniform field along x with constant D_perp = 0.05 the positions spread across the field
-    (binned in y); in the dipole a rigidity and |B| power law (kappa_perp = 0.01 kappa_par ~ 1/B)
-    adds the perpendicular drift of its gradient."""
+    (binned in y); in the dipole a rigidity and |B| power law (kappa_perp = 0.01 kappa_par ~ B)
+    adds the perpendicular drift of its gradient. (With kappa ~ 1/B ~ r^3 the guiding centres would
+    run away outward within seconds.)"""
     from spectrum_gb300 import units as U
     from spectrum_gb300.datacontainer import DataContainer as DC
     from spectrum_gb300.plugins import (BackgroundDipole, BackgroundUniform, BoundarySphereAbsorb, BoundaryTimeExpire,
@@ -158,7 +159,7 @@ def _guiding_perp(traj: int, n_traj: int, dipole: bool):
         pb.AddBackground(BackgroundDipole(), c.double(r_e).double(0.1))
         pb.AddInitial(InitialSpaceFixed(), DC().vec((4.0 * r_e, 0.0, 0.0)))
         pb.AddDiffusion(DiffusionRigidityMagneticFieldPowerLaw(),
-                        DC().double(0.2).double(U.Rigidity(p0)).double(b_eq / 64.0).double(0.5).double(-1.0).double(0.01))
+                        DC().double(0.2).double(U.Rigidity(p0)).double(b_eq / 64.0).double(0.5).double(1.0).double(0.01))
         t_end = 30.0 / U.unit_time
         pb.AddBoundary(BoundaryTimeExpire(), workloads._boundary(DC(), 1, [0]).double(t_end))
         pb.AddBoundary(BoundarySphereAbsorb(), workloads._boundary(DC(), 1, [-1]).vec((0, 0, 0)).double(r_e))
