@@ -75,6 +75,7 @@ extern "C" {
 #define SPX_OPT_MAX_ATTEMPTS 5      /* retries of a discarded trajectory, default 100 */
 #define SPX_OPT_RUN_INDEX 6         /* index of the next run: problem p's trajectory ids start at index * n_traj(p);
                                        each run advances it by one (set per rank to shard one job over GPUs) */
+#define SPX_OPT_RECORD_CAPACITY 7   /* records kept per distribution with keep_records, default 65536 */
 /* plugin kinds: see spectrum_gb300/plugins.py; e.g. background 1 uniform, 3 smooth shock,
  * 4 dipole, 5 solar wind; diffusion 5 full constant, 8 rigidity/field power law; boundary
  * 1 time expire, 10 plane absorb, 14 sphere absorb, 30 momentum inject; distribution 2 position
@@ -194,6 +195,15 @@ int spx_get_distribution(spx_ctx_t ctx, int problem, int distro, int32_t* counts
 /* Final states of the trajectories of one problem (SPX_OPT_RECORD_FINAL must be set). Returns the
  * number written (<= max_records) or an error code. */
 int64_t spx_get_records(spx_ctx_t ctx, int problem, spx_traj_record* out, int64_t max_records);
+
+/* The records of a distribution whose container set keep_records (DistributionTemplated::AddRecord,
+ * src/distribution_templated.cc:188-192; the values_record / weights_record arrays): the value
+ * (3 doubles) and the weight (width doubles, spx_get_distribution_info) of every processed event,
+ * outliers included, in the order the device appended them. At most SPX_OPT_RECORD_CAPACITY are
+ * stored; *n_events receives the number recorded. Returns the number written (<= max_records), or
+ * SPX_ERR_STATE when the distribution keeps no records. */
+int64_t spx_get_distribution_records(spx_ctx_t ctx, int problem, int distro, double* values, double* weights,
+                                     int64_t max_records, int64_t* n_events);
 
 /* Clear all distributions (DistributionTemplated::ResetDistribution). */
 int spx_reset_distributions(spx_ctx_t ctx);

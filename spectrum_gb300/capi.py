@@ -21,6 +21,7 @@ SPX_OPT_PA_SCATTERING = 3
 SPX_OPT_RECORD_FINAL = 4
 SPX_OPT_MAX_ATTEMPTS = 5
 SPX_OPT_RUN_INDEX = 6
+SPX_OPT_RECORD_CAPACITY = 7
 SPX_ERR_INVALID_ARG = -1
 SPX_ERR_IO = -12
 SPX_ERR_MISMATCH = -14
@@ -29,7 +30,8 @@ SPX_ERR_MISMATCH = -14
 EXPORTS = ["spx_create", "spx_set_option", "spx_add_plugin", "spx_add_problem", "spx_run", "spx_sync",
            "spx_get_distribution_info", "spx_get_distribution", "spx_get_records", "spx_reset_distributions",
            "spx_dump", "spx_restore", "spx_strerror", "spx_destroy", "spx_version", "spx_run_static",
-           "spx_autotune", "spx_set_background_grid", "spx_dump_distribution", "spx_restore_distribution"]
+           "spx_autotune", "spx_set_background_grid", "spx_dump_distribution", "spx_restore_distribution",
+           "spx_get_distribution_records"]
 
 #: bytes of the fixed device array spx_run_static works in (SPX_STATIC_SCRATCH_BYTES)
 STATIC_SCRATCH_BYTES = 512 * 1024
@@ -84,6 +86,9 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         lib.spx_dump.argtypes = [c_vp, ctypes.c_char_p]
         lib.spx_restore.argtypes = [c_vp, ctypes.c_char_p]
         lib.spx_dump_distribution.argtypes = [c_vp, c_int, c_int, ctypes.c_char_p]
+        lib.spx_get_distribution_records.argtypes = [c_vp, c_int, c_int, c_vp, c_vp, ctypes.c_int64,
+                                                     ctypes.POINTER(ctypes.c_int64)]
+        lib.spx_get_distribution_records.restype = ctypes.c_int64
         lib.spx_restore_distribution.argtypes = [c_vp, c_int, c_int, ctypes.c_char_p]
         lib.spx_strerror.argtypes = [c_int]
         lib.spx_strerror.restype = ctypes.c_char_p
@@ -193,6 +198,21 @@ class Context:
                                             sums.ctypes.data_as(ctypes.c_void_p), ctypes.byref(ne)),
               "spx_get_distribution")
         return counts, sums.reshape(nb, w), ne.value
+
+    def distribution_records(self, problem: int, distro: int):
+        """(values[k, 3], weights[k, width], events recorded) of a keep_records distribution
+        (DistributionTemplated::AddRecord): k = min(events, SPX_OPT_RECORD_CAPACITY)."""
+        _, w = self.distribution_info(problem, distro)
+        total = ctypes.c_int64()
+        check(self.lib.spx_get_distribution_records(self._h, problem, distro, None, None, 0, ctypes.byref(total)),
+              "spx_get_distribution_records")
+        n = total.value
+        vals = np.zeros((max(n, 1), 3))
+        wts = np.zeros((max(n, 1), w))
+        k = check(self.lib.spx_get_distribution_records(self._h, problem, distro, vals.ctypes.data_as(ctypes.c_void_p),
+                                                        wts.ctypes.data_as(ctypes.c_void_p), n, ctypes.byref(total)),
+                  "spx_get_distribution_records")
+        return vals[:k], wts[:k], total.value
 
     def records(self, problem: int, n: int) -> np.ndarray:
         out = np.zeros(n, dtype=RECORD_DTYPE)

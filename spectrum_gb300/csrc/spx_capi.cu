@@ -83,6 +83,13 @@ struct spx_ctx {
    double grid_cent[3] = {0, 0, 0}, grid_zone[3] = {0, 0, 0};
    double* d_grid64 = nullptr;
    float* d_grid32 = nullptr;
+   // distribution records (keep_records): per such distribution rec_capacity slots of 3 values and
+   // width weights, and one event counter per (problem, distribution)
+   int64_t rec_capacity = 65536;
+   double* d_rvals = nullptr;
+   double* d_rwts = nullptr;
+   unsigned long long* d_rn = nullptr;
+   int64_t n_rvals = 0, n_rwts = 0;
 };
 
 namespace {
@@ -104,6 +111,13 @@ void free_buffers(spx_ctx* c)
    cudaFree(c->d_sums);
    cudaFree(c->d_nev);
    cudaFree(c->d_rec);
+   cudaFree(c->d_rvals);
+   cudaFree(c->d_rwts);
+   cudaFree(c->d_rn);
+   c->d_rvals = nullptr;
+   c->d_rwts = nullptr;
+   c->d_rn = nullptr;
+   c->n_rvals = c->n_rwts = 0;
    c->d_pd = nullptr;
    c->d_pr = nullptr;
    c->d_ctr = nullptr;
@@ -180,10 +194,48 @@ int upload(spx_ctx* c)
    }
    if (c->d_ctr == nullptr) SPX_CUDA(cudaMalloc(&c->d_ctr, sizeof(spx::RunCounters)));
    if (grid_missing(c)) return SPX_ERR_STATE;
+   // record buffers of the keep_records distributions (DistributionBase::AddRecord)
+   int64_t rv = 0, rw = 0;
+   for (int k = 0; k < n; k++)
+      for (int d = 0; d < c->problems[k].pd.nd; d++)
+         if (c->problems[k].pd.d[d].keep_records) {
+            rv += 3 * c->rec_capacity;
+            rw += (int64_t)c->problems[k].pd.d[d].width * c->rec_capacity;
+         }
+   if (rv != c->n_rvals || rw != c->n_rwts || (rv > 0 && c->d_rn == nullptr)) {
+      cudaFree(c->d_rvals);
+      cudaFree(c->d_rwts);
+      cudaFree(c->d_rn);
+      c->d_rvals = c->d_rwts = nullptr;
+      c->d_rn = nullptr;
+      c->n_rvals = c->n_rwts = 0;
+      if (rv > 0) {
+         SPX_CUDA(cudaMalloc(&c->d_rvals, sizeof(double) * rv));
+         SPX_CUDA(cudaMalloc(&c->d_rwts, sizeof(double) * rw));
+         SPX_CUDA(cudaMalloc(&c->d_rn, sizeof(unsigned long long) * n * spx::kMaxDistro));
+         SPX_CUDA(cudaMemsetAsync(c->d_rn, 0, sizeof(unsigned long long) * n * spx::kMaxDistro, c->stream));
+         c->n_rvals = rv;
+         c->n_rwts = rw;
+      }
+   }
    std::vector<spx::ProblemDesc> hd(n);
+   rv = rw = 0;
    for (int k = 0; k < n; k++) {
       hd[k] = c->problems[k].pd;
       apply_grid(c, hd[k]);
+      for (int d = 0; d < hd[k].nd; d++) {
+         spx::DistParams& dp = hd[k].d[d];
+         dp.rec_vals = dp.rec_wts = nullptr;
+         dp.rec_n = nullptr;
+         dp.rec_cap = 0;
+         if (!dp.keep_records || c->d_rn == nullptr) continue;
+         dp.rec_vals = c->d_rvals + rv;
+         dp.rec_wts = c->d_rwts + rw;
+         dp.rec_n = c->d_rn + (int64_t)k * spx::kMaxDistro + d;
+         dp.rec_cap = c->rec_capacity;
+         rv += 3 * c->rec_capacity;
+         rw += (int64_t)dp.width * c->rec_capacity;
+      }
    }
    SPX_CUDA(cudaMemcpyAsync(c->d_pd, hd.data(), sizeof(spx::ProblemDesc) * n, cudaMemcpyHostToDevice, c->stream));
    if (c->precision == SPX_FP64) {
@@ -468,6 +520,12 @@ int spx_set_option(spx_ctx_t c, int option, double value)
    case SPX_OPT_MAX_ATTEMPTS:
       if (!(value >= 1.0)) return SPX_ERR_INVALID_ARG;
       c->max_attempts = (int)value;
+      return SPX_OK;
+   case SPX_OPT_RECORD_CAPACITY:
+      // records kept per keep_records distribution; further events are counted, not stored
+      if (!(value >= 0.0) || value != (double)(int64_t)value || value > 2147483647.0) return SPX_ERR_INVALID_ARG;
+      c->rec_capacity = (int64_t)value;
+      c->dirty = true;
       return SPX_OK;
    case SPX_OPT_RUN_INDEX:
       // shards of one job: rank r starting at index r draws trajectory ids disjoint from the others'
@@ -853,8 +911,58 @@ int spx_reset_distributions(spx_ctx_t c)
    SPX_CUDA(cudaMemsetAsync(c->d_counts, 0, sizeof(int32_t) * std::max<int64_t>(c->n_counts, 1), c->stream));
    SPX_CUDA(cudaMemsetAsync(c->d_sums, 0, sizeof(double) * std::max<int64_t>(c->n_sums, 1), c->stream));
    SPX_CUDA(cudaMemsetAsync(c->d_nev, 0, sizeof(unsigned long long) * c->problems.size() * spx::kMaxDistro, c->stream));
+   if (c->d_rn)
+      SPX_CUDA(cudaMemsetAsync(c->d_rn, 0, sizeof(unsigned long long) * c->problems.size() * spx::kMaxDistro, c->stream));
    SPX_CUDA(cudaStreamSynchronize(c->stream));
    return SPX_OK;
+}
+
+// The records slice of one keep_records distribution: device pointers and the slot count.
+static bool record_slice(const spx_ctx* c, int problem, int distro, double** vals, double** wts, unsigned long long** n)
+{
+   if (c->d_rn == nullptr) return false;
+   int64_t rv = 0, rw = 0;
+   for (int k = 0; k < (int)c->problems.size(); k++)
+      for (int d = 0; d < c->problems[k].pd.nd; d++) {
+         const spx::DistParams& dp = c->problems[k].pd.d[d];
+         if (!dp.keep_records) continue;
+         if (k == problem && d == distro) {
+            *vals = c->d_rvals + rv;
+            *wts = c->d_rwts + rw;
+            *n = c->d_rn + (int64_t)k * spx::kMaxDistro + d;
+            return true;
+         }
+         rv += 3 * c->rec_capacity;
+         rw += (int64_t)dp.width * c->rec_capacity;
+      }
+   return false;
+}
+
+int64_t spx_get_distribution_records(spx_ctx_t c, int problem, int distro, double* values, double* weights,
+                                     int64_t max_records, int64_t* n_events)
+{
+   int64_t nb = 0;
+   int w = 0;
+   int rc = spx_get_distribution_info(c, problem, distro, &nb, &w);
+   if (rc != SPX_OK) return rc;
+   if (max_records < 0 || (max_records > 0 && (!values || !weights))) return SPX_ERR_INVALID_ARG;
+   if (!c->problems[problem].pd.d[distro].keep_records) return SPX_ERR_STATE;
+   double *dv = nullptr, *dw = nullptr;
+   unsigned long long* dn = nullptr;
+   if (c->dirty || !record_slice(c, problem, distro, &dv, &dw, &dn)) {
+      if (n_events) *n_events = 0;
+      return 0;
+   }
+   unsigned long long total = 0;
+   SPX_CUDA(cudaStreamSynchronize(c->stream));
+   SPX_CUDA(cudaMemcpy(&total, dn, sizeof total, cudaMemcpyDeviceToHost));
+   if (n_events) *n_events = (int64_t)total;
+   const int64_t k = std::min<int64_t>(std::min<int64_t>((int64_t)total, c->rec_capacity), max_records);
+   if (k > 0) {
+      SPX_CUDA(cudaMemcpy(values, dv, sizeof(double) * 3 * k, cudaMemcpyDeviceToHost));
+      SPX_CUDA(cudaMemcpy(weights, dw, sizeof(double) * w * k, cudaMemcpyDeviceToHost));
+   }
+   return k;
 }
 
 // Checkpoint file: "SPXD" u32 version=1, u32 n_problems, i64 run_index, then per problem u32 nd and
@@ -938,8 +1046,9 @@ int spx_restore(spx_ctx_t c, const char* path)
 // One distribution in the file layout of DistributionTemplated::Dump (src/distribution_templated.cc:
 // 394-425), native little-endian: u32 name length, the class name, one byte of Specie (a class of
 // static members only, so sizeof is 1 and the byte is 0), u32 records and u32 bytes of the parameter
-// container and its bytes, i32 n_events, i32 counts[bins], the per-bin sums (1, 3 or 9 doubles), then
-// u32 0 and u32 0 for the two empty record arrays (records are not kept on the device).
+// container and its bytes, i32 n_events, i32 counts[bins], the per-bin sums (1, 3 or 9 doubles), then the
+// record arrays: u32 n and the values (3 doubles each), u32 n and the weights (width doubles each); both
+// are empty unless the distribution keeps records.
 int spx_dump_distribution(spx_ctx_t c, int problem, int distro, const char* path)
 {
    int64_t nb = 0;
@@ -956,15 +1065,29 @@ int spx_dump_distribution(spx_ctx_t c, int problem, int distro, const char* path
    rc = spx_get_distribution(c, problem, distro, counts.data(), sums.data(), &ne);
    if (rc != SPX_OK) return rc;
    if (ne > INT32_MAX) return SPX_ERR_LIMIT;  // the file's event count is an int
+   std::vector<double> rvals, rwts;
+   uint32_t n_kept = 0;
+   if (c->problems[problem].pd.d[distro].keep_records) {
+      int64_t total = 0;
+      int64_t k = spx_get_distribution_records(c, problem, distro, nullptr, nullptr, 0, &total);
+      if (k < 0) return (int)k;
+      const int64_t stored = std::min<int64_t>(total, c->rec_capacity);
+      if (stored > (int64_t)UINT32_MAX) return SPX_ERR_LIMIT;
+      rvals.resize(3 * stored);
+      rwts.resize((size_t)w * stored);
+      k = spx_get_distribution_records(c, problem, distro, rvals.data(), rwts.data(), stored, &total);
+      if (k < 0) return (int)k;
+      n_kept = (uint32_t)k;
+   }
    FILE* f = std::fopen(path, "wb");
    if (!f) return SPX_ERR_IO;
    const uint32_t name_len = (uint32_t)std::strlen(name), n_rec = pb.n_records, blob_len = (uint32_t)pb.blob.size();
    const uint8_t specie = 0;
    const int32_t ne32 = (int32_t)ne;
-   const uint32_t no_records[2] = {0, 0};
    bool ok = put(f, &name_len, 1) && put(f, name, name_len) && put(f, &specie, 1) && put(f, &n_rec, 1) &&
              put(f, &blob_len, 1) && put(f, pb.blob.data(), blob_len) && put(f, &ne32, 1) &&
-             put(f, counts.data(), (size_t)nb) && put(f, sums.data(), (size_t)(nb * w)) && put(f, no_records, 2);
+             put(f, counts.data(), (size_t)nb) && put(f, sums.data(), (size_t)(nb * w)) && put(f, &n_kept, 1) &&
+             put(f, rvals.data(), 3 * (size_t)n_kept) && put(f, &n_kept, 1) && put(f, rwts.data(), (size_t)w * n_kept);
    ok = (std::fclose(f) == 0) && ok;
    return ok ? SPX_OK : SPX_ERR_IO;
 }
@@ -972,7 +1095,8 @@ int spx_dump_distribution(spx_ctx_t c, int problem, int distro, const char* path
 // DistributionTemplated::Restore (src/distribution_templated.cc:433-466) for a distribution whose binning
 // is already fixed by its problem: the file's class name and parameter container must equal this
 // distribution's (else SPX_ERR_MISMATCH, where the reference returns without restoring); its counts,
-// sums and event count replace the device histogram. Record arrays in the file are read past.
+// sums and event count replace the device histogram, and the file's records the distribution's records
+// when it keeps them (SPX_ERR_TOO_LARGE beyond SPX_OPT_RECORD_CAPACITY); otherwise they are read past.
 int spx_restore_distribution(spx_ctx_t c, int problem, int distro, const char* path)
 {
    int64_t nb = 0;
@@ -1010,12 +1134,41 @@ int spx_restore_distribution(spx_ctx_t c, int problem, int distro, const char* p
       if (!get(f, blob.data(), blob_len)) rc = SPX_ERR_IO;
       else if (blob != pb.blob || n_rec != pb.n_records) rc = SPX_ERR_MISMATCH;
    }
+   const bool keep = c->problems[problem].pd.d[distro].keep_records != 0;
+   std::vector<double> rvals, rwts;
    if (rc == SPX_OK && !(get(f, &ne, 1) && ne >= 0 && get(f, counts.data(), (size_t)nb) &&
-                         get(f, sums.data(), (size_t)(nb * w)) && get(f, &n_values, 1) &&
-                         std::fseek(f, (long)n_values * 24, SEEK_CUR) == 0 && get(f, &n_weights, 1)))
+                         get(f, sums.data(), (size_t)(nb * w)) && get(f, &n_values, 1)))
       rc = SPX_ERR_IO;
+   if (rc == SPX_OK && keep && (int64_t)n_values > c->rec_capacity) rc = SPX_ERR_TOO_LARGE;
+   if (rc == SPX_OK) {
+      if (keep) {
+         rvals.resize(3 * (size_t)n_values);
+         if (!get(f, rvals.data(), rvals.size())) rc = SPX_ERR_IO;
+      }
+      else if (std::fseek(f, (long)n_values * 24, SEEK_CUR) != 0) rc = SPX_ERR_IO;
+   }
+   if (rc == SPX_OK && !get(f, &n_weights, 1)) rc = SPX_ERR_IO;
+   if (rc == SPX_OK && keep) {
+      if (n_weights != n_values) rc = SPX_ERR_IO;
+      else {
+         rwts.resize((size_t)w * n_weights);
+         if (!get(f, rwts.data(), rwts.size())) rc = SPX_ERR_IO;
+      }
+   }
    std::fclose(f);
    if (rc != SPX_OK) return rc;
+   if (keep) {
+      double *dv = nullptr, *dw = nullptr;
+      unsigned long long* dn = nullptr;
+      if (!record_slice(c, problem, distro, &dv, &dw, &dn)) return SPX_ERR_STATE;
+      const unsigned long long nv = n_values;
+      SPX_CUDA(cudaStreamSynchronize(c->stream));
+      if (n_values) {
+         SPX_CUDA(cudaMemcpy(dv, rvals.data(), sizeof(double) * rvals.size(), cudaMemcpyHostToDevice));
+         SPX_CUDA(cudaMemcpy(dw, rwts.data(), sizeof(double) * rwts.size(), cudaMemcpyHostToDevice));
+      }
+      SPX_CUDA(cudaMemcpy(dn, &nv, sizeof nv, cudaMemcpyHostToDevice));
+   }
    const spx::DistParams& dp = c->problems[problem].pd.d[distro];
    const unsigned long long neu = (unsigned long long)ne;
    SPX_CUDA(cudaStreamSynchronize(c->stream));

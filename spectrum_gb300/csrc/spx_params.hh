@@ -114,6 +114,14 @@ struct DistParamsT {
    R J0, T0, pow_law, T_b, pow_law_comb, bend, A0;
    int64_t offset_counts;     // into the context's counts array
    int64_t offset_sums;       // into the context's sums array (doubles)
+   // DistributionBase::AddRecord (keep_records): the value and weight of every processed event are
+   // appended at rec_vals[3k], rec_wts[width k] for slot k = atomicAdd(rec_n, 1) below rec_cap (set in the
+   // FP64 descriptors only; null when records are not kept)
+   int keep_records;
+   double* rec_vals;
+   double* rec_wts;
+   unsigned long long* rec_n;
+   int64_t rec_cap;
 };
 
 template <class R>

@@ -341,7 +341,7 @@ int parse_distribution(Reader& r, int kind, DistParams& d)
    r.mi(d.bin_outside);
    r.skip();  // unit_distro
    r.skip();  // unit_val
-   r.b();     // keep_records
+   d.keep_records = r.b() ? 1 : 0;
    d.dims = 0;
    for (int k = 0; k < 3; k++) {
       if (d.n_bins[k] > 0) d.dims |= 1 << k;

@@ -287,6 +287,14 @@ static __device__ __noinline__ void process_event(int traj, const EventPoint& e,
    }
    case kDsDivergenceFlow: w[0] = action == 0 ? d.A0 * pow(fabs(e.divU), d.pow_law) : d.val_cold; break;
    }
+   // AddRecord follows AddEvent for every processed event, outliers included (src/distribution_base.cc:192-193)
+   if (d.rec_n) {
+      const unsigned long long k = atomicAdd(d.rec_n, 1ull);
+      if (k < (unsigned long long)d.rec_cap) {
+         for (int i = 0; i < 3; i++) d.rec_vals[3 * k + i] = value[i];
+         for (int j = 0; j < d.width; j++) d.rec_wts[(int64_t)d.width * k + j] = w[j];
+      }
+   }
    int bin[3] = {0, 0, 0};
    for (int k = 0; k < 3; k++) {
       if (!(d.dims & (1 << k))) continue;

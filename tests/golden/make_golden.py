@@ -109,11 +109,12 @@ def _guiding_dipole(n_traj: int):
     return pb
 
 
-def _slab_between_mirrors(traj: int, n_traj: int, d0: float = 0.0):
+def _slab_between_mirrors(traj: int, n_traj: int, d0: float = 0.0, keep_records: bool = False):
     """A uniform field along x between two reflecting planes at x = -1 and x = +1 (code units):
     10 MeV protons from the origin, isotropic, 5 time units (several crossings of the slab). The
     pitch-angle cosine at the time boundary is binned. With ``d0`` the pitch angle scatters with
-    D_mumu = d0 (1 - mu^2) (DiffusionIsotropicConstant)."""
+    D_mumu = d0 (1 - mu^2) (DiffusionIsotropicConstant). With ``keep_records`` the distribution also
+    keeps the value and weight of every event (DistributionTemplated::AddRecord)."""
     from spectrum_gb300 import units as U
     from spectrum_gb300.datacontainer import DataContainer as DC
     from spectrum_gb300.plugins import (BackgroundUniform, BoundaryPlaneReflect, BoundaryTimeExpire,
@@ -130,7 +131,7 @@ def _slab_between_mirrors(traj: int, n_traj: int, d0: float = 0.0):
     pb.AddBoundary(BoundaryTimeExpire(), workloads._boundary(DC(), 1, [0]).double(5.0))
     pb.AddBoundary(BoundaryPlaneReflect(), workloads._boundary(DC(), -1, [-1]).vec((1.0, 0, 0)).vec((1.0, 0, 0)))
     pb.AddBoundary(BoundaryPlaneReflect(), workloads._boundary(DC(), -1, [-1]).vec((-1.0, 0, 0)).vec((-1.0, 0, 0)))
-    c = distro_header(DC(), (0, 20, 0), (0.0, -1.0, 0.0), (1.0, 1.0, 1.0))
+    c = distro_header(DC(), (0, 20, 0), (0.0, -1.0, 0.0), (1.0, 1.0, 1.0), keep_records=keep_records)
     pb.AddDistribution(DistributionMomentumUniform(), c.double(1.0).double(0.0).int(1).int(1))
     return pb
 
@@ -186,6 +187,7 @@ def cases():
     out.append(("focused_fwd_solarwind", _focused_reference_classes(6)))
     from spectrum_gb300.problem import TRAJ_FOCUSED, TRAJ_GUIDING_SCATT
     out.append(("focused_fwd_slab_reflect", _slab_between_mirrors(TRAJ_FOCUSED, 8)))
+    out.append(("focused_fwd_slab_records", _slab_between_mirrors(TRAJ_FOCUSED, 12, keep_records=True)))
     out.append(("guiding_fwd_dipole", _guiding_dipole(6)))
     out.append(("guidingscatt_fwd_slab_reflect", _slab_between_mirrors(TRAJ_GUIDING_SCATT, 8, d0=0.5)))
     from spectrum_gb300.problem import TRAJ_GUIDING_DIFF, TRAJ_GUIDING_DIFF_SCATT

@@ -2,7 +2,8 @@
 394-425), read on the CPU. The files under tests/golden/*.out were written by the reference's own
 Dump() (tests/golden/make_golden.py --dumps); these tests pin the reader and the layout the C ABI
 writes against them: class name, the one Specie byte, the parameter container exactly as the
-plugin blob, the event count, counts and sums exactly as the same run's histograms."""
+plugin blob, the event count, counts and sums exactly as the same run's histograms, and the record
+arrays of a distribution that keeps records."""
 import glob
 import os
 import struct
@@ -47,7 +48,13 @@ def test_reference_dump_matches_plugin_and_histogram(path):
     assert dump.n_events == n_events
     assert np.array_equal(dump.counts, counts)
     assert np.array_equal(dump.sums, sums)
-    assert dump.values_record.shape == (0, 3) and dump.weights_record.shape[0] == 0
+    if name.endswith("_records"):
+        # keep_records: one record per processed event; here every event is the final state (p, mu, 0)
+        assert dump.values_record.shape == (len(ref.traj), 3) and dump.weights_record.shape == (len(ref.traj), 1)
+        key = lambda a: a[np.lexsort(a.T[::-1])]  # noqa: E731
+        assert np.array_equal(key(dump.values_record), key(ref.traj["mom"]))
+    else:
+        assert dump.values_record.shape == (0, 3) and dump.weights_record.shape[0] == 0
     nb = dump.n_bins
     assert nb[0] * nb[1] * nb[2] == len(counts)
 

@@ -7,6 +7,9 @@
   of it is byte-identical, and a run adds its events on top (the reference's restart,
   src/simulation.cc:714-720).
 - A file of another class, a truncated or a missing file is refused with its code.
+- Records (keep_records): the device appends every event's value and weight; as a set they equal the
+  records in the reference's dump; dumped and restored with the histogram; beyond
+  SPX_OPT_RECORD_CAPACITY events are counted and not stored.
 - The whole-context checkpoint (spx_dump / spx_restore) resumes a run: restore + one run equals two
   runs in one context, since trajectory ids continue from the saved run index.
 """
@@ -148,3 +151,56 @@ def test_checkpoint_resumes_a_run(built_lib, tmp_path):
     finally:
         a.close()
         b.close()
+
+
+def _rows(a):
+    return a[np.lexsort(a.T[::-1])]
+
+
+def test_records_equal_the_reference_records(built_lib, tmp_path):
+    name = "focused_fwd_slab_records"
+    ref = distro_file.read(os.path.join(GOLDEN, name + ".distro0.out"))
+    sim = open_problems(CASES[name], capi.SPX_FP64)
+    try:
+        sim.DistroFileName(str(tmp_path / "rec"))
+        sim.MainLoop()
+        vals, wts, n = sim.ctx.distribution_records(0, 0)
+        assert n == len(ref.values_record) == 12
+        np.testing.assert_allclose(_rows(vals), _rows(ref.values_record), rtol=1e-12, atol=1e-14)
+        np.testing.assert_array_equal(wts, ref.weights_record)
+        ours = distro_file.read(sim.distro_path(0))
+        np.testing.assert_allclose(_rows(ours.values_record), _rows(ref.values_record), rtol=1e-12, atol=1e-14)
+        # a restored reference file brings its records back
+        sim.ctx.restore_distribution(0, 0, os.path.join(GOLDEN, name + ".distro0.out"))
+        vals2, wts2, n2 = sim.ctx.distribution_records(0, 0)
+        assert n2 == 12
+        np.testing.assert_array_equal(vals2, ref.values_record)
+    finally:
+        sim.close()
+
+
+def test_record_capacity(built_lib, tmp_path):
+    name = "focused_fwd_slab_records"
+    sim = open_problems(CASES[name], capi.SPX_FP64)
+    try:
+        sim.ctx.set_option(capi.SPX_OPT_RECORD_CAPACITY, 5)
+        sim.MainLoop()
+        vals, wts, n = sim.ctx.distribution_records(0, 0)
+        assert n == 12 and len(vals) == 5 and len(wts) == 5
+        path = str(tmp_path / "cap.out")
+        sim.ctx.dump_distribution(0, 0, path)
+        assert len(distro_file.read(path).values_record) == 5
+        with pytest.raises(capi.SpxError) as e:
+            sim.ctx.restore_distribution(0, 0, os.path.join(GOLDEN, name + ".distro0.out"))
+        assert e.value.code == -13
+        # distributions without keep_records have none
+        with pytest.raises(capi.SpxError) as e:
+            other = open_problems(CASES["focused_fwd_slab_reflect"], capi.SPX_FP64)
+            try:
+                other.ctx.distribution_records(0, 0)
+            finally:
+                other.close()
+        assert e.value.code == -8
+    finally:
+        sim.close()
+
