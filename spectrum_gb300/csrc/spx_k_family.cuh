@@ -1,6 +1,6 @@
 // spx_k_family.cuh -- launch and occupancy entry points of the stepping kernel for one
 // trajectory family, arithmetic and field-derivative method, switching over the background
-// classes. Each spx_k_*.cu instantiates it once, so the nine kernel sets compile in parallel.
+// classes. Each spx_k_*.cu instantiates it once, so the twelve kernel sets compile in parallel.
 #pragma once
 
 #include "spx_launch.hh"
