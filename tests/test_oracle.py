@@ -3,6 +3,7 @@ against its published known-answer vectors, the stepping path against the golden
 written from the reference's own code, and -- where the reference sources were built here --
 against the reference run live on inputs the fixtures do not hold. CPU only."""
 import os
+import sys
 
 import numpy as np
 import pytest
@@ -101,6 +102,32 @@ def test_oracle_matches_reference_live_solarwind():
     pbs = workloads.gcr_modulation(n_traj=4, energies_mev=[55.0], t_max_years=0.05)
     pb = pbs[0]
     pb.seed = 0xC0FFEE
+    _assert_same(ot.run_oracle(pb), ot.run_reference(pb))
+
+
+needs_gc_ref = pytest.mark.skipif(not os.path.exists(os.path.join(ot.REF_DIR, "ref_guidingdiffscatt_fwd_rk25")),
+                                  reason="reference harness not built (needs the reference sources)")
+
+
+def _golden_builders():
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden"))
+    import make_golden
+    return make_golden
+
+
+@needs_gc_ref
+@pytest.mark.parametrize("kind", ["guiding_dipole", "guidingscatt_slab", "guidingdiff_dipole", "guidingdiffscatt_slab",
+                                  "focused_slab_reflect"])
+def test_oracle_matches_reference_live_guiding(kind):
+    """The guiding-centre types and focused reflection on seeds and sizes the fixtures do not hold."""
+    from spectrum_gb300.problem import TRAJ_FOCUSED, TRAJ_GUIDING_DIFF, TRAJ_GUIDING_DIFF_SCATT, TRAJ_GUIDING_SCATT
+    mg = _golden_builders()
+    pb = {"guiding_dipole": lambda: mg._guiding_dipole(10),
+          "guidingscatt_slab": lambda: mg._slab_between_mirrors(TRAJ_GUIDING_SCATT, 16, d0=2.0),
+          "guidingdiff_dipole": lambda: mg._guiding_perp(TRAJ_GUIDING_DIFF, 10, dipole=True),
+          "guidingdiffscatt_slab": lambda: mg._guiding_perp(TRAJ_GUIDING_DIFF_SCATT, 16, dipole=False),
+          "focused_slab_reflect": lambda: mg._slab_between_mirrors(TRAJ_FOCUSED, 16, keep_records=True)}[kind]()
+    pb.seed = 0xBADC0DE + len(kind)
     _assert_same(ot.run_oracle(pb), ot.run_reference(pb))
 
 
