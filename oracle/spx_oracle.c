@@ -1971,20 +1971,77 @@ static void pa_physical_step(trj_t* T)
    T->dt_physical = fmin(T->dt_physical, 0.5 * dmumax / fabs(T->Vmu));
 }
 
-/* TrajectoryGuidingScatt::EulerPitchAngleScatt (src/trajectory_guiding_scatt.cc:61-84). The k-th normal of
- * a trajectory is the first of the SPX_RNG_STEP block with index k, redraws included (one normal per
- * block). */
+/* The k-th normal of a guiding-centre trajectory, redraws included, is the first of the SPX_RNG_STEP
+ * block with index k (one normal per block). */
+static double gc_normal(trj_t* T)
+{
+   double n[4];
+   uint32_t b[4];
+   spx_rng_block(T->pb->seed, (uint32_t)T->n_normal++, T->traj_id, T->pb->problem, SPX_RNG_STEP, T->attempt, b);
+   spx_normals4(b, n);
+   return n[0];
+}
+
+/* D_mumu at (p, mu) of the step's point (GetComponent(2, ...) with a modified momentum) */
+static double dmumu_at(trj_t* T, double t, double p, double mu)
+{
+   dstate st;
+   memset(&st, 0, sizeof st);
+   return get_component(T, 2, t, T->pos, V(p, mu, 0.0), &T->sp, &st);
+}
+
+/* The pitch-angle steps of TrajectoryGuidingScatt (src/trajectory_guiding_scatt.cc:61-247):
+ * STOCHASTIC_METHOD_MU 0 Euler (:61-84), 1 Milstein (:91-130), 2 RK2 (:137-247), each redrawing while
+ * |mu| > 1 (here at most 256 times, then mu is clamped). */
 static void guiding_pa_scatter(trj_t* T)
 {
    v3 mc = convert_mom(T);
-   double mu_new, n[4];
-   uint32_t b[4];
+   const double dt = T->dt;
+   double mu_new;
    int tries = 0;
-   do {
-      spx_rng_block(T->pb->seed, (uint32_t)T->n_normal++, T->traj_id, T->pb->problem, SPX_RNG_STEP, T->attempt, b);
-      spx_normals4(b, n);
-      mu_new = mc.x[1] + T->Vmu * T->dt + sqrt(2.0 * T->Dmumu * T->dt) * n[0];
-   } while (fabs(mu_new) > 1.0 && ++tries < 256);
+   if (T->o->mu_method == 1) {
+      double mu = T->mom.x[2] / vnorm(T->mom);
+      double b = sqrt(2.0 * T->Dmumu);
+      double dmu = SP_SMALL * (mu + SP_SMALL < 1.0 ? 1.0 : -1.0);
+      double b1 = (sqrt(2.0 * dmumu_at(T, T->t, mc.x[0], mc.x[1] + dmu)) - b) / dmu;
+      do {
+         double dw = sqrt(dt) * gc_normal(T);
+         mu_new = mu + T->Vmu * dt + b * dw + 0.5 * b * b1 * (dw * dw - dt);
+      } while (fabs(mu_new) > 1.0 && ++tries < 256);
+   }
+   else if (T->o->mu_method == 2) {
+      const double gambar = 1.0 / sqrt(3.0);
+      double mu = T->mom.x[2] / vnorm(T->mom);
+      double sv0 = T->Vmu, sv1 = 0.0, sd0 = sqrt(2.0 * T->Dmumu), sd1 = 0.0, sd2 = 0.0;
+      do {
+         double dw = sqrt(dt) * gc_normal(T), d, dn, dmu, dfit;
+         mu_new = mu + sd0 * dw;
+         mu_new += sv0 * dt;
+         if (fabs(mu_new) > 1.0) continue;
+         d = dmumu_at(T, T->t + dt, mc.x[0], mu_new);
+         dmu = SP_SMALL * (mu_new + SP_SMALL < 1.0 ? 1.0 : -1.0);
+         dn = dmumu_at(T, T->t + dt, mc.x[0], mu_new + dmu);
+         sv1 = (dn - d) / dmu;
+         mu_new = mu + gambar * sd0 * dw;
+         mu_new += sv0 * dt;
+         if (fabs(mu_new) > 1.0) continue;
+         sd1 = sqrt(2.0 * dmumu_at(T, T->t + dt, mc.x[0], mu_new));
+         mu_new = mu - sd0 / (3.0 * gambar) * dw;
+         mu_new += sv0 * dt;
+         if (fabs(mu_new) > 1.0) continue;
+         sd2 = sqrt(2.0 * dmumu_at(T, T->t + dt, mc.x[0], mu_new));
+         dmu = SP_SMALL * (mu + SP_SMALL < 1.0 ? 1.0 : -1.0);
+         dfit = (sqrt(2.0 * dmumu_at(T, T->t, mc.x[0], mu + dmu)) - sd0) / dmu;
+         mu_new = mu + (0.5 * sd0 + (sd1 + 3.0 * (gambar * gambar) * sd2) / (2.0 + 6.0 * (gambar * gambar))) * dw;
+         mu_new += 0.5 * dt * (sv0 + sv1);
+         mu_new += 0.5 * sd0 * dfit * (dw * dw - dt);
+      } while (fabs(mu_new) > 1.0 && ++tries < 256);
+   }
+   else {
+      do {
+         mu_new = mc.x[1] + T->Vmu * dt + sqrt(2.0 * T->Dmumu * dt) * gc_normal(T);
+      } while (fabs(mu_new) > 1.0 && ++tries < 256);
+   }
    if (fabs(mu_new) > 1.0) mu_new = (mu_new > 0.0) ? 1.0 : -1.0;
    T->mom.x[0] = mc.x[0] * sqrt(1.0 - mu_new * mu_new);
    T->mom.x[2] = mc.x[0] * mu_new;

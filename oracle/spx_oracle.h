@@ -30,7 +30,7 @@ typedef struct {
 } spx_oracle_traj;
 
 typedef struct {
-   int traj_type;          /* 200 Lorentz, 205 Focused, 206 Parker, 207 Parker+source */
+   int traj_type;          /* 200 Lorentz, 201-204 guiding centre, 205 Focused, 206 Parker, 207 Parker+source */
    int time_flow;          /* 0 forward, 1 backward */
    int rk;                 /* Butcher table number of common/rk_config.hh (0 or 25) */
    int deriv_mode;         /* 0: the reference's compiled-in defaults; 1: analytic derivatives */
@@ -40,6 +40,7 @@ typedef struct {
    int reference_quirks;   /* 1: reproduce deviation D1 as the reference has it (the smooth shock's dmax
                               from the previous field evaluation), to compare with the reference's own
                               output; 0: the corrected behaviour the CUDA kernels share */
+   int mu_method;          /* guiding-centre pitch-angle step: 0 Euler, 1 Milstein, 2 RK2 (STOCHASTIC_METHOD_MU) */
 } spx_oracle_opts;
 
 /*

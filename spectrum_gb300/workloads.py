@@ -348,3 +348,4 @@ SPX_OPT_STEPS_PER_ORBIT = 1
 SPX_OPT_DERIV_MODE = 2
 SPX_OPT_PA_SCATTERING = 3
 SPX_OPT_RECORD_FINAL = 4
+SPX_OPT_MU_METHOD = 8

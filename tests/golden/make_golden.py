@@ -28,7 +28,7 @@ sys.path.insert(0, ROOT)
 sys.path.insert(0, os.path.dirname(HERE))
 
 from spectrum_gb300 import workloads  # noqa: E402
-from spectrum_gb300.workloads import SPX_OPT_PA_SCATTERING, SPX_OPT_STEPS_PER_ORBIT  # noqa: E402
+from spectrum_gb300.workloads import SPX_OPT_MU_METHOD, SPX_OPT_PA_SCATTERING, SPX_OPT_STEPS_PER_ORBIT  # noqa: E402
 
 
 def _dipole_reference_classes(n_traj: int):
@@ -190,6 +190,10 @@ def cases():
     out.append(("focused_fwd_slab_records", _slab_between_mirrors(TRAJ_FOCUSED, 12, keep_records=True)))
     out.append(("guiding_fwd_dipole", _guiding_dipole(6)))
     out.append(("guidingscatt_fwd_slab_reflect", _slab_between_mirrors(TRAJ_GUIDING_SCATT, 8, d0=0.5)))
+    for mu in (1, 2):  # the Milstein and RK2 pitch-angle schemes (STOCHASTIC_METHOD_MU)
+        pb = _slab_between_mirrors(TRAJ_GUIDING_SCATT, 8, d0=0.5)
+        pb.options[SPX_OPT_MU_METHOD] = mu
+        out.append((f"guidingscatt_mu{mu}_fwd_slab_reflect", pb))
     from spectrum_gb300.problem import TRAJ_GUIDING_DIFF, TRAJ_GUIDING_DIFF_SCATT
     out.append(("guidingdiff_fwd_uniform", _guiding_perp(TRAJ_GUIDING_DIFF, 8, dipole=False)))
     out.append(("guidingdiff_fwd_dipole", _guiding_perp(TRAJ_GUIDING_DIFF, 6, dipole=True)))
@@ -246,6 +250,7 @@ def main():
               "traj_kind": np.int64(pb.traj), "time_flow": np.int64(pb.time_flow), "rk": np.int64(pb.rk),
               "steps_per_orbit": np.float64(pb.options.get(SPX_OPT_STEPS_PER_ORBIT, 100.0)),
               "pa_scattering": np.int64(pb.options.get(SPX_OPT_PA_SCATTERING, 0)),
+              "mu_method": np.int64(pb.options.get(SPX_OPT_MU_METHOD, 0)),
               "n_traj": np.int64(pb.n_traj)}
         fx.update(sparse(ref.distros))
         path = os.path.join(HERE, name + ".npz")
