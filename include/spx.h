@@ -76,6 +76,9 @@ extern "C" {
 #define SPX_OPT_RUN_INDEX 6         /* index of the next run: problem p's trajectory ids start at index * n_traj(p);
                                        each run advances it by one (set per rank to shard one job over GPUs) */
 #define SPX_OPT_RECORD_CAPACITY 7   /* records kept per distribution with keep_records, default 65536 */
+#define SPX_OPT_MU_METHOD 8         /* GuidingScatt / GuidingDiffScatt pitch-angle scheme, the reference's compile-time
+                                       STOCHASTIC_METHOD_MU (src/trajectory_guiding_scatt.hh:24): 0 Euler (default),
+                                       1 Milstein, 2 RK2 */
 /* plugin kinds: see spectrum_gb300/plugins.py; e.g. background 1 uniform, 3 smooth shock,
  * 4 dipole, 5 solar wind; diffusion 5 full constant, 8 rigidity/field power law; boundary
  * 1 time expire, 10 plane absorb, 14 sphere absorb, 30 momentum inject; distribution 2 position

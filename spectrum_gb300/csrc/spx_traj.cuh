@@ -766,12 +766,56 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
       R sq = m_sqrt(R(2) * Dmumu * L.dt);
       R mu_new;
       if (TT == kGuiding) {
-         // the k-th normal of the trajectory, redraws included, is the first of step block k
+         // the k-th normal of the trajectory, redraws included, is the first of step block k; the
+         // schemes of src/trajectory_guiding_scatt.cc:61-247 redraw while |mu| > 1 (here at most 256 times).
+         // Their finite differences in mu shift by sp_small = 1e-8, below float resolution, so the FP32
+         // kernels shift by 1e-3.
+         const R ds = sizeof(R) == sizeof(double) ? Lim<R>::small : R(1e-3);
          int tries = 0;
-         do {
-            normals4<R>(rng_block(P.seed, L.nrm++, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
-            mu_new = mu + Vmu * L.dt + sq * n[0];
-         } while (m_abs(mu_new) > R(1) && ++tries < 256);
+         if (cfg.mu_method == 1) {  // MilsteinPitchAngleScatt (:91-130)
+            const R b = m_sqrt(R(2) * Dmumu);
+            const R dmu = ds * (mu + ds < R(1) ? R(1) : R(-1));
+            const R b1 = (m_sqrt(R(2) * kappa_mumu(P.df, vmag, Omega, mu + dmu)) - b) / dmu;
+            do {
+               normals4<R>(rng_block(P.seed, L.nrm++, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
+               const R dw = m_sqrt(L.dt) * n[0];
+               mu_new = mu + Vmu * L.dt + b * dw + R(0.5) * b * b1 * (dw * dw - L.dt);
+            } while (m_abs(mu_new) > R(1) && ++tries < 256);
+         }
+         else if (cfg.mu_method == 2) {  // RK2PitchAngleScatt (:137-247)
+            const R g = R(1) / m_sqrt(R(3));
+            const R sv0 = Vmu, sd0 = m_sqrt(R(2) * Dmumu);
+            R sv1 = R(0), sd1 = R(0), sd2 = R(0);
+            do {
+               normals4<R>(rng_block(P.seed, L.nrm++, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
+               const R dw = m_sqrt(L.dt) * n[0];
+               mu_new = mu + sd0 * dw;
+               mu_new += sv0 * L.dt;
+               if (m_abs(mu_new) > R(1)) continue;
+               const R d = kappa_mumu(P.df, vmag, Omega, mu_new);
+               R dmu = ds * (mu_new + ds < R(1) ? R(1) : R(-1));
+               sv1 = (kappa_mumu(P.df, vmag, Omega, mu_new + dmu) - d) / dmu;
+               mu_new = mu + g * sd0 * dw;
+               mu_new += sv0 * L.dt;
+               if (m_abs(mu_new) > R(1)) continue;
+               sd1 = m_sqrt(R(2) * kappa_mumu(P.df, vmag, Omega, mu_new));
+               mu_new = mu - sd0 / (R(3) * g) * dw;
+               mu_new += sv0 * L.dt;
+               if (m_abs(mu_new) > R(1)) continue;
+               sd2 = m_sqrt(R(2) * kappa_mumu(P.df, vmag, Omega, mu_new));
+               dmu = ds * (mu + ds < R(1) ? R(1) : R(-1));
+               const R dfit = (m_sqrt(R(2) * kappa_mumu(P.df, vmag, Omega, mu + dmu)) - sd0) / dmu;
+               mu_new = mu + (R(0.5) * sd0 + (sd1 + R(3) * (g * g) * sd2) / (R(2) + R(6) * (g * g))) * dw;
+               mu_new += R(0.5) * L.dt * (sv0 + sv1);
+               mu_new += R(0.5) * sd0 * dfit * (dw * dw - L.dt);
+            } while (m_abs(mu_new) > R(1) && ++tries < 256);
+         }
+         else {  // EulerPitchAngleScatt (:61-84)
+            do {
+               normals4<R>(rng_block(P.seed, L.nrm++, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
+               mu_new = mu + Vmu * L.dt + sq * n[0];
+            } while (m_abs(mu_new) > R(1) && ++tries < 256);
+         }
       }
       else {
          normals4<R>(rng_block(P.seed, L.steps, L.traj_id, P.problem_id, kRngStep, L.attempt), n);

@@ -8,7 +8,8 @@ and the reflection of focused trajectories (ReverseMomentum negates mu only).
   centres as <y^2 + z^2> = 4 D_perp t; an equatorial proton in a dipole drifts at the gradient-drift rate
   omega = 1.5 r_L v / r^2 and keeps its radius; in the dipole the magnetic moment p_perp^2 / B
   and |p| are conserved along the orbit (PPERP_METHOD 1 integrates dp_perp/dt = p_perp/(2B) dB/dt);
-  pure pitch-angle scattering relaxes <mu> as mu0 exp(-2 D0 t).
+  pure pitch-angle scattering relaxes <mu> as mu0 exp(-2 D0 t) with each of the reference's three
+  pitch-angle schemes (Euler, Milstein, RK2).
 - Shock backgrounds are refused for the guiding types (their drift needs dB/dt).
 """
 import math
@@ -32,6 +33,11 @@ from spectrum_gb300.problem import (TRAJ_FOCUSED, TRAJ_GUIDING, TRAJ_GUIDING_DIF
                                     TRAJ_GUIDING_SCATT)
 
 
+def _with_mu(pb, mu):
+    pb.options[workloads.SPX_OPT_MU_METHOD] = float(mu)
+    return pb
+
+
 def _agree(rec, ref, tol):
     agree = rec["steps"] == ref.traj["steps"]
     assert agree.mean() >= 0.9, agree.mean()
@@ -47,6 +53,8 @@ def _agree(rec, ref, tol):
     ("guidingdiff_uniform", lambda: make_golden._guiding_perp(TRAJ_GUIDING_DIFF, 256, dipole=False)),
     ("guidingdiff_dipole", lambda: make_golden._guiding_perp(TRAJ_GUIDING_DIFF, 64, dipole=True)),
     ("guidingdiffscatt_uniform", lambda: make_golden._guiding_perp(TRAJ_GUIDING_DIFF_SCATT, 256, dipole=False)),
+    ("guidingscatt_milstein", lambda: _with_mu(make_golden._slab_between_mirrors(TRAJ_GUIDING_SCATT, 256, d0=0.5), 1)),
+    ("guidingscatt_rk2", lambda: _with_mu(make_golden._slab_between_mirrors(TRAJ_GUIDING_SCATT, 256, d0=0.5), 2)),
 ])
 def test_fp64_matches_oracle(built_lib, name, problem):
     pb = problem()
@@ -131,8 +139,9 @@ def test_equatorial_gradient_drift_rate(built_lib, precision):
     assert np.all(np.abs(rec["pos"][:, 2]) < 1e-6 * r)
 
 
+@pytest.mark.parametrize("mu_method", [0, 1, 2])
 @pytest.mark.parametrize("precision", [capi.SPX_FP64, capi.SPX_MIXED])
-def test_guiding_scatt_isotropisation(built_lib, precision):
+def test_guiding_scatt_isotropisation(built_lib, precision, mu_method):
     from spectrum_gb300.datacontainer import DataContainer as DC
     from spectrum_gb300.plugins import (BackgroundUniform, BoundaryTimeExpire, DiffusionIsotropicConstant,
                                         DistributionTimeUniform, InitialMomentumRing, InitialSpaceFixed,
@@ -148,6 +157,7 @@ def test_guiding_scatt_isotropisation(built_lib, precision):
     pb.AddBoundary(BoundaryTimeExpire(), workloads._boundary(DC(), 1, [0]).double(t_end))
     c = distro_header(DC(), (4, 0, 0), (0.0, 0, 0), (1.0, 0, 0))
     pb.AddDistribution(DistributionTimeUniform(), c.double(1.0).double(0.0).int(1))
+    pb.options[workloads.SPX_OPT_MU_METHOD] = float(mu_method)  # Euler, Milstein, RK2
     rec = run_problems(pb, precision=precision, record=True).records[0]
     p = np.linalg.norm(rec["mom"], axis=1)
     mu = rec["mom"][:, 2] / p
