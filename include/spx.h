@@ -181,7 +181,8 @@ int spx_autotune(spx_ctx_t ctx, int64_t sample_traj, spx_tuning* best);
  * the array and it keeps the last call's contents (each call clears the counters it needs):
  * calls whose launches overlap on the GPU race and give wrong results. Trajectory ids continue
  * from spx_run's, so a sequence of spx_run_static calls draws the same trajectories as the same
- * sequence of spx_run calls; spx_sync reports spx_run launches only. */
+ * sequence of spx_run calls; spx_sync reports spx_run launches only. Distribution records
+ * (keep_records) are not kept by this call: it has no buffer for them. */
 int spx_run_static(spx_ctx_t ctx, const spx_tuning* tuning, int32_t* counts, int64_t n_counts, double* sums,
                    int64_t n_sums, unsigned long long* n_events, int64_t n_events_len, spx_traj_record* records,
                    int64_t n_records, spx_stats* stats);
@@ -211,7 +212,9 @@ int64_t spx_get_distribution_records(spx_ctx_t ctx, int problem, int distro, dou
 /* Clear all distributions (DistributionTemplated::ResetDistribution). */
 int spx_reset_distributions(spx_ctx_t ctx);
 
-/* Write / read all distributions (the checkpoint of src/simulation.cc:592-594, 714-720). */
+/* Write / read all distributions and the run index (this library's whole-run checkpoint, the role of
+ * src/simulation.cc:592-594, 714-720); distribution records are not part of it (spx_dump_distribution
+ * writes them). */
 int spx_dump(spx_ctx_t ctx, const char* path);
 int spx_restore(spx_ctx_t ctx, const char* path);
 
