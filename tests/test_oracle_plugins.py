@@ -1,0 +1,290 @@
+"""The oracle against the reference's own code, one plugin class at a time.
+
+The golden fixtures exercise the plugin classes the benchmark set-ups use. Here every other
+boundary, initial condition, diffusion model, distribution and background class of the reference
+is swapped into a small problem and run by both the C restatement and the reference's sources
+(oracle/_ref, built where the sources are present): trajectories (attempts, outcome bits, steps,
+initial and final state, weights) and every histogram bin must agree bit for bit. Runs on the CPU;
+skipped where the reference harness is not built.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import oracle_tools as ot
+from spectrum_gb300 import units as U
+from spectrum_gb300 import workloads as W
+from spectrum_gb300.datacontainer import DataContainer as DC
+from spectrum_gb300.plugins import (BackgroundShock, BackgroundSmoothShock, BackgroundSolarWind, BackgroundUniform,
+                                    BoundaryBoxReflect, BoundaryCylinderAbsorb, BoundaryMomentumInjectRestrictShell,
+                                    BoundaryMomentumInjectRestrictSlab, BoundaryMomentumPass, BoundaryPlanePass,
+                                    BoundaryRankineAbsorb, BoundaryRegionAbsorb,
+                                    BoundarySphereReflect, BoundaryTimeExpire, BoundaryTimePass, BoundaryTimeRecurrent,
+                                    DiffusionEmpiricalSOQLTandUNLT, DiffusionFlowMomentumPowerLaw, DiffusionFullConstant,
+                                    DiffusionKineticEnergyRadialDistancePowerLaw, DiffusionParaConstant,
+                                    DiffusionPotgieterEtAl2015, DiffusionQLTConstant, DiffusionStraussEtAl2013,
+                                    DistributionDivergenceFlowPowerLaw, DistributionMomentumUniform,
+                                    DistributionPositionCumulativeOrder1, DistributionPositionCumulativeOrder2,
+                                    DistributionPositionMomentumUniform, DistributionPositionUniform,
+                                    DistributionSpectrumKineticEnergyBentPowerLaw, DistributionTimeUniform,
+                                    InitialMomentumBeam, InitialMomentumFixed, InitialMomentumMaxwell,
+                                    InitialMomentumRing, InitialMomentumShell, InitialMomentumThickShell,
+                                    InitialSpaceBox, InitialSpaceCircle, InitialSpaceFixed, InitialSpaceLine,
+                                    InitialSpaceRankineHalfBody, InitialSpaceSphere, InitialSpaceSphereSector,
+                                    InitialTimeFixed, InitialTimeInterval, SourceMomentumInjection)
+from spectrum_gb300.problem import (BACKWARD, FORWARD, TRAJ_FOCUSED, TRAJ_GUIDING_SCATT, TRAJ_LORENTZ, TRAJ_PARKER,
+                                    TRAJ_PARKER_SOURCE, Problem, distro_header)
+
+pytestmark = pytest.mark.skipif(not os.path.exists(os.path.join(ot.REF_DIR, "ref_guidingdiffscatt_fwd_rk25")),
+                                reason="reference harness not built (needs the reference sources)")
+
+B = W._boundary
+OUTCOME = 0x01F0 | 0x10000
+
+
+def _same(pb):
+    # deviation D1 (the smooth shock's step limit) reproduced as the reference has it, as for the fixtures
+    a, b = ot.run_oracle(pb, reference_quirks=1), ot.run_reference(pb)
+    assert len(a.traj) == len(b.traj)
+    for f in a.traj.dtype.names:
+        if f == "status":
+            assert np.array_equal(a.traj[f] & OUTCOME, b.traj[f] & OUTCOME), f
+        else:
+            assert np.array_equal(a.traj[f], b.traj[f]), f
+    for (ca, sa, na), (cb, sb, nb) in zip(a.distros, b.distros):
+        assert na == nb and np.array_equal(ca, cb) and np.array_equal(sa, sb)
+    return a
+
+
+def _parker(n=24, t_end=0.2, bg=None, diff=None, it=None, is_=None, im=None, dist=None, bnds=(), seed=0xFACE,
+            traj=TRAJ_PARKER, flow=FORWARD, t_action=(0,), src=None):
+    """Parker (or another type) in a uniform field along z, isotropic kappa = 1, dmax 0.05."""
+    rk = 0 if traj in (TRAJ_PARKER, TRAJ_PARKER_SOURCE) else 25
+    pb = Problem(traj=traj, time_flow=flow, rk=rk, seed=seed, n_traj=n)
+    pb.AddBackground(*(bg or (BackgroundUniform(), DC().double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0, 0, 1.0))
+                              .double(0.05))))
+    if diff is not False:
+        pb.AddDiffusion(*(diff or (DiffusionFullConstant(), DC().double(1.0).double(1.0))))
+    if src is not None:
+        pb.AddSource(*src)
+    pb.AddInitial(*(it or (InitialTimeFixed(), DC().double(0.0))))
+    pb.AddInitial(*(is_ or (InitialSpaceFixed(), DC().vec((0, 0, 0)))))
+    pb.AddInitial(*(im or (InitialMomentumShell(), DC().double(1.0))))
+    pb.AddBoundary(BoundaryTimeExpire(), B(DC(), 1, list(t_action)).double(t_end))
+    for bnd in bnds:
+        pb.AddBoundary(*bnd)
+    if dist is None:
+        c = distro_header(DC(), (20, 0, 0), (-1.0, 0, 0), (1.0, 0, 0))
+        dist = (DistributionPositionUniform(), c.double(1.0).double(0.0).int(1).int(0))
+    pb.AddDistribution(*dist)
+    return pb
+
+
+def _shock(smooth=True):
+    """The diffusive-shock set-up: upstream flow 1 along x into a shock of compression 4."""
+    c = DC().double(0.0).vec((0, 0, 0)).vec((1.0, 0, 0)).vec((0, 0, 1.0)).double(0.02)
+    c.vec((1.0, 0, 0)).double(0.0).double(4.0)
+    if smooth:
+        return BackgroundSmoothShock(), c.double(0.01).double(0.1)
+    return BackgroundShock(), c
+
+
+# -- spatial and time boundaries -----------------------------------------------------------------
+BOUNDARY_CASES = {
+    "plane_pass": (BoundaryPlanePass(), B(DC(), -1, [0]).vec((0.2, 0, 0)).vec((1.0, 0, 0))),
+    "sphere_reflect": (BoundarySphereReflect(), B(DC(), -1, [-1]).vec((0, 0, 0)).double(0.4)),
+    "box_reflect": (BoundaryBoxReflect(), B(DC(), -1, [-1]).vec((-0.3, -0.3, -0.3)).vec((0.6, 0, 0)).vec((0, 0.6, 0))
+                    .vec((0, 0, 0.6))),
+    "cylinder_absorb": (BoundaryCylinderAbsorb(), B(DC(), 1, [0]).vec((0, 0, 0)).vec((0, 0, 1.0)).double(0.3)),
+    "rankine_absorb": (BoundaryRankineAbsorb(), B(DC(), 1, [0]).vec((-0.4, 0, 0)).vec((1.0, 0, 0)).double(0.2)),
+    "time_pass": (BoundaryTimePass(), B(DC(), -1, [0]).double(0.1)),
+    "time_recurrent": (BoundaryTimeRecurrent(), B(DC(), 5, [0]).double(0.03)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(BOUNDARY_CASES))
+def test_boundary_classes(name):
+    _same(_parker(bnds=[BOUNDARY_CASES[name]]))
+
+
+def test_region_absorb_at_a_shock():
+    """BoundaryRegionAbsorb on the shock's region indicator (upstream/downstream)."""
+    pb = _parker(bg=_shock(smooth=False), bnds=[(BoundaryRegionAbsorb(), B(DC(), 1, [0]).int(0).double(1.5))],
+                 is_=(InitialSpaceFixed(), DC().vec((-0.05, 0, 0))), t_end=0.05)
+    _same(pb)
+
+
+@pytest.mark.parametrize("kind", ["pass", "slab", "shell"])
+def test_momentum_boundaries_at_a_shock(kind):
+    p_b = 0.995  # momenta fall through it in this set-up (expansion where the particles start)
+    bnd = {"pass": (BoundaryMomentumPass(), B(DC(), -1, [0]).double(p_b)),
+           "slab": (BoundaryMomentumInjectRestrictSlab(), B(DC(), 1, [0]).double(p_b).vec((-0.5, 0, 0)).vec((0.5, 0, 0))
+                    .vec((1.0, 0, 0))),
+           "shell": (BoundaryMomentumInjectRestrictShell(), B(DC(), 1, [0]).double(p_b).vec((0, 0, 0)).double(0.01)
+                     .double(0.5))}[kind]
+    c = distro_header(DC(), (20, 0, 0), (0.9, 0, 0), (1.2, 0, 0))
+    dist = (DistributionMomentumUniform(), c.double(1.0).double(0.0).int(1).int(0))
+    pb = _parker(bg=_shock(), bnds=[bnd], dist=dist, diff=(DiffusionFullConstant(), DC().double(0.01).double(0.01)),
+                 t_end=0.5)
+    _same(pb)
+
+
+def test_sharp_shock_background():
+    _same(_parker(bg=_shock(smooth=False), t_end=0.1))
+
+
+# -- initial conditions ----------------------------------------------------------------------------
+INITIAL_CASES = {
+    "time_interval": {"it": (InitialTimeInterval(), DC().double(0.0).double(0.05).int(0))},
+    "space_line": {"is_": (InitialSpaceLine(), DC().vec((-0.2, 0, 0)).vec((0.2, 0.1, 0)).int(0))},
+    "space_box": {"is_": (InitialSpaceBox(), DC().vec((-0.2, -0.2, -0.2)).vec((0.2, 0.2, 0.2)).int(0))},
+    "space_circle": {"is_": (InitialSpaceCircle(), DC().vec((0, 0, 0)).vec((0, 0.6, 0.8)).double(0.3))},
+    "space_sphere": {"is_": (InitialSpaceSphere(), DC().vec((0.1, 0, 0)).double(0.3))},
+    "space_sector": {"is_": (InitialSpaceSphereSector(), DC().vec((0, 0, 0)).double(0.3).double(0.5).double(1.2)
+                             .double(0.3).double(2.0))},
+    "space_rankine": {"is_": (InitialSpaceRankineHalfBody(), DC().vec((0, 0, 0)).double(0.2).double(0.5))},
+    "momentum_thick_shell_lin": {"im": (InitialMomentumThickShell(), DC().double(0.5).double(2.0).bool(False))},
+    "momentum_thick_shell_log": {"im": (InitialMomentumThickShell(), DC().double(0.5).double(2.0).bool(True))},
+    "momentum_maxwell": {"im": (InitialMomentumMaxwell(), DC().double(1.0).double(0.3).double(0.2))},
+}
+
+
+@pytest.mark.parametrize("name", sorted(INITIAL_CASES))
+def test_initial_classes(name):
+    c = distro_header(DC(), (10, 0, 0), (0.0, 0, 0), (3.0, 0, 0))
+    dist = (DistributionMomentumUniform(), c.double(1.0).double(0.0).int(0).int(0))
+    _same(_parker(dist=dist, t_end=0.05, **INITIAL_CASES[name]))
+
+
+@pytest.mark.parametrize("name", ["beam", "ring", "maxwell", "shell"])
+def test_focused_momentum_initials(name):
+    """The momentum samplers in the focused (p, mu) coordinates, recorded in (p, mu)."""
+    im = {"beam": (InitialMomentumBeam(), DC().double(1.0)),
+          "ring": (InitialMomentumRing(), DC().double(1.0).double(0.7)),
+          "maxwell": (InitialMomentumMaxwell(), DC().double(1.0).double(0.3).double(0.2)),
+          "shell": (InitialMomentumShell(), DC().double(1.0))}[name]
+    c = distro_header(DC(), (10, 10, 0), (0.0, -1.0, 0), (3.0, 1.0, 0))
+    dist = (DistributionMomentumUniform(), c.double(1.0).double(0.0).int(0).int(0))
+    _same(_parker(traj=TRAJ_FOCUSED, im=im, dist=dist, diff=False, t_end=0.05))
+
+
+@pytest.mark.parametrize("name", ["fixed", "beam", "ring", "maxwell"])
+def test_lorentz_momentum_initials(name):
+    """The samplers in Cartesian momentum about the local field (Lorentz)."""
+    im = {"fixed": (InitialMomentumFixed(), DC().vec((0.3, 0.4, 0.5))),
+          "beam": (InitialMomentumBeam(), DC().double(1.0)),
+          "ring": (InitialMomentumRing(), DC().double(1.0).double(0.7)),
+          "maxwell": (InitialMomentumMaxwell(), DC().double(1.0).double(0.3).double(0.2))}[name]
+    c = distro_header(DC(), (10, 10, 0), (0.0, -1.0, 0), (3.0, 1.0, 0))
+    dist = (DistributionMomentumUniform(), c.double(1.0).double(0.0).int(0).int(1))
+    pb = _parker(traj=TRAJ_LORENTZ, im=im, dist=dist, diff=False, t_end=0.01)
+    pb.options[W.SPX_OPT_STEPS_PER_ORBIT] = 100.0
+    _same(pb)
+
+
+# -- diffusion models ------------------------------------------------------------------------------
+def _sw_bg():
+    return BackgroundSolarWind(), W.solarwind_params(DC())
+
+
+_R1 = U.Rigidity(U.mev_to_mom(1000.0))  # 1 GV-ish reference rigidity
+_B5 = 5.0e-5 / U.unit_magnetic          # 5 nT
+_LAM = 0.1 * W.ONE_AU
+
+DIFFUSION_CASES = {
+    "para_constant": ((DiffusionParaConstant(), DC().double(1.0)), None),
+    "flow_momentum": ((DiffusionFlowMomentumPowerLaw(), DC().double(0.5).double(0.5).double(0.3).double(1.0).double(0.5)
+                       .double(0.1)), "flow"),
+    # kap0, T0, r0, pow_law_T, pow_law_r, kap_rat, stream_dep_idx, u_up, w_sh, s_sh
+    "kin_energy_radial": ((DiffusionKineticEnergyRadialDistancePowerLaw(),
+                           DC().double(0.5).double(1.0).double(0.2).double(0.5).double(1.0).double(0.1).int(0).double(1.0)
+                           .double(0.1).double(4.0)), "offset"),
+    # LISM_idx, lam_in, lam_out, R0, B0, kap_rat_in, kap_rat_out
+    "strauss": ((DiffusionStraussEtAl2013(), DC().int(-1).double(_LAM).double(_LAM).double(_R1).double(_B5).double(0.02)
+                 .double(0.02)), "sw"),
+    # LISM_idx, kappa_in, kappa_out, R0, B0, kap_rat_in, kap_rat_out
+    "potgieter": ((DiffusionPotgieterEtAl2015(), DC().int(-1).double(500.0).double(500.0).double(_R1).double(_B5)
+                   .double(0.02).double(0.02)), "sw"),
+    # lam_para, lam_perp, R0, B0, Bmix_idx, kap_rat_red, radial_limit_perp_red, solar_cycle_idx, solar_cycle_effect
+    "empirical": ((DiffusionEmpiricalSOQLTandUNLT(), DC().double(_LAM).double(0.01 * _LAM).double(_R1).double(_B5)
+                   .int(0).double(0.5).double(50.0 * W.ONE_AU).int(0).double(0.5)), "sw"),
+}
+
+
+@pytest.mark.parametrize("name", sorted(DIFFUSION_CASES))
+def test_diffusion_models(name):
+    diff, where = DIFFUSION_CASES[name]
+    if where == "sw":
+        au = W.ONE_AU
+        c = distro_header(DC(), (20, 0, 0), (0.5 * au, 0, 0), (1.5 * au, 0, 0))
+        dist = (DistributionPositionUniform(), c.double(1.0).double(0.0).int(1).int(1))
+        pb = _parker(bg=_sw_bg(), diff=diff, is_=(InitialSpaceFixed(), DC().vec((au, 0, 0))),
+                     im=(InitialMomentumShell(), DC().double(U.mev_to_mom(100.0))), dist=dist, t_end=0.002, n=12)
+    elif where == "offset":
+        pb = _parker(diff=diff, is_=(InitialSpaceFixed(), DC().vec((0.3, 0, 0))))
+    elif where == "flow":
+        bg = (BackgroundUniform(), DC().double(0.0).vec((0, 0, 0)).vec((0.5, 0, 0)).vec((0, 0, 1.0)).double(0.05))
+        pb = _parker(bg=bg, diff=diff)
+    else:
+        pb = _parker(diff=diff)
+    _same(pb)
+
+
+def test_qlt_pitch_angle_diffusion():
+    """DiffusionQLTConstant (D_mumu) in the guiding-centre scattering type."""
+    c = distro_header(DC(), (0, 20, 0), (0.0, -1.0, 0), (1.0, 1.0, 1.0))
+    dist = (DistributionMomentumUniform(), c.double(1.0).double(0.0).int(1).int(1))
+    pb = _parker(traj=TRAJ_GUIDING_SCATT, diff=(DiffusionQLTConstant(), DC().double(0.1).double(1.0).double(5.0 / 3.0)),
+                 dist=dist, t_end=0.5, im=(InitialMomentumShell(), DC().double(U.mev_to_mom(10.0))), n=12)
+    _same(pb)
+
+
+# -- distributions -------------------------------------------------------------------------------
+DIST_CASES = {
+    "cumulative1": (DistributionPositionCumulativeOrder1(), distro_header(DC(), (10, 0, 0), (0.0, 0, 0), (0.2, 0, 0),
+                                                                         width=3)),
+    "cumulative2": (DistributionPositionCumulativeOrder2(), distro_header(DC(), (10, 0, 0), (0.0, 0, 0), (0.2, 0, 0),
+                                                                         width=9)),
+    "position_momentum": (DistributionPositionMomentumUniform(),
+                          distro_header(DC(), (10, 10, 0), (-1.0, 0.5, 0), (1.0, 1.5, 0)).double(1.0).double(0.0).int(1)
+                          .int(3).int(0)),
+}
+
+
+@pytest.mark.parametrize("name", sorted(DIST_CASES))
+def test_distribution_classes(name):
+    _same(_parker(dist=DIST_CASES[name]))
+
+
+def test_divergence_flow_distribution_at_a_shock():
+    c = distro_header(DC(), (10, 0, 0), (0.0, 0, 0), (2.0, 0, 0))
+    dist = (DistributionDivergenceFlowPowerLaw(), c.double(2.0).double(1.5).double(0.0))
+    _same(_parker(bg=_shock(), dist=dist, t_end=0.05))
+
+
+def test_bent_power_law_spectrum():
+    """The modulation set-up with its spectrum recorded by the bent power law (T_b = 1 GeV)."""
+    from spectrum_gb300.datacontainer import read_records
+    from spectrum_gb300.problem import PluginEntry
+    pb = W.gcr_modulation(n_traj=6, energies_mev=[3000.0], t_max_years=0.05)[0]
+    for i, e in enumerate(pb.plugins):
+        if type(e.plugin).__name__ == "DistributionSpectrumKineticEnergyPowerLaw":
+            c = DC()
+            for rec in read_records(e.blob):  # the power-law container, then T_b, pow_law_b, bend
+                c._add(rec)
+            c.double(1000.0 * U.MEV / U.unit_energy).double(1.5).double(2.0)
+            pb.plugins[i] = PluginEntry(DistributionSpectrumKineticEnergyBentPowerLaw(), c.data(), c.size())
+    _same(pb)
+
+
+# -- the Parker source type ---------------------------------------------------------------------------
+def test_parker_source_injection():
+    """TrajectoryParkerSource with SourceMomentumInjection (backward in time at a smooth shock)."""
+    src = (SourceMomentumInjection(), DC().double(1.0).double(2.0))
+    c = distro_header(DC(), (10, 0, 0), (0.5, 0, 0), (2.0, 0, 0))
+    dist = (DistributionMomentumUniform(), c.double(1.0).double(0.0).int(1).int(0))
+    pb = _parker(traj=TRAJ_PARKER_SOURCE, flow=BACKWARD, bg=_shock(), src=src, dist=dist,
+                 im=(InitialMomentumShell(), DC().double(0.95)), t_end=-0.2, n=16)
+    r = _same(pb)
+    assert (r.traj["amp"] != 0.0).sum() >= 4  # momenta rise through p_inj = 1 and the source injects
