@@ -1,0 +1,117 @@
+"""Every plugin class on the device: the FP64 kernel against the oracle, trajectory by trajectory,
+on the one-class-at-a-time problems whose oracle runs tests/test_oracle_plugins.py pins bit for
+bit to the reference's own code. FMA contraction on the device perturbs the last bits, so step
+counts must agree for at least 90% of the trajectories, the median position error stays below
+1e-9 relative, and the histograms agree to within 10% of their events (a perturbed crossing moves
+an event)."""
+import numpy as np
+import pytest
+
+import oracle_tools as ot
+import test_oracle_plugins as cases
+from spectrum_gb300 import capi
+from spectrum_gb300.datacontainer import DataContainer as DC
+from spectrum_gb300.simulation import run_problems
+
+pytestmark = pytest.mark.gpu
+
+
+def _problems():
+    out = {}
+    for k, v in cases.BOUNDARY_CASES.items():
+        out["boundary_" + k] = lambda v=v: cases._parker(bnds=[v])
+    for k, v in cases.INITIAL_CASES.items():
+        def make(v=v):
+            c = cases.distro_header(DC(), (10, 0, 0), (0.0, 0, 0), (3.0, 0, 0))
+            dist = (cases.DistributionMomentumUniform(), c.double(1.0).double(0.0).int(0).int(0))
+            return cases._parker(dist=dist, t_end=0.05, **v)
+        out["initial_" + k] = make
+    for k in cases.DIST_CASES:
+        out["distribution_" + k] = lambda k=k: cases._parker(dist=cases.DIST_CASES[k])
+    out["sharp_shock"] = lambda: cases._parker(bg=cases._shock(smooth=False), t_end=0.1)
+    out["region_absorb"] = lambda: cases._parker(
+        bg=cases._shock(smooth=False), bnds=[(cases.BoundaryRegionAbsorb(), cases.B(DC(), 1, [0]).int(0).double(1.5))],
+        is_=(cases.InitialSpaceFixed(), DC().vec((-0.05, 0, 0))), t_end=0.05)
+    for k, (diff, where) in cases.DIFFUSION_CASES.items():
+        out["diffusion_" + k] = lambda k=k: _diffusion_case(k)
+    for kind in ("pass", "slab", "shell"):
+        out["momentum_boundary_" + kind] = lambda kind=kind: _momentum_case(kind)
+    for name in ("beam", "ring", "maxwell", "shell"):
+        out["focused_initial_" + name] = lambda name=name: _focused_initial(name)
+    out["divergence_flow"] = lambda: cases._parker(
+        bg=cases._shock(), t_end=0.05,
+        dist=(cases.DistributionDivergenceFlowPowerLaw(),
+              cases.distro_header(DC(), (10, 0, 0), (0.0, 0, 0), (2.0, 0, 0)).double(2.0).double(1.5).double(0.0)))
+    out["parker_source"] = _source_case
+    return out
+
+
+def _diffusion_case(name):
+    diff, where = cases.DIFFUSION_CASES[name]
+    if where == "sw":
+        au = cases.W.ONE_AU
+        c = cases.distro_header(DC(), (20, 0, 0), (0.5 * au, 0, 0), (1.5 * au, 0, 0))
+        dist = (cases.DistributionPositionUniform(), c.double(1.0).double(0.0).int(1).int(1))
+        return cases._parker(bg=cases._sw_bg(), diff=diff, is_=(cases.InitialSpaceFixed(), DC().vec((au, 0, 0))),
+                             im=(cases.InitialMomentumShell(), DC().double(cases.U.mev_to_mom(100.0))), dist=dist,
+                             t_end=0.002, n=12)
+    if where == "offset":
+        return cases._parker(diff=diff, is_=(cases.InitialSpaceFixed(), DC().vec((0.3, 0, 0))))
+    if where == "flow":
+        bg = (cases.BackgroundUniform(), DC().double(0.0).vec((0, 0, 0)).vec((0.5, 0, 0)).vec((0, 0, 1.0)).double(0.05))
+        return cases._parker(bg=bg, diff=diff)
+    return cases._parker(diff=diff)
+
+
+def _momentum_case(kind):
+    p_b = 0.995
+    B = cases.B
+    bnd = {"pass": (cases.BoundaryMomentumPass(), B(DC(), -1, [0]).double(p_b)),
+           "slab": (cases.BoundaryMomentumInjectRestrictSlab(), B(DC(), 1, [0]).double(p_b).vec((-0.5, 0, 0))
+                    .vec((0.5, 0, 0)).vec((1.0, 0, 0))),
+           "shell": (cases.BoundaryMomentumInjectRestrictShell(), B(DC(), 1, [0]).double(p_b).vec((0, 0, 0))
+                     .double(0.01).double(0.5))}[kind]
+    c = cases.distro_header(DC(), (20, 0, 0), (0.9, 0, 0), (1.2, 0, 0))
+    dist = (cases.DistributionMomentumUniform(), c.double(1.0).double(0.0).int(1).int(0))
+    return cases._parker(bg=cases._shock(), bnds=[bnd], dist=dist,
+                         diff=(cases.DiffusionFullConstant(), DC().double(0.01).double(0.01)), t_end=0.5)
+
+
+def _focused_initial(name):
+    im = {"beam": (cases.InitialMomentumBeam(), DC().double(1.0)),
+          "ring": (cases.InitialMomentumRing(), DC().double(1.0).double(0.7)),
+          "maxwell": (cases.InitialMomentumMaxwell(), DC().double(1.0).double(0.3).double(0.2)),
+          "shell": (cases.InitialMomentumShell(), DC().double(1.0))}[name]
+    c = cases.distro_header(DC(), (10, 10, 0), (0.0, -1.0, 0), (3.0, 1.0, 0))
+    dist = (cases.DistributionMomentumUniform(), c.double(1.0).double(0.0).int(0).int(0))
+    return cases._parker(traj=cases.TRAJ_FOCUSED, im=im, dist=dist, diff=False, t_end=0.05)
+
+
+def _source_case():
+    src = (cases.SourceMomentumInjection(), DC().double(1.0).double(2.0))
+    c = cases.distro_header(DC(), (10, 0, 0), (0.5, 0, 0), (2.0, 0, 0))
+    dist = (cases.DistributionMomentumUniform(), c.double(1.0).double(0.0).int(1).int(0))
+    return cases._parker(traj=cases.TRAJ_PARKER_SOURCE, flow=cases.BACKWARD, bg=cases._shock(), src=src, dist=dist,
+                         im=(cases.InitialMomentumShell(), DC().double(0.95)), t_end=-0.2, n=16)
+
+
+PROBLEMS = _problems()
+
+
+def _check(pb):
+    res = run_problems(pb, precision=capi.SPX_FP64, record=True)
+    ref = ot.run_oracle(pb)
+    rec = res.records[0]
+    agree = rec["steps"] == ref.traj["steps"]
+    assert agree.mean() >= 0.9, agree.mean()
+    scale = np.maximum(np.linalg.norm(ref.traj["pos"], axis=1), 1e-30)
+    err = np.linalg.norm(rec["pos"] - ref.traj["pos"], axis=1) / scale
+    assert np.median(err[agree]) < 1e-9, np.median(err[agree])
+    for (c_gpu, _, n_gpu), (c_ref, _, n_ref) in zip(res.distros[0], ref.distros):
+        assert abs(n_gpu - n_ref) <= max(1, 0.1 * n_ref), (n_gpu, n_ref)
+        assert np.abs(c_gpu.astype(np.int64) - c_ref).sum() <= max(2, 0.2 * n_ref)
+
+
+@pytest.mark.parametrize("name", sorted(PROBLEMS))
+def test_plugin_class_on_device(built_lib, name):
+    _check(PROBLEMS[name]())
