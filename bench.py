@@ -26,6 +26,7 @@ import os
 import statistics
 import subprocess
 import sys
+import tempfile
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -215,7 +216,7 @@ def per_bin_error(a, b, min_count):
     return worst_c, worst_s, nb
 
 
-# Throughput of the other workload families, for the per-family figures of the design doc. Each entry:
+# Throughput of the other workload families (the per-family figures). Each entry:
 # builder of the problem list (FP32 run), its description, and the share of it the FP64 plain
 # kernel runs for the ratio.
 def _other_workloads():
@@ -364,8 +365,10 @@ def main():
     for _ in range(args.warmup):
         sim.MainLoop(tun)
     sim.ctx.reset_distributions()
-    os.makedirs(os.path.join(ROOT, "gpurun_out"), exist_ok=True)
-    clocks = Clocks(local, os.path.join(ROOT, "gpurun_out", f"clocks_rank{rank}.csv"))
+    # nvidia-smi samples of the timed region go to SPX_CLOCKS_DIR (default: the temporary directory)
+    clocks_dir = os.environ.get("SPX_CLOCKS_DIR", tempfile.gettempdir())
+    os.makedirs(clocks_dir, exist_ok=True)
+    clocks = Clocks(local, os.path.join(clocks_dir, f"clocks_rank{rank}.csv"))
     kms = []
     steps_done = 0
     traj_done = 0
