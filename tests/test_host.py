@@ -74,6 +74,21 @@ def test_header_and_binding_agree():
     assert _declared_symbols() == sorted(capi.EXPORTS)
 
 
+def test_header_constants_match_binding():
+    """Every SPX_* constant the ctypes binding (and the workload options) defines has the value of
+    include/spx.h."""
+    hdr = open(os.path.join(ROOT, "include", "spx.h")).read()
+    defs = {m.group(1): int(m.group(2)) for m in re.finditer(r"^#define\s+(SPX_\w+)\s+(-?\d+)\b", hdr, re.M)}
+    checked = 0
+    for mod in (capi, workloads):
+        for name in dir(mod):
+            if name.startswith("SPX_") and isinstance(getattr(mod, name), int):
+                assert name in defs, name
+                assert getattr(mod, name) == defs[name], name
+                checked += 1
+    assert checked >= 15
+
+
 def test_library_exports_every_declared_symbol(built_lib):
     lib = ctypes.CDLL(built_lib)
     for name in _declared_symbols():
