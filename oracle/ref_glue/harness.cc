@@ -162,6 +162,8 @@ void AddPlugin(Probe& traj, uint32_t role, const std::string& name, const DataCo
       SPX_TRY_INI(InitialSpaceSphere)
       SPX_TRY_INI(InitialSpaceSphereSector)
       SPX_TRY_INI(InitialSpaceRankineHalfBody)
+      SPX_TRY_INI(InitialSpaceCylinder)
+      SPX_TRY_INI(InitialSpaceCylinderSector)
 #if (TRAJ_TYPE == TRAJ_LORENTZ) || (TRAJ_TYPE == TRAJ_FIELDLINE)
       SPX_TRY_INI(InitialMomentumFixed)
 #endif

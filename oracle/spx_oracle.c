@@ -242,6 +242,7 @@ typedef struct {
 } bnd_t;
 
 enum { IT_FIXED = 1, IT_INTERVAL, IS_FIXED = 10, IS_LINE, IS_CIRCLE, IS_BOX, IS_SPHERE, IS_SECTOR, IS_RANKINE,
+       IS_CYLINDER, IS_CYL_SECTOR,
        IM_FIXED = 30, IM_BEAM, IM_RING, IM_SHELL, IM_THICK, IM_MAXWELL, IM_LOGE_PITCH = 40, IS_EQ_BAND };
 typedef struct {
    int kind;
@@ -265,7 +266,7 @@ typedef struct {
 typedef struct {
    uint64_t seed;
    uint32_t n_traj, problem;
-   int has_bg, has_diff, has_src;
+   int has_bg, has_diff, has_src, src_kind;  /* src_kind 1 SourceConstant, 2 SourceMomentumInjection */
    bg_t bg;
    df_t df;
    double src_p_inj, src_rate;
@@ -465,6 +466,24 @@ static void setup_ini(ini_t* q, rd_t* r, int kind)
       q->a[5] = cos(q->a[1]);
       q->a[6] = cos(q->a[2]);
       break;
+   case IS_CYLINDER: case IS_CYL_SECTOR:
+      /* InitialSpaceCylinder(Sector)::SetupInitial (src/initial_space.cc:561-570, 621-631): origin, height vector,
+       * radius vector x; radius vector y = unit(height) x radius x; the sector's azimuths clamped to
+       * [phi1, min(phi2, 2 pi)] */
+      q->v0 = rd_v(r);
+      q->v1 = rd_v(r);
+      q->v2 = rd_v(r);
+      {
+         v3 ry = vcross(vunit(q->v1), q->v2);
+         q->a[0] = ry.x[0]; q->a[1] = ry.x[1]; q->a[2] = ry.x[2];
+      }
+      if (kind == IS_CYL_SECTOR) {
+         q->a[3] = rd_d(r);
+         q->a[4] = rd_d(r);
+         if (q->a[4] > M_2PI_) q->a[4] = M_2PI_;
+         if (q->a[4] < q->a[3]) q->a[4] = q->a[3];
+      }
+      break;
    case IS_RANKINE:
       q->v0 = rd_v(r); q->a[0] = rd_d(r); q->a[1] = rd_d(r);
       q->a[2] = (2.0 * q->a[0] * q->a[0] - q->a[1] * q->a[1]) / (q->a[1] * q->a[1]);
@@ -551,7 +570,7 @@ static int kind_of(uint32_t role, const char* nm, size_t nl)
       K("DiffusionPotgieterEtAl2015", DF_POTGIETER) K("DiffusionEmpiricalSOQLTandUNLT", DF_EMPIRICAL)
    }
    else if (role == 2) {
-      K("SourceMomentumInjection", 2)
+      K("SourceConstant", 1) K("SourceMomentumInjection", 2)
    }
    else if (role == 3) {
       K("BoundaryTimeExpire", BT_TIME) K("BoundaryTimePass", BT_TIME_PASS) K("BoundaryTimeRecurrent", BT_TIME_REC)
@@ -567,6 +586,7 @@ static int kind_of(uint32_t role, const char* nm, size_t nl)
       K("InitialSpaceLine", IS_LINE) K("InitialSpaceCircle", IS_CIRCLE) K("InitialSpaceBox", IS_BOX)
       K("InitialSpaceSphere", IS_SPHERE) K("InitialSpaceSphereSector", IS_SECTOR)
       K("InitialSpaceRankineHalfBody", IS_RANKINE) K("InitialSpaceEquatorialBand", IS_EQ_BAND)
+      K("InitialSpaceCylinder", IS_CYLINDER) K("InitialSpaceCylinderSector", IS_CYL_SECTOR)
       K("InitialMomentumFixed", IM_FIXED) K("InitialMomentumBeam", IM_BEAM) K("InitialMomentumRing", IM_RING)
       K("InitialMomentumShell", IM_SHELL) K("InitialMomentumThickShell", IM_THICK)
       K("InitialMomentumMaxwell", IM_MAXWELL) K("InitialMomentumLogEnergyPitchBand", IM_LOGE_PITCH)
@@ -619,7 +639,14 @@ static int parse_spec(const uint8_t* s, size_t n, prob_t* pb, char* err, size_t 
       if (kind < 0) { snprintf(err, el, "unknown plugin %.*s", (int)nl, nm); return -2; }
       if (role == 0) { setup_bg(&pb->bg, &r, kind); pb->has_bg = 1; }
       else if (role == 1) { setup_df(&pb->df, &r, kind); pb->has_diff = 1; }
-      else if (role == 2) { pb->src_p_inj = rd_d(&r); pb->src_rate = rd_d(&r); pb->has_src = 1; }
+      else if (role == 2) {
+         /* SourceConstant::SetupSource reads S0 (src/source_other.cc:41-50); SourceMomentumInjection p_inj
+          * and the rate (:98-107) */
+         pb->src_kind = kind;
+         if (kind == 1) pb->src_rate = rd_d(&r);
+         else { pb->src_p_inj = rd_d(&r); pb->src_rate = rd_d(&r); }
+         pb->has_src = 1;
+      }
       else if (role == 3) {
          bnd_t b;
          setup_bnd(&b, &r, kind);
@@ -1493,6 +1520,14 @@ static v3 sample_pos(trj_t* T)
       double phi = M_2PI_ * next_uniform(T);
       return vadd(q->v0, V(s * cos(phi), s * sin(phi), z));
    }
+   case IS_CYLINDER: case IS_CYL_SECTOR: {
+      /* src/initial_space.cc:576-583, 638-645 */
+      double z = next_uniform(T), phi;
+      v3 ry = V(q->a[0], q->a[1], q->a[2]);
+      if (q->kind == IS_CYLINDER) phi = M_2PI_ * next_uniform(T);
+      else phi = q->a[3] + (q->a[4] - q->a[3]) * next_uniform(T);
+      return vadd(vadd(vadd(q->v0, vscale(cos(phi), q->v2)), vscale(sin(phi), ry)), vscale(z, q->v1));
+   }
    case IS_EQ_BAND: {
       double L = q->a[1] + (q->a[2] - q->a[1]) * next_uniform(T);
       double phi = M_2PI_ * next_uniform(T);
@@ -1685,7 +1720,8 @@ static int parker_slopes(trj_t* T, v3* sp, v3* sm, double* sa)
    *sp = fwd(T) ? vadd(T->drift_vel, T->divK) : vsub(T->drift_vel, T->divK);
    *sm = V(-T->mom.x[0] * sd_divU(&T->sp) / 3.0, 0.0, 0.0);
    *sa = 0.0;
-   if (T->o->traj_type == 207 && T->pb->has_src) {
+   if (T->o->traj_type == 207 && T->pb->has_src && T->pb->src_kind == 1) *sa = T->pb->src_rate;  /* SourceConstant */
+   else if (T->o->traj_type == 207 && T->pb->has_src) {
       /* TrajectoryParkerSource::Slopes -> SourceMomentumInjection::EvaluateSource
        * (src/trajectory_parker_source.cc:58-66, src/source_other.cc:113-119): a crossing of
        * p_inj since the previous step start gives rate / dt, with dt still the previous step's */

@@ -42,7 +42,7 @@ enum BndKind : int {
 
 enum IniKind : int {
    kItFixed = 1, kItInterval,
-   kIsFixed = 10, kIsLine, kIsCircle, kIsBox, kIsSphere, kIsSphereSector, kIsRankine,
+   kIsFixed = 10, kIsLine, kIsCircle, kIsBox, kIsSphere, kIsSphereSector, kIsRankine, kIsCylinder, kIsCylinderSector,
    kImFixed = 30, kImBeam, kImRing, kImShell, kImThickShell, kImMaxwell,
    kImLogEnergyPitchBand = 40, kIsEquatorialBand = 41
 };

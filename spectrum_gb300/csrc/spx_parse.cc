@@ -303,6 +303,23 @@ int parse_initial(Reader& r, int kind, int traj, IniParams& q)
       q.a[2] = (2.0 * q.a[0] * q.a[0] - q.a[1] * q.a[1]) / (q.a[1] * q.a[1]);
       break;
    case kIsEquatorialBand: r.v3(q.v0); q.a[0] = r.d(); q.a[1] = r.d(); q.a[2] = r.d(); break;
+   case kIsCylinder: case kIsCylinderSector: {
+      // InitialSpaceCylinder(Sector)::SetupInitial (src/initial_space.cc:561-570, 621-631): origin, height
+      // vector, radius vector x; radius vector y = unit(height) x radius x; the sector's azimuth range
+      // clamped to [phi1, min(phi2, 2 pi)]
+      r.v3(q.v0); r.v3(q.v1); r.v3(q.v2);
+      double h[3] = {q.v1[0], q.v1[1], q.v1[2]}, ry[3];
+      normalize(h);
+      cross(h, q.v2, ry);
+      q.a[0] = ry[0]; q.a[1] = ry[1]; q.a[2] = ry[2];
+      if (kind == kIsCylinderSector) {
+         q.a[3] = r.d();
+         q.a[4] = r.d();
+         if (q.a[4] > 6.283185307179586476925286766559) q.a[4] = 6.283185307179586476925286766559;
+         if (q.a[4] < q.a[3]) q.a[4] = q.a[3];
+      }
+      break;
+   }
    case kImFixed:  // only compiled for Lorentz (src/initial_momentum.hh:21)
       if (traj != kLorentz) return SPX_ERR_UNKNOWN_PLUGIN;
       r.v3(q.v0);
@@ -394,10 +411,12 @@ int parse_plugin(ProblemDesc& pd, int traj, int role, int kind, const uint8_t* b
       if (rc == SPX_OK) pd.has_diff = 1;
       return rc;
    }
-   case SPX_ROLE_SOURCE:  // SourceMomentumInjection::SetupSource, src/source_other.cc:98-107
-      if (kind != 2) return SPX_ERR_UNKNOWN_PLUGIN;
-      pd.src.kind = 2;
-      pd.src.p_inj = r.d();
+   case SPX_ROLE_SOURCE:
+      // SourceConstant::SetupSource (src/source_other.cc:41-50): S0; SourceMomentumInjection (:98-107):
+      // the injection momentum and the rate
+      if (kind != 1 && kind != 2) return SPX_ERR_UNKNOWN_PLUGIN;
+      pd.src.kind = kind;
+      if (kind == 2) pd.src.p_inj = r.d();
       pd.src.rate = r.d();
       return r.bad ? SPX_ERR_BAD_BLOB : SPX_OK;
    case SPX_ROLE_BOUNDARY: {

@@ -137,6 +137,13 @@ static __device__ __noinline__ V3<double> sample_pos(InitRng& rng, const Problem
       double phi = two_pi * rng.uniform();
       return v0 + mk(s * cos(phi), s * sin(phi), z);
    }
+   case kIsCylinder: case kIsCylinderSector: {  // src/initial_space.cc:576-583, 638-645
+      double z = rng.uniform(), phi;
+      V3<double> ry = mk(q.a[0], q.a[1], q.a[2]);
+      if (q.kind == kIsCylinder) phi = two_pi * rng.uniform();
+      else phi = q.a[3] + (q.a[4] - q.a[3]) * rng.uniform();
+      return ((v0 + cos(phi) * v2) + sin(phi) * ry) + z * v1;
+   }
    case kIsEquatorialBand: {
       double Lv = q.a[1] + (q.a[2] - q.a[1]) * rng.uniform();
       double phi = two_pi * rng.uniform();
@@ -545,7 +552,8 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, con
    R divU = sd_divU(sp);
    R slope_p = -p * divU / R(3);
    R sa = R(0);
-   if (P.src.kind == 2) {
+   if (P.src.kind == 1) sa = P.src.rate;  // SourceConstant: S0 every step (src/source_other.cc:41-59)
+   else if (P.src.kind == 2) {
       // TrajectoryParkerSource::Slopes / SourceMomentumInjection::EvaluateSource
       // (src/trajectory_parker_source.cc:58-66, src/source_other.cc:113-119); dt is the previous step's
       R del = p - P.src.p_inj;

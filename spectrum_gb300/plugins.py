@@ -254,6 +254,14 @@ class InitialSpaceSphereSector(Plugin): pass  # src/initial_space.cc:357-394
 class InitialSpaceRankineHalfBody(Plugin): pass  # src/initial_space.cc:432-463
 
 
+@_plugin(ROLE_INITIAL, 17)
+class InitialSpaceCylinder(Plugin): pass  # src/initial_space.cc:561-583 (origin, height, radius vector)
+
+
+@_plugin(ROLE_INITIAL, 18)
+class InitialSpaceCylinderSector(Plugin): pass  # src/initial_space.cc:621-645 (... and phi1, phi2)
+
+
 @_plugin(ROLE_INITIAL, 30)
 class InitialMomentumFixed(Plugin): pass  # src/initial_momentum.cc:51-98
 

@@ -30,9 +30,10 @@ from spectrum_gb300.plugins import (BackgroundShock, BackgroundSmoothShock, Back
                                     DistributionSpectrumKineticEnergyBentPowerLaw, DistributionTimeUniform,
                                     InitialMomentumBeam, InitialMomentumFixed, InitialMomentumMaxwell,
                                     InitialMomentumRing, InitialMomentumShell, InitialMomentumThickShell,
-                                    InitialSpaceBox, InitialSpaceCircle, InitialSpaceFixed, InitialSpaceLine,
+                                    InitialSpaceBox, InitialSpaceCircle, InitialSpaceCylinder, InitialSpaceCylinderSector,
+                                    InitialSpaceFixed, InitialSpaceLine,
                                     InitialSpaceRankineHalfBody, InitialSpaceSphere, InitialSpaceSphereSector,
-                                    InitialTimeFixed, InitialTimeInterval, SourceMomentumInjection)
+                                    InitialTimeFixed, InitialTimeInterval, SourceConstant, SourceMomentumInjection)
 from spectrum_gb300.problem import (BACKWARD, FORWARD, TRAJ_FOCUSED, TRAJ_GUIDING_SCATT, TRAJ_LORENTZ, TRAJ_PARKER,
                                     TRAJ_PARKER_SOURCE, Problem, distro_header)
 
@@ -144,6 +145,9 @@ INITIAL_CASES = {
     "space_sector": {"is_": (InitialSpaceSphereSector(), DC().vec((0, 0, 0)).double(0.3).double(0.5).double(1.2)
                              .double(0.3).double(2.0))},
     "space_rankine": {"is_": (InitialSpaceRankineHalfBody(), DC().vec((0, 0, 0)).double(0.2).double(0.5))},
+    "space_cylinder": {"is_": (InitialSpaceCylinder(), DC().vec((0.1, 0, 0)).vec((0, 0.2, 0.3)).vec((0.3, 0, 0)))},
+    "space_cylinder_sector": {"is_": (InitialSpaceCylinderSector(), DC().vec((0.1, 0, 0)).vec((0, 0.2, 0.3))
+                                      .vec((0.3, 0, 0)).double(0.5).double(2.5))},
     "momentum_thick_shell_lin": {"im": (InitialMomentumThickShell(), DC().double(0.5).double(2.0).bool(False))},
     "momentum_thick_shell_log": {"im": (InitialMomentumThickShell(), DC().double(0.5).double(2.0).bool(True))},
     "momentum_maxwell": {"im": (InitialMomentumMaxwell(), DC().double(1.0).double(0.3).double(0.2))},
@@ -288,3 +292,13 @@ def test_parker_source_injection():
                  im=(InitialMomentumShell(), DC().double(0.95)), t_end=-0.2, n=16)
     r = _same(pb)
     assert (r.traj["amp"] != 0.0).sum() >= 4  # momenta rise through p_inj = 1 and the source injects
+
+
+def test_parker_source_constant():
+    """TrajectoryParkerSource with SourceConstant: the amplitude grows by S0 dt exp(weight) every step."""
+    src = (SourceConstant(), DC().double(0.7))
+    pb = _parker(traj=TRAJ_PARKER_SOURCE, flow=BACKWARD, src=src, t_end=-0.05, n=12)
+    r = _same(pb)
+    # the time boundary ends the run a few 1e-8 past |t| = 0.05, as the reference's proximity check does
+    np.testing.assert_allclose(r.traj["amp"], 0.7 * np.abs(r.traj["t"]), rtol=1e-12)
+
