@@ -266,10 +266,12 @@ typedef struct {
 typedef struct {
    uint64_t seed;
    uint32_t n_traj, problem;
-   int has_bg, has_diff, has_src, src_kind;  /* src_kind 1 SourceConstant, 2 SourceMomentumInjection */
+   int has_bg, has_diff, has_src, src_kind;  /* src_kind 1 SourceConstant, 2 SourceMomentumInjection,
+                                                3 SourceSphericalShockInjection */
    bg_t bg;
    df_t df;
-   double src_p_inj, src_rate;
+   double src_p_inj, src_rate, src_r_sh, src_w_sh;
+   v3 src_r0;
    int nbt, nbs, nbm;
    bnd_t bt[MAXB], bs[MAXB], bm[MAXB];
    ini_t it, is, im;
@@ -570,7 +572,7 @@ static int kind_of(uint32_t role, const char* nm, size_t nl)
       K("DiffusionPotgieterEtAl2015", DF_POTGIETER) K("DiffusionEmpiricalSOQLTandUNLT", DF_EMPIRICAL)
    }
    else if (role == 2) {
-      K("SourceConstant", 1) K("SourceMomentumInjection", 2)
+      K("SourceConstant", 1) K("SourceMomentumInjection", 2) K("SourceSphericalShockInjection", 3)
    }
    else if (role == 3) {
       K("BoundaryTimeExpire", BT_TIME) K("BoundaryTimePass", BT_TIME_PASS) K("BoundaryTimeRecurrent", BT_TIME_REC)
@@ -644,7 +646,11 @@ static int parse_spec(const uint8_t* s, size_t n, prob_t* pb, char* err, size_t 
           * and the rate (:98-107) */
          pb->src_kind = kind;
          if (kind == 1) pb->src_rate = rd_d(&r);
-         else { pb->src_p_inj = rd_d(&r); pb->src_rate = rd_d(&r); }
+         else if (kind == 2) { pb->src_p_inj = rd_d(&r); pb->src_rate = rd_d(&r); }
+         else {  /* SourceSphericalShockInjection::SetupSource, src/source_other.cc:150-160 */
+            pb->src_p_inj = rd_d(&r); pb->src_r0 = rd_v(&r); pb->src_r_sh = rd_d(&r); pb->src_w_sh = rd_d(&r);
+            pb->src_rate = rd_d(&r);
+         }
          pb->has_src = 1;
       }
       else if (role == 3) {
@@ -1726,7 +1732,14 @@ static int parker_slopes(trj_t* T, v3* sp, v3* sm, double* sa)
        * (src/trajectory_parker_source.cc:58-66, src/source_other.cc:113-119): a crossing of
        * p_inj since the previous step start gives rate / dt, with dt still the previous step's */
       double del = T->mom.x[0] - T->pb->src_p_inj;
-      if (del * T->src_del_old < 0.0) *sa = T->pb->src_rate / T->dt;
+      if (del * T->src_del_old < 0.0) {
+         if (T->pb->src_kind == 2) *sa = T->pb->src_rate / T->dt;
+         else {
+            /* SourceSphericalShockInjection::EvaluateSource (src/source_other.cc:166-177): only in the shell */
+            double r = vnorm(vsub(T->pos, T->pb->src_r0));
+            if (T->pb->src_r_sh <= r && r <= T->pb->src_r_sh + T->pb->src_w_sh) *sa = T->pb->src_rate / T->dt;
+         }
+      }
       T->src_del_old = del;
    }
    return 0;

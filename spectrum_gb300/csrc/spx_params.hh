@@ -80,8 +80,9 @@ struct DiffParamsT {
 
 template <class R>
 struct SrcParamsT {
-   int kind;                  // 0 none, 2 momentum injection
+   int kind;                  // 0 none, 1 constant, 2 momentum injection, 3 momentum injection in a spherical shell
    R p_inj, rate;
+   R r0[3], r_sh, w_sh;       // the shell of kind 3
 };
 
 template <class R>

@@ -414,9 +414,11 @@ int parse_plugin(ProblemDesc& pd, int traj, int role, int kind, const uint8_t* b
    case SPX_ROLE_SOURCE:
       // SourceConstant::SetupSource (src/source_other.cc:41-50): S0; SourceMomentumInjection (:98-107):
       // the injection momentum and the rate
-      if (kind != 1 && kind != 2) return SPX_ERR_UNKNOWN_PLUGIN;
+      // SourceSphericalShockInjection (:150-160): p_inj, the shell's centre, radius and width, the rate
+      if (kind < 1 || kind > 3) return SPX_ERR_UNKNOWN_PLUGIN;
       pd.src.kind = kind;
-      if (kind == 2) pd.src.p_inj = r.d();
+      if (kind >= 2) pd.src.p_inj = r.d();
+      if (kind == 3) { r.v3(pd.src.r0); pd.src.r_sh = r.d(); pd.src.w_sh = r.d(); }
       pd.src.rate = r.d();
       return r.bad ? SPX_ERR_BAD_BLOB : SPX_OK;
    case SPX_ROLE_BOUNDARY: {
@@ -526,6 +528,7 @@ void convert_problem(const ProblemDesc& s, ProblemDescT<R>& d)
 
    d.df.kind = s.df.kind; d.df.i0 = s.df.i0; d.df.i1 = s.df.i1; cp(s.df.a, d.df.a);
    d.src.kind = s.src.kind; d.src.p_inj = (R)s.src.p_inj; d.src.rate = (R)s.src.rate;
+   cp(s.src.r0, d.src.r0); d.src.r_sh = (R)s.src.r_sh; d.src.w_sh = (R)s.src.w_sh;
 
    auto ini = [](const IniParams& x, IniParamsT<R>& y) {
       y.kind = x.kind; y.n_int = x.n_int; y.flag = x.flag;

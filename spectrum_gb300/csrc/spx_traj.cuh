@@ -553,11 +553,18 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, con
    R slope_p = -p * divU / R(3);
    R sa = R(0);
    if (P.src.kind == 1) sa = P.src.rate;  // SourceConstant: S0 every step (src/source_other.cc:41-59)
-   else if (P.src.kind == 2) {
+   else if (P.src.kind >= 2) {
       // TrajectoryParkerSource::Slopes / SourceMomentumInjection::EvaluateSource
-      // (src/trajectory_parker_source.cc:58-66, src/source_other.cc:113-119); dt is the previous step's
+      // (src/trajectory_parker_source.cc:58-66, src/source_other.cc:113-119); dt is the previous step's.
+      // SourceSphericalShockInjection (:166-177) injects only inside the shell r_sh <= |r - r0| <= r_sh + w_sh.
       R del = p - P.src.p_inj;
-      if (del * L.src_del_old < R(0)) sa = P.src.rate / L.dt;
+      if (del * L.src_del_old < R(0)) {
+         if (P.src.kind == 2) sa = P.src.rate / L.dt;
+         else {
+            R r = norm(pos - ld3(P.src.r0));
+            if (P.src.r_sh <= r && r <= P.src.r_sh + P.src.w_sh) sa = P.src.rate / L.dt;
+         }
+      }
       L.src_del_old = del;
    }
    // PhysicalStep (src/trajectory_parker.cc:212-221)
@@ -995,7 +1002,7 @@ __device__ __noinline__ void set_start(Lane<R, A>& L, BndView<R> bv, Start& s0, 
       bv.st(j, st);
    }
    // TrajectoryParkerSource::SetStart (src/trajectory_parker_source.cc:43-50)
-   if (P.src.kind == 2) L.src_del_old = mr.x - P.src.p_inj;
+   if (P.src.kind >= 2) L.src_del_old = mr.x - P.src.p_inj;
 }
 
 // ---- the kernel --------------------------------------------------------------------------------

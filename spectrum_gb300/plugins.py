@@ -139,6 +139,10 @@ class SourceConstant(Plugin): pass
 class SourceMomentumInjection(Plugin): pass  # src/source_other.cc:113-118
 
 
+@_plugin(ROLE_SOURCE, 3)
+class SourceSphericalShockInjection(Plugin): pass  # src/source_other.cc:150-177 (p_inj, r0, r_sh, w_sh, rate)
+
+
 # -- boundaries (src/boundary_*.hh) ------------------------------------------------------------
 @_plugin(ROLE_BOUNDARY, 1)
 class BoundaryTimeExpire(Plugin): pass  # src/boundary_time.cc:70-118

@@ -43,6 +43,7 @@ def _problems():
         dist=(cases.DistributionDivergenceFlowPowerLaw(),
               cases.distro_header(DC(), (10, 0, 0), (0.0, 0, 0), (2.0, 0, 0)).double(2.0).double(1.5).double(0.0)))
     out["parker_source"] = _source_case
+    out["parker_source_spherical"] = cases._spherical_source_problem
     out["parker_source_constant"] = lambda: cases._parker(
         traj=cases.TRAJ_PARKER_SOURCE, flow=cases.BACKWARD, src=(cases.SourceConstant(), DC().double(0.7)),
         t_end=-0.05, n=12)

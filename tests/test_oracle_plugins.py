@@ -33,7 +33,8 @@ from spectrum_gb300.plugins import (BackgroundShock, BackgroundSmoothShock, Back
                                     InitialSpaceBox, InitialSpaceCircle, InitialSpaceCylinder, InitialSpaceCylinderSector,
                                     InitialSpaceFixed, InitialSpaceLine,
                                     InitialSpaceRankineHalfBody, InitialSpaceSphere, InitialSpaceSphereSector,
-                                    InitialTimeFixed, InitialTimeInterval, SourceConstant, SourceMomentumInjection)
+                                    InitialTimeFixed, InitialTimeInterval, SourceConstant, SourceMomentumInjection,
+                                    SourceSphericalShockInjection)
 from spectrum_gb300.problem import (BACKWARD, FORWARD, TRAJ_FOCUSED, TRAJ_GUIDING_SCATT, TRAJ_LORENTZ, TRAJ_PARKER,
                                     TRAJ_PARKER_SOURCE, Problem, distro_header)
 
@@ -301,4 +302,19 @@ def test_parker_source_constant():
     r = _same(pb)
     # the time boundary ends the run a few 1e-8 past |t| = 0.05, as the reference's proximity check does
     np.testing.assert_allclose(r.traj["amp"], 0.7 * np.abs(r.traj["t"]), rtol=1e-12)
+
+
+def _spherical_source_problem():
+    src = (SourceSphericalShockInjection(), DC().double(1.0).vec((0, 0, 0)).double(0.0).double(0.2).double(2.0))
+    c = distro_header(DC(), (10, 0, 0), (0.5, 0, 0), (2.0, 0, 0))
+    dist = (DistributionMomentumUniform(), c.double(1.0).double(0.0).int(1).int(0))
+    return _parker(traj=TRAJ_PARKER_SOURCE, flow=BACKWARD, bg=_shock(), src=src, dist=dist,
+                   im=(InitialMomentumShell(), DC().double(0.95)), t_end=-0.2, n=24)
+
+
+def test_parker_source_spherical_shell_injection():
+    """SourceSphericalShockInjection: injection at p_inj only within 0.2 of the origin."""
+    r = _same(_spherical_source_problem())
+    injected = (r.traj["amp"] != 0.0).sum()
+    assert 0 < injected < len(r.traj), injected  # both sides of the shell condition
 
