@@ -297,6 +297,24 @@ public:
             check(spx_dump_distribution(ctx_, p, d, DistroPath(d, p).c_str()), "DumpDistro");
    }
 
+   // The records of a distribution whose container set keep_records (DistributionTemplated::AddRecord):
+   // values (3 per event) and weights (width per event), at most SPX_OPT_RECORD_CAPACITY of them.
+   int64_t DistributionRecords(int distro, std::vector<double>& values, std::vector<double>& weights, int problem = 0) const
+   {
+      int64_t nb = 0, total = 0;
+      int w = 0;
+      check(spx_get_distribution_info(ctx_, problem, distro, &nb, &w), "DistributionRecords");
+      int64_t k = spx_get_distribution_records(ctx_, problem, distro, nullptr, nullptr, 0, &total);
+      if (k < 0) check((int)k, "DistributionRecords");
+      values.assign(3 * (size_t)total, 0.0);
+      weights.assign((size_t)w * total, 0.0);
+      k = spx_get_distribution_records(ctx_, problem, distro, values.data(), weights.data(), total, &total);
+      if (k < 0) check((int)k, "DistributionRecords");
+      values.resize(3 * (size_t)k);
+      weights.resize((size_t)w * k);
+      return k;
+   }
+
    // Bin index, count and mean weight per bin of one distribution of one problem (the columns of
    // DistributionTemplated::Print1D, src/distribution_templated.cc:546-590, in code units).
    void PrintDistro1D(int distro, int /*ijk*/, const std::string& file_name, bool /*phys_units*/, int problem = 0) const
