@@ -69,9 +69,9 @@ def test_run_static_matches_run(built_lib, precision):
         sim.close()
 
 
-@pytest.mark.parametrize("precision,n_problems", [(capi.SPX_FP64, 71), (capi.SPX_MIXED, 45)])
+@pytest.mark.parametrize("precision,n_problems", [(capi.SPX_FP64, 70), (capi.SPX_MIXED, 45)])
 def test_run_static_rejects_sizes_beyond_its_array(built_lib, precision, n_problems):
-    """A batch whose descriptors do not fit the fixed array (70 problems in FP64, 44 in mixed
+    """A batch whose descriptors do not fit the fixed array (69 problems in FP64, 44 in mixed
     precision) is refused before anything runs."""
     torch = pytest.importorskip("torch")
     pbs = workloads.gcr_modulation(n_traj=4, energies_mev=workloads.modulation_energies(n=n_problems),
