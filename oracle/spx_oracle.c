@@ -1855,11 +1855,12 @@ static void focused_drift(trj_t* T)
 {
    double ct2 = T->mom.x[1] * T->mom.x[1], st2 = 1.0 - ct2;
    const spdata* s = &T->sp;
+   /* the operations in the reference's order: ((0.5 st2) (b x grad B)) / B, and ((0.5 st2) b) (B . curl B) */
    v3 bxg = vcross(s->bhat, s->gradBmag);
-   v3 dv = vscale(0.5 * st2, vdiv(bxg, s->Bmag));
+   v3 dv = vdiv(vscale(0.5 * st2, bxg), s->Bmag);
    v3 curlB = sd_curlB(s);
    v3 bgb = vmmul(s->B, &s->gradB);
-   v3 cur = vadd(vscale(0.5 * st2 * vdot(s->B, curlB), s->bhat), vscale(ct2, vcross(s->bhat, bgb)));
+   v3 cur = vadd(vscale(vdot(s->B, curlB), vscale(0.5 * st2, s->bhat)), vscale(ct2, vcross(s->bhat, bgb)));
    dv = vadd(dv, vdiv(cur, s->Bmag * s->Bmag));
    dv = vscale(larmor(T->mom.x[0], s->Bmag) * T->vel.x[0], dv);
    T->drift_vel = vadd(dv, vadd(s->U, vscale(T->vel.x[0] * T->mom.x[1], s->bhat)));
@@ -1874,8 +1875,14 @@ static void focused_slopes(trj_t* T, v3* sp, v3* sm)
    focused_drift(T);
    *sp = T->drift_vel;
    st2 = 1.0 - T->mom.x[1] * T->mom.x[1];
-   for (i = 0; i < 3; i++)
-      for (j = 0; j < 3; j++) bbgu += s->bhat.x[i] * s->bhat.x[j] * s->gradU.m[i][j];
+   /* bb : grad U as GeoMatrix::operator% sums it: row by row, each row a dot product
+    * (common/matrix.hh:556-561) */
+   for (i = 0; i < 3; i++) {
+      double row = 0.0;
+      for (j = 0; j < 3; j++) row = (j == 0) ? s->bhat.x[i] * s->bhat.x[j] * s->gradU.m[i][j]
+                                             : row + s->bhat.x[i] * s->bhat.x[j] * s->gradU.m[i][j];
+      bbgu += row;
+   }
    cd = vadd(s->dUdt, vmmul(s->U, &s->gradU));
    bcd = 2.0 * vdot(s->bhat, cd) / T->vel.x[0];
    divU = sd_divU(s);

@@ -634,9 +634,10 @@ __device__ __forceinline__ V3<R> vel_load(V3<R> mom)
 template <class R>
 __device__ __forceinline__ V3<R> focused_drift(const SD<R>& s, V3<R> mom, V3<R> vel)
 {
+   // the operations in the reference's order: ((0.5 st2) (b x grad B)) / B and ((0.5 st2) b) (B . curl B)
    R ct2 = mom.y * mom.y, st2 = R(1) - ct2;
-   V3<R> dv = (R(0.5) * st2) * (cross(s.bhat, s.gradBmag) / s.Bmag);
-   V3<R> cur = (R(0.5) * st2 * dot(s.B, sd_curlB(s))) * s.bhat + ct2 * cross(s.bhat, vm(s.B, s.gradB));
+   V3<R> dv = ((R(0.5) * st2) * cross(s.bhat, s.gradBmag)) / s.Bmag;
+   V3<R> cur = dot(s.B, sd_curlB(s)) * ((R(0.5) * st2) * s.bhat) + ct2 * cross(s.bhat, vm(s.B, s.gradB));
    dv = dv + cur / (s.Bmag * s.Bmag);
    dv = (larmor(mom.x, s.Bmag) * vel.x) * dv;
    return dv + (s.U + (vel.x * mom.y) * s.bhat);
@@ -697,11 +698,12 @@ __device__ __forceinline__ void rk_slopes(const SD<R>& s, V3<R> mom, V3<R> vel, 
    else {  // src/trajectory_focused.cc:100-128
       drift = focused_drift(s, mom, vel);
       sp = drift;
+      // bb : grad U as GeoMatrix::operator% sums it, row by row (common/matrix.hh:556-561)
       R st2 = R(1) - mom.y * mom.y, bbgu = R(0);
 #pragma unroll
       for (int i = 0; i < 3; i++)
-#pragma unroll
-         for (int j = 0; j < 3; j++) bbgu += s.bhat[i] * s.bhat[j] * s.gradU.m[i][j];
+         bbgu += (s.bhat[i] * s.bhat[0] * s.gradU.m[i][0] + s.bhat[i] * s.bhat[1] * s.gradU.m[i][1]) +
+                 s.bhat[i] * s.bhat[2] * s.gradU.m[i][2];
       V3<R> cd = s.dUdt + vm(s.U, s.gradU);
       R bcd = R(2) * dot(s.bhat, cd) / vel.x;
       R divU = sd_divU(s);

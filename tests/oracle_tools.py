@@ -180,7 +180,9 @@ def oracle_uniforms(seed, index, traj, problem=0, attempt=0):
 REF_VARIANTS = {(206, 0, 0): "parker_fwd_rk0", (206, 1, 0): "parker_bwd_rk0", (207, 1, 0): "parkersrc_bwd_rk0",
                 (200, 0, 25): "lorentz_fwd_rk25", (205, 0, 25): "focused_fwd_rk25",
                 (201, 0, 25): "guiding_fwd_rk25", (202, 0, 25): "guidingscatt_fwd_rk25",
-                (203, 0, 25): "guidingdiff_fwd_rk25", (204, 0, 25): "guidingdiffscatt_fwd_rk25"}
+                (203, 0, 25): "guidingdiff_fwd_rk25", (204, 0, 25): "guidingdiffscatt_fwd_rk25",
+                (200, 1, 25): "lorentz_bwd_rk25", (205, 1, 25): "focused_bwd_rk25", (204, 1, 25): "guidingdiffscatt_bwd_rk25",
+                (207, 0, 0): "parkersrc_fwd_rk0"}
 
 
 def ref_binary(problem) -> str | None:

@@ -23,7 +23,8 @@ from spectrum_gb300.plugins import (BackgroundShock, BackgroundSmoothShock, Back
                                     BoundarySphereReflect, BoundaryTimeExpire, BoundaryTimePass, BoundaryTimeRecurrent,
                                     DiffusionEmpiricalSOQLTandUNLT, DiffusionFlowMomentumPowerLaw, DiffusionFullConstant,
                                     DiffusionKineticEnergyRadialDistancePowerLaw, DiffusionParaConstant,
-                                    DiffusionPotgieterEtAl2015, DiffusionQLTConstant, DiffusionStraussEtAl2013,
+                                    DiffusionPerpConstant, DiffusionPotgieterEtAl2015, DiffusionQLTConstant,
+                                    DiffusionStraussEtAl2013,
                                     DistributionDivergenceFlowPowerLaw, DistributionMomentumUniform,
                                     DistributionPositionCumulativeOrder1, DistributionPositionCumulativeOrder2,
                                     DistributionPositionMomentumUniform, DistributionPositionUniform,
@@ -35,7 +36,8 @@ from spectrum_gb300.plugins import (BackgroundShock, BackgroundSmoothShock, Back
                                     InitialSpaceRankineHalfBody, InitialSpaceSphere, InitialSpaceSphereSector,
                                     InitialTimeFixed, InitialTimeInterval, SourceConstant, SourceMomentumInjection,
                                     SourceSphericalShockInjection)
-from spectrum_gb300.problem import (BACKWARD, FORWARD, TRAJ_FOCUSED, TRAJ_GUIDING_SCATT, TRAJ_LORENTZ, TRAJ_PARKER,
+from spectrum_gb300.problem import (BACKWARD, FORWARD, TRAJ_FOCUSED, TRAJ_GUIDING_DIFF_SCATT, TRAJ_GUIDING_SCATT,
+                                    TRAJ_LORENTZ, TRAJ_PARKER,
                                     TRAJ_PARKER_SOURCE, Problem, distro_header)
 
 pytestmark = pytest.mark.skipif(not os.path.exists(os.path.join(ot.REF_DIR, "ref_guidingdiffscatt_fwd_rk25")),
@@ -317,4 +319,40 @@ def test_parker_source_spherical_shell_injection():
     r = _same(_spherical_source_problem())
     injected = (r.traj["amp"] != 0.0).sum()
     assert 0 < injected < len(r.traj), injected  # both sides of the shell condition
+
+
+# -- backward time for the Runge-Kutta types, forward time for the source type --------------------------
+def _lorentz_backward():
+    pb = _parker(traj=TRAJ_LORENTZ, flow=BACKWARD, diff=False, t_end=-0.1, n=12)
+    pb.options[W.SPX_OPT_STEPS_PER_ORBIT] = 50.0
+    return pb
+
+
+def _focused_backward():
+    au = W.ONE_AU
+    c = distro_header(DC(), (20, 0, 0), (0.5 * au, 0, 0), (1.5 * au, 0, 0))
+    dist = (DistributionPositionUniform(), c.double(1.0).double(0.0).int(1).int(1))
+    return _parker(traj=TRAJ_FOCUSED, flow=BACKWARD, diff=False, bg=_sw_bg(), dist=dist, n=12, t_end=-2000.0,
+                   is_=(InitialSpaceFixed(), DC().vec((au, 0, 0))),
+                   im=(InitialMomentumShell(), DC().double(U.mev_to_mom(10.0))))
+
+
+def _guiding_diff_scatt_backward():
+    return _parker(traj=TRAJ_GUIDING_DIFF_SCATT, flow=BACKWARD, diff=(DiffusionPerpConstant(), DC().double(0.05)),
+                   im=(InitialMomentumShell(), DC().double(U.mev_to_mom(10.0))), t_end=-0.5, n=12)
+
+
+def _parker_source_forward():
+    return _parker(traj=TRAJ_PARKER_SOURCE, flow=FORWARD, src=(SourceConstant(), DC().double(0.3)), t_end=0.05, n=12)
+
+
+TIME_FLOW_CASES = {"lorentz_backward": _lorentz_backward, "focused_backward": _focused_backward,
+                   "guiding_diff_scatt_backward": _guiding_diff_scatt_backward,
+                   "parker_source_forward": _parker_source_forward}
+
+
+@pytest.mark.parametrize("name", sorted(TIME_FLOW_CASES))
+def test_time_flow_variants(name):
+    r = _same(TIME_FLOW_CASES[name]())
+    assert (r.traj["steps"] > 1).all()
 
