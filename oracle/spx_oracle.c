@@ -805,7 +805,10 @@ static void eval_bg(const bg_t* g, double t, v3 pos, unsigned mask, spdata* s, d
       costheta = pp.x[2] / r;
       s->region = V(r < (117.0 * 1.495978707E+13 / 1.0e10) ? 1.0 : -1.0, -1.0, s->region.x[2]);
       ur = g->ur0;
-      if (mask & BG_U) s->U = from_basis(vscale(ur, vunit(pp)), g->eprime);
+      /* D4: U also when only E is asked for (the Lorentz mask), as BackgroundSmoothShock does
+       * (src/background_smooth_shock.cc:148); the reference's solar wind leaves U unset then and forms
+       * E from an uninitialised velocity */
+      if (mask & (BG_U | BG_E)) s->U = from_basis(vscale(ur, vunit(pp)), g->eprime);
       if (mask & BG_B) {
          double sintheta = sqrt(fmax(1.0 - costheta * costheta, 0.0));
          double sr = sqrt(pp.x[0] * pp.x[0] + pp.x[1] * pp.x[1]);

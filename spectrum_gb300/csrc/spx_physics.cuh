@@ -152,7 +152,8 @@ __device__ __forceinline__ void eval_bg(const BgParamsT<R>& g, R t, V3<R> pos, u
       V3<R> pp = eframe_to(g, pos - ld3(g.r0));
       R r = norm(pp), r_mns = r - g.r_ref, costheta = pp.z / r, ur = g.ur0;
       s.region = mk(r < R(117.0 * 1.495978707E+13 / 1.0e10) ? R(1) : R(-1), R(-1), s.region.z);
-      if (mask & kU) s.U = eframe_from(g, ur * unit(pp));
+      // U also when only E is asked for (the Lorentz mask): E = -U x B / c needs it (deviation D4)
+      if (mask & (kU | kE)) s.U = eframe_from(g, ur * unit(pp));
       if (mask & kB) {
          R sintheta = m_sqrt(m_max(R(1) - costheta * costheta, R(0)));
          R sr = m_sqrt(pp.x * pp.x + pp.y * pp.y), cosphi, sinphi;

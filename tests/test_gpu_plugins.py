@@ -44,6 +44,7 @@ def _problems():
               cases.distro_header(DC(), (10, 0, 0), (0.0, 0, 0), (2.0, 0, 0)).double(2.0).double(1.5).double(0.0)))
     out["parker_source"] = _source_case
     out["parker_source_spherical"] = cases._spherical_source_problem
+    out["lorentz_solar_wind"] = _lorentz_solar_wind
     out["parker_source_constant"] = lambda: cases._parker(
         traj=cases.TRAJ_PARKER_SOURCE, flow=cases.BACKWARD, src=(cases.SourceConstant(), DC().double(0.7)),
         t_end=-0.05, n=12)
@@ -97,6 +98,17 @@ def _source_case():
     dist = (cases.DistributionMomentumUniform(), c.double(1.0).double(0.0).int(1).int(0))
     return cases._parker(traj=cases.TRAJ_PARKER_SOURCE, flow=cases.BACKWARD, bg=cases._shock(), src=src, dist=dist,
                          im=(cases.InitialMomentumShell(), DC().double(0.95)), t_end=-0.2, n=16)
+
+
+def _lorentz_solar_wind():
+    """Full orbits in the solar wind, where E = -U x B / c (deviation D4: the reference's solar wind leaves U
+    unset under the Lorentz mask, so this case is checked against the oracle only)."""
+    au = cases.W.ONE_AU
+    c = cases.distro_header(DC(), (20, 0, 0), (0.0, 0, 0), (2.0 * au, 0, 0))
+    dist = (cases.DistributionPositionUniform(), c.double(1.0).double(0.0).int(1).int(1))
+    return cases._parker(traj=cases.TRAJ_LORENTZ, diff=False, bg=cases._sw_bg(), dist=dist, n=24, t_end=2.0,
+                         is_=(cases.InitialSpaceFixed(), DC().vec((au, 0.1 * au, 0.05 * au))),
+                         im=(cases.InitialMomentumShell(), DC().double(cases.U.mev_to_mom(10.0))))
 
 
 PROBLEMS = _problems()

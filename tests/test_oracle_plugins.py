@@ -323,8 +323,9 @@ def test_parker_source_spherical_shell_injection():
 
 # -- backward time for the Runge-Kutta types, forward time for the source type --------------------------
 def _lorentz_backward():
+    # the reference's compiled steps per orbit (src/trajectory_lorentz.hh:26), which its harness runs with
     pb = _parker(traj=TRAJ_LORENTZ, flow=BACKWARD, diff=False, t_end=-0.1, n=12)
-    pb.options[W.SPX_OPT_STEPS_PER_ORBIT] = 50.0
+    pb.options[W.SPX_OPT_STEPS_PER_ORBIT] = 100.0
     return pb
 
 
