@@ -357,3 +357,47 @@ def test_time_flow_variants(name):
     r = _same(TIME_FLOW_CASES[name]())
     assert (r.traj["steps"] > 1).all()
 
+
+# -- more background and trajectory combinations --------------------------------------------------------
+def _dipole_bg():
+    from spectrum_gb300.plugins import BackgroundDipole
+    r_e = W.R_EARTH_CM / U.unit_length
+    b_eq = W.B_EARTH_G / U.unit_magnetic
+    c = DC().double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0.0, 0.0, -b_eq)).double(0.1 * r_e)
+    return (BackgroundDipole(), c.double(r_e).double(0.1)), r_e
+
+
+def _moving_smooth_shock():
+    """A smooth shock moving at 0.5 with an oblique field: dU/dt and grad U both nonzero."""
+    c = DC().double(0.0).vec((0, 0, 0)).vec((1.0, 0, 0)).vec((0.3, 0.2, 1.0)).double(0.02)
+    c.vec((1.0, 0, 0)).double(0.5).double(4.0)
+    return BackgroundSmoothShock(), c.double(0.05).double(0.1)
+
+
+def _combo(name):
+    if name == "parker_dipole":
+        bg, r_e = _dipole_bg()
+        return _parker(bg=bg, diff=(DiffusionFullConstant(), DC().double(1e-4).double(1e-3)), t_end=1.0, n=12,
+                       is_=(InitialSpaceFixed(), DC().vec((3.0 * r_e, 0, 0.1 * r_e))))
+    if name == "parker_backward_smooth_shock":
+        return _parker(bg=_shock(), flow=BACKWARD, diff=(DiffusionFullConstant(), DC().double(0.01).double(0.01)),
+                       t_end=-0.5, n=12)
+    if name == "focused_moving_smooth_shock":
+        return _parker(traj=TRAJ_FOCUSED, bg=_moving_smooth_shock(), diff=False, t_end=0.3, n=12,
+                       is_=(InitialSpaceFixed(), DC().vec((-0.2, 0, 0))))
+    if name == "lorentz_sharp_shock":
+        pb = _parker(traj=TRAJ_LORENTZ, bg=_shock(smooth=False), diff=False, t_end=0.3, n=12,
+                     is_=(InitialSpaceFixed(), DC().vec((-0.05, 0, 0))))
+        pb.options[W.SPX_OPT_STEPS_PER_ORBIT] = 100.0
+        return pb
+    raise KeyError(name)
+
+
+COMBO_CASES = ["focused_moving_smooth_shock", "lorentz_sharp_shock", "parker_backward_smooth_shock", "parker_dipole"]
+
+
+@pytest.mark.parametrize("name", COMBO_CASES)
+def test_background_trajectory_combinations(name):
+    r = _same(_combo(name))
+    assert (r.traj["steps"] > 1).all()
+
