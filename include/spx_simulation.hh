@@ -137,8 +137,11 @@ SPX_PROTOTYPE(DiffusionRigidityMagneticFieldPowerLaw, DiffusionBase, 8)
 SPX_PROTOTYPE(DiffusionStraussEtAl2013, DiffusionBase, 9)
 SPX_PROTOTYPE(DiffusionPotgieterEtAl2015, DiffusionBase, 10)
 SPX_PROTOTYPE(DiffusionEmpiricalSOQLTandUNLT, DiffusionBase, 11)
+SPX_PROTOTYPE(DiffusionWNLTConstant, DiffusionBase, 12)
+SPX_PROTOTYPE(DiffusionWNLTRampVLISM, DiffusionBase, 13)
 SPX_PROTOTYPE(SourceConstant, SourceBase, 1)
 SPX_PROTOTYPE(SourceMomentumInjection, SourceBase, 2)
+SPX_PROTOTYPE(SourceSphericalShockInjection, SourceBase, 3)
 SPX_PROTOTYPE(BoundaryTimeExpire, BoundaryBase, 1)
 SPX_PROTOTYPE(BoundaryTimePass, BoundaryBase, 2)
 SPX_PROTOTYPE(BoundaryTimeRecurrent, BoundaryBase, 3)
@@ -166,6 +169,8 @@ SPX_PROTOTYPE(InitialSpaceBox, InitialBase, 13)
 SPX_PROTOTYPE(InitialSpaceSphere, InitialBase, 14)
 SPX_PROTOTYPE(InitialSpaceSphereSector, InitialBase, 15)
 SPX_PROTOTYPE(InitialSpaceRankineHalfBody, InitialBase, 16)
+SPX_PROTOTYPE(InitialSpaceCylinder, InitialBase, 17)
+SPX_PROTOTYPE(InitialSpaceCylinderSector, InitialBase, 18)
 SPX_PROTOTYPE(InitialMomentumFixed, InitialBase, 30)
 SPX_PROTOTYPE(InitialMomentumBeam, InitialBase, 31)
 SPX_PROTOTYPE(InitialMomentumRing, InitialBase, 32)

@@ -115,6 +115,8 @@ void AddPlugin(Probe& traj, uint32_t role, const std::string& name, const DataCo
 #if (TRAJ_TYPE != TRAJ_PARKER) && (TRAJ_TYPE != TRAJ_PARKER_SOURCE)
       SPX_TRY_DIFF(DiffusionIsotropicConstant)
       SPX_TRY_DIFF(DiffusionQLTConstant)
+      SPX_TRY_DIFF(DiffusionWNLTConstant)
+      SPX_TRY_DIFF(DiffusionWNLTRampVLISM)
 #endif
       SPX_TRY_DIFF(DiffusionParaConstant)
       SPX_TRY_DIFF(DiffusionPerpConstant)

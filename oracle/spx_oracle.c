@@ -218,7 +218,8 @@ typedef struct {
 
 /* the guiding-centre types: Guiding, GuidingScatt, GuidingDiff, GuidingDiffScatt (configure.ac:239-242) */
 #define IS_GC(tt) ((tt) >= 201 && (tt) <= 204)
-enum { DF_ISO = 1, DF_QLT, DF_PARA, DF_PERP, DF_FULL, DF_FLOWMOM, DF_KINRAD, DF_RIGB, DF_STRAUSS, DF_POTGIETER, DF_EMPIRICAL };
+enum { DF_ISO = 1, DF_QLT, DF_PARA, DF_PERP, DF_FULL, DF_FLOWMOM, DF_KINRAD, DF_RIGB, DF_STRAUSS, DF_POTGIETER, DF_EMPIRICAL,
+       DF_WNLT, DF_WNLT_RAMP };
 typedef struct {
    int kind;
    double a[10];
@@ -342,6 +343,14 @@ static void setup_df(df_t* d, rd_t* r, int kind)
    switch (kind) {
    case DF_ISO: case DF_PARA: case DF_PERP: d->a[0] = rd_d(r); break;
    case DF_QLT: for (k = 0; k < 3; k++) d->a[k] = rd_d(r); d->a[3] = M_2PI_ / d->a[1]; d->a[4] = d->a[2] - 1.0; break;
+   case DF_WNLT: case DF_WNLT_RAMP:
+      /* src/diffusion_other.cc:202-208 (A2A, l_max, ps_index as QLT, then A2T, A2L) and :281-295 (l_max_HP,
+       * z_nose, z_sheath) */
+      for (k = 0; k < 3; k++) d->a[k] = rd_d(r);
+      d->a[3] = M_2PI_ / d->a[1]; d->a[4] = d->a[2] - 1.0;
+      d->a[5] = rd_d(r); d->a[6] = rd_d(r);
+      if (kind == DF_WNLT_RAMP) { d->a[7] = rd_d(r); d->a[8] = rd_d(r); d->a[9] = rd_d(r); }
+      break;
    case DF_FULL: d->a[0] = rd_d(r); d->a[1] = rd_d(r); break;
    case DF_FLOWMOM: for (k = 0; k < 6; k++) d->a[k] = rd_d(r); break;
    case DF_KINRAD:
@@ -570,6 +579,7 @@ static int kind_of(uint32_t role, const char* nm, size_t nl)
       K("DiffusionFlowMomentumPowerLaw", DF_FLOWMOM) K("DiffusionKineticEnergyRadialDistancePowerLaw", DF_KINRAD)
       K("DiffusionRigidityMagneticFieldPowerLaw", DF_RIGB) K("DiffusionStraussEtAl2013", DF_STRAUSS)
       K("DiffusionPotgieterEtAl2015", DF_POTGIETER) K("DiffusionEmpiricalSOQLTandUNLT", DF_EMPIRICAL)
+      K("DiffusionWNLTConstant", DF_WNLT) K("DiffusionWNLTRampVLISM", DF_WNLT_RAMP)
    }
    else if (role == 2) {
       K("SourceConstant", 1) K("SourceMomentumInjection", 2) K("SourceSphericalShockInjection", 3)
@@ -1110,6 +1120,20 @@ typedef struct {
    double vmag, mu, st2, Omega;
 } dstate;
 
+/* DiffusionWNLTRampVLISM::EvaluateDiffusion (src/diffusion_other.cc:301-324): the largest turbulent scale grows
+ * linearly from l_max_HP at the heliopause nose to l_max at the sheath, on the Rankine half body through "pos";
+ * the three variances scale with (k_min_ref / k_min)^(ps_index - 1). Beyond the sheath the constant values. */
+static void wnlt_ramp(const df_t* d, v3 pos, double* kmin, double* a2a, double* a2t, double* a2l)
+{
+   double r0 = vnorm(pos), z0 = sqrt(0.5 * r0 * (r0 + pos.x[2])), k_ratio;
+   if (z0 > d->a[9]) return;
+   *kmin = M_2PI_ / (d->a[7] + (d->a[1] - d->a[7]) * (z0 - d->a[8]) / (d->a[9] - d->a[8]));
+   k_ratio = pow(d->a[3] / *kmin, d->a[4]);
+   *a2a = d->a[0] * k_ratio;
+   *a2t = d->a[5] * k_ratio;
+   *a2l = d->a[6] * k_ratio;
+}
+
 static void eval_diff(const df_t* d, int comp, double t, v3 pos, v3 mom, const spdata* s, dstate* st)
 {
    double* K = st->K;
@@ -1124,6 +1148,22 @@ static void eval_diff(const df_t* d, int comp, double t, v3 pos, v3 mom, const s
       if (comp == 0 || comp == 1) return;
       K[2] = 0.25 * M_PI_ * d->a[4] * fabs(st->Omega) * st->st2 * pow(st->vmag * d->a[3] * fabs(st->mu / st->Omega), d->a[4]) * d->a[0];
       break;
+   case DF_WNLT: case DF_WNLT_RAMP: {
+      /* DiffusionWNLTConstant::EvaluateDiffusion (src/diffusion_other.cc:215-243). The reference defines
+       * USE_QLT_SCATT_WITH_WNLT_DIFF (src/diffusion_other.hh:137), so after K_perp the pitch-angle component is the
+       * QLT one and the hypergeometric correction is never reached. */
+      double kmin = d->a[3], a2a = d->a[0], a2t = d->a[5], a2l = d->a[6], ct, cl, q;
+      if (comp == 1) return;
+      if (d->kind == DF_WNLT_RAMP) wnlt_ramp(d, pos, &kmin, &a2a, &a2t, &a2l);
+      q = st->mu / kmin;
+      ct = 0.5 * d->a[4] / (d->a[2] + 1.0) * (q * q) * a2t;
+      q = st->vmag * st->st2 / st->Omega;
+      cl = 0.125 * (q * q) * a2l;
+      K[0] = st->vmag * sqrt(ct + cl);
+      if (comp == 0) return;
+      K[2] = 0.25 * M_PI_ * d->a[4] * fabs(st->Omega) * st->st2 * pow(st->vmag * kmin * fabs(st->mu / st->Omega), d->a[4]) * a2a;
+      break;
+   }
    case DF_PARA: if (comp == 0 || comp == 2) return; K[1] = d->a[0]; break;
    case DF_PERP: if (comp == 1 || comp == 2) return; K[0] = d->a[0]; break;
    case DF_FULL: if (comp == 2) return; K[0] = d->a[0]; K[1] = d->a[1]; break;
@@ -1253,7 +1293,7 @@ static double mu_derivative(trj_t* T, int comp, double t, v3 pos, v3 mom, const 
    const df_t* d = &T->pb->df;
    if (d->kind == DF_ISO) return -2.0 * d->a[0] * st->mu;
    if (d->kind == DF_PARA || d->kind == DF_PERP || d->kind == DF_FULL || d->kind == DF_FLOWMOM ||
-       d->kind == DF_KINRAD || d->kind == DF_RIGB || d->kind >= DF_STRAUSS) return 0.0;
+       d->kind == DF_KINRAD || d->kind == DF_RIGB || (d->kind >= DF_STRAUSS && d->kind <= DF_EMPIRICAL)) return 0.0;
    {
       dstate s2 = *st;
       double dmu = SP_SMALL * (st->mu + SP_SMALL < 1.0 ? 1.0 : -1.0);

@@ -30,7 +30,7 @@ enum BgKind : int { kBgUniform = 1, kBgShock = 2, kBgSmoothShock = 3, kBgDipole 
 
 enum DiffKind : int {
    kDfIsotropic = 1, kDfQLT, kDfPara, kDfPerp, kDfFull, kDfFlowMomentum, kDfKinEnergyRadial, kDfRigidityB,
-   kDfStrauss2013, kDfPotgieter2015, kDfEmpiricalSOQLT
+   kDfStrauss2013, kDfPotgieter2015, kDfEmpiricalSOQLT, kDfWNLT, kDfWNLTRamp
 };
 
 enum BndKind : int {

@@ -161,6 +161,16 @@ int parse_diffusion(Reader& r, int kind, int traj, DiffParams& d)
       d.a[3] = 6.283185307179586476925286766559005768 / d.a[1];
       d.a[4] = d.a[2] - 1.0;
       break;
+   case kDfWNLT: case kDfWNLTRamp:
+      // src/diffusion_other.cc:202-208: the QLT parameters, then A2T, A2L; the ramp adds l_max_HP, z_nose,
+      // z_sheath (:281-295). Neither class is compiled for Parker (src/diffusion_other.hh:126).
+      if (parker) return SPX_ERR_UNKNOWN_PLUGIN;
+      d.a[0] = r.d(); d.a[1] = r.d(); d.a[2] = r.d();
+      d.a[3] = 6.283185307179586476925286766559005768 / d.a[1];
+      d.a[4] = d.a[2] - 1.0;
+      d.a[5] = r.d(); d.a[6] = r.d();
+      if (kind == kDfWNLTRamp) { d.a[7] = r.d(); d.a[8] = r.d(); d.a[9] = r.d(); }
+      break;
    case kDfPara: case kDfPerp: d.a[0] = r.d(); break;
    case kDfFull: d.a[0] = r.d(); d.a[1] = r.d(); break;
    case kDfFlowMomentum: for (int k = 0; k < 6; k++) d.a[k] = r.d(); break;

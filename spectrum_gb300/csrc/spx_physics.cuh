@@ -470,14 +470,37 @@ struct Kap {
    R perp, para;
 };
 
-// The field values the coefficient models read: |B|, U and the region indicators. Passed by value
-// so the coefficient evaluation never takes the address of the lane's field record.
+// The field values the coefficient models read: |B|, U and the region indicators, and for the WNLT models
+// the pitch-angle cosine and the cyclotron frequency (DiffusionBase's mu and Omega, set once per
+// GetComponent and not moved by the spatial difference quotients, src/diffusion_base.cc:105-174). Passed
+// by value so the coefficient evaluation never takes the address of the lane's field record.
 template <class R>
 struct KapIn {
    R Bmag;
    V3<R> U, region;
+   R mu, Omega;
 };
-template <class R> __device__ __forceinline__ KapIn<R> kap_in(const SD<R>& s) { return {s.Bmag, s.U, s.region}; }
+template <class R> __device__ __forceinline__ KapIn<R> kap_in(const SD<R>& s) { return {s.Bmag, s.U, s.region, R(0), R(0)}; }
+template <class R> __device__ __forceinline__ KapIn<R> kap_in(const SD<R>& s, R mu, R Omega)
+{
+   return {s.Bmag, s.U, s.region, mu, Omega};
+}
+
+// DiffusionWNLTRampVLISM::EvaluateDiffusion (src/diffusion_other.cc:301-324): on the Rankine half body
+// through "pos", the largest turbulent scale grows linearly from l_max_HP at the nose (a[8]) to l_max at
+// the sheath (a[9]), and the three variances scale with (k_min_ref / k_min)^(ps_index - 1). Beyond the
+// sheath the constant values stand.
+template <class R>
+__device__ __forceinline__ void wnlt_ramp(const DiffParamsT<R>& d, V3<R> pos, R& kmin, R& a2a, R& a2t, R& a2l)
+{
+   const R r0 = norm(pos), z0 = m_sqrt(R(0.5) * r0 * (r0 + pos.z));
+   if (z0 > d.a[9]) return;
+   kmin = R(6.283185307179586476925286766559005768) / (d.a[7] + (d.a[1] - d.a[7]) * (z0 - d.a[8]) / (d.a[9] - d.a[8]));
+   const R k_ratio = m_pow(d.a[3] / kmin, d.a[4]);
+   a2a = d.a[0] * k_ratio;
+   a2t = d.a[5] * k_ratio;
+   a2l = d.a[6] * k_ratio;
+}
 
 template <class R>
 __device__ __forceinline__ Kap<R> kappa_pp(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const KapIn<R>& s)
@@ -529,32 +552,48 @@ __device__ __forceinline__ Kap<R> kappa_pp(const DiffParamsT<R>& d, V3<R> pos, R
       K.perp = ((lam * vmag / R(3)) * m_cbrt(q * (R(1) + q * q)) * (d.a[3] / s.Bmag)) / damp;
       break;
    }
+   case kDfWNLT: case kDfWNLTRamp: {                          // :215-228, 301-327
+      R kmin = d.a[3], a2a = d.a[0], a2t = d.a[5], a2l = d.a[6];
+      if (d.kind == kDfWNLTRamp) wnlt_ramp(d, pos, kmin, a2a, a2t, a2l);
+      R q = s.mu / kmin;
+      const R ct = R(0.5) * d.a[4] / (d.a[2] + R(1)) * (q * q) * a2t;
+      q = vmag * (R(1) - s.mu * s.mu) / s.Omega;
+      const R cl = R(0.125) * (q * q) * a2l;
+      K.perp = vmag * m_sqrt(ct + cl);
+      break;
+   }
    default: break;
    }
    return K;
 }
 
-// Pitch-angle component D_mumu (Kappa[2]) of the pitch-angle models.
+// Pitch-angle component D_mumu (Kappa[2]) of the pitch-angle models at "pos". The WNLT models give the
+// QLT coefficient, with the ramp's local k_min and A2A: the reference defines
+// USE_QLT_SCATT_WITH_WNLT_DIFF (src/diffusion_other.hh:137), so DiffusionWNLTConstant::EvaluateDiffusion
+// returns before its hypergeometric correction (src/diffusion_other.cc:227-232).
 template <class R>
-__device__ __forceinline__ R kappa_mumu(const DiffParamsT<R>& d, R vmag, R Omega, R mu)
+__device__ __forceinline__ R kappa_mumu(const DiffParamsT<R>& d, V3<R> pos, R vmag, R Omega, R mu)
 {
    R st2 = R(1) - mu * mu;
    if (d.kind == kDfIsotropic) return d.a[0] * st2;  // src/diffusion_other.cc:64-68
-   if (d.kind == kDfQLT)                              // src/diffusion_other.cc:145-149
+   if (d.kind == kDfQLT || d.kind == kDfWNLT || d.kind == kDfWNLTRamp) {  // src/diffusion_other.cc:145-149
+      R kmin = d.a[3], a2a = d.a[0], a2t, a2l;
+      if (d.kind == kDfWNLTRamp) wnlt_ramp(d, pos, kmin, a2a, a2t, a2l);
       return R(0.25) * R(3.141592653589793238462643383279502884) * d.a[4] * m_abs(Omega) * st2 *
-             m_pow(vmag * d.a[3] * m_abs(mu / Omega), d.a[4]) * d.a[0];
+             m_pow(vmag * kmin * m_abs(mu / Omega), d.a[4]) * a2a;
+   }
    return R(0);
 }
 
 // d D_mumu / d mu: analytic for the isotropic model (src/diffusion_other.cc:76-79), else the
 // one-sided difference of DiffusionBase::GetMuDerivative (src/diffusion_base.cc:226-255).
 template <class R>
-__device__ __forceinline__ R kappa_mumu_dmu(const DiffParamsT<R>& d, R vmag, R Omega, R mu, R dmumu)
+__device__ __forceinline__ R kappa_mumu_dmu(const DiffParamsT<R>& d, V3<R> pos, R vmag, R Omega, R mu, R dmumu)
 {
    if (d.kind == kDfIsotropic) return R(-2) * d.a[0] * mu;
-   if (d.kind != kDfQLT) return R(0);
+   if (d.kind != kDfQLT && d.kind != kDfWNLT && d.kind != kDfWNLTRamp) return R(0);
    R dmu = Lim<R>::small * (mu + Lim<R>::small < R(1) ? R(1) : R(-1));
-   return (kappa_mumu(d, vmag, Omega, mu + dmu) - dmumu) / dmu;
+   return (kappa_mumu(d, pos, vmag, Omega, mu + dmu) - dmumu) / dmu;
 }
 
 // Models whose gradient needs no field-gradient matrix (only grad|B| or grad U . U).
@@ -577,11 +616,13 @@ __device__ __noinline__ Kap<R> kappa_pp_call(const DiffParamsT<R>& d, V3<R> pos,
 }
 
 template <class R>
-__device__ __forceinline__ void kappa_grad(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const SD<R>& s, Kap<R> K, V3<R>& gperp,
-                           V3<R>& gpara)
+__device__ __forceinline__ void kappa_grad(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const SD<R>& s, KapIn<R> q, Kap<R> K,
+                                           V3<R>& gperp, V3<R>& gpara)
 {
    switch (d.kind) {
-   case kDfPara: case kDfPerp: case kDfFull:
+   // DiffusionWNLTConstant reads neither the position nor |B| (mu and Omega stay fixed), so the base
+   // class's difference quotient is exactly zero
+   case kDfPara: case kDfPerp: case kDfFull: case kDfWNLT:
       gperp = mk(R(0), R(0), R(0));
       gpara = gperp;
       return;
@@ -613,7 +654,6 @@ __device__ __forceinline__ void kappa_grad(const DiffParamsT<R>& d, V3<R> pos, R
    }
    default: {
       R gpe[3], gpa[3];
-      KapIn<R> q = kap_in(s);
 #pragma unroll
       for (int xyz = 0; xyz < 3; xyz++) {
          R dr = R(0.5) * s.dr[xyz];

@@ -544,7 +544,7 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, con
    else {
       // TRAJ_PARKER_DIVK_METHOD 1 (src/trajectory_parker.cc:120-140)
       V3<R> gpe, gpa;
-      kappa_grad(P.df, pos, p, vmag, sp, K, gpe, gpa);
+      kappa_grad(P.df, pos, p, vmag, sp, kap_in(sp), K, gpe, gpa);
       V3<R> t1 = gpa - gpe;
       divK = (gpe + dot(sp.bhat, t1) * sp.bhat) + (K.para - K.perp) * (sd_divbhat(sp) * sp.bhat + sd_b_gradbhat(sp));
    }
@@ -672,9 +672,10 @@ __device__ __forceinline__ V3<R> guiding_vperp(const DiffParamsT<R>& df, const S
 {
    const R p = m_sqrt(mom.x * mom.x + mom.z * mom.z);  // ConvertMomentum()[0]
    const R vmag = vel_of(p);
-   Kap<R> K = kappa_pp(df, pos, p, vmag, kap_in(s));
+   const KapIn<R> q = kap_in(s, mom.z / norm(mom), cyclotron(vmag, s.Bmag));  // ConvertMomentum()[1], Omega
+   Kap<R> K = kappa_pp(df, pos, p, vmag, q);
    V3<R> gpe, gpa;
-   kappa_grad(df, pos, p, vmag, s, K, gpe, gpa);
+   kappa_grad(df, pos, p, vmag, s, q, K, gpe, gpa);
    fa[2] = s.bhat;
    fa[0] = second_unit(s.bhat);
    fa[1] = cross(fa[2], fa[0]);
@@ -753,8 +754,9 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
       else { pmag = mom.x; mu = mom.y; }
       R vmag = vel_of(pmag);
       R Omega = cyclotron(vmag, sp.Bmag);
-      R Dmumu = kappa_mumu(P.df, vmag, Omega, mu);
-      R Vmu = kappa_mumu_dmu(P.df, vmag, Omega, mu, Dmumu);
+      const V3<R> pos0 = val3<R>(L.pos);
+      R Dmumu = kappa_mumu(P.df, pos0, vmag, Omega, mu);
+      R Vmu = kappa_mumu_dmu(P.df, pos0, vmag, Omega, mu, Dmumu);
       R dtp;
       if (TT == kGuiding) {
          R d1, d2;
@@ -792,7 +794,7 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
          if (cfg.mu_method == 1) {  // MilsteinPitchAngleScatt (:91-130)
             const R b = m_sqrt(R(2) * Dmumu);
             const R dmu = ds * (mu + ds < R(1) ? R(1) : R(-1));
-            const R b1 = (m_sqrt(R(2) * kappa_mumu(P.df, vmag, Omega, mu + dmu)) - b) / dmu;
+            const R b1 = (m_sqrt(R(2) * kappa_mumu(P.df, pos0, vmag, Omega, mu + dmu)) - b) / dmu;
             do {
                normals4<R>(rng_block(P.seed, L.nrm++, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
                const R dw = m_sqrt(L.dt) * n[0];
@@ -809,19 +811,19 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
                mu_new = mu + sd0 * dw;
                mu_new += sv0 * L.dt;
                if (m_abs(mu_new) > R(1)) continue;
-               const R d = kappa_mumu(P.df, vmag, Omega, mu_new);
+               const R d = kappa_mumu(P.df, pos0, vmag, Omega, mu_new);
                R dmu = ds * (mu_new + ds < R(1) ? R(1) : R(-1));
-               sv1 = (kappa_mumu(P.df, vmag, Omega, mu_new + dmu) - d) / dmu;
+               sv1 = (kappa_mumu(P.df, pos0, vmag, Omega, mu_new + dmu) - d) / dmu;
                mu_new = mu + g * sd0 * dw;
                mu_new += sv0 * L.dt;
                if (m_abs(mu_new) > R(1)) continue;
-               sd1 = m_sqrt(R(2) * kappa_mumu(P.df, vmag, Omega, mu_new));
+               sd1 = m_sqrt(R(2) * kappa_mumu(P.df, pos0, vmag, Omega, mu_new));
                mu_new = mu - sd0 / (R(3) * g) * dw;
                mu_new += sv0 * L.dt;
                if (m_abs(mu_new) > R(1)) continue;
-               sd2 = m_sqrt(R(2) * kappa_mumu(P.df, vmag, Omega, mu_new));
+               sd2 = m_sqrt(R(2) * kappa_mumu(P.df, pos0, vmag, Omega, mu_new));
                dmu = ds * (mu + ds < R(1) ? R(1) : R(-1));
-               const R dfit = (m_sqrt(R(2) * kappa_mumu(P.df, vmag, Omega, mu + dmu)) - sd0) / dmu;
+               const R dfit = (m_sqrt(R(2) * kappa_mumu(P.df, pos0, vmag, Omega, mu + dmu)) - sd0) / dmu;
                mu_new = mu + (R(0.5) * sd0 + (sd1 + R(3) * (g * g) * sd2) / (R(2) + R(6) * (g * g))) * dw;
                mu_new += R(0.5) * L.dt * (sv0 + sv1);
                mu_new += R(0.5) * sd0 * dfit * (dw * dw - L.dt);

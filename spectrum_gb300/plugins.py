@@ -130,6 +130,18 @@ class DiffusionPotgieterEtAl2015(Plugin): pass  # src/diffusion_other.cc:968-996
 class DiffusionEmpiricalSOQLTandUNLT(Plugin): pass  # src/diffusion_other.cc:1049-1082
 
 
+@_plugin(ROLE_DIFFUSION, 12)
+class DiffusionWNLTConstant(Plugin):
+    """A2A, l_max, ps_index (as QLT), A2T, A2L (src/diffusion_other.cc:202-243): K_perp from the weakly nonlinear
+    model and the QLT pitch-angle coefficient (USE_QLT_SCATT_WITH_WNLT_DIFF, src/diffusion_other.hh:137)."""
+
+
+@_plugin(ROLE_DIFFUSION, 13)
+class DiffusionWNLTRampVLISM(Plugin):
+    """The WNLT parameters, then l_max_HP, z_nose, z_sheath (src/diffusion_other.cc:281-327): the largest
+    turbulent scale ramps linearly across the heliosheath between two Rankine half bodies."""
+
+
 # -- sources (src/source_other.hh) -------------------------------------------------------------
 @_plugin(ROLE_SOURCE, 1)
 class SourceConstant(Plugin): pass

@@ -35,6 +35,10 @@ def test_bad_set_ups_are_refused(built_lib):
     assert _code(lambda: capi.Context(TRAJ_PARKER, 0, 25, capi.SPX_FP64)) == -1
     # unknown background class: refused when the plugin is added
     assert _code(lambda: _ctx_with(pb, kind_edit=(0, 99))) == -2
+    # the pitch-angle models are not compiled for Parker (src/diffusion_other.hh:17, :126): the QLT and
+    # WNLT classes are refused there
+    for kind in (2, 12, 13):
+        assert _code(lambda: _ctx_with(pb, kind_edit=(1, kind))) == -2
     # parameter blob shorter than the class's list: refused when the plugin is added
     assert _code(lambda: _ctx_with(pb, blob_edit=(0, lambda b: b[: len(b) // 2]))) == -3
     # no time boundary: TrajectoryBase::IsSimmulationReady is false

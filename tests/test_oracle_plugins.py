@@ -16,7 +16,8 @@ import oracle_tools as ot
 from spectrum_gb300 import units as U
 from spectrum_gb300 import workloads as W
 from spectrum_gb300.datacontainer import DataContainer as DC
-from spectrum_gb300.plugins import (BackgroundShock, BackgroundSmoothShock, BackgroundSolarWind, BackgroundUniform,
+from spectrum_gb300.plugins import (BackgroundDipole, BackgroundShock, BackgroundSmoothShock, BackgroundSolarWind,
+                                    BackgroundUniform,
                                     BoundaryBoxReflect, BoundaryCylinderAbsorb, BoundaryMomentumInjectRestrictShell,
                                     BoundaryMomentumInjectRestrictSlab, BoundaryMomentumPass, BoundaryPlanePass,
                                     BoundaryRankineAbsorb, BoundaryRegionAbsorb,
@@ -24,7 +25,7 @@ from spectrum_gb300.plugins import (BackgroundShock, BackgroundSmoothShock, Back
                                     DiffusionEmpiricalSOQLTandUNLT, DiffusionFlowMomentumPowerLaw, DiffusionFullConstant,
                                     DiffusionKineticEnergyRadialDistancePowerLaw, DiffusionParaConstant,
                                     DiffusionPerpConstant, DiffusionPotgieterEtAl2015, DiffusionQLTConstant,
-                                    DiffusionStraussEtAl2013,
+                                    DiffusionStraussEtAl2013, DiffusionWNLTConstant, DiffusionWNLTRampVLISM,
                                     DistributionDivergenceFlowPowerLaw, DistributionMomentumUniform,
                                     DistributionPositionCumulativeOrder1, DistributionPositionCumulativeOrder2,
                                     DistributionPositionMomentumUniform, DistributionPositionUniform,
@@ -36,8 +37,8 @@ from spectrum_gb300.plugins import (BackgroundShock, BackgroundSmoothShock, Back
                                     InitialSpaceRankineHalfBody, InitialSpaceSphere, InitialSpaceSphereSector,
                                     InitialTimeFixed, InitialTimeInterval, SourceConstant, SourceMomentumInjection,
                                     SourceSphericalShockInjection)
-from spectrum_gb300.problem import (BACKWARD, FORWARD, TRAJ_FOCUSED, TRAJ_GUIDING_DIFF_SCATT, TRAJ_GUIDING_SCATT,
-                                    TRAJ_LORENTZ, TRAJ_PARKER,
+from spectrum_gb300.problem import (BACKWARD, FORWARD, TRAJ_FOCUSED, TRAJ_GUIDING_DIFF, TRAJ_GUIDING_DIFF_SCATT,
+                                    TRAJ_GUIDING_SCATT, TRAJ_LORENTZ, TRAJ_PARKER,
                                     TRAJ_PARKER_SOURCE, Problem, distro_header)
 
 pytestmark = pytest.mark.skipif(not os.path.exists(os.path.join(ot.REF_DIR, "ref_guidingdiffscatt_fwd_rk25")),
@@ -400,4 +401,46 @@ COMBO_CASES = ["focused_moving_smooth_shock", "lorentz_sharp_shock", "parker_bac
 def test_background_trajectory_combinations(name):
     r = _same(_combo(name))
     assert (r.traj["steps"] > 1).all()
+
+
+# -- the weakly nonlinear models: K_perp with the QLT pitch-angle coefficient ---------------------------------
+def _wnlt(ramp=False):
+    """A2A 0.1, l_max 1, ps_index 5/3, A2T = A2L = 0.1; the ramp from l_max_HP 0.3 at z_nose 0.1 to the
+    sheath at 0.6, which the trajectories starting at (0.3, 0, 0.2) (z0 = 0.32) cross both ways."""
+    c = DC().double(0.1).double(1.0).double(5.0 / 3.0).double(0.1).double(0.1)
+    if ramp:
+        return DiffusionWNLTRampVLISM(), c.double(0.3).double(0.1).double(0.6)
+    return DiffusionWNLTConstant(), c
+
+
+def _wnlt_problem(traj, ramp, mu_method=0, dipole=False, t_end=0.3):
+    c = distro_header(DC(), (0, 20, 0), (0.0, -1.0, 0), (1.0, 1.0, 1.0))
+    dist = (DistributionMomentumUniform(), c.double(1.0).double(0.0).int(1).int(1))
+    kw = {}
+    if dipole:
+        kw["bg"] = (BackgroundDipole(), DC().double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0, 0, -1.0)).double(0.05)
+                    .double(1.0).double(0.1))
+    pb = _parker(traj=traj, diff=_wnlt(ramp), dist=dist, t_end=t_end, n=12,
+                 is_=(InitialSpaceFixed(), DC().vec((1.5, 0, 0.2) if dipole else (0.3, 0, 0.2))),
+                 im=(InitialMomentumShell(), DC().double(U.mev_to_mom(10.0))), **kw)
+    if mu_method:
+        pb.options[W.SPX_OPT_MU_METHOD] = float(mu_method)
+    return pb
+
+
+WNLT_CASES = {
+    "constant_guiding_diff_scatt": lambda: _wnlt_problem(TRAJ_GUIDING_DIFF_SCATT, False),
+    "constant_guiding_diff_scatt_dipole": lambda: _wnlt_problem(TRAJ_GUIDING_DIFF_SCATT, False, dipole=True),
+    "ramp_guiding_diff_scatt": lambda: _wnlt_problem(TRAJ_GUIDING_DIFF_SCATT, True),
+    "ramp_guiding_diff": lambda: _wnlt_problem(TRAJ_GUIDING_DIFF, True),
+    "ramp_guiding_scatt": lambda: _wnlt_problem(TRAJ_GUIDING_SCATT, True, t_end=1.0),
+    "ramp_guiding_scatt_milstein": lambda: _wnlt_problem(TRAJ_GUIDING_SCATT, True, mu_method=1, t_end=1.0),
+    "ramp_guiding_scatt_rk2": lambda: _wnlt_problem(TRAJ_GUIDING_SCATT, True, mu_method=2, t_end=1.0),
+}
+
+
+@pytest.mark.parametrize("name", sorted(WNLT_CASES))
+def test_wnlt_diffusion(name):
+    r = _same(WNLT_CASES[name]())
+    assert (r.traj["steps"] > 3).all()
 
