@@ -1985,9 +1985,31 @@ static void guiding_diff_coeff(trj_t* T)
    T->v_perp = from_basis(V(vdot(g, fa[0]), vdot(g, fa[1]), 0.0), fa);
 }
 
-/* TrajectoryGuidingDiff::EulerPerpDiffSlopes (src/trajectory_guiding_diff.cc:92-107), STOCHASTIC_METHOD_PERP 0:
- * two normals (the next of the trajectory's count, as for the pitch-angle step) */
-static void guiding_perp_step(trj_t* T)
+/* sqrt(2 D_perp) at a displaced point: CommonFields(t, pos, ...) into a separate record, then GetComponent(0, ...)
+ * (src/trajectory_guiding_diff.cc:152-155). "dmax" receives that evaluation's dmax, which the background's
+ * GetSafeIncr reads for the next increment (src/background_base.cc:409-413). The reference's record there has an
+ * uninitialised field mask; here it takes the trajectory's. */
+static double perp_slope_at(trj_t* T, double t, v3 pos, v3 m, double* dmax)
+{
+   spdata s;
+   dstate st;
+   memset(&st, 0, sizeof st);
+   s = T->sp;
+   if (get_fields(T, t, pos, m, T->sp.mask, &s)) {
+      T->status |= TRAJ_DISCARD;
+      return 0.0;
+   }
+   *dmax = s.dmax;
+   return sqrt(2.0 * get_component(T, 0, t, pos, m, &s, &st));
+}
+
+#define INCR_DMAX_RATIO 0.0001  /* src/background_base.hh:42 */
+
+/* TrajectoryGuidingDiff::EulerPerpDiffSlopes (src/trajectory_guiding_diff.cc:103-122), STOCHASTIC_METHOD_PERP 0:
+ * two normals (the next of the trajectory's count, as for the pitch-angle step). With perp_method 1 the Milstein
+ * terms of MilsteinPerpDiffSlopes (:129-176), with 2 the RK2PerpDiffSlopes stages (:182-300); both draw one uniform
+ * for the sign of the Levy-area stand-in. Returns 1 when an RK2 trial point crosses a terminal boundary. */
+static int guiding_perp_step(trj_t* T)
 {
    dstate st;
    v3 m = convert_mom(T);
@@ -2005,10 +2027,64 @@ static void guiding_perp_step(trj_t* T)
    d = get_component(T, 0, T->t, T->pos, m, &T->sp, &st);
    T->Kperp = d;
    {
-      v3 fa[3];
+      v3 fa[3], xhat, yhat, p;
       int i;
+      const double dt = T->dt, b0 = sqrt(2.0 * d);
+      double dmax = T->sp.dmax, dx, dy, bx, by, dbdx, dbdy, vxy, drx, dry;
       for (i = 0; i < 3; i++) fa[i] = T->fa[i];
-      T->dr_perp = from_basis(V(sqrt(2.0 * d) * dwx, sqrt(2.0 * d) * dwy, 0.0), fa);
+      if (T->o->perp_method != 1 && T->o->perp_method != 2) {
+         T->dr_perp = from_basis(V(b0 * dwx, b0 * dwy, 0.0), fa);
+         return 0;
+      }
+      xhat = from_basis(V(1.0, 0.0, 0.0), fa);
+      yhat = from_basis(V(0.0, 1.0, 0.0), fa);
+      if (T->o->perp_method == 1) {
+         dx = INCR_DMAX_RATIO * dmax;
+         bx = perp_slope_at(T, T->t, vadd(T->pos, vscale(dx, xhat)), m, &dmax);
+         dbdx = (bx - b0) / dx;
+         dy = INCR_DMAX_RATIO * dmax;
+         by = perp_slope_at(T, T->t, vadd(T->pos, vscale(dy, yhat)), m, &dmax);
+         dbdy = (by - b0) / dy;
+         vxy = next_uniform(T) < 0.5 ? dt : -dt;
+         drx = b0 * dwx + 0.5 * b0 * (dbdx * (dwx * dwx - dt) + dbdy * (dwx * dwy - vxy));
+         dry = b0 * dwy + 0.5 * b0 * (dbdy * (dwy * dwy - dt) + dbdx * (dwx * dwy + vxy));
+      }
+      else {
+         const double g = 1.0 / sqrt(3.0);
+         double b1, b2, bxx, byy, bxy, d2x, d2y, d2xy, rx, ry, bmid;
+         v3 dpos = from_basis(V(b0 * dwx, b0 * dwy, 0.0), fa);
+         T->pos = vadd(T->pos, vscale(g, dpos));
+         if (space_terminate(T)) return 1;
+         b1 = perp_slope_at(T, T->t + dt, T->pos, m, &dmax);
+         T->pos = T->local_pos;
+         T->pos = vsub(T->pos, V(dpos.x[0] / (3.0 * g), dpos.x[1] / (3.0 * g), dpos.x[2] / (3.0 * g)));
+         if (space_terminate(T)) return 1;
+         b2 = perp_slope_at(T, T->t + dt, T->pos, m, &dmax);
+         T->pos = T->local_pos;
+         dx = INCR_DMAX_RATIO * dmax;
+         bxx = perp_slope_at(T, T->t, vadd(T->pos, vscale(dx, xhat)), m, &dmax);
+         dx *= 0.5;
+         bx = perp_slope_at(T, T->t, vadd(T->pos, vscale(dx, xhat)), m, &dmax);
+         dbdx = (bx - b0) / dx;
+         d2x = (bxx - 2.0 * bx + b0) / (dx * dx);
+         dy = INCR_DMAX_RATIO * dmax;
+         byy = perp_slope_at(T, T->t, vadd(T->pos, vscale(dy, yhat)), m, &dmax);
+         dy *= 0.5;
+         by = perp_slope_at(T, T->t, vadd(T->pos, vscale(dy, yhat)), m, &dmax);
+         dbdy = (by - b0) / dy;
+         d2y = (byy - 2.0 * by + b0) / (dy * dy);
+         p = vadd(vadd(T->pos, vscale(dx, xhat)), vscale(dy, yhat));
+         bxy = perp_slope_at(T, T->t, p, m, &dmax);
+         d2xy = (bxy - bx - by + b0) / (dx * dy);
+         vxy = next_uniform(T) < 0.5 ? dt : -dt;
+         rx = 0.5 * b0 * (dbdx * (dwx * dwx - dt) + dbdy * (dwx * dwy - vxy)) + dt * (b0 * b0) * (d2y * dwx - d2xy * dwy) / 6.0;
+         ry = 0.5 * b0 * (dbdy * (dwy * dwy - dt) + dbdx * (dwx * dwy + vxy)) + dt * (b0 * b0) * (d2x * dwy - d2xy * dwx) / 6.0;
+         bmid = 0.5 * (b0 + (b1 + 3.0 * (g * g) * b2) / (1.0 + 3.0 * (g * g)));
+         drx = bmid * dwx + rx;
+         dry = bmid * dwy + ry;
+      }
+      T->dr_perp = from_basis(V(drx, dry, 0.0), fa);
+      return 0;
    }
 }
 
@@ -2200,7 +2276,7 @@ static int rk_advance(trj_t* T)
       T->dt = fmin(T->dt_physical, T->dt_adaptive);
       time_proximity(T);
    }
-   if (perp) guiding_perp_step(T);
+   if (perp && guiding_perp_step(T)) return 1;
    /* RKSlopes */
    for (is = 1; is < R->stages; is++) {
       for (il = 0; il < is; il++) {

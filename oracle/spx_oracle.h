@@ -41,6 +41,7 @@ typedef struct {
                               from the previous field evaluation), to compare with the reference's own
                               output; 0: the corrected behaviour the CUDA kernels share */
    int mu_method;          /* guiding-centre pitch-angle step: 0 Euler, 1 Milstein, 2 RK2 (STOCHASTIC_METHOD_MU) */
+   int perp_method;        /* guiding-centre perpendicular step: 0 Euler, 1 Milstein, 2 RK2 (STOCHASTIC_METHOD_PERP) */
 } spx_oracle_opts;
 
 /*

@@ -47,7 +47,7 @@ struct spx_ctx {
    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
    int traj = 0, flow = 0, rk = 0, precision = 0;
    double steps_per_orbit = 100.0;
-   int deriv_mode = 0, pa_scattering = 0, record_final = 0, max_attempts = 100, mu_method = 0;
+   int deriv_mode = 0, pa_scattering = 0, record_final = 0, max_attempts = 100, mu_method = 0, perp_method = 0;
    std::vector<PluginBlob> base;
    std::vector<ProblemHost> problems;
    int bg_kind = 0;
@@ -528,6 +528,13 @@ int spx_set_option(spx_ctx_t c, int option, double value)
          return SPX_ERR_INVALID_ARG;
       c->mu_method = (int)value;
       return SPX_OK;
+   case SPX_OPT_PERP_METHOD:
+      // the perpendicular scheme of the guiding-centre diffusion types (STOCHASTIC_METHOD_PERP)
+      if (value != 0.0 && value != 1.0 && value != 2.0) return SPX_ERR_INVALID_ARG;
+      if (value != 0.0 && c->traj != SPX_TRAJ_GUIDING_DIFF && c->traj != SPX_TRAJ_GUIDING_DIFF_SCATT)
+         return SPX_ERR_INVALID_ARG;
+      c->perp_method = (int)value;
+      return SPX_OK;
    case SPX_OPT_RECORD_CAPACITY:
       // records kept per keep_records distribution; further events are counted, not stored
       if (!(value >= 0.0) || value != (double)(int64_t)value || value > 2147483647.0) return SPX_ERR_INVALID_ARG;
@@ -689,6 +696,7 @@ int spx_run(spx_ctx_t c, const spx_tuning* tuning)
    a.cfg.deriv_mode = c->deriv_mode;
    a.cfg.pa_scattering = c->pa_scattering;
    a.cfg.mu_method = c->mu_method;
+   a.cfg.perp_method = c->perp_method;
    a.cfg.max_attempts = c->max_attempts;
    a.cfg.steps_per_orbit = c->steps_per_orbit;
    a.cfg.steps_per_orbit_f = (float)c->steps_per_orbit;
@@ -806,6 +814,7 @@ int spx_autotune(spx_ctx_t c, int64_t sample_traj, spx_tuning* best)
       a.cfg.deriv_mode = c->deriv_mode;
       a.cfg.pa_scattering = c->pa_scattering;
       a.cfg.mu_method = c->mu_method;
+      a.cfg.perp_method = c->perp_method;
       a.cfg.max_attempts = c->max_attempts;
       a.cfg.steps_per_orbit = c->steps_per_orbit;
       a.cfg.steps_per_orbit_f = (float)c->steps_per_orbit;
@@ -1358,6 +1367,7 @@ int spx_run_static(spx_ctx_t c, const spx_tuning* tuning, int32_t* counts, int64
    a.cfg.deriv_mode = c->deriv_mode;
    a.cfg.pa_scattering = c->pa_scattering;
    a.cfg.mu_method = c->mu_method;
+   a.cfg.perp_method = c->perp_method;
    a.cfg.max_attempts = c->max_attempts;
    a.cfg.steps_per_orbit = c->steps_per_orbit;
    a.cfg.steps_per_orbit_f = (float)c->steps_per_orbit;

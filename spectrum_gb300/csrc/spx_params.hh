@@ -168,6 +168,7 @@ struct RunConfig {
    int steps_per_sync;
    uint32_t step_cap;         // 0, or the steps after which a trajectory is dropped (autotuning samples)
    int mu_method;             // guiding-centre pitch-angle step: 0 Euler, 1 Milstein, 2 RK2 (STOCHASTIC_METHOD_MU)
+   int perp_method;           // guiding-centre perpendicular step: 0 Euler, 1 Milstein, 2 RK2 (STOCHASTIC_METHOD_PERP)
    int64_t total_traj;
    int64_t run_index;         // trajectory ids of run r are r * n_traj + local (new streams per run)
 };

@@ -470,21 +470,14 @@ struct Kap {
    R perp, para;
 };
 
-// The field values the coefficient models read: |B|, U and the region indicators, and for the WNLT models
-// the pitch-angle cosine and the cyclotron frequency (DiffusionBase's mu and Omega, set once per
-// GetComponent and not moved by the spatial difference quotients, src/diffusion_base.cc:105-174). Passed
-// by value so the coefficient evaluation never takes the address of the lane's field record.
+// The field values the coefficient models read: |B|, U and the region indicators. Passed by value
+// so the coefficient evaluation never takes the address of the lane's field record.
 template <class R>
 struct KapIn {
    R Bmag;
    V3<R> U, region;
-   R mu, Omega;
 };
-template <class R> __device__ __forceinline__ KapIn<R> kap_in(const SD<R>& s) { return {s.Bmag, s.U, s.region, R(0), R(0)}; }
-template <class R> __device__ __forceinline__ KapIn<R> kap_in(const SD<R>& s, R mu, R Omega)
-{
-   return {s.Bmag, s.U, s.region, mu, Omega};
-}
+template <class R> __device__ __forceinline__ KapIn<R> kap_in(const SD<R>& s) { return {s.Bmag, s.U, s.region}; }
 
 // DiffusionWNLTRampVLISM::EvaluateDiffusion (src/diffusion_other.cc:301-324): on the Rankine half body
 // through "pos", the largest turbulent scale grows linearly from l_max_HP at the nose (a[8]) to l_max at
@@ -502,8 +495,12 @@ __device__ __forceinline__ void wnlt_ramp(const DiffParamsT<R>& d, V3<R> pos, R&
    a2l = d.a[6] * k_ratio;
 }
 
+// "mu" and "Omega" are DiffusionBase's pitch-angle cosine and cyclotron frequency, which only the WNLT models
+// read; they are set once per GetComponent and not moved by the spatial difference quotients
+// (src/diffusion_base.cc:105-174). The Parker types pass neither.
 template <class R>
-__device__ __forceinline__ Kap<R> kappa_pp(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const KapIn<R>& s)
+__device__ __forceinline__ Kap<R> kappa_pp(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const KapIn<R>& s, R mu = R(0),
+                                           R Omega = R(0))
 {
    Kap<R> K{R(0), R(0)};
    switch (d.kind) {
@@ -555,9 +552,9 @@ __device__ __forceinline__ Kap<R> kappa_pp(const DiffParamsT<R>& d, V3<R> pos, R
    case kDfWNLT: case kDfWNLTRamp: {                          // :215-228, 301-327
       R kmin = d.a[3], a2a = d.a[0], a2t = d.a[5], a2l = d.a[6];
       if (d.kind == kDfWNLTRamp) wnlt_ramp(d, pos, kmin, a2a, a2t, a2l);
-      R q = s.mu / kmin;
+      R q = mu / kmin;
       const R ct = R(0.5) * d.a[4] / (d.a[2] + R(1)) * (q * q) * a2t;
-      q = vmag * (R(1) - s.mu * s.mu) / s.Omega;
+      q = vmag * (R(1) - mu * mu) / Omega;
       const R cl = R(0.125) * (q * q) * a2l;
       K.perp = vmag * m_sqrt(ct + cl);
       break;
@@ -616,8 +613,15 @@ __device__ __noinline__ Kap<R> kappa_pp_call(const DiffParamsT<R>& d, V3<R> pos,
 }
 
 template <class R>
-__device__ __forceinline__ void kappa_grad(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const SD<R>& s, KapIn<R> q, Kap<R> K,
-                                           V3<R>& gperp, V3<R>& gpara)
+__device__ __noinline__ Kap<R> kappa_wnlt_call(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, KapIn<R> s, R mu, R Omega)
+{
+   return kappa_pp(d, pos, p, vmag, s, mu, Omega);
+}
+
+// kPitch: the caller is a type with a pitch angle, for which the WNLT ramp (never compiled for Parker) exists.
+template <class R, bool kPitch = false>
+__device__ __forceinline__ void kappa_grad(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const SD<R>& s, Kap<R> K, V3<R>& gperp,
+                                           V3<R>& gpara, R mu = R(0), R Omega = R(0))
 {
    switch (d.kind) {
    // DiffusionWNLTConstant reads neither the position nor |B| (mu and Omega stay fixed), so the base
@@ -654,16 +658,19 @@ __device__ __forceinline__ void kappa_grad(const DiffParamsT<R>& d, V3<R> pos, R
    }
    default: {
       R gpe[3], gpa[3];
+      KapIn<R> q = kap_in(s);
 #pragma unroll
       for (int xyz = 0; xyz < 3; xyz++) {
          R dr = R(0.5) * s.dr[xyz];
          R e[3] = {R(0), R(0), R(0)};
          e[xyz] = dr;
          q.Bmag = s.Bmag + s.gradBmag[xyz] * dr;
-         Kap<R> kf = kappa_pp_call(d, pos + mk(e[0], e[1], e[2]), p, vmag, q);
+         Kap<R> kf = kPitch && d.kind == kDfWNLTRamp ? kappa_wnlt_call(d, pos + mk(e[0], e[1], e[2]), p, vmag, q, mu, Omega)
+                                           : kappa_pp_call(d, pos + mk(e[0], e[1], e[2]), p, vmag, q);
          q.Bmag = q.Bmag - s.gradBmag[xyz] * (R(2) * dr);
          e[xyz] = dr - R(2) * dr;
-         Kap<R> kb = kappa_pp_call(d, pos + mk(e[0], e[1], e[2]), p, vmag, q);
+         Kap<R> kb = kPitch && d.kind == kDfWNLTRamp ? kappa_wnlt_call(d, pos + mk(e[0], e[1], e[2]), p, vmag, q, mu, Omega)
+                                           : kappa_pp_call(d, pos + mk(e[0], e[1], e[2]), p, vmag, q);
          gpe[xyz] = (kf.perp - kb.perp) / (R(2) * dr);
          gpa[xyz] = (kf.para - kb.para) / (R(2) * dr);
       }

@@ -37,6 +37,8 @@ struct Lane {
 struct Start {
    double t0;
    V3<double> pos0, mom0, bhat0;
+   uint32_t nuni;  // guiding types: uniforms drawn so far, set-up included (the perpendicular Milstein and RK2
+                   // schemes draw one a step); kept here, with the lane's other memory-resident state
 };
 
 struct Sinks {
@@ -544,7 +546,7 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, con
    else {
       // TRAJ_PARKER_DIVK_METHOD 1 (src/trajectory_parker.cc:120-140)
       V3<R> gpe, gpa;
-      kappa_grad(P.df, pos, p, vmag, sp, kap_in(sp), K, gpe, gpa);
+      kappa_grad(P.df, pos, p, vmag, sp, K, gpe, gpa);
       V3<R> t1 = gpa - gpe;
       divK = (gpe + dot(sp.bhat, t1) * sp.bhat) + (K.para - K.perp) * (sd_divbhat(sp) * sp.bhat + sd_b_gradbhat(sp));
    }
@@ -672,15 +674,44 @@ __device__ __forceinline__ V3<R> guiding_vperp(const DiffParamsT<R>& df, const S
 {
    const R p = m_sqrt(mom.x * mom.x + mom.z * mom.z);  // ConvertMomentum()[0]
    const R vmag = vel_of(p);
-   const KapIn<R> q = kap_in(s, mom.z / norm(mom), cyclotron(vmag, s.Bmag));  // ConvertMomentum()[1], Omega
-   Kap<R> K = kappa_pp(df, pos, p, vmag, q);
+   const R mu = mom.z / norm(mom), Omega = cyclotron(vmag, s.Bmag);  // ConvertMomentum()[1], CyclotronFrequency
+   Kap<R> K = kappa_pp(df, pos, p, vmag, kap_in(s), mu, Omega);
    V3<R> gpe, gpa;
-   kappa_grad(df, pos, p, vmag, s, q, K, gpe, gpa);
+   kappa_grad<R, true>(df, pos, p, vmag, s, K, gpe, gpa, mu, Omega);
    fa[2] = s.bhat;
    fa[0] = second_unit(s.bhat);
    fa[1] = cross(fa[2], fa[0]);
    d_perp = K.perp;
    return from_basis(mk(dot(gpe, fa[0]), dot(gpe, fa[1]), R(0)), fa);
+}
+
+// sqrt(2 D_perp) at a displaced point (src/trajectory_guiding_diff.cc:152-155): the fields there, then diffusion
+// component 0 with the step's momentum. "dmax" receives that evaluation's dmax, which the background's
+// GetSafeIncr reads for the next increment (src/background_base.cc:409-413). The reference evaluates these
+// points into a record whose field mask is uninitialised; here it is the trajectory's mask.
+template <int BG, class R>
+__device__ __noinline__ R perp_slope_at(const ProblemDescT<R>& P, int deriv_mode, R t, V3<R> pos, V3<R> mom, R& dmax, bool& ok)
+{
+   SD<R> s;
+   if (!get_fields<BG>(P.bg, deriv_mode, t, pos, norm(mom), traj_mask<kGuiding>(), s)) {
+      ok = false;
+      return R(0);
+   }
+   dmax = s.dmax;
+   const R p = m_sqrt(mom.x * mom.x + mom.z * mom.z);
+   const R vmag = vel_of(p);
+   const Kap<R> K = kappa_pp(P.df, pos, p, vmag, kap_in(s), mom.z / norm(mom), cyclotron(vmag, s.Bmag));
+   return m_sqrt(R(2) * K.perp);
+}
+
+// The trajectory's next uniform deviate: component k % 4 of set-up block k / 4, the count continuing from the
+// initial conditions (the reference draws every uniform from one generator, common/random.hh:99-122).
+template <class R, class A>
+__device__ __forceinline__ double lane_uniform(const Lane<R, A>& L, Start& s0, uint64_t seed, uint32_t problem_id)
+{
+   const uint32_t k = s0.nuni++;
+   const uint4 b = rng_block(seed, k >> 2, L.traj_id, problem_id, kRngInit, L.attempt);
+   return u01d((k & 3) == 0 ? b.x : ((k & 3) == 1 ? b.y : ((k & 3) == 2 ? b.z : b.w)));
 }
 
 template <int TT, class R>
@@ -724,7 +755,7 @@ __device__ __forceinline__ void clamp_mu(AV3<A>& mom)
 }
 
 template <int TT, int BG, class R, class A, int STAGES>
-__device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const Start& s0, const ProblemDescT<R>& P,
+__device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, Start& s0, const ProblemDescT<R>& P,
                                            const ProblemDesc& Pd, const RunConfig& cfg, const Sinks& S)
 {
    constexpr bool kFP64 = sizeof(R) == sizeof(double);
@@ -897,8 +928,71 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, const S
       const R dwx = m_sqrt(L.dt) * n[0];
       normals4<R>(rng_block(P.seed, L.nrm++, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
       const R dwy = m_sqrt(L.dt) * n[0];
-      const R sq = m_sqrt(R(2) * d_perp);
-      dr_perp = from_basis(mk(sq * dwx, sq * dwy, R(0)), fa);
+      const R b0 = m_sqrt(R(2) * d_perp);
+      R drx = b0 * dwx, dry = b0 * dwy;
+      if (cfg.perp_method == 1 || cfg.perp_method == 2) {
+         // MilsteinPerpDiffSlopes (src/trajectory_guiding_diff.cc:129-176) and RK2PerpDiffSlopes (:182-300):
+         // one-sided differences of sqrt(2 D_perp) across the field with GetSafeIncr's 1e-4 dmax steps (1e-2
+         // in the FP32 kernels, where 1e-4 is below the resolution of the quotients), and one uniform for the
+         // sign of the Levy-area stand-in
+         const R incr = kFP64 ? R(1e-4) : R(1e-2);
+         const R t0 = (R)acc_val(L.t), dt = L.dt;
+         const V3<R> x0 = val3<R>(pos_loc);
+         const V3<R> xhat = from_basis(mk(R(1), R(0), R(0)), fa), yhat = from_basis(mk(R(0), R(1), R(0)), fa);
+         R dmax = sp.dmax, dx, dy, bx, by, dbdx, dbdy;
+         bool ok = true;
+         if (cfg.perp_method == 1) {
+            dx = incr * dmax;
+            bx = perp_slope_at<BG>(P, deriv_mode, t0, x0 + dx * xhat, mom, dmax, ok);
+            dbdx = (bx - b0) / dx;
+            dy = incr * dmax;
+            by = perp_slope_at<BG>(P, deriv_mode, t0, x0 + dy * yhat, mom, dmax, ok);
+            dbdy = (by - b0) / dy;
+            const R vxy = lane_uniform(L, s0, P.seed, P.problem_id) < 0.5 ? dt : -dt;
+            drx = b0 * dwx + R(0.5) * b0 * (dbdx * (dwx * dwx - dt) + dbdy * (dwx * dwy - vxy));
+            dry = b0 * dwy + R(0.5) * b0 * (dbdy * (dwy * dwy - dt) + dbdx * (dwx * dwy + vxy));
+         }
+         else {
+            const R g = R(1) / m_sqrt(R(3));
+            const V3<R> dpos = from_basis(mk(b0 * dwx, b0 * dwy, R(0)), fa);
+            // the two trial points; a terminal crossing at either ends the trajectory there (:204-205, :213-214)
+            add3(L.pos, g * dpos);
+            if (space_terminate<TT>(L, bv, sp, s0, P, Pd, S)) return;
+            const R b1 = perp_slope_at<BG>(P, deriv_mode, t0 + dt, val3<R>(L.pos), mom, dmax, ok);
+            L.pos = pos_loc;
+            add3(L.pos, R(-1) * mk(dpos.x / (R(3) * g), dpos.y / (R(3) * g), dpos.z / (R(3) * g)));
+            if (space_terminate<TT>(L, bv, sp, s0, P, Pd, S)) return;
+            const R b2 = perp_slope_at<BG>(P, deriv_mode, t0 + dt, val3<R>(L.pos), mom, dmax, ok);
+            L.pos = pos_loc;
+            dx = incr * dmax;
+            const R bxx = perp_slope_at<BG>(P, deriv_mode, t0, x0 + dx * xhat, mom, dmax, ok);
+            dx *= R(0.5);
+            bx = perp_slope_at<BG>(P, deriv_mode, t0, x0 + dx * xhat, mom, dmax, ok);
+            dbdx = (bx - b0) / dx;
+            const R d2x = (bxx - R(2) * bx + b0) / (dx * dx);
+            dy = incr * dmax;
+            const R byy = perp_slope_at<BG>(P, deriv_mode, t0, x0 + dy * yhat, mom, dmax, ok);
+            dy *= R(0.5);
+            by = perp_slope_at<BG>(P, deriv_mode, t0, x0 + dy * yhat, mom, dmax, ok);
+            dbdy = (by - b0) / dy;
+            const R d2y = (byy - R(2) * by + b0) / (dy * dy);
+            const R bxy = perp_slope_at<BG>(P, deriv_mode, t0, (x0 + dx * xhat) + dy * yhat, mom, dmax, ok);
+            const R d2xy = (bxy - bx - by + b0) / (dx * dy);
+            const R vxy = lane_uniform(L, s0, P.seed, P.problem_id) < 0.5 ? dt : -dt;
+            const R rx = R(0.5) * b0 * (dbdx * (dwx * dwx - dt) + dbdy * (dwx * dwy - vxy)) +
+                         dt * (b0 * b0) * (d2y * dwx - d2xy * dwy) / R(6);
+            const R ry = R(0.5) * b0 * (dbdy * (dwy * dwy - dt) + dbdx * (dwx * dwy + vxy)) +
+                         dt * (b0 * b0) * (d2x * dwy - d2xy * dwx) / R(6);
+            const R bmid = R(0.5) * (b0 + (b1 + R(3) * (g * g) * b2) / (R(1) + R(3) * (g * g)));
+            drx = bmid * dwx + rx;
+            dry = bmid * dwy + ry;
+         }
+         if (!ok) {
+            L.status |= TRAJ_DISCARD;
+            return;
+         }
+      }
+      dr_perp = from_basis(mk(drx, dry, R(0)), fa);
    }
    // RKSlopes
 #pragma unroll
@@ -991,6 +1085,7 @@ __device__ __noinline__ void set_start(Lane<R, A>& L, BndView<R> bv, Start& s0, 
    if (!get_fields<BG>(P.bg, deriv_mode, (R)t, pr, pm, traj_mask<TT>(), sp)) { L.status |= TRAJ_DISCARD; return; }
    V3<double> bh = mk((double)sp.bhat.x, (double)sp.bhat.y, (double)sp.bhat.z);
    mom = sample_mom(rng, Pd, TT, bh);
+   if constexpr (TT == kGuiding) s0.nuni = rng.n_uniform;
    acc_set(L.mom.x, mom.x); acc_set(L.mom.y, mom.y); acc_set(L.mom.z, mom.z);
    s0.t0 = t;
    s0.pos0 = pos;

@@ -349,3 +349,4 @@ SPX_OPT_DERIV_MODE = 2
 SPX_OPT_PA_SCATTERING = 3
 SPX_OPT_RECORD_FINAL = 4
 SPX_OPT_MU_METHOD = 8
+SPX_OPT_PERP_METHOD = 9

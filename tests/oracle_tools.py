@@ -28,7 +28,7 @@ class _Opts(ctypes.Structure):
     _fields_ = [("traj_type", ctypes.c_int), ("time_flow", ctypes.c_int), ("rk", ctypes.c_int),
                 ("deriv_mode", ctypes.c_int), ("steps_per_orbit", ctypes.c_double),
                 ("pa_scattering", ctypes.c_int), ("max_attempts", ctypes.c_int), ("reference_quirks", ctypes.c_int),
-                ("mu_method", ctypes.c_int)]
+                ("mu_method", ctypes.c_int), ("perp_method", ctypes.c_int)]
 
 
 def build_oracle() -> str:
@@ -71,7 +71,8 @@ def run_oracle(problem, first: int = 0, n: int | None = None, deriv_mode: int = 
                pa_scattering: int | None = None, max_attempts: int = 100, record: bool = True,
                reference_quirks: int = 0) -> OracleResult:
     """Run the C restatement on ``problem`` (a spectrum_gb300.problem.Problem)."""
-    from spectrum_gb300.workloads import SPX_OPT_MU_METHOD, SPX_OPT_PA_SCATTERING, SPX_OPT_STEPS_PER_ORBIT
+    from spectrum_gb300.workloads import (SPX_OPT_MU_METHOD, SPX_OPT_PA_SCATTERING, SPX_OPT_PERP_METHOD,
+                                          SPX_OPT_STEPS_PER_ORBIT)
     if steps_per_orbit is None:
         steps_per_orbit = problem.options.get(SPX_OPT_STEPS_PER_ORBIT, 100.0)
     if pa_scattering is None:
@@ -82,16 +83,18 @@ def run_oracle(problem, first: int = 0, n: int | None = None, deriv_mode: int = 
                            problem.n_traj if n is None else n, first=first, deriv_mode=deriv_mode,
                            steps_per_orbit=steps_per_orbit, pa_scattering=pa_scattering, max_attempts=max_attempts,
                            record=record, reference_quirks=reference_quirks,
-                           mu_method=int(problem.options.get(SPX_OPT_MU_METHOD, 0)))
+                           mu_method=int(problem.options.get(SPX_OPT_MU_METHOD, 0)),
+                           perp_method=int(problem.options.get(SPX_OPT_PERP_METHOD, 0)))
 
 
 def run_oracle_spec(spec: bytes, traj_kind: int, time_flow: int, rk: int, n: int, first: int = 0, deriv_mode: int = 0,
                     steps_per_orbit: float = 100.0, pa_scattering: int = 0, max_attempts: int = 100,
-                    record: bool = True, reference_quirks: int = 0, mu_method: int = 0) -> OracleResult:
+                    record: bool = True, reference_quirks: int = 0, mu_method: int = 0,
+                    perp_method: int = 0) -> OracleResult:
     """Run the C restatement on a problem spec (the bytes Problem.to_spec() makes). With
     reference_quirks=1 the listed deviation D1 is reproduced as the reference has it."""
     opts = _Opts(traj_kind, time_flow, rk, deriv_mode, float(steps_per_orbit), int(pa_scattering), max_attempts,
-                 int(reference_quirks), int(mu_method))
+                 int(reference_quirks), int(mu_method), int(perp_method))
     sizes = distro_sizes(spec)
     tot = sum(s for s, _ in sizes)
     counts = np.zeros(max(tot, 1), dtype=np.int32)
@@ -186,10 +189,15 @@ REF_VARIANTS = {(206, 0, 0): "parker_fwd_rk0", (206, 1, 0): "parker_bwd_rk0", (2
 
 
 def ref_binary(problem) -> str | None:
-    from spectrum_gb300.workloads import SPX_OPT_MU_METHOD
+    from spectrum_gb300.workloads import SPX_OPT_MU_METHOD, SPX_OPT_PERP_METHOD
     v = REF_VARIANTS.get((problem.traj, problem.time_flow, problem.rk))
     if v is None:
         return None
+    perp = int(problem.options.get(SPX_OPT_PERP_METHOD, 0))
+    if perp:  # the reference compiled with that perpendicular scheme (oracle/ref_glue/perp_wrap.cc)
+        if problem.traj not in (203, 204) or problem.time_flow != 0:
+            return None
+        v = v.replace("_fwd_", f"_perp{perp}_fwd_")
     mu = int(problem.options.get(SPX_OPT_MU_METHOD, 0))
     if mu:  # the reference compiled with that pitch-angle scheme (oracle/ref_glue/mu_wrap.cc)
         if problem.traj != 202:

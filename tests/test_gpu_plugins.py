@@ -47,6 +47,8 @@ def _problems():
     out["lorentz_solar_wind"] = _lorentz_solar_wind
     for name, make in cases.WNLT_CASES.items():
         out["wnlt_" + name] = make
+    for name, make in cases.PERP_CASES.items():
+        out["perp_" + name] = make
     for name in cases.COMBO_CASES:
         out["combination_" + name] = lambda name=name: cases._combo(name)
     out["parker_source_constant"] = lambda: cases._parker(

@@ -21,7 +21,7 @@ from spectrum_gb300.plugins import (BackgroundDipole, BackgroundShock, Backgroun
                                     BoundaryBoxReflect, BoundaryCylinderAbsorb, BoundaryMomentumInjectRestrictShell,
                                     BoundaryMomentumInjectRestrictSlab, BoundaryMomentumPass, BoundaryPlanePass,
                                     BoundaryRankineAbsorb, BoundaryRegionAbsorb,
-                                    BoundarySphereReflect, BoundaryTimeExpire, BoundaryTimePass, BoundaryTimeRecurrent,
+                                    BoundarySphereAbsorb, BoundarySphereReflect, BoundaryTimeExpire, BoundaryTimePass, BoundaryTimeRecurrent,
                                     DiffusionEmpiricalSOQLTandUNLT, DiffusionFlowMomentumPowerLaw, DiffusionFullConstant,
                                     DiffusionKineticEnergyRadialDistancePowerLaw, DiffusionParaConstant,
                                     DiffusionPerpConstant, DiffusionPotgieterEtAl2015, DiffusionQLTConstant,
@@ -444,3 +444,39 @@ def test_wnlt_diffusion(name):
     r = _same(WNLT_CASES[name]())
     assert (r.traj["steps"] > 3).all()
 
+
+# -- the perpendicular Milstein and RK2 schemes (STOCHASTIC_METHOD_PERP 1, 2) --------------------------------------
+# The reference evaluates the displaced points into a SpatialData whose field mask is never initialised
+# (src/trajectory_guiding_diff.cc:133, 188), so which fields reach the diffusion model there is undefined. The
+# cases are chosen so that nothing depends on it: a uniform |B|, with D_perp varying through the position alone
+# (the WNLT ramp) or constant.
+def _perp_problem(traj, perp_method, ramp=True):
+    pb = _wnlt_problem(traj, True) if ramp else _parker(
+        traj=traj, diff=(DiffusionPerpConstant(), DC().double(0.05)), t_end=0.3, n=12,
+        im=(InitialMomentumShell(), DC().double(U.mev_to_mom(10.0))))
+    pb.options[W.SPX_OPT_PERP_METHOD] = float(perp_method)
+    return pb
+
+
+PERP_CASES = {
+    "milstein_ramp_guiding_diff": lambda: _perp_problem(TRAJ_GUIDING_DIFF, 1),
+    "rk2_ramp_guiding_diff": lambda: _perp_problem(TRAJ_GUIDING_DIFF, 2),
+    "milstein_constant_guiding_diff": lambda: _perp_problem(TRAJ_GUIDING_DIFF, 1, ramp=False),
+    "rk2_constant_guiding_diff": lambda: _perp_problem(TRAJ_GUIDING_DIFF, 2, ramp=False),
+    "rk2_ramp_guiding_diff_scatt": lambda: _perp_problem(TRAJ_GUIDING_DIFF_SCATT, 2),
+    "rk2_ramp_guiding_diff_absorbed": lambda: _perp_absorbed(),
+}
+
+
+def _perp_absorbed():
+    """RK2 with an absorbing sphere that the trajectories reach: a trial point of the scheme can cross it
+    (src/trajectory_guiding_diff.cc:205, 214), which ends the trajectory there."""
+    pb = _perp_problem(TRAJ_GUIDING_DIFF, 2)
+    pb.AddBoundary(BoundarySphereAbsorb(), B(DC(), 1, [0]).vec((0.3, 0, 0.2)).double(0.25))
+    return pb
+
+
+@pytest.mark.parametrize("name", sorted(PERP_CASES))
+def test_perpendicular_schemes(name):
+    r = _same(PERP_CASES[name]())
+    assert (r.traj["steps"] > 3).all()
