@@ -48,8 +48,8 @@ extern "C" {
 /* trajectory types: the numbers of configure.ac:236-244 */
 #define SPX_TRAJ_LORENTZ 200
 #define SPX_TRAJ_GUIDING 201        /* guiding centre, static backgrounds (uniform, dipole, solar wind, grid) */
-#define SPX_TRAJ_GUIDING_SCATT 202  /* guiding centre with Euler pitch-angle scattering; needs a diffusion model */
-#define SPX_TRAJ_GUIDING_DIFF 203   /* guiding centre with Euler perpendicular diffusion; needs a diffusion model */
+#define SPX_TRAJ_GUIDING_SCATT 202  /* guiding centre with pitch-angle scattering (SPX_OPT_MU_METHOD); needs a diffusion model */
+#define SPX_TRAJ_GUIDING_DIFF 203   /* guiding centre with perpendicular diffusion (SPX_OPT_PERP_METHOD); needs a diffusion model */
 #define SPX_TRAJ_GUIDING_DIFF_SCATT 204  /* both stochastic steps; needs a diffusion model */
 #define SPX_TRAJ_FOCUSED 205
 #define SPX_TRAJ_PARKER 206

@@ -4,7 +4,7 @@ nothing is launched, and the context stays usable. Needs a device only because c
 import pytest
 
 from spectrum_gb300 import capi, workloads
-from spectrum_gb300.problem import TRAJ_PARKER
+from spectrum_gb300.problem import TRAJ_GUIDING_DIFF, TRAJ_PARKER
 
 pytestmark = pytest.mark.gpu
 
@@ -61,3 +61,17 @@ def test_negative_trajectory_count_is_refused(built_lib):
     ctx = _ctx_with(pb)
     assert _code(lambda: ctx.add_problem(-1, 1)) == -1
     ctx.close()
+
+
+def test_scheme_options_are_checked(built_lib):
+    """The pitch-angle and perpendicular schemes exist only for the types that have those steps, and only
+    0, 1 and 2 name a scheme."""
+    ctx = capi.Context(TRAJ_PARKER, 0, 0, capi.SPX_FP64)
+    assert _code(lambda: ctx.set_option(capi.SPX_OPT_PERP_METHOD, 1.0)) == capi.SPX_ERR_INVALID_ARG
+    assert _code(lambda: ctx.set_option(capi.SPX_OPT_MU_METHOD, 2.0)) == capi.SPX_ERR_INVALID_ARG
+    ctx.close()
+    ctx = capi.Context(TRAJ_GUIDING_DIFF, 0, 25, capi.SPX_FP64)
+    ctx.set_option(capi.SPX_OPT_PERP_METHOD, 2.0)
+    assert _code(lambda: ctx.set_option(capi.SPX_OPT_PERP_METHOD, 3.0)) == capi.SPX_ERR_INVALID_ARG
+    ctx.close()
+
