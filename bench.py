@@ -1,8 +1,12 @@
 """Benchmark of the test-particle stepping path on one GB300 (or N GPUs as independent shards).
 
 Workload (one step = one launch over the whole batch): backward-time GCR modulation in the
-Parker-spiral solar wind, 32 log-spaced energies 10 MeV - 10 GeV, ``--per-energy`` trajectories
-each, LIS-weighted spectrum at the 100 AU boundary (spectrum_gb300.workloads.gcr_modulation).
+Parker-spiral solar wind, 32 log-spaced energies 10 MeV - 10 GeV, lambda proportional to P^0.5
+with no field dependence, kappa_perp = 0.02 kappa_par, absorbing spheres at 0.05 AU (cold) and
+100 AU (LIS-weighted), and the one time boundary the reference requires 100 years back, which no
+trajectory reaches (spectrum_gb300.workloads.gcr_modulation). The named job is
+1e6 trajectories per energy; one step integrates ``--per-energy`` of them (by default 1e5, a tenth:
+run k takes trajectory ids k*1e5 ... (k+1)*1e5 - 1 of every energy, so ten steps are the job).
 
 Reported (one JSON line on rank 0):
   value       trajectories/s of the batched FP32 stepper (persistent work queue, float-float
@@ -35,13 +39,16 @@ sys.path.insert(0, ROOT)
 METRIC = "SDE trajectories/s at <=1% bin error: batched FP32 vs plain FP64 GPU, 1 GB300"
 UNIT = "trajectories/s"
 WORKLOAD = "gcr_modulation_parker_spiral_32E"
-# Per-step work of the FP32 Parker solar-wind kernel, from one ncu capture of a 64,000-trajectory
-# batch of this workload (profiles/step_kernel_parker_solarwind_f32_gcr2k.md): executed FP32
-# operations (FFMA x 2 + FADD + FMUL) and thread instructions per accepted step, and DRAM bytes
-# per trajectory (2.84 MB over 64,000 trajectories; the kernel reads no field data from HBM).
-FP32_FLOP_PER_STEP = float(os.environ.get("SPX_FP32_FLOP_PER_STEP", "421"))
-THREAD_INST_PER_STEP = 812.0
-DRAM_BYTES_PER_TRAJ = 2.835e6 / 64000
+# Credited work per accepted step: the reference's formulation with analytic derivatives, counted by
+# the op-counting build of the CPU restatement (oracle/count_ops.py) and frozen in the benchmark spec.
+FROZEN_FLOP_PER_STEP = {"gcr": 1076.0, "diffusion": 273.0, "shock": 423.0, "dipole": 1130.2, "focused": 4291.0}
+FROZEN_SPECIAL_PER_STEP = {"gcr": 200.0, "diffusion": 93.0, "shock": 102.0, "dipole": 219.7, "focused": 468.0}
+# Executed by the FP32 Parker solar-wind kernel per accepted step, from the ncu capture of this workload
+# (profiles/step_kernel_parker_solarwind_f32_gcr.md): FP32 operations (FFMA x 2 + FADD + FMUL) and
+# thread instructions; and its DRAM bytes per trajectory (it reads no field data from HBM).
+EXEC_FP32_OPS_PER_STEP = float(os.environ.get("SPX_EXEC_FP32_OPS_PER_STEP", "421"))
+THREAD_INST_PER_STEP = float(os.environ.get("SPX_THREAD_INST_PER_STEP", "812"))
+DRAM_BYTES_PER_TRAJ = float(os.environ.get("SPX_DRAM_BYTES_PER_TRAJ", str(2.835e6 / 64000)))
 # run indices reserved per rank under torchrun: rank r integrates trajectory ids of runs
 # r*RUNS_PER_RANK ... (disjoint shards of one job)
 RUNS_PER_RANK = 256
@@ -216,6 +223,61 @@ def per_bin_error(a, b, min_count):
     return worst_c, worst_s, nb
 
 
+def compare_fp32_fp64(sub, tun, tuning64, torch, dev):
+    """The batched FP32 stepper against the FP64 kernel on identical Philox keys (the same problems in
+    fresh contexts): both throughputs and, per energy, the relative difference of the LIS-weighted
+    spectrum (the sum over the spectrum's bins) with its Monte Carlo standard error. Paths part in
+    the last bits and then decorrelate, so the error of the difference is formed from the paired
+    per-trajectory weights: sigma = sqrt(N var(w32 - w64)) / S64, the weights from the final records
+    (an exit at the outer sphere weighs the LIS at the exit momentum, src/distribution_other.cc:567-591)."""
+    import numpy as np
+    from spectrum_gb300 import capi, workloads
+    from spectrum_gb300.simulation import open_problems
+    res = {}
+    for name, prec, tn in (("fp64", capi.SPX_FP64, tuning64), ("fp32", capi.SPX_MIXED, tun)):
+        s = open_problems(sub, precision=prec, deriv_mode=1, record=True)
+        flush_l2(torch, dev)
+        st = s.MainLoop(tn)
+        recs = [s.ctx.records(k, p.n_traj) for k, p in enumerate(sub)]
+        dist = [[s.ctx.distribution(k, d) for d in range(2)] for k in range(len(sub))]
+        s.close()
+        res[name] = (st, recs, dist)
+    st64, r64, d64 = res["fp64"]
+    st32, r32, d32 = res["fp32"]
+    r_hot = 50.0 * workloads.ONE_AU  # between the spheres at 0.05 and 100 AU: an exit at the outer one is hot
+    rows = []
+    for k, pb in enumerate(sub):
+        s64 = float(d64[k][0][1][:, 0].sum())
+        s32 = float(d32[k][0][1][:, 0].sum())
+        w = []
+        for rec in (r64[k], r32[k]):
+            hot = np.linalg.norm(rec["pos"], axis=1) > r_hot
+            w.append(np.where(hot, workloads.lis_weights(np.abs(rec["mom"][:, 0])), 0.0))
+        n = len(w[0])
+        e_mev = workloads.modulation_energies()[pb.problem_id]
+        rows.append({"energy_mev": round(e_mev, 3), "events_fp64": int(d64[k][0][2]),
+                     "rel_err": s32 / s64 - 1.0 if s64 else None,
+                     "sigma": float(np.sqrt(n * np.var(w[1] - w[0])) / s64) if s64 else None,
+                     "sigma_fp64_alone": float(np.sqrt(n * np.var(w[0])) / s64) if s64 else None,
+                     "records_vs_histogram": float(w[0].sum() / s64 - 1.0) if s64 else None})
+    ok = [r for r in rows if r["rel_err"] is not None]
+    # counts of every histogram bin with an FP64 count >= 1e4 (the criterion's bins)
+    ec, _, nbins = per_bin_error([x for r in d32 for x in r], [x for r in d64 for x in r], 10000)
+    return {"value": st64.trajectories / (st64.kernel_ms / 1e3), "unit": UNIT, "kernel_ms": st64.kernel_ms,
+            "trajectories": st64.trajectories, "energies": [r["energy_mev"] for r in rows],
+            "per_energy": sub[0].n_traj, "steps_per_s": st64.steps / (st64.kernel_ms / 1e3),
+            "derivatives": "analytic (the FP32 kernel's formulation)",
+            "fp32_same_batch": st32.trajectories / (st32.kernel_ms / 1e3),
+            "ratio_fp32_batched_over_fp64_plain": (st32.trajectories / (st32.kernel_ms / 1e3)) /
+                                                  (st64.trajectories / (st64.kernel_ms / 1e3)),
+            "weighted_spectrum": rows,
+            "weighted_spectrum_max_rel_err": max(abs(r["rel_err"]) for r in ok) if ok else None,
+            "weighted_spectrum_max_sigma": max(r["sigma"] for r in ok) if ok else None,
+            "weighted_spectrum_within_1pct": bool(ok and all(abs(r["rel_err"]) <= 0.01 for r in ok)),
+            "weighted_spectrum_resolved": bool(ok and all(r["sigma"] <= 0.003 for r in ok)),
+            "count_bin_error": ec, "count_bins_compared": nbins}
+
+
 # Throughput of the other workload families (the per-family figures). Each entry:
 # builder of the problem list (FP32 run), its description, and the share of it the FP64 plain
 # kernel runs for the ratio.
@@ -298,6 +360,26 @@ def bench_other(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def bench_accuracy(args):
+    """One JSON line: the per-bin criterion on the LIS-weighted spectrum at a sample large enough to
+    resolve it (the FP64 kernel on the persistent queue: results do not depend on the schedule)."""
+    import torch
+    from spectrum_gb300 import capi
+    from spectrum_gb300.simulation import open_problems
+    dev = torch.device("cuda", 0)
+    torch.cuda.set_device(dev)
+    sim = open_problems(problems(args.per_energy), precision=capi.SPX_MIXED)
+    tun = sim.ctx.autotune(0)
+    sim.close()
+    sub = problems(args.accuracy)[::8]
+    t0 = time.perf_counter()
+    cmp = compare_fp32_fp64(sub, tun, capi.Tuning(128, 0, 16, 1), torch, dev)
+    cmp["schedule"] = "persistent work queue (both)"
+    line = {"metric": "FP32 vs FP64 LIS-weighted spectrum, per-energy relative error and Monte Carlo sigma",
+            "workload": WORKLOAD, "per_energy": args.accuracy, "wall_s": time.perf_counter() - t0, **cmp}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -305,9 +387,15 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="spectrum_gb300", choices=["spectrum_gb300", "reference"])
     ap.add_argument("--per-energy", type=int, default=int(os.environ.get("SPX_BENCH_PER_ENERGY", "100000")))
-    ap.add_argument("--fp64-per-energy", type=int, default=16000,
+    ap.add_argument("--accuracy", type=int, default=0, metavar="N",
+                    help="instead of the benchmark: the FP32 stepper against the FP64 kernel (persistent queue) on "
+                         "identical keys, every eighth energy x N trajectories, per-energy weighted-spectrum error "
+                         "with its Monte Carlo sigma")
+    ap.add_argument("--fp64-per-energy", type=int, default=4000,
                     help="trajectories per energy of the FP64 comparison (every fourth energy)")
     ap.add_argument("--cpu-seconds", type=float, default=20.0)
+    ap.add_argument("--tuning", default="", metavar="BLOCK,BLOCKS_PER_SM,STEPS_PER_SYNC",
+                    help="a fixed launch shape for the persistent queue instead of the autotuner's (profiling)")
     ap.add_argument("--no-fp64", action="store_true")
     ap.add_argument("--workload", default="gcr", choices=["gcr"] + sorted(OTHER_WORKLOADS),
                     help="gcr: the headline modulation batch; the others print throughput lines for the "
@@ -316,10 +404,19 @@ def main():
     rank, world, local = rank_info()
     if args.workload != "gcr":
         return bench_other(args, rank, world, local)
+    if args.accuracy:
+        return bench_accuracy(args)
     cfg = {"workload": WORKLOAD, "energies": 32, "per_energy": args.per_energy,
            "trajectories_per_step": 32 * args.per_energy * world, "time_flow": "backward", "background": "solar wind",
-           "diffusion": "kappa_par = lam v/3 (R/1GV)^0.5 (B/5nT)^-1, kappa_perp = 0.02 kappa_par",
-           "boundaries": "0.05 AU absorb (cold), 100 AU absorb (LIS-weighted), 1 yr", "l2": "flushed between steps"}
+           "diffusion": "kappa_par = (0.1 AU) v/3 (R/1GV)^0.5, kappa_perp = 0.02 kappa_par",
+           "kappa_b_exponent": 0.0, "kappa_perp_ratio": 0.02,
+           "time_cap": "BoundaryTimeExpire 100 yr back: the reference requires one time boundary "
+                       "(src/trajectory_base.cc:626-627); exits_per_energy.neither counts the trajectories that reach it",
+           "boundaries": "0.05 AU absorb (cold), 100 AU absorb (LIS-weighted), 100 yr time limit",
+           "fraction_of_named_job": args.per_energy / 1.0e6,
+           "trajectory_ids": f"step k integrates ids k*{args.per_energy} ... (k+1)*{args.per_energy}-1 of each "
+                             f"energy; the named job is 1e6 per energy",
+           "l2": "flushed between steps"}
 
     if args.impl == "reference":
         if rank != 0:
@@ -361,7 +458,11 @@ def main():
     if world > 1:
         shard.assign(sim, rank, RUNS_PER_RANK)
     # the launch shape: the project's autotuner, timed on a sample of this batch (set-up, untimed)
-    tun = sim.ctx.autotune(0)
+    if args.tuning:
+        b, bps, sps = (int(x) for x in args.tuning.split(","))
+        tun = capi.Tuning(b, bps, sps, 1)
+    else:
+        tun = sim.ctx.autotune(0)
     for _ in range(args.warmup):
         sim.MainLoop(tun)
     sim.ctx.reset_distributions()
@@ -378,7 +479,7 @@ def main():
     torch.cuda.synchronize(dev)
     t_wall0 = time.perf_counter()
     with clocks:
-        first_distros = None
+        ends = None
         for k in range(args.steps):
             flush_l2(torch, dev)
             st = sim.MainLoop(tun)
@@ -386,50 +487,30 @@ def main():
             steps_done += st.steps
             traj_done += st.trajectories
             if k == 0:
-                first_distros = [sim.ctx.distribution(p, 0) for p in range(len(pbs))]
+                # where step 0's trajectories ended: the spectrum records both spheres (the inner one
+                # cold), the exit-time histogram the outer one only
+                ends = [(sim.ctx.distribution(p, 1)[2], sim.ctx.distribution(p, 0)[2]) for p in range(len(pbs))]
                 sim.ctx.reset_distributions()
     torch.cuda.synchronize(dev)
     wall = time.perf_counter() - t_wall0
     tuning = {"block_size": st.tuning.block_size, "blocks_per_sm": st.tuning.blocks_per_sm,
               "steps_per_sync": st.tuning.steps_per_sync,
               "schedule": "persistent work queue" if st.tuning.schedule == 1 else "one thread per trajectory",
-              "chosen_by": "spx_autotune"}
+              "chosen_by": "--tuning" if args.tuning else "spx_autotune"}
     sim.close()
     t_dev = sum(kms) / 1e3
     t_max = shard.max_over_ranks(t_dev) if world > 1 else t_dev
     value = traj_done * world / t_max
     steps_rate = steps_done * world / t_max
 
-    # ---- plain FP64 drop-in on step 0's keys: comparison and per-bin error -------------------
+    # ---- plain FP64 drop-in on identical keys: throughput ratio and per-bin error ----------------
     fp64 = None
     if not args.no_fp64:
-        # Every fourth energy, at a per-energy count that keeps the FP64 leg to about a minute (each
-        # spectrum bin still holds >= 1e4 events); fresh contexts with the same problem list draw
-        # identical Philox streams.
-        sub = problems(min(args.per_energy, args.fp64_per_energy))[::4]
-        sim64 = open_problems(sub, precision=capi.SPX_FP64, deriv_mode=1)
-        flush_l2(torch, dev)
-        st64 = sim64.MainLoop(capi.Tuning(0, 0, 1, 0))
-        d64 = [[sim64.ctx.distribution(p, d) for d in range(2)] for p in range(len(sub))]
-        sim64.close()
-        sim32 = open_problems(sub, precision=capi.SPX_MIXED)
-        flush_l2(torch, dev)
-        st32 = sim32.MainLoop(tun)
-        d32 = [[sim32.ctx.distribution(p, d) for d in range(2)] for p in range(len(sub))]
-        sim32.close()
-        # counts of every histogram (the criterion: bins with an FP64 count >= 1e4)
-        ec, _, nbins = per_bin_error([x for r in d32 for x in r], [x for r in d64 for x in r], 10000)
-        # the LIS-weighted spectrum (one bin per energy)
-        _, es, nbs = per_bin_error([r[0] for r in d32], [r[0] for r in d64], 10000)
-        fp64 = {"value": st64.trajectories / (st64.kernel_ms / 1e3), "unit": UNIT, "kernel_ms": st64.kernel_ms,
-                "trajectories": st64.trajectories, "energies": "every 4th of the 32",
-                "per_energy": min(args.per_energy, args.fp64_per_energy),
-                "steps_per_s": st64.steps / (st64.kernel_ms / 1e3), "schedule": "one thread per trajectory",
-                "derivatives": "analytic (the FP32 kernel's formulation)",
-                "bin_error": ec, "bins_compared": nbins, "bin_error_ok": bool(nbins > 0 and ec <= 0.01),
-                "weighted_spectrum_error": es, "weighted_bins_compared": nbs,
-                "ratio_fp32_batched_over_fp64_plain": (st32.trajectories / (st32.kernel_ms / 1e3)) /
-                                                      (st64.trajectories / (st64.kernel_ms / 1e3))}
+        # Every eighth energy, at a per-energy count that keeps the FP64 leg to about a minute; fresh
+        # contexts with the same problem list draw identical Philox streams.
+        sub = problems(min(args.per_energy, args.fp64_per_energy))[::8]
+        fp64 = compare_fp32_fp64(sub, tun, capi.Tuning(0, 0, 1, 0), torch, dev)
+        fp64["schedule"] = "one thread per trajectory"
 
     # ---- end to end through the C ABI --------------------------------------------------------
     e2e_times = []
@@ -457,22 +538,34 @@ def main():
     sm_max = peaks.get("sm_max_mhz", 2070.0)
     props = torch.cuda.get_device_properties(dev)
     fp32_peak = props.multi_processor_count * 128 * 2 * sm_max * 1e6 / 1e12  # TFLOP/s, FFMA pipe
-    roof = {"bound": "fp32", "unit": "TFLOP/s", "peak": fp32_peak,
+    per_gpu_steps = steps_rate / world
+    ach = per_gpu_steps * FROZEN_FLOP_PER_STEP["gcr"] / 1e12
+    roof = {"bound": "fp32", "unit": "TFLOP/s", "peak": fp32_peak, "achieved": ach, "frac": ach / fp32_peak,
             "peak_source": "nominal FP32 FMA pipe: SMs x 128 lanes x 2 x sm_max_mhz of MEASURED_PEAKS.json "
                            "(the file has no FP32 figure; HBM and tensor peaks do not bound this kernel)",
-            "traffic": None}
-    ach = steps_rate / world * FP32_FLOP_PER_STEP / 1e12
-    roof.update({"achieved": ach, "frac": ach / fp32_peak, "flop_per_step": FP32_FLOP_PER_STEP,
-                 "traffic": DRAM_BYTES_PER_TRAJ * traj_done / max(args.steps, 1) / world,
-                 "traffic_unit": "bytes per launch (ncu, scaled by trajectories)"})
+            "flop_per_step": FROZEN_FLOP_PER_STEP["gcr"],
+            "flop_source": "credited: the reference's formulation with analytic derivatives, counted by the "
+                           "op-counting CPU restatement (oracle/count_ops.py), frozen in BASELINE.md",
+            "traffic": DRAM_BYTES_PER_TRAJ * traj_done / max(args.steps, 1) / world,
+            "traffic_unit": "bytes per launch (ncu, scaled by trajectories)"}
+    # what the kernel executes: its own FP32 operations and instructions per step (ncu), which its
+    # closed forms keep below the credited count
+    roof["executed"] = {"fp32_ops_per_step": EXEC_FP32_OPS_PER_STEP,
+                        "tflops": per_gpu_steps * EXEC_FP32_OPS_PER_STEP / 1e12,
+                        "frac": per_gpu_steps * EXEC_FP32_OPS_PER_STEP / 1e12 / fp32_peak}
     # the binding resource: instruction issue (4 schedulers per SM, one warp instruction per cycle)
     issue_peak = props.multi_processor_count * 4 * sm_max * 1e6
     roof["issue"] = {"thread_inst_per_step": THREAD_INST_PER_STEP,
-                     "warp_inst_per_s_at_full_simt": steps_rate / world * THREAD_INST_PER_STEP / 32.0,
+                     "warp_inst_per_s_at_full_simt": per_gpu_steps * THREAD_INST_PER_STEP / 32.0,
                      "peak_warp_inst_per_s": issue_peak,
-                     "frac_at_full_simt": steps_rate / world * THREAD_INST_PER_STEP / 32.0 / issue_peak}
+                     "frac_at_full_simt": per_gpu_steps * THREAD_INST_PER_STEP / 32.0 / issue_peak}
 
     clk = clocks.summary()
+    if ends is not None:
+        n0 = args.per_energy
+        cfg["exits_per_energy"] = {"outer_100AU": [round(o / n0, 4) for o, _ in ends],
+                                   "inner_0.05AU": [round((b - o) / n0, 4) for o, b in ends],
+                                   "neither": [round(1.0 - b / n0, 4) for _, b in ends]}
     line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (float-float accumulation)",

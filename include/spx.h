@@ -119,7 +119,14 @@ typedef struct {
 /* ---- calls ----------------------------------------------------------------------------- */
 /* Create a context on the current CUDA device. Replaces CreateSimulation
  * (src/simulation.cc:899-907) plus the configure-time choice of TRAJ_TYPE, TRAJ_TIME_FLOW and
- * RK_INTEGRATOR_TYPE (configure.ac:236-295; Runge-Kutta tables 0 and 25 are supported). */
+ * RK_INTEGRATOR_TYPE (configure.ac:236-295). rk_method is any Butcher table of
+ * common/rk_config.hh:72-520 but 30 (which does not compile in the reference), with the
+ * reference's adaptive step control and step rejection for the adaptive ones
+ * (src/trajectory_base.cc:366-406); the Parker types apply it to their drift and add the
+ * Euler-Maruyama displacement after the step (src/trajectory_parker.cc:255-306). Euler (0), and the
+ * classic RK4 (25) for the Runge-Kutta types, run in both arithmetics; the other tables in SPX_FP64
+ * only (SPX_MIXED gives SPX_ERR_INVALID_ARG: FP32 cannot meet the tables' 1e-9 error tolerance).
+ * The arguments are checked before the device is looked for. */
 int spx_create(spx_ctx_t* ctx, int traj_kind, int time_flow, int rk_method, int precision);
 
 /* Set an SPX_OPT_* option (no reference counterpart: these are the reference's compile-time
@@ -179,8 +186,11 @@ int spx_autotune(spx_ctx_t ctx, int64_t sample_traj, spx_tuning* best);
  * problem descriptors live in a fixed array of SPX_STATIC_SCRATCH_BYTES; a context whose
  * descriptors do not fit is rejected with SPX_ERR_TOO_LARGE. The call allocates no device memory
  * (no cudaMalloc, cudaFree or allocating library routine); it blocks until the launch is done
- * and fills stats (may be NULL). The first call on a device looks up the array's address there
- * (and may load the library's device code), so make it before any stream capture. All calls share
+ * and fills stats (may be NULL). The launch shape is chosen as spx_run chooses it (tuning, else the
+ * spx_autotune result, else the defaults). The first call on a device looks up the array's address
+ * there (and may load the library's device code), so make it before any stream capture; the
+ * address is kept for the life of the process, so resetting the device (cudaDeviceReset) while the
+ * library is loaded is not supported. All calls share
  * the array and it keeps the last call's contents (each call clears the counters it needs):
  * calls whose launches overlap on the GPU race and give wrong results. Trajectory ids continue
  * from spx_run's, so a sequence of spx_run_static calls draws the same trajectories as the same

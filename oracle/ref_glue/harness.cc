@@ -188,6 +188,7 @@ void AddPlugin(Probe& traj, uint32_t role, const std::string& name, const DataCo
       SPX_TRY_DIST(DistributionDivergenceFlowPowerLaw)
       W = 3;
       SPX_TRY_DIST(DistributionPositionCumulativeOrder1)
+      SPX_TRY_DIST(DistributionLossCone)
       W = 9;
       SPX_TRY_DIST(DistributionPositionCumulativeOrder2)
    }

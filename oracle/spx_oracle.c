@@ -20,11 +20,30 @@
  */
 #include "spx_oracle.h"
 #include "spx_rng.h"
+#include "spx_rk_tables.h"
 
 #include <math.h>
 #include <stdio.h>
 #include <stdlib.h>
 #include <string.h>
+
+/* With nudge_libm (a test option) every result of the transcendental functions below is moved one
+ * ulp away from zero: a model of another libm rounding them differently in the last bit, with which
+ * the parity tests measure a problem's conditioning. The macros leave sqrt and the arithmetic alone
+ * (both round correctly everywhere); inside each macro the name refers to the function itself. */
+static int g_nudge_libm = 0;
+static double nudged(double v) { return g_nudge_libm ? nextafter(v, v >= 0.0 ? INFINITY : -INFINITY) : v; }
+#define exp(x) nudged(exp(x))
+#define log(x) nudged(log(x))
+#define log10(x) nudged(log10(x))
+#define pow(x, y) nudged(pow(x, y))
+#define sin(x) nudged(sin(x))
+#define cos(x) nudged(cos(x))
+#define tanh(x) nudged(tanh(x))
+#define acos(x) nudged(acos(x))
+#define asin(x) nudged(asin(x))
+#define atan2(y, x) nudged(atan2(y, x))
+#define cbrt(x) nudged(cbrt(x))
 
 /* ------------------------------------------------------------------------------------------ */
 /* constants: common/definitions.hh:54-66, common/specie.hh:30-82, common/physical_constants.hh */
@@ -252,7 +271,8 @@ typedef struct {
    int n_int, flag;
 } ini_t;
 
-enum { DS_TIME = 1, DS_POS, DS_MOM, DS_POSMOM, DS_SPEC, DS_SPECBENT, DS_CUM1, DS_CUM2, DS_DIVFLOW, DS_TIMEMU = 20 };
+enum { DS_TIME = 1, DS_POS, DS_MOM, DS_POSMOM, DS_SPEC, DS_SPECBENT, DS_CUM1, DS_CUM2, DS_DIVFLOW, DS_LOSSCONE,
+       DS_TIMEMU = 20 };
 typedef struct {
    int kind, width;
    int n_bins[3], log_bins[3], bin_outside[3], dims;
@@ -521,7 +541,7 @@ static int setup_dist(dist_t* d, rd_t* r, int kind)
    v3 mn, mx;
    memset(d, 0, sizeof *d);
    d->kind = kind;
-   d->width = (kind == DS_CUM1) ? 3 : (kind == DS_CUM2 ? 9 : 1);
+   d->width = (kind == DS_CUM1 || kind == DS_LOSSCONE) ? 3 : (kind == DS_CUM2 ? 9 : 1);
    /* DistributionTemplated::SetupDistribution, src/distribution_templated.cc:92-137 */
    rd_mi(r, d->n_bins);
    mn = rd_v(r);
@@ -561,6 +581,14 @@ static int setup_dist(dist_t* d, rd_t* r, int kind)
       break;
    case DS_CUM1: case DS_CUM2: d->n_actions = 1; break;
    case DS_DIVFLOW: d->A0 = rd_d(r); d->pow_law = rd_d(r); d->val_cold = rd_d(r); d->n_actions = 2; break;
+   case DS_LOSSCONE:
+      /* DistributionLossCone::SetupDistribution, src/distribution_other.cc:826-840: one action, all three
+       * dimensions active */
+      d->val_time = rd_i(r);
+      d->val_coord = rd_i(r);
+      d->n_actions = 1;
+      if (d->dims != 7) return -3;
+      break;
    }
    return 0;
 }
@@ -610,6 +638,7 @@ static int kind_of(uint32_t role, const char* nm, size_t nl)
       K("DistributionSpectrumKineticEnergyBentPowerLaw", DS_SPECBENT)
       K("DistributionPositionCumulativeOrder1", DS_CUM1) K("DistributionPositionCumulativeOrder2", DS_CUM2)
       K("DistributionDivergenceFlowPowerLaw", DS_DIVFLOW) K("DistributionTimeMu", DS_TIMEMU)
+      K("DistributionLossCone", DS_LOSSCONE)
    }
 #undef K
    return -1;
@@ -692,9 +721,25 @@ static int parse_spec(const uint8_t* s, size_t n, prob_t* pb, char* err, size_t 
 /* ------------------------------------------------------------------------------------------ */
 /* trajectory object                                                                          */
 /* ------------------------------------------------------------------------------------------ */
+/* A Butcher table (common/rk_config.hh:36-65) */
+typedef struct {
+   int number, stages, order, adaptive;
+   double a[SPX_RK_MAX_STAGES], b[SPX_RK_MAX_STAGES][SPX_RK_MAX_STAGES], v[SPX_RK_MAX_STAGES], w[SPX_RK_MAX_STAGES];
+} rk_t;
+
+/* adaptive step control of RKStep (common/rk_config.hh:25-34) and Integrate's limit on consecutive
+ * rejected steps (src/trajectory_base.hh:41) */
+#define RK_TOL_ABS 1.0e-9
+#define RK_TOL_REL 1.0e-9
+#define RK_SAFETY 2.0
+#define RK_ADJUST 0.995
+#define MAX_TIME_ADAPTATIONS 100
+
 typedef struct {
    const prob_t* pb;
    const spx_oracle_opts* o;
+   const rk_t* rk;
+   int time_adaptations;
    /* RNG */
    uint32_t traj_id, attempt;
    uint64_t n_normal, n_uniform, n_init_normal;
@@ -708,6 +753,12 @@ typedef struct {
    uint64_t segments;
    double local_t, local_amp, local_wgt;
    v3 local_pos, local_mom;
+   /* |B| extrema along the trajectory (TrajectoryBase with RECORD_BMAG_EXTREMA, src/trajectory_base.cc:
+      581-592, 884-888, 959-962), read by DistributionLossCone */
+   double bmag_min, bmag_max;
+   /* the last stored point of the trajectory (Store(), read back by Load()) */
+   double stored_t;
+   v3 stored_pos, stored_mom;
    bnd_t bt[MAXB], bs[MAXB], bm[MAXB];
    int bactive_t, bactive_s, bactive_m;
    /* Parker */
@@ -731,6 +782,15 @@ typedef struct {
    int error;
 } trj_t;
 
+/* The normal deviates of one random block; with nudge_libm each is moved one ulp away from zero. */
+static void normals4(const uint32_t b[4], double n[4])
+{
+   int i;
+   spx_normals4(b, n);
+   if (g_nudge_libm)
+      for (i = 0; i < 4; i++) n[i] = nextafter(n[i], n[i] >= 0.0 ? INFINITY : -INFINITY);
+}
+
 static double next_uniform(trj_t* T)
 {
    uint64_t k = T->n_uniform++;
@@ -745,7 +805,7 @@ static double next_init_normal(trj_t* T)
    uint32_t b[4];
    double n[4];
    spx_rng_block(T->pb->seed, (uint32_t)(k / 4), T->traj_id, T->pb->problem, SPX_RNG_INIT_NORMAL, T->attempt, b);
-   spx_normals4(b, n);
+   normals4(b, n);
    return n[k % 4];
 }
 
@@ -1427,7 +1487,7 @@ static void process_trajectory(trj_t* T, int di, int action)
    /* EvaluateValue */
    switch (d->kind) {
    case DS_TIME: value.x[0] = (d->val_time == 0) ? T->t0 : T->t; break;
-   case DS_POS:
+   case DS_POS: case DS_LOSSCONE:
       value = (d->val_time == 0) ? T->pos0 : T->pos;
       if (d->val_coord == 1) pos_to_rtp(&value);
       break;
@@ -1480,6 +1540,13 @@ static void process_trajectory(trj_t* T, int di, int action)
       break;
    }
    case DS_DIVFLOW: w[0] = (action == 0) ? d->A0 * pow(fabs(sd_divU(s2)), d->pow_law) : d->val_cold; break;
+   case DS_LOSSCONE:
+      /* DistributionLossCone::RecordLossCone, src/distribution_other.cc:858-862: the |B| extrema along
+       * the trajectory and the loss-cone half-angle at the first or the second point */
+      w[0] = T->bmag_min;
+      w[1] = T->bmag_max;
+      w[2] = asin(sqrt(((d->val_time == 0) ? s1->Bmag : s2->Bmag) / T->bmag_max));
+      break;
    }
    /* AddEvent */
    for (ijk = 0; ijk < 3; ijk++) {
@@ -1803,7 +1870,13 @@ static void time_proximity(trj_t* T)
    else { if (T->dt >= dn) T->dt = fmax((1.0 + SP_LITTLE) * dn, SP_SMALL * T->sp.dmax / c); }
 }
 
-static void store(trj_t* T) { T->segments++; }
+static void store(trj_t* T)
+{
+   T->segments++;
+   T->stored_t = T->t;
+   T->stored_pos = T->pos;
+   T->stored_mom = T->mom;
+}
 
 /* HandleBoundaries, src/trajectory_base.cc:413-535 */
 /* ReverseMomentum: the base negates the vector (src/trajectory_base.cc:139-142), Focused its mu
@@ -1879,12 +1952,30 @@ static int space_terminate(trj_t* T)
    return 0;
 }
 
-/* Butcher tables: Euler (#0) and classic RK4 (#25), common/rk_config.hh:72-78, 380-390 */
-typedef struct { int stages; double a[4], b[4][4], v[4]; } rk_t;
-static const rk_t RK0 = {1, {0.0}, {{0.0}}, {1.0}};
-static const rk_t RK4 = {4, {0.0, 0.5, 0.5, 1.0},
-                         {{0.0, 0.0, 0.0, 0.0}, {0.5, 0.0, 0.0, 0.0}, {0.0, 0.5, 0.0, 0.0}, {0.0, 0.0, 1.0, 0.0}},
-                         {1.0 / 6.0, 1.0 / 3.0, 1.0 / 3.0, 1.0 / 6.0}};
+/* Butcher tables (common/rk_config.hh:72-520), from the exact table the library shares
+ * (spx_rk_tables.h, pinned to the reference's header by tests/test_rk_tables.py). RKSlopes reads only
+ * the strictly lower triangle of b; the rest stays zero. */
+static int rk_load(int number, rk_t* R)
+{
+   int k, i, j;
+   memset(R, 0, sizeof *R);
+   for (k = 0; k < SPX_RK_N_TABLES; k++) {
+      const spx_rk_entry* e = &spx_rk_index[k];
+      const double* c = spx_rk_coeffs + e->offset;
+      if (e->number != number) continue;
+      R->number = number;
+      R->stages = e->stages;
+      R->order = e->order;
+      R->adaptive = e->adaptive;
+      for (i = 0; i < e->stages; i++) R->a[i] = *c++;
+      for (i = 1; i < e->stages; i++)
+         for (j = 0; j < i; j++) R->b[i][j] = *c++;
+      for (i = 0; i < e->stages; i++) R->v[i] = *c++;
+      for (i = 0; i < e->stages; i++) R->w[i] = *c++;
+      return 0;
+   }
+   return -1;
+}
 
 static void lorentz_slopes(trj_t* T, v3* sp, v3* sm)
 {
@@ -2017,10 +2108,10 @@ static int guiding_perp_step(trj_t* T)
    uint32_t b[4];
    memset(&st, 0, sizeof st);
    spx_rng_block(T->pb->seed, (uint32_t)T->n_normal++, T->traj_id, T->pb->problem, SPX_RNG_STEP, T->attempt, b);
-   spx_normals4(b, n);
+   normals4(b, n);
    n1 = n[0];
    spx_rng_block(T->pb->seed, (uint32_t)T->n_normal++, T->traj_id, T->pb->problem, SPX_RNG_STEP, T->attempt, b);
-   spx_normals4(b, n);
+   normals4(b, n);
    n2 = n[0];
    dwx = sqrt(T->dt) * n1;
    dwy = sqrt(T->dt) * n2;
@@ -2153,7 +2244,7 @@ static double gc_normal(trj_t* T)
    double n[4];
    uint32_t b[4];
    spx_rng_block(T->pb->seed, (uint32_t)T->n_normal++, T->traj_id, T->pb->problem, SPX_RNG_STEP, T->attempt, b);
-   spx_normals4(b, n);
+   normals4(b, n);
    return n[0];
 }
 
@@ -2231,11 +2322,11 @@ static void pa_scatter(trj_t* T, uint32_t step)
    uint32_t b[4];
    int k = 0, blk = 0;
    spx_rng_block(T->pb->seed, step, T->traj_id, T->pb->problem, SPX_RNG_STEP, T->attempt, b);
-   spx_normals4(b, n);
+   normals4(b, n);
    do {
       if (k == 4) {
          spx_rng_block(T->pb->seed, step * 64u + (uint32_t)blk, T->traj_id, T->pb->problem, SPX_RNG_EXTRA, T->attempt, b);
-         spx_normals4(b, n);
+         normals4(b, n);
          blk++;
          k = 0;
       }
@@ -2245,11 +2336,67 @@ static void pa_scatter(trj_t* T, uint32_t step)
    T->mom.x[1] = mu_new;
 }
 
+/* RKStep, src/trajectory_base.cc:366-406: the step with the table's weights v, and for an adaptive
+ * table the lower-order position with the weights w, the error against rk_tol_abs + rk_tol_rel
+ * (|r| + |r_lo|), the next dt_adaptive and the rejection of a step whose error exceeds 1. Returns 1
+ * for a rejected step (FINISH is cleared, as the reference does). */
+static int rk_step(trj_t* T, const v3* slp, const v3* slm, const double* sla)
+{
+   const rk_t* R = T->rk;
+   v3 pos_lo = T->pos;
+   int il;
+   double err;
+   if (fwd(T)) T->t += T->dt; else T->t -= T->dt;
+   for (il = 0; il < R->stages; il++) {
+      if (fwd(T)) {
+         T->pos = vadd(T->pos, vscale(T->dt * R->v[il], slp[il]));
+         T->mom = vadd(T->mom, vscale(T->dt * R->v[il], slm[il]));
+         if (R->adaptive) pos_lo = vadd(pos_lo, vscale(T->dt * R->w[il], slp[il]));
+      }
+      else {
+         T->pos = vsub(T->pos, vscale(T->dt * R->v[il], slp[il]));
+         T->mom = vsub(T->mom, vscale(T->dt * R->v[il], slm[il]));
+         if (R->adaptive) pos_lo = vsub(pos_lo, vscale(T->dt * R->w[il], slp[il]));
+      }
+      if (sla) T->amp += T->dt * R->v[il] * sla[il] * exp(T->wgt);
+   }
+   T->vel = vel_cart(T->mom);
+   if (!R->adaptive) return 0;
+   err = RK_TOL_ABS + RK_TOL_REL * (vnorm(T->pos) + vnorm(pos_lo));
+   err = sqrt(vnorm2(vsub(T->pos, pos_lo)) / (err * err));
+   T->dt_adaptive = T->dt * RK_ADJUST * pow(err, -1.0 / R->order);
+   T->dt_adaptive = fmin(T->dt * RK_SAFETY, T->dt_adaptive);
+   T->dt_adaptive = fmax(T->dt / RK_SAFETY, T->dt_adaptive);
+   if (err > 1.0 + SP_TINY) {
+      T->status &= ~TRAJ_FINISH;
+      return 1;
+   }
+   return 0;
+}
+
+/* After a rejected step the next Advance starts with Load(), which puts back time, position and
+ * momentum of the last stored point (src/trajectory_base.hh:507-515); the amplitude and log-weight
+ * keep the rejected step's increments. The reference keeps the fields of the rejected step's last
+ * stage point too (nothing re-evaluates them before the next Slopes); with reference_quirks that is
+ * reproduced, else (deviation D6, shared with the CUDA kernels) the fields are those of the restored
+ * point, as at the start of the rejected step. */
+static uint64_t g_rejections = 0;  /* rejected steps of the last spx_oracle_run */
+
+static void rk_reject(trj_t* T)
+{
+   g_rejections++;
+   T->t = T->stored_t;
+   T->pos = T->stored_pos;
+   T->mom = T->stored_mom;
+   set_vel_load(T);
+   if (!T->o->reference_quirks) common_fields(T);
+}
+
 /* RKAdvance, src/trajectory_base.cc:545-579 (Lorentz and Focused) */
 static int rk_advance(trj_t* T)
 {
-   const rk_t* R = (T->o->rk == 25) ? &RK4 : &RK0;
-   v3 slp[4], slm[4];
+   const rk_t* R = T->rk;
+   v3 slp[SPX_RK_MAX_STAGES], slm[SPX_RK_MAX_STAGES];
    int is, il;
    int scatt = (T->o->traj_type == 205 && T->o->pa_scattering) || T->o->traj_type == 202 || T->o->traj_type == 204;
    int perp = is_guiding_diff(T);
@@ -2299,19 +2446,11 @@ static int rk_advance(trj_t* T)
       T->t = T->local_t; T->pos = T->local_pos; T->mom = T->local_mom; T->amp = T->local_amp; T->wgt = T->local_wgt;
       set_vel_load(T);
    }
-   /* RKStep */
-   if (fwd(T)) T->t += T->dt; else T->t -= T->dt;
-   for (il = 0; il < R->stages; il++) {
-      if (fwd(T)) {
-         T->pos = vadd(T->pos, vscale(T->dt * R->v[il], slp[il]));
-         T->mom = vadd(T->mom, vscale(T->dt * R->v[il], slm[il]));
-      }
-      else {
-         T->pos = vsub(T->pos, vscale(T->dt * R->v[il], slp[il]));
-         T->mom = vsub(T->mom, vscale(T->dt * R->v[il], slm[il]));
-      }
+   /* RKStep; a rejected step of an adaptive table is not taken */
+   if (rk_step(T, slp, slm, NULL)) {
+      rk_reject(T);
+      return 0;
    }
-   T->vel = vel_cart(T->mom);
    if (perp) T->pos = vadd(T->pos, T->dr_perp);
    handle_boundaries(T);
    if (!(T->status & TRAJ_FINISH)) {
@@ -2322,29 +2461,35 @@ static int rk_advance(trj_t* T)
    return 1;
 }
 
-/* TrajectoryParker::Advance, src/trajectory_parker.cc:255-306 */
+/* TrajectoryParker::Advance, src/trajectory_parker.cc:255-306, with any Butcher table: the slopes of
+ * the step's start, PhysicalStep, the stochastic displacement (EulerDiffSlopes), RKSlopes with the
+ * Parker slopes at each stage point (TrajectoryParkerSource evaluates its source there too,
+ * src/trajectory_parker_source.cc:58-66), RKStep, then the displacement. Returns 0 for a step an
+ * adaptive table rejected. */
 static int parker_advance(trj_t* T)
 {
-   v3 sp, sm, fa[3];
-   double sa, dWx, dWy, dWz;
+   const rk_t* R = T->rk;
+   v3 slp[SPX_RK_MAX_STAGES], slm[SPX_RK_MAX_STAGES], fa[3];
+   double sla[SPX_RK_MAX_STAGES], dWx, dWy, dWz;
    dstate st;
    uint32_t b[4];
    double n[4];
+   int is, il;
    set_vel_load(T);
    T->local_t = T->t; T->local_pos = T->pos; T->local_mom = T->mom; T->local_amp = T->amp; T->local_wgt = T->wgt;
-   if (parker_slopes(T, &sp, &sm, &sa)) return 1;
+   if (parker_slopes(T, &slp[0], &slm[0], &sla[0])) return 1;
    /* PhysicalStep, src/trajectory_parker.cc:212-221 */
    T->dt_physical = 0.5 * T->sp.dmax / vnorm(fwd(T) ? vadd(T->drift_vel, T->divK) : vsub(T->drift_vel, T->divK));
    T->dt_physical = fmin(T->dt_physical, 0.5 * (T->sp.dmax * T->sp.dmax) / fmax(T->Kperp, T->Kpara));
    T->dt_physical = fmin(T->dt_physical, 0.5 * 3.0 * 0.01 / fabs(sd_divU(&T->sp)));
    T->dt = fmin(T->dt_physical, T->dt_adaptive);
    time_proximity(T);
-   /* EulerDiffSlopes, src/trajectory_parker.cc:159-180 */
+   /* EulerDiffSlopes, src/trajectory_parker.cc:159-180: the trajectory's next three normals */
    fa[2] = T->sp.bhat;
    fa[0] = second_unit(T->sp.bhat);
    fa[1] = vcross(fa[2], fa[0]);
-   spx_rng_block(T->pb->seed, (uint32_t)T->segments, T->traj_id, T->pb->problem, SPX_RNG_STEP, T->attempt, b);
-   spx_normals4(b, n);
+   spx_rng_block(T->pb->seed, (uint32_t)(T->n_normal / 3), T->traj_id, T->pb->problem, SPX_RNG_STEP, T->attempt, b);
+   normals4(b, n);
    T->n_normal += 3;
    dWx = sqrt(T->dt) * n[0];
    dWy = sqrt(T->dt) * n[1];
@@ -2354,19 +2499,32 @@ static int parker_advance(trj_t* T)
    T->Kpara = get_component(T, 1, T->t, T->pos, T->mom, &T->sp, &st);
    T->dr_perp = V(sqrt(2.0 * T->Kperp) * dWx, sqrt(2.0 * T->Kperp) * dWy, sqrt(2.0 * T->Kpara) * dWz);
    T->dr_perp = from_basis(T->dr_perp, fa);
-   /* RKStep with the Euler table */
-   if (fwd(T)) {
-      T->t += T->dt;
-      T->pos = vadd(T->pos, vscale(T->dt * 1.0, sp));
-      T->mom = vadd(T->mom, vscale(T->dt * 1.0, sm));
+   /* RKSlopes */
+   for (is = 1; is < R->stages; is++) {
+      for (il = 0; il < is; il++) {
+         if (fwd(T)) {
+            T->t += R->a[is] * T->dt;
+            T->pos = vadd(T->pos, vscale(T->dt * R->b[is][il], slp[il]));
+            T->mom = vadd(T->mom, vscale(T->dt * R->b[is][il], slm[il]));
+         }
+         else {
+            T->t -= R->a[is] * T->dt;
+            T->pos = vsub(T->pos, vscale(T->dt * R->b[is][il], slp[il]));
+            T->mom = vsub(T->mom, vscale(T->dt * R->b[is][il], slm[il]));
+         }
+      }
+      if (space_terminate(T)) return 1;
+      if (common_fields(T)) return 1;
+      T->vel = vel_cart(T->mom);
+      if (parker_slopes(T, &slp[is], &slm[is], &sla[is])) return 1;
+      T->t = T->local_t; T->pos = T->local_pos; T->mom = T->local_mom; T->amp = T->local_amp; T->wgt = T->local_wgt;
+      set_vel_load(T);
    }
-   else {
-      T->t -= T->dt;
-      T->pos = vsub(T->pos, vscale(T->dt * 1.0, sp));
-      T->mom = vsub(T->mom, vscale(T->dt * 1.0, sm));
+   /* RKStep, then the stochastic displacement */
+   if (rk_step(T, slp, slm, sla)) {
+      rk_reject(T);
+      return 0;
    }
-   T->amp += T->dt * 1.0 * sa * exp(T->wgt);
-   T->vel = vel_cart(T->mom);
    T->pos = vadd(T->pos, T->dr_perp);
    handle_boundaries(T);
    if (!(T->status & TRAJ_FINISH)) if (common_fields(T)) return 1;
@@ -2391,6 +2549,7 @@ static int set_start(trj_t* T)
    T->mom = sample_mom(T, T->sp.bhat);
    set_vel_load(T);
    T->sp0 = T->sp;
+   T->bmag_min = T->bmag_max = T->sp.Bmag;
    T->dt_adaptive = SP_LARGE * T->sp.dmax / c;
    T->t0 = T->t; T->pos0 = T->pos; T->mom0 = T->mom;
    T->bactive_t = T->bactive_s = T->bactive_m = -1;
@@ -2408,6 +2567,8 @@ static int set_start(trj_t* T)
    }
    T->amp = 0.0;
    T->wgt = 0.0;
+   T->stored_t = T->t; T->stored_pos = T->pos; T->stored_mom = T->mom;
+   T->time_adaptations = 0;
    /* TrajectoryParkerSource::SetStart initialises the source (src/trajectory_parker_source.cc:43-50) */
    if (T->o->traj_type == 207 && T->pb->has_src) T->src_del_old = T->mom.x[0] - T->pb->src_p_inj;
    return 0;
@@ -2418,11 +2579,17 @@ static int integrate(trj_t* T)
 {
    double c = c_code();
    while (!(T->status & TRAJ_FINISH) && !(T->status & TRAJ_DISCARD)) {
-      if (is_parker(T)) parker_advance(T);
-      else rk_advance(T);
+      int advanced = is_parker(T) ? parker_advance(T) : rk_advance(T);
+      if (advanced) {  /* UpdateBmagExtrema with the fields the step ended with */
+         T->bmag_min = fmin(T->bmag_min, T->sp.Bmag);
+         T->bmag_max = fmax(T->bmag_max, T->sp.Bmag);
+      }
       if (T->error) return 1;
       if (T->status & TRAJ_DISCARD) return 1;
       if (T->segments > MAX_TRAJ_STEPS) { T->status |= TRAJ_DISCARD; return 1; }
+      /* consecutive steps an adaptive table rejected (src/trajectory_base.cc:969-979) */
+      if (advanced) T->time_adaptations = 0;
+      else if (++T->time_adaptations > MAX_TIME_ADAPTATIONS) { T->status |= TRAJ_DISCARD; return 1; }
       if (T->dt < SP_TINY * T->sp.dmax / c) { T->status |= TRAJ_DISCARD; return 1; }
       if (!isnormal(T->dt)) { T->status |= TRAJ_DISCARD; return 1; }
    }
@@ -2451,6 +2618,8 @@ int spx_oracle_run(const uint8_t* spec, size_t spec_len, const spx_oracle_opts* 
    uint32_t k;
    int d, rc = 0;
    if (!pb || !T) { free(pb); free(T); return -10; }
+   g_nudge_libm = opts->nudge_libm;
+   g_rejections = 0;
    rc = parse_spec(spec, spec_len, pb, err, err_len);
    if (rc) { free(pb); free(T); return rc; }
    if (!pb->has_bg || !pb->has_it || !pb->has_is || !pb->has_im || pb->nbt == 0) {
@@ -2467,6 +2636,15 @@ int spx_oracle_run(const uint8_t* spec, size_t spec_len, const spx_oracle_opts* 
    for (d = 0; d < pb->nd; d++) {
       pb->d[d].offset_bins = off;
       off += (int64_t)pb->d[d].n_bins[0] * pb->d[d].n_bins[1] * pb->d[d].n_bins[2];
+   }
+   {
+      static rk_t tab;
+      if (rk_load(opts->rk, &tab)) {
+         snprintf(err, err_len, "unknown Runge-Kutta table %d", opts->rk);
+         free(pb); free(T);
+         return -6;
+      }
+      T->rk = &tab;
    }
    T->pb = pb;
    T->o = opts;
@@ -2505,6 +2683,19 @@ int spx_oracle_run(const uint8_t* spec, size_t spec_len, const spx_oracle_opts* 
    free(T);
    return 0;
 }
+
+uint64_t spx_oracle_rejections(void) { return g_rejections; }
+
+#ifdef SPX_OPCOUNT
+/* the op-counting build (oracle/opcount.hh): the counts since the last reset */
+spx_opcount_t spx_opcount;
+void spx_oracle_opcount(uint64_t out[6])
+{
+   out[0] = spx_opcount.add; out[1] = spx_opcount.mul; out[2] = spx_opcount.div;
+   out[3] = spx_opcount.sqrt; out[4] = spx_opcount.trans; out[5] = spx_opcount.philox;
+   memset(&spx_opcount, 0, sizeof spx_opcount);
+}
+#endif
 
 void spx_oracle_normals(uint64_t seed, uint32_t index, uint32_t traj, uint32_t problem, uint32_t attempt, double out[4])
 {

@@ -32,16 +32,21 @@ typedef struct {
 typedef struct {
    int traj_type;          /* 200 Lorentz, 201-204 guiding centre, 205 Focused, 206 Parker, 207 Parker+source */
    int time_flow;          /* 0 forward, 1 backward */
-   int rk;                 /* Butcher table number of common/rk_config.hh (0 or 25) */
+   int rk;                 /* Butcher table number of common/rk_config.hh (any but 30) */
    int deriv_mode;         /* 0: the reference's compiled-in defaults; 1: analytic derivatives */
    double steps_per_orbit; /* Lorentz orbit resolution (reference: 100, src/trajectory_lorentz.hh:26) */
    int pa_scattering;      /* Focused: add the Euler pitch-angle scattering step */
    int max_attempts;       /* retries of a discarded trajectory (src/simulation.cc:262-288) */
-   int reference_quirks;   /* 1: reproduce deviation D1 as the reference has it (the smooth shock's dmax
-                              from the previous field evaluation), to compare with the reference's own
-                              output; 0: the corrected behaviour the CUDA kernels share */
+   int reference_quirks;   /* 1: reproduce deviations D1 (the smooth shock's dmax from the previous field
+                              evaluation) and D6 (after a rejected adaptive step, the fields of that step's
+                              last stage point) as the reference has them, to compare with the reference's
+                              own output; 0: the corrected behaviour the CUDA kernels share */
    int mu_method;          /* guiding-centre pitch-angle step: 0 Euler, 1 Milstein, 2 RK2 (STOCHASTIC_METHOD_MU) */
    int perp_method;        /* guiding-centre perpendicular step: 0 Euler, 1 Milstein, 2 RK2 (STOCHASTIC_METHOD_PERP) */
+   int nudge_libm;         /* 1: every normal deviate and every result of exp, log, pow, sin, cos, tanh and
+                              the inverse trigonometric functions one ulp larger in magnitude: a model of
+                              the last-bit differences between two libm implementations; the parity tests
+                              measure a problem's conditioning with it */
 } spx_oracle_opts;
 
 /*
@@ -53,6 +58,13 @@ typedef struct {
 int spx_oracle_run(const uint8_t* spec, size_t spec_len, const spx_oracle_opts* opts, uint32_t first,
                    uint32_t n, spx_oracle_traj* traj_out, int32_t* counts, double* sums, int64_t* n_events,
                    char* err, size_t err_len);
+
+/* Steps an adaptive Butcher table rejected during the last spx_oracle_run. */
+uint64_t spx_oracle_rejections(void);
+
+/* The op-counting build only (make -C oracle opcount): additions, multiplications, divisions, square
+ * roots, transcendental calls and Philox blocks since the previous call, which resets them. */
+void spx_oracle_opcount(uint64_t out[6]);
 
 /* Sizes of the distributions of a spec: returns the number of distributions, fills up to
  * "max" entries of n_bins[] and width[]. Negative on a malformed spec. */

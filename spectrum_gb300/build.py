@@ -41,14 +41,28 @@ def _newest_header() -> float:
 def _compile(src: str, nvcc: str, extra: list[str]) -> tuple[str, int, str]:
     obj = os.path.join(OBJ, os.path.splitext(src)[0] + ".o")
     path = os.path.join(CSRC, src)
-    if os.path.exists(obj) and os.path.getmtime(obj) >= max(os.path.getmtime(path), _newest_header()):
-        return obj, 0, ""
     lang = ["-x", "cu"] if src.endswith(".cu") else ["-x", "c++"]
     # The FP32 kernels use the hardware approximations of division, square root, log, exp, sin,
-    # cos and pow (relative errors of a few 1e-7); the FP64 kernels keep IEEE arithmetic.
-    fast = ["-use_fast_math"] if src.endswith("_f32.cu") else []
+    # cos and pow (relative errors of a few 1e-7). The FP64 kernels keep IEEE arithmetic and are
+    # compiled without multiply-add contraction, so every +, -, *, / and sqrt rounds as in the
+    # reference's own (uncontracted) build and in the oracle.
+    if src.endswith("_f32.cu"):
+        fast = ["-use_fast_math"]
+    elif src.endswith(("_f64.cu", "_f64fd.cu", "_f64rk.cu", "_f64fdrk.cu")):
+        fast = ["-fmad=false"]
+    else:
+        fast = []
     cmd = [nvcc, *lang, *ARCH, *CFLAGS, *fast, *extra, "-c", path, "-o", obj]
+    # an object is reused only if it is newer than its sources and was made by the same command
+    stamp = obj + ".cmd"
+    line = " ".join(cmd)
+    if (os.path.exists(obj) and os.path.exists(stamp) and open(stamp).read() == line
+            and os.path.getmtime(obj) >= max(os.path.getmtime(path), _newest_header())):
+        return obj, 0, ""
     r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode == 0:
+        with open(stamp, "w") as f:
+            f.write(line)
     return obj, r.returncode, r.stdout + r.stderr
 
 

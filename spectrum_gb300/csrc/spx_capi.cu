@@ -21,6 +21,7 @@
 #include "../../include/spx.h"
 #include "spx_launch.hh"
 #include "spx_parse.hh"
+#include "spx_rk_tables.h"
 
 static_assert(sizeof(spx_traj_record) == sizeof(spx::TrajRecord), "record layouts differ");
 
@@ -46,6 +47,10 @@ struct spx_ctx {
    cudaStream_t stream = nullptr;
    cudaEvent_t ev0 = nullptr, ev1 = nullptr;
    int traj = 0, flow = 0, rk = 0, precision = 0;
+   // the Butcher table: general (not Euler or, for the RK types, the classic RK4) tables run on the
+   // *_f64rk / *_f64fdrk kernels, which read it from constant memory
+   bool general_rk = false;
+   int rk_stages = 1, rk_order = 1, rk_adaptive = 0, rk_offset = 0;
    double steps_per_orbit = 100.0;
    int deriv_mode = 0, pa_scattering = 0, record_final = 0, max_attempts = 100, mu_method = 0, perp_method = 0;
    std::vector<PluginBlob> base;
@@ -73,7 +78,7 @@ struct spx_ctx {
    cudaGraphExec_t gexec = nullptr;
    cudaGraphNode_t gkernel = nullptr;
    cudaKernelNodeParams gparams{};
-   unsigned char gkey[160] = {};
+   unsigned char gkey[192] = {};
    // launch shape chosen by spx_autotune (used by spx_run when it gets no tuning)
    bool has_tuned = false;
    spx_tuning tuned{};
@@ -93,6 +98,9 @@ struct spx_ctx {
 };
 
 namespace {
+
+// the Butcher tables a context may select (spx_rk_tables.h)
+constexpr spx_rk_entry kRkIndex[SPX_RK_N_TABLES] = SPX_RK_INDEX_INIT;
 
 int cuda_err(cudaError_t e) { return e == cudaSuccess ? SPX_OK : (e == cudaErrorMemoryAllocation ? SPX_ERR_OUT_OF_MEMORY : SPX_ERR_CUDA); }
 
@@ -266,6 +274,15 @@ cudaError_t launch(spx_ctx* c, const spx::LaunchArgs& a)
 {
    const bool f64 = c->precision == SPX_FP64, fd = f64 && c->deriv_mode == 0;
    const int bg = c->bg_kind;
+   if (c->general_rk) {  // FP64 only (spx_create)
+      switch (c->traj) {
+      case SPX_TRAJ_PARKER:
+      case SPX_TRAJ_PARKER_SOURCE: return fd ? spx::launch_parker_f64fdrk(bg, a) : spx::launch_parker_f64rk(bg, a);
+      case SPX_TRAJ_LORENTZ: return fd ? spx::launch_lorentz_f64fdrk(bg, a) : spx::launch_lorentz_f64rk(bg, a);
+      case SPX_TRAJ_FOCUSED: return fd ? spx::launch_focused_f64fdrk(bg, a) : spx::launch_focused_f64rk(bg, a);
+      default: return fd ? spx::launch_guiding_f64fdrk(bg, a) : spx::launch_guiding_f64rk(bg, a);
+      }
+   }
    switch (c->traj) {
    case SPX_TRAJ_PARKER:
    case SPX_TRAJ_PARKER_SOURCE:
@@ -287,6 +304,19 @@ int occupancy(spx_ctx* c, int block, int slots)
 {
    const bool f64 = c->precision == SPX_FP64, fd = f64 && c->deriv_mode == 0;
    const int bg = c->bg_kind;
+   if (c->general_rk) {
+      switch (c->traj) {
+      case SPX_TRAJ_PARKER:
+      case SPX_TRAJ_PARKER_SOURCE:
+         return fd ? spx::occupancy_parker_f64fdrk(bg, block, slots) : spx::occupancy_parker_f64rk(bg, block, slots);
+      case SPX_TRAJ_LORENTZ:
+         return fd ? spx::occupancy_lorentz_f64fdrk(bg, block, slots) : spx::occupancy_lorentz_f64rk(bg, block, slots);
+      case SPX_TRAJ_FOCUSED:
+         return fd ? spx::occupancy_focused_f64fdrk(bg, block, slots) : spx::occupancy_focused_f64rk(bg, block, slots);
+      default:
+         return fd ? spx::occupancy_guiding_f64fdrk(bg, block, slots) : spx::occupancy_guiding_f64rk(bg, block, slots);
+      }
+   }
    switch (c->traj) {
    case SPX_TRAJ_PARKER:
    case SPX_TRAJ_PARKER_SOURCE:
@@ -317,6 +347,47 @@ int bnd_slots(const spx_ctx* c)
 }
 
 bool valid_ctx(spx_ctx* c) { return c != nullptr; }
+
+// the context's Butcher table, and whether |B| extrema are tracked (a problem has a
+// DistributionLossCone), in a run configuration
+void set_rk(const spx_ctx* c, spx::RunConfig& cfg)
+{
+   cfg.rk_stages = c->rk_stages;
+   cfg.rk_order = c->rk_order;
+   cfg.rk_adaptive = c->rk_adaptive;
+   cfg.rk_offset = c->rk_offset;
+   cfg.track_bmag = 0;
+   for (const auto& p : c->problems)
+      for (int d = 0; d < p.pd.nd; d++)
+         if (p.pd.d[d].kind == spx::kDsLossCone) cfg.track_bmag = 1;
+}
+
+// The launch shape of a run: the caller's, else the one spx_autotune chose, else the defaults (the
+// FP64 drop-in keeps one thread per trajectory; the FP32 stepper takes the persistent queue in
+// blocks of 64 refilled every 8 steps, the shape that measured fastest on the modulation batch).
+// Unset fields are completed and checked; blocks per SM is capped by the kernel's occupancy for
+// "slots" boundary states per lane. Shared by spx_run and spx_run_static.
+int resolve_tuning(spx_ctx* c, const spx_tuning* tuning, int slots, spx_tuning& tu)
+{
+   tu = spx_tuning{};
+   if (tuning) tu = *tuning;
+   else if (c->has_tuned) tu = c->tuned;
+   else {
+      tu.schedule = c->precision == SPX_MIXED ? 1 : 0;
+      if (tu.schedule) {
+         tu.block_size = 64;
+         tu.steps_per_sync = 8;
+      }
+   }
+   if (tu.schedule != 0 && tu.schedule != 1) return SPX_ERR_INVALID_ARG;
+   if (tu.block_size <= 0) tu.block_size = 128;
+   if (tu.block_size % 32 || tu.block_size > 128) return SPX_ERR_INVALID_ARG;
+   if (tu.steps_per_sync <= 0) tu.steps_per_sync = tu.schedule ? 16 : 1 << 30;
+   int occ = occupancy(c, tu.block_size, slots);
+   if (occ <= 0) occ = 1;
+   if (tu.blocks_per_sm <= 0 || tu.blocks_per_sm > occ) tu.blocks_per_sm = occ;
+   return SPX_OK;
+}
 
 
 // What a captured graph depends on: launch shape, the run configuration apart from the run
@@ -440,6 +511,7 @@ const char* distro_class_name(int kind)
    case spx::kDsCumulative1: return "DistributionPositionCumulativeOrder1";
    case spx::kDsCumulative2: return "DistributionPositionCumulativeOrder2";
    case spx::kDsDivergenceFlow: return "DistributionDivergenceFlowPowerLaw";
+   case spx::kDsLossCone: return "DistributionLossCone";
    case spx::kDsTimeMu: return "DistributionTimeMu";  // a class of this library only
    default: return nullptr;
    }
@@ -464,10 +536,17 @@ int spx_create(spx_ctx_t* out, int traj_kind, int time_flow, int rk_method, int 
       return SPX_ERR_INVALID_ARG;
    if (time_flow != SPX_FORWARD && time_flow != SPX_BACKWARD) return SPX_ERR_INVALID_ARG;
    if (precision != SPX_FP64 && precision != SPX_MIXED) return SPX_ERR_INVALID_ARG;
-   // Parker is an Euler-Maruyama scheme (RK table 0, src/trajectory_parker.cc:415-419); the RK
-   // trajectories take table 0 or the classic fourth-order table 25.
-   if ((traj_kind == SPX_TRAJ_PARKER || traj_kind == SPX_TRAJ_PARKER_SOURCE) && rk_method != 0) return SPX_ERR_INVALID_ARG;
-   if (rk_method != 0 && rk_method != 25) return SPX_ERR_INVALID_ARG;
+   // The Butcher table (RK_INTEGRATOR_TYPE, common/rk_config.hh:72-520): any of the reference's tables
+   // but 30, which does not compile there. Euler, and the classic RK4 for the RK types, run on kernels
+   // with the coefficients unrolled, in both arithmetics; the other tables run on the FP64 kernels of
+   // any table (their error control works at the reference's 1e-9 tolerance, which FP32 cannot reach).
+   const spx_rk_entry* tab = nullptr;
+   for (const auto& e : kRkIndex)
+      if (e.number == rk_method) tab = &e;
+   if (!tab) return SPX_ERR_INVALID_ARG;
+   const bool parker = traj_kind == SPX_TRAJ_PARKER || traj_kind == SPX_TRAJ_PARKER_SOURCE;
+   const bool general = !(rk_method == 0 || (rk_method == 25 && !parker));
+   if (general && precision != SPX_FP64) return SPX_ERR_INVALID_ARG;
    int ndev = 0;
    if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) {
       cudaGetLastError();
@@ -482,6 +561,11 @@ int spx_create(spx_ctx_t* out, int traj_kind, int time_flow, int rk_method, int 
    c->traj = traj_kind;
    c->flow = time_flow;
    c->rk = rk_method;
+   c->general_rk = general;
+   c->rk_stages = tab->stages;
+   c->rk_order = tab->order;
+   c->rk_adaptive = tab->adaptive;
+   c->rk_offset = tab->offset;
    c->precision = precision;
    if (precision == SPX_MIXED) c->deriv_mode = 1;
    // TrajectoryGuidingScatt is the guiding-centre stepper with its pitch-angle step always on
@@ -660,26 +744,10 @@ int spx_run(spx_ctx_t c, const spx_tuning* tuning)
       int rc = upload(c);
       if (rc != SPX_OK) return rc;
    }
-   spx_tuning tu{};
-   if (tuning) tu = *tuning;
-   else if (c->has_tuned) tu = c->tuned;  // chosen by spx_autotune
-   else {
-      // untuned defaults: the FP64 drop-in keeps one thread per trajectory; the FP32 stepper takes
-      // the persistent queue with the shape that measured fastest on the modulation batch
-      tu.schedule = c->precision == SPX_MIXED ? 1 : 0;
-      if (tu.schedule) {
-         tu.block_size = 64;
-         tu.steps_per_sync = 8;
-      }
-   }
-   if (tu.schedule != 0 && tu.schedule != 1) return SPX_ERR_INVALID_ARG;
-   if (tu.block_size <= 0) tu.block_size = 128;
-   if (tu.block_size % 32 || tu.block_size > 128) return SPX_ERR_INVALID_ARG;
-   if (tu.steps_per_sync <= 0) tu.steps_per_sync = tu.schedule ? 16 : 1 << 30;
+   spx_tuning tu;
    const int slots = bnd_slots(c);
-   int occ = occupancy(c, tu.block_size, slots);
-   if (occ <= 0) occ = 1;
-   if (tu.blocks_per_sm <= 0 || tu.blocks_per_sm > occ) tu.blocks_per_sm = occ;
+   const int trc = resolve_tuning(c, tuning, slots, tu);
+   if (trc != SPX_OK) return trc;
    spx::LaunchArgs a;
    a.block = dim3(tu.block_size);
    int64_t grid;
@@ -693,6 +761,7 @@ int spx_run(spx_ctx_t c, const spx_tuning* tuning)
    a.cfg.traj_kind = c->traj;
    a.cfg.time_flow = c->flow;
    a.cfg.rk = c->rk;
+   set_rk(c, a.cfg);
    a.cfg.deriv_mode = c->deriv_mode;
    a.cfg.pa_scattering = c->pa_scattering;
    a.cfg.mu_method = c->mu_method;
@@ -811,6 +880,7 @@ int spx_autotune(spx_ctx_t c, int64_t sample_traj, spx_tuning* best)
       a.cfg.traj_kind = c->traj;
       a.cfg.time_flow = c->flow;
       a.cfg.rk = c->rk;
+      set_rk(c, a.cfg);
       a.cfg.deriv_mode = c->deriv_mode;
       a.cfg.pa_scattering = c->pa_scattering;
       a.cfg.mu_method = c->mu_method;
@@ -1326,19 +1396,11 @@ int spx_run_static(spx_ctx_t c, const spx_tuning* tuning, int32_t* counts, int64
    int rc = static_scratch(c->device, &scratch);
    if (rc != SPX_OK) return rc;
 
-   // launch shape: the defaults of spx_run
-   spx_tuning tu{};
-   if (tuning) tu = *tuning;
-   if (tu.schedule != 0 && tu.schedule != 1) return SPX_ERR_INVALID_ARG;
-   if (tu.block_size <= 0) tu.block_size = 128;
-   if (tu.block_size % 32 || tu.block_size > 128) return SPX_ERR_INVALID_ARG;
-   if (!tuning) tu.schedule = c->precision == SPX_MIXED ? 1 : 0;
-   if (tu.steps_per_sync <= 0) tu.steps_per_sync = tu.schedule ? 16 : 1 << 30;
-   int slots = 1;
-   for (int k = 0; k < n; k++) slots = std::max(slots, hd[k].nbt + hd[k].nbs + hd[k].nbm);
-   int occ = occupancy(c, tu.block_size, slots);
-   if (occ <= 0) occ = 1;
-   if (tu.blocks_per_sm <= 0 || tu.blocks_per_sm > occ) tu.blocks_per_sm = occ;
+   // launch shape: chosen as spx_run chooses it (the caller's, the autotuned one, or the defaults)
+   spx_tuning tu;
+   const int slots = bnd_slots(c);
+   rc = resolve_tuning(c, tuning, slots, tu);
+   if (rc != SPX_OK) return rc;
    int64_t grid = tu.schedule == 1 ? (int64_t)c->sm_count * tu.blocks_per_sm : (total + tu.block_size - 1) / tu.block_size;
    grid = std::max<int64_t>(1, std::min<int64_t>(grid, 0x7fffffff));
 
@@ -1364,6 +1426,7 @@ int spx_run_static(spx_ctx_t c, const spx_tuning* tuning, int32_t* counts, int64
    a.cfg.traj_kind = c->traj;
    a.cfg.time_flow = c->flow;
    a.cfg.rk = c->rk;
+   set_rk(c, a.cfg);
    a.cfg.deriv_mode = c->deriv_mode;
    a.cfg.pa_scattering = c->pa_scattering;
    a.cfg.mu_method = c->mu_method;

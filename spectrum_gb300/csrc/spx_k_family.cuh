@@ -1,6 +1,7 @@
 // spx_k_family.cuh -- launch and occupancy entry points of the stepping kernel for one
-// trajectory family, arithmetic and field-derivative method, switching over the background
-// classes. Each spx_k_*.cu instantiates it once, so the twelve kernel sets compile in parallel.
+// trajectory family, arithmetic, field-derivative method and table kind (Euler and the classic RK4
+// with unrolled constants, or any Butcher table from constant memory), switching over the background
+// classes. Each spx_k_*.cu instantiates it once, so the twenty kernel sets compile in parallel.
 #pragma once
 
 #include "spx_launch.hh"
@@ -8,7 +9,7 @@
 
 namespace spx {
 
-template <int TT, class R, int DM>
+template <int TT, class R, int DM, bool GT>
 struct FamilyTU {
    // dynamic shared memory: the boundary states of every lane of a block
    static size_t smem(int slots, int block) { return (size_t)(slots > 0 ? slots : 1) * block * sizeof(BndState<R>); }
@@ -22,7 +23,7 @@ struct FamilyTU {
    {
       if constexpr (kBuilt<BG>) {
          const auto* P = static_cast<const ProblemDescT<R>*>(a.problems_r);
-         step_kernel<TT, BG, R, DM><<<a.grid, a.block, smem(a.bnd_slots, a.block.x), a.stream>>>(
+         step_kernel<TT, BG, R, DM, GT><<<a.grid, a.block, smem(a.bnd_slots, a.block.x), a.stream>>>(
              P, a.problems_d, a.cfg, a.ctr, a.counts, a.sums, a.n_events, a.records, a.queue);
          return cudaGetLastError();
       }
@@ -34,7 +35,7 @@ struct FamilyTU {
    {
       int n = 0;
       if constexpr (kBuilt<BG>) {
-         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<TT, BG, R, DM>, block, smem(slots, block)) !=
+         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<TT, BG, R, DM, GT>, block, smem(slots, block)) !=
              cudaSuccess)
             n = 0;
       }
@@ -70,10 +71,11 @@ struct FamilyTU {
 
 }  // namespace spx
 
-// One translation unit: the kernels of one family, arithmetic and derivative method (DM 1:
-// analytic field derivatives; DM 0: the reference's compiled-in numerical ones, FP64 only).
-#define SPX_FAMILY_TU(fam, prec, TT, R, DM)                                                                    \
-   namespace spx {                                                                                              \
-   cudaError_t launch_##fam##_##prec(int bg, const LaunchArgs& a) { return FamilyTU<TT, R, DM>::launch(bg, a); } \
-   int occupancy_##fam##_##prec(int bg, int block, int slots) { return FamilyTU<TT, R, DM>::occupancy(bg, block, slots); } \
+// One translation unit: the kernels of one family, arithmetic, derivative method (DM 1: analytic
+// field derivatives; DM 0: the reference's compiled-in numerical ones, FP64 only) and table kind
+// (GT 1: any Butcher table, FP64 only).
+#define SPX_FAMILY_TU(fam, prec, TT, R, DM, GT)                                                                    \
+   namespace spx {                                                                                                  \
+   cudaError_t launch_##fam##_##prec(int bg, const LaunchArgs& a) { return FamilyTU<TT, R, DM, GT>::launch(bg, a); } \
+   int occupancy_##fam##_##prec(int bg, int block, int slots) { return FamilyTU<TT, R, DM, GT>::occupancy(bg, block, slots); } \
    }

@@ -2,4 +2,4 @@
 // derivatives, one per background.
 #include "spx_k_family.cuh"
 
-SPX_FAMILY_TU(focused, f64, kFocused, double, 1)
+SPX_FAMILY_TU(focused, f64, kFocused, double, 1, false)

@@ -2,4 +2,4 @@
 // TrajectoryGuidingScatt) in float arithmetic (analytic field derivatives), one per static background.
 #include "spx_k_family.cuh"
 
-SPX_FAMILY_TU(guiding, f32, kGuiding, float, 1)
+SPX_FAMILY_TU(guiding, f32, kGuiding, float, 1, false)

@@ -2,4 +2,4 @@
 // TrajectoryGuidingScatt) in double arithmetic (analytic field derivatives), one per static background.
 #include "spx_k_family.cuh"
 
-SPX_FAMILY_TU(guiding, f64, kGuiding, double, 1)
+SPX_FAMILY_TU(guiding, f64, kGuiding, double, 1, false)

@@ -2,4 +2,4 @@
 // TrajectoryGuidingScatt) in double arithmetic with the reference's numerical field derivatives, one per static background.
 #include "spx_k_family.cuh"
 
-SPX_FAMILY_TU(guiding, f64fd, kGuiding, double, 0)
+SPX_FAMILY_TU(guiding, f64fd, kGuiding, double, 0, false)

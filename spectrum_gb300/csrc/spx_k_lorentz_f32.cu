@@ -2,4 +2,4 @@
 // one per background.
 #include "spx_k_family.cuh"
 
-SPX_FAMILY_TU(lorentz, f32, kLorentz, float, 1)
+SPX_FAMILY_TU(lorentz, f32, kLorentz, float, 1, false)

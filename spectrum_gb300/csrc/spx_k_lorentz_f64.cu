@@ -2,4 +2,4 @@
 // derivatives, one per background.
 #include "spx_k_family.cuh"
 
-SPX_FAMILY_TU(lorentz, f64, kLorentz, double, 1)
+SPX_FAMILY_TU(lorentz, f64, kLorentz, double, 1, false)

@@ -2,4 +2,4 @@
 // compiled-in numerical field derivatives, one per background.
 #include "spx_k_family.cuh"
 
-SPX_FAMILY_TU(lorentz, f64fd, kLorentz, double, 0)
+SPX_FAMILY_TU(lorentz, f64fd, kLorentz, double, 0, false)

@@ -1,5 +1,6 @@
 // spx_launch.hh -- host entry points of the stepping kernels, one translation unit per trajectory
-// family, arithmetic and (FP64) field-derivative method so they compile in parallel.
+// family, arithmetic, (FP64) field-derivative method and table kind so they compile in parallel.
+// The *_f64rk and *_f64fdrk kernels take any Butcher table; the others Euler and the classic RK4.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -27,9 +28,13 @@ struct LaunchArgs {
    cudaError_t launch_##fam##_f64(int bg, const LaunchArgs& a);        \
    cudaError_t launch_##fam##_f64fd(int bg, const LaunchArgs& a);      \
    cudaError_t launch_##fam##_f32(int bg, const LaunchArgs& a);        \
+   cudaError_t launch_##fam##_f64rk(int bg, const LaunchArgs& a);      \
+   cudaError_t launch_##fam##_f64fdrk(int bg, const LaunchArgs& a);    \
    int occupancy_##fam##_f64(int bg, int block, int slots);            \
    int occupancy_##fam##_f64fd(int bg, int block, int slots);          \
-   int occupancy_##fam##_f32(int bg, int block, int slots);
+   int occupancy_##fam##_f32(int bg, int block, int slots);            \
+   int occupancy_##fam##_f64rk(int bg, int block, int slots);          \
+   int occupancy_##fam##_f64fdrk(int bg, int block, int slots);
 SPX_DECLARE_FAMILY(parker)
 SPX_DECLARE_FAMILY(lorentz)
 SPX_DECLARE_FAMILY(focused)

@@ -49,7 +49,7 @@ enum IniKind : int {
 
 enum DistKind : int {
    kDsTimeUniform = 1, kDsPositionUniform, kDsMomentumUniform, kDsPositionMomentumUniform, kDsSpectrumPowerLaw,
-   kDsSpectrumBentPowerLaw, kDsCumulative1, kDsCumulative2, kDsDivergenceFlow, kDsTimeMu = 20
+   kDsSpectrumBentPowerLaw, kDsCumulative1, kDsCumulative2, kDsDivergenceFlow, kDsLossCone, kDsTimeMu = 20
 };
 
 template <class R>
@@ -171,6 +171,12 @@ struct RunConfig {
    int perp_method;           // guiding-centre perpendicular step: 0 Euler, 1 Milstein, 2 RK2 (STOCHASTIC_METHOD_PERP)
    int64_t total_traj;
    int64_t run_index;         // trajectory ids of run r are r * n_traj + local (new streams per run)
+   // the Butcher table of the general-table kernels: stages, order, adaptive, and the offset of its
+   // coefficients in the shared table (spx_rk_tables.h)
+   int rk_stages, rk_order, rk_adaptive, rk_offset;
+   // 1 when a problem has a DistributionLossCone: the |B| extrema along each trajectory are tracked
+   // (the reference's RECORD_BMAG_EXTREMA build, src/trajectory_base.cc:581-592)
+   int track_bmag;
 };
 
 // Device-side counters of one run (scratch memory, zeroed before each launch).

@@ -358,7 +358,7 @@ int parse_distribution(Reader& r, int kind, DistParams& d)
 {
    std::memset(&d, 0, sizeof d);
    d.kind = kind;
-   d.width = (kind == kDsCumulative1) ? 3 : (kind == kDsCumulative2 ? 9 : 1);
+   d.width = (kind == kDsCumulative1 || kind == kDsLossCone) ? 3 : (kind == kDsCumulative2 ? 9 : 1);
    double mn[3], mx[3];
    // DistributionTemplated::SetupDistribution, src/distribution_templated.cc:92-137
    r.mi(d.n_bins);
@@ -403,6 +403,12 @@ int parse_distribution(Reader& r, int kind, DistParams& d)
       break;
    case kDsCumulative1: case kDsCumulative2: d.n_actions = 1; break;
    case kDsDivergenceFlow: d.A0 = r.d(); d.pow_law = r.d(); d.val_cold = r.d(); d.n_actions = 2; break;
+   case kDsLossCone:  // src/distribution_other.cc:826-840: one action, all three dimensions active
+      d.val_time = r.i();
+      d.val_coord = r.i();
+      d.n_actions = 1;
+      if (d.dims != 7) return SPX_ERR_BAD_BLOB;
+      break;
    default:
       return SPX_ERR_UNKNOWN_PLUGIN;
    }

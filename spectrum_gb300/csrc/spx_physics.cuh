@@ -785,7 +785,11 @@ __device__ __forceinline__ void eval_bnd(const BndParamsT<R>& b, BndState<R>& st
          if (rd < b.r1 || rd > b.r2) st.delta_old = st.delta;
       }
       break;
-   case kBtMirror: st.delta = (traj == kFocused) ? mom.x * mom.y : dot(mom, bhat); break;
+   // BoundaryMirror::EvaluateBoundary (src/boundary_momentum.cc:329-339): the parallel momentum, which is
+   // p mu for Focused, the native third component for the guiding-centre types and p . bhat for Lorentz
+   case kBtMirror:
+      st.delta = (traj == kFocused) ? mom.x * mom.y : (traj == kGuiding ? mom.z : dot(mom, bhat));
+      break;
    }
 }
 

@@ -12,6 +12,7 @@
 #pragma once
 
 #include "spx_physics.cuh"
+#include "spx_rk_tables.h"
 
 namespace spx {
 
@@ -27,7 +28,9 @@ template <class R, class A>
 struct Lane {
    int prob;
    uint32_t traj_id, attempt, steps, status;
-   uint32_t nrm;     // GuidingScatt: normals drawn so far (the k-th is the first of step block k)
+   uint32_t nrm;     // GuidingScatt: normals drawn so far (the k-th is the first of step block k); Parker with
+                     // a general Butcher table: step blocks drawn so far (rejected steps draw too)
+   uint32_t n_adapt; // general Butcher tables: consecutive rejected steps
    A t;
    AV3<A> pos, mom;  // mom: Parker (p,-,-), Focused (p, mu, -), Lorentz (px, py, pz), Guiding (p_perp, -, p_para)
    R amp, wgt, dt, dt_adapt, src_del_old;
@@ -37,6 +40,9 @@ struct Lane {
 struct Start {
    double t0;
    V3<double> pos0, mom0, bhat0;
+   // |B| at the first point and its extrema along the trajectory (DistributionLossCone; tracked only
+   // with RunConfig::track_bmag)
+   double bmag0, bmag_min, bmag_max;
    uint32_t nuni;  // guiding types: uniforms drawn so far, set-up included (the perpendicular Milstein and RK2
                    // schemes draw one a step); kept here, with the lane's other memory-resident state
 };
@@ -227,7 +233,7 @@ static __device__ __noinline__ V3<double> sample_mom(InitRng& rng, const Problem
 struct EventPoint {
    double t;
    V3<double> pos, mom, bhat;
-   double divU, amp, wgt;
+   double divU, amp, wgt, bmag;
 };
 
 static __device__ __noinline__ void process_event(int traj, const EventPoint& e, const Start& s0, const ProblemDesc& P,
@@ -242,7 +248,7 @@ static __device__ __noinline__ void process_event(int traj, const EventPoint& e,
    double w[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
    switch (d.kind) {
    case kDsTimeUniform: value.x = d.val_time == 0 ? s0.t0 : e.t; break;
-   case kDsPositionUniform:
+   case kDsPositionUniform: case kDsLossCone:
       value = d.val_time == 0 ? s0.pos0 : e.pos;
       if (d.val_coord == 1) {  // Metric<SphericalRTP>::PosToCurv, common/coordinates.hh:124-135
          double r = norm(value), phi = atan2(value.y, value.x);
@@ -295,6 +301,11 @@ static __device__ __noinline__ void process_event(int traj, const EventPoint& e,
       break;
    }
    case kDsDivergenceFlow: w[0] = action == 0 ? d.A0 * pow(fabs(e.divU), d.pow_law) : d.val_cold; break;
+   case kDsLossCone:  // DistributionLossCone::RecordLossCone, src/distribution_other.cc:858-862
+      w[0] = s0.bmag_min;
+      w[1] = s0.bmag_max;
+      w[2] = asin(sqrt((d.val_time == 0 ? s0.bmag0 : e.bmag) / s0.bmag_max));
+      break;
    }
    // AddRecord follows AddEvent for every processed event, outliers included (src/distribution_base.cc:192-193)
    if (d.rec_n) {
@@ -337,6 +348,7 @@ __device__ __forceinline__ EventPoint event_point(const Lane<R, A>& L, const SD<
    e.mom = mk(acc_dbl(L.mom.x), acc_dbl(L.mom.y), acc_dbl(L.mom.z));
    e.bhat = mk((double)sp.bhat.x, (double)sp.bhat.y, (double)sp.bhat.z);
    e.divU = (double)sd_divU(sp);
+   e.bmag = (double)sp.Bmag;
    e.amp = (double)L.amp;
    e.wgt = (double)L.wgt;
    return e;
@@ -479,6 +491,18 @@ __device__ __forceinline__ R time_proximity(R dt, R dmax, BndView<R> bv, int nbt
    return dt;
 }
 
+// UpdateBmagExtrema (src/trajectory_base.cc:586-592) of the previous step: the reference folds in the
+// fields each advanced step ends with, which are this step's start fields; a retried step's start was
+// folded in already.
+template <class R>
+__device__ __forceinline__ void track_bmag(Start& s0, const RunConfig& cfg, const SD<R>& sp)
+{
+   if (cfg.track_bmag) {
+      s0.bmag_min = fmin(s0.bmag_min, (double)sp.Bmag);
+      s0.bmag_max = fmax(s0.bmag_max, (double)sp.Bmag);
+   }
+}
+
 // Integrate's time-step check (src/trajectory_base.cc:979-983) of the previous step: dt against the
 // dmax of the point where that step ended. That point is where this step starts, so the dmax of
 // this step's field evaluation is the same number the reference compares with; a failed check
@@ -522,7 +546,7 @@ __device__ __noinline__ bool parker_divk_fd(const ProblemDescT<R>& P, int deriv_
 }
 
 template <int BG, class R, class A>
-__device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, const Start& s0,
+__device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, Start& s0,
                                                const ProblemDescT<R>& P, const ProblemDesc& Pd, const RunConfig& cfg,
                                                const Sinks& S)
 {
@@ -536,6 +560,7 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, con
    const unsigned mask = traj_mask<kParker>() | (kappa_grad_is_analytic(P.df) ? kDerivedOnly : 0u);
    if (!get_fields<BG>(P.bg, deriv_mode, t, pos, p, mask, sp)) { L.status |= TRAJ_DISCARD; return; }
    if (!prev_step_ok(L, sp.dmax)) return;
+   track_bmag(s0, cfg, sp);
    R vmag = vel_of(p);
    // DiffusionCoeff (src/trajectory_parker.cc:83-153)
    Kap<R> K = kappa_pp(P.df, pos, p, vmag, kap_in(sp));
@@ -618,12 +643,201 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, con
 }
 
 // ---- Runge-Kutta advance for Lorentz and Focused (src/trajectory_base.cc:315-406, 545-579) ----
-template <class R> __device__ __forceinline__ R rk_a(int s) { return s == 0 ? R(0) : (s == 3 ? R(1) : R(0.5)); }
-template <class R> __device__ __forceinline__ R rk_b(int s, int l)
+// Butcher tables. FixedRk: Euler (S = 1) and the classic fourth-order table (S = 4), with their
+// coefficients as constants so that every stage unrolls into registers. TableRk: any table of
+// spx_rk_tables.h (the general-table FP64 kernels), read from constant memory; its slopes live in
+// local memory and its adaptive tables estimate the error and reject steps (RKStep,
+// src/trajectory_base.cc:366-406).
+template <int S>
+struct FixedRk {
+   static constexpr int kMax = S;
+   static constexpr bool kGeneral = false;
+   __host__ __device__ static constexpr int stages() { return S; }
+   template <class R> __device__ __forceinline__ R a(int s) const { return s == 0 ? R(0) : (s == 3 ? R(1) : R(0.5)); }
+   template <class R> __device__ __forceinline__ R b(int s, int l) const
+   {
+      return (s == 1 && l == 0) ? R(0.5) : ((s == 2 && l == 1) ? R(0.5) : ((s == 3 && l == 2) ? R(1) : R(0)));
+   }
+   template <class R> __device__ __forceinline__ R v(int l) const
+   {
+      return S == 1 ? R(1) : ((l == 0 || l == 3) ? R(1.0 / 6.0) : R(1.0 / 3.0));
+   }
+};
+
+static __constant__ double c_rk_coeffs[] = SPX_RK_COEFFS_INIT;
+
+struct TableRk {
+   static constexpr int kMax = SPX_RK_MAX_STAGES;
+   static constexpr bool kGeneral = true;
+   int s, order, adaptive, off;
+   __device__ __forceinline__ int stages() const { return s; }
+   template <class R> __device__ __forceinline__ R a(int i) const { return (R)c_rk_coeffs[off + i]; }
+   template <class R> __device__ __forceinline__ R b(int i, int j) const { return (R)c_rk_coeffs[off + s + i * (i - 1) / 2 + j]; }
+   template <class R> __device__ __forceinline__ R v(int j) const { return (R)c_rk_coeffs[off + s + s * (s - 1) / 2 + j]; }
+   template <class R> __device__ __forceinline__ R w(int j) const { return (R)c_rk_coeffs[off + 2 * s + s * (s - 1) / 2 + j]; }
+};
+
+// RKStep's adaptive control (common/rk_config.hh:25-34, src/trajectory_base.cc:391-404): the error
+// of the step's position against its lower-order estimate, the next dt_adaptive, and whether the
+// step is rejected. Consecutive rejections beyond max_time_adaptations (src/trajectory_base.hh:41)
+// discard the attempt.
+template <class R, class A>
+__device__ __forceinline__ bool rk_rejects(Lane<R, A>& L, V3<R> pos, V3<R> pos_lo, int order)
 {
-   return (s == 1 && l == 0) ? R(0.5) : ((s == 2 && l == 1) ? R(0.5) : ((s == 3 && l == 2) ? R(1) : R(0)));
+   R e = R(1e-9) + R(1e-9) * (norm(pos) + norm(pos_lo));
+   e = m_sqrt(norm2(pos - pos_lo) / (e * e));
+   L.dt_adapt = L.dt * R(0.995) * m_pow(e, R(-1) / R(order));
+   L.dt_adapt = m_min(L.dt * R(2), L.dt_adapt);
+   L.dt_adapt = m_max(L.dt / R(2), L.dt_adapt);
+   if (e > R(1) + Lim<R>::tiny) {
+      L.status &= ~TRAJ_FINISH;
+      if (++L.n_adapt > 100u) L.status |= TRAJ_DISCARD;
+      return true;
+   }
+   L.n_adapt = 0;
+   return false;
 }
-template <class R> __device__ __forceinline__ R rk_v(int l) { return (l == 0 || l == 3) ? R(1.0 / 6.0) : R(1.0 / 3.0); }
+
+// ---- Parker with any Butcher table (src/trajectory_parker.cc:255-306) ---------------------------
+// TrajectoryParker::Slopes at one point (src/trajectory_parker.cc:229-245): DriftCoeff, DiffusionCoeff
+// (the divergence of the diffusion tensor by central differences in the reference's derivative
+// method, else from the analytic gradients), the position slope U +- div K and the momentum slope
+// -p div U / 3.
+template <int BG, class R>
+__device__ __forceinline__ bool parker_slopes(const ProblemDescT<R>& P, int deriv_mode, R t, V3<R> pos, R p,
+                                              const SD<R>& sp, bool fwd, Kap<R>& K, V3<R>& slope, R& slope_p)
+{
+   const R vmag = vel_of(p);
+   K = kappa_pp(P.df, pos, p, vmag, kap_in(sp));
+   V3<R> divK;
+   if (sizeof(R) == sizeof(double) && deriv_mode == 0) {
+      if (!parker_divk_fd<BG>(P, deriv_mode, t, pos, p, vmag, sp, divK)) return false;
+   }
+   else {
+      V3<R> gpe, gpa;
+      kappa_grad(P.df, pos, p, vmag, sp, K, gpe, gpa);
+      V3<R> t1 = gpa - gpe;
+      divK = (gpe + dot(sp.bhat, t1) * sp.bhat) + (K.para - K.perp) * (sd_divbhat(sp) * sp.bhat + sd_b_gradbhat(sp));
+   }
+   slope = fwd ? sp.U + divK : sp.U - divK;
+   slope_p = -p * sd_divU(sp) / R(3);
+   return true;
+}
+
+// The amplitude slope of TrajectoryParkerSource at one point (src/trajectory_parker_source.cc:58-66,
+// src/source_other.cc:41-59, 113-119, 166-177): the source's rate with the lane's dt; the injection
+// sources remember the momentum of their last evaluation, the stage points' included.
+template <class R, class A>
+__device__ __forceinline__ R parker_source(Lane<R, A>& L, const ProblemDescT<R>& P, R p, V3<R> pos)
+{
+   R sa = R(0);
+   if (P.src.kind == 1) sa = P.src.rate;
+   else if (P.src.kind >= 2) {
+      const R del = p - P.src.p_inj;
+      if (del * L.src_del_old < R(0)) {
+         if (P.src.kind == 2) sa = P.src.rate / L.dt;
+         else {
+            const R r = norm(pos - ld3(P.src.r0));
+            if (P.src.r_sh <= r && r <= P.src.r_sh + P.src.w_sh) sa = P.src.rate / L.dt;
+         }
+      }
+      L.src_del_old = del;
+   }
+   return sa;
+}
+
+// The slopes of the step's start, PhysicalStep, the stochastic displacement (EulerDiffSlopes, with
+// the trajectory's next step block: a rejected step draws one too, as the reference draws its next
+// three normals), RKSlopes with the Parker slopes at every stage point, RKStep (an adaptive table may
+// reject the step), then the displacement and the boundaries. FP64 only.
+template <int BG, class R, class A>
+__device__ __forceinline__ void parker_advance_gt(Lane<R, A>& L, BndView<R> bv, Start& s0, const ProblemDescT<R>& P,
+                                                  const ProblemDesc& Pd, const RunConfig& cfg, const Sinks& S,
+                                                  const TableRk tab)
+{
+   const bool fwd = cfg.time_flow == 0;
+   const int deriv_mode = cfg.deriv_mode;
+   const unsigned mask = traj_mask<kParker>() | (kappa_grad_is_analytic(P.df) ? kDerivedOnly : 0u);
+   const A t_loc = L.t;
+   const AV3<A> pos_loc = L.pos, mom_loc = L.mom;
+   const V3<R> pos = val3<R>(L.pos);
+   const R p = (R)acc_val(L.mom.x);
+   SD<R> sp;
+   if (!get_fields<BG>(P.bg, deriv_mode, (R)acc_val(L.t), pos, p, mask, sp)) { L.status |= TRAJ_DISCARD; return; }
+   if (!prev_step_ok(L, sp.dmax)) return;
+   track_bmag(s0, cfg, sp);
+   V3<R> slp[SPX_RK_MAX_STAGES];
+   R slm[SPX_RK_MAX_STAGES], sla[SPX_RK_MAX_STAGES];
+   Kap<R> K;
+   if (!parker_slopes<BG>(P, deriv_mode, (R)acc_val(L.t), pos, p, sp, fwd, K, slp[0], slm[0])) {
+      L.status |= TRAJ_DISCARD;
+      return;
+   }
+   sla[0] = parker_source(L, P, p, pos);  // with the previous step's dt, as the reference has it
+   // PhysicalStep (src/trajectory_parker.cc:212-221)
+   R dtp = R(0.5) * sp.dmax / norm(slp[0]);
+   dtp = m_min(dtp, R(0.5) * (sp.dmax * sp.dmax) / m_max(K.perp, K.para));
+   dtp = m_min(dtp, R(0.5) * R(3) * R(0.01) / m_abs(sd_divU(sp)));
+   L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bv, P.nbt, fwd);
+   // EulerDiffSlopes (src/trajectory_parker.cc:159-180)
+   R n[4];
+   normals4<R>(rng_block(P.seed, L.nrm++, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
+   const R sdt = m_sqrt(L.dt);
+   const R sperp = m_sqrt(R(2) * K.perp), spara = m_sqrt(R(2) * K.para);
+   V3<R> fa[3];
+   fa[2] = sp.bhat;
+   fa[0] = second_unit(sp.bhat);
+   fa[1] = cross(fa[2], fa[0]);
+   const V3<R> dr = from_basis(mk(sperp * (sdt * n[0]), sperp * (sdt * n[1]), spara * (sdt * n[2])), fa);
+   // RKSlopes; sp holds the latest stage's fields, which the events of a crossing read
+#pragma unroll 1
+   for (int is = 1; is < tab.s; is++) {
+#pragma unroll 1
+      for (int il = 0; il < is; il++) {
+         const R ds = L.dt * tab.template b<R>(is, il);
+         const R dta = tab.template a<R>(is) * L.dt;
+         if (fwd) { acc_add(L.t, dta); add3(L.pos, ds * slp[il]); acc_add(L.mom.x, ds * slm[il]); }
+         else { acc_add(L.t, -dta); add3(L.pos, R(-1) * (ds * slp[il])); acc_add(L.mom.x, -(ds * slm[il])); }
+      }
+      if (space_terminate<kParker>(L, bv, sp, s0, P, Pd, S)) return;
+      const V3<R> ps = val3<R>(L.pos);
+      const R pst = (R)acc_val(L.mom.x), ts = (R)acc_val(L.t);
+      Kap<R> Ks;
+      if (!get_fields<BG>(P.bg, deriv_mode, ts, ps, pst, mask, sp) ||
+          !parker_slopes<BG>(P, deriv_mode, ts, ps, pst, sp, fwd, Ks, slp[is], slm[is])) {
+         L.status |= TRAJ_DISCARD;
+         return;
+      }
+      sla[is] = parker_source(L, P, pst, ps);
+      L.t = t_loc;
+      L.pos = pos_loc;
+      L.mom = mom_loc;
+   }
+   // RKStep
+   if (fwd) acc_add(L.t, L.dt); else acc_add(L.t, -L.dt);
+   V3<R> pos_lo = val3<R>(L.pos);
+#pragma unroll 1
+   for (int il = 0; il < tab.s; il++) {
+      const R w = L.dt * tab.template v<R>(il);
+      if (fwd) { add3(L.pos, w * slp[il]); acc_add(L.mom.x, w * slm[il]); }
+      else { add3(L.pos, R(-1) * (w * slp[il])); acc_add(L.mom.x, -(w * slm[il])); }
+      if (tab.adaptive) {
+         const R wl = L.dt * tab.template w<R>(il);
+         pos_lo = fwd ? pos_lo + wl * slp[il] : pos_lo - wl * slp[il];
+      }
+      if (sla[il] != R(0)) L.amp += L.dt * tab.template v<R>(il) * sla[il] * m_exp(L.wgt);
+   }
+   if (tab.adaptive && rk_rejects(L, val3<R>(L.pos), pos_lo, tab.order)) {
+      // back to the stored point; the amplitude keeps the rejected increment, as in the reference
+      L.t = t_loc;
+      L.pos = pos_loc;
+      L.mom = mom_loc;
+      return;
+   }
+   acc_add(L.pos.x, dr.x); acc_add(L.pos.y, dr.y); acc_add(L.pos.z, dr.z);
+   handle_boundaries<kParker>(L, bv, sp, s0, P, Pd, S);
+   L.steps++;
+}
 
 template <int TT, class R>
 __device__ __forceinline__ V3<R> vel_load(V3<R> mom)
@@ -754,9 +968,9 @@ __device__ __forceinline__ void clamp_mu(AV3<A>& mom)
    else if (mu < R(-1)) acc_setf(mom.y, R(-1));
 }
 
-template <int TT, int BG, class R, class A, int STAGES>
+template <int TT, int BG, class R, class A, class TAB>
 __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, Start& s0, const ProblemDescT<R>& P,
-                                           const ProblemDesc& Pd, const RunConfig& cfg, const Sinks& S)
+                                           const ProblemDesc& Pd, const RunConfig& cfg, const Sinks& S, const TAB tab)
 {
    constexpr bool kFP64 = sizeof(R) == sizeof(double);
    const bool fwd = cfg.time_flow == 0;
@@ -766,6 +980,9 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, Start& 
    const bool gc_perp = TT == kGuiding && (cfg.traj_kind == kGuidingDiff || cfg.traj_kind == kGuidingDiffScatt);
    SD<R> sp;
    V3<R> mom = lane_mom(L);
+   // the last stored point's momentum (the pitch-angle step below changes it before the stages): a
+   // rejected step returns to it, as the reference's Load() does
+   [[maybe_unused]] const AV3<A> mom_stored = L.mom;
    if (!get_fields<BG>(P.bg, deriv_mode, (R)acc_val(L.t), val3<R>(L.pos), field_p<TT>(mom), traj_mask<TT>(), sp)) {
       L.status |= TRAJ_DISCARD;
       return;
@@ -775,6 +992,7 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, Start& 
    R d_perp = R(0);
    V3<R> fa[3];
    if (!prev_step_ok(L, sp.dmax)) return;
+   track_bmag(s0, cfg, sp);
    V3<R> vel = vel_load<TT>(mom);
    V3<R> drift = mk(R(0), R(0), R(0));
    if (scatt) {
@@ -891,7 +1109,7 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, Start& 
    }
    const A t_loc = L.t;
    const AV3<A> pos_loc = L.pos, mom_loc = L.mom;
-   V3<R> slp[STAGES], slm[STAGES];
+   V3<R> slp[TAB::kMax], slm[TAB::kMax];
    rk_slopes<TT>(sp, mom, vel, slp[0], slm[0], drift);
    V3<R> vperp = mk(R(0), R(0), R(0));
    if (gc_perp) {  // TrajectoryGuidingDiff::Slopes (src/trajectory_guiding_diff.cc:327-336)
@@ -996,11 +1214,11 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, Start& 
    }
    // RKSlopes
 #pragma unroll
-   for (int is = 1; is < STAGES; is++) {
+   for (int is = 1; is < (TAB::kGeneral ? tab.stages() : TAB::kMax); is++) {
 #pragma unroll
       for (int il = 0; il < is; il++) {
-         R ds = L.dt * rk_b<R>(is, il);
-         R dta = rk_a<R>(is) * L.dt;
+         R ds = L.dt * tab.template b<R>(is, il);
+         R dta = tab.template a<R>(is) * L.dt;
          if (fwd) { acc_add(L.t, dta); add3(L.pos, ds * slp[il]); add3(L.mom, ds * slm[il]); }
          else { acc_add(L.t, -dta); add3(L.pos, R(-1) * (ds * slp[il])); add3(L.mom, R(-1) * (ds * slm[il])); }
       }
@@ -1028,18 +1246,34 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, Start& 
    // RKStep
    if (fwd) acc_add(L.t, L.dt); else acc_add(L.t, -L.dt);
    if constexpr (kFP64) {
+      [[maybe_unused]] V3<R> pos_lo = val3<R>(L.pos);
 #pragma unroll
-      for (int il = 0; il < STAGES; il++) {
-         R w = L.dt * (STAGES == 1 ? R(1) : rk_v<R>(il));
+      for (int il = 0; il < (TAB::kGeneral ? tab.stages() : TAB::kMax); il++) {
+         R w = L.dt * tab.template v<R>(il);
          if (fwd) { add3(L.pos, w * slp[il]); add3(L.mom, w * slm[il]); }
          else { add3(L.pos, R(-1) * (w * slp[il])); add3(L.mom, R(-1) * (w * slm[il])); }
+         if constexpr (TAB::kGeneral) {
+            if (tab.adaptive) {
+               R wl = L.dt * tab.template w<R>(il);
+               pos_lo = fwd ? pos_lo + wl * slp[il] : pos_lo - wl * slp[il];
+            }
+         }
+      }
+      if constexpr (TAB::kGeneral) {
+         // an adaptive table may reject the step: back to the stored point, nothing recorded
+         if (tab.adaptive && rk_rejects(L, val3<R>(L.pos), pos_lo, tab.order)) {
+            L.t = t_loc;
+            L.pos = pos_loc;
+            L.mom = mom_stored;
+            return;
+         }
       }
    }
    else {
       V3<R> dp = mk(R(0), R(0), R(0)), dm = mk(R(0), R(0), R(0));
 #pragma unroll
-      for (int il = 0; il < STAGES; il++) {
-         R w = STAGES == 1 ? R(1) : rk_v<R>(il);
+      for (int il = 0; il < (TAB::kGeneral ? tab.stages() : TAB::kMax); il++) {
+         R w = tab.template v<R>(il);
          dp = dp + w * slp[il];
          dm = dm + w * slm[il];
       }
@@ -1067,6 +1301,7 @@ __device__ __noinline__ void set_start(Lane<R, A>& L, BndView<R> bv, Start& s0, 
    L.status = 0;
    L.steps = 0;
    L.nrm = 0;
+   L.n_adapt = 0;
    L.amp = R(0);
    L.wgt = R(0);
    L.dt = R(0);
@@ -1091,6 +1326,7 @@ __device__ __noinline__ void set_start(Lane<R, A>& L, BndView<R> bv, Start& s0, 
    s0.pos0 = pos;
    s0.mom0 = mom;
    s0.bhat0 = bh;
+   s0.bmag0 = s0.bmag_min = s0.bmag_max = (double)sp.Bmag;
    R c = c_code<R>();
    L.dt_adapt = Lim<R>::large * sp.dmax / c;
    V3<R> mr = lane_mom(L);
@@ -1150,6 +1386,7 @@ __device__ __forceinline__ void start_lane(Lane<R, A>& L, BndView<R> bv, Start& 
    n.attempt = attempt;
    set_start<TT, BG>(n, bv, s0, P[n.prob], Pd[n.prob], cfg, local);
    L.prob = n.prob; L.traj_id = n.traj_id; L.attempt = n.attempt; L.steps = n.steps; L.status = n.status; L.nrm = n.nrm;
+   L.n_adapt = n.n_adapt;
    L.t = n.t;
    L.pos.x = n.pos.x; L.pos.y = n.pos.y; L.pos.z = n.pos.z;
    L.mom.x = n.mom.x; L.mom.y = n.mom.y; L.mom.z = n.mom.z;
@@ -1172,7 +1409,7 @@ __device__ __forceinline__ void start_lane(Lane<R, A>& L, BndView<R> bv, Start& 
 // DM is the field-derivative method (SPX_OPT_DERIV_MODE) fixed per instantiation, so the analytic
 // kernels carry no finite-difference code (whose out-of-line calls would pin the field record to
 // the stack).
-template <int TT, int BG, class R, int DM>
+template <int TT, int BG, class R, int DM, bool GT>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? SPX_MIN_BLOCKS_F32 : SPX_MIN_BLOCKS_F64)
 step_kernel(const ProblemDescT<R>* __restrict__ P, const ProblemDesc* __restrict__ Pd, RunConfig cfg,
             RunCounters* ctr, int32_t* counts, double* sums, unsigned long long* n_events, TrajRecord* rec, int queue)
@@ -1238,9 +1475,15 @@ step_kernel(const ProblemDescT<R>* __restrict__ P, const ProblemDesc* __restrict
          }
          else {
             const ProblemDescT<R>& Pp = P[L.prob];
-            if (TT == kParker) parker_advance<BG>(L, bv, s0, Pp, Pd[L.prob], cfg, S);
-            else if (cfg.rk == 25) rk_advance<TT, BG, R, A, 4>(L, bv, s0, Pp, Pd[L.prob], cfg, S);
-            else rk_advance<TT, BG, R, A, 1>(L, bv, s0, Pp, Pd[L.prob], cfg, S);
+            if constexpr (GT) {
+               // any Butcher table (FP64): the table of the context, from constant memory
+               const TableRk tab{cfg.rk_stages, cfg.rk_order, cfg.rk_adaptive, cfg.rk_offset};
+               if (TT == kParker) parker_advance_gt<BG>(L, bv, s0, Pp, Pd[L.prob], cfg, S, tab);
+               else rk_advance<TT, BG, R, A>(L, bv, s0, Pp, Pd[L.prob], cfg, S, tab);
+            }
+            else if (TT == kParker) parker_advance<BG>(L, bv, s0, Pp, Pd[L.prob], cfg, S);
+            else if (cfg.rk == 25) rk_advance<TT, BG, R, A>(L, bv, s0, Pp, Pd[L.prob], cfg, S, FixedRk<4>{});
+            else rk_advance<TT, BG, R, A>(L, bv, s0, Pp, Pd[L.prob], cfg, S, FixedRk<1>{});
             // Integrate's safety limits (src/trajectory_base.cc:964-992)
             if (L.steps > kMaxTrajSteps || !isfinite(L.dt) || L.dt == R(0)) L.status |= TRAJ_DISCARD;
             done = (L.status & TRAJ_FINISH) && !(L.status & TRAJ_DISCARD);

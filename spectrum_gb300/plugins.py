@@ -356,6 +356,14 @@ class DistributionPositionCumulativeOrder2(Plugin): pass
 class DistributionDivergenceFlowPowerLaw(Plugin): pass
 
 
+@_plugin(ROLE_DISTRIBUTION, 10)
+class DistributionLossCone(Plugin):
+    """src/distribution_other.cc:794-862: the first or the final position (val_time), Cartesian or
+    spherical (val_coord), weighted by (|B|_min, |B|_max, asin(sqrt(|B| / |B|_max))) along the
+    trajectory. The extrema are tracked whenever a problem has this distribution, as a reference
+    build with RECORD_BMAG_EXTREMA does (src/trajectory_base.hh:31). All three dimensions binned."""
+
+
 @_plugin(ROLE_DISTRIBUTION, 20, reference=False)
 class DistributionTimeMu(Plugin):
     """Extension: a (t, mu) histogram of the second point (the event), for observer crossings
@@ -365,4 +373,4 @@ class DistributionTimeMu(Plugin):
 
 
 #: number of doubles per bin of a distribution kind (DistributionTemplated<double|GeoVector|GeoMatrix>)
-DISTRO_WIDTH = {1: 1, 2: 1, 3: 1, 4: 1, 5: 1, 6: 1, 7: 3, 8: 9, 9: 1, 20: 1}
+DISTRO_WIDTH = {1: 1, 2: 1, 3: 1, 4: 1, 5: 1, 6: 1, 7: 3, 8: 9, 9: 1, 10: 3, 20: 1}

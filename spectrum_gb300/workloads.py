@@ -204,19 +204,29 @@ def modulation_energies(n: int = 32, e1_mev: float = 10.0, e2_mev: float = 1.0e4
 
 
 def gcr_modulation(n_traj: int = 1_000_000, energies_mev=None, lam0_au: float = 0.1, pow_law_r: float = 0.5,
-                   pow_law_b: float = -1.0, kap_rat: float = 0.02, r_inner_au: float = 0.05,
-                   r_outer_au: float = 100.0, t_max_years: float = 1.0, lis_gamma: float = -1.8) -> list[Problem]:
+                   pow_law_b: float = 0.0, kap_rat: float = 0.02, r_inner_au: float = 0.05,
+                   r_outer_au: float = 100.0, t_max_years: float = 100.0, lis_gamma: float = -1.8,
+                   t_hist_years: float = 10.0) -> list[Problem]:
     """One problem per energy: start at 1 AU, trace backward until the 100 AU outer boundary
-    (hot: weighted by the LIS J0 (T/T0)^gamma / p^2 * v, src/distribution_other.cc:553-602), the
-    0.05 AU inner boundary (cold) or the time limit.
+    (hot: weighted by the LIS J0 (T/T0)^gamma / p^2 * v, src/distribution_other.cc:553-602) or the
+    0.05 AU inner boundary (cold).
 
     kappa_par = (lam0 v / 3)(R/R0)^0.5 (B/B0)^pow_law_b, kappa_perp = kap_rat kappa_par
-    (src/diffusion_other.cc:804-809); the run example uses pow_law_b = -1.
+    (src/diffusion_other.cc:804-809). The defaults are the modulation configuration of 32 energies
+    x 1e6 trajectories: lambda grows as P^0.5 with no field dependence (pow_law_b = 0). Every
+    trajectory ends at one of the two spheres within about four years and 1e6 steps; the reference
+    requires one time boundary (src/trajectory_base.cc:626-627), so a BoundaryTimeExpire sits
+    ``t_max_years`` = 100 years back, which no trajectory reaches (its crossings are neither hot nor
+    cold). The reference's run example (runs/gcr_modulation_example.cc:177-220) instead uses
+    pow_law_b = -1, kap_rat = 0.05 and a limit one year back. The exit-time histogram spans the
+    shorter of ``t_hist_years`` and the limit, outliers in its end bins.
     """
     if energies_mev is None:
         energies_mev = modulation_energies()
     out = []
+    # (years * 365 * 24 * 3600) / unit_time, in this order: the blobs must round as the reference's mains do
     t_max = t_max_years * 365.0 * 24.0 * 3600.0 / U.unit_time
+    t_hist = t_max if t_max_years <= t_hist_years else t_hist_years * 365.0 * 24.0 * 3600.0 / U.unit_time
     r0_rig = 3.33e6 / (U.unit_energy / U.unit_charge)
     unit_distro = 1.0 / (U.unit_length ** 2 * U.unit_time * 4.0 * math.pi * U.unit_energy)
     for p_idx, e in enumerate(energies_mev):
@@ -240,13 +250,29 @@ def gcr_modulation(n_traj: int = 1_000_000, energies_mev=None, lam0_au: float = 
         c.double(1.0 / unit_distro).double(1.0 * U.GEV / U.unit_energy).double(lis_gamma).double(0.0)
         pb.AddDistribution(DistributionSpectrumKineticEnergyPowerLaw(), c)
         # exit-time histogram of the run example (runs/gcr_modulation_example.cc:280-330): bins from 0
-        # to the (negative) time limit, outliers into the end bins
-        c = distro_header(DataContainer(), (32, 0, 0), (0.0, 0, 0), (-t_max, 0, 0), bin_outside=(1, 0, 0),
+        # to the (negative) end of the histogram span, outliers into the end bins
+        c = distro_header(DataContainer(), (32, 0, 0), (0.0, 0, 0), (-t_hist, 0, 0), bin_outside=(1, 0, 0),
                           unit_val=(U.unit_time, 1.0, 1.0))
         c.double(1.0).double(0.0).int(1)
         pb.AddDistribution(DistributionTimeUniform(), c)
         out.append(pb)
     return out
+
+
+def lis_weights(p, lis_gamma: float = -1.8):
+    """The spectrum's event weight for exit momenta ``p`` (numpy array, code units): the LIS
+    J0 v (T/T0)^gamma / p^2 of DistributionSpectrumKineticEnergyPowerLaw
+    (src/distribution_other.cc:567-591) with J0 = 1 / unit_distro and T0 = 1 GeV, as gcr_modulation
+    sets them. Used to form per-trajectory weights from final records (Monte Carlo errors)."""
+    import numpy as np
+    p = np.asarray(p, dtype=np.float64)
+    unit_distro = 1.0 / (U.unit_length ** 2 * U.unit_time * 4.0 * math.pi * U.unit_energy)
+    mc2 = U.mass * U.c_code * U.c_code
+    etot = np.sqrt(p * p + (U.mass * U.c_code) ** 2) * U.c_code
+    ke = etot - mc2
+    v = p * U.c_code * U.c_code / etot
+    t0 = 1.0 * U.GEV / U.unit_energy
+    return (1.0 / unit_distro) * v * np.power(ke / t0, lis_gamma) / (p * p)
 
 
 # ------------------------------------------------------------------------------------------------

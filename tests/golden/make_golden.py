@@ -181,7 +181,8 @@ def cases():
     out.append(("parker_fwd_uniform", workloads.diffusion_uniform(n_traj=200)))
     dsa = workloads.shock_acceleration(n_traj=12, x_escape=-2.0, x_downstream=2.0, p_max=20.0)
     out.append(("parker_fwd_smoothshock", dsa))
-    for k, pb in enumerate(workloads.gcr_modulation(n_traj=6, energies_mev=[30.0, 3000.0], t_max_years=0.05)):
+    for k, pb in enumerate(workloads.gcr_modulation(n_traj=6, energies_mev=[30.0, 3000.0], t_max_years=0.05,
+                                                              pow_law_b=-1.0)):
         out.append((f"parker_bwd_solarwind_{k}", pb))
     out.append(("lorentz_fwd_dipole", _dipole_reference_classes(6)))
     out.append(("focused_fwd_solarwind", _focused_reference_classes(6)))

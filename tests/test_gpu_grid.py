@@ -27,11 +27,8 @@ def test_grid_fp64_matches_oracle(built_lib, deriv_mode):
     pbs = workloads.gcr_modulation_grid(n_traj=64, n_nodes=48, energies_mev=[300.0], t_max_years=0.05)
     gpu = run_problems(pbs, precision=capi.SPX_FP64, record=True, deriv_mode=deriv_mode)
     ref = ot.run_oracle(pbs[0], deriv_mode=deriv_mode)
-    rec = gpu.records[0]
-    agree = rec["steps"] == ref.traj["steps"]
-    assert agree.mean() >= 0.9, agree.mean()
-    err = np.linalg.norm(rec["pos"] - ref.traj["pos"], axis=1) / np.linalg.norm(ref.traj["pos"], axis=1)
-    assert np.median(err[agree]) < 1e-9, np.median(err[agree])
+    ot.assert_fp64_parity(gpu.records[0], ref, ot.run_oracle(pbs[0], deriv_mode=deriv_mode, nudge_libm=1),
+                          distros=gpu.distros[0])
     assert gpu.stats.given_up == 0
 
 

@@ -40,22 +40,16 @@ def test_gcr_solarwind_fp64_reference_derivatives(built_lib):
     gpu = run_problems(pbs, record=True, deriv_mode=0)
     for k, pb in enumerate(pbs):
         ref = ot.run_oracle(pb, deriv_mode=0)
-        rec = gpu.records[k]
-        agree = (rec["steps"] == ref.traj["steps"]) & ((rec["status"] & STATUS_MASK) == (ref.traj["status"] & STATUS_MASK))
-        assert agree.mean() >= 0.9, agree
-        e = np.linalg.norm(rec["pos"] - ref.traj["pos"], axis=1) / np.linalg.norm(ref.traj["pos"], axis=1)
-        assert np.median(e[agree]) < 1e-6
+        ot.assert_fp64_parity(gpu.records[k], ref, ot.run_oracle(pb, deriv_mode=0, nudge_libm=1),
+                              distros=gpu.distros[k])
 
 
 def test_gcr_solarwind_fp64_analytic(built_lib):
     pbs = workloads.gcr_modulation(n_traj=16, energies_mev=[300.0], t_max_years=0.2)
     gpu = run_problems(pbs, record=True, deriv_mode=1)
     ref = ot.run_oracle(pbs[0], deriv_mode=1)
-    rec = gpu.records[0]
-    agree = (rec["steps"] == ref.traj["steps"])
-    assert agree.mean() >= 0.9
-    e = np.linalg.norm(rec["pos"] - ref.traj["pos"], axis=1) / np.linalg.norm(ref.traj["pos"], axis=1)
-    assert np.median(e[agree]) < 1e-6
+    ot.assert_fp64_parity(gpu.records[0], ref, ot.run_oracle(pbs[0], deriv_mode=1, nudge_libm=1),
+                          distros=gpu.distros[0])
 
 
 def test_diffusion_uniform_gaussian_spread(built_lib):
@@ -97,7 +91,8 @@ def test_fp32_position_histogram_within_3sigma_of_oracle(built_lib):
 def test_fp32_modulation_spectrum_within_3sigma_of_oracle(built_lib):
     """LIS-weighted modulation counts and exit-time histogram of the FP32 stepper against the oracle
     (FP64, analytic field derivatives), per bin within 3 sigma."""
-    pbs = workloads.gcr_modulation(n_traj=300, energies_mev=[200.0, 2000.0], t_max_years=0.2)
+    # kappa ~ 1/B, as in the reference's run example: a fifth of a year takes many trajectories to 100 AU
+    pbs = workloads.gcr_modulation(n_traj=300, energies_mev=[200.0, 2000.0], t_max_years=0.2, pow_law_b=-1.0)
     gpu = run_problems(pbs, precision=capi.SPX_MIXED)
     for k, pb in enumerate(pbs):
         ref = ot.run_oracle(pb, deriv_mode=1, record=False)

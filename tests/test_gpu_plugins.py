@@ -1,9 +1,11 @@
 """Every plugin class on the device: the FP64 kernel against the oracle, trajectory by trajectory,
 on the one-class-at-a-time problems whose oracle runs tests/test_oracle_plugins.py pins bit for
-bit to the reference's own code. FMA contraction on the device perturbs the last bits, so step
-counts must agree for at least 90% of the trajectories, the median position error stays below
-1e-9 relative, and the histograms agree to within 10% of their events (a perturbed crossing moves
-an event)."""
+bit to the reference's own code. Every trajectory takes the same steps to the same outcome, every
+histogram bin and event count is equal, and positions agree to within a fixed multiple of the
+spread the oracle itself shows when its normal deviates change by one ulp
+(oracle_tools.assert_fp64_parity): the device's log, sin and cos may round the last bit
+differently from the host's, and some schemes amplify that (the perpendicular RK2 scheme's second
+differences over 1e-4 dmax by about 1e8 a step)."""
 import numpy as np
 import pytest
 
@@ -51,6 +53,8 @@ def _problems():
         out["perp_" + name] = make
     for name in cases.COMBO_CASES:
         out["combination_" + name] = lambda name=name: cases._combo(name)
+    for name, make in cases.LOSSCONE_CASES.items():
+        out["loss_cone_" + name] = make
     out["parker_source_constant"] = lambda: cases._parker(
         traj=cases.TRAJ_PARKER_SOURCE, flow=cases.BACKWARD, src=(cases.SourceConstant(), DC().double(0.7)),
         t_end=-0.05, n=12)
@@ -123,15 +127,7 @@ PROBLEMS = _problems()
 def _check(pb):
     res = run_problems(pb, precision=capi.SPX_FP64, record=True)
     ref = ot.run_oracle(pb)
-    rec = res.records[0]
-    agree = rec["steps"] == ref.traj["steps"]
-    assert agree.mean() >= 0.9, agree.mean()
-    scale = np.maximum(np.linalg.norm(ref.traj["pos"], axis=1), 1e-30)
-    err = np.linalg.norm(rec["pos"] - ref.traj["pos"], axis=1) / scale
-    assert np.median(err[agree]) < 1e-9, np.median(err[agree])
-    for (c_gpu, _, n_gpu), (c_ref, _, n_ref) in zip(res.distros[0], ref.distros):
-        assert abs(n_gpu - n_ref) <= max(1, 0.1 * n_ref), (n_gpu, n_ref)
-        assert np.abs(c_gpu.astype(np.int64) - c_ref).sum() <= max(2, 0.2 * n_ref)
+    ot.assert_fp64_parity(res.records[0], ref, ot.run_oracle(pb, nudge_libm=1), distros=res.distros[0])
 
 
 @pytest.mark.parametrize("name", sorted(PROBLEMS))

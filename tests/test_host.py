@@ -111,6 +111,23 @@ def test_library_refuses_without_a_device(built_lib):
     assert rc < 0 and not h.value
 
 
+def test_butcher_tables_checked_before_the_device(built_lib):
+    """spx_create takes any of the reference's tables but 30 (which does not compile there); the tables
+    other than Euler and RK4 in FP64 only. The checks come before the device is looked for, so a valid
+    choice reaches SPX_ERR_NO_DEVICE here and an invalid one SPX_ERR_INVALID_ARG."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    lib = ctypes.CDLL(built_lib)
+    lib.spx_create.argtypes = [ctypes.POINTER(ctypes.c_void_p), ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int]
+    h = ctypes.c_void_p()
+    fp64, mixed = 0, 1
+    for traj, rk, prec, want in [(206, 29, fp64, -11), (206, 25, fp64, -11), (200, 32, fp64, -11), (205, 21, fp64, -11),
+                                 (206, 0, mixed, -11), (200, 25, mixed, -11), (206, 25, mixed, -1), (200, 29, mixed, -1),
+                                 (200, 30, fp64, -1), (200, 33, fp64, -1), (200, -1, fp64, -1)]:
+        assert lib.spx_create(ctypes.byref(h), traj, 0, rk, prec) == want, (traj, rk, prec)
+
+
 def test_record_dtype_matches_oracle():
     assert capi.RECORD_DTYPE == ot.TRAJ_DTYPE
     assert capi.RECORD_DTYPE.itemsize == 144
@@ -140,7 +157,9 @@ def test_cpp_host_mirror_blobs_equal_python(built_lib, tmp_path):
     exe = _build_example(built_lib, tmp_path)
     out = subprocess.run([exe, "--dump"], check=True, capture_output=True, text=True).stdout.split("\n")
     cpp = [tuple(line.split()) for line in out if line.strip()]
-    pb = workloads.gcr_modulation(n_traj=1, energies_mev=workloads.modulation_energies(4))[0]
+    # the example follows the reference's run example: kappa ~ 1/B and a one-year time limit
+    pb = workloads.gcr_modulation(n_traj=1, energies_mev=workloads.modulation_energies(4), pow_law_b=-1.0,
+                                  t_max_years=1.0)[0]
     py = [(str(e.plugin.role), str(e.plugin.kind), str(e.n_records), e.blob.hex()) for e in pb.plugins]
     assert sorted(cpp) == sorted(py)
     # the same order within each role (slots are positional)

@@ -37,7 +37,7 @@ from spectrum_gb300.plugins import (BackgroundDipole, BackgroundShock, Backgroun
                                     InitialSpaceRankineHalfBody, InitialSpaceSphere, InitialSpaceSphereSector,
                                     InitialTimeFixed, InitialTimeInterval, SourceConstant, SourceMomentumInjection,
                                     SourceSphericalShockInjection)
-from spectrum_gb300.problem import (BACKWARD, FORWARD, TRAJ_FOCUSED, TRAJ_GUIDING_DIFF, TRAJ_GUIDING_DIFF_SCATT,
+from spectrum_gb300.problem import (BACKWARD, FORWARD, TRAJ_FOCUSED, TRAJ_GUIDING, TRAJ_GUIDING_DIFF, TRAJ_GUIDING_DIFF_SCATT,
                                     TRAJ_GUIDING_SCATT, TRAJ_LORENTZ, TRAJ_PARKER,
                                     TRAJ_PARKER_SOURCE, Problem, distro_header)
 
@@ -58,7 +58,7 @@ def _same(pb):
         else:
             assert np.array_equal(a.traj[f], b.traj[f]), f
     for (ca, sa, na), (cb, sb, nb) in zip(a.distros, b.distros):
-        assert na == nb and np.array_equal(ca, cb) and np.array_equal(sa, sb)
+        assert na == nb and np.array_equal(ca, cb) and np.array_equal(sa, sb, equal_nan=True)
     return a
 
 
@@ -480,3 +480,51 @@ def _perp_absorbed():
 def test_perpendicular_schemes(name):
     r = _same(PERP_CASES[name]())
     assert (r.traj["steps"] > 3).all()
+
+
+# -- DistributionLossCone (src/distribution_other.cc:794-862) ------------------------------------------
+# The |B| extrema it reads are tracked by the reference only when compiled with RECORD_BMAG_EXTREMA
+# (src/trajectory_base.hh:31); the reference harness variants *_bmag are built that way. Orbits in the
+# dipole: |B| changes by a factor of several along a bounce.
+def _losscone_problem(traj, val_time=1, val_coord=0, n=6):
+    import math
+    from spectrum_gb300.plugins import DistributionLossCone
+    r_e = W.R_EARTH_CM / U.unit_length
+    b_eq = W.B_EARTH_G / U.unit_magnetic
+    bg = (BackgroundDipole(), DC().double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0.0, 0.0, -b_eq)).double(0.1 * r_e)
+          .double(r_e).double(0.1))
+    if val_coord == 1:
+        lo, hi = (2.0 * r_e, 0.0, 0.0), (6.0 * r_e, math.pi, 2.0 * math.pi)
+    else:
+        lo, hi = (-6.0 * r_e,) * 3, (6.0 * r_e,) * 3
+    c = distro_header(DC(), (6, 6, 6), lo, hi, bin_outside=(1, 1, 1), width=3)
+    dist = (DistributionLossCone(), c.int(val_time).int(val_coord))
+    kw = dict(diff=(DiffusionFullConstant(), DC().double(1e-4).double(1e-3)), t_end=1.0) if traj == TRAJ_PARKER else \
+        dict(diff=False, t_end=(10.0 if traj == TRAJ_GUIDING else 0.3) / U.unit_time)
+    return _parker(traj=traj, bg=bg, dist=dist, n=n, is_=(InitialSpaceFixed(), DC().vec((4.0 * r_e, 0.0, 0.0))),
+                   im=(InitialMomentumShell(), DC().double(U.mev_to_mom(10.0))), **kw)
+
+
+LOSSCONE_CASES = {
+    "guiding_final_cartesian": lambda: _losscone_problem(TRAJ_GUIDING),
+    "guiding_initial_spherical": lambda: _losscone_problem(TRAJ_GUIDING, val_time=0, val_coord=1),
+    "lorentz_final_spherical": lambda: _losscone_problem(TRAJ_LORENTZ, val_coord=1),
+    "parker_final_cartesian": lambda: _losscone_problem(TRAJ_PARKER),
+}
+
+
+@pytest.mark.parametrize("name", sorted(LOSSCONE_CASES))
+def test_loss_cone(name):
+    pb = LOSSCONE_CASES[name]()
+    if ot.ref_binary(pb) is None:
+        pytest.skip("reference harness with RECORD_BMAG_EXTREMA not built (needs the reference sources)")
+    r = _same(pb)
+    counts, sums, n_ev = r.distros[0]
+    assert n_ev == len(r.traj)
+    # the extrema bracket the field at the start, and the half-angle lies in (0, pi/2]. A Runge-Kutta
+    # event reads |B| at the step's last stage point, which can exceed the maximum along the stored
+    # points: the reference's asin then gives NaN, which both sides carry alike.
+    bmin, bmax, ang = (sums[counts > 0] / counts[counts > 0][:, None]).T
+    ok = np.isfinite(ang)
+    assert (bmin < bmax).all() and (ang[ok] > 0).all() and (ang[ok] <= np.pi / 2 + 1e-12).all()
+    assert ok.any()

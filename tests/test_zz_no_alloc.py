@@ -2,6 +2,9 @@
 the same context set-up, two calls in a row, per-trajectory final states and every distribution
 compared. The output buffers are the caller's (allocated here by torch); the library works in its
 fixed device array. Collected last so it also runs after every other GPU test in one process."""
+import os
+import re
+
 import numpy as np
 import pytest
 
@@ -41,9 +44,14 @@ def test_run_static_matches_run(built_lib, precision):
         recs = torch.zeros(total * capi.RECORD_DTYPE.itemsize, dtype=torch.uint8, device=dev)
         for call in range(2):
             st_ref = ref.MainLoop()
+            torch.cuda.synchronize(dev)
+            free_before = torch.cuda.mem_get_info(dev)[0]
             st = sim.ctx.run_static(counts.data_ptr(), counts.numel(), sums.data_ptr(), sums.numel(), n_ev.data_ptr(),
                                     n_ev.numel(), recs.data_ptr(), total)
             torch.cuda.synchronize(dev)
+            if call == 1:
+                # the second call finds its array already set up on this device: nothing is allocated
+                assert torch.cuda.mem_get_info(dev)[0] == free_before
             assert st.trajectories == st_ref.trajectories == total
             assert st.steps == st_ref.steps
             # per-trajectory final states of this call
@@ -69,11 +77,14 @@ def test_run_static_matches_run(built_lib, precision):
         sim.close()
 
 
-@pytest.mark.parametrize("precision,n_problems", [(capi.SPX_FP64, 70), (capi.SPX_MIXED, 45)])
-def test_run_static_rejects_sizes_beyond_its_array(built_lib, precision, n_problems):
-    """A batch whose descriptors do not fit the fixed array (69 problems in FP64, 44 in mixed
-    precision) is refused before anything runs."""
-    torch = pytest.importorskip("torch")
+def _capacity():
+    """The documented capacity of the fixed array, in problems per call, from include/spx.h."""
+    hdr = open(os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "include", "spx.h")).read()
+    m = re.search(r"(\d+) problems in SPX_MIXED, (\d+) in SPX_FP64", hdr)
+    return {capi.SPX_MIXED: int(m.group(1)), capi.SPX_FP64: int(m.group(2))}
+
+
+def _static_call(torch, precision, n_problems):
     pbs = workloads.gcr_modulation(n_traj=4, energies_mev=workloads.modulation_energies(n=n_problems),
                                    t_max_years=0.01)
     sim = open_problems(pbs, precision=precision)
@@ -83,10 +94,33 @@ def test_run_static_rejects_sizes_beyond_its_array(built_lib, precision, n_probl
         counts = torch.zeros(n_counts, dtype=torch.int32, device=dev)
         sums = torch.zeros(n_sums, dtype=torch.float64, device=dev)
         n_ev = torch.zeros(len(pbs) * 4, dtype=torch.int64, device=dev)
-        with pytest.raises(capi.SpxError) as e:
-            sim.ctx.run_static(counts.data_ptr(), counts.numel(), sums.data_ptr(), sums.numel(), n_ev.data_ptr(),
-                               n_ev.numel())
-        assert e.value.code == -13  # SPX_ERR_TOO_LARGE
-        assert int(counts.sum().item()) == 0
+        try:
+            st = sim.ctx.run_static(counts.data_ptr(), counts.numel(), sums.data_ptr(), sums.numel(),
+                                    n_ev.data_ptr(), n_ev.numel())
+            return st, int(counts.sum().item())
+        except capi.SpxError as e:
+            return e, int(counts.sum().item())
     finally:
         sim.close()
+
+
+@pytest.mark.parametrize("precision", [capi.SPX_FP64, capi.SPX_MIXED])
+def test_run_static_accepts_its_documented_capacity(built_lib, precision):
+    """Exactly as many problems as the header states fit the fixed array, and run."""
+    torch = pytest.importorskip("torch")
+    n = _capacity()[precision]
+    st, _ = _static_call(torch, precision, n)
+    assert not isinstance(st, Exception), st
+    assert st.trajectories == 4 * n
+    assert st.steps > 0
+
+
+@pytest.mark.parametrize("precision", [capi.SPX_FP64, capi.SPX_MIXED])
+def test_run_static_rejects_sizes_beyond_its_array(built_lib, precision):
+    """One problem more than the header's capacity does not fit the fixed array and is refused
+    before anything runs."""
+    torch = pytest.importorskip("torch")
+    err, events = _static_call(torch, precision, _capacity()[precision] + 1)
+    assert isinstance(err, capi.SpxError)
+    assert err.code == -13  # SPX_ERR_TOO_LARGE
+    assert events == 0
