@@ -46,9 +46,9 @@ FROZEN_SPECIAL_PER_STEP = {"gcr": 200.0, "diffusion": 93.0, "shock": 102.0, "dip
 # Executed by the FP32 Parker solar-wind kernel per accepted step, from the ncu capture of this workload
 # (profiles/step_kernel_parker_solarwind_f32_gcr.md): FP32 operations (FFMA x 2 + FADD + FMUL) and
 # thread instructions; and its DRAM bytes per trajectory (it reads no field data from HBM).
-EXEC_FP32_OPS_PER_STEP = float(os.environ.get("SPX_EXEC_FP32_OPS_PER_STEP", "421"))
-THREAD_INST_PER_STEP = float(os.environ.get("SPX_THREAD_INST_PER_STEP", "812"))
-DRAM_BYTES_PER_TRAJ = float(os.environ.get("SPX_DRAM_BYTES_PER_TRAJ", str(2.835e6 / 64000)))
+EXEC_FP32_OPS_PER_STEP = float(os.environ.get("SPX_EXEC_FP32_OPS_PER_STEP", "429"))
+THREAD_INST_PER_STEP = float(os.environ.get("SPX_THREAD_INST_PER_STEP", "835"))
+DRAM_BYTES_PER_TRAJ = float(os.environ.get("SPX_DRAM_BYTES_PER_TRAJ", str(35.375e6 / 320000)))
 # run indices reserved per rank under torchrun: rank r integrates trajectory ids of runs
 # r*RUNS_PER_RANK ... (disjoint shards of one job)
 RUNS_PER_RANK = 256
@@ -255,7 +255,15 @@ def compare_fp32_fp64(sub, tun, tuning64, torch, dev):
             w.append(np.where(hot, workloads.lis_weights(np.abs(rec["mom"][:, 0])), 0.0))
         n = len(w[0])
         e_mev = workloads.modulation_energies()[pb.problem_id]
+        # the count of the spectrum's hot events (exits at the outer sphere), paired: its difference
+        # between the arithmetics is the discordant pairs' difference, with sigma sqrt(n10 + n01)
+        h64, h32 = w[0] > 0, w[1] > 0
+        n10, n01 = int((h32 & ~h64).sum()), int((h64 & ~h32).sum())
+        hot64 = int(h64.sum())
         rows.append({"energy_mev": round(e_mev, 3), "events_fp64": int(d64[k][0][2]),
+                     "outer_exits_fp64": hot64,
+                     "outer_exit_count_rel_err": (n10 - n01) / hot64 if hot64 else None,
+                     "outer_exit_count_sigma": float(np.sqrt(n10 + n01)) / hot64 if hot64 else None,
                      "rel_err": s32 / s64 - 1.0 if s64 else None,
                      "sigma": float(np.sqrt(n * np.var(w[1] - w[0])) / s64) if s64 else None,
                      "sigma_fp64_alone": float(np.sqrt(n * np.var(w[0])) / s64) if s64 else None,
@@ -275,6 +283,8 @@ def compare_fp32_fp64(sub, tun, tuning64, torch, dev):
             "weighted_spectrum_max_sigma": max(r["sigma"] for r in ok) if ok else None,
             "weighted_spectrum_within_1pct": bool(ok and all(abs(r["rel_err"]) <= 0.01 for r in ok)),
             "weighted_spectrum_resolved": bool(ok and all(r["sigma"] <= 0.003 for r in ok)),
+            "outer_exit_count_max_rel_err": max(abs(r["outer_exit_count_rel_err"]) for r in ok) if ok else None,
+            "outer_exit_count_max_sigma": max(r["outer_exit_count_sigma"] for r in ok) if ok else None,
             "count_bin_error": ec, "count_bins_compared": nbins}
 
 
@@ -308,6 +318,28 @@ def _other_workloads():
 
 
 OTHER_WORKLOADS = ("diffusion", "shock", "dipole", "focused", "grid", "guiding")
+
+
+def orbit_errors(r64, r32):
+    """Per trajectory of the dipole orbits, FP32 against FP64 from identical initial conditions: the
+    relative |p| difference, the energy drift |p|/|p0| - 1 of each, and the error of the azimuth the
+    orbit turned (radians, and relative to the turn where the turn exceeds 0.5 rad, i.e. the error of the
+    drift period measured from it)."""
+    import numpy as np
+    same = (r64["status"] & 0x1F0) == (r32["status"] & 0x1F0)
+    p64, p32 = np.linalg.norm(r64["mom"], axis=1), np.linalg.norm(r32["mom"], axis=1)
+    p0 = np.linalg.norm(r64["mom0"], axis=1)
+    az = lambda r: np.arctan2(r["pos"][:, 1], r["pos"][:, 0])  # noqa: E731
+    az0 = np.arctan2(r64["pos0"][:, 1], r64["pos0"][:, 0])
+    turn = np.mod(az0 - az(r64), 2.0 * np.pi)  # westward drift
+    daz = np.abs(np.angle(np.exp(1j * (az(r32) - az(r64)))))
+    fast = same & (turn > 0.5) & (turn < 6.0)
+    q = lambda x: {"median": float(np.median(x)), "p99": float(np.percentile(x, 99)), "max": float(x.max())} if len(x) else None  # noqa: E731
+    return {"trajectories": int(len(p64)), "same_outcome": float(same.mean()),
+            "momentum_rel_diff": q(np.abs(p32 / p64 - 1.0)[same]),
+            "energy_drift_fp64": q(np.abs(p64 / p0 - 1.0)), "energy_drift_fp32": q(np.abs(p32 / p0 - 1.0)),
+            "azimuth_abs_diff_rad": q(daz[same]),
+            "drift_period_rel_diff": q(daz[fast] / turn[fast]), "trajectories_turning_over_0.5_rad": int(fast.sum())}
 
 
 def bench_other(args, rank, world, local):
@@ -344,18 +376,23 @@ def bench_other(args, rank, world, local):
         sub = build()
         for p in sub:
             p.n_traj = max(1, int(p.n_traj * share))
-        s64 = open_problems(sub, precision=capi.SPX_FP64, deriv_mode=1)
+        rec = args.workload == "dipole"
+        s64 = open_problems(sub, precision=capi.SPX_FP64, deriv_mode=1, record=rec)
         flush_l2(torch, dev)
         st64 = s64.MainLoop(capi.Tuning(0, 0, 1, 0))
+        r64 = [s64.ctx.records(k, p.n_traj) for k, p in enumerate(sub)] if rec else None
         s64.close()
-        s32 = open_problems(sub, precision=capi.SPX_MIXED)
+        s32 = open_problems(sub, precision=capi.SPX_MIXED, record=rec)
         flush_l2(torch, dev)
         st32 = s32.MainLoop(tun)
+        r32 = [s32.ctx.records(k, p.n_traj) for k, p in enumerate(sub)] if rec else None
         s32.close()
         line["fp64_plain"] = {"trajectories": st64.trajectories, "value": st64.trajectories / st64.kernel_ms * 1e3,
                               "steps_per_s": st64.steps / st64.kernel_ms * 1e3,
                               "ratio_fp32_batched_over_fp64_plain": (st32.trajectories / st32.kernel_ms) /
                                                                     (st64.trajectories / st64.kernel_ms)}
+        if rec:
+            line["fp32_vs_fp64_per_trajectory"] = orbit_errors(r64[0], r32[0])
     if rank == 0:
         print(json.dumps(line), flush=True)
 

@@ -82,6 +82,9 @@ extern "C" {
 #define SPX_OPT_PERP_METHOD 9       /* GuidingDiff / GuidingDiffScatt perpendicular scheme, the reference's compile-time
                                        STOCHASTIC_METHOD_PERP (src/trajectory_guiding_diff.hh:19): 0 Euler (default),
                                        1 Milstein, 2 RK2 */
+#define SPX_OPT_SPECIALIZE 10       /* 1 (default): SPX_MIXED Parker contexts whose problems share the diffusion class
+                                       FullConstant or RigidityMagneticFieldPowerLaw run on kernels compiled for that
+                                       class; 0: on the kernel that dispatches at run time. Same trajectories. */
 /* plugin kinds: see spectrum_gb300/plugins.py; e.g. background 1 uniform, 3 smooth shock,
  * 4 dipole, 5 solar wind; diffusion 5 full constant, 8 rigidity/field power law; boundary
  * 1 time expire, 10 plane absorb, 14 sphere absorb, 30 momentum inject; distribution 2 position

@@ -46,7 +46,7 @@ def _compile(src: str, nvcc: str, extra: list[str]) -> tuple[str, int, str]:
     # cos and pow (relative errors of a few 1e-7). The FP64 kernels keep IEEE arithmetic and are
     # compiled without multiply-add contraction, so every +, -, *, / and sqrt rounds as in the
     # reference's own (uncontracted) build and in the oracle.
-    if src.endswith("_f32.cu"):
+    if "_f32" in src:  # spx_k_<family>_f32.cu and the FP32 units specialised for one diffusion class
         fast = ["-use_fast_math"]
     elif src.endswith(("_f64.cu", "_f64fd.cu", "_f64rk.cu", "_f64fdrk.cu")):
         fast = ["-fmad=false"]

@@ -50,6 +50,9 @@ struct spx_ctx {
    // the Butcher table: general (not Euler or, for the RK types, the classic RK4) tables run on the
    // *_f64rk / *_f64fdrk kernels, which read it from constant memory
    bool general_rk = false;
+   // SPX_OPT_SPECIALIZE 0: the FP32 Parker kernels dispatch on the diffusion class at run time even where
+   // a kernel specialised for it exists (the specialised and generic kernels give the same trajectories)
+   bool no_special = false;
    int rk_stages = 1, rk_order = 1, rk_adaptive = 0, rk_offset = 0;
    double steps_per_orbit = 100.0;
    int deriv_mode = 0, pa_scattering = 0, record_final = 0, max_attempts = 100, mu_method = 0, perp_method = 0;
@@ -270,6 +273,26 @@ int upload(spx_ctx* c)
    return SPX_OK;
 }
 
+// The diffusion class every problem of the context shares, or -1 (kernels specialised for it exist for
+// the FP32 Parker types: spx_k_parker_f32rb.cu, spx_k_parker_f32fc.cu).
+int common_diffusion(const spx_ctx* c)
+{
+   int k = -2;
+   for (const auto& p : c->problems) {
+      if (k == -2) k = p.pd.df.kind;
+      else if (k != p.pd.df.kind) return -1;
+   }
+   return k < 0 ? -1 : k;
+}
+
+int parker_f32_special(const spx_ctx* c)
+{
+   if (c->precision != SPX_MIXED || c->general_rk || c->no_special) return -1;
+   if (c->traj != SPX_TRAJ_PARKER && c->traj != SPX_TRAJ_PARKER_SOURCE) return -1;
+   const int k = common_diffusion(c);
+   return (k == spx::kDfRigidityB || k == spx::kDfFull) ? k : -1;
+}
+
 cudaError_t launch(spx_ctx* c, const spx::LaunchArgs& a)
 {
    const bool f64 = c->precision == SPX_FP64, fd = f64 && c->deriv_mode == 0;
@@ -282,6 +305,11 @@ cudaError_t launch(spx_ctx* c, const spx::LaunchArgs& a)
       case SPX_TRAJ_FOCUSED: return fd ? spx::launch_focused_f64fdrk(bg, a) : spx::launch_focused_f64rk(bg, a);
       default: return fd ? spx::launch_guiding_f64fdrk(bg, a) : spx::launch_guiding_f64rk(bg, a);
       }
+   }
+   switch (parker_f32_special(c)) {
+   case spx::kDfRigidityB: return spx::launch_parker_f32rb(bg, a);
+   case spx::kDfFull: return spx::launch_parker_f32fc(bg, a);
+   default: break;
    }
    switch (c->traj) {
    case SPX_TRAJ_PARKER:
@@ -316,6 +344,11 @@ int occupancy(spx_ctx* c, int block, int slots)
       default:
          return fd ? spx::occupancy_guiding_f64fdrk(bg, block, slots) : spx::occupancy_guiding_f64rk(bg, block, slots);
       }
+   }
+   switch (parker_f32_special(c)) {
+   case spx::kDfRigidityB: return spx::occupancy_parker_f32rb(bg, block, slots);
+   case spx::kDfFull: return spx::occupancy_parker_f32fc(bg, block, slots);
+   default: break;
    }
    switch (c->traj) {
    case SPX_TRAJ_PARKER:
@@ -624,6 +657,12 @@ int spx_set_option(spx_ctx_t c, int option, double value)
       if (!(value >= 0.0) || value != (double)(int64_t)value || value > 2147483647.0) return SPX_ERR_INVALID_ARG;
       c->rec_capacity = (int64_t)value;
       c->dirty = true;
+      return SPX_OK;
+   case SPX_OPT_SPECIALIZE:
+      // 0: no kernel specialised for the diffusion class (a captured launch is re-captured)
+      if (value != 0.0 && value != 1.0) return SPX_ERR_INVALID_ARG;
+      c->no_special = value == 0.0;
+      drop_graph(c);
       return SPX_OK;
    case SPX_OPT_RUN_INDEX:
       // shards of one job: rank r starting at index r draws trajectory ids disjoint from the others'

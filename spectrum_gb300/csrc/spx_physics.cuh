@@ -497,13 +497,14 @@ __device__ __forceinline__ void wnlt_ramp(const DiffParamsT<R>& d, V3<R> pos, R&
 
 // "mu" and "Omega" are DiffusionBase's pitch-angle cosine and cyclotron frequency, which only the WNLT models
 // read; they are set once per GetComponent and not moved by the spatial difference quotients
-// (src/diffusion_base.cc:105-174). The Parker types pass neither.
-template <class R>
+// (src/diffusion_base.cc:105-174). The Parker types pass neither. DK >= 0 fixes the diffusion class at
+// compile time (kernels specialised for one class); -1 dispatches on the descriptor.
+template <class R, int DK = -1>
 __device__ __forceinline__ Kap<R> kappa_pp(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const KapIn<R>& s, R mu = R(0),
                                            R Omega = R(0))
 {
    Kap<R> K{R(0), R(0)};
-   switch (d.kind) {
+   switch (DK >= 0 ? DK : d.kind) {
    case kDfPara: K.para = d.a[0]; break;                      // src/diffusion_other.cc:381-385
    case kDfPerp: K.perp = d.a[0]; break;                      // :459-463
    case kDfFull: K.perp = d.a[0]; K.para = d.a[1]; break;     // :538-543
@@ -595,10 +596,11 @@ __device__ __forceinline__ R kappa_mumu_dmu(const DiffParamsT<R>& d, V3<R> pos, 
 
 // Models whose gradient needs no field-gradient matrix (only grad|B| or grad U . U).
 template <class R>
-__device__ __forceinline__ bool kappa_grad_is_analytic(const DiffParamsT<R>& d)
+__device__ __forceinline__ bool kappa_grad_is_analytic(const DiffParamsT<R>& d, int dk = -1)
 {
-   return d.kind == kDfPara || d.kind == kDfPerp || d.kind == kDfFull || d.kind == kDfFlowMomentum ||
-          d.kind == kDfKinEnergyRadial || d.kind == kDfRigidityB;
+   const int kind = dk >= 0 ? dk : d.kind;
+   return kind == kDfPara || kind == kDfPerp || kind == kDfFull || kind == kDfFlowMomentum ||
+          kind == kDfKinEnergyRadial || kind == kDfRigidityB;
 }
 
 // Spatial gradients of K_perp and K_para: the analytic GetDirectionalDerivative overrides
@@ -619,11 +621,12 @@ __device__ __noinline__ Kap<R> kappa_wnlt_call(const DiffParamsT<R>& d, V3<R> po
 }
 
 // kPitch: the caller is a type with a pitch angle, for which the WNLT ramp (never compiled for Parker) exists.
-template <class R, bool kPitch = false>
+// DK as for kappa_pp.
+template <class R, bool kPitch = false, int DK = -1>
 __device__ __forceinline__ void kappa_grad(const DiffParamsT<R>& d, V3<R> pos, R p, R vmag, const SD<R>& s, Kap<R> K, V3<R>& gperp,
                                            V3<R>& gpara, R mu = R(0), R Omega = R(0))
 {
-   switch (d.kind) {
+   switch (DK >= 0 ? DK : d.kind) {
    // DiffusionWNLTConstant reads neither the position nor |B| (mu and Omega stay fixed), so the base
    // class's difference quotient is exactly zero
    case kDfPara: case kDfPerp: case kDfFull: case kDfWNLT:

@@ -493,14 +493,18 @@ __device__ __forceinline__ R time_proximity(R dt, R dmax, BndView<R> bv, int nbt
 
 // UpdateBmagExtrema (src/trajectory_base.cc:586-592) of the previous step: the reference folds in the
 // fields each advanced step ends with, which are this step's start fields; a retried step's start was
-// folded in already.
+// folded in already. Out of line behind a branch on the run configuration: inlined, the compiler
+// predicates the double comparisons and conversion into every step of every kernel.
+static __device__ __noinline__ void fold_bmag(Start& s0, double bmag)
+{
+   s0.bmag_min = fmin(s0.bmag_min, bmag);
+   s0.bmag_max = fmax(s0.bmag_max, bmag);
+}
+
 template <class R>
 __device__ __forceinline__ void track_bmag(Start& s0, const RunConfig& cfg, const SD<R>& sp)
 {
-   if (cfg.track_bmag) {
-      s0.bmag_min = fmin(s0.bmag_min, (double)sp.Bmag);
-      s0.bmag_max = fmax(s0.bmag_max, (double)sp.Bmag);
-   }
+   if (cfg.track_bmag) fold_bmag(s0, (double)sp.Bmag);
 }
 
 // Integrate's time-step check (src/trajectory_base.cc:979-983) of the previous step: dt against the
@@ -545,7 +549,7 @@ __device__ __noinline__ bool parker_divk_fd(const ProblemDescT<R>& P, int deriv_
    return true;
 }
 
-template <int BG, class R, class A>
+template <int BG, int DK, class R, class A>
 __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, Start& s0,
                                                const ProblemDescT<R>& P, const ProblemDesc& Pd, const RunConfig& cfg,
                                                const Sinks& S)
@@ -557,13 +561,13 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, Sta
    R p = (R)acc_val(L.mom.x);
    R t = (R)acc_val(L.t);
    SD<R> sp;
-   const unsigned mask = traj_mask<kParker>() | (kappa_grad_is_analytic(P.df) ? kDerivedOnly : 0u);
+   const unsigned mask = traj_mask<kParker>() | (kappa_grad_is_analytic(P.df, DK) ? kDerivedOnly : 0u);
    if (!get_fields<BG>(P.bg, deriv_mode, t, pos, p, mask, sp)) { L.status |= TRAJ_DISCARD; return; }
    if (!prev_step_ok(L, sp.dmax)) return;
    track_bmag(s0, cfg, sp);
    R vmag = vel_of(p);
    // DiffusionCoeff (src/trajectory_parker.cc:83-153)
-   Kap<R> K = kappa_pp(P.df, pos, p, vmag, kap_in(sp));
+   Kap<R> K = kappa_pp<R, DK>(P.df, pos, p, vmag, kap_in(sp));
    V3<R> divK;
    if (kFP64 && deriv_mode == 0) {
       if (!parker_divk_fd<BG>(P, deriv_mode, t, pos, p, vmag, sp, divK)) { L.status |= TRAJ_DISCARD; return; }
@@ -571,7 +575,7 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, Sta
    else {
       // TRAJ_PARKER_DIVK_METHOD 1 (src/trajectory_parker.cc:120-140)
       V3<R> gpe, gpa;
-      kappa_grad(P.df, pos, p, vmag, sp, K, gpe, gpa);
+      kappa_grad<R, false, DK>(P.df, pos, p, vmag, sp, K, gpe, gpa);
       V3<R> t1 = gpa - gpe;
       divK = (gpe + dot(sp.bhat, t1) * sp.bhat) + (K.para - K.perp) * (sd_divbhat(sp) * sp.bhat + sd_b_gradbhat(sp));
    }
@@ -1409,7 +1413,8 @@ __device__ __forceinline__ void start_lane(Lane<R, A>& L, BndView<R> bv, Start& 
 // DM is the field-derivative method (SPX_OPT_DERIV_MODE) fixed per instantiation, so the analytic
 // kernels carry no finite-difference code (whose out-of-line calls would pin the field record to
 // the stack).
-template <int TT, int BG, class R, int DM, bool GT>
+// DK >= 0: a kernel specialised for one diffusion class (the Parker types); -1 dispatches at run time.
+template <int TT, int BG, class R, int DM, bool GT, int DK>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? SPX_MIN_BLOCKS_F32 : SPX_MIN_BLOCKS_F64)
 step_kernel(const ProblemDescT<R>* __restrict__ P, const ProblemDesc* __restrict__ Pd, RunConfig cfg,
             RunCounters* ctr, int32_t* counts, double* sums, unsigned long long* n_events, TrajRecord* rec, int queue)
@@ -1481,7 +1486,7 @@ step_kernel(const ProblemDescT<R>* __restrict__ P, const ProblemDesc* __restrict
                if (TT == kParker) parker_advance_gt<BG>(L, bv, s0, Pp, Pd[L.prob], cfg, S, tab);
                else rk_advance<TT, BG, R, A>(L, bv, s0, Pp, Pd[L.prob], cfg, S, tab);
             }
-            else if (TT == kParker) parker_advance<BG>(L, bv, s0, Pp, Pd[L.prob], cfg, S);
+            else if (TT == kParker) parker_advance<BG, DK>(L, bv, s0, Pp, Pd[L.prob], cfg, S);
             else if (cfg.rk == 25) rk_advance<TT, BG, R, A>(L, bv, s0, Pp, Pd[L.prob], cfg, S, FixedRk<4>{});
             else rk_advance<TT, BG, R, A>(L, bv, s0, Pp, Pd[L.prob], cfg, S, FixedRk<1>{});
             // Integrate's safety limits (src/trajectory_base.cc:964-992)
