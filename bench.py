@@ -434,6 +434,8 @@ def main():
     ap.add_argument("--tuning", default="", metavar="BLOCK,BLOCKS_PER_SM,STEPS_PER_SYNC",
                     help="a fixed launch shape for the persistent queue instead of the autotuner's (profiling)")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--per-launch-steps", type=int, default=2,
+                    help="one-slice launches timed for comparison (each pays the drain of the queue)")
     ap.add_argument("--workload", default="gcr", choices=["gcr"] + sorted(OTHER_WORKLOADS),
                     help="gcr: the headline modulation batch; the others print throughput lines for the "
                          "other workload families (shortened where the full configuration takes hours)")
@@ -452,8 +454,11 @@ def main():
            "boundaries": "0.05 AU absorb (cold), 100 AU absorb (LIS-weighted), 100 yr time limit",
            "fraction_of_named_job": args.per_energy / 1.0e6,
            "trajectory_ids": f"step k integrates ids k*{args.per_energy} ... (k+1)*{args.per_energy}-1 of each "
-                             f"energy; the named job is 1e6 per energy",
-           "l2": "flushed between steps"}
+                             f"energy (rank r adds r*K*{args.per_energy}); the named job is 1e6 per energy",
+           "launch": "the K timed steps run as one launch of the persistent queue over their K slices; "
+                     "per_launch_per_step times one launch per slice",
+           "l2": "flushed before the timed launch; the kernel reads a few KB of descriptors and keeps its state "
+                 "in registers"}
 
     if args.impl == "reference":
         if rank != 0:
@@ -491,10 +496,11 @@ def main():
     n_step = 32 * args.per_energy
 
     # ---- batched FP32 stepper: value ---------------------------------------------------------
+    # Set-up (untimed) on a context of one slice: the launch shape from the project's autotuner, timed
+    # on a sample of this batch, and the warm-up steps.
     sim = open_problems(pbs, precision=capi.SPX_MIXED)
     if world > 1:
         shard.assign(sim, rank, RUNS_PER_RANK)
-    # the launch shape: the project's autotuner, timed on a sample of this batch (set-up, untimed)
     if args.tuning:
         b, bps, sps = (int(x) for x in args.tuning.split(","))
         tun = capi.Tuning(b, bps, sps, 1)
@@ -502,40 +508,48 @@ def main():
         tun = sim.ctx.autotune(0)
     for _ in range(args.warmup):
         sim.MainLoop(tun)
-    sim.ctx.reset_distributions()
+    # For comparison, not the value: one launch per slice, which pays the drain of the persistent
+    # queue (the last long trajectories on nearly empty warps) once per slice.
+    per_launch = None
+    if args.per_launch_steps > 0:
+        ms = []
+        for _ in range(args.per_launch_steps):
+            flush_l2(torch, dev)
+            st1 = sim.MainLoop(tun)
+            ms.append(st1.kernel_ms)
+        per_launch = {"value": st1.trajectories * len(ms) / (sum(ms) / 1e3), "unit": UNIT, "launches": len(ms),
+                      "ms_per_launch": statistics.mean(ms), "trajectories_per_launch": st1.trajectories}
+    sim.close()
+    # The timed region: the K steps as one launch of the persistent queue over K slices. Slice k is
+    # trajectory ids k*pe ... (k+1)*pe-1 of every energy (pe trajectories per energy), the ids that K
+    # launches of one slice draw, so the results are the same; a job of 1e6 per energy is one launch in
+    # the library too. Under torchrun rank r takes the block of K slices at run index r.
+    simk = open_problems(problems(args.steps * args.per_energy), precision=capi.SPX_MIXED)
+    if world > 1:
+        simk.ctx.set_option(capi.SPX_OPT_RUN_INDEX, rank)
     # nvidia-smi samples of the timed region go to SPX_CLOCKS_DIR (default: the temporary directory)
     clocks_dir = os.environ.get("SPX_CLOCKS_DIR", tempfile.gettempdir())
     os.makedirs(clocks_dir, exist_ok=True)
     clocks = Clocks(local, os.path.join(clocks_dir, f"clocks_rank{rank}.csv"))
-    kms = []
-    steps_done = 0
-    traj_done = 0
-    # the timed region: K launches, each preceded by an L2 flush, device time from CUDA events
+    flush_l2(torch, dev)
     if world > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize(dev)
     t_wall0 = time.perf_counter()
     with clocks:
-        ends = None
-        for k in range(args.steps):
-            flush_l2(torch, dev)
-            st = sim.MainLoop(tun)
-            kms.append(st.kernel_ms)
-            steps_done += st.steps
-            traj_done += st.trajectories
-            if k == 0:
-                # where step 0's trajectories ended: the spectrum records both spheres (the inner one
-                # cold), the exit-time histogram the outer one only
-                ends = [(sim.ctx.distribution(p, 1)[2], sim.ctx.distribution(p, 0)[2]) for p in range(len(pbs))]
-                sim.ctx.reset_distributions()
+        st = simk.MainLoop(tun)
     torch.cuda.synchronize(dev)
     wall = time.perf_counter() - t_wall0
+    steps_done, traj_done = st.steps, st.trajectories
+    # where the trajectories ended: the spectrum records both spheres (the inner one cold), the
+    # exit-time histogram the outer one only
+    ends = [(simk.ctx.distribution(p, 1)[2], simk.ctx.distribution(p, 0)[2]) for p in range(len(pbs))]
     tuning = {"block_size": st.tuning.block_size, "blocks_per_sm": st.tuning.blocks_per_sm,
               "steps_per_sync": st.tuning.steps_per_sync,
               "schedule": "persistent work queue" if st.tuning.schedule == 1 else "one thread per trajectory",
               "chosen_by": "--tuning" if args.tuning else "spx_autotune"}
-    sim.close()
-    t_dev = sum(kms) / 1e3
+    simk.close()
+    t_dev = st.kernel_ms / 1e3
     t_max = shard.max_over_ranks(t_dev) if world > 1 else t_dev
     value = traj_done * world / t_max
     steps_rate = steps_done * world / t_max
@@ -550,21 +564,21 @@ def main():
         fp64["schedule"] = "one thread per trajectory"
 
     # ---- end to end through the C ABI --------------------------------------------------------
-    e2e_times = []
-    h2d = d2h = 0
-    for k in range(max(1, min(args.steps, 2))):
-        flush_l2(torch, dev)
-        t0 = time.perf_counter()
-        s = open_problems(pbs, precision=capi.SPX_MIXED)
-        if world > 1:
-            s.ctx.set_option(capi.SPX_OPT_RUN_INDEX, shard.first_run_index(rank, RUNS_PER_RANK) + RUNS_PER_RANK // 2 + k)
-        st_e = s.MainLoop(tun)
-        outs = [s.ctx.distribution(p, 0) for p in range(len(pbs))]
-        s.close()
-        e2e_times.append(time.perf_counter() - t0)
-        d2h = sum(c.nbytes + x.nbytes + 8 for c, x, _ in outs) + 64
-        h2d = len(pbs) * (6800 * 2)  # FP64 and FP32 descriptors per problem (sizeof ProblemDescT)
-    e2e_val = st_e.trajectories * world / statistics.mean(e2e_times)
+    # A fresh context per measurement: descriptors host to device, one launch over E slices, the
+    # spectra device to host. E = min(K, 4) keeps the leg short; its drain weighs more than the
+    # K-slice launch's.
+    n_e2e = max(1, min(args.steps, 4))
+    flush_l2(torch, dev)
+    t0 = time.perf_counter()
+    s = open_problems(problems(n_e2e * args.per_energy), precision=capi.SPX_MIXED)
+    s.ctx.set_option(capi.SPX_OPT_RUN_INDEX, world + rank)
+    st_e = s.MainLoop(tun)
+    outs = [s.ctx.distribution(p, 0) for p in range(len(pbs))]
+    s.close()
+    e2e_t = time.perf_counter() - t0
+    d2h = (sum(c.nbytes + x.nbytes + 8 for c, x, _ in outs) + 64) / n_e2e
+    h2d = len(pbs) * (6800 * 2) / n_e2e  # FP64 and FP32 descriptors per problem (sizeof ProblemDescT)
+    e2e_val = st_e.trajectories * world / e2e_t
 
     # ---- roofline of the dominant kernel -------------------------------------------------------
     peaks = {}
@@ -599,7 +613,7 @@ def main():
 
     clk = clocks.summary()
     if ends is not None:
-        n0 = args.per_energy
+        n0 = args.per_energy * args.steps
         cfg["exits_per_energy"] = {"outer_100AU": [round(o / n0, 4) for o, _ in ends],
                                    "inner_0.05AU": [round((b - o) / n0, 4) for o, b in ends],
                                    "neither": [round(1.0 - b / n0, 4) for _, b in ends]}
@@ -607,7 +621,8 @@ def main():
             "warmup": args.warmup, "ms_per_step": t_max / args.steps * 1e3, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (float-float accumulation)",
             "data": "synthetic (seeded Philox streams)", "config": cfg, "steps_per_s": steps_rate,
-            "wall_s": wall, "tuning": tuning, "gpu_launches": args.steps, "fp64_plain": fp64,
+            "wall_s": wall, "tuning": tuning, "gpu_launches": 1, "per_launch_per_step": per_launch,
+            "fp64_plain": fp64,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": roof, "clocks": clk}
     if rank == 0:

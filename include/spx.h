@@ -85,6 +85,9 @@ extern "C" {
 #define SPX_OPT_SPECIALIZE 10       /* 1 (default): SPX_MIXED Parker contexts whose problems share the diffusion class
                                        FullConstant or RigidityMagneticFieldPowerLaw run on kernels compiled for that
                                        class; 0: on the kernel that dispatches at run time. Same trajectories. */
+#define SPX_OPT_STEP_CAP 11         /* 0 (default): off. N > 0: spx_run stops every trajectory after N steps, as the
+                                       autotuner's timing samples do: a steady-state throughput sample with no drain
+                                       of the queue; trajectories stopped by the cap are neither finished nor binned */
 /* plugin kinds: see spectrum_gb300/plugins.py; e.g. background 1 uniform, 3 smooth shock,
  * 4 dipole, 5 solar wind; diffusion 5 full constant, 8 rigidity/field power law; boundary
  * 1 time expire, 10 plane absorb, 14 sphere absorb, 30 momentum inject; distribution 2 position

@@ -53,6 +53,7 @@ struct spx_ctx {
    // SPX_OPT_SPECIALIZE 0: the FP32 Parker kernels dispatch on the diffusion class at run time even where
    // a kernel specialised for it exists (the specialised and generic kernels give the same trajectories)
    bool no_special = false;
+   uint32_t step_cap = 0;  // SPX_OPT_STEP_CAP
    int rk_stages = 1, rk_order = 1, rk_adaptive = 0, rk_offset = 0;
    double steps_per_orbit = 100.0;
    int deriv_mode = 0, pa_scattering = 0, record_final = 0, max_attempts = 100, mu_method = 0, perp_method = 0;
@@ -664,6 +665,11 @@ int spx_set_option(spx_ctx_t c, int option, double value)
       c->no_special = value == 0.0;
       drop_graph(c);
       return SPX_OK;
+   case SPX_OPT_STEP_CAP:
+      if (!(value >= 0.0) || value != (double)(int64_t)value || value > 4294967295.0) return SPX_ERR_INVALID_ARG;
+      c->step_cap = (uint32_t)value;
+      drop_graph(c);
+      return SPX_OK;
    case SPX_OPT_RUN_INDEX:
       // shards of one job: rank r starting at index r draws trajectory ids disjoint from the others'
       if (!(value >= 0.0) || value != (double)(int64_t)value || value > 4294967295.0) return SPX_ERR_INVALID_ARG;
@@ -811,7 +817,7 @@ int spx_run(spx_ctx_t c, const spx_tuning* tuning)
    a.cfg.record_final = c->record_final;
    a.cfg.n_problems = (int)c->problems.size();
    a.cfg.steps_per_sync = tu.steps_per_sync;
-   a.cfg.step_cap = 0;
+   a.cfg.step_cap = c->step_cap;
    a.cfg.total_traj = c->total_traj;
    a.cfg.run_index = c->run_index;
    a.ctr = c->d_ctr;
@@ -1476,7 +1482,7 @@ int spx_run_static(spx_ctx_t c, const spx_tuning* tuning, int32_t* counts, int64
    a.cfg.record_final = c->record_final;
    a.cfg.n_problems = n;
    a.cfg.steps_per_sync = tu.steps_per_sync;
-   a.cfg.step_cap = 0;
+   a.cfg.step_cap = c->step_cap;
    a.cfg.total_traj = total;
    a.cfg.run_index = c->run_index;
    a.ctr = reinterpret_cast<spx::RunCounters*>(scratch);

@@ -192,6 +192,16 @@ template <class R> __device__ __forceinline__ R u01(uint32_t x);
 template <> __device__ __forceinline__ double u01<double>(uint32_t x) { return u01d(x); }
 template <> __device__ __forceinline__ float u01<float>(uint32_t x) { return u01f(x); }
 
+// sin and cos of 2 pi u for u in (0,1). Double: sincospi. Float: the angle reduced to [-pi, pi]
+// (2 pi (u - rint(u)), the same sine and cosine) and the special-function unit's approximations,
+// absolute error below 2^-21 on that interval; sincospif is a software routine of some thirty
+// instructions that the fast-math build does not replace.
+__device__ __forceinline__ void sincos_2pi(double u, double* s, double* c) { sincospi(2.0 * u, s, c); }
+__device__ __forceinline__ void sincos_2pi(float u, float* s, float* c)
+{
+   __sincosf(6.28318530717958647692f * (u - rintf(u)), s, c);
+}
+
 // Four standard normals (Box-Muller on (u0,u1) and (u2,u3)): n0 = r cos(2 pi u1), n1 = r sin(2 pi u1)
 template <class R>
 __device__ __forceinline__ void normals4(uint4 b, R n[4])
@@ -199,8 +209,8 @@ __device__ __forceinline__ void normals4(uint4 b, R n[4])
    R r0 = m_sqrt(R(-2) * m_log(u01<R>(b.x)));
    R r1 = m_sqrt(R(-2) * m_log(u01<R>(b.z)));
    R s0, c0, s1, c1;
-   m_sincospi(R(2) * u01<R>(b.y), &s0, &c0);
-   m_sincospi(R(2) * u01<R>(b.w), &s1, &c1);
+   sincos_2pi(u01<R>(b.y), &s0, &c0);
+   sincos_2pi(u01<R>(b.w), &s1, &c1);
    n[0] = r0 * c0;
    n[1] = r0 * s0;
    n[2] = r1 * c1;

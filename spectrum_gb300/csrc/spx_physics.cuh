@@ -733,19 +733,28 @@ __device__ V3<R> bnd_normal(const BndParamsT<R>& b, V3<R> pos)
    }
 }
 
-// EvaluateBoundary of every boundary class (src/boundary_time.cc, src/boundary_space.cc,
-// src/boundary_momentum.cc). For time boundaries the delta is formed from the accumulated time.
+// EvaluateBoundary (src/boundary_time.cc, src/boundary_space.cc, src/boundary_momentum.cc), one
+// evaluator per boundary class so that a loop over the boundaries of one class dispatches over that
+// class's kinds only. For time boundaries the delta is formed from the accumulated time.
 template <class R, class A>
-__device__ __forceinline__ void eval_bnd(const BndParamsT<R>& b, BndState<R>& st, const A& t, V3<R> pos, V3<R> mom,
-                                         V3<R> bhat, V3<R> region, int traj)
+__device__ __forceinline__ void eval_time_bnd(const BndParamsT<R>& b, BndState<R>& st, const A& t)
 {
-   switch (b.kind) {
-   case kBtTimeExpire: case kBtTimePass: st.delta = (R)acc_diff(t, b.timemark, b.timemark_lo); break;
-   case kBtTimeRecurrent: {
+   if (b.kind == kBtTimeRecurrent) {
       R k = (R)((b.max_crossings - st.crossings_left) + 1);
       st.delta = (R)acc_diff(t, k * b.timemark, k * b.timemark_lo);
-      break;
    }
+   else st.delta = (R)acc_diff(t, b.timemark, b.timemark_lo);  // expire, pass
+}
+
+template <class R>
+__device__ __forceinline__ void eval_space_bnd(const BndParamsT<R>& b, BndState<R>& st, V3<R> pos, V3<R> region)
+{
+   // spheres first: the usual inner and outer boundaries of the heliospheric set-ups
+   if (b.kind == kBtSphereAbsorb || b.kind == kBtSphereReflect || b.kind == kBtSpherePass) {
+      st.delta = norm(pos - ld3(b.origin)) - b.radius;
+      return;
+   }
+   switch (b.kind) {
    case kBtPlaneAbsorb: case kBtPlaneReflect: case kBtPlanePass:
       st.delta = dot(pos - ld3(b.origin), ld3(b.norm));
       break;
@@ -761,10 +770,6 @@ __device__ __forceinline__ void eval_bnd(const BndParamsT<R>& b, BndState<R>& st
       }
       break;
    }
-   case kBtSphereAbsorb: case kBtSphereReflect: case kBtSpherePass: {
-      st.delta = norm(pos - ld3(b.origin)) - b.radius;
-      break;
-   }
    case kBtRankineAbsorb: {
       V3<R> pr = pos - ld3(b.origin);
       R z = dot(pr, ld3(b.axis)), r = norm(pr);
@@ -778,22 +783,38 @@ __device__ __forceinline__ void eval_bnd(const BndParamsT<R>& b, BndState<R>& st
       break;
    }
    case kBtRegionAbsorb: st.delta = region[b.region_ind] - b.region_val; break;
-   case kBtMomentumInject: case kBtMomentumPass: case kBtMomentumSlab: case kBtMomentumShell:
-      st.delta = (traj == kLorentz ? norm(mom) : mom.x) - b.momentum;
-      if (b.kind == kBtMomentumSlab && st.delta * st.delta_old < R(0)) {
-         if (dot(pos - ld3(b.slab_r0), ld3(b.slab_n)) * dot(pos - ld3(b.slab_r1), ld3(b.slab_n)) > R(0)) st.delta_old = st.delta;
-      }
-      if (b.kind == kBtMomentumShell && st.delta * st.delta_old < R(0)) {
-         R rd = norm(pos - ld3(b.slab_r0));
-         if (rd < b.r1 || rd > b.r2) st.delta_old = st.delta;
-      }
-      break;
+   }
+}
+
+template <class R>
+__device__ __forceinline__ void eval_mom_bnd(const BndParamsT<R>& b, BndState<R>& st, V3<R> pos, V3<R> mom,
+                                             V3<R> bhat, int traj)
+{
    // BoundaryMirror::EvaluateBoundary (src/boundary_momentum.cc:329-339): the parallel momentum, which is
    // p mu for Focused, the native third component for the guiding-centre types and p . bhat for Lorentz
-   case kBtMirror:
+   if (b.kind == kBtMirror) {
       st.delta = (traj == kFocused) ? mom.x * mom.y : (traj == kGuiding ? mom.z : dot(mom, bhat));
-      break;
+      return;
    }
+   st.delta = (traj == kLorentz ? norm(mom) : mom.x) - b.momentum;
+   if (b.kind == kBtMomentumSlab && st.delta * st.delta_old < R(0)) {
+      if (dot(pos - ld3(b.slab_r0), ld3(b.slab_n)) * dot(pos - ld3(b.slab_r1), ld3(b.slab_n)) > R(0)) st.delta_old = st.delta;
+   }
+   if (b.kind == kBtMomentumShell && st.delta * st.delta_old < R(0)) {
+      R rd = norm(pos - ld3(b.slab_r0));
+      if (rd < b.r1 || rd > b.r2) st.delta_old = st.delta;
+   }
+}
+
+// CLS: the class of the boundary when the caller knows it (0 time, 1 space, 2 momentum), -1 from b.cls
+template <int CLS, class R, class A>
+__device__ __forceinline__ void eval_bnd(const BndParamsT<R>& b, BndState<R>& st, const A& t, V3<R> pos, V3<R> mom,
+                                         V3<R> bhat, V3<R> region, int traj)
+{
+   const int cls = CLS >= 0 ? CLS : b.cls;
+   if (cls == 0) eval_time_bnd(b, st, t);
+   else if (cls == 1) eval_space_bnd(b, st, pos, region);
+   else eval_mom_bnd(b, st, pos, mom, bhat, traj);
 }
 
 // BoundaryBase::ResetBoundary (src/boundary_base.cc:138-162)
@@ -803,18 +824,18 @@ __device__ __forceinline__ void reset_bnd(const BndParamsT<R>& b, BndState<R>& s
 {
    st.crossings_left = b.max_crossings;
    st.delta_old = R(0);
-   eval_bnd(b, st, t, pos, mom, bhat, region, traj);
+   eval_bnd<-1>(b, st, t, pos, mom, bhat, region, traj);
    st.delta_old = st.delta;
    if (st.delta_old == R(0)) st.delta_old = -Lim<R>::tiny * m_abs(scale);
    st.crossed = 0;
 }
 
 // BoundaryBase::ComputeBoundary (src/boundary_base.cc:105-127)
-template <class R, class A>
+template <int CLS, class R, class A>
 __device__ __forceinline__ void compute_bnd(const BndParamsT<R>& b, BndState<R>& st, const A& t, V3<R> pos, V3<R> mom,
                                             V3<R> bhat, V3<R> region, int traj)
 {
-   eval_bnd(b, st, t, pos, mom, bhat, region, traj);
+   eval_bnd<CLS>(b, st, t, pos, mom, bhat, region, traj);
    if (st.delta * st.delta_old <= R(0)) {
       st.crossed = 1;
       if (st.delta * st.delta_old == R(0)) st.delta = -st.delta_old;
@@ -823,13 +844,13 @@ __device__ __forceinline__ void compute_bnd(const BndParamsT<R>& b, BndState<R>&
 }
 
 // BoundaryBase::RecordBoundary (src/boundary_base.cc:168-191)
-template <class R, class A>
+template <int CLS, class R, class A>
 __device__ __forceinline__ void record_bnd(const BndParamsT<R>& b, BndState<R>& st, const A& t, V3<R> pos, V3<R> mom,
                                            V3<R> bhat, V3<R> region, int traj)
 {
    if (st.crossed) {
       st.crossings_left--;
-      if (b.recurrent) eval_bnd(b, st, t, pos, mom, bhat, region, traj);
+      if (b.recurrent) eval_bnd<CLS>(b, st, t, pos, mom, bhat, region, traj);
       else st.delta_old = st.delta;
       st.crossed = 0;
    }

@@ -381,22 +381,23 @@ __device__ __forceinline__ void handle_crossings(Lane<R, A>& L, BndView<R> bv, c
                                                  unsigned crossed)
 {
    V3<R> pos = val3<R>(L.pos), mom = lane_mom(L);
-   const int nb = P.nbt + P.nbs + P.nbm;
    const int s_lo = P.nbt, m_lo = P.nbt + P.nbs;
    // momentum boundaries
    int active = -1;
-   for (int j = m_lo; j < nb; j++) {
+   for (int i = 0; i < P.nbm; i++) {
+      const int j = m_lo + i;
       if (!(crossed & (1u << j))) continue;
       active = j;
-      if (!bnd_param(P, j).reflect && bv.ld(j).crossings_left == 1) L.status |= TRAJ_MOMENTUM_CROSSED | TRAJ_FINISH;
+      if (!P.bm[i].reflect && bv.ld(j).crossings_left == 1) L.status |= TRAJ_MOMENTUM_CROSSED | TRAJ_FINISH;
    }
    if (active >= 0) distro_events<TT>(L, sp, s0, Pd, active, S);
    // spatial boundaries
    active = -1;
-   for (int j = s_lo; j < m_lo; j++) {
+   for (int i = 0; i < P.nbs; i++) {
+      const int j = s_lo + i;
       if (!(crossed & (1u << j))) continue;
       active = j;
-      const BndParamsT<R>& b = bnd_param(P, j);
+      const BndParamsT<R>& b = P.bs[i];
       BndState<R> st = bv.ld(j);
       if (b.reflect) {
          // src/trajectory_base.cc:462-483: mirror the position, reverse the momentum
@@ -410,7 +411,7 @@ __device__ __forceinline__ void handle_crossings(Lane<R, A>& L, BndView<R> bv, c
          else if (TT == kGuiding) L.mom.z = neg(L.mom.z);
          pos = val3<R>(L.pos);
          mom = lane_mom(L);
-         compute_bnd(b, st, L.t, pos, mom, sp.bhat, sp.region, TT);
+         compute_bnd<1>(b, st, L.t, pos, mom, sp.bhat, sp.region, TT);
          st.crossings_left--;
          bv.st(j, st);
       }
@@ -425,11 +426,24 @@ __device__ __forceinline__ void handle_crossings(Lane<R, A>& L, BndView<R> bv, c
       if (bv.ld(j).crossings_left == 1) L.status |= TRAJ_TIME_CROSSED | TRAJ_FINISH;
    }
    if (active >= 0) distro_events<TT>(L, sp, s0, Pd, active, S);
-   for (int j = 0; j < nb; j++)
+   // RecordBoundary of the crossed ones, in slot order
+   for (int j = 0; j < s_lo; j++)
       if (crossed & (1u << j)) {
          BndState<R> st = bv.ld(j);
-         record_bnd(bnd_param(P, j), st, L.t, pos, mom, sp.bhat, sp.region, TT);
+         record_bnd<0>(P.bt[j], st, L.t, pos, mom, sp.bhat, sp.region, TT);
          bv.st(j, st);
+      }
+   for (int i = 0; i < P.nbs; i++)
+      if (crossed & (1u << (s_lo + i))) {
+         BndState<R> st = bv.ld(s_lo + i);
+         record_bnd<1>(P.bs[i], st, L.t, pos, mom, sp.bhat, sp.region, TT);
+         bv.st(s_lo + i, st);
+      }
+   for (int i = 0; i < P.nbm; i++)
+      if (crossed & (1u << (m_lo + i))) {
+         BndState<R> st = bv.ld(m_lo + i);
+         record_bnd<2>(P.bm[i], st, L.t, pos, mom, sp.bhat, sp.region, TT);
+         bv.st(m_lo + i, st);
       }
 }
 
@@ -442,11 +456,27 @@ __device__ __forceinline__ void handle_boundaries(Lane<R, A>& L, BndView<R> bv, 
                                                   const ProblemDescT<R>& P, const ProblemDesc& Pd, const Sinks& S)
 {
    V3<R> pos = val3<R>(L.pos), mom = lane_mom(L);
-   const int nb = P.nbt + P.nbs + P.nbm;
    unsigned crossed = 0;
-   for (int j = 0; j < nb; j++) {
+   // one loop per class, each evaluating its own kinds: time, spatial, momentum slots in order
+   for (int j = 0; j < P.nbt; j++) {
       BndState<R> b = bv.ld(j);
-      compute_bnd(bnd_param(P, j), b, L.t, pos, mom, sp.bhat, sp.region, TT);
+      compute_bnd<0>(P.bt[j], b, L.t, pos, mom, sp.bhat, sp.region, TT);
+      if (b.crossed) crossed |= 1u << j;
+      else b.delta_old = b.delta;
+      bv.st(j, b);
+   }
+   for (int i = 0; i < P.nbs; i++) {
+      const int j = P.nbt + i;
+      BndState<R> b = bv.ld(j);
+      compute_bnd<1>(P.bs[i], b, L.t, pos, mom, sp.bhat, sp.region, TT);
+      if (b.crossed) crossed |= 1u << j;
+      else b.delta_old = b.delta;
+      bv.st(j, b);
+   }
+   for (int i = 0; i < P.nbm; i++) {
+      const int j = P.nbt + P.nbs + i;
+      BndState<R> b = bv.ld(j);
+      compute_bnd<2>(P.bm[i], b, L.t, pos, mom, sp.bhat, sp.region, TT);
       if (b.crossed) crossed |= 1u << j;
       else b.delta_old = b.delta;
       bv.st(j, b);
@@ -461,9 +491,10 @@ __device__ __forceinline__ bool space_terminate(Lane<R, A>& L, BndView<R> bv, co
                                                 const ProblemDescT<R>& P, const ProblemDesc& Pd, const Sinks& S)
 {
    V3<R> pos = val3<R>(L.pos), mom = lane_mom(L);
-   for (int j = P.nbt; j < P.nbt + P.nbs; j++) {
+   for (int i = 0; i < P.nbs; i++) {
+      const int j = P.nbt + i;
       BndState<R> b = bv.ld(j);
-      compute_bnd(bnd_param(P, j), b, L.t, pos, mom, sp.bhat, sp.region, TT);
+      compute_bnd<1>(P.bs[i], b, L.t, pos, mom, sp.bhat, sp.region, TT);
       bv.st(j, b);
       if (b.crossed && b.crossings_left == 1) {
          L.status |= TRAJ_SPATIAL_CROSSED | TRAJ_FINISH;
