@@ -397,6 +397,37 @@ def bench_other(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+def steady_rate(sim, tun, cap: int, launches: int = 3):
+    """Steps/s of the batch with every trajectory stopped after ``cap`` steps: every lane busy for the
+    whole launch, no drain (the best of ``launches`` launches)."""
+    from spectrum_gb300 import capi
+    sim.ctx.set_option(capi.SPX_OPT_STEP_CAP, cap)
+    best = 0.0
+    for _ in range(launches):
+        st = sim.MainLoop(tun)
+        best = max(best, st.steps / st.kernel_ms * 1e3)
+    sim.ctx.set_option(capi.SPX_OPT_STEP_CAP, 0)
+    return best
+
+
+def bench_steady(args):
+    import torch
+    from spectrum_gb300 import capi
+    from spectrum_gb300.simulation import open_problems
+    torch.cuda.set_device(torch.device("cuda", 0))
+    sim = open_problems(problems(args.per_energy), precision=capi.SPX_MIXED)
+    if args.tuning:
+        b, bps, sps = (int(x) for x in args.tuning.split(","))
+        tun = capi.Tuning(b, bps, sps, 1)
+    else:
+        tun = sim.ctx.autotune(0)
+    rate = steady_rate(sim, tun, args.steady, max(1, args.steps))
+    sim.close()
+    print(json.dumps({"metric": f"steady-state steps/s, every trajectory stopped after {args.steady} steps",
+                      "workload": WORKLOAD, "per_energy": args.per_energy, "value": rate, "unit": "steps/s",
+                      "tuning": [tun.block_size, tun.blocks_per_sm, tun.steps_per_sync]}), flush=True)
+
+
 def bench_accuracy(args):
     """One JSON line: the per-bin criterion on the LIS-weighted spectrum at a sample large enough to
     resolve it (the FP64 kernel on the persistent queue: results do not depend on the schedule)."""
@@ -434,6 +465,9 @@ def main():
     ap.add_argument("--tuning", default="", metavar="BLOCK,BLOCKS_PER_SM,STEPS_PER_SYNC",
                     help="a fixed launch shape for the persistent queue instead of the autotuner's (profiling)")
     ap.add_argument("--no-fp64", action="store_true")
+    ap.add_argument("--steady", type=int, default=0, metavar="CAP",
+                    help="instead of the benchmark: steady-state steps/s of the batch with every trajectory stopped "
+                         "after CAP steps (SPX_OPT_STEP_CAP), no drain of the queue (profiling)")
     ap.add_argument("--per-launch-steps", type=int, default=2,
                     help="one-slice launches timed for comparison (each pays the drain of the queue)")
     ap.add_argument("--workload", default="gcr", choices=["gcr"] + sorted(OTHER_WORKLOADS),
@@ -445,6 +479,8 @@ def main():
         return bench_other(args, rank, world, local)
     if args.accuracy:
         return bench_accuracy(args)
+    if args.steady:
+        return bench_steady(args)
     cfg = {"workload": WORKLOAD, "energies": 32, "per_energy": args.per_energy,
            "trajectories_per_step": 32 * args.per_energy * world, "time_flow": "backward", "background": "solar wind",
            "diffusion": "kappa_par = (0.1 AU) v/3 (R/1GV)^0.5, kappa_perp = 0.02 kappa_par",
@@ -519,6 +555,9 @@ def main():
             ms.append(st1.kernel_ms)
         per_launch = {"value": st1.trajectories * len(ms) / (sum(ms) / 1e3), "unit": UNIT, "launches": len(ms),
                       "ms_per_launch": statistics.mean(ms), "trajectories_per_launch": st1.trajectories}
+    # the rate with every lane busy (trajectories stopped after 4096 steps): the bound the drain keeps
+    # the whole run below
+    steady = steady_rate(sim, tun, 4096)
     sim.close()
     # The timed region: the K steps as one launch of the persistent queue over K slices. Slice k is
     # trajectory ids k*pe ... (k+1)*pe-1 of every energy (pe trajectories per energy), the ids that K
@@ -622,6 +661,7 @@ def main():
             "scaling": "weak", "vs_baseline": None, "dtype": "f32 (float-float accumulation)",
             "data": "synthetic (seeded Philox streams)", "config": cfg, "steps_per_s": steps_rate,
             "wall_s": wall, "tuning": tuning, "gpu_launches": 1, "per_launch_per_step": per_launch,
+            "steady_steps_per_s": steady,
             "fp64_plain": fp64,
             "e2e": {"value": e2e_val, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "roofline": roof, "clocks": clk}

@@ -84,7 +84,9 @@ extern "C" {
                                        1 Milstein, 2 RK2 */
 #define SPX_OPT_SPECIALIZE 10       /* 1 (default): SPX_MIXED Parker contexts whose problems share the diffusion class
                                        FullConstant or RigidityMagneticFieldPowerLaw run on kernels compiled for that
-                                       class; 0: on the kernel that dispatches at run time. Same trajectories. */
+                                       class, and, where every problem has one expiry or pass time boundary, two
+                                       spheres and no momentum boundary, for that layout; 2: for the class only;
+                                       0: on the kernel that dispatches at run time. Same trajectories. */
 #define SPX_OPT_STEP_CAP 11         /* 0 (default): off. N > 0: spx_run stops every trajectory after N steps, as the
                                        autotuner's timing samples do: a steady-state throughput sample with no drain
                                        of the queue; trajectories stopped by the cap are neither finished nor binned */

@@ -50,9 +50,10 @@ struct spx_ctx {
    // the Butcher table: general (not Euler or, for the RK types, the classic RK4) tables run on the
    // *_f64rk / *_f64fdrk kernels, which read it from constant memory
    bool general_rk = false;
-   // SPX_OPT_SPECIALIZE 0: the FP32 Parker kernels dispatch on the diffusion class at run time even where
-   // a kernel specialised for it exists (the specialised and generic kernels give the same trajectories)
-   bool no_special = false;
+   // SPX_OPT_SPECIALIZE: 1 the FP32 Parker kernels compiled for the problems' diffusion class and, where
+   // it matches, their boundary layout; 2 for the diffusion class only; 0 the kernels that dispatch at
+   // run time (all give the same trajectories)
+   int specialize = 1;
    uint32_t step_cap = 0;  // SPX_OPT_STEP_CAP
    int rk_stages = 1, rk_order = 1, rk_adaptive = 0, rk_offset = 0;
    double steps_per_orbit = 100.0;
@@ -288,10 +289,27 @@ int common_diffusion(const spx_ctx* c)
 
 int parker_f32_special(const spx_ctx* c)
 {
-   if (c->precision != SPX_MIXED || c->general_rk || c->no_special) return -1;
+   if (c->precision != SPX_MIXED || c->general_rk || c->specialize == 0) return -1;
    if (c->traj != SPX_TRAJ_PARKER && c->traj != SPX_TRAJ_PARKER_SOURCE) return -1;
    const int k = common_diffusion(c);
    return (k == spx::kDfRigidityB || k == spx::kDfFull) ? k : -1;
+}
+
+// Whether every problem has the boundary layout spx::kLayoutSpheres: one expiry or pass time boundary,
+// two spheres, no momentum boundary.
+bool layout_spheres(const spx_ctx* c)
+{
+   if (c->specialize != 1 || c->problems.empty()) return false;
+   for (const auto& p : c->problems) {
+      const spx::ProblemDesc& d = p.pd;
+      if (d.nbt != 1 || d.nbs != 2 || d.nbm != 0) return false;
+      if ((d.bt[0].kind != spx::kBtTimeExpire && d.bt[0].kind != spx::kBtTimePass) || d.bt[0].recurrent) return false;
+      for (int i = 0; i < 2; i++) {
+         const int k = d.bs[i].kind;
+         if (k != spx::kBtSphereAbsorb && k != spx::kBtSphereReflect && k != spx::kBtSpherePass) return false;
+      }
+   }
+   return true;
 }
 
 cudaError_t launch(spx_ctx* c, const spx::LaunchArgs& a)
@@ -308,8 +326,8 @@ cudaError_t launch(spx_ctx* c, const spx::LaunchArgs& a)
       }
    }
    switch (parker_f32_special(c)) {
-   case spx::kDfRigidityB: return spx::launch_parker_f32rb(bg, a);
-   case spx::kDfFull: return spx::launch_parker_f32fc(bg, a);
+   case spx::kDfRigidityB: return layout_spheres(c) ? spx::launch_parker_f32rbs(bg, a) : spx::launch_parker_f32rb(bg, a);
+   case spx::kDfFull: return layout_spheres(c) ? spx::launch_parker_f32fcs(bg, a) : spx::launch_parker_f32fc(bg, a);
    default: break;
    }
    switch (c->traj) {
@@ -347,8 +365,10 @@ int occupancy(spx_ctx* c, int block, int slots)
       }
    }
    switch (parker_f32_special(c)) {
-   case spx::kDfRigidityB: return spx::occupancy_parker_f32rb(bg, block, slots);
-   case spx::kDfFull: return spx::occupancy_parker_f32fc(bg, block, slots);
+   case spx::kDfRigidityB:
+      return layout_spheres(c) ? spx::occupancy_parker_f32rbs(bg, block, slots) : spx::occupancy_parker_f32rb(bg, block, slots);
+   case spx::kDfFull:
+      return layout_spheres(c) ? spx::occupancy_parker_f32fcs(bg, block, slots) : spx::occupancy_parker_f32fc(bg, block, slots);
    default: break;
    }
    switch (c->traj) {
@@ -660,9 +680,10 @@ int spx_set_option(spx_ctx_t c, int option, double value)
       c->dirty = true;
       return SPX_OK;
    case SPX_OPT_SPECIALIZE:
-      // 0: no kernel specialised for the diffusion class (a captured launch is re-captured)
-      if (value != 0.0 && value != 1.0) return SPX_ERR_INVALID_ARG;
-      c->no_special = value == 0.0;
+      // 0: no specialised kernel; 1: diffusion class and boundary layout; 2: diffusion class only
+      // (a captured launch is re-captured)
+      if (value != 0.0 && value != 1.0 && value != 2.0) return SPX_ERR_INVALID_ARG;
+      c->specialize = (int)value;
       drop_graph(c);
       return SPX_OK;
    case SPX_OPT_STEP_CAP:

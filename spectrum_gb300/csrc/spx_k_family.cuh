@@ -9,7 +9,7 @@
 
 namespace spx {
 
-template <int TT, class R, int DM, bool GT, int DK = -1>
+template <int TT, class R, int DM, bool GT, int DK = -1, int BL = kLayoutAny>
 struct FamilyTU {
    // dynamic shared memory: the boundary states of every lane of a block
    static size_t smem(int slots, int block) { return (size_t)(slots > 0 ? slots : 1) * block * sizeof(BndState<R>); }
@@ -23,7 +23,7 @@ struct FamilyTU {
    {
       if constexpr (kBuilt<BG>) {
          const auto* P = static_cast<const ProblemDescT<R>*>(a.problems_r);
-         step_kernel<TT, BG, R, DM, GT, DK><<<a.grid, a.block, smem(a.bnd_slots, a.block.x), a.stream>>>(
+         step_kernel<TT, BG, R, DM, GT, DK, BL><<<a.grid, a.block, smem(a.bnd_slots, a.block.x), a.stream>>>(
              P, a.problems_d, a.cfg, a.ctr, a.counts, a.sums, a.n_events, a.records, a.queue);
          return cudaGetLastError();
       }
@@ -35,7 +35,7 @@ struct FamilyTU {
    {
       int n = 0;
       if constexpr (kBuilt<BG>) {
-         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<TT, BG, R, DM, GT, DK>, block, smem(slots, block)) !=
+         if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, step_kernel<TT, BG, R, DM, GT, DK, BL>, block, smem(slots, block)) !=
              cudaSuccess)
             n = 0;
       }
@@ -74,11 +74,12 @@ struct FamilyTU {
 // One translation unit: the kernels of one family, arithmetic, derivative method (DM 1: analytic
 // field derivatives; DM 0: the reference's compiled-in numerical ones, FP64 only) and table kind
 // (GT 1: any Butcher table, FP64 only).
-// SPX_FAMILY_TU_DK: the FP32 analytic kernels with the diffusion class fixed at compile time (DK).
-#define SPX_FAMILY_TU_DK(fam, prec, TT, DK)                                                                        \
+// SPX_FAMILY_TU_DK: the FP32 analytic kernels with the diffusion class fixed at compile time (DK), and
+// with it the boundary layout (BL, a BndLayout).
+#define SPX_FAMILY_TU_DK(fam, prec, TT, DK, BL)                                                                    \
    namespace spx {                                                                                                  \
-   cudaError_t launch_##fam##_##prec(int bg, const LaunchArgs& a) { return FamilyTU<TT, float, 1, false, DK>::launch(bg, a); } \
-   int occupancy_##fam##_##prec(int bg, int block, int slots) { return FamilyTU<TT, float, 1, false, DK>::occupancy(bg, block, slots); } \
+   cudaError_t launch_##fam##_##prec(int bg, const LaunchArgs& a) { return FamilyTU<TT, float, 1, false, DK, BL>::launch(bg, a); } \
+   int occupancy_##fam##_##prec(int bg, int block, int slots) { return FamilyTU<TT, float, 1, false, DK, BL>::occupancy(bg, block, slots); } \
    }
 
 #define SPX_FAMILY_TU(fam, prec, TT, R, DM, GT)                                                                    \

@@ -3,4 +3,4 @@
 // over the other diffusion classes and no difference-quotient gradients.
 #include "spx_k_family.cuh"
 
-SPX_FAMILY_TU_DK(parker, f32fc, kParker, kDfFull)
+SPX_FAMILY_TU_DK(parker, f32fc, kParker, kDfFull, kLayoutAny)

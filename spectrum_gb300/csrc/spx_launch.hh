@@ -36,11 +36,16 @@ struct LaunchArgs {
    int occupancy_##fam##_f64rk(int bg, int block, int slots);          \
    int occupancy_##fam##_f64fdrk(int bg, int block, int slots);
 SPX_DECLARE_FAMILY(parker)
-// the FP32 Parker kernels specialised for one diffusion class
+// the FP32 Parker kernels specialised for one diffusion class, and for it and the layout of one time
+// boundary and two spheres (kLayoutSpheres)
 cudaError_t launch_parker_f32rb(int bg, const LaunchArgs& a);
 cudaError_t launch_parker_f32fc(int bg, const LaunchArgs& a);
+cudaError_t launch_parker_f32rbs(int bg, const LaunchArgs& a);
+cudaError_t launch_parker_f32fcs(int bg, const LaunchArgs& a);
 int occupancy_parker_f32rb(int bg, int block, int slots);
 int occupancy_parker_f32fc(int bg, int block, int slots);
+int occupancy_parker_f32rbs(int bg, int block, int slots);
+int occupancy_parker_f32fcs(int bg, int block, int slots);
 SPX_DECLARE_FAMILY(lorentz)
 SPX_DECLARE_FAMILY(focused)
 SPX_DECLARE_FAMILY(guiding)

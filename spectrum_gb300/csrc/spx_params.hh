@@ -40,6 +40,11 @@ enum BndKind : int {
    kBtMomentumInject = 30, kBtMomentumPass, kBtMomentumSlab, kBtMomentumShell, kBtMirror
 };
 
+// Boundary layouts a kernel can be compiled for. kLayoutAny: counts and kinds from the descriptor.
+// kLayoutSpheres: exactly one time boundary (expiry or pass), two spheres (absorbing, reflecting or
+// passing) and no momentum boundary, the set-up of the heliospheric modulation runs.
+enum BndLayout : int { kLayoutAny = 0, kLayoutSpheres = 1 };
+
 enum IniKind : int {
    kItFixed = 1, kItInterval,
    kIsFixed = 10, kIsLine, kIsCircle, kIsBox, kIsSphere, kIsSphereSector, kIsRankine, kIsCylinder, kIsCylinderSector,

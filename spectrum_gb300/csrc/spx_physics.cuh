@@ -736,21 +736,23 @@ __device__ V3<R> bnd_normal(const BndParamsT<R>& b, V3<R> pos)
 // EvaluateBoundary (src/boundary_time.cc, src/boundary_space.cc, src/boundary_momentum.cc), one
 // evaluator per boundary class so that a loop over the boundaries of one class dispatches over that
 // class's kinds only. For time boundaries the delta is formed from the accumulated time.
-template <class R, class A>
+// BL 1: the boundary layout fixed at compile time (one expiry or pass time boundary and spheres, see
+// BndLayout); its evaluators skip the other kinds.
+template <int BL, class R, class A>
 __device__ __forceinline__ void eval_time_bnd(const BndParamsT<R>& b, BndState<R>& st, const A& t)
 {
-   if (b.kind == kBtTimeRecurrent) {
+   if (BL != 1 && b.kind == kBtTimeRecurrent) {
       R k = (R)((b.max_crossings - st.crossings_left) + 1);
       st.delta = (R)acc_diff(t, k * b.timemark, k * b.timemark_lo);
    }
    else st.delta = (R)acc_diff(t, b.timemark, b.timemark_lo);  // expire, pass
 }
 
-template <class R>
+template <int BL, class R>
 __device__ __forceinline__ void eval_space_bnd(const BndParamsT<R>& b, BndState<R>& st, V3<R> pos, V3<R> region)
 {
    // spheres first: the usual inner and outer boundaries of the heliospheric set-ups
-   if (b.kind == kBtSphereAbsorb || b.kind == kBtSphereReflect || b.kind == kBtSpherePass) {
+   if (BL == 1 || b.kind == kBtSphereAbsorb || b.kind == kBtSphereReflect || b.kind == kBtSpherePass) {
       st.delta = norm(pos - ld3(b.origin)) - b.radius;
       return;
    }
@@ -807,13 +809,13 @@ __device__ __forceinline__ void eval_mom_bnd(const BndParamsT<R>& b, BndState<R>
 }
 
 // CLS: the class of the boundary when the caller knows it (0 time, 1 space, 2 momentum), -1 from b.cls
-template <int CLS, class R, class A>
+template <int CLS, int BL = 0, class R, class A>
 __device__ __forceinline__ void eval_bnd(const BndParamsT<R>& b, BndState<R>& st, const A& t, V3<R> pos, V3<R> mom,
                                          V3<R> bhat, V3<R> region, int traj)
 {
    const int cls = CLS >= 0 ? CLS : b.cls;
-   if (cls == 0) eval_time_bnd(b, st, t);
-   else if (cls == 1) eval_space_bnd(b, st, pos, region);
+   if (cls == 0) eval_time_bnd<BL>(b, st, t);
+   else if (cls == 1) eval_space_bnd<BL>(b, st, pos, region);
    else eval_mom_bnd(b, st, pos, mom, bhat, traj);
 }
 
@@ -831,11 +833,11 @@ __device__ __forceinline__ void reset_bnd(const BndParamsT<R>& b, BndState<R>& s
 }
 
 // BoundaryBase::ComputeBoundary (src/boundary_base.cc:105-127)
-template <int CLS, class R, class A>
+template <int CLS, int BL = 0, class R, class A>
 __device__ __forceinline__ void compute_bnd(const BndParamsT<R>& b, BndState<R>& st, const A& t, V3<R> pos, V3<R> mom,
                                             V3<R> bhat, V3<R> region, int traj)
 {
-   eval_bnd<CLS>(b, st, t, pos, mom, bhat, region, traj);
+   eval_bnd<CLS, BL>(b, st, t, pos, mom, bhat, region, traj);
    if (st.delta * st.delta_old <= R(0)) {
       st.crossed = 1;
       if (st.delta * st.delta_old == R(0)) st.delta = -st.delta_old;

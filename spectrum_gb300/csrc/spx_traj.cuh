@@ -451,37 +451,45 @@ __device__ __forceinline__ void handle_crossings(Lane<R, A>& L, BndView<R> bv, c
 // ComputeAllBoundaries, the momentum/space/time handlers with their distribution events, and
 // UpdateAllBoundaries. A boundary that was not crossed is recorded right after it is computed
 // (RecordBoundary only copies delta to delta_old for it); crossed ones after their events.
-template <int TT, class R, class A>
+// Boundary counts per class: from the descriptor, or constants of the layout the kernel is compiled for
+// (the loops below then unroll).
+template <int BL, class R> __device__ __forceinline__ int n_time_bnd(const ProblemDescT<R>& P) { return BL == kLayoutSpheres ? 1 : P.nbt; }
+template <int BL, class R> __device__ __forceinline__ int n_space_bnd(const ProblemDescT<R>& P) { return BL == kLayoutSpheres ? 2 : P.nbs; }
+template <int BL, class R> __device__ __forceinline__ int n_mom_bnd(const ProblemDescT<R>& P) { return BL == kLayoutSpheres ? 0 : P.nbm; }
+
+template <int TT, int BL, class R, class A>
 __device__ __forceinline__ void handle_boundaries(Lane<R, A>& L, BndView<R> bv, const SD<R>& sp, const Start& s0,
                                                   const ProblemDescT<R>& P, const ProblemDesc& Pd, const Sinks& S)
 {
    V3<R> pos = val3<R>(L.pos), mom = lane_mom(L);
    unsigned crossed = 0;
+   const int nbt = n_time_bnd<BL>(P), nbs = n_space_bnd<BL>(P), nbm = n_mom_bnd<BL>(P);
    // one loop per class, each evaluating its own kinds: time, spatial, momentum slots in order
-   for (int j = 0; j < P.nbt; j++) {
+   for (int j = 0; j < nbt; j++) {
       BndState<R> b = bv.ld(j);
-      compute_bnd<0>(P.bt[j], b, L.t, pos, mom, sp.bhat, sp.region, TT);
+      compute_bnd<0, BL>(P.bt[j], b, L.t, pos, mom, sp.bhat, sp.region, TT);
       if (b.crossed) crossed |= 1u << j;
       else b.delta_old = b.delta;
       bv.st(j, b);
    }
-   for (int i = 0; i < P.nbs; i++) {
-      const int j = P.nbt + i;
+   for (int i = 0; i < nbs; i++) {
+      const int j = nbt + i;
       BndState<R> b = bv.ld(j);
-      compute_bnd<1>(P.bs[i], b, L.t, pos, mom, sp.bhat, sp.region, TT);
+      compute_bnd<1, BL>(P.bs[i], b, L.t, pos, mom, sp.bhat, sp.region, TT);
       if (b.crossed) crossed |= 1u << j;
       else b.delta_old = b.delta;
       bv.st(j, b);
    }
-   for (int i = 0; i < P.nbm; i++) {
-      const int j = P.nbt + P.nbs + i;
+   for (int i = 0; i < nbm; i++) {
+      const int j = nbt + nbs + i;
       BndState<R> b = bv.ld(j);
-      compute_bnd<2>(P.bm[i], b, L.t, pos, mom, sp.bhat, sp.region, TT);
+      compute_bnd<2, BL>(P.bm[i], b, L.t, pos, mom, sp.bhat, sp.region, TT);
       if (b.crossed) crossed |= 1u << j;
       else b.delta_old = b.delta;
       bv.st(j, b);
    }
-   if (!crossed) return;
+   // a crossing is rare: keep its handling off the straight-line path
+   if (__builtin_expect(crossed == 0u, 1)) return;
    handle_crossings<TT>(L, bv, sp, s0, P, Pd, S, crossed);
 }
 
@@ -580,7 +588,7 @@ __device__ __noinline__ bool parker_divk_fd(const ProblemDescT<R>& P, int deriv_
    return true;
 }
 
-template <int BG, int DK, class R, class A>
+template <int BG, int DK, int BL, class R, class A>
 __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, Start& s0,
                                                const ProblemDescT<R>& P, const ProblemDesc& Pd, const RunConfig& cfg,
                                                const Sinks& S)
@@ -633,7 +641,7 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, Sta
    R dtp = R(0.5) * sp.dmax / norm(slope);
    dtp = m_min(dtp, R(0.5) * (sp.dmax * sp.dmax) / m_max(K.perp, K.para));
    dtp = m_min(dtp, R(0.5) * R(3) * R(0.01) / m_abs(divU));
-   L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bv, P.nbt, fwd);
+   L.dt = time_proximity(m_min(dtp, L.dt_adapt), sp.dmax, bv, n_time_bnd<BL>(P), fwd);
    // EulerDiffSlopes (src/trajectory_parker.cc:159-180)
    R n[4];
    normals4<R>(rng_block(P.seed, L.steps, L.traj_id, P.problem_id, kRngStep, L.attempt), n);
@@ -673,7 +681,7 @@ __device__ __forceinline__ void parker_advance(Lane<R, A>& L, BndView<R> bv, Sta
       }
    }
    if (sa != R(0)) L.amp += dts * sa * m_exp(L.wgt);
-   handle_boundaries<kParker>(L, bv, sp, s0, P, Pd, S);
+   handle_boundaries<kParker, BL>(L, bv, sp, s0, P, Pd, S);
    L.steps++;
 }
 
@@ -870,7 +878,7 @@ __device__ __forceinline__ void parker_advance_gt(Lane<R, A>& L, BndView<R> bv, 
       return;
    }
    acc_add(L.pos.x, dr.x); acc_add(L.pos.y, dr.y); acc_add(L.pos.z, dr.z);
-   handle_boundaries<kParker>(L, bv, sp, s0, P, Pd, S);
+   handle_boundaries<kParker, kLayoutAny>(L, bv, sp, s0, P, Pd, S);
    L.steps++;
 }
 
@@ -1320,7 +1328,7 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, Start& 
       if constexpr (kFP64) { acc_add(L.pos.x, dr_perp.x); acc_add(L.pos.y, dr_perp.y); acc_add(L.pos.z, dr_perp.z); }
       else add3(L.pos, dr_perp);
    }
-   handle_boundaries<TT>(L, bv, sp, s0, P, Pd, S);
+   handle_boundaries<TT, kLayoutAny>(L, bv, sp, s0, P, Pd, S);
    if (!(L.status & TRAJ_FINISH) && TT == kFocused) clamp_mu<A, R>(L.mom);
    L.steps++;
 }
@@ -1445,7 +1453,9 @@ __device__ __forceinline__ void start_lane(Lane<R, A>& L, BndView<R> bv, Start& 
 // kernels carry no finite-difference code (whose out-of-line calls would pin the field record to
 // the stack).
 // DK >= 0: a kernel specialised for one diffusion class (the Parker types); -1 dispatches at run time.
-template <int TT, int BG, class R, int DM, bool GT, int DK>
+// BL: the boundary layout (BndLayout) the Parker step is compiled for; kLayoutAny reads it from the
+// descriptor.
+template <int TT, int BG, class R, int DM, bool GT, int DK, int BL>
 __global__ void __launch_bounds__(128, sizeof(R) == 4 ? SPX_MIN_BLOCKS_F32 : SPX_MIN_BLOCKS_F64)
 step_kernel(const ProblemDescT<R>* __restrict__ P, const ProblemDesc* __restrict__ Pd, RunConfig cfg,
             RunCounters* ctr, int32_t* counts, double* sums, unsigned long long* n_events, TrajRecord* rec, int queue)
@@ -1517,7 +1527,7 @@ step_kernel(const ProblemDescT<R>* __restrict__ P, const ProblemDesc* __restrict
                if (TT == kParker) parker_advance_gt<BG>(L, bv, s0, Pp, Pd[L.prob], cfg, S, tab);
                else rk_advance<TT, BG, R, A>(L, bv, s0, Pp, Pd[L.prob], cfg, S, tab);
             }
-            else if (TT == kParker) parker_advance<BG, DK>(L, bv, s0, Pp, Pd[L.prob], cfg, S);
+            else if (TT == kParker) parker_advance<BG, DK, BL>(L, bv, s0, Pp, Pd[L.prob], cfg, S);
             else if (cfg.rk == 25) rk_advance<TT, BG, R, A>(L, bv, s0, Pp, Pd[L.prob], cfg, S, FixedRk<4>{});
             else rk_advance<TT, BG, R, A>(L, bv, s0, Pp, Pd[L.prob], cfg, S, FixedRk<1>{});
             // Integrate's safety limits (src/trajectory_base.cc:964-992)

@@ -306,25 +306,27 @@ def test_run_refuses_trajectory_ids_beyond_32_bits(built_lib):
 @pytest.mark.parametrize("workload", ["modulation", "diffusion"])
 def test_specialised_kernels_equal_the_generic_one(built_lib, workload):
     """SPX_MIXED Parker contexts run on kernels compiled for their diffusion class (RigidityMagneticField-
-    PowerLaw, FullConstant); SPX_OPT_SPECIALIZE 0 forces the kernel that dispatches at run time. The same
-    trajectories, bin for bin (the two differ only in the dispatch the compiler removed)."""
+    PowerLaw, FullConstant) and, for the modulation set-up (a time limit and two spheres), for that
+    boundary layout; SPX_OPT_SPECIALIZE 2 keeps the class only, 0 forces the kernel that dispatches at run
+    time. The same trajectories, bin for bin (they differ only in the dispatch the compiler removed)."""
     from spectrum_gb300.simulation import open_problems
     if workload == "modulation":
         pbs = workloads.gcr_modulation(n_traj=2000, energies_mev=[100.0, 1000.0], t_max_years=0.1)
     else:
         pbs = [workloads.diffusion_uniform(n_traj=4000, t_end=0.2)]
     out = []
-    for special in (1, 0):
+    for special in (0, 1, 2):
         sim = open_problems(pbs, precision=capi.SPX_MIXED, record=True)
         sim.ctx.set_option(capi.SPX_OPT_SPECIALIZE, float(special))
         st = sim.MainLoop()
         out.append((st, [sim.ctx.records(k, p.n_traj) for k, p in enumerate(pbs)],
                     [sim.ctx.distribution(k, 0) for k in range(len(pbs))]))
         sim.close()
-    (sa, ra, da), (sb, rb, db) = out
-    assert sa.steps == sb.steps
-    for x, y in zip(ra, rb):
-        assert np.array_equal(x["steps"], y["steps"])
-        assert np.array_equal(x["pos"], y["pos"])
-    for x, y in zip(da, db):
-        assert np.array_equal(x[0], y[0])
+    sa, ra, da = out[0]
+    for sb, rb, db in out[1:]:
+        assert sa.steps == sb.steps
+        for x, y in zip(ra, rb):
+            assert np.array_equal(x["steps"], y["steps"])
+            assert np.array_equal(x["pos"], y["pos"])
+        for x, y in zip(da, db):
+            assert np.array_equal(x[0], y[0])
