@@ -163,6 +163,25 @@ int spx_add_problem(spx_ctx_t ctx, int64_t n_traj, uint64_t seed, const uint8_t*
 int spx_set_background_grid(spx_ctx_t ctx, const int64_t n[3], const double cent_min[3], const double zone_length[3],
                             const double* values);
 
+/* The data of a gridded background (kind 6) as the reference's Cartesian server holds it: the
+ * layout of its reader's data file (src/reader_cartesian.cc:28-166), n_blocks[0] x n_blocks[1] x
+ * n_blocks[2] blocks of 4 x 4 x 4 zones spanning [domain_min, domain_max] (the .info header, in
+ * au), blocks x fastest and in each block zones x fastest, six doubles per zone (U, then B, in the
+ * reference's fluid units). Each point is interpolated in its own block with that block's
+ * zone-centre origin and zone length, as the front end does (src/server_cartesian.cc:274-330,
+ * 549-865), with ghost_cells (0 or 1) ghost layers per block side (SERVER_NUM_GHOST_CELLS); the
+ * values of zones past a block's faces are its neighbours'. Fields are converted to code units
+ * after the sums with the ratios spx_grid_units gives. Copies to device memory now (this call
+ * allocates); replaces a grid set by spx_set_background_grid. Replaces the server's data file and
+ * MPI block service. */
+int spx_set_background_blocks(spx_ctx_t ctx, const int32_t n_blocks[3], const double domain_min[3],
+                              const double domain_max[3], int ghost_cells, const double* values);
+
+/* The unit conversion of the reference's data server (src/server_cartesian.cc:710-716): out[0..3] =
+ * Fluid/Particle ratios of length, velocity and magnetic field, and Fluid::c_code
+ * (common/physics.hh:18-55, common/specie.hh:25-64). Needs no device. */
+void spx_grid_units(double out[4]);
+
 /* Integrate every trajectory of every problem; replaces MainLoop (src/simulation.cc:818-835).
  * Enqueues on the context stream and returns; tuning may be NULL (autotuned). Each call draws
  * fresh trajectory ids, so repeated calls add new trajectories to the distributions. */

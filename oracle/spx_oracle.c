@@ -56,6 +56,7 @@ static double nudged(double v) { return g_nudge_libm ? nextafter(v, v >= 0.0 ? I
 #define M_PI_ 3.141592653589793238462643383279502884E+0
 
 static const double c_light = 2.99792458e+10;
+#define AU_CM 1.495978707e+13 /* Fluid::unit_length, the astronomical unit in cm */
 static double unit_velocity(void) { return 0.1 * c_light; }
 static double c_code(void) { return c_light / unit_velocity(); }
 static const double p_mass = 1.0;   /* proton mass / unit_mass */
@@ -1018,6 +1019,11 @@ static struct {
    v3 cent, zone;
    double zone_min;
    double* v; /* 8 per node: U, B, |B|, unused */
+   /* block mode (the reference's Cartesian server over its reader's data): nb[0] nb[1] nb[2] blocks
+    * of 4^3 zones over [dmin, dmax] (file units), values in fluid units, ghost cells per block side */
+   int nb[3], ghost;
+   v3 dmin, dmax, blen;
+   double units[4]; /* Fluid/Particle length, velocity and magnetic ratios; Fluid::c_code */
 } g_grid;
 
 void spx_oracle_set_grid(const int64_t n[3], const double cent_min[3], const double zone_length[3],
@@ -1025,6 +1031,7 @@ void spx_oracle_set_grid(const int64_t n[3], const double cent_min[3], const dou
 {
    int64_t i, nodes = n[0] * n[1] * n[2];
    int k, q;
+   g_grid.nb[0] = g_grid.nb[1] = g_grid.nb[2] = 0;
    free(g_grid.v);
    g_grid.v = (double*)calloc((size_t)nodes * 8, sizeof(double));
    for (k = 0; k < 3; k++) {
@@ -1041,15 +1048,131 @@ void spx_oracle_set_grid(const int64_t n[3], const double cent_min[3], const dou
    }
 }
 
+/* Block mode: the reader's layout (src/reader_cartesian.cc:117-166) -- blocks x fastest, in each
+ * block 4^3 zones x fastest, six values per zone -- regrouped by dimension (its variables_by_dimen)
+ * with |B| per node appended. */
+void spx_oracle_set_grid_blocks(const int nb[3], const double dmin[3], const double dmax[3], int ghost,
+                                const double* values, const double units[4])
+{
+   int64_t nodes, b, z;
+   int k, q, n[3];
+   for (k = 0; k < 3; k++) n[k] = 4 * nb[k];
+   nodes = (int64_t)n[0] * n[1] * n[2];
+   free(g_grid.v);
+   g_grid.v = (double*)calloc((size_t)nodes * 8, sizeof(double));
+   for (k = 0; k < 3; k++) {
+      g_grid.n[k] = n[k];
+      g_grid.nb[k] = nb[k];
+      g_grid.dmin.x[k] = dmin[k];
+      g_grid.dmax.x[k] = dmax[k];
+      g_grid.blen.x[k] = (dmax[k] - dmin[k]) / (double)nb[k];  /* block_length, :97 */
+   }
+   for (k = 0; k < 4; k++) g_grid.units[k] = units[k];
+   g_grid.ghost = ghost;
+   for (b = 0; b < (int64_t)nb[0] * nb[1] * nb[2]; b++) {
+      int64_t bi = b % nb[0], bj = (b / nb[0]) % nb[1], bk = b / ((int64_t)nb[0] * nb[1]);
+      for (z = 0; z < 64; z++) {
+         int64_t i = 4 * bi + z % 4, j = 4 * bj + (z / 4) % 4, kk = 4 * bk + z / 16;
+         const double* v = values + 6 * (64 * b + z);
+         double* o = g_grid.v + 8 * (i + n[0] * (j + (int64_t)n[1] * kk));
+         for (q = 0; q < 6; q++) o[q] = v[q];
+         o[6] = sqrt(v[3] * v[3] + v[4] * v[4] + v[5] * v[5]);  /* src/server_cartesian.cc:566-569 */
+      }
+   }
+}
+
+/* The reference's unit conversion for server data (common/physics.hh:18-55 Fluid,
+ * common/specie.hh:25-64 Particle): Fluid/Particle length, velocity, magnetic ratios, Fluid::c_code. */
+void spx_oracle_grid_units(double out[4])
+{
+   const double m_p = 1.67262192596e-24, e = 4.8032044e-10;
+   const double p_vel = 0.1 * c_light, p_len = 1.0e10, p_time = p_len / p_vel;
+   const double p_mag = (m_p * p_vel) / (e * p_time), f_vel = 1.0e7, f_mag = f_vel * sqrt(m_p * 1.0);
+   out[0] = AU_CM / p_len;
+   out[1] = f_vel / p_vel;
+   out[2] = f_mag / p_mag;
+   out[3] = c_light / f_vel;
+}
+
+/* The primary block of "pos" and its stencil geometry, block mode: ReadCartesianGetNode
+ * (src/reader_cartesian.cc:264-277) on the position in file units; the block's faces as the reader
+ * and BlockBase::LoadDimensions form them (:291-300, src/block_base.cc:133-152, ghost layers
+ * included); ConfigureProperties (:158-171); GetZoneOffset (:194-203). Nonzero outside the domain. */
+static int grid_block_geometry(v3 pos, int bidx[3], v3* cent, v3* zl, int zone[3], double off[3])
+{
+   int k;
+   const double len = g_grid.units[0];
+   for (k = 0; k < 3; k++) {
+      double pc = pos.x[k] / AU_CM * 1.0e10;  /* pos / Fluid::unit_length * Particle::unit_length */
+      if (pc < g_grid.dmin.x[k] || pc > g_grid.dmax.x[k]) return 1;
+      bidx[k] = (int)((pc - g_grid.dmin.x[k]) / g_grid.blen.x[k]);
+      if (bidx[k] >= g_grid.nb[k]) return 1;
+   }
+   for (k = 0; k < 3; k++) {
+      double fmin_ = g_grid.dmin.x[k] + g_grid.blen.x[k] * bidx[k], fmax_ = fmin_ + g_grid.blen.x[k];
+      double o;
+      int bs = 4;
+      fmin_ *= len;
+      fmax_ *= len;
+      if (g_grid.ghost > 0) {
+         double incr = (fmax_ - fmin_) * ((double)g_grid.ghost / 4.0);
+         fmin_ -= incr;
+         fmax_ += incr;
+         bs += 2 * g_grid.ghost;
+      }
+      zl->x[k] = (fmax_ - fmin_) / (double)bs;
+      cent->x[k] = fmin_ + 0.5 * zl->x[k];
+      o = (pos.x[k] - cent->x[k]) / zl->x[k];
+      zone[k] = (int)o;
+      if (o < 0.0) zone[k]--;
+      off[k] = o - (double)zone[k];
+   }
+   return 0;
+}
+
+/* InteriorInterpolationStencil (src/server_cartesian.cc:206-268): weights and their derivatives */
+static void grid_stencil(const double lo[3], const double hi[3], v3 zl, double w[8], double der[24])
+{
+   int c;
+   for (c = 0; c < 8; c++) {
+      int ci = c & 1, cj = (c >> 1) & 1, ck = (c >> 2) & 1;
+      double fx = ci ? lo[0] : hi[0], fy = cj ? lo[1] : hi[1], fz = ck ? lo[2] : hi[2];
+      w[c] = fx * fy * fz;
+      der[3 * c + 0] = (ci ? fy * fz : -fy * fz) / zl.x[0];
+      der[3 * c + 1] = (cj ? fx * fz : -fx * fz) / zl.x[1];
+      der[3 * c + 2] = (ck ? fx * fy : -fx * fy) / zl.x[2];
+   }
+}
+
+int spx_oracle_grid_stencil(const double pos[3], int node[3], double cent_min[3], double zone_length[3], int zone[3],
+                            double offset[3], double w[8], double der[24])
+{
+   v3 cent, zl;
+   double hi[3];
+   int k;
+   if (g_grid.nb[0] == 0 || grid_block_geometry(V(pos[0], pos[1], pos[2]), node, &cent, &zl, zone, offset)) return 1;
+   for (k = 0; k < 3; k++) {
+      hi[k] = 1.0 - offset[k];
+      cent_min[k] = cent.x[k];
+      zone_length[k] = zl.x[k];
+   }
+   grid_stencil(offset, hi, zl, w, der);
+   return 0;
+}
+
 /* GetZoneOffset (src/block_base.cc:194-203), InteriorInterpolationStencil
  * (src/server_cartesian.cc:206-268), GetVariablesInterp1 (:551-666), GetVariables' dmax cap (:687)
  * and GetGradientsInterp1 (:724-823) for a point inside the block. Nonzero outside. */
+static int grid_fields_blocks(double dmax0, v3 pos, spdata* s);
+
 static int grid_fields(double dmax0, v3 pos, unsigned mask, spdata* s)
 {
    double lo[3], hi[3], w[8], der[24], var[6] = {0, 0, 0, 0, 0, 0}, grads[6][3], gbm[3] = {0, 0, 0};
    int z[3], k, c, q, u;
    int64_t nx = g_grid.n[0], nxy = nx * g_grid.n[1];
    if (!g_grid.v) return 1;
+   (void)mask;
+   if (g_grid.nb[0] > 0) return grid_fields_blocks(dmax0, pos, s);
    for (k = 0; k < 3; k++) {
       double o = (pos.x[k] - g_grid.cent.x[k]) / g_grid.zone.x[k];
       if (!(o >= 0.0 && o < (double)(g_grid.n[k] - 1))) return 1;
@@ -1097,7 +1220,85 @@ static int grid_fields(double dmax0, v3 pos, unsigned mask, spdata* s)
    s->dUdt = V(0, 0, 0);
    s->dBdt = V(0, 0, 0);
    s->dBmagdt = 0.0;
-   (void)mask;
+   return 0;
+}
+
+/* Block mode: GetVariables / GetGradients of the Cartesian front end at first order
+ * (src/server_cartesian.cc:549-716, 724-865). The weights come from the primary block's stencil; the
+ * values of zones past its faces are its neighbours' (the same global zones). Sums in fluid units,
+ * then the unit ratios; E = -(U x B) / Fluid::c_code before its ratio; dmax capped by the block's
+ * smallest zone length. A stencil that leaves the domain is a field error. */
+static int grid_fields_blocks(double dmax0, v3 pos, spdata* s)
+{
+   int bidx[3], zone[3], k, c, q, u, g[3];
+   v3 cent, zl;
+   double lo[3], hi[3], w[8], der[24], var[6] = {0, 0, 0, 0, 0, 0}, grads[6][3], gbm[3] = {0, 0, 0}, bm = 0.0;
+   const double vel = g_grid.units[1], mag = g_grid.units[2], cf = g_grid.units[3];
+   int64_t nx = g_grid.n[0], nxy = nx * g_grid.n[1];
+   if (grid_block_geometry(pos, bidx, &cent, &zl, zone, lo)) return 1;
+   for (k = 0; k < 3; k++) {
+      hi[k] = 1.0 - lo[k];
+      g[k] = 4 * bidx[k] + zone[k] - g_grid.ghost;  /* global zone of the stencil's corner 0 */
+      if (g[k] < 0 || g[k] + 1 >= g_grid.n[k]) return 1;
+   }
+   grid_stencil(lo, hi, zl, w, der);
+   for (q = 0; q < 6; q++) grads[q][0] = grads[q][1] = grads[q][2] = 0.0;
+   for (c = 0; c < 8; c++) {
+      int ci = c & 1, cj = (c >> 1) & 1, ck = (c >> 2) & 1;
+      const double* v = g_grid.v + 8 * ((g[2] + ck) * nxy + (int64_t)(g[1] + cj) * nx + (g[0] + ci));
+      for (q = 0; q < 6; q++) var[q] += w[c] * v[q];
+      bm += w[c] * v[6];
+      for (q = 0; q < 6; q++)
+         for (u = 0; u < 3; u++) grads[q][u] += der[3 * c + u] * v[q];
+      for (u = 0; u < 3; u++) gbm[u] += der[3 * c + u] * v[6];
+   }
+   s->dmax = fmin(dmax0, fmin(zl.x[0], fmin(zl.x[1], zl.x[2])));
+   {
+      v3 U = V(var[0], var[1], var[2]), B = V(var[3], var[4], var[5]), x = vcross(U, B);
+      for (k = 0; k < 3; k++) {
+         s->E.x[k] = (-x.x[k] / cf) * mag;
+         s->U.x[k] = U.x[k] * vel;
+         s->B.x[k] = B.x[k] * mag;
+      }
+   }
+   s->Bmag = bm * mag;
+   s->region = V(0.0, 0.0, 0.0);
+   if (s->Bmag < SP_TINY) return 1;
+   s->bhat = vdiv(s->B, s->Bmag);
+   for (u = 0; u < 3; u++) {
+      for (k = 0; k < 3; k++) {
+         s->gradU.m[u][k] = grads[k][u] * vel;
+         s->gradB.m[u][k] = grads[3 + k][u] * mag;
+      }
+      s->gradBmag.x[u] = gbm[u] * mag;
+   }
+   s->dUdt = V(0, 0, 0);
+   s->dBdt = V(0, 0, 0);
+   s->dBmagdt = 0.0;
+   return 0;
+}
+
+/* The gridded background's fields at one point, in the grid harness's order: U[3] B[3] Bmag E[3] dmax
+ * gradU[9] gradB[9] gradBmag[3]. Nonzero on a field error. */
+int spx_oracle_grid_fields(const double pos[3], double dmax0, double out[32])
+{
+   spdata s;
+   int k, a, b;
+   memset(&s, 0, sizeof s);
+   if (grid_fields(dmax0, V(pos[0], pos[1], pos[2]), 0xffffu, &s)) return 1;
+   for (k = 0; k < 3; k++) {
+      out[k] = s.U.x[k];
+      out[3 + k] = s.B.x[k];
+      out[7 + k] = s.E.x[k];
+      out[29 + k] = s.gradBmag.x[k];
+   }
+   out[6] = s.Bmag;
+   out[10] = s.dmax;
+   for (a = 0; a < 3; a++)
+      for (b = 0; b < 3; b++) {
+         out[11 + 3 * a + b] = s.gradU.m[a][b];
+         out[20 + 3 * a + b] = s.gradB.m[a][b];
+      }
    return 0;
 }
 

@@ -80,6 +80,22 @@ void spx_oracle_uniforms(uint64_t seed, uint32_t index, uint32_t traj, uint32_t 
 void spx_oracle_set_grid(const int64_t n[3], const double cent_min[3], const double zone_length[3],
                          const double* values);
 
+/* The gridded background in the layout of the reference's Cartesian reader (block mode): nb[0] x
+ * nb[1] x nb[2] blocks of 4^3 zones over [dmin, dmax] in file units (au), blocks x fastest and in
+ * each block zones x fastest, six fluid-unit values per zone (U, B); "ghost" ghost cells per block
+ * side; units = {Fluid/Particle length ratio, velocity ratio, magnetic ratio, Fluid::c_code}. */
+void spx_oracle_set_grid_blocks(const int nb[3], const double dmin[3], const double dmax[3], int ghost,
+                                const double* values, const double units[4]);
+/* The fields of the gridded background (either mode) at one point: U[3] B[3] Bmag E[3] dmax gradU[9]
+ * gradB[9] gradBmag[3]. Nonzero on a field error. */
+int spx_oracle_grid_fields(const double pos[3], double dmax0, double out[32]);
+/* The Fluid/Particle length, velocity and magnetic ratios and Fluid::c_code of the reference. */
+void spx_oracle_grid_units(double out[4]);
+/* The primary block and stencil of "pos" in block mode (block indices, zone-centre origin, zone
+ * length, zone, offset, the eight weights and 24 derivative weights). Nonzero outside the domain. */
+int spx_oracle_grid_stencil(const double pos[3], int node[3], double cent_min[3], double zone_length[3], int zone[3],
+                            double offset[3], double w[8], double der[24]);
+
 /* Philox4x32-10 of one counter under one key (for the generator's known-answer tests). */
 void spx_oracle_philox(const uint32_t ctr[4], const uint32_t key[2], uint32_t out[4]);
 

@@ -35,7 +35,7 @@ EXPORTS = ["spx_create", "spx_set_option", "spx_add_plugin", "spx_add_problem", 
            "spx_get_distribution_info", "spx_get_distribution", "spx_get_records", "spx_reset_distributions",
            "spx_dump", "spx_restore", "spx_strerror", "spx_destroy", "spx_version", "spx_run_static",
            "spx_autotune", "spx_set_background_grid", "spx_dump_distribution", "spx_restore_distribution",
-           "spx_get_distribution_records"]
+           "spx_get_distribution_records", "spx_set_background_blocks", "spx_grid_units"]
 
 #: bytes of the fixed device array spx_run_static works in (SPX_STATIC_SCRATCH_BYTES)
 STATIC_SCRATCH_BYTES = 512 * 1024
@@ -101,10 +101,20 @@ def load(path: str = LIB_PATH) -> ctypes.CDLL:
         lib.spx_version.restype = ctypes.c_char_p
         lib.spx_autotune.argtypes = [c_vp, ctypes.c_int64, ctypes.POINTER(Tuning)]
         lib.spx_set_background_grid.argtypes = [c_vp, c_vp, c_vp, c_vp, c_vp]
+        lib.spx_set_background_blocks.argtypes = [c_vp, c_vp, c_vp, c_vp, c_int, c_vp]
+        lib.spx_grid_units.argtypes = [c_vp]
+        lib.spx_grid_units.restype = None
         lib.spx_run_static.argtypes = [c_vp, ctypes.POINTER(Tuning), c_vp, ctypes.c_int64, c_vp, ctypes.c_int64, c_vp,
                                        ctypes.c_int64, c_vp, ctypes.c_int64, ctypes.POINTER(Stats)]
         _lib = lib
     return _lib
+
+
+def grid_units() -> np.ndarray:
+    """spx_grid_units: the Fluid/Particle length, velocity and magnetic ratios and Fluid::c_code."""
+    out = np.zeros(4)
+    load().spx_grid_units(out.ctypes.data)
+    return out
 
 
 def strerror(code: int) -> str:
@@ -180,6 +190,18 @@ class Context:
             raise ValueError("values must hold 6 numbers per node")
         check(self.lib.spx_set_background_grid(self._h, nn.ctypes.data, cm.ctypes.data, zl.ctypes.data, v.ctypes.data),
               "spx_set_background_grid")
+
+    def set_background_blocks(self, n_blocks, domain_min, domain_max, ghost_cells, values) -> None:
+        """spx_set_background_blocks: the reference Cartesian reader's blocks (values: blocks x fastest, in
+        each block 4^3 zones x fastest, 6 fluid-unit numbers per zone)."""
+        nb = np.ascontiguousarray(np.asarray(n_blocks, dtype=np.int32))
+        lo = np.ascontiguousarray(np.asarray(domain_min, dtype=np.float64))
+        hi = np.ascontiguousarray(np.asarray(domain_max, dtype=np.float64))
+        v = np.ascontiguousarray(np.asarray(values, dtype=np.float64))
+        if v.size != 6 * 64 * int(np.prod(nb.astype(np.int64))):
+            raise ValueError("values must hold 6 numbers per zone, 64 zones per block")
+        check(self.lib.spx_set_background_blocks(self._h, nb.ctypes.data, lo.ctypes.data, hi.ctypes.data,
+                                                 int(ghost_cells), v.ctypes.data), "spx_set_background_blocks")
 
     def sync(self) -> Stats:
         st = Stats()

@@ -91,6 +91,10 @@ struct spx_ctx {
    bool has_grid = false;
    int grid_n[3] = {0, 0, 0};
    double grid_cent[3] = {0, 0, 0}, grid_zone[3] = {0, 0, 0};
+   // block mode (spx_set_background_blocks): blocks per axis (0: one uniform block), ghost layers,
+   // domain in file units and block length
+   int grid_nb[3] = {0, 0, 0}, grid_ghost = 0;
+   double grid_dmin[3] = {0, 0, 0}, grid_dmax[3] = {0, 0, 0}, grid_blen[3] = {0, 0, 0};
    double* d_grid64 = nullptr;
    float* d_grid32 = nullptr;
    // distribution records (keep_records): per such distribution rec_capacity slots of 3 values and
@@ -152,6 +156,14 @@ void apply_grid(const spx_ctx* c, spx::ProblemDesc& pd)
    }
    pd.bg.zone_min = std::min(c->grid_zone[0], std::min(c->grid_zone[1], c->grid_zone[2]));
    pd.bg.grid = c->d_grid64;
+   for (int k = 0; k < 3; k++) {
+      pd.bg.grid_nb[k] = c->grid_nb[k];
+      pd.bg.dom_min[k] = c->grid_dmin[k];
+      pd.bg.dom_max[k] = c->grid_dmax[k];
+      pd.bg.blk_len[k] = c->grid_blen[k];
+   }
+   pd.bg.grid_ghost = c->grid_ghost;
+   spx_grid_units(pd.bg.gunits);
 }
 
 void apply_grid(const spx_ctx* c, spx::ProblemDescT<float>& pd)
@@ -795,7 +807,85 @@ int spx_set_background_grid(spx_ctx_t c, const int64_t n[3], const double cent_m
       c->grid_n[k] = (int)n[k];
       c->grid_cent[k] = cent_min[k];
       c->grid_zone[k] = zone_length[k];
+      c->grid_nb[k] = 0;
    }
+   c->grid_ghost = 0;
+   c->has_grid = true;
+   c->dirty = true;
+   return SPX_OK;
+}
+
+void spx_grid_units(double out[4])
+{
+   if (!out) return;
+   // the reference's unit systems: Fluid (au, 100 km/s, m_p cm^-3) and Particle (1e10 cm, c/10, m_p, e)
+   const double au = 1.495978707e+13, c_light = 2.99792458e+10, m_p = 1.67262192596e-24, e = 4.8032044e-10;
+   const double p_vel = 0.1 * c_light, p_len = 1.0e10;
+   const double p_time = p_len / p_vel, p_mag = (m_p * p_vel) / (e * p_time);
+   const double f_vel = 1.0e7, f_mag = f_vel * std::sqrt(m_p * 1.0);
+   out[0] = au / p_len;
+   out[1] = f_vel / p_vel;
+   out[2] = f_mag / p_mag;
+   out[3] = c_light / f_vel;
+}
+
+int spx_set_background_blocks(spx_ctx_t c, const int32_t n_blocks[3], const double domain_min[3],
+                              const double domain_max[3], int ghost_cells, const double* values)
+{
+   if (!valid_ctx(c) || !n_blocks || !domain_min || !domain_max || !values) return SPX_ERR_INVALID_ARG;
+   if (ghost_cells < 0 || ghost_cells > 1) return SPX_ERR_INVALID_ARG;
+   const int bz = spx::kGridBlockZones;
+   int64_t blocks = 1;
+   for (int k = 0; k < 3; k++) {
+      if (n_blocks[k] < 1 || n_blocks[k] > 100000 || !std::isfinite(domain_min[k]) || !std::isfinite(domain_max[k]) ||
+          !(domain_max[k] > domain_min[k]))
+         return SPX_ERR_INVALID_ARG;
+      blocks *= n_blocks[k];
+   }
+   if (blocks * bz * bz * bz > ((int64_t)1 << 31)) return SPX_ERR_TOO_LARGE;
+   SPX_CUDA(cudaSetDevice(c->device));
+   SPX_CUDA(cudaStreamSynchronize(c->stream));
+   cudaFree(c->d_grid64);
+   cudaFree(c->d_grid32);
+   c->d_grid64 = nullptr;
+   c->d_grid32 = nullptr;
+   c->has_grid = false;
+   int n[3];
+   for (int k = 0; k < 3; k++) n[k] = bz * n_blocks[k];
+   const int64_t nodes = (int64_t)n[0] * n[1] * n[2];
+   const size_t count = (size_t)nodes * spx::kGridStride;
+   // the reader's regrouping by dimension (src/reader_cartesian.cc:136-162), |B| of every zone appended
+   std::vector<double> h(count, 0.0);
+   for (int64_t b = 0; b < blocks; b++) {
+      const int64_t bi = b % n_blocks[0], bj = (b / n_blocks[0]) % n_blocks[1], bk = b / ((int64_t)n_blocks[0] * n_blocks[1]);
+      for (int z = 0; z < bz * bz * bz; z++) {
+         const int64_t i = bz * bi + z % bz, j = bz * bj + (z / bz) % bz, k = bz * bk + z / (bz * bz);
+         const double* v = values + 6 * (bz * bz * bz * b + z);
+         double* o = h.data() + spx::kGridStride * (i + n[0] * (j + (int64_t)n[1] * k));
+         for (int q = 0; q < 6; q++) o[q] = v[q];
+         const double bx2 = v[3] * v[3], by2 = v[4] * v[4], bz2 = v[5] * v[5];
+         o[6] = std::sqrt(bx2 + by2 + bz2);
+      }
+   }
+   if (c->precision == SPX_FP64) {
+      SPX_CUDA(cudaMalloc(&c->d_grid64, sizeof(double) * count));
+      SPX_CUDA(cudaMemcpy(c->d_grid64, h.data(), sizeof(double) * count, cudaMemcpyHostToDevice));
+   }
+   else {
+      std::vector<float> f(h.begin(), h.end());
+      SPX_CUDA(cudaMalloc(&c->d_grid32, sizeof(float) * count));
+      SPX_CUDA(cudaMemcpy(c->d_grid32, f.data(), sizeof(float) * count, cudaMemcpyHostToDevice));
+   }
+   for (int k = 0; k < 3; k++) {
+      c->grid_n[k] = n[k];
+      c->grid_nb[k] = n_blocks[k];
+      c->grid_dmin[k] = domain_min[k];
+      c->grid_dmax[k] = domain_max[k];
+      c->grid_blen[k] = (domain_max[k] - domain_min[k]) / (double)n_blocks[k];  // block_length (:97)
+      c->grid_cent[k] = 0.0;
+      c->grid_zone[k] = 1.0;
+   }
+   c->grid_ghost = ghost_cells;
    c->has_grid = true;
    c->dirty = true;
    return SPX_OK;

@@ -72,7 +72,16 @@ struct BgParamsT {
    R cent_min[3], zone[3], zone_min;
    int grid_n[3];
    const R* grid;             // device address of the node values (set when the context uploads)
+   // block mode (grid_nb[0] > 0): the reference's Cartesian data server over its reader's blocks of
+   // kGridBlockZones^3 zones, grid_nb[k] blocks per axis over [dom_min, dom_max] (file units, au),
+   // grid_ghost ghost cells per block side; node values in fluid units, and the ratios
+   // {length, velocity, magnetic field} Fluid/Particle and Fluid::c_code in gunits
+   int grid_nb[3], grid_ghost;
+   R dom_min[3], dom_max[3], blk_len[3], gunits[4];
 };
+
+// Zones per block edge of the reference's Cartesian blocks (block_size_cartesian, src/reader_cartesian.hh:17)
+constexpr int kGridBlockZones = 4;
 
 // Values per grid node: U (3), B (3), |B| (the magnitude at the node), one pad (32 B per node in FP32)
 constexpr int kGridStride = 8;

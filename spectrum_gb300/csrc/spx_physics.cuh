@@ -261,9 +261,111 @@ __device__ __forceinline__ void load_node(const double* p, double* v)
    v[0] = a.x; v[1] = a.y; v[2] = b.x; v[3] = b.y; v[4] = c.x; v[5] = c.y; v[6] = d.x;
 }
 
+// Block mode: the reference's Cartesian front end at first-order interpolation over its reader's
+// blocks. The primary block is the one ReadCartesianGetNode finds for the position in file units
+// (src/reader_cartesian.cc:264-277); its faces are the reader's corners scaled to code units, with
+// the ghost layers of BlockBase::LoadDimensions (src/block_base.cc:133-152), and its zone length
+// and zone-centre origin those of ConfigureProperties (:158-171); GetZoneOffset (:194-203) and the
+// stencil (src/server_cartesian.cc:206-268) follow. Zones past the block's faces are its
+// neighbours' zones, i.e. the same zones of the whole domain (:291-330). The sums are in fluid
+// units and the Fluid/Particle ratios come after (:549-716, 724-865): E = -(U x B) / Fluid::c_code
+// before its ratio, dmax capped by the block's smallest zone length (:687). A stencil that leaves
+// the domain is a field error.
+template <class R>
+__device__ __forceinline__ bool grid_fields_blocks(const BgParamsT<R>& g, V3<R> pos, unsigned mask, SD<R>& s)
+{
+   const R len = g.gunits[0], vel = g.gunits[1], mag = g.gunits[2], cf = g.gunits[3];
+   R lo[3], hi[3], zl[3];
+   int gz[3];
+#pragma unroll
+   for (int k = 0; k < 3; k++) {
+      const R pc = pos[k] / R(1.495978707e+13) * R(1.0e10);  // pos / Fluid::unit_length * Particle::unit_length
+      if (!(pc >= g.dom_min[k] && pc <= g.dom_max[k])) return false;
+      const int b = (int)((pc - g.dom_min[k]) / g.blk_len[k]);
+      if (b >= g.grid_nb[k]) return false;
+      R fmn = g.dom_min[k] + g.blk_len[k] * (R)b, fmx = fmn + g.blk_len[k];
+      fmn *= len;
+      fmx *= len;
+      int bs = kGridBlockZones;
+      if (g.grid_ghost > 0) {
+         const R incr = (fmx - fmn) * ((R)g.grid_ghost / (R)kGridBlockZones);
+         fmn -= incr;
+         fmx += incr;
+         bs += 2 * g.grid_ghost;
+      }
+      zl[k] = (fmx - fmn) / (R)bs;
+      const R cent = fmn + R(0.5) * zl[k];
+      const R o = (pos[k] - cent) / zl[k];
+      int z = (int)o;
+      if (o < R(0)) z--;
+      lo[k] = o - (R)z;
+      hi[k] = R(1) - lo[k];
+      gz[k] = kGridBlockZones * b + z - g.grid_ghost;
+      if (gz[k] < 0 || gz[k] + 1 >= g.grid_n[k]) return false;
+   }
+   const int64_t nx = g.grid_n[0], nxy = nx * (int64_t)g.grid_n[1];
+   const R* base = g.grid + ((int64_t)gz[2] * nxy + (int64_t)gz[1] * nx + gz[0]) * kGridStride;
+   const bool grads = (mask & (kGradU | kGradB | kDUdt)) != 0;
+   R var[6] = {R(0), R(0), R(0), R(0), R(0), R(0)}, bmag = R(0);
+   R gr[6][3], gbm[3] = {R(0), R(0), R(0)};
+#pragma unroll
+   for (int q = 0; q < 6; q++) gr[q][0] = gr[q][1] = gr[q][2] = R(0);
+#pragma unroll
+   for (int c = 0; c < 8; c++) {
+      const int ci = c & 1, cj = (c >> 1) & 1, ck = (c >> 2) & 1;
+      const R fx = ci ? lo[0] : hi[0], fy = cj ? lo[1] : hi[1], fz = ck ? lo[2] : hi[2];
+      R v[7];
+      load_node(base + ((int64_t)ck * nxy + (int64_t)cj * nx + ci) * kGridStride, v);
+      const R w = fx * fy * fz;
+#pragma unroll
+      for (int q = 0; q < 6; q++) var[q] += w * v[q];
+      bmag += w * v[6];
+      if (grads) {
+         const R d0 = (ci ? fy * fz : -fy * fz) / zl[0];
+         const R d1 = (cj ? fx * fz : -fx * fz) / zl[1];
+         const R d2 = (ck ? fx * fy : -fx * fy) / zl[2];
+#pragma unroll
+         for (int q = 0; q < 6; q++) {
+            gr[q][0] += d0 * v[q];
+            gr[q][1] += d1 * v[q];
+            gr[q][2] += d2 * v[q];
+         }
+         gbm[0] += d0 * v[6];
+         gbm[1] += d1 * v[6];
+         gbm[2] += d2 * v[6];
+      }
+   }
+   s.dmax = m_min(g.dmax0, m_min(zl[0], m_min(zl[1], zl[2])));
+   const V3<R> U = mk(var[0], var[1], var[2]), B = mk(var[3], var[4], var[5]);
+   if (mask & kE) {
+      const V3<R> x = cross(U, B);
+      s.E = mk((-x.x / cf) * mag, (-x.y / cf) * mag, (-x.z / cf) * mag);
+   }
+   s.U = mk(U.x * vel, U.y * vel, U.z * vel);
+   s.B = mk(B.x * mag, B.y * mag, B.z * mag);
+   s.region = mk(R(0), R(0), R(0));
+   s.Bmag = bmag * mag;
+   if (!(s.Bmag >= Lim<R>::tiny)) return false;
+   s.bhat = s.B / s.Bmag;
+   if (!grads) return true;
+#pragma unroll
+   for (int u = 0; u < 3; u++) {
+#pragma unroll
+      for (int x = 0; x < 3; x++) {
+         s.gradU.m[u][x] = gr[x][u] * vel;
+         s.gradB.m[u][x] = gr[3 + x][u] * mag;
+      }
+   }
+   s.gradBmag = mk(gbm[0] * mag, gbm[1] * mag, gbm[2] * mag);
+   s.dUdt = mk(R(0), R(0), R(0));
+   derive_from_matrices(s);
+   return true;
+}
+
 template <class R>
 __device__ __forceinline__ bool grid_fields(const BgParamsT<R>& g, V3<R> pos, unsigned mask, SD<R>& s)
 {
+   if (g.grid_nb[0] > 0) return grid_fields_blocks(g, pos, mask, s);
    R lo[3], hi[3];
    int z[3];
 #pragma unroll

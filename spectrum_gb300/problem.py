@@ -61,6 +61,57 @@ class Grid:
 
 
 @dataclass
+class BlockGrid:
+    """The data of the reference's Cartesian data server (its reader's files, src/reader_cartesian.cc):
+    n_blocks blocks of 4^3 zones per axis spanning [domain_min, domain_max] (au); values of shape
+    (blocks, 64, 6) -- blocks x fastest, in each block zones x fastest -- holding U then B in the
+    reference's fluid units; ghost_cells ghost layers per block side (SERVER_NUM_GHOST_CELLS)."""
+    n_blocks: tuple
+    domain_min: tuple
+    domain_max: tuple
+    values: "object"
+    ghost_cells: int = 0
+
+    @classmethod
+    def read(cls, dat_path: str, ghost_cells: int = 0) -> "BlockGrid":
+        """The reader's pair of files: the binary block data ``name.dat`` and its text header
+        ``name.info`` (blocks per axis, domain minimum, domain maximum, variables per zone)."""
+        import numpy as np
+        with open(dat_path[:-4] + ".info") as f:
+            tok = f.read().split()
+        nb = tuple(int(x) for x in tok[0:3])
+        dmin = tuple(float(x) for x in tok[3:6])
+        dmax = tuple(float(x) for x in tok[6:9])
+        nvar = int(tok[9])
+        if nvar != 6:
+            raise ValueError("the Cartesian server reads six variables per zone (U, B)")
+        values = np.fromfile(dat_path, dtype="<f8", count=nb[0] * nb[1] * nb[2] * 64 * nvar)
+        return cls(nb, dmin, dmax, values.reshape(-1, 64, nvar), ghost_cells)
+
+    def write(self, dat_path: str) -> None:
+        """Write the reader's two files (name.dat and name.info)."""
+        import numpy as np
+        with open(dat_path[:-4] + ".info", "w") as f:
+            f.write("%d %d %d\n%r %r %r\n%r %r %r\n6\n" % (*self.n_blocks, *self.domain_min, *self.domain_max))
+        np.ascontiguousarray(self.values, dtype="<f8").tofile(dat_path)
+
+    @classmethod
+    def sample(cls, n_blocks, domain_min, domain_max, fields, ghost_cells: int = 0) -> "BlockGrid":
+        """Sample fields(x, y, z) -> (U, B) (arrays of shape (..., 3), fluid units, x in au) at the zone
+        centres of every block."""
+        import numpy as np
+        nb = [int(v) for v in n_blocks]
+        zl = [(domain_max[k] - domain_min[k]) / nb[k] / 4.0 for k in range(3)]
+        ax = [domain_min[k] + zl[k] * (np.arange(4 * nb[k]) + 0.5) for k in range(3)]
+        z, y, x = np.meshgrid(ax[2], ax[1], ax[0], indexing="ij")
+        u, b = fields(x, y, z)
+        glob = np.concatenate([u, b], axis=-1).astype(np.float64)  # (4 nz, 4 ny, 4 nx, 6)
+        blk = glob.reshape(nb[2], 4, nb[1], 4, nb[0], 4, 6).transpose(0, 2, 4, 1, 3, 5, 6)
+        return cls(tuple(nb), tuple(float(v) for v in domain_min), tuple(float(v) for v in domain_max),
+                   np.ascontiguousarray(blk.reshape(-1, 64, 6)), int(ghost_cells))
+
+
+@dataclass
 class Problem:
     traj: int = TRAJ_PARKER
     time_flow: int = FORWARD
@@ -71,8 +122,9 @@ class Problem:
     problem_id: int = 0
     #: options of the stepping kernel (see include/spx.h, SPX_OPT_*)
     options: dict[int, float] = field(default_factory=dict)
-    #: the block of a gridded background (BackgroundServerCartesian): a Grid, or None
-    grid: "Grid | None" = None
+    #: the data of a gridded background (BackgroundServerCartesian): a Grid (one uniform block in code
+    #: units), a BlockGrid (the reference server's blocks), or None
+    grid: "Grid | BlockGrid | None" = None
 
     def add(self, plugin: P.Plugin, container: DataContainer) -> "Problem":
         self.plugins.append(PluginEntry(plugin, container.data(), container.size()))

@@ -172,7 +172,10 @@ def open_problems(problems: list[Problem] | Problem, precision: int = capi.SPX_F
     sim = SimulationGPU(base.traj, base.time_flow, base.rk, precision, opts)
     if base.grid is not None:
         g = base.grid
-        sim.ctx.set_background_grid(g.n, g.cent_min, g.zone_length, g.values)
+        if hasattr(g, "n_blocks"):
+            sim.ctx.set_background_blocks(g.n_blocks, g.domain_min, g.domain_max, g.ghost_cells, g.values)
+        else:
+            sim.ctx.set_background_grid(g.n, g.cent_min, g.zone_length, g.values)
     for e in base.plugins:
         sim.ctx.add_plugin(e.plugin.role, e.plugin.kind, e.blob, e.n_records)
     for e in base.plugins:

@@ -323,6 +323,44 @@ def gcr_modulation_grid(n_traj: int = 100_000, n_nodes: int = 256, half_width_au
     return pbs
 
 
+def server_unit_ratios() -> tuple:
+    """The reference data server's unit conversion (spx_grid_units): Fluid/Particle ratios of
+    length, velocity and magnetic field, and Fluid::c_code (common/physics.hh:18-55,
+    common/specie.hh:25-64)."""
+    au, c, m_p, e = 1.495978707e+13, 2.99792458e+10, 1.67262192596e-24, 4.8032044e-10
+    p_vel, p_len = 0.1 * c, 1.0e10
+    p_mag = (m_p * p_vel) / (e * (p_len / p_vel))
+    return au / p_len, 1.0e7 / p_vel, (1.0e7 * math.sqrt(m_p * 1.0)) / p_mag, c / 1.0e7
+
+
+def gcr_modulation_blocks(n_traj: int = 100_000, n_blocks: int = 16, half_width_au: float = 6.0,
+                          ghost_cells: int = 0, energies_mev=None, r_inner_au: float = 0.3,
+                          r_outer_au: float = 5.0, t_max_years: float = 0.2, **kw) -> list[Problem]:
+    """The modulation problems with the Parker spiral held as the reference's Cartesian data server
+    holds a data file: n_blocks^3 blocks of 4^3 zones over [-half_width, half_width]^3 au, the
+    spiral sampled at the zone centres in fluid units (BlockGrid). Boundaries as gcr_modulation_grid."""
+    from .plugins import BackgroundServerCartesian
+    from .problem import BlockGrid
+    if energies_mev is None:
+        energies_mev = modulation_energies(8, 30.0, 3.0e3)
+    len_r, vel_r, mag_r, _ = server_unit_ratios()
+
+    def fluid_fields(x, y, z):
+        u, b = parker_spiral_fields(x * len_r, y * len_r, z * len_r)
+        return u / vel_r, b / mag_r
+
+    h = half_width_au
+    grid = BlockGrid.sample((n_blocks,) * 3, (-h,) * 3, (h,) * 3, fluid_fields, ghost_cells)
+    pbs = gcr_modulation(n_traj=n_traj, energies_mev=energies_mev, r_inner_au=r_inner_au, r_outer_au=r_outer_au,
+                         t_max_years=t_max_years, **kw)
+    for pb in pbs:
+        c = DataContainer()
+        c.double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0, 0, 0)).double(ONE_AU)
+        pb.plugins[0] = type(pb.plugins[0])(BackgroundServerCartesian(), c.data(), c.size())
+        pb.grid = grid
+    return pbs
+
+
 # ------------------------------------------------------------------------------------------------
 # 5. focused transport with pitch-angle scattering
 # ------------------------------------------------------------------------------------------------

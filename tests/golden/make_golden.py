@@ -11,6 +11,7 @@ including where the sources are not.
     python tests/golden/make_golden.py          # rewrites tests/golden/*.npz
     python tests/golden/make_golden.py NAME...  # rewrites the named fixtures only
     python tests/golden/make_golden.py --dumps  # rewrites tests/golden/*.distro<d>.out
+    python tests/golden/make_golden.py --grid   # rewrites tests/golden/grid_blocks_ref.npz
 
 The second form keeps the reference's own distribution dump files (DistributionTemplated::Dump)
 of the fixtures whose distributions have at most DUMP_MAX_BINS bins: the pins of the dump format.
@@ -237,10 +238,33 @@ def write_dumps():
                 print(f"{name}.distro{d}.out: {len(data)} bytes")
 
 
+def write_grid():
+    """Fields and gradients of the reference's Cartesian data server (oracle/_ref/ref_grid0) at the
+    probe points of tests/test_oracle_grid_blocks.py, with the grid they were computed on."""
+    import pathlib
+    import tempfile
+
+    import test_oracle_grid_blocks as tg
+    g = tg.synthetic_grid()
+    pts = tg.probe_points(g)
+    dmax0 = 0.05 * tg.AU / tg.L
+    with tempfile.TemporaryDirectory() as td:
+        rows = tg.run_harness(0, g, pts, dmax0, pathlib.Path(td))
+    fields = np.array([[float(x) for x in r[1:]] for r in rows])
+    path = os.path.join(HERE, "grid_blocks_ref.npz")
+    np.savez_compressed(path, n_blocks=np.array(g.n_blocks), domain_min=np.array(g.domain_min),
+                        domain_max=np.array(g.domain_max), values=g.values, points=pts, fields=fields,
+                        status=np.array([int(r[0]) for r in rows]), dmax0=np.float64(dmax0))
+    print(f"grid_blocks_ref: {len(pts)} points, {os.path.getsize(path)} bytes")
+
+
 def main():
     args = sys.argv[1:]
     if "--dumps" in args:
         write_dumps()
+        return
+    if "--grid" in args:
+        write_grid()
         return
     import oracle_tools as ot
     for name, pb in cases():

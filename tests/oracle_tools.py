@@ -127,8 +127,46 @@ def run_oracle_spec(spec: bytes, traj_kind: int, time_flow: int, rk: int, n: int
     return OracleResult(traj, distros)
 
 
+def grid_units() -> np.ndarray:
+    """The oracle's Fluid/Particle length, velocity, magnetic ratios and Fluid::c_code."""
+    out = np.zeros(4)
+    lib().spx_oracle_grid_units(out.ctypes.data_as(ctypes.c_void_p))
+    return out
+
+
+def grid_stencil(pos):
+    """The oracle's block-mode primary block and stencil of one position (None outside the domain)."""
+    p = np.ascontiguousarray(np.asarray(pos, dtype=np.float64))
+    node, zone = np.zeros(3, np.int32), np.zeros(3, np.int32)
+    cm, zl, off, w, d = np.zeros(3), np.zeros(3), np.zeros(3), np.zeros(8), np.zeros(24)
+    vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    if lib().spx_oracle_grid_stencil(vp(p), vp(node), vp(cm), vp(zl), vp(zone), vp(off), vp(w), vp(d)):
+        return None
+    return {"node": node, "cent_min": cm, "zone_length": zl, "zone": zone, "offset": off, "weights": w, "derivs": d}
+
+
+def grid_fields(pos, dmax0):
+    """The oracle's gridded-background fields at one point: U[3] B[3] Bmag E[3] dmax gradU[9] gradB[9]
+    gradBmag[3] (None on a field error)."""
+    p = np.ascontiguousarray(np.asarray(pos, dtype=np.float64))
+    out = np.zeros(32)
+    if lib().spx_oracle_grid_fields(p.ctypes.data_as(ctypes.c_void_p), ctypes.c_double(dmax0),
+                                    out.ctypes.data_as(ctypes.c_void_p)):
+        return None
+    return out
+
+
 def set_grid(grid) -> None:
-    """Hand a problem.Grid to the oracle (one grid at a time)."""
+    """Hand a problem.Grid or problem.BlockGrid to the oracle (one grid at a time)."""
+    if hasattr(grid, "n_blocks"):
+        nb = np.ascontiguousarray(np.asarray(grid.n_blocks, dtype=np.int32))
+        lo = np.ascontiguousarray(np.asarray(grid.domain_min, dtype=np.float64))
+        hi = np.ascontiguousarray(np.asarray(grid.domain_max, dtype=np.float64))
+        v = np.ascontiguousarray(np.asarray(grid.values, dtype=np.float64))
+        u = grid_units()
+        vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+        lib().spx_oracle_set_grid_blocks(vp(nb), vp(lo), vp(hi), ctypes.c_int(int(grid.ghost_cells)), vp(v), vp(u))
+        return
     n = np.ascontiguousarray(np.asarray(grid.n, dtype=np.int64))
     cm = np.ascontiguousarray(np.asarray(grid.cent_min, dtype=np.float64))
     zl = np.ascontiguousarray(np.asarray(grid.zone_length, dtype=np.float64))
@@ -149,7 +187,8 @@ GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def golden_names():
-    return sorted(f[:-4] for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz"))
+    # trajectory fixtures (the grid fixture holds fields at points, test_oracle_grid_blocks.py)
+    return sorted(f[:-4] for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz") and not f.startswith("grid_"))
 
 
 def load_golden(name: str):

@@ -63,6 +63,42 @@ def test_grid_spiral_matches_closed_form(built_lib):
             assert n >= 1 and ok.mean() >= 0.95, (k, d, rg.distros[k][d][0], rc.distros[k][d][0])
 
 
+@pytest.mark.parametrize("ghost", [0, 1])
+def test_block_grid_fp64_matches_oracle(built_lib, ghost):
+    """The reference server's block layout (spx_set_background_blocks, 12^3 blocks of 4^3 zones):
+    trajectory by trajectory against the oracle, whose block-mode fields equal the reference's
+    server bit for bit (test_oracle_grid_blocks.py); without and with a ghost layer per block side."""
+    pbs = workloads.gcr_modulation_blocks(n_traj=64, n_blocks=12, ghost_cells=ghost, energies_mev=[300.0],
+                                          t_max_years=0.05)
+    gpu = run_problems(pbs, precision=capi.SPX_FP64, record=True)
+    ref = ot.run_oracle(pbs[0])
+    ot.assert_fp64_parity(gpu.records[0], ref, ot.run_oracle(pbs[0], nudge_libm=1), distros=gpu.distros[0])
+    assert gpu.stats.given_up == 0
+
+
+def test_block_grid_fp32_matches_fp64(built_lib):
+    pbs = workloads.gcr_modulation_blocks(n_traj=3000, n_blocks=24, energies_mev=[100.0, 1000.0], t_max_years=0.1)
+    r64 = run_problems(pbs, precision=capi.SPX_FP64)
+    r32 = run_problems(pbs, precision=capi.SPX_MIXED)
+    for k in range(len(pbs)):
+        for d in range(2):
+            n, ok = _within_3sigma(r32.distros[k][d][0], r64.distros[k][d][0])
+            assert n >= 1 and ok.all(), (k, d)
+
+
+def test_block_grid_rejects_bad_layouts(built_lib):
+    pbs = workloads.gcr_modulation_blocks(n_traj=10, n_blocks=2, energies_mev=[300.0])
+    ctx = capi.Context(pbs[0].traj, pbs[0].time_flow, pbs[0].rk, capi.SPX_MIXED)
+    try:
+        g = pbs[0].grid
+        for nb, lo, hi, ghost in [((0, 2, 2), g.domain_min, g.domain_max, 0), (g.n_blocks, g.domain_max, g.domain_min, 0),
+                                  (g.n_blocks, g.domain_min, g.domain_max, 2)]:
+            with pytest.raises((capi.SpxError, ValueError)):
+                ctx.set_background_blocks(nb, lo, hi, ghost, g.values)
+    finally:
+        ctx.close()
+
+
 def test_grid_background_needs_its_grid(built_lib):
     pbs = workloads.gcr_modulation_grid(n_traj=10, n_nodes=8, energies_mev=[300.0])
     ctx = capi.Context(pbs[0].traj, pbs[0].time_flow, pbs[0].rk, capi.SPX_MIXED)
