@@ -301,7 +301,8 @@ def _other_workloads():
                       "(10x the named 1e5, so one launch lasts long enough to time)", 0.1),
         "shock": (lambda: [W.shock_acceleration(n_traj=100_000, x_downstream=40.0, p_max=1.0e2)],
                   "Parker fwd, smooth shock s = 4, width 1e-3, momentum boundary 1e2 p0: 1e5 of the named 1e7 "
-                  "trajectories (each makes ~1e5-1e6 steps in the shock layer)", 0.01),
+                  "trajectories (each makes ~3e6 steps in the shock layer; 1e5 is one trajectory per lane, so "
+                  "a launch lasts as long as its longest trajectory)", 0.1),
         "dipole": (lambda: [W.dipole_orbits(n_traj=1_000_000, t_end=1.0 / U.unit_time)],
                    "Lorentz RK4 in the dipole, 1e6 protons 1-100 MeV, L 2-6, 32 steps per gyro-orbit, for 1 s "
                    "of flight (100 drift periods take ~3e8 steps for the slowest trajectory)", 0.01),
@@ -319,6 +320,10 @@ def _other_workloads():
 
 
 OTHER_WORKLOADS = ("diffusion", "shock", "dipole", "focused", "grid", "guiding")
+# the steady-state sample of every family: trajectories stopped after this many steps
+STEADY_CAP = 4096
+# families whose trajectories run millions of steps: their FP64 ratio comes from the capped sample
+CAPPED_FP64 = ("shock",)
 
 
 def orbit_errors(r64, r32):
@@ -364,6 +369,7 @@ def bench_other(args, rank, world, local):
         kms.append(st.kernel_ms)
         traj += st.trajectories
         steps += st.steps
+    steady = steady_rate(sim, tun, STEADY_CAP)
     sim.close()
     t = sum(kms) / 1e3
     line = {"metric": f"SDE trajectories/s, {args.workload} workload, batched FP32, 1 GB300",
@@ -372,8 +378,23 @@ def bench_other(args, rank, world, local):
             "dtype": "f32 (float-float accumulation)", "data": "synthetic (seeded Philox streams)",
             "config": {"workload": args.workload, "description": desc, "problems": len(pbs),
                        "trajectories_per_step": sum(p.n_traj for p in pbs), "l2": "flushed between steps"},
-            "tuning": {"block_size": tun.block_size, "steps_per_sync": tun.steps_per_sync, "schedule": tun.schedule}}
-    if not args.no_fp64:
+            "tuning": {"block_size": tun.block_size, "steps_per_sync": tun.steps_per_sync, "schedule": tun.schedule},
+            "steady_steps_per_s": steady, "steady_cap": STEADY_CAP}
+    if not args.no_fp64 and args.workload in CAPPED_FP64:
+        # trajectories of millions of steps: the FP64 plain kernel (one thread per trajectory) and the
+        # FP32 batched kernel on the same trajectories, every one stopped after STEADY_CAP steps
+        sub = build()
+        for p in sub:
+            p.n_traj = max(1, int(p.n_traj * share))
+        rates = {}
+        for name, prec, tn in (("fp64", capi.SPX_FP64, capi.Tuning(0, 0, 1, 0)), ("fp32", capi.SPX_MIXED, tun)):
+            s_ = open_problems(sub, precision=prec, deriv_mode=1)
+            rates[name] = steady_rate(s_, tn, STEADY_CAP, 1)
+            s_.close()
+        line["fp64_plain"] = {"trajectories": sum(p.n_traj for p in sub), "steps_per_s": rates["fp64"],
+                              "fp32_steps_per_s_same_batch": rates["fp32"], "cap": STEADY_CAP,
+                              "ratio_fp32_batched_over_fp64_plain": rates["fp32"] / rates["fp64"]}
+    elif not args.no_fp64:
         sub = build()
         for p in sub:
             p.n_traj = max(1, int(p.n_traj * share))

@@ -165,3 +165,28 @@ def test_cpp_host_mirror_blobs_equal_python(built_lib, tmp_path):
     # the same order within each role (slots are positional)
     for role in range(6):
         assert [x for x in cpp if x[0] == str(role)] == [x for x in py if x[0] == str(role)]
+
+
+def test_static_capacity_matches_the_descriptor_sizes(tmp_path):
+    """The capacity include/spx.h documents for spx_run_static is what its fixed array holds: the run
+    counters (256 B), the FP64 descriptors and, in mixed precision, the FP32 ones at the next 256-B
+    boundary (spx_capi.cu, spx_run_static), with the descriptor sizes of this build."""
+    import shutil
+    import subprocess
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    src = tmp_path / "sz.cc"
+    src.write_text('#include <cstdio>\n#include "spx_params.hh"\n'
+                   'int main() { std::printf("%zu %zu", sizeof(spx::ProblemDesc), sizeof(spx::ProblemDescT<float>)); }\n')
+    exe = str(tmp_path / "sz")
+    subprocess.run([gxx, "-std=c++17", "-I", os.path.join(ROOT, "spectrum_gb300", "csrc"), str(src), "-o", exe], check=True)
+    pd, pr = (int(x) for x in subprocess.run([exe], capture_output=True, text=True, check=True).stdout.split())
+    hdr = open(os.path.join(ROOT, "include", "spx.h")).read()
+    scratch = 512 * 1024
+    assert "#define SPX_STATIC_SCRATCH_BYTES (512u * 1024u)" in hdr
+    up = lambda x: (x + 255) // 256 * 256  # noqa: E731
+    fp64 = max(n for n in range(1, 1000) if 256 + pd * n <= scratch)
+    mixed = max(n for n in range(1, 1000) if up(256 + pd * n) + pr * n <= scratch)
+    m = re.search(r"(\d+) problems in SPX_MIXED, (\d+) in SPX_FP64", hdr)
+    assert (int(m.group(1)), int(m.group(2))) == (mixed, fp64)
