@@ -198,7 +198,7 @@ int spx_sync(spx_ctx_t ctx, spx_stats* stats);
 int spx_autotune(spx_ctx_t ctx, int64_t sample_traj, spx_tuning* best);
 
 /* Size of the fixed device array spx_run_static works in (every GPU that loads the library holds
- * it until the process exits): 43 problems in SPX_MIXED, 68 in SPX_FP64. */
+ * it until the process exits): 41 problems in SPX_MIXED, 64 in SPX_FP64. */
 #define SPX_STATIC_SCRATCH_BYTES (512u * 1024u)
 
 /* spx_run without any device allocation. No counterpart in the reference: it is for callers that

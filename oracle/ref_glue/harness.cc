@@ -186,6 +186,9 @@ void AddPlugin(Probe& traj, uint32_t role, const std::string& name, const DataCo
       SPX_TRY_DIST(DistributionSpectrumKineticEnergyPowerLaw)
       SPX_TRY_DIST(DistributionSpectrumKineticEnergyBentPowerLaw)
       SPX_TRY_DIST(DistributionDivergenceFlowPowerLaw)
+#if SPX_REF_TRAJ == TRAJ_LORENTZ
+      SPX_TRY_DIST(DistributionAnisotropyLISM)
+#endif
       W = 3;
       SPX_TRY_DIST(DistributionPositionCumulativeOrder1)
       SPX_TRY_DIST(DistributionLossCone)

@@ -273,7 +273,7 @@ typedef struct {
 } ini_t;
 
 enum { DS_TIME = 1, DS_POS, DS_MOM, DS_POSMOM, DS_SPEC, DS_SPECBENT, DS_CUM1, DS_CUM2, DS_DIVFLOW, DS_LOSSCONE,
-       DS_TIMEMU = 20 };
+       DS_ANISO_LISM, DS_TIMEMU = 20 };
 typedef struct {
    int kind, width;
    int n_bins[3], log_bins[3], bin_outside[3], dims;
@@ -282,6 +282,7 @@ typedef struct {
    double val_hot, val_cold;
    int val_time, val_coord, pos_idx, mom_idx;
    double J0, T0, pow_law, T_b, pow_law_comb, bend, A0;
+   v3 rot[3], u_lism, grad_perp; /* DistributionAnisotropyLISM */
    int64_t offset_bins;
 } dist_t;
 
@@ -590,6 +591,19 @@ static int setup_dist(dist_t* d, rd_t* r, int kind)
       d->n_actions = 1;
       if (d->dims != 7) return -3;
       break;
+   case DS_ANISO_LISM:
+      /* DistributionAnisotropyLISM::SetupDistribution, src/distribution_other.cc:388-409: the binning
+       * frame, the LISM flow, the momentum slope, the perpendicular density gradient; five actions; its
+       * set-up accepts dims 5 only */
+      d->rot[0] = rd_v(r);
+      d->rot[1] = rd_v(r);
+      d->rot[2] = rd_v(r);
+      d->u_lism = rd_v(r);
+      d->pow_law = rd_d(r);
+      d->grad_perp = rd_v(r);
+      d->n_actions = 5;
+      if (d->dims != 5) return -3;
+      break;
    }
    return 0;
 }
@@ -639,7 +653,7 @@ static int kind_of(uint32_t role, const char* nm, size_t nl)
       K("DistributionSpectrumKineticEnergyBentPowerLaw", DS_SPECBENT)
       K("DistributionPositionCumulativeOrder1", DS_CUM1) K("DistributionPositionCumulativeOrder2", DS_CUM2)
       K("DistributionDivergenceFlowPowerLaw", DS_DIVFLOW) K("DistributionTimeMu", DS_TIMEMU)
-      K("DistributionLossCone", DS_LOSSCONE)
+      K("DistributionLossCone", DS_LOSSCONE) K("DistributionAnisotropyLISM", DS_ANISO_LISM)
    }
 #undef K
    return -1;
@@ -710,7 +724,10 @@ static int parse_spec(const uint8_t* s, size_t n, prob_t* pb, char* err, size_t 
       }
       else if (role == 5) {
          if (pb->nd >= MAXD) { snprintf(err, el, "too many distributions"); return -2; }
-         setup_dist(&pb->d[pb->nd++], &r, kind);
+         if (setup_dist(&pb->d[pb->nd++], &r, kind)) {
+            snprintf(err, el, "set-up of %.*s incomplete (active dimensions)", (int)nl, nm);
+            return -3;
+         }
       }
       if (r.bad) { snprintf(err, el, "malformed blob for %.*s", (int)nl, nm); return -3; }
    }
@@ -1713,6 +1730,15 @@ static void process_trajectory(trj_t* T, int di, int action)
       value.x[0] = T->t;
       value.x[1] = (tt == 200) ? vdot(T->mom, s2->bhat) / vnorm(T->mom) : IS_GC(tt) ? T->mom.x[2] / vnorm(T->mom) : T->mom.x[1];
       break;
+   case DS_ANISO_LISM: {
+      /* DistributionAnisotropyLISM::EvaluateValue, src/distribution_other.cc:416-426: the first point's
+       * momentum in the binning frame (GeoVector::ChangeToBasis), as spherical (r, theta, phi); theta
+       * and phi binned. The reference leaves the third value unset while binning dims 5; 0 here. */
+      v3 q = V(vdot(T->mom0, d->rot[0]), vdot(T->mom0, d->rot[1]), vdot(T->mom0, d->rot[2]));
+      pos_to_rtp(&q);
+      value = V(q.x[1], q.x[2], 0.0);
+      break;
+   }
    }
    /* EvaluateWeight */
    switch (d->kind) {
@@ -1748,6 +1774,29 @@ static void process_trajectory(trj_t* T, int di, int action)
       w[1] = T->bmag_max;
       w[2] = asin(sqrt(((d->val_time == 0) ? s1->Bmag : s2->Bmag) / T->bmag_max));
       break;
+   case DS_ANISO_LISM: {
+      /* src/distribution_other.cc:433-483; the relative momentum p2 - RelFactor1(|p2|) m U_LISM
+       * (common/physics.hh:260-263) of EvaluateValue, m = 1 and q = 1 for the proton in code units */
+      double m1 = vnorm(T->mom0), m2 = vnorm(T->mom), rf = sqrt(1.0 + (m2 / 1.0 / c_code()) * (m2 / 1.0 / c_code()));
+      v3 rel = vsub(T->mom, vscale(rf * 1.0, d->u_lism)), ru;
+      double rn = vnorm(rel);
+      ru = V(rel.x[0] / rn, rel.x[1] / rn, rel.x[2] / rn);
+      if (action == 0) {  /* ComptonGettingFactor */
+         v3 mh = V(T->mom0.x[0] / m1, T->mom0.x[1] / m1, T->mom0.x[2] / m1);
+         w[0] = 1.0 - vdot(vscale(d->pow_law, d->u_lism), mh) / vel_of(m1);
+      }
+      else if (action == 1) w[0] = pow(rn / m1, d->pow_law);           /* MomPowerLawAnisotropy */
+      else if (action == 2) w[0] = vdot(ru, s2->bhat);                 /* FirstLegendreAnisotropy */
+      else if (action == 3) {                                           /* SecondLegendreAnisotropy */
+         double c = vdot(ru, s2->bhat);
+         w[0] = 0.5 * (3.0 * (c * c) - 1.0);
+      }
+      else {                                                            /* bCrossGradientAnisotropy */
+         double rl = rn * c_code() / (fabs(1.0) * s2->Bmag);
+         w[0] = vdot(d->grad_perp, vadd(T->pos, vscale(rl, vcross(ru, s2->bhat))));
+      }
+      break;
+   }
    }
    /* AddEvent */
    for (ijk = 0; ijk < 3; ijk++) {
@@ -2835,6 +2884,12 @@ int spx_oracle_run(const uint8_t* spec, size_t spec_len, const spx_oracle_opts* 
       return -4;
    }
    for (d = 0; d < pb->nd; d++) {
+      /* DistributionAnisotropyLISM exists for Lorentz trajectories only (src/distribution_other.hh:245) */
+      if (pb->d[d].kind == DS_ANISO_LISM && opts->traj_type != 200) {
+         snprintf(err, err_len, "DistributionAnisotropyLISM needs Lorentz trajectories");
+         free(pb); free(T);
+         return -4;
+      }
       pb->d[d].offset_bins = off;
       off += (int64_t)pb->d[d].n_bins[0] * pb->d[d].n_bins[1] * pb->d[d].n_bins[2];
    }

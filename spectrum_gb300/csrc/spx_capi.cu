@@ -578,6 +578,7 @@ const char* distro_class_name(int kind)
    case spx::kDsCumulative2: return "DistributionPositionCumulativeOrder2";
    case spx::kDsDivergenceFlow: return "DistributionDivergenceFlowPowerLaw";
    case spx::kDsLossCone: return "DistributionLossCone";
+   case spx::kDsAnisotropyLISM: return "DistributionAnisotropyLISM";
    case spx::kDsTimeMu: return "DistributionTimeMu";  // a class of this library only
    default: return nullptr;
    }

@@ -54,7 +54,8 @@ enum IniKind : int {
 
 enum DistKind : int {
    kDsTimeUniform = 1, kDsPositionUniform, kDsMomentumUniform, kDsPositionMomentumUniform, kDsSpectrumPowerLaw,
-   kDsSpectrumBentPowerLaw, kDsCumulative1, kDsCumulative2, kDsDivergenceFlow, kDsLossCone, kDsTimeMu = 20
+   kDsSpectrumBentPowerLaw, kDsCumulative1, kDsCumulative2, kDsDivergenceFlow, kDsLossCone, kDsAnisotropyLISM,
+   kDsTimeMu = 20
 };
 
 template <class R>
@@ -127,6 +128,9 @@ struct DistParamsT {
    R val_hot, val_cold;
    int val_time, val_coord, pos_idx, mom_idx;
    R J0, T0, pow_law, T_b, pow_law_comb, bend, A0;
+   // DistributionAnisotropyLISM: the binning frame (rows), the LISM flow velocity, the density gradient
+   // across the LISM field (pow_law holds its momentum power-law slope)
+   R rot[3][3], u_lism[3], grad_perp[3];
    int64_t offset_counts;     // into the context's counts array
    int64_t offset_sums;       // into the context's sums array (doubles)
    // DistributionBase::AddRecord (keep_records): the value and weight of every processed event are

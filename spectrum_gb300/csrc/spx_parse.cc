@@ -409,6 +409,14 @@ int parse_distribution(Reader& r, int kind, DistParams& d)
       d.n_actions = 1;
       if (d.dims != 7) return SPX_ERR_BAD_BLOB;
       break;
+   case kDsAnisotropyLISM:  // src/distribution_other.cc:388-409: five actions; its set-up accepts dims 5 only
+      for (int k = 0; k < 3; k++) r.v3(d.rot[k]);
+      r.v3(d.u_lism);
+      d.pow_law = r.d();
+      r.v3(d.grad_perp);
+      d.n_actions = 5;
+      if (d.dims != 5) return SPX_ERR_BAD_BLOB;
+      break;
    default:
       return SPX_ERR_UNKNOWN_PLUGIN;
    }
@@ -462,6 +470,8 @@ int parse_plugin(ProblemDesc& pd, int traj, int role, int kind, const uint8_t* b
       return SPX_OK;
    }
    case SPX_ROLE_DISTRIBUTION: {
+      // DistributionAnisotropyLISM is compiled for Lorentz trajectories only (src/distribution_other.hh:245)
+      if (kind == kDsAnisotropyLISM && traj != kLorentz) return SPX_ERR_UNKNOWN_PLUGIN;
       DistParams d;
       int rc = parse_distribution(r, kind, d);
       if (rc != SPX_OK) return rc;
@@ -582,6 +592,7 @@ void convert_problem(const ProblemDesc& s, ProblemDescT<R>& d)
       y.val_time = x.val_time; y.val_coord = x.val_coord; y.pos_idx = x.pos_idx; y.mom_idx = x.mom_idx;
       y.J0 = (R)x.J0; y.T0 = (R)x.T0; y.pow_law = (R)x.pow_law; y.T_b = (R)x.T_b;
       y.pow_law_comb = (R)x.pow_law_comb; y.bend = (R)x.bend; y.A0 = (R)x.A0;
+      cp(x.rot, y.rot); cp(x.u_lism, y.u_lism); cp(x.grad_perp, y.grad_perp);
       y.offset_counts = x.offset_counts; y.offset_sums = x.offset_sums;
    }
    d.nbt = s.nbt; d.nbs = s.nbs; d.nbm = s.nbm; d.nd = s.nd; d.has_diff = s.has_diff;

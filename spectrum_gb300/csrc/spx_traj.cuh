@@ -279,6 +279,19 @@ static __device__ __noinline__ void process_event(int traj, const EventPoint& e,
       value.x = e.t;
       value.y = traj == kLorentz ? dot(e.mom, e.bhat) / norm(e.mom) : traj == kGuiding ? e.mom.z / norm(e.mom) : e.mom.y;
       break;
+   case kDsAnisotropyLISM: {  // EvaluateValue, src/distribution_other.cc:416-426
+      // the first point's momentum in the binning frame, as (theta, phi) of its direction; the
+      // reference leaves the third value unset although its set-up bins the first and the third
+      // (dims 5): here it is 0
+      const V3<double> m = s0.mom0;
+      V3<double> q = mk(m.x * d.rot[0][0] + m.y * d.rot[0][1] + m.z * d.rot[0][2],
+                        m.x * d.rot[1][0] + m.y * d.rot[1][1] + m.z * d.rot[1][2],
+                        m.x * d.rot[2][0] + m.y * d.rot[2][1] + m.z * d.rot[2][2]);
+      double r = norm(q), phi = atan2(q.y, q.x);
+      if (phi < 0.0) phi += 6.283185307179586476925286766559;
+      value = mk(acos(q.z / r), phi, 0.0);
+      break;
+   }
    }
    switch (d.kind) {
    case kDsTimeUniform: case kDsPositionUniform: case kDsMomentumUniform: case kDsPositionMomentumUniform: case kDsTimeMu:
@@ -306,6 +319,28 @@ static __device__ __noinline__ void process_event(int traj, const EventPoint& e,
       w[1] = s0.bmag_max;
       w[2] = asin(sqrt((d.val_time == 0 ? s0.bmag0 : e.bmag) / s0.bmag_max));
       break;
+   case kDsAnisotropyLISM: {  // the five anisotropy weights, src/distribution_other.cc:433-483
+      const V3<double> ul = mk(d.u_lism[0], d.u_lism[1], d.u_lism[2]);
+      const double m1 = norm(s0.mom0), m2 = norm(e.mom);
+      // the second point's momentum in the LISM frame: p - gamma m U (RelFactor1, common/physics.hh:260-263)
+      const double rf = sqrt(1.0 + (m2 / 1.0 / c_code<double>()) * (m2 / 1.0 / c_code<double>()));
+      const V3<double> rel = e.mom - (rf * 1.0) * ul;
+      const double rn = norm(rel);
+      const V3<double> ru = mk(rel.x / rn, rel.y / rn, rel.z / rn);
+      if (action == 0) {  // Compton-Getting factor
+         const V3<double> mh = mk(s0.mom0.x / m1, s0.mom0.y / m1, s0.mom0.z / m1);
+         w[0] = 1.0 - dot(d.pow_law * ul, mh) / vel_of<double>(m1);
+      }
+      else if (action == 1) w[0] = pow(rn / m1, d.pow_law);
+      else if (action == 2) w[0] = dot(ru, e.bhat);
+      else if (action == 3) { const double c = dot(ru, e.bhat); w[0] = 0.5 * (3.0 * (c * c) - 1.0); }
+      else {  // b x gradient: the guiding centre dotted with the density gradient
+         const V3<double> gp = mk(d.grad_perp[0], d.grad_perp[1], d.grad_perp[2]);
+         const double rl = rn * c_code<double>() / (fabs(1.0) * e.bmag);
+         w[0] = dot(gp, e.pos + rl * cross(ru, e.bhat));
+      }
+      break;
+   }
    }
    // AddRecord follows AddEvent for every processed event, outliers included (src/distribution_base.cc:192-193)
    if (d.rec_n) {

@@ -364,6 +364,17 @@ class DistributionLossCone(Plugin):
     build with RECORD_BMAG_EXTREMA does (src/trajectory_base.hh:31). All three dimensions binned."""
 
 
+@_plugin(ROLE_DISTRIBUTION, 11)
+class DistributionAnisotropyLISM(Plugin):
+    """src/distribution_other.cc:364-483 (Lorentz trajectories only): the first point's momentum
+    direction in a given frame, binned in (theta, phi); weights: Compton-Getting factor, momentum
+    power-law, first and second Legendre anisotropy of the LISM-frame momentum against the field, and
+    the guiding centre dotted with a density gradient. Parameters: the DistributionTemplated header,
+    GeoVector rot_matrix[3], GeoVector U_LISM, double mom_pow_law, GeoVector grad_perp_dens. The
+    reference's set-up accepts bins in the first and third dimensions only (dims 5) while it sets the
+    first two values; the third value is 0 here (unset there)."""
+
+
 @_plugin(ROLE_DISTRIBUTION, 20, reference=False)
 class DistributionTimeMu(Plugin):
     """Extension: a (t, mu) histogram of the second point (the event), for observer crossings

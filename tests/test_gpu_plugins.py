@@ -55,6 +55,8 @@ def _problems():
         out["combination_" + name] = lambda name=name: cases._combo(name)
     for name, make in cases.LOSSCONE_CASES.items():
         out["loss_cone_" + name] = make
+    for name, make in cases.ANISO_CASES.items():
+        out["anisotropy_lism_" + name] = make
     out["parker_source_constant"] = lambda: cases._parker(
         traj=cases.TRAJ_PARKER_SOURCE, flow=cases.BACKWARD, src=(cases.SourceConstant(), DC().double(0.7)),
         t_end=-0.05, n=12)

@@ -513,6 +513,55 @@ LOSSCONE_CASES = {
 }
 
 
+# -- DistributionAnisotropyLISM (src/distribution_other.cc:364-483, Lorentz only) ----------------------
+# Dipole orbits from a fixed point; each case sends the time boundary's event to one of the five
+# weights. The reference's set-up accepts bins in the first and third dimensions only (dims 5) and
+# leaves the third value unset: the third axis has one bin over [-1e300, 1e300] with outliers kept,
+# so any finite value lands in it.
+def _aniso_problem(action, n=8):
+    import math
+    from spectrum_gb300.plugins import DistributionAnisotropyLISM
+    r_e = W.R_EARTH_CM / U.unit_length
+    b_eq = W.B_EARTH_G / U.unit_magnetic
+    bg = (BackgroundDipole(), DC().double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0.0, 0.0, -b_eq)).double(0.1 * r_e)
+          .double(r_e).double(0.1))
+    c = distro_header(DC(), (9, 0, 1), (0.0, 0.0, -1e300), (math.pi, 1.0, 1e300), bin_outside=(1, 1, 1))
+    c3 = 1.0 / math.sqrt(3.0)
+    rot = ((c3, c3, c3), (1.0 / math.sqrt(2.0), -1.0 / math.sqrt(2.0), 0.0), (c3 / math.sqrt(2.0), c3 / math.sqrt(2.0), -2.0 * c3 / math.sqrt(2.0)))
+    c.vec(rot[0]).vec(rot[1]).vec(rot[2]).vec((2.0e-3, -1.0e-3, 5.0e-4)).double(2.7).vec((0.3, -0.2, 0.1))
+    return _parker(traj=TRAJ_LORENTZ, bg=bg, dist=(DistributionAnisotropyLISM(), c), n=n, diff=False,
+                   t_end=0.2 / U.unit_time, t_action=(action,),
+                   is_=(InitialSpaceFixed(), DC().vec((4.0 * r_e, 0.0, 0.0))),
+                   im=(InitialMomentumShell(), DC().double(U.mev_to_mom(10.0))))
+
+
+ANISO_CASES = {f"action{a}": (lambda a=a: _aniso_problem(a)) for a in range(5)}
+
+
+@pytest.mark.parametrize("name", sorted(ANISO_CASES))
+def test_anisotropy_lism(name):
+    pb = ANISO_CASES[name]()
+    r = _same(pb)
+    counts, sums, n_ev = r.distros[0]
+    assert n_ev == len(r.traj) and counts.sum() == len(r.traj)
+    assert np.isfinite(sums).all() and (sums != 0.0).any()
+
+
+def test_anisotropy_lism_refused_outside_lorentz():
+    """The class exists for Lorentz trajectories only; dims other than 5 fail its set-up."""
+    from spectrum_gb300.plugins import DistributionAnisotropyLISM
+    pb = _aniso_problem(0)
+    pb.traj = TRAJ_GUIDING
+    with pytest.raises(Exception):
+        ot.run_oracle(pb)
+    c = distro_header(DC(), (9, 4, 0), (0.0, 0.0, 0.0), (3.0, 6.0, 1.0))
+    c.vec((1, 0, 0)).vec((0, 1, 0)).vec((0, 0, 1)).vec((0, 0, 0)).double(2.7).vec((0, 0, 0))
+    pb = _aniso_problem(0)
+    pb.plugins[-1] = type(pb.plugins[-1])(DistributionAnisotropyLISM(), c.data(), c.size())
+    with pytest.raises(Exception):
+        ot.run_oracle(pb)
+
+
 @pytest.mark.parametrize("name", sorted(LOSSCONE_CASES))
 def test_loss_cone(name):
     pb = LOSSCONE_CASES[name]()
