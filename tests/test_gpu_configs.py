@@ -330,3 +330,25 @@ def test_specialised_kernels_equal_the_generic_one(built_lib, workload):
             assert np.array_equal(x["pos"], y["pos"])
         for x, y in zip(da, db):
             assert np.array_equal(x[0], y[0])
+
+
+def test_dipole_orbits_per_trajectory_errors(built_lib):
+    """Full orbits in the dipole (the reference's drift-period benchmark set-up) from identical initial
+    conditions, trajectory by trajectory: the FP64 kernel against the oracle at the libm level, and the
+    FP32 kernel against FP64 -- relative |p| difference, azimuth (drift phase) difference and the
+    difference of the energy drifts |p|/|p0| - 1, which RK4 truncation dominates in both."""
+    pb = workloads.dipole_orbits(n_traj=512, t_end=1.0 / units.unit_time)
+    r64 = run_problems(pb, precision=capi.SPX_FP64, record=True).records[0]
+    r32 = run_problems(pb, precision=capi.SPX_MIXED, record=True).records[0]
+    ot.assert_fp64_parity(r64, ot.run_oracle(pb), ot.run_oracle(pb, nudge_libm=1))
+    same = (r64["status"] & STATUS_MASK) == (r32["status"] & STATUS_MASK)
+    assert same.mean() >= 0.99
+    p0 = np.linalg.norm(r64["mom0"], axis=1)
+    p64, p32 = np.linalg.norm(r64["mom"], axis=1), np.linalg.norm(r32["mom"], axis=1)
+    rel = np.abs(p32 / p64 - 1.0)[same]
+    assert np.median(rel) < 1e-6 and rel.max() < 1e-4, (np.median(rel), rel.max())
+    az = lambda r: np.arctan2(r["pos"][:, 1], r["pos"][:, 0])  # noqa: E731
+    daz = np.abs(np.angle(np.exp(1j * (az(r32) - az(r64)))))[same]
+    assert np.median(daz) < 1e-5 and np.percentile(daz, 99) < 1e-3, (np.median(daz), np.percentile(daz, 99))
+    ddrift = np.abs(np.abs(p32 / p0 - 1.0) - np.abs(p64 / p0 - 1.0))[same]
+    assert np.median(ddrift) < 1e-6, np.median(ddrift)
