@@ -49,7 +49,7 @@ FROZEN_SPECIAL_PER_STEP = {"gcr": 200.0, "diffusion": 93.0, "shock": 102.0, "dip
 # thread instructions; and its DRAM bytes per trajectory (it reads no field data from HBM).
 EXEC_FP32_OPS_PER_STEP = float(os.environ.get("SPX_EXEC_FP32_OPS_PER_STEP", "358"))
 THREAD_INST_PER_STEP = float(os.environ.get("SPX_THREAD_INST_PER_STEP", "571"))
-DRAM_BYTES_PER_TRAJ = float(os.environ.get("SPX_DRAM_BYTES_PER_TRAJ", str(35.375e6 / 320000)))
+DRAM_BYTES_PER_TRAJ = float(os.environ.get("SPX_DRAM_BYTES_PER_TRAJ", str(55.882e6 / 320000)))
 # run indices reserved per rank under torchrun: rank r integrates trajectory ids of runs
 # r*RUNS_PER_RANK ... (disjoint shards of one job)
 RUNS_PER_RANK = 256
@@ -490,6 +490,9 @@ def main():
     ap.add_argument("--steady", type=int, default=0, metavar="CAP",
                     help="instead of the benchmark: steady-state steps/s of the batch with every trajectory stopped "
                          "after CAP steps (SPX_OPT_STEP_CAP), no drain of the queue (profiling)")
+    ap.add_argument("--no-steady", action="store_true",
+                    help="skip the steady-state sample (profiling: the timed launch is then the first step launch "
+                         "after the warm-up)")
     ap.add_argument("--per-launch-steps", type=int, default=2,
                     help="one-slice launches timed for comparison (each pays the drain of the queue)")
     ap.add_argument("--workload", default="gcr", choices=["gcr"] + sorted(OTHER_WORKLOADS),
@@ -579,7 +582,7 @@ def main():
                       "ms_per_launch": statistics.mean(ms), "trajectories_per_launch": st1.trajectories}
     # the rate with every lane busy (trajectories stopped after 4096 steps): the bound the drain keeps
     # the whole run below
-    steady = steady_rate(sim, tun, 4096)
+    steady = None if args.no_steady else steady_rate(sim, tun, 4096)
     sim.close()
     # The timed region: the K steps as one launch of the persistent queue over K slices. Slice k is
     # trajectory ids k*pe ... (k+1)*pe-1 of every energy (pe trajectories per energy), the ids that K
