@@ -246,7 +246,7 @@ def compare_fp32_fp64(sub, tun, tuning64, torch, dev):
     st64, r64, d64 = res["fp64"]
     st32, r32, d32 = res["fp32"]
     r_hot = 50.0 * workloads.ONE_AU  # between the spheres at 0.05 and 100 AU: an exit at the outer one is hot
-    rows = []
+    rows, time_bins = [], []
     for k, pb in enumerate(sub):
         s64 = float(d64[k][0][1][:, 0].sum())
         s32 = float(d32[k][0][1][:, 0].sum())
@@ -261,6 +261,19 @@ def compare_fp32_fp64(sub, tun, tuning64, torch, dev):
         h64, h32 = w[0] > 0, w[1] > 0
         n10, n01 = int((h32 & ~h64).sum()), int((h64 & ~h32).sum())
         hot64 = int(h64.sum())
+        # the exit-time histogram (outer exits, 32 bins from 0 to -t_hist, outliers into the last bin), bin by
+        # bin from the records, paired: count difference and its sigma sqrt(#discordant) per bin
+        t_bin = -workloads.T_HIST_YEARS * 365.0 * 24.0 * 3600.0 / workloads.U.unit_time / 32.0
+        bins = [np.where(hot, np.minimum(np.floor(rec["t"] / t_bin), 31), -1).astype(int)
+                for hot, rec in ((h64, r64[k]), (h32, r32[k]))]
+        for b in range(32):
+            c64 = int((bins[0] == b).sum())
+            if c64 < 10000:
+                continue
+            dd = (bins[1] == b).astype(int) - (bins[0] == b).astype(int)
+            time_bins.append({"energy_mev": round(e_mev, 3), "bin": b, "count_fp64": c64,
+                              "count_histogram_fp64": int(d64[k][1][0][b]),
+                              "rel_err": float(dd.sum()) / c64, "sigma": float(np.sqrt(np.abs(dd).sum())) / c64})
         rows.append({"energy_mev": round(e_mev, 3), "events_fp64": int(d64[k][0][2]),
                      "outer_exits_fp64": hot64,
                      "outer_exit_count_rel_err": (n10 - n01) / hot64 if hot64 else None,
@@ -286,6 +299,11 @@ def compare_fp32_fp64(sub, tun, tuning64, torch, dev):
             "weighted_spectrum_resolved": bool(ok and all(r["sigma"] <= 0.003 for r in ok)),
             "outer_exit_count_max_rel_err": max(abs(r["outer_exit_count_rel_err"]) for r in ok) if ok else None,
             "outer_exit_count_max_sigma": max(r["outer_exit_count_sigma"] for r in ok) if ok else None,
+            "exit_time_bins": time_bins,
+            "exit_time_bin_max_rel_err": max((abs(b["rel_err"]) for b in time_bins), default=None),
+            "exit_time_bin_max_sigma": max((b["sigma"] for b in time_bins), default=None),
+            "exit_time_bin_max_abs_z": max((abs(b["rel_err"]) / b["sigma"] for b in time_bins if b["sigma"] > 0),
+                                           default=None),
             "count_bin_error": ec, "count_bins_compared": nbins}
 
 

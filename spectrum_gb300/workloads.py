@@ -203,10 +203,14 @@ def modulation_energies(n: int = 32, e1_mev: float = 10.0, e2_mev: float = 1.0e4
     return [e1_mev * (e2_mev / e1_mev) ** (i / (n - 1)) for i in range(n)] if n > 1 else [e1_mev]
 
 
+#: span of the modulation runs' exit-time histogram (32 bins from 0 back to this many years)
+T_HIST_YEARS = 10.0
+
+
 def gcr_modulation(n_traj: int = 1_000_000, energies_mev=None, lam0_au: float = 0.1, pow_law_r: float = 0.5,
                    pow_law_b: float = 0.0, kap_rat: float = 0.02, r_inner_au: float = 0.05,
                    r_outer_au: float = 100.0, t_max_years: float = 100.0, lis_gamma: float = -1.8,
-                   t_hist_years: float = 10.0) -> list[Problem]:
+                   t_hist_years: float = T_HIST_YEARS) -> list[Problem]:
     """One problem per energy: start at 1 AU, trace backward until the 100 AU outer boundary
     (hot: weighted by the LIS J0 (T/T0)^gamma / p^2 * v, src/distribution_other.cc:553-602) or the
     0.05 AU inner boundary (cold).
