@@ -87,6 +87,10 @@ extern "C" {
                                        class, and, where every problem has one expiry or pass time boundary, two
                                        spheres and no momentum boundary, for that layout; 2: for the class only;
                                        0: on the kernel that dispatches at run time. Same trajectories. */
+#define SPX_OPT_GRID_INTERP 12      /* SERVER_INTERP_ORDER of a block-layout grid (spx_set_background_blocks):
+                                       1 (default) the 8-zone stencil with its gradients, 0 the values of the zone
+                                       holding the point with zero gradients, -1 the reader's interpolation over
+                                       the domain with numerical gradients (SPX_FP64 contexts only) */
 #define SPX_OPT_STEP_CAP 11         /* 0 (default): off. N > 0: spx_run stops every trajectory after N steps, as the
                                        autotuner's timing samples do: a steady-state throughput sample with no drain
                                        of the queue; trajectories stopped by the cap are neither finished nor binned */

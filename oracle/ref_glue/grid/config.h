@@ -1,7 +1,7 @@
 /* Hand-written stand-in for the reference's autotools config.h (test oracle only), for the grid
  * harness: a parallel build with the Cartesian data server at first-order interpolation, the way
  * configure.ac:301-350 fixes SERVER_TYPE, SERVER_INTERP_ORDER and SERVER_NUM_GHOST_CELLS. The ghost
- * cell count comes from oracle/Makefile (-DSPX_GRID_GHOST). */
+ * cell count and the interpolation order come from oracle/Makefile (-DSPX_GRID_GHOST, -DSPX_GRID_ORDER). */
 #ifndef SPX_REF_GRID_CONFIG_H
 #define SPX_REF_GRID_CONFIG_H
 
@@ -15,7 +15,10 @@
 #define SERVER_CARTESIAN 300
 #define SERVER_BATL 301
 #define SERVER_TYPE SERVER_CARTESIAN
-#define SERVER_INTERP_ORDER 1
+#ifndef SPX_GRID_ORDER
+#define SPX_GRID_ORDER 1
+#endif
+#define SERVER_INTERP_ORDER SPX_GRID_ORDER
 
 #ifndef SPX_GRID_GHOST
 #error "SPX_GRID_GHOST must give the ghost cells per block side (0 or 1)"

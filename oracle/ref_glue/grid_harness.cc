@@ -10,6 +10,8 @@
 //         then one position per line: x y z (code units)
 // stdout, per position, with SERVER_NUM_GHOST_CELLS 0:
 //         status U[3] B[3] Bmag E[3] dmax gradU[9] gradB[9] gradBmag[3]   (%.17g)
+//         (SERVER_INTERP_ORDER 0 and -1: |B| of the converted B, as the background's EvaluateBmag forms it;
+//         order -1 prints zero gradients, the background takes numerical ones)
 //         with SERVER_NUM_GHOST_CELLS 1 (the reader fills no ghost zones, so only the geometry):
 //         node cent_min[3] zone_length[3] zone[3] offset[3] weights[8] derivatives[24]
 // "ERR" for a position whose evaluation throws.
@@ -87,8 +89,23 @@ struct Probe : public ServerCartesianFront {
    }
 };
 
+// SERVER_INTERP_ORDER -1: the front end asks the boss for the variables at a position (GetVariablesFromReader,
+// src/server_cartesian.cc:381-447); the boss answers with the reader's interpolation at the position scaled back
+// to file units (ServerCartesianBack, :1015-1017). Played here in process through the stand-in MPI header.
+static int boss_answer(int tag, void* buf, int count)
+{
+   if (tag != tag_sendvars) return MPI_ERR_OTHER;
+   const Inquiry* inq = static_cast<const Inquiry*>(spx_mpi_last_send());
+   GeoVector pos_cart = inq->pos / Fluid::unit_length * Particle::unit_length;
+   int found = 0;
+   ReadCartesianGetBlockData(pos_cart.Data(), static_cast<double*>(buf), &found);
+   (void)count;
+   return MPI_SUCCESS;
+}
+
 int main(void)
 {
+   spx_mpi_recv_hook() = boss_answer;
    std::string path;
    double dmax0;
    if (!(std::cin >> path)) return 2;
@@ -119,7 +136,18 @@ int main(void)
       sp.dmax = dmax0;
       try {
          srv.GetVariables(0.0, pos, sp);
+#if SERVER_INTERP_ORDER <= 0
+         // the background's EvaluateBmag at these orders (src/background_base.cc:388-391)
+         sp.Bmag = sp.Bvec.Norm();
+#endif
+#if SERVER_INTERP_ORDER == -1
+         // GetGradients only flags the numerical derivatives the background then takes: none here
+         sp.gradUvec = gm_zeros;
+         sp.gradBvec = gm_zeros;
+         sp.gradBmag = gv_zeros;
+#else
          srv.GetGradients(sp);
+#endif
       }
       catch (...) {
          std::printf("ERR\n");

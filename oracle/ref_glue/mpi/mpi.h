@@ -2,7 +2,8 @@
  * server and block sources name, for one process that never sends a message. The grid harness
  * (oracle/ref_glue/grid_harness.cc) drives only BlockBase::GetZoneOffset and the Cartesian
  * server's stencil construction, neither of which communicates; every call that would move data
- * reports failure (MPI_ERR_OTHER) so that an unexpected use shows. */
+ * reports failure (MPI_ERR_OTHER) so that an unexpected use shows, unless the harness answers it (the reader's
+ * interpolation of SERVER_INTERP_ORDER -1, which the front end asks of the boss). */
 #ifndef SPX_MPI_STANDIN_H
 #define SPX_MPI_STANDIN_H
 
@@ -52,8 +53,21 @@ inline int MPI_Request_free(MPI_Request* r) { *r = MPI_REQUEST_NULL; return MPI_
 inline int MPI_Cancel(MPI_Request*) { return MPI_SUCCESS; }
 inline int MPI_Waitall(int, MPI_Request*, MPI_Status*) { return MPI_SUCCESS; }
 inline int MPI_Testsome(int, MPI_Request*, int* outcount, int*, MPI_Status*) { *outcount = MPI_UNDEFINED; return MPI_SUCCESS; }
-inline int MPI_Send(const void*, int, MPI_Datatype, int, int, MPI_Comm) { return MPI_ERR_OTHER; }
-inline int MPI_Recv(void*, int, MPI_Datatype, int, int, MPI_Comm, MPI_Status*) { return MPI_ERR_OTHER; }
+// A harness that plays the other side in process: the last buffer sent, and a hook that answers a receive
+// (tag, buffer, count); without a hook a receive fails.
+inline const void*& spx_mpi_last_send() { static const void* p = nullptr; return p; }
+typedef int (*spx_mpi_recv_fn)(int tag, void* buf, int count);
+inline spx_mpi_recv_fn& spx_mpi_recv_hook() { static spx_mpi_recv_fn h = nullptr; return h; }
+
+inline int MPI_Send(const void* buf, int, MPI_Datatype, int, int, MPI_Comm)
+{
+   spx_mpi_last_send() = buf;
+   return MPI_SUCCESS;
+}
+inline int MPI_Recv(void* buf, int count, MPI_Datatype, int, int tag, MPI_Comm, MPI_Status*)
+{
+   return spx_mpi_recv_hook() ? spx_mpi_recv_hook()(tag, buf, count) : MPI_ERR_OTHER;
+}
 inline int MPI_Irecv(void*, int, MPI_Datatype, int, int, MPI_Comm, MPI_Request* r) { *r = MPI_REQUEST_NULL; return MPI_ERR_OTHER; }
 inline int MPI_Bcast(void*, int, MPI_Datatype, int, MPI_Comm) { return MPI_SUCCESS; }
 inline int MPI_Allreduce(const void*, void*, int, MPI_Datatype, MPI_Op, MPI_Comm) { return MPI_ERR_OTHER; }

@@ -837,9 +837,14 @@ static double shock_trd(double x) { double th = tanh(8.0 * x); return 0.5 * 8.0 
 
 /* EvaluateBackground of each analytic background; fills U, B, E (by mask) and region. Returns
  * the smooth-shock coordinate through *ds (used by EvaluateDmax and the derivatives). */
+static void grid_reader_values(v3 pos, spdata* s);
+
 static void eval_bg(const bg_t* g, double t, v3 pos, unsigned mask, spdata* s, double* ds)
 {
    switch (g->kind) {
+   case BG_GRID: /* the points of numerical derivatives under SERVER_INTERP_ORDER -1 */
+      grid_reader_values(pos, s);
+      break;
    case BG_UNIFORM: /* src/background_uniform.cc:63-72 */
       if (mask & BG_U) s->U = g->u0;
       if (mask & BG_B) s->B = g->B0;
@@ -1039,6 +1044,7 @@ static struct {
    /* block mode (the reference's Cartesian server over its reader's data): nb[0] nb[1] nb[2] blocks
     * of 4^3 zones over [dmin, dmax] (file units), values in fluid units, ghost cells per block side */
    int nb[3], ghost;
+   int order;       /* SERVER_INTERP_ORDER: 1 the stencil, 0 the zone's values, -1 the reader's interpolation */
    v3 dmin, dmax, blen;
    double units[4]; /* Fluid/Particle length, velocity and magnetic ratios; Fluid::c_code */
 } g_grid;
@@ -1086,6 +1092,7 @@ void spx_oracle_set_grid_blocks(const int nb[3], const double dmin[3], const dou
    }
    for (k = 0; k < 4; k++) g_grid.units[k] = units[k];
    g_grid.ghost = ghost;
+   g_grid.order = 1;
    for (b = 0; b < (int64_t)nb[0] * nb[1] * nb[2]; b++) {
       int64_t bi = b % nb[0], bj = (b / nb[0]) % nb[1], bk = b / ((int64_t)nb[0] * nb[1]);
       for (z = 0; z < 64; z++) {
@@ -1097,6 +1104,9 @@ void spx_oracle_set_grid_blocks(const int nb[3], const double dmin[3], const dou
       }
    }
 }
+
+/* SERVER_INTERP_ORDER of the block mode (1, 0 or -1) */
+void spx_oracle_set_grid_order(int order) { g_grid.order = order; }
 
 /* The reference's unit conversion for server data (common/physics.hh:18-55 Fluid,
  * common/specie.hh:25-64 Particle): Fluid/Particle length, velocity, magnetic ratios, Fluid::c_code. */
@@ -1115,7 +1125,7 @@ void spx_oracle_grid_units(double out[4])
  * (src/reader_cartesian.cc:264-277) on the position in file units; the block's faces as the reader
  * and BlockBase::LoadDimensions form them (:291-300, src/block_base.cc:133-152, ghost layers
  * included); ConfigureProperties (:158-171); GetZoneOffset (:194-203). Nonzero outside the domain. */
-static int grid_block_geometry(v3 pos, int bidx[3], v3* cent, v3* zl, int zone[3], double off[3])
+static int grid_block_geometry(v3 pos, int bidx[3], v3* cent, v3* zl, int zone[3], double off[3], v3* face)
 {
    int k;
    const double len = g_grid.units[0];
@@ -1139,6 +1149,7 @@ static int grid_block_geometry(v3 pos, int bidx[3], v3* cent, v3* zl, int zone[3
       }
       zl->x[k] = (fmax_ - fmin_) / (double)bs;
       cent->x[k] = fmin_ + 0.5 * zl->x[k];
+      face->x[k] = fmin_;
       o = (pos.x[k] - cent->x[k]) / zl->x[k];
       zone[k] = (int)o;
       if (o < 0.0) zone[k]--;
@@ -1167,7 +1178,8 @@ int spx_oracle_grid_stencil(const double pos[3], int node[3], double cent_min[3]
    v3 cent, zl;
    double hi[3];
    int k;
-   if (g_grid.nb[0] == 0 || grid_block_geometry(V(pos[0], pos[1], pos[2]), node, &cent, &zl, zone, offset)) return 1;
+   v3 face;
+   if (g_grid.nb[0] == 0 || grid_block_geometry(V(pos[0], pos[1], pos[2]), node, &cent, &zl, zone, offset, &face)) return 1;
    for (k = 0; k < 3; k++) {
       hi[k] = 1.0 - offset[k];
       cent_min[k] = cent.x[k];
@@ -1245,6 +1257,47 @@ static int grid_fields(double dmax0, v3 pos, unsigned mask, spdata* s)
  * values of zones past its faces are its neighbours' (the same global zones). Sums in fluid units,
  * then the unit ratios; E = -(U x B) / Fluid::c_code before its ratio; dmax capped by the block's
  * smallest zone length. A stencil that leaves the domain is a field error. */
+/* U, B and E from fluid-unit values, converted after the interpolation (src/server_cartesian.cc:610-628, 710-716) */
+static void grid_convert(const double var[6], spdata* s)
+{
+   const double vel = g_grid.units[1], mag = g_grid.units[2], cf = g_grid.units[3];
+   v3 U = V(var[0], var[1], var[2]), B = V(var[3], var[4], var[5]), x = vcross(U, B);
+   int k;
+   for (k = 0; k < 3; k++) {
+      s->E.x[k] = (-x.x[k] / cf) * mag;
+      s->U.x[k] = U.x[k] * vel;
+      s->B.x[k] = B.x[k] * mag;
+   }
+}
+
+/* SERVER_INTERP_ORDER -1: the boss's interpolation, ReadCartesianGetBlockData (src/reader_cartesian.cc:193-254),
+ * over the whole domain in file units, for the position scaled as the back end scales it (:1016); the zone
+ * index is truncated, as there. Zero fields outside the domain (the front end's zero-initialised buffer). */
+static void grid_reader_values(v3 pos, spdata* s)
+{
+   double pc[3], lo[3], hi[3], var[6] = {0, 0, 0, 0, 0, 0};
+   int z[3], k, c, q;
+   int64_t nx = g_grid.n[0], nxy = nx * g_grid.n[1];
+   for (k = 0; k < 3; k++) {
+      pc[k] = pos.x[k] / AU_CM * 1.0e10;
+      if (pc[k] < g_grid.dmin.x[k] || pc[k] > g_grid.dmax.x[k]) { grid_convert(var, s); return; }
+   }
+   for (k = 0; k < 3; k++) {
+      double o = (pc[k] - g_grid.dmin.x[k]) / (g_grid.blen.x[k] / 4.0) - 0.5;
+      z[k] = (int)o;
+      lo[k] = o - (double)z[k];
+      hi[k] = 1.0 - lo[k];
+      if (z[k] < 0 || z[k] + 1 >= g_grid.n[k]) { grid_convert(var, s); return; }
+   }
+   for (c = 0; c < 8; c++) {
+      int ci = c & 1, cj = (c >> 1) & 1, ck = (c >> 2) & 1;
+      double fx = ci ? lo[0] : hi[0], fy = cj ? lo[1] : hi[1], fz = ck ? lo[2] : hi[2], w = fx * fy * fz;
+      const double* v = g_grid.v + 8 * ((z[2] + ck) * nxy + (int64_t)(z[1] + cj) * nx + (z[0] + ci));
+      for (q = 0; q < 6; q++) var[q] += w * v[q];
+   }
+   grid_convert(var, s);
+}
+
 static int grid_fields_blocks(double dmax0, v3 pos, spdata* s)
 {
    int bidx[3], zone[3], k, c, q, u, g[3];
@@ -1252,7 +1305,38 @@ static int grid_fields_blocks(double dmax0, v3 pos, spdata* s)
    double lo[3], hi[3], w[8], der[24], var[6] = {0, 0, 0, 0, 0, 0}, grads[6][3], gbm[3] = {0, 0, 0}, bm = 0.0;
    const double vel = g_grid.units[1], mag = g_grid.units[2], cf = g_grid.units[3];
    int64_t nx = g_grid.n[0], nxy = nx * g_grid.n[1];
-   if (grid_block_geometry(pos, bidx, &cent, &zl, zone, lo)) return 1;
+   v3 face;
+   if (grid_block_geometry(pos, bidx, &cent, &zl, zone, lo, &face)) return 1;
+   if (g_grid.order <= 0) {
+      /* GetVariablesInterp0 (src/server_cartesian.cc:479-540): the values of the zone holding the point,
+       * BlockBase::GetZone (src/block_base.cc:180-185); or the reader's interpolation (order -1). |B| is
+       * the norm of the converted B (BackgroundBase::EvaluateBmag); order 0 has zero gradients (:848-852),
+       * order -1 numerical ones (the caller). */
+      s->dmax = fmin(dmax0, fmin(zl.x[0], fmin(zl.x[1], zl.x[2])));
+      if (g_grid.order == 0) {
+         for (k = 0; k < 3; k++) {
+            g[k] = 4 * bidx[k] + (int)((pos.x[k] - face.x[k]) / zl.x[k]) - g_grid.ghost;
+            if (g[k] < 0 || g[k] >= g_grid.n[k]) return 1;
+         }
+         {
+            const double* v = g_grid.v + 8 * (g[2] * nxy + (int64_t)g[1] * nx + g[0]);
+            for (q = 0; q < 6; q++) var[q] = v[q];
+         }
+         grid_convert(var, s);
+      }
+      else grid_reader_values(pos, s);
+      s->region = V(0.0, 0.0, 0.0);
+      s->Bmag = vnorm(s->B);
+      if (s->Bmag < SP_TINY) return 1;
+      s->bhat = vdiv(s->B, s->Bmag);
+      s->gradU = mzero();
+      s->gradB = mzero();
+      s->gradBmag = V(0, 0, 0);
+      s->dUdt = V(0, 0, 0);
+      s->dBdt = V(0, 0, 0);
+      s->dBmagdt = 0.0;
+      return 0;
+   }
    for (k = 0; k < 3; k++) {
       hi[k] = 1.0 - lo[k];
       g[k] = 4 * bidx[k] + zone[k] - g_grid.ghost;  /* global zone of the stencil's corner 0 */
@@ -1328,7 +1412,11 @@ static int get_fields(trj_t* T, double t, v3 pos, v3 mom_pmu, unsigned mask, spd
    s->mask = mask;
    if (g->kind == BG_GRID) {
       for (i = 0; i < 3; i++) s->dr[i] = 0.0001 * g->dmax0;
-      return grid_fields(g->dmax0, pos, mask, s);
+      if (grid_fields(g->dmax0, pos, mask, s)) return 1;
+      /* SERVER_INTERP_ORDER -1 raises BACKGROUND_grad_FAIL (src/server_cartesian.cc:843-846), and the
+       * background then takes numerical derivatives (src/background_server.cc, EvaluateBackgroundDerivatives) */
+      if (g_grid.nb[0] > 0 && g_grid.order == -1) numerical_derivs(g, t, pos, mom_pmu, s);
+      return 0;
    }
    if (g->kind == BG_SMOOTHSHOCK && T->o->reference_quirks)  /* D1 as the reference has it */
       s->dmax = fmin(g->dmax_fraction * g->width * fmax(1.0, fabs(T->bg_ds_prev)), g->dmax0);

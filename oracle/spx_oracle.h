@@ -89,6 +89,8 @@ void spx_oracle_set_grid_blocks(const int nb[3], const double dmin[3], const dou
 /* The fields of the gridded background (either mode) at one point: U[3] B[3] Bmag E[3] dmax gradU[9]
  * gradB[9] gradBmag[3]. Nonzero on a field error. */
 int spx_oracle_grid_fields(const double pos[3], double dmax0, double out[32]);
+/* SERVER_INTERP_ORDER of the block mode: 1 (default), 0 or -1. */
+void spx_oracle_set_grid_order(int order);
 /* The Fluid/Particle length, velocity and magnetic ratios and Fluid::c_code of the reference. */
 void spx_oracle_grid_units(double out[4]);
 /* The primary block and stencil of "pos" in block mode (block indices, zone-centre origin, zone

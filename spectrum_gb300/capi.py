@@ -23,6 +23,7 @@ SPX_OPT_MAX_ATTEMPTS = 5
 SPX_OPT_RUN_INDEX = 6
 SPX_OPT_SPECIALIZE = 10
 SPX_OPT_STEP_CAP = 11
+SPX_OPT_GRID_INTERP = 12
 SPX_OPT_RECORD_CAPACITY = 7
 SPX_OPT_MU_METHOD = 8
 SPX_OPT_PERP_METHOD = 9

@@ -93,7 +93,7 @@ struct spx_ctx {
    double grid_cent[3] = {0, 0, 0}, grid_zone[3] = {0, 0, 0};
    // block mode (spx_set_background_blocks): blocks per axis (0: one uniform block), ghost layers,
    // domain in file units and block length
-   int grid_nb[3] = {0, 0, 0}, grid_ghost = 0;
+   int grid_nb[3] = {0, 0, 0}, grid_ghost = 0, grid_order = 1;
    double grid_dmin[3] = {0, 0, 0}, grid_dmax[3] = {0, 0, 0}, grid_blen[3] = {0, 0, 0};
    double* d_grid64 = nullptr;
    float* d_grid32 = nullptr;
@@ -163,6 +163,7 @@ void apply_grid(const spx_ctx* c, spx::ProblemDesc& pd)
       pd.bg.blk_len[k] = c->grid_blen[k];
    }
    pd.bg.grid_ghost = c->grid_ghost;
+   pd.bg.grid_order = c->grid_nb[0] > 0 ? c->grid_order : 1;  // a uniform grid interpolates at first order
    spx_grid_units(pd.bg.gunits);
 }
 
@@ -697,6 +698,14 @@ int spx_set_option(spx_ctx_t c, int option, double value)
       // (a captured launch is re-captured)
       if (value != 0.0 && value != 1.0 && value != 2.0) return SPX_ERR_INVALID_ARG;
       c->specialize = (int)value;
+      drop_graph(c);
+      return SPX_OK;
+   case SPX_OPT_GRID_INTERP:
+      // the reader's interpolation needs numerical gradients, which the FP64 kernels carry
+      if (value != 1.0 && value != 0.0 && value != -1.0) return SPX_ERR_INVALID_ARG;
+      if (value == -1.0 && c->precision != SPX_FP64) return SPX_ERR_INVALID_ARG;
+      c->grid_order = (int)value;
+      c->dirty = true;
       drop_graph(c);
       return SPX_OK;
    case SPX_OPT_STEP_CAP:

@@ -78,6 +78,8 @@ struct BgParamsT {
    // grid_ghost ghost cells per block side; node values in fluid units, and the ratios
    // {length, velocity, magnetic field} Fluid/Particle and Fluid::c_code in gunits
    int grid_nb[3], grid_ghost;
+   int grid_order;            // SERVER_INTERP_ORDER of the block mode: 1 the stencil, 0 the zone's values,
+                              // -1 the reader's interpolation with numerical gradients (FP64)
    R dom_min[3], dom_max[3], blk_len[3], gunits[4];
 };
 

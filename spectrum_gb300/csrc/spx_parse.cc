@@ -553,6 +553,7 @@ void convert_problem(const ProblemDesc& s, ProblemDescT<R>& d)
    b.grid = nullptr;  // the context points it at its own copy of the grid in this arithmetic
    for (int k = 0; k < 3; k++) b.grid_nb[k] = a.grid_nb[k];
    b.grid_ghost = a.grid_ghost;
+   b.grid_order = a.grid_order;
    cp(a.dom_min, b.dom_min); cp(a.dom_max, b.dom_max); cp(a.blk_len, b.blk_len); cp(a.gunits, b.gunits);
 
    d.df.kind = s.df.kind; d.df.i0 = s.df.i0; d.df.i1 = s.df.i1; cp(s.df.a, d.df.a);

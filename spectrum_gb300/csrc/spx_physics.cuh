@@ -101,8 +101,11 @@ template <class R> __device__ __forceinline__ void derive_from_matrices(SD<R>& s
    s.bgradb = mat_b_gradbhat(s);
 }
 
+template <class R>
+__device__ void grid_reader_values(const BgParamsT<R>& g, V3<R> pos, SD<R>& s);
+
 // EvaluateBackground of the analytic backgrounds: U, B, E by mask, region; *ds is the smooth-shock
-// coordinate (used by the derivatives).
+// coordinate (used by the derivatives); for a grid, the reader's interpolation.
 template <int BG, class R>
 __device__ __forceinline__ void eval_bg(const BgParamsT<R>& g, R t, V3<R> pos, unsigned mask, SD<R>& s, R& ds)
 {
@@ -166,6 +169,7 @@ __device__ __forceinline__ void eval_bg(const BgParamsT<R>& g, R t, V3<R> pos, u
       }
       if (mask & kE) s.E = (R(-1) / c_code<R>()) * cross(s.U, s.B);
    }
+   else if (BG == kBgGrid) grid_reader_values(g, pos, s);  // the points of numerical derivatives (order -1)
 }
 
 // EvaluateDmax (src/background_base.cc:378-382 and overrides). The smooth shock uses the shock
@@ -271,12 +275,59 @@ __device__ __forceinline__ void load_node(const double* p, double* v)
 // units and the Fluid/Particle ratios come after (:549-716, 724-865): E = -(U x B) / Fluid::c_code
 // before its ratio, dmax capped by the block's smallest zone length (:687). A stencil that leaves
 // the domain is a field error.
+// Fluid-unit U and B to code units after the interpolation, E = -(U x B) / Fluid::c_code before its ratio
+// (src/server_cartesian.cc:610-628, 710-716).
+template <class R>
+__device__ __forceinline__ void grid_convert(const BgParamsT<R>& g, const R var[6], SD<R>& s)
+{
+   const R vel = g.gunits[1], mag = g.gunits[2], cf = g.gunits[3];
+   const V3<R> U = mk(var[0], var[1], var[2]), B = mk(var[3], var[4], var[5]), x = cross(U, B);
+   s.E = mk((-x.x / cf) * mag, (-x.y / cf) * mag, (-x.z / cf) * mag);
+   s.U = mk(U.x * vel, U.y * vel, U.z * vel);
+   s.B = mk(B.x * mag, B.y * mag, B.z * mag);
+}
+
+// SERVER_INTERP_ORDER -1: the boss's interpolation, ReadCartesianGetBlockData (src/reader_cartesian.cc:193-254),
+// over the whole domain in file units for the position scaled as the back end scales it (:1016); the zone
+// index is truncated there, and here. Zero fields outside the domain (the front end's zero-initialised buffer).
+template <class R>
+__device__ void grid_reader_values(const BgParamsT<R>& g, V3<R> pos, SD<R>& s)
+{
+   R var[6] = {R(0), R(0), R(0), R(0), R(0), R(0)}, lo[3], hi[3];
+   int z[3];
+   bool inside = true;
+#pragma unroll
+   for (int k = 0; k < 3; k++) {
+      const R pc = pos[k] / R(1.495978707e+13) * R(1.0e10);
+      if (!(pc >= g.dom_min[k] && pc <= g.dom_max[k])) inside = false;
+      const R o = (pc - g.dom_min[k]) / (g.blk_len[k] / R(kGridBlockZones)) - R(0.5);
+      z[k] = (int)o;
+      lo[k] = o - (R)z[k];
+      hi[k] = R(1) - lo[k];
+      if (z[k] < 0 || z[k] + 1 >= g.grid_n[k]) inside = false;
+   }
+   if (inside) {
+      const int64_t nx = g.grid_n[0], nxy = nx * (int64_t)g.grid_n[1];
+      const R* base = g.grid + ((int64_t)z[2] * nxy + (int64_t)z[1] * nx + z[0]) * kGridStride;
+#pragma unroll
+      for (int c = 0; c < 8; c++) {
+         const int ci = c & 1, cj = (c >> 1) & 1, ck = (c >> 2) & 1;
+         const R w = (ci ? lo[0] : hi[0]) * (cj ? lo[1] : hi[1]) * (ck ? lo[2] : hi[2]);
+         R v[7];
+         load_node(base + ((int64_t)ck * nxy + (int64_t)cj * nx + ci) * kGridStride, v);
+#pragma unroll
+         for (int q = 0; q < 6; q++) var[q] += w * v[q];
+      }
+   }
+   grid_convert(g, var, s);
+}
+
 template <class R>
 __device__ __forceinline__ bool grid_fields_blocks(const BgParamsT<R>& g, V3<R> pos, unsigned mask, SD<R>& s)
 {
    const R len = g.gunits[0], vel = g.gunits[1], mag = g.gunits[2], cf = g.gunits[3];
-   R lo[3], hi[3], zl[3];
-   int gz[3];
+   R lo[3], hi[3], zl[3], face[3];
+   int gz[3], bk[3];
 #pragma unroll
    for (int k = 0; k < 3; k++) {
       const R pc = pos[k] / R(1.495978707e+13) * R(1.0e10);  // pos / Fluid::unit_length * Particle::unit_length
@@ -294,6 +345,8 @@ __device__ __forceinline__ bool grid_fields_blocks(const BgParamsT<R>& g, V3<R> 
          bs += 2 * g.grid_ghost;
       }
       zl[k] = (fmx - fmn) / (R)bs;
+      face[k] = fmn;
+      bk[k] = b;
       const R cent = fmn + R(0.5) * zl[k];
       const R o = (pos[k] - cent) / zl[k];
       int z = (int)o;
@@ -301,9 +354,40 @@ __device__ __forceinline__ bool grid_fields_blocks(const BgParamsT<R>& g, V3<R> 
       lo[k] = o - (R)z;
       hi[k] = R(1) - lo[k];
       gz[k] = kGridBlockZones * b + z - g.grid_ghost;
-      if (gz[k] < 0 || gz[k] + 1 >= g.grid_n[k]) return false;
+      if (g.grid_order == 1 && (gz[k] < 0 || gz[k] + 1 >= g.grid_n[k])) return false;
    }
    const int64_t nx = g.grid_n[0], nxy = nx * (int64_t)g.grid_n[1];
+   if (g.grid_order <= 0) {
+      // GetVariablesInterp0 (src/server_cartesian.cc:479-540): the values of the zone holding the point,
+      // BlockBase::GetZone (src/block_base.cc:180-185); or the reader's interpolation (order -1). |B| is the
+      // norm of the converted B (BackgroundBase::EvaluateBmag); order 0 has zero gradients (:848-852),
+      // order -1 numerical ones (get_fields).
+      s.dmax = m_min(g.dmax0, m_min(zl[0], m_min(zl[1], zl[2])));
+      if (g.grid_order == 0) {
+         R var[6], v[7];
+         int zz[3];
+#pragma unroll
+         for (int k = 0; k < 3; k++) {
+            zz[k] = kGridBlockZones * bk[k] + (int)((pos[k] - face[k]) / zl[k]) - g.grid_ghost;
+            if (zz[k] < 0 || zz[k] >= g.grid_n[k]) return false;
+         }
+         load_node(g.grid + ((int64_t)zz[2] * nxy + (int64_t)zz[1] * nx + zz[0]) * kGridStride, v);
+#pragma unroll
+         for (int q = 0; q < 6; q++) var[q] = v[q];
+         grid_convert(g, var, s);
+      }
+      else grid_reader_values(g, pos, s);
+      s.region = mk(R(0), R(0), R(0));
+      s.Bmag = norm(s.B);
+      if (!(s.Bmag >= Lim<R>::tiny)) return false;
+      s.bhat = s.B / s.Bmag;
+      zero(s.gradU);
+      zero(s.gradB);
+      s.gradBmag = mk(R(0), R(0), R(0));
+      s.dUdt = mk(R(0), R(0), R(0));
+      derive_from_matrices(s);
+      return true;
+   }
    const R* base = g.grid + ((int64_t)gz[2] * nxy + (int64_t)gz[1] * nx + gz[0]) * kGridStride;
    const bool grads = (mask & (kGradU | kGradB | kDUdt)) != 0;
    R var[6] = {R(0), R(0), R(0), R(0), R(0), R(0)}, bmag = R(0);
@@ -502,7 +586,16 @@ __device__ __forceinline__ bool get_fields(const BgParamsT<R>& g, int deriv_mode
    }
    if (BG == kBgGrid) {
       s.dr[0] = s.dr[1] = s.dr[2] = R(0.0001) * g.dmax0;
-      return grid_fields(g, pos, mask, s);
+      if (!grid_fields(g, pos, mask, s)) return false;
+      // SERVER_INTERP_ORDER -1 raises BACKGROUND_grad_FAIL (src/server_cartesian.cc:843-846) and the background
+      // takes numerical derivatives; the contexts that select it are FP64 (spx_set_option)
+      if constexpr (sizeof(R) == sizeof(double)) {
+         if (g.grid_nb[0] > 0 && g.grid_order == -1 && (mask & (kGradU | kGradB | kDUdt))) {
+            numerical_derivs<BG>(g, t, pos, p, s, mask);
+            derive_from_matrices(s);
+         }
+      }
+      return true;
    }
    R ds = R(0);
    s.dmax = eval_dmax<BG>(g, t, pos);

@@ -71,6 +71,8 @@ class BlockGrid:
     domain_max: tuple
     values: "object"
     ghost_cells: int = 0
+    #: SERVER_INTERP_ORDER: 1 the 8-zone stencil, 0 the zone's values, -1 the reader's interpolation
+    interp_order: int = 1
 
     @classmethod
     def read(cls, dat_path: str, ghost_cells: int = 0) -> "BlockGrid":

@@ -174,6 +174,8 @@ def open_problems(problems: list[Problem] | Problem, precision: int = capi.SPX_F
         g = base.grid
         if hasattr(g, "n_blocks"):
             sim.ctx.set_background_blocks(g.n_blocks, g.domain_min, g.domain_max, g.ghost_cells, g.values)
+            if g.interp_order != 1:
+                sim.ctx.set_option(capi.SPX_OPT_GRID_INTERP, float(g.interp_order))
         else:
             sim.ctx.set_background_grid(g.n, g.cent_min, g.zone_length, g.values)
     for e in base.plugins:

@@ -166,6 +166,7 @@ def set_grid(grid) -> None:
         u = grid_units()
         vp = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
         lib().spx_oracle_set_grid_blocks(vp(nb), vp(lo), vp(hi), ctypes.c_int(int(grid.ghost_cells)), vp(v), vp(u))
+        lib().spx_oracle_set_grid_order(ctypes.c_int(int(getattr(grid, "interp_order", 1))))
         return
     n = np.ascontiguousarray(np.asarray(grid.n, dtype=np.int64))
     cm = np.ascontiguousarray(np.asarray(grid.cent_min, dtype=np.float64))

@@ -63,13 +63,15 @@ def test_grid_spiral_matches_closed_form(built_lib):
             assert n >= 1 and ok.mean() >= 0.95, (k, d, rg.distros[k][d][0], rc.distros[k][d][0])
 
 
-@pytest.mark.parametrize("ghost", [0, 1])
-def test_block_grid_fp64_matches_oracle(built_lib, ghost):
+@pytest.mark.parametrize("ghost,order", [(0, 1), (1, 1), (0, 0), (0, -1)])
+def test_block_grid_fp64_matches_oracle(built_lib, ghost, order):
     """The reference server's block layout (spx_set_background_blocks, 12^3 blocks of 4^3 zones):
     trajectory by trajectory against the oracle, whose block-mode fields equal the reference's
-    server bit for bit (test_oracle_grid_blocks.py); without and with a ghost layer per block side."""
+    server bit for bit (test_oracle_grid_blocks.py); without and with a ghost layer per block side, and at
+    SERVER_INTERP_ORDER 0 (zone values) and -1 (the reader's interpolation, numerical gradients)."""
     pbs = workloads.gcr_modulation_blocks(n_traj=64, n_blocks=12, ghost_cells=ghost, energies_mev=[300.0],
                                           t_max_years=0.05)
+    pbs[0].grid.interp_order = order
     gpu = run_problems(pbs, precision=capi.SPX_FP64, record=True)
     ref = ot.run_oracle(pbs[0])
     ot.assert_fp64_parity(gpu.records[0], ref, ot.run_oracle(pbs[0], nudge_libm=1), distros=gpu.distros[0])
@@ -84,6 +86,18 @@ def test_block_grid_fp32_matches_fp64(built_lib):
         for d in range(2):
             n, ok = _within_3sigma(r32.distros[k][d][0], r64.distros[k][d][0])
             assert n >= 1 and ok.all(), (k, d)
+
+
+def test_reader_interpolation_needs_fp64(built_lib):
+    """Order -1 takes numerical gradients, which only the FP64 kernels carry."""
+    pbs = workloads.gcr_modulation_blocks(n_traj=10, n_blocks=2, energies_mev=[300.0])
+    ctx = capi.Context(pbs[0].traj, pbs[0].time_flow, pbs[0].rk, capi.SPX_MIXED)
+    try:
+        with pytest.raises(capi.SpxError):
+            ctx.set_option(capi.SPX_OPT_GRID_INTERP, -1.0)
+        ctx.set_option(capi.SPX_OPT_GRID_INTERP, 0.0)
+    finally:
+        ctx.close()
 
 
 def test_block_grid_rejects_bad_layouts(built_lib):

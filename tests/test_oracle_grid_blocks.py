@@ -21,8 +21,8 @@ AU = 1.495978707e13
 L = 1.0e10
 
 
-def _harness(ghost):
-    exe = os.path.join(REF, f"ref_grid{ghost}")
+def _harness(ghost, variant=""):
+    exe = os.path.join(REF, f"ref_grid{ghost}{variant}")
     if not os.path.exists(exe):
         pytest.skip("the reference's grid harness is not built here (make -C oracle grid-ref)")
     return exe
@@ -56,11 +56,11 @@ def probe_points(g, seed=4):
     return np.array(pts) * AU / L
 
 
-def run_harness(ghost, g, pts, dmax0, tmp_path):
+def run_harness(ghost, g, pts, dmax0, tmp_path, variant=""):
     dat = str(tmp_path / "grid.dat")
     g.write(dat)
     text = f"{dat} {dmax0!r}\n" + "".join(" ".join(repr(float(x)) for x in p) + "\n" for p in pts)
-    out = subprocess.run([_harness(ghost)], input=text, capture_output=True, text=True, check=True).stdout
+    out = subprocess.run([_harness(ghost, variant)], input=text, capture_output=True, text=True, check=True).stdout
     return [None if line.strip() == "ERR" else line.split() for line in out.strip().split("\n")]
 
 
@@ -101,6 +101,27 @@ def test_block_fields_equal_the_reference(tmp_path):
         assert mine is not None, p
         assert np.array_equal(mine, ref), (p, np.flatnonzero(mine != ref), mine - ref)
     assert {0, 1, 2, 4} <= statuses  # interior, planes in x and y, edges and corners
+
+
+@pytest.mark.parametrize("order,variant", [(0, "_order0"), (-1, "_reader")])
+def test_other_orders_equal_the_reference(tmp_path, order, variant):
+    """SERVER_INTERP_ORDER 0 (the values of the zone holding the point, zero gradients) and -1 (the boss's
+    reader interpolation over the whole domain, played in process by the harness): U, B, |B|, E and dmax
+    equal the oracle's bit for bit, and order 0's gradients are zero in both. (Order -1's gradients are
+    the background's numerical derivatives, the routine pinned for the analytic backgrounds.)"""
+    g = synthetic_grid()
+    g.interp_order = order
+    pts = probe_points(g)
+    dmax0 = 0.05 * AU / L
+    rows = run_harness(0, g, pts, dmax0, tmp_path, variant)
+    ot.set_grid(g)
+    for p, row in zip(pts, rows):
+        assert row is not None, p
+        ref = np.array([float(x) for x in row[1:]])
+        mine = ot.grid_fields(p, dmax0)
+        assert mine is not None, p
+        n = 11 if order == -1 else 32  # U B Bmag E dmax; order 0 also its (zero) gradients
+        assert np.array_equal(mine[:n], ref[:n]), (p, np.flatnonzero(mine[:n] != ref[:n]))
 
 
 def test_ghost_cell_geometry_equals_the_reference(tmp_path):
