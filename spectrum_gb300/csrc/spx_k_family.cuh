@@ -1,7 +1,8 @@
 // spx_k_family.cuh -- launch and occupancy entry points of the stepping kernel for one
 // trajectory family, arithmetic, field-derivative method and table kind (Euler and the classic RK4
-// with unrolled constants, or any Butcher table from constant memory), switching over the background
-// classes. Each spx_k_*.cu instantiates it once, so the twenty kernel sets compile in parallel.
+// with unrolled constants, or any Butcher table from constant memory), and for the FP32 Parker kernels
+// a diffusion class and boundary layout fixed at compile time, switching over the background classes.
+// Each spx_k_*.cu instantiates it once, so the 24 kernel sets compile in parallel.
 #pragma once
 
 #include "spx_launch.hh"
