@@ -446,6 +446,7 @@ def steady_rate(sim, tun, cap: int, launches: int = 3):
     for _ in range(launches):
         st = sim.MainLoop(tun)
         best = max(best, st.steps / st.kernel_ms * 1e3)
+    steady_rate.last_steps = st.steps  # accepted steps of the last launch (per-step counter figures)
     sim.ctx.set_option(capi.SPX_OPT_STEP_CAP, 0)
     return best
 
@@ -455,7 +456,11 @@ def bench_steady(args):
     from spectrum_gb300 import capi
     from spectrum_gb300.simulation import open_problems
     torch.cuda.set_device(torch.device("cuda", 0))
-    sim = open_problems(problems(args.per_energy), precision=capi.SPX_MIXED)
+    if args.workload == "gcr":
+        pbs, name = problems(args.per_energy), WORKLOAD
+    else:
+        pbs, name = _other_workloads()[args.workload][0](), args.workload
+    sim = open_problems(pbs, precision=capi.SPX_MIXED)
     if args.tuning:
         b, bps, sps = (int(x) for x in args.tuning.split(","))
         tun = capi.Tuning(b, bps, sps, 1)
@@ -464,7 +469,8 @@ def bench_steady(args):
     rate = steady_rate(sim, tun, args.steady, max(1, args.steps))
     sim.close()
     print(json.dumps({"metric": f"steady-state steps/s, every trajectory stopped after {args.steady} steps",
-                      "workload": WORKLOAD, "per_energy": args.per_energy, "value": rate, "unit": "steps/s",
+                      "workload": name, "per_energy": args.per_energy if args.workload == "gcr" else None,
+                      "value": rate, "unit": "steps/s", "steps_last_launch": steady_rate.last_steps,
                       "tuning": [tun.block_size, tun.blocks_per_sm, tun.steps_per_sync]}), flush=True)
 
 
@@ -518,12 +524,12 @@ def main():
                          "other workload families (shortened where the full configuration takes hours)")
     args = ap.parse_args()
     rank, world, local = rank_info()
+    if args.steady:
+        return bench_steady(args)
     if args.workload != "gcr":
         return bench_other(args, rank, world, local)
     if args.accuracy:
         return bench_accuracy(args)
-    if args.steady:
-        return bench_steady(args)
     cfg = {"workload": WORKLOAD, "energies": 32, "per_energy": args.per_energy,
            "trajectories_per_step": 32 * args.per_energy * world, "time_flow": "backward", "background": "solar wind",
            "diffusion": "kappa_par = (0.1 AU) v/3 (R/1GV)^0.5, kappa_perp = 0.02 kappa_par",
