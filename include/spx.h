@@ -86,7 +86,12 @@ extern "C" {
                                        FullConstant or RigidityMagneticFieldPowerLaw run on kernels compiled for that
                                        class, and, where every problem has one expiry or pass time boundary, two
                                        spheres and no momentum boundary, for that layout; 2: for the class only;
-                                       0: on the kernel that dispatches at run time. Same trajectories. */
+                                       0: on the kernel that dispatches at run time. 1 and 2 also run SPX_MIXED
+                                       TrajectoryGuiding contexts on kernels without the scattering and
+                                       perpendicular steps of the other guiding-centre types. The Parker kernels
+                                       give the same trajectories bit for bit; the guiding-centre one the same
+                                       steps and outcomes, with positions equal to FP32 rounding (the compiler
+                                       contracts some multiply-adds differently). */
 #define SPX_OPT_GRID_INTERP 12      /* SERVER_INTERP_ORDER of a block-layout grid (spx_set_background_blocks):
                                        1 (default) the 8-zone stencil with its gradients, 0 the values of the zone
                                        holding the point with zero gradients, -1 the reader's interpolation over

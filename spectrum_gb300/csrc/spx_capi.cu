@@ -308,6 +308,13 @@ int parker_f32_special(const spx_ctx* c)
    return (k == spx::kDfRigidityB || k == spx::kDfFull) ? k : -1;
 }
 
+// TrajectoryGuiding proper in FP32, Euler or RK4: the kernels without the scattering and perpendicular steps.
+bool guiding_plain(const spx_ctx* c)
+{
+   return c->precision == SPX_MIXED && !c->general_rk && c->specialize != 0 && c->traj == SPX_TRAJ_GUIDING &&
+          !c->pa_scattering;
+}
+
 // Whether every problem has the boundary layout spx::kLayoutSpheres: one expiry or pass time boundary,
 // two spheres, no momentum boundary.
 bool layout_spheres(const spx_ctx* c)
@@ -338,6 +345,7 @@ cudaError_t launch(spx_ctx* c, const spx::LaunchArgs& a)
       default: return fd ? spx::launch_guiding_f64fdrk(bg, a) : spx::launch_guiding_f64rk(bg, a);
       }
    }
+   if (guiding_plain(c)) return spx::launch_guiding_f32p(bg, a);
    switch (parker_f32_special(c)) {
    case spx::kDfRigidityB: return layout_spheres(c) ? spx::launch_parker_f32rbs(bg, a) : spx::launch_parker_f32rb(bg, a);
    case spx::kDfFull: return layout_spheres(c) ? spx::launch_parker_f32fcs(bg, a) : spx::launch_parker_f32fc(bg, a);
@@ -377,6 +385,7 @@ int occupancy(spx_ctx* c, int block, int slots)
          return fd ? spx::occupancy_guiding_f64fdrk(bg, block, slots) : spx::occupancy_guiding_f64rk(bg, block, slots);
       }
    }
+   if (guiding_plain(c)) return spx::occupancy_guiding_f32p(bg, block, slots);
    switch (parker_f32_special(c)) {
    case spx::kDfRigidityB:
       return layout_spheres(c) ? spx::occupancy_parker_f32rbs(bg, block, slots) : spx::occupancy_parker_f32rb(bg, block, slots);

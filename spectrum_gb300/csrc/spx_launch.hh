@@ -46,6 +46,9 @@ int occupancy_parker_f32rb(int bg, int block, int slots);
 int occupancy_parker_f32fc(int bg, int block, int slots);
 int occupancy_parker_f32rbs(int bg, int block, int slots);
 int occupancy_parker_f32fcs(int bg, int block, int slots);
+// the FP32 guiding-centre kernels for TrajectoryGuiding proper (kDkNoDiffusion)
+cudaError_t launch_guiding_f32p(int bg, const LaunchArgs& a);
+int occupancy_guiding_f32p(int bg, int block, int slots);
 SPX_DECLARE_FAMILY(lorentz)
 SPX_DECLARE_FAMILY(focused)
 SPX_DECLARE_FAMILY(guiding)

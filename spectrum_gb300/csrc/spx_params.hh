@@ -83,6 +83,10 @@ struct BgParamsT {
    R dom_min[3], dom_max[3], blk_len[3], gunits[4];
 };
 
+// The DK of the guiding-centre kernels compiled for TrajectoryGuiding proper: no pitch-angle scattering and
+// no perpendicular diffusion, so neither step is in the kernel.
+constexpr int kDkNoDiffusion = -2;
+
 // Zones per block edge of the reference's Cartesian blocks (block_size_cartesian, src/reader_cartesian.hh:17)
 constexpr int kGridBlockZones = 4;
 

@@ -1046,16 +1046,18 @@ __device__ __forceinline__ void clamp_mu(AV3<A>& mom)
    else if (mu < R(-1)) acc_setf(mom.y, R(-1));
 }
 
-template <int TT, int BG, class R, class A, class TAB>
+// NODIFF: compiled for a type without pitch-angle scattering and perpendicular diffusion (TrajectoryGuiding
+// proper), so neither step is in the kernel.
+template <int TT, int BG, class R, class A, class TAB, bool NODIFF = false>
 __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, Start& s0, const ProblemDescT<R>& P,
                                            const ProblemDesc& Pd, const RunConfig& cfg, const Sinks& S, const TAB tab)
 {
    constexpr bool kFP64 = sizeof(R) == sizeof(double);
    const bool fwd = cfg.time_flow == 0;
    const int deriv_mode = kFP64 ? cfg.deriv_mode : 1;
-   const bool scatt = (TT == kFocused || TT == kGuiding) && cfg.pa_scattering;
+   const bool scatt = !NODIFF && (TT == kFocused || TT == kGuiding) && cfg.pa_scattering;
    // TrajectoryGuidingDiff / GuidingDiffScatt: perpendicular diffusion on top of the guiding-centre step
-   const bool gc_perp = TT == kGuiding && (cfg.traj_kind == kGuidingDiff || cfg.traj_kind == kGuidingDiffScatt);
+   const bool gc_perp = !NODIFF && TT == kGuiding && (cfg.traj_kind == kGuidingDiff || cfg.traj_kind == kGuidingDiffScatt);
    SD<R> sp;
    V3<R> mom = lane_mom(L);
    // the last stored point's momentum (the pitch-angle step below changes it before the stages): a
@@ -1487,7 +1489,8 @@ __device__ __forceinline__ void start_lane(Lane<R, A>& L, BndView<R> bv, Start& 
 // DM is the field-derivative method (SPX_OPT_DERIV_MODE) fixed per instantiation, so the analytic
 // kernels carry no finite-difference code (whose out-of-line calls would pin the field record to
 // the stack).
-// DK >= 0: a kernel specialised for one diffusion class (the Parker types); -1 dispatches at run time.
+// DK >= 0: a kernel specialised for one diffusion class (the Parker types); -1 dispatches at run time;
+// kDkNoDiffusion: the guiding-centre kernels for TrajectoryGuiding proper (no scattering, no perpendicular step).
 // BL: the boundary layout (BndLayout) the Parker step is compiled for; kLayoutAny reads it from the
 // descriptor.
 template <int TT, int BG, class R, int DM, bool GT, int DK, int BL>
@@ -1563,8 +1566,9 @@ step_kernel(const ProblemDescT<R>* __restrict__ P, const ProblemDesc* __restrict
                else rk_advance<TT, BG, R, A>(L, bv, s0, Pp, Pd[L.prob], cfg, S, tab);
             }
             else if (TT == kParker) parker_advance<BG, DK, BL>(L, bv, s0, Pp, Pd[L.prob], cfg, S);
-            else if (cfg.rk == 25) rk_advance<TT, BG, R, A>(L, bv, s0, Pp, Pd[L.prob], cfg, S, FixedRk<4>{});
-            else rk_advance<TT, BG, R, A>(L, bv, s0, Pp, Pd[L.prob], cfg, S, FixedRk<1>{});
+            else if (cfg.rk == 25)
+               rk_advance<TT, BG, R, A, FixedRk<4>, DK == kDkNoDiffusion>(L, bv, s0, Pp, Pd[L.prob], cfg, S, FixedRk<4>{});
+            else rk_advance<TT, BG, R, A, FixedRk<1>, DK == kDkNoDiffusion>(L, bv, s0, Pp, Pd[L.prob], cfg, S, FixedRk<1>{});
             // Integrate's safety limits (src/trajectory_base.cc:964-992)
             if (L.steps > kMaxTrajSteps || !isfinite(L.dt) || L.dt == R(0)) L.status |= TRAJ_DISCARD;
             done = (L.status & TRAJ_FINISH) && !(L.status & TRAJ_DISCARD);
