@@ -150,7 +150,7 @@ void AddPlugin(Probe& traj, uint32_t role, const std::string& name, const DataCo
       SPX_TRY_BND(BoundaryMomentumPass)
       SPX_TRY_BND(BoundaryMomentumInjectRestrictSlab)
       SPX_TRY_BND(BoundaryMomentumInjectRestrictShell)
-#if (TRAJ_TYPE != TRAJ_PARKER) && (TRAJ_TYPE != TRAJ_PARKER_SOURCE)
+#if (TRAJ_TYPE != TRAJ_PARKER) && (TRAJ_TYPE != TRAJ_PARKER_SOURCE) && (TRAJ_TYPE != TRAJ_FIELDLINE)
       SPX_TRY_BND(BoundaryMirror)
 #endif
    }
@@ -169,7 +169,7 @@ void AddPlugin(Probe& traj, uint32_t role, const std::string& name, const DataCo
 #if (TRAJ_TYPE == TRAJ_LORENTZ) || (TRAJ_TYPE == TRAJ_FIELDLINE)
       SPX_TRY_INI(InitialMomentumFixed)
 #endif
-#if (TRAJ_TYPE != TRAJ_PARKER) && (TRAJ_TYPE != TRAJ_PARKER_SOURCE)
+#if (TRAJ_TYPE != TRAJ_PARKER) && (TRAJ_TYPE != TRAJ_PARKER_SOURCE) && (TRAJ_TYPE != TRAJ_FIELDLINE)
       SPX_TRY_INI(InitialMomentumBeam)
       SPX_TRY_INI(InitialMomentumRing)
 #endif

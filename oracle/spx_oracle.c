@@ -1800,7 +1800,8 @@ static void process_trajectory(trj_t* T, int di, int action)
    case DS_MOM: {
       v3 m = (d->val_time == 0) ? T->mom0 : T->mom;
       v3 bh = (d->val_time == 0) ? s1->bhat : s2->bhat;
-      if (d->val_coord == 0 || (tt != 200 && !IS_GC(tt))) value = m;
+      if (d->val_coord == 0 || (tt != 200 && tt != 199 && !IS_GC(tt))) value = m;
+      else if (tt == 199) value = V(m.x[2], 0.0, 0.0);  /* src/distribution_other.cc:276-279 */
       else if (tt == 200) { value.x[0] = vnorm(m); value.x[1] = vdot(m, bh) / value.x[0]; value.x[2] = 0.0; }
       else { value.x[0] = vnorm(m); value.x[1] = m.x[2] / value.x[0]; value.x[2] = 0.0; }
       break;
@@ -1811,7 +1812,10 @@ static void process_trajectory(trj_t* T, int di, int action)
       value.x[1] = m.x[d->mom_idx];
       break;
    }
-   case DS_SPEC: case DS_SPECBENT: value.x[0] = enr_kin((tt >= 200 && tt <= 204) ? vnorm(T->mom0) : T->mom0.x[0]); break;
+   case DS_SPEC: case DS_SPECBENT:
+      /* src/distribution_other.cc:553-561: Fieldline takes the parallel component */
+      value.x[0] = enr_kin((tt >= 200 && tt <= 204) ? vnorm(T->mom0) : (tt == 199 ? T->mom0.x[2] : T->mom0.x[0]));
+      break;
    case DS_CUM1: case DS_CUM2: value.x[0] = T->t; break;
    case DS_DIVFLOW: value = T->mom0; break;
    case DS_TIMEMU:
@@ -1835,7 +1839,7 @@ static void process_trajectory(trj_t* T, int di, int action)
       break;
    case DS_SPEC: case DS_SPECBENT:
       if (action == 0) {
-         double m2 = (tt >= 200 && tt <= 204) ? vnorm(T->mom) : T->mom.x[0];
+         double m2 = (tt >= 200 && tt <= 204) ? vnorm(T->mom) : (tt == 199 ? T->mom.x[2] : T->mom.x[0]);
          double ke = enr_kin(m2), v = vel_of(m2);
          w[0] = d->J0 * v * pow(ke / d->T0, d->pow_law) / (m2 * m2);
          if (d->kind == DS_SPECBENT) w[0] /= pow(1.0 + pow(ke / d->T_b, d->pow_law_comb), d->bend);
@@ -1998,7 +2002,7 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
    int tt = T->o->traj_type;
    v3 axis = vunit(axis_in);
    switch (q->kind) {
-   case IM_FIXED: return q->v0;
+   case IM_FIXED: return q->v0;  /* Lorentz and Fieldline only */
    case IM_BEAM:
       if (tt == 200) return vscale(q->a[0], axis);
       if (IS_GC(tt)) return V(0.0, 0.0, q->a[0]);
@@ -2019,6 +2023,7 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
          else p = q->a[0] + (q->a[1] - q->a[0]) * next_uniform(T);
       }
       if (tt == 206 || tt == 207) return V(p, 0.0, 0.0);
+      if (tt == 199) return V(0.0, 0.0, p);  /* src/initial_momentum.cc:290-291, 390-391 */
       if (tt == 205) {
          double mu = -1.0 + 2.0 * next_uniform(T);
          return V(p, mu, 0.0);
@@ -2033,8 +2038,11 @@ static v3 sample_mom(trj_t* T, v3 axis_in)
       }
    }
    case IM_MAXWELL: {
-      double p_para = q->a[0] + q->a[1] * next_init_normal(T);
-      double p_perp = q->a[2] * sqrt(-2.0 * log(next_uniform(T)));
+      double p_para, p_perp;
+      /* Fieldline: the mean momentum along the line, no draws (src/initial_momentum.cc:522-525) */
+      if (tt == 199) return V(0.0, 0.0, q->a[0]);
+      p_para = q->a[0] + q->a[1] * next_init_normal(T);
+      p_perp = q->a[2] * sqrt(-2.0 * log(next_uniform(T)));
       if (tt == 200) {
          double phi = M_2PI_ * next_uniform(T);
          v3 e1 = second_unit(axis), e2 = vcross(axis, e1);
@@ -2074,9 +2082,10 @@ static int is_guiding_diff(const trj_t* T) { return T->o->traj_type == 203 || T-
 static int fwd(const trj_t* T) { return T->o->time_flow == 0; }
 
 /* ConvertMomentum: Parker/Focused native (p, mu, -); Lorentz (|p|, p.b/|p|, 0)
- * (src/trajectory_lorentz.hh:84-87) */
+ * (src/trajectory_lorentz.hh:84-87); Fieldline (|p_para|, 0, 0) (src/trajectory_fieldline.hh:80-83) */
 static v3 convert_mom(const trj_t* T)
 {
+   if (T->o->traj_type == 199) return V(fabs(T->mom.x[2]), 0.0, 0.0);
    if (T->o->traj_type == 200) {
       double m = vnorm(T->mom);
       return V(m, vdot(T->mom, T->sp.bhat) / m, 0.0);
@@ -2089,6 +2098,7 @@ static v3 convert_mom(const trj_t* T)
 static unsigned traj_mask(const trj_t* T)
 {
    switch (T->o->traj_type) {
+   case 199: return BG_B;                                         /* src/trajectory_fieldline.cc:37-38, .hh:30 */
    case 200: return BG_E | BG_B;                                  /* src/trajectory_lorentz.cc:36 */
    case 205: return BG_ALL | BG_gradB | BG_gradU | BG_dUdt;       /* src/trajectory_focused.cc:40 */
    /* src/trajectory_guiding.cc:51-52 adds dB/dt, which is zero for every static background */
@@ -2517,9 +2527,18 @@ static int guiding_perp_step(trj_t* T)
    }
 }
 
+/* TrajectoryFieldline::Slopes, src/trajectory_fieldline.cc:58-66: along b at the parallel speed
+ * (which_field_to_follow is BACKGROUND_B, src/trajectory_fieldline.hh:30) */
+static void fieldline_slopes(trj_t* T, v3* sp, v3* sm)
+{
+   *sp = vscale(T->vel.x[2], T->sp.bhat);
+   *sm = V(0.0, 0.0, 0.0);
+}
+
 static void slopes_rk(trj_t* T, v3* sp, v3* sm)
 {
-   if (T->o->traj_type == 200) lorentz_slopes(T, sp, sm);
+   if (T->o->traj_type == 199) fieldline_slopes(T, sp, sm);
+   else if (T->o->traj_type == 200) lorentz_slopes(T, sp, sm);
    else if (is_guiding(T)) {
       guiding_slopes(T, sp, sm);
       if (is_guiding_diff(T)) {
@@ -2533,7 +2552,11 @@ static void slopes_rk(trj_t* T, v3* sp, v3* sm)
 
 static void physical_step_rk(trj_t* T)
 {
-   if (T->o->traj_type == 200) {
+   if (T->o->traj_type == 199) {
+      /* src/trajectory_fieldline.cc:47-50, cfl_adv_tf = 0.5 (src/trajectory_fieldline.hh:27) */
+      T->dt_physical = 0.5 * T->sp.dmax / fabs(T->vel.x[2]);
+   }
+   else if (T->o->traj_type == 200) {
       /* src/trajectory_lorentz.cc:51-59 */
       double vn = vnorm(T->vel);
       double Om = fmax(cyclotron(vn, T->sp.Bmag), SP_TINY);
@@ -2968,6 +2991,25 @@ int spx_oracle_run(const uint8_t* spec, size_t spec_len, const spx_oracle_opts* 
    if ((opts->traj_type == 206 || opts->traj_type == 207 || (opts->traj_type >= 202 && opts->traj_type <= 204)) &&
        !pb->has_diff) {
       snprintf(err, err_len, "Parker, GuidingScatt, GuidingDiff and GuidingDiffScatt trajectories need a diffusion model");
+      free(pb); free(T);
+      return -4;
+   }
+   /* Fieldline: no momentum boundaries (BoundaryMomentum::EvaluateBoundary sets no delta for it,
+    * src/boundary_momentum.cc:69-75; BoundaryMirror is not compiled for it, src/boundary_momentum.hh:225),
+    * no beam or ring initials (src/initial_momentum.hh:86, 131), and no divergence-flow distribution (its
+    * weight reads grad U, which the field-line mask never evaluates) */
+   if (opts->traj_type == 199) {
+      int bad = pb->nbm > 0 || pb->im.kind == IM_BEAM || pb->im.kind == IM_RING || pb->im.kind == IM_LOGE_PITCH;
+      for (d = 0; d < pb->nd; d++) bad |= pb->d[d].kind == DS_DIVFLOW;
+      if (bad) {
+         snprintf(err, err_len, "a plugin class that TrajectoryFieldline does not have");
+         free(pb); free(T);
+         return -4;
+      }
+   }
+   else if (pb->im.kind == IM_FIXED && opts->traj_type != 200) {
+      /* InitialMomentumFixed is compiled for Lorentz and Fieldline only (src/initial_momentum.hh:21) */
+      snprintf(err, err_len, "InitialMomentumFixed needs Lorentz or Fieldline trajectories");
       free(pb); free(T);
       return -4;
    }

@@ -15,6 +15,7 @@ from . import plugins as P
 from .datacontainer import DataContainer
 
 # trajectory types: the reference's configure.ac:236-244 numbering
+TRAJ_FIELDLINE = 199
 TRAJ_LORENTZ = 200
 TRAJ_GUIDING = 201
 TRAJ_GUIDING_SCATT = 202
@@ -23,7 +24,7 @@ TRAJ_GUIDING_DIFF_SCATT = 204
 TRAJ_FOCUSED = 205
 TRAJ_PARKER = 206
 TRAJ_PARKER_SOURCE = 207
-TRAJ_NAMES = {TRAJ_LORENTZ: "TrajectoryLorentz", TRAJ_GUIDING: "TrajectoryGuiding",
+TRAJ_NAMES = {TRAJ_FIELDLINE: "TrajectoryFieldline", TRAJ_LORENTZ: "TrajectoryLorentz", TRAJ_GUIDING: "TrajectoryGuiding",
               TRAJ_GUIDING_SCATT: "TrajectoryGuidingScatt", TRAJ_GUIDING_DIFF: "TrajectoryGuidingDiff",
               TRAJ_GUIDING_DIFF_SCATT: "TrajectoryGuidingDiffScatt", TRAJ_FOCUSED: "TrajectoryFocused",
               TRAJ_PARKER: "TrajectoryParker", TRAJ_PARKER_SOURCE: "TrajectoryParkerSource"}

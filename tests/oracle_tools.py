@@ -235,6 +235,8 @@ REF_VARIANTS = {(206, 0, 0): "parker_fwd_rk0", (206, 1, 0): "parker_bwd_rk0", (2
                 (203, 0, 25): "guidingdiff_fwd_rk25", (204, 0, 25): "guidingdiffscatt_fwd_rk25",
                 (200, 1, 25): "lorentz_bwd_rk25", (205, 1, 25): "focused_bwd_rk25", (204, 1, 25): "guidingdiffscatt_bwd_rk25",
                 (207, 0, 0): "parkersrc_fwd_rk0",
+                (199, 0, 25): "fieldline_fwd_rk25", (199, 1, 25): "fieldline_bwd_rk25", (199, 0, 0): "fieldline_fwd_rk0",
+                (199, 0, 29): "fieldline_fwd_rk29",
                 # other Butcher tables (the reference's benchmarks use 29, Dormand-Prince)
                 (206, 0, 29): "parker_fwd_rk29", (206, 0, 16): "parker_fwd_rk16", (206, 1, 29): "parker_bwd_rk29",
                 (207, 1, 29): "parkersrc_bwd_rk29", (205, 0, 29): "focused_fwd_rk29", (201, 0, 29): "guiding_fwd_rk29",

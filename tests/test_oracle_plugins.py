@@ -37,7 +37,7 @@ from spectrum_gb300.plugins import (BackgroundDipole, BackgroundShock, Backgroun
                                     InitialSpaceRankineHalfBody, InitialSpaceSphere, InitialSpaceSphereSector,
                                     InitialTimeFixed, InitialTimeInterval, SourceConstant, SourceMomentumInjection,
                                     SourceSphericalShockInjection)
-from spectrum_gb300.problem import (BACKWARD, FORWARD, TRAJ_FOCUSED, TRAJ_GUIDING, TRAJ_GUIDING_DIFF, TRAJ_GUIDING_DIFF_SCATT,
+from spectrum_gb300.problem import (BACKWARD, FORWARD, TRAJ_FIELDLINE, TRAJ_FOCUSED, TRAJ_GUIDING, TRAJ_GUIDING_DIFF, TRAJ_GUIDING_DIFF_SCATT,
                                     TRAJ_GUIDING_SCATT, TRAJ_LORENTZ, TRAJ_PARKER,
                                     TRAJ_PARKER_SOURCE, Problem, distro_header)
 
@@ -577,3 +577,88 @@ def test_loss_cone(name):
     ok = np.isfinite(ang)
     assert (bmin < bmax).all() and (ang[ok] > 0).all() and (ang[ok] <= np.pi / 2 + 1e-12).all()
     assert ok.any()
+
+
+# -- TrajectoryFieldline (src/trajectory_fieldline.cc): the field-line tracer ----------------------------
+# Lines of the dipole traced from random points of a sphere of 3 Earth radii at the parallel speed of the
+# momentum's third component; the fields are B only (which_field_to_follow), the step 0.5 dmax / |v_para|.
+# The outer sphere absorbs the lines that reach 8 radii, the inner one reflects (ReverseMomentum negates the
+# whole momentum), and the final points are binned in spherical coordinates.
+def _fieldline_problem(flow=FORWARD, rk=25, im=None, dist=None, reflect=True, n=8, t_end=None, bg=None, scale=None):
+    r_e = scale or W.R_EARTH_CM / U.unit_length  # the length scale of the set-up
+    b_eq = W.B_EARTH_G / U.unit_magnetic
+    if bg is None:
+        bg = (BackgroundDipole(), DC().double(0.0).vec((0, 0, 0)).vec((0, 0, 0)).vec((0.0, 0.0, -b_eq))
+              .double(0.2 * r_e).double(r_e).double(0.05))
+    if dist is None:
+        import math
+        c = distro_header(DC(), (8, 8, 8), (0.5 * r_e, 0.0, 0.0), (10.0 * r_e, math.pi, 2.0 * math.pi),
+                          bin_outside=(1, 1, 1))
+        dist = (DistributionPositionUniform(), c.double(1.0).double(0.0).int(1).int(1))
+    p = U.mev_to_mom(1.0)
+    if t_end is None:  # long enough to reach the outer sphere
+        t_end = (12.0 * r_e / U.Vel(p)) * (1.0 if flow == FORWARD else -1.0)
+    pb = _parker(traj=TRAJ_FIELDLINE, flow=flow, bg=bg, diff=False, dist=dist, n=n, t_end=t_end,
+                 is_=(InitialSpaceSphere(), DC().vec((0.0, 0.0, 0.0)).double(3.0 * r_e)),
+                 im=im or (InitialMomentumShell(), DC().double(p)),
+                 bnds=[(BoundarySphereAbsorb(), B(DC(), 1, [0]).vec((0, 0, 0)).double(8.0 * r_e))] +
+                      ([(BoundarySphereReflect(), B(DC(), -1, [-1]).vec((0, 0, 0)).double(1.5 * r_e))] if reflect else []))
+    pb.rk = rk
+    return pb
+
+
+
+def _fieldline_spectrum():
+    c = distro_header(DC(), (10, 0, 0), (1e-3, 0, 0), (10.0, 0, 0), log_bins=(1, 0, 0), bin_outside=(1, 0, 0))
+    # DistributionSpectrumKineticEnergyPowerLaw: J0, T0, power law, cold value
+    from spectrum_gb300.plugins import DistributionSpectrumKineticEnergyPowerLaw
+    c.double(1.0).double(U.MEV / U.unit_energy).double(-2.5).double(0.0)
+    return DistributionSpectrumKineticEnergyPowerLaw(), c
+
+
+FIELDLINE_CASES = {
+    "dipole_rk4": lambda: _fieldline_problem(),
+    "dipole_rk4_backward": lambda: _fieldline_problem(flow=BACKWARD),
+    "dipole_euler": lambda: _fieldline_problem(rk=0),
+    "dipole_dormand_prince": lambda: _fieldline_problem(rk=29),
+    # against the field: a fixed momentum with a negative parallel component
+    "fixed_antiparallel": lambda: _fieldline_problem(im=(InitialMomentumFixed(), DC().vec((0.3, -0.2, -0.45)))),
+    # one uniform per sample (drawn twice at the start, as SetStart samples twice), log-uniform
+    "thick_shell_log": lambda: _fieldline_problem(im=(InitialMomentumThickShell(), DC().double(0.2).double(0.9)
+                                                      .bool(True))),
+    # the mean momentum only, no draws
+    "maxwell": lambda: _fieldline_problem(im=(InitialMomentumMaxwell(), DC().double(0.5).double(0.1).double(0.05))),
+    # the momentum recorded as (p_para, 0, 0)
+    "momentum_spherical": lambda: _fieldline_problem(
+        dist=(DistributionMomentumUniform(),
+              distro_header(DC(), (10, 0, 0), (-0.5, 0, 0), (0.5, 0, 0)).double(1.0).double(0.0).int(1).int(1)),
+        im=(InitialMomentumFixed(), DC().vec((0.0, 0.0, -0.45)))),
+    # the parallel component's kinetic energy, with the hot weight of the final (reflected, negative) momentum
+    "spectrum": lambda: _fieldline_problem(dist=_fieldline_spectrum()),
+    # Parker-spiral lines from 3 au, absorbed at 8 au
+    "solar_wind_spiral": lambda: _fieldline_problem(bg=_sw_bg(), reflect=False, n=6, scale=W.ONE_AU),
+}
+
+
+@pytest.mark.parametrize("name", sorted(FIELDLINE_CASES))
+def test_fieldline(name):
+    pb = FIELDLINE_CASES[name]()
+    if ot.ref_binary(pb) is None:
+        pytest.skip("reference harness for TrajectoryFieldline not built (needs the reference sources)")
+    r = _same(pb)
+    assert (r.traj["steps"] > 1).all()
+
+
+def test_fieldline_refuses_what_the_reference_does_not_have():
+    """No momentum boundaries, beam or ring initials, or divergence-flow distribution for field lines."""
+    for extra in ("mom_bnd", "beam", "divflow"):
+        pb = _fieldline_problem()
+        if extra == "mom_bnd":
+            pb.AddBoundary(BoundaryMomentumPass(), B(DC(), -1, [0]).double(0.5))
+        elif extra == "beam":
+            pb.replace(4, 2, InitialMomentumBeam(), DC().double(0.02))
+        else:
+            pb.AddDistribution(DistributionDivergenceFlowPowerLaw(), distro_header(DC(), (4, 0, 0), (0, 0, 0), (1, 0, 0))
+                               .double(1.0).double(1.0).double(0.0))
+        with pytest.raises(Exception):
+            ot.run_oracle(pb)
