@@ -46,6 +46,7 @@ extern "C" {
 
 /* ---- enumerations ---------------------------------------------------------------------- */
 /* trajectory types: the numbers of configure.ac:236-244 */
+#define SPX_TRAJ_FIELDLINE 199      /* field-line tracer: B only, no momentum boundaries */
 #define SPX_TRAJ_LORENTZ 200
 #define SPX_TRAJ_GUIDING 201        /* guiding centre, static backgrounds (uniform, dipole, solar wind, grid) */
 #define SPX_TRAJ_GUIDING_SCATT 202  /* guiding centre with pitch-angle scattering (SPX_OPT_MU_METHOD); needs a diffusion model */

@@ -342,6 +342,7 @@ cudaError_t launch(spx_ctx* c, const spx::LaunchArgs& a)
       case SPX_TRAJ_PARKER_SOURCE: return fd ? spx::launch_parker_f64fdrk(bg, a) : spx::launch_parker_f64rk(bg, a);
       case SPX_TRAJ_LORENTZ: return fd ? spx::launch_lorentz_f64fdrk(bg, a) : spx::launch_lorentz_f64rk(bg, a);
       case SPX_TRAJ_FOCUSED: return fd ? spx::launch_focused_f64fdrk(bg, a) : spx::launch_focused_f64rk(bg, a);
+      case SPX_TRAJ_FIELDLINE: return spx::launch_fieldline_f64rk(bg, a);
       default: return fd ? spx::launch_guiding_f64fdrk(bg, a) : spx::launch_guiding_f64rk(bg, a);
       }
    }
@@ -364,6 +365,7 @@ cudaError_t launch(spx_ctx* c, const spx::LaunchArgs& a)
    case SPX_TRAJ_GUIDING_DIFF:
    case SPX_TRAJ_GUIDING_DIFF_SCATT:
       return fd ? spx::launch_guiding_f64fd(bg, a) : f64 ? spx::launch_guiding_f64(bg, a) : spx::launch_guiding_f32(bg, a);
+   case SPX_TRAJ_FIELDLINE: return f64 ? spx::launch_fieldline_f64(bg, a) : spx::launch_fieldline_f32(bg, a);
    default: return cudaErrorInvalidValue;
    }
 }
@@ -381,6 +383,7 @@ int occupancy(spx_ctx* c, int block, int slots)
          return fd ? spx::occupancy_lorentz_f64fdrk(bg, block, slots) : spx::occupancy_lorentz_f64rk(bg, block, slots);
       case SPX_TRAJ_FOCUSED:
          return fd ? spx::occupancy_focused_f64fdrk(bg, block, slots) : spx::occupancy_focused_f64rk(bg, block, slots);
+      case SPX_TRAJ_FIELDLINE: return spx::occupancy_fieldline_f64rk(bg, block, slots);
       default:
          return fd ? spx::occupancy_guiding_f64fdrk(bg, block, slots) : spx::occupancy_guiding_f64rk(bg, block, slots);
       }
@@ -410,6 +413,8 @@ int occupancy(spx_ctx* c, int block, int slots)
    case SPX_TRAJ_GUIDING_DIFF_SCATT:
       return fd ? spx::occupancy_guiding_f64fd(bg, block, slots)
                 : f64 ? spx::occupancy_guiding_f64(bg, block, slots) : spx::occupancy_guiding_f32(bg, block, slots);
+   case SPX_TRAJ_FIELDLINE:
+      return f64 ? spx::occupancy_fieldline_f64(bg, block, slots) : spx::occupancy_fieldline_f32(bg, block, slots);
    default: return 0;
    }
 }
@@ -609,7 +614,8 @@ int spx_create(spx_ctx_t* out, int traj_kind, int time_flow, int rk_method, int 
    if (!out) return SPX_ERR_INVALID_ARG;
    *out = nullptr;
    if (traj_kind != SPX_TRAJ_PARKER && traj_kind != SPX_TRAJ_PARKER_SOURCE && traj_kind != SPX_TRAJ_LORENTZ &&
-       traj_kind != SPX_TRAJ_FOCUSED && (traj_kind < SPX_TRAJ_GUIDING || traj_kind > SPX_TRAJ_GUIDING_DIFF_SCATT))
+       traj_kind != SPX_TRAJ_FOCUSED && traj_kind != SPX_TRAJ_FIELDLINE &&
+       (traj_kind < SPX_TRAJ_GUIDING || traj_kind > SPX_TRAJ_GUIDING_DIFF_SCATT))
       return SPX_ERR_INVALID_ARG;
    if (time_flow != SPX_FORWARD && time_flow != SPX_BACKWARD) return SPX_ERR_INVALID_ARG;
    if (precision != SPX_FP64 && precision != SPX_MIXED) return SPX_ERR_INVALID_ARG;

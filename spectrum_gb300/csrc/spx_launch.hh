@@ -53,5 +53,12 @@ SPX_DECLARE_FAMILY(lorentz)
 SPX_DECLARE_FAMILY(focused)
 SPX_DECLARE_FAMILY(guiding)
 #undef SPX_DECLARE_FAMILY
+// the field-line tracer (B only: no field derivatives, so no *_f64fd units)
+cudaError_t launch_fieldline_f64(int bg, const LaunchArgs& a);
+cudaError_t launch_fieldline_f64rk(int bg, const LaunchArgs& a);
+cudaError_t launch_fieldline_f32(int bg, const LaunchArgs& a);
+int occupancy_fieldline_f64(int bg, int block, int slots);
+int occupancy_fieldline_f64rk(int bg, int block, int slots);
+int occupancy_fieldline_f32(int bg, int block, int slots);
 
 }  // namespace spx

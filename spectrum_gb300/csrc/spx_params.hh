@@ -20,9 +20,9 @@ constexpr int kMaxDistro = 4;  // distributions per problem
 // kGuiding is the kernel family of all four guiding-centre types: TrajectoryGuiding (201), with
 // RunConfig::pa_scattering TrajectoryGuidingScatt (202), and with RunConfig::traj_kind 203/204 the
 // perpendicular-diffusion types TrajectoryGuidingDiff and TrajectoryGuidingDiffScatt, as the reference
-// derives the last three from the first.
+// derives the last three from the first. kFieldline is the field-line tracer TrajectoryFieldline.
 enum TrajKind : int {
-   kLorentz = 200, kGuiding = 201, kGuidingScatt = 202, kGuidingDiff = 203, kGuidingDiffScatt = 204, kFocused = 205,
+   kFieldline = 199, kLorentz = 200, kGuiding = 201, kGuidingScatt = 202, kGuidingDiff = 203, kGuidingDiffScatt = 204, kFocused = 205,
    kParker = 206, kParkerSource = 207
 };
 

@@ -259,14 +259,16 @@ int parse_boundary(Reader& r, int kind, int traj, BndParams& b)
       if (b.region_ind < 0 || b.region_ind > 2) return SPX_ERR_BAD_BLOB;
       break;
    case kBtMomentumInject: case kBtMomentumPass: case kBtMomentumSlab: case kBtMomentumShell:  // src/boundary_momentum.cc
+      // BoundaryMomentum::EvaluateBoundary sets no delta for field lines (src/boundary_momentum.cc:69-75)
+      if (traj == kFieldline) return SPX_ERR_UNKNOWN_PLUGIN;
       b.cls = 2;
       b.momentum = r.d();
       if (kind != kBtMomentumPass) b.max_crossings = 1;
       if (kind == kBtMomentumSlab) { r.v3(b.slab_r0); r.v3(b.slab_r1); r.v3(b.slab_n); }
       if (kind == kBtMomentumShell) { r.v3(b.slab_r0); b.r1 = r.d(); b.r2 = r.d(); }
       break;
-   case kBtMirror:  // src/boundary_momentum.cc:317-339 (not compiled for Parker)
-      if (traj == kParker || traj == kParkerSource) return SPX_ERR_UNKNOWN_PLUGIN;
+   case kBtMirror:  // src/boundary_momentum.cc:317-339 (not compiled for Parker or Fieldline, src/boundary_momentum.hh:225)
+      if (traj == kParker || traj == kParkerSource || traj == kFieldline) return SPX_ERR_UNKNOWN_PLUGIN;
       b.cls = 2;
       b.reflect = 1;
       break;
@@ -330,12 +332,12 @@ int parse_initial(Reader& r, int kind, int traj, IniParams& q)
       }
       break;
    }
-   case kImFixed:  // only compiled for Lorentz (src/initial_momentum.hh:21)
-      if (traj != kLorentz) return SPX_ERR_UNKNOWN_PLUGIN;
+   case kImFixed:  // only compiled for Lorentz and Fieldline (src/initial_momentum.hh:21)
+      if (traj != kLorentz && traj != kFieldline) return SPX_ERR_UNKNOWN_PLUGIN;
       r.v3(q.v0);
       break;
-   case kImBeam: case kImRing:  // not compiled for Parker (src/initial_momentum.hh:86,131)
-      if (parker) return SPX_ERR_UNKNOWN_PLUGIN;
+   case kImBeam: case kImRing:  // not compiled for Parker or Fieldline (src/initial_momentum.hh:86,131)
+      if (parker || traj == kFieldline) return SPX_ERR_UNKNOWN_PLUGIN;
       q.a[0] = r.d();
       if (kind == kImRing) { q.a[1] = r.d(); q.a[2] = std::cos(q.a[1]); q.a[3] = std::sin(q.a[1]); }
       break;
@@ -347,7 +349,10 @@ int parse_initial(Reader& r, int kind, int traj, IniParams& q)
    case kImMaxwell:  // src/initial_momentum.cc:503-514
       q.a[0] = r.d(); q.a[1] = r.d() / std::sqrt(2.0); q.a[2] = r.d() / std::sqrt(2.0);
       break;
-   case kImLogEnergyPitchBand: q.a[0] = r.d(); q.a[1] = r.d(); q.a[2] = r.d(); q.a[3] = r.d(); break;
+   case kImLogEnergyPitchBand:  // a pitch-angle band: no meaning along a field line
+      if (traj == kFieldline) return SPX_ERR_UNKNOWN_PLUGIN;
+      q.a[0] = r.d(); q.a[1] = r.d(); q.a[2] = r.d(); q.a[3] = r.d();
+      break;
    default:
       return SPX_ERR_UNKNOWN_PLUGIN;
    }
@@ -472,6 +477,8 @@ int parse_plugin(ProblemDesc& pd, int traj, int role, int kind, const uint8_t* b
    case SPX_ROLE_DISTRIBUTION: {
       // DistributionAnisotropyLISM is compiled for Lorentz trajectories only (src/distribution_other.hh:245)
       if (kind == kDsAnisotropyLISM && traj != kLorentz) return SPX_ERR_UNKNOWN_PLUGIN;
+      // the divergence-flow weight reads grad U, which a field line's mask (B only) never evaluates
+      if (kind == kDsDivergenceFlow && traj == kFieldline) return SPX_ERR_UNKNOWN_PLUGIN;
       DistParams d;
       int rc = parse_distribution(r, kind, d);
       if (rc != SPX_OK) return rc;

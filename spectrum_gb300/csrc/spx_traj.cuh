@@ -32,7 +32,8 @@ struct Lane {
                      // a general Butcher table: step blocks drawn so far (rejected steps draw too)
    uint32_t n_adapt; // general Butcher tables: consecutive rejected steps
    A t;
-   AV3<A> pos, mom;  // mom: Parker (p,-,-), Focused (p, mu, -), Lorentz (px, py, pz), Guiding (p_perp, -, p_para)
+   AV3<A> pos, mom;  // mom: Parker (p,-,-), Focused (p, mu, -), Lorentz (px, py, pz), Guiding (p_perp, -, p_para),
+                     // Fieldline (-, -, p_para)
    R amp, wgt, dt, dt_adapt, src_del_old;
 };
 
@@ -64,14 +65,19 @@ template <int TT>
 __device__ __forceinline__ constexpr unsigned traj_mask()
 {
    return TT == kLorentz ? (kE | kB)                                 // src/trajectory_lorentz.cc:36
+        : TT == kFieldline ? kB  // which_field_to_follow, src/trajectory_fieldline.hh:30 and .cc:37-38
         : TT == kFocused ? (kAll | kGradB | kGradU | kDUdt)           // src/trajectory_focused.cc:40
         : TT == kGuiding ? (kAll | kGradB)  // src/trajectory_guiding.cc:51-52; dB/dt is zero for the static backgrounds
                          : (kU | kB | kGradU | kGradB);               // src/trajectory_parker.cc:204
 }
 
-// Momentum magnitude passed to the field evaluators (ConvertMomentum()[0]).
+// Momentum magnitude passed to the field evaluators (ConvertMomentum()[0]; Fieldline |p_para|,
+// src/trajectory_fieldline.hh:80-83).
 template <int TT, class R>
-__device__ __forceinline__ R field_p(V3<R> mom) { return (TT == kLorentz || TT == kGuiding) ? norm(mom) : mom.x; }
+__device__ __forceinline__ R field_p(V3<R> mom)
+{
+   return (TT == kLorentz || TT == kGuiding) ? norm(mom) : (TT == kFieldline ? m_abs(mom.z) : mom.x);
+}
 
 // ---- random numbers for set-up -----------------------------------------------------------
 struct InitRng {
@@ -169,7 +175,7 @@ static __device__ __noinline__ V3<double> sample_mom(InitRng& rng, const Problem
    V3<double> axis = unit(axis_in);
    const double two_pi = 6.283185307179586476925286766559;
    switch (q.kind) {
-   case kImFixed: return ld3(q.v0);
+   case kImFixed: return ld3(q.v0);  // Lorentz and Fieldline
    case kImBeam:
       if (traj == kLorentz) return q.a[0] * axis;
       if (traj == kGuiding) return mk(0.0, 0.0, q.a[0]);
@@ -190,12 +196,14 @@ static __device__ __noinline__ V3<double> sample_mom(InitRng& rng, const Problem
          else p = q.a[0] + (q.a[1] - q.a[0]) * rng.uniform();
       }
       if (traj == kParker || traj == kParkerSource) return mk(p, 0.0, 0.0);
+      if (traj == kFieldline) return mk(0.0, 0.0, p);  // src/initial_momentum.cc:290-291, 390-391
       if (traj == kFocused) { double mu = -1.0 + 2.0 * rng.uniform(); return mk(p, mu, 0.0); }
       if (traj == kGuiding) { double mu = -1.0 + 2.0 * rng.uniform(), st = sqrt(1.0 - mu * mu); return mk(p * st, 0.0, p * mu); }
       double mu = -1.0 + 2.0 * rng.uniform(), st = sqrt(1.0 - mu * mu), phi = two_pi * rng.uniform();
       return mk(p * st * cos(phi), p * st * sin(phi), p * mu);
    }
    case kImMaxwell: {
+      if (traj == kFieldline) return mk(0.0, 0.0, q.a[0]);  // the mean only, no draws (src/initial_momentum.cc:522-525)
       double p_para = q.a[0] + q.a[1] * rng.normal();
       double p_perp = q.a[2] * sqrt(-2.0 * log(rng.uniform()));
       if (traj == kLorentz) {
@@ -259,7 +267,8 @@ static __device__ __noinline__ void process_event(int traj, const EventPoint& e,
    case kDsMomentumUniform: {
       V3<double> m = d.val_time == 0 ? s0.mom0 : e.mom;
       V3<double> bh = d.val_time == 0 ? s0.bhat0 : e.bhat;
-      if (d.val_coord == 0 || (traj != kLorentz && traj != kGuiding)) value = m;
+      if (d.val_coord == 0 || (traj != kLorentz && traj != kGuiding && traj != kFieldline)) value = m;
+      else if (traj == kFieldline) value = mk(m.z, 0.0, 0.0);  // src/distribution_other.cc:276-279
       else if (traj == kLorentz) { double mm = norm(m); value = mk(mm, dot(m, bh) / mm, 0.0); }
       else { double mm = norm(m); value = mk(mm, m.z / mm, 0.0); }
       break;
@@ -271,7 +280,9 @@ static __device__ __noinline__ void process_event(int traj, const EventPoint& e,
       break;
    }
    case kDsSpectrumPowerLaw: case kDsSpectrumBentPowerLaw:
-      value.x = enr_kin<double>((traj == kLorentz || traj == kGuiding) ? norm(s0.mom0) : s0.mom0.x);
+      // the parallel component for Fieldline (src/distribution_other.cc:557)
+      value.x = enr_kin<double>((traj == kLorentz || traj == kGuiding) ? norm(s0.mom0)
+                                : (traj == kFieldline ? s0.mom0.z : s0.mom0.x));
       break;
    case kDsCumulative1: case kDsCumulative2: value.x = e.t; break;
    case kDsDivergenceFlow: value = s0.mom0; break;
@@ -299,7 +310,7 @@ static __device__ __noinline__ void process_event(int traj, const EventPoint& e,
       break;
    case kDsSpectrumPowerLaw: case kDsSpectrumBentPowerLaw:
       if (action == 0) {  // DISTRO_KINETIC_ENERGY_POWER_LAW_TYPE 0, src/distribution_other.cc:567-591
-         double m2 = (traj == kLorentz || traj == kGuiding) ? norm(e.mom) : e.mom.x;
+         double m2 = (traj == kLorentz || traj == kGuiding) ? norm(e.mom) : (traj == kFieldline ? e.mom.z : e.mom.x);
          double ke = enr_kin<double>(m2), v = vel_of<double>(m2);
          w[0] = d.J0 * v * pow(ke / d.T0, d.pow_law) / (m2 * m2);
          if (d.kind == kDsSpectrumBentPowerLaw) w[0] /= pow(1.0 + pow(ke / d.T_b, d.pow_law_comb), d.bend);
@@ -438,10 +449,10 @@ __device__ __forceinline__ void handle_crossings(Lane<R, A>& L, BndView<R> bv, c
          // src/trajectory_base.cc:462-483: mirror the position, reverse the momentum
          V3<R> shift = (R(2) * st.delta) * bnd_normal(b, pos);
          add3(L.pos, R(-1) * shift);
-         // ReverseMomentum: the base negates the vector (src/trajectory_base.cc:139-142), Focused its
-         // mu (src/trajectory_focused.hh:141-144), Guiding its parallel component
+         // ReverseMomentum: the base negates the vector (src/trajectory_base.cc:139-142; Lorentz and
+         // Fieldline), Focused its mu (src/trajectory_focused.hh:141-144), Guiding its parallel component
          // (src/trajectory_guiding.hh:123-126), Parker nothing
-         if (TT == kLorentz) { L.mom.x = neg(L.mom.x); L.mom.y = neg(L.mom.y); L.mom.z = neg(L.mom.z); }
+         if (TT == kLorentz || TT == kFieldline) { L.mom.x = neg(L.mom.x); L.mom.y = neg(L.mom.y); L.mom.z = neg(L.mom.z); }
          else if (TT == kFocused) L.mom.y = neg(L.mom.y);
          else if (TT == kGuiding) L.mom.z = neg(L.mom.z);
          pos = val3<R>(L.pos);
@@ -1013,6 +1024,10 @@ __device__ __forceinline__ void rk_slopes(const SD<R>& s, V3<R> mom, V3<R> vel, 
       sp = vel;
       sm = s.E + cross(vel, s.B) / c_code<R>();
    }
+   else if (TT == kFieldline) {  // src/trajectory_fieldline.cc:58-66: along b at the parallel speed
+      sp = vel.z * s.bhat;
+      sm = mk(R(0), R(0), R(0));
+   }
    else if (TT == kGuiding) {
       R dpp, dpl;
       drift = guiding_drift(s, mom, vel, dpp, dpl);
@@ -1204,6 +1219,9 @@ __device__ __forceinline__ void rk_advance(Lane<R, A>& L, BndView<R> bv, Start& 
          R spo = kFP64 ? (R)cfg.steps_per_orbit : (R)cfg.steps_per_orbit_f;
          dtp = R(6.283185307179586476925286766559005768) / Om / spo;
          dtp = m_min(dtp, R(0.1) * sp.dmax / vn);
+      }
+      else if (TT == kFieldline) {  // src/trajectory_fieldline.cc:47-50, cfl_adv_tf = 0.5
+         dtp = R(0.5) * sp.dmax / m_abs(vel.z);
       }
       else if (TT == kGuiding && gc_perp) {  // src/trajectory_guiding_diff.cc:343-351
          V3<R> dv = fwd ? drift + vperp : drift - vperp;
@@ -1411,7 +1429,7 @@ __device__ __noinline__ void set_start(Lane<R, A>& L, BndView<R> bv, Start& s0, 
    acc_set(L.mom.x, mom.x); acc_set(L.mom.y, mom.y); acc_set(L.mom.z, mom.z);
    SD<R> sp;
    V3<R> pr = val3<R>(L.pos);
-   R pm = (TT == kLorentz || TT == kGuiding) ? (R)norm(mom) : (R)mom.x;
+   R pm = (TT == kLorentz || TT == kGuiding) ? (R)norm(mom) : (TT == kFieldline ? (R)fabs(mom.z) : (R)mom.x);
    if (!get_fields<BG>(P.bg, deriv_mode, (R)t, pr, pm, traj_mask<TT>(), sp)) { L.status |= TRAJ_DISCARD; return; }
    V3<double> bh = mk((double)sp.bhat.x, (double)sp.bhat.y, (double)sp.bhat.z);
    mom = sample_mom(rng, Pd, TT, bh);
