@@ -35,6 +35,8 @@
 #include "src/background_uniform.hh"
 #include "src/background_shock.hh"
 #include "src/background_smooth_shock.hh"
+#include "src/background_discontinuity.hh"
+#include "src/background_smooth_discontinuity.hh"
 #include "src/background_dipole.hh"
 #include "src/background_solarwind.hh"
 #include "src/diffusion_other.hh"
@@ -108,6 +110,8 @@ void AddPlugin(Probe& traj, uint32_t role, const std::string& name, const DataCo
       SPX_TRY_BG(BackgroundUniform)
       SPX_TRY_BG(BackgroundShock)
       SPX_TRY_BG(BackgroundSmoothShock)
+      SPX_TRY_BG(BackgroundDiscontinuity)
+      SPX_TRY_BG(BackgroundSmoothDiscontinuity)
       SPX_TRY_BG(BackgroundDipole)
       SPX_TRY_BG(BackgroundSolarWind)
    }

@@ -221,7 +221,7 @@ static int rd_ints(rd_t* r, int* out, int max)
 #define MAXB 8
 #define MAXD 4
 
-enum { BG_UNIFORM = 1, BG_SHOCK, BG_SMOOTHSHOCK, BG_DIPOLE, BG_SOLARWIND, BG_GRID };
+enum { BG_UNIFORM = 1, BG_SHOCK, BG_SMOOTHSHOCK, BG_DIPOLE, BG_SOLARWIND, BG_GRID, BG_DISCONT, BG_SMOOTHDISCONT };
 typedef struct {
    int kind;
    double t0, dmax0;
@@ -229,6 +229,7 @@ typedef struct {
    /* shock (src/background_shock.cc:56-80) */
    v3 n_shock, u1, B1, E0, E1;
    double v_shock, compression, width, dmax_fraction;
+   double tanh_k;  /* the smooth transition's tanh_width_factor */
    /* dipole */
    v3 M;
    /* solar wind */
@@ -334,6 +335,27 @@ static void setup_bg(bg_t* g, rd_t* r, int kind)
          g->width = rd_d(r);
          g->dmax_fraction = rd_d(r);
       }
+      g->tanh_k = 8.0;  /* src/background_smooth_shock.hh:23 */
+   }
+   else if (kind == BG_DISCONT || kind == BG_SMOOTHDISCONT) {
+      /* BackgroundDiscontinuity::SetupBackground, src/background_discontinuity.cc:51-63, and the smooth
+       * one's width and dmax fraction (src/background_smooth_discontinuity.cc:109-116), steepness 4 (its
+       * .hh:49). EvaluateBackground, the derivatives and EvaluateDmax have the shock's forms
+       * (src/background_discontinuity.cc:75-104, src/background_smooth_discontinuity.cc:121-178), so the
+       * two run as a shock and a smooth shock with this downstream state. */
+      g->n_shock = rd_v(r);
+      g->v_shock = rd_d(r);
+      g->u1 = rd_v(r);
+      g->B1 = rd_v(r);
+      g->n_shock = vunit(g->n_shock);
+      g->E0 = vscale(-1.0, vdiv(vcross(g->u0, g->B0), c_code()));
+      g->E1 = vscale(-1.0, vdiv(vcross(g->u1, g->B1), c_code()));
+      g->tanh_k = 4.0;
+      if (kind == BG_SMOOTHDISCONT) {
+         g->width = rd_d(r);
+         g->dmax_fraction = rd_d(r);
+      }
+      g->kind = (kind == BG_DISCONT) ? BG_SHOCK : BG_SMOOTHSHOCK;
    }
    else if (kind == BG_UNIFORM) {
       g->E0 = vscale(-1.0, vdiv(vcross(g->u0, g->B0), c_code()));
@@ -613,6 +635,7 @@ static int kind_of(uint32_t role, const char* nm, size_t nl)
 #define K(s, v) if (name_is(nm, nl, s)) return v;
    if (role == 0) {
       K("BackgroundUniform", BG_UNIFORM) K("BackgroundShock", BG_SHOCK) K("BackgroundSmoothShock", BG_SMOOTHSHOCK)
+      K("BackgroundDiscontinuity", BG_DISCONT) K("BackgroundSmoothDiscontinuity", BG_SMOOTHDISCONT)
       K("BackgroundDipole", BG_DIPOLE) K("BackgroundSolarWind", BG_SOLARWIND)
       K("BackgroundServerCartesian", BG_GRID)
    }
@@ -832,8 +855,8 @@ static double next_init_normal(trj_t* T)
 /* ------------------------------------------------------------------------------------------ */
 
 /* Smooth shock transition (SMOOTH_SHOCK_ORDER 4, src/background_smooth_shock.cc:46-105) */
-static double shock_tr(double x) { return 0.5 * (1.0 + tanh(8.0 * x)); }
-static double shock_trd(double x) { double th = tanh(8.0 * x); return 0.5 * 8.0 * (1.0 - th * th); }
+static double shock_tr(double k, double x) { return 0.5 * (1.0 + tanh(k * x)); }
+static double shock_trd(double k, double x) { double th = tanh(k * x); return 0.5 * k * (1.0 - th * th); }
 
 /* EvaluateBackground of each analytic background; fills U, B, E (by mask) and region. Returns
  * the smooth-shock coordinate through *ds (used by EvaluateDmax and the derivatives). */
@@ -868,7 +891,7 @@ static void eval_bg(const bg_t* g, double t, v3 pos, unsigned mask, spdata* s, d
    case BG_SMOOTHSHOCK: { /* src/background_smooth_shock.cc:124-140 */
       double a1, a2;
       *ds = (vdot(vsub(pos, g->r0), g->n_shock) - g->v_shock * t) / g->width;
-      a1 = shock_tr(*ds);
+      a1 = shock_tr(g->tanh_k, *ds);
       a2 = 1.0 - a1;
       if ((mask & BG_U) || (mask & BG_E)) s->U = vadd(vscale(a1, g->u0), vscale(a2, g->u1));
       if (mask & BG_B) s->B = vadd(vscale(a1, g->B0), vscale(a2, g->B1));
@@ -1437,7 +1460,7 @@ static int get_fields(trj_t* T, double t, v3 pos, v3 mom_pmu, unsigned mask, spd
       s->gradBmag = V(0, 0, 0); s->dUdt = V(0, 0, 0); s->dBdt = V(0, 0, 0); s->dBmagdt = 0.0;
       break;
    case BG_SMOOTHSHOCK: { /* src/background_smooth_shock.cc:149-183 */
-      double fac = shock_trd(ds) / g->width;
+      double fac = shock_trd(g->tanh_k, ds) / g->width;
       v3 du = vsub(g->u0, g->u1), db = vsub(g->B0, g->B1);
       int a, b;
       for (a = 0; a < 3; a++)
@@ -1446,8 +1469,8 @@ static int get_fields(trj_t* T, double t, v3 pos, v3 mom_pmu, unsigned mask, spd
             s->gradB.m[a][b] = g->n_shock.x[a] * db.x[b] * fac;
          }
       s->gradBmag = mvmul(&s->gradB, s->bhat);
-      s->dUdt = vscale(shock_trd(ds) * g->v_shock / g->width, vsub(g->u1, g->u0));
-      s->dBdt = vscale(shock_trd(ds) * g->v_shock / g->width, vsub(g->B1, g->B0));
+      s->dUdt = vscale(shock_trd(g->tanh_k, ds) * g->v_shock / g->width, vsub(g->u1, g->u0));
+      s->dBdt = vscale(shock_trd(g->tanh_k, ds) * g->v_shock / g->width, vsub(g->B1, g->B0));
       s->dBmagdt = 0.0;
       break;
    }

@@ -27,6 +27,10 @@ enum TrajKind : int {
 };
 
 enum BgKind : int { kBgUniform = 1, kBgShock = 2, kBgSmoothShock = 3, kBgDipole = 4, kBgSolarWind = 5, kBgGrid = 6 };
+// BackgroundDiscontinuity and BackgroundSmoothDiscontinuity: plugin kinds only. The parser turns them into
+// kBgShock and kBgSmoothShock descriptors with the downstream state given instead of derived from the
+// jump conditions (and the smooth one's own transition steepness), so they run on the shock kernels.
+enum BgPluginKind : int { kBgDiscontinuity = 7, kBgSmoothDiscontinuity = 8 };
 
 enum DiffKind : int {
    kDfIsotropic = 1, kDfQLT, kDfPara, kDfPerp, kDfFull, kDfFlowMomentum, kDfKinEnergyRadial, kDfRigidityB,
@@ -65,6 +69,7 @@ struct BgParamsT {
    R r0[3], u0[3], B0[3];
    R n_shock[3], u1[3], B1[3], E0[3], E1[3];
    R v_shock, compression, width, dmax_fraction;
+   R tanh_k;                  // the smooth transition's tanh_width_factor: 8 (shock), 4 (discontinuity)
    R M[3];                    // dipole moment B0 r_ref^3
    R eprime[3][3];            // solar wind rotation frame (rows)
    R w0, r_ref, ur0, A;       // A = Br0 r_ref^2

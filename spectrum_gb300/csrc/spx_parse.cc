@@ -114,8 +114,29 @@ int parse_background(Reader& r, int kind, BgParams& g)
          g.width = r.d();
          g.dmax_fraction = r.d();
       }
+      g.tanh_k = 8.0;  // src/background_smooth_shock.hh:23
       break;
    }
+   case kBgDiscontinuity:
+   case kBgSmoothDiscontinuity:
+      // BackgroundDiscontinuity::SetupBackground (src/background_discontinuity.cc:51-63): the normal, its
+      // speed and the state behind it, given; the smooth one adds its width and dmax fraction
+      // (src/background_smooth_discontinuity.cc:109-116) and steepness 4 (its .hh:49). Evaluated by the
+      // shock kernels: the same piecewise and tanh forms (:75-92 and :121-170 of the two files)
+      r.v3(g.n_shock);
+      g.v_shock = r.d();
+      r.v3(g.u1);
+      r.v3(g.B1);
+      normalize(g.n_shock);
+      induced_e(g.u0, g.B0, g.E0);
+      induced_e(g.u1, g.B1, g.E1);
+      g.tanh_k = 4.0;
+      if (kind == kBgSmoothDiscontinuity) {
+         g.width = r.d();
+         g.dmax_fraction = r.d();
+      }
+      g.kind = kind == kBgDiscontinuity ? kBgShock : kBgSmoothShock;
+      break;
    case kBgDipole:  // src/background_dipole.cc:48-58
       g.r_ref = r.d();
       g.dmax_fraction = r.d();
@@ -552,7 +573,7 @@ void convert_problem(const ProblemDesc& s, ProblemDescT<R>& d)
    cp(a.r0, b.r0); cp(a.u0, b.u0); cp(a.B0, b.B0); cp(a.n_shock, b.n_shock); cp(a.u1, b.u1); cp(a.B1, b.B1);
    cp(a.E0, b.E0); cp(a.E1, b.E1);
    b.v_shock = (R)a.v_shock; b.compression = (R)a.compression; b.width = (R)a.width;
-   b.dmax_fraction = (R)a.dmax_fraction;
+   b.dmax_fraction = (R)a.dmax_fraction; b.tanh_k = (R)a.tanh_k;
    cp(a.M, b.M); cp(a.eprime, b.eprime);
    b.w0 = (R)a.w0; b.r_ref = (R)a.r_ref; b.ur0 = (R)a.ur0; b.A = (R)a.A;
    cp(a.cent_min, b.cent_min); cp(a.zone, b.zone); b.zone_min = (R)a.zone_min;

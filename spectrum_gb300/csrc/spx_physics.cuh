@@ -77,9 +77,10 @@ template <class R> __device__ __forceinline__ void zero(M3<R>& a)
 }
 
 // ---- backgrounds -------------------------------------------------------------------------------
-// Smooth transition of SMOOTH_SHOCK_ORDER 4 (src/background_smooth_shock.cc:46-105)
-template <class R> __device__ __forceinline__ R shock_tr(R x) { return R(0.5) * (R(1) + m_tanh(R(8) * x)); }
-template <class R> __device__ __forceinline__ R shock_trd(R x) { R th = m_tanh(R(8) * x); return R(0.5) * R(8) * (R(1) - th * th); }
+// Smooth transition of SMOOTH_SHOCK_ORDER 4 (src/background_smooth_shock.cc:46-105) and SMOOTH_DISCONT_ORDER 4
+// (src/background_smooth_discontinuity.cc:46-105); k is the class's tanh_width_factor
+template <class R> __device__ __forceinline__ R shock_tr(R k, R x) { return R(0.5) * (R(1) + m_tanh(k * x)); }
+template <class R> __device__ __forceinline__ R shock_trd(R k, R x) { R th = m_tanh(k * x); return R(0.5) * k * (R(1) - th * th); }
 
 template <class R> __device__ __forceinline__ V3<R> eframe_to(const BgParamsT<R>& g, V3<R> a)
 {
@@ -131,10 +132,10 @@ __device__ __forceinline__ void eval_bg(const BgParamsT<R>& g, R t, V3<R> pos, u
    }
    else if (BG == kBgSmoothShock) {  // src/background_smooth_shock.cc:124-140
       ds = (dot(pos - ld3(g.r0), ld3(g.n_shock)) - g.v_shock * t) / g.width;
-      R a1 = shock_tr(ds), a2 = R(1) - a1;
+      R a1 = shock_tr(g.tanh_k, ds), a2 = R(1) - a1;
       if ((mask & kU) || (mask & kE)) s.U = a1 * ld3(g.u0) + a2 * ld3(g.u1);
       if (mask & kB) s.B = a1 * ld3(g.B0) + a2 * ld3(g.B1);
-      if (mask & kE) s.E = (R(-1) / c_code<R>()) * cross(s.U, s.B);
+      if (mask & kE) s.E = R(-1) * (cross(s.U, s.B) / c_code<R>());  // InducedEfield: -(U x B) / c
       R rg = R(1) * a1 + R(2) * a2;
       s.region = mk(rg, rg, rg);
    }
@@ -167,7 +168,7 @@ __device__ __forceinline__ void eval_bg(const BgParamsT<R>& g, R t, V3<R> pos, u
          R Bp = -Br * sintheta * r_mns * g.w0 / ur;
          s.B = eframe_from(g, mk(Br * sintheta * cosphi - Bp * sinphi, Br * sintheta * sinphi + Bp * cosphi, Br * costheta));
       }
-      if (mask & kE) s.E = (R(-1) / c_code<R>()) * cross(s.U, s.B);
+      if (mask & kE) s.E = R(-1) * (cross(s.U, s.B) / c_code<R>());  // InducedEfield: -(U x B) / c
    }
    else if (BG == kBgGrid) grid_reader_values(g, pos, s);  // the points of numerical derivatives (order -1)
 }
@@ -208,7 +209,7 @@ __device__ __forceinline__ bool solarwind_closed(const BgParamsT<R>& g, V3<R> po
    V3<R> w = cross(x, O);
    s.U = (g.ur0 * ir) * x;
    s.B = (g.A * ir3) * x + (k * f) * w;
-   if (mask & kE) s.E = (R(-1) / c_code<R>()) * cross(s.U, s.B);
+   if (mask & kE) s.E = R(-1) * (cross(s.U, s.B) / c_code<R>());  // InducedEfield: -(U x B) / c
    s.Bmag = norm(s.B);
    if (!(s.Bmag >= Lim<R>::tiny)) return false;
    R iB = R(1) / s.Bmag;
@@ -618,7 +619,7 @@ __device__ __forceinline__ bool get_fields(const BgParamsT<R>& g, int deriv_mode
       return true;
    }
    else if (BG == kBgSmoothShock) {  // src/background_smooth_shock.cc:149-183
-      R tr = shock_trd(ds);
+      R tr = shock_trd(g.tanh_k, ds);
       R fac = tr / g.width;
       V3<R> du = ld3(g.u0) - ld3(g.u1), db = ld3(g.B0) - ld3(g.B1), n = ld3(g.n_shock);
 #pragma unroll

@@ -78,6 +78,14 @@ class BackgroundDipole(Plugin): pass  # src/background_dipole.cc:48-125
 class BackgroundSolarWind(Plugin): pass  # src/background_solarwind.cc:58-314
 
 
+@_plugin(ROLE_BACKGROUND, 7)
+class BackgroundDiscontinuity(Plugin): pass  # src/background_discontinuity.cc:51-104 (runs on the shock kernels)
+
+
+@_plugin(ROLE_BACKGROUND, 8)
+class BackgroundSmoothDiscontinuity(Plugin): pass  # src/background_smooth_discontinuity.cc:46-178 (smooth-shock kernels)
+
+
 @_plugin(ROLE_BACKGROUND, 6)
 class BackgroundServerCartesian(Plugin):
     """The base parameters only (src/background_base.cc:342-346); the grid itself comes with

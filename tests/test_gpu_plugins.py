@@ -57,6 +57,9 @@ def _problems():
         out["loss_cone_" + name] = make
     for name, make in cases.ANISO_CASES.items():
         out["anisotropy_lism_" + name] = make
+    for name, make in cases.DISCONT_CASES.items():
+        if not name.startswith("fieldline"):  # the field-line case runs with the other field lines
+            out["discontinuity_" + name] = make
     out["parker_source_constant"] = lambda: cases._parker(
         traj=cases.TRAJ_PARKER_SOURCE, flow=cases.BACKWARD, src=(cases.SourceConstant(), DC().double(0.7)),
         t_end=-0.05, n=12)

@@ -1,7 +1,8 @@
 """TrajectoryFieldline on the device: the FP64 kernels against the oracle on the field-line problems
 whose oracle runs tests/test_oracle_plugins.py pins bit for bit to the reference's own field-line builds
 (dipole lines with a reflecting and an absorbing sphere, both time flows, Euler, RK4 and
-Dormand-Prince, the momentum samplers, the momentum and spectrum distributions, Parker-spiral lines).
+Dormand-Prince, the momentum samplers, the momentum and spectrum distributions, Parker-spiral lines,
+lines through a moving smooth discontinuity).
 Every trajectory takes the same steps to the same outcome, every histogram bin and event count is
 equal, and positions agree to within the oracle's own one-ulp libm spread. The FP32 kernels trace the
 same dipole lines to within single-precision accuracy."""
@@ -17,9 +18,12 @@ from spectrum_gb300.simulation import run_problems
 pytestmark = pytest.mark.gpu
 
 
-@pytest.mark.parametrize("name", sorted(cases.FIELDLINE_CASES))
+FP64_CASES = {**cases.FIELDLINE_CASES, "smooth_discontinuity": cases.DISCONT_CASES["fieldline_smooth"]}
+
+
+@pytest.mark.parametrize("name", sorted(FP64_CASES))
 def test_fieldline_fp64_equals_the_oracle(built_lib, name):
-    pb = cases.FIELDLINE_CASES[name]()
+    pb = FP64_CASES[name]()
     res = run_problems(pb, precision=capi.SPX_FP64, record=True)
     ref = ot.run_oracle(pb)
     ot.assert_fp64_parity(res.records[0], ref, ot.run_oracle(pb, nudge_libm=1), distros=res.distros[0])

@@ -662,3 +662,49 @@ def test_fieldline_refuses_what_the_reference_does_not_have():
                                .double(1.0).double(1.0).double(0.0))
         with pytest.raises(Exception):
             ot.run_oracle(pb)
+
+
+# -- BackgroundDiscontinuity and BackgroundSmoothDiscontinuity (src/background_discontinuity.cc,
+# src/background_smooth_discontinuity.cc): a moving plane across which U and B jump to a given state, sharp
+# or through a tanh of steepness 4 (the smooth shock's is 8). The reference's smooth discontinuity is
+# compiled through oracle/ref_glue/smooth_discont_wrap.cc (it names c_code unqualified).
+def _discontinuity(smooth):
+    from spectrum_gb300.plugins import BackgroundDiscontinuity, BackgroundSmoothDiscontinuity
+    c = DC().double(0.0).vec((0, 0, 0)).vec((0.8, 0.1, 0.0)).vec((0.2, 0.1, 1.0)).double(0.02)
+    c.vec((1.0, 0.3, 0.0)).double(0.3).vec((0.25, -0.2, 0.05)).vec((0.5, 0.6, 1.4))
+    if smooth:
+        return BackgroundSmoothDiscontinuity(), c.double(0.05).double(0.1)
+    return BackgroundDiscontinuity(), c
+
+
+def _discontinuity_problem(traj, smooth, flow=FORWARD, n=12):
+    c = distro_header(DC(), (20, 0, 0), (-1.0, 0, 0), (1.0, 0, 0), bin_outside=(1, 0, 0))
+    dist = (DistributionPositionUniform(), c.double(1.0).double(0.0).int(1).int(0))
+    kw = dict(diff=(DiffusionFullConstant(), DC().double(0.01).double(0.02)), t_end=0.5) if traj == TRAJ_PARKER else \
+        dict(diff=False, t_end=0.3)
+    pb = _parker(traj=traj, bg=_discontinuity(smooth), dist=dist, n=n, flow=flow,
+                 is_=(InitialSpaceFixed(), DC().vec((-0.05, 0.0, 0.0))), **kw)
+    if traj == TRAJ_LORENTZ:
+        pb.options[W.SPX_OPT_STEPS_PER_ORBIT] = 100.0
+    if traj == TRAJ_FIELDLINE:
+        pb.replace(4, 2, InitialMomentumShell(), DC().double(0.2))
+    return pb
+
+
+DISCONT_CASES = {
+    "parker_sharp": lambda: _discontinuity_problem(TRAJ_PARKER, False),
+    "parker_smooth": lambda: _discontinuity_problem(TRAJ_PARKER, True),
+    "focused_smooth": lambda: _discontinuity_problem(TRAJ_FOCUSED, True),
+    "lorentz_sharp": lambda: _discontinuity_problem(TRAJ_LORENTZ, False),
+    "lorentz_smooth": lambda: _discontinuity_problem(TRAJ_LORENTZ, True),
+    "fieldline_smooth": lambda: _discontinuity_problem(TRAJ_FIELDLINE, True),
+}
+
+
+@pytest.mark.parametrize("name", sorted(DISCONT_CASES))
+def test_discontinuity_backgrounds(name):
+    pb = DISCONT_CASES[name]()
+    if ot.ref_binary(pb) is None:
+        pytest.skip("reference harness not built for this trajectory type")
+    r = _same(pb)
+    assert (r.traj["steps"] > 1).all()
