@@ -126,6 +126,8 @@ SPX_PROTOTYPE(BackgroundSmoothShock, BackgroundBase, 3)
 SPX_PROTOTYPE(BackgroundDipole, BackgroundBase, 4)
 SPX_PROTOTYPE(BackgroundSolarWind, BackgroundBase, 5)
 SPX_PROTOTYPE(BackgroundServerCartesian, BackgroundBase, 6)
+SPX_PROTOTYPE(BackgroundDiscontinuity, BackgroundBase, 7)
+SPX_PROTOTYPE(BackgroundSmoothDiscontinuity, BackgroundBase, 8)
 SPX_PROTOTYPE(DiffusionIsotropicConstant, DiffusionBase, 1)
 SPX_PROTOTYPE(DiffusionQLTConstant, DiffusionBase, 2)
 SPX_PROTOTYPE(DiffusionParaConstant, DiffusionBase, 3)
@@ -188,6 +190,8 @@ SPX_PROTOTYPE(DistributionSpectrumKineticEnergyBentPowerLaw, DistributionBase, 6
 SPX_PROTOTYPE(DistributionPositionCumulativeOrder1, DistributionBase, 7)
 SPX_PROTOTYPE(DistributionPositionCumulativeOrder2, DistributionBase, 8)
 SPX_PROTOTYPE(DistributionDivergenceFlowPowerLaw, DistributionBase, 9)
+SPX_PROTOTYPE(DistributionLossCone, DistributionBase, 10)
+SPX_PROTOTYPE(DistributionAnisotropyLISM, DistributionBase, 11)  // Lorentz trajectories only
 SPX_PROTOTYPE(DistributionTimeMu, DistributionBase, 20)  // extension: no reference class
 #undef SPX_PROTOTYPE
 
@@ -253,6 +257,7 @@ public:
    std::string GetTrajectoryName(void) const
    {
       switch (traj_) {
+      case SPX_TRAJ_FIELDLINE: return "TrajectoryFieldline";
       case SPX_TRAJ_LORENTZ: return "TrajectoryLorentz";
       case SPX_TRAJ_GUIDING: return "TrajectoryGuiding";
       case SPX_TRAJ_GUIDING_SCATT: return "TrajectoryGuidingScatt";

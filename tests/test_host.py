@@ -190,3 +190,21 @@ def test_static_capacity_matches_the_descriptor_sizes(tmp_path):
     mixed = max(n for n in range(1, 1000) if up(256 + pd * n) + pr * n <= scratch)
     m = re.search(r"(\d+) problems in SPX_MIXED, (\d+) in SPX_FP64", hdr)
     assert (int(m.group(1)), int(m.group(2))) == (mixed, fp64)
+
+
+def test_cpp_host_mirror_has_every_plugin_class():
+    """The C++ host mirror (include/spx_simulation.hh) declares one prototype per plugin class of the
+    Python registry, with the same role and kind, and names every trajectory type the header defines."""
+    from spectrum_gb300 import plugins as P
+    from spectrum_gb300.problem import TRAJ_NAMES
+    src = open(os.path.join(ROOT, "include", "spx_simulation.hh")).read()
+    base_role = {"BackgroundBase": P.ROLE_BACKGROUND, "DiffusionBase": P.ROLE_DIFFUSION, "SourceBase": P.ROLE_SOURCE,
+                 "BoundaryBase": P.ROLE_BOUNDARY, "InitialBase": P.ROLE_INITIAL, "DistributionBase": P.ROLE_DISTRIBUTION}
+    cpp = {m.group(1): (base_role[m.group(2)], int(m.group(3)))
+           for m in re.finditer(r"^SPX_PROTOTYPE\((\w+), (\w+), (\d+)\)", src, re.M)}
+    py = {c.__name__: (c.role, c.kind) for c in P.all_plugins()}
+    assert cpp == py
+    hdr = open(os.path.join(ROOT, "include", "spx.h")).read()
+    for num, name in TRAJ_NAMES.items():
+        assert re.search(rf"#define SPX_TRAJ_\w+ {num}\b", hdr), num
+        assert f'return "{name}";' in src, name
