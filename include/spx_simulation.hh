@@ -16,10 +16,13 @@
 #ifndef SPX_SIMULATION_HH
 #define SPX_SIMULATION_HH
 
+#include <algorithm>
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
 #include <cstring>
+#include <fstream>
+#include <iomanip>
 #include <stdexcept>
 #include <string>
 #include <vector>
@@ -195,6 +198,139 @@ SPX_PROTOTYPE(DistributionAnisotropyLISM, DistributionBase, 11)  // Lorentz traj
 SPX_PROTOTYPE(DistributionTimeMu, DistributionBase, 20)  // extension: no reference class
 #undef SPX_PROTOTYPE
 
+// ---- text output of a distribution ---------------------------------------------------------------
+// DistributionTemplated::Print1D, Print2D and PrintRecords (src/distribution_templated.cc:472-686),
+// written from a distribution's parameter container, histogram and records. The binning is
+// SetupDistribution's (src/distribution_templated.cc:92-137); the files go through an std::ofstream as
+// the reference writes them: a comment line, an empty line, then rows of setw(20) columns at 10
+// significant digits (PrintRecords keeps the stream's default 6).
+struct DistroLayout {
+   int n_bins[3] = {1, 1, 1}, log_bins[3] = {0, 0, 0}, width = 1;
+   double limits0[3] = {0, 0, 0}, bin_size[3] = {0, 0, 0}, unit_distro[9] = {}, unit_val[3] = {1, 1, 1};
+
+   // From the container's first seven records; false if they are not those of a DistributionTemplated
+   // of this width (1, 3 or 9 doubles per bin).
+   bool Read(const uint8_t* blob, size_t len, int width_in)
+   {
+      const size_t expect[7] = {12, 24, 24, 12, 12, 8 * (size_t)width_in, 24};
+      const uint8_t* rec[7];
+      size_t pos = 0;
+      for (int r = 0; r < 7; r++) {
+         if (pos >= len || blob[pos] != expect[r] || pos + 1 + blob[pos] > len) return false;
+         rec[r] = blob + pos + 1;
+         pos += 1 + blob[pos];
+      }
+      double minval[3], maxval[3];
+      width = width_in;
+      std::memcpy(n_bins, rec[0], 12);
+      std::memcpy(minval, rec[1], 24);
+      std::memcpy(maxval, rec[2], 24);
+      std::memcpy(log_bins, rec[3], 12);
+      std::memcpy(unit_distro, rec[5], 8 * (size_t)width);
+      std::memcpy(unit_val, rec[6], 24);
+      for (int k = 0; k < 3; k++) {
+         n_bins[k] = std::max(n_bins[k], 1);
+         const double lo = log_bins[k] ? std::log10(minval[k]) : minval[k];
+         const double hi = log_bins[k] ? std::log10(maxval[k]) : maxval[k];
+         limits0[k] = lo;
+         bin_size[k] = (hi - lo) / n_bins[k];
+      }
+      return true;
+   }
+
+   // DistributionBase::BinCent (src/distribution_base.hh:267-272)
+   double BinCent(int ijk, int bin) const
+   {
+      if (bin < 0 || bin >= n_bins[ijk]) return 0.0;
+      const double x = limits0[ijk] + (bin + 0.5) * bin_size[ijk];
+      return log_bins[ijk] ? std::pow(10.0, x) : x;
+   }
+
+   long Lin(const int b[3]) const { return ((long)b[0] * n_bins[1] + b[1]) * n_bins[2] + b[2]; }
+
+   // PrintSumDistro (src/distribution_templated.cc:472-535): the mean and the sum of the weights
+   void SumColumns(std::ofstream& f, long n, const double* s, bool phys) const
+   {
+      if (width == 1) {
+         f << std::setw(20) << (n ? s[0] / n : 0.0) * (phys ? unit_distro[0] : 1.0) << std::setw(20)
+           << s[0] * (phys ? unit_distro[0] : 1.0);
+      }
+      else if (n) {
+         for (int i = 0; i < width; i++) f << std::setw(20) << (phys ? s[i] / n * unit_distro[i] : s[i] / n);
+         for (int i = 0; i < width; i++) f << std::setw(20) << (phys ? s[i] * unit_distro[i] : s[i]);
+      }
+      else
+         for (int i = 0; i < 2 * width; i++) f << std::setw(20) << 0.0;
+   }
+
+   // Print1D: axis ijk, the other two collapsed
+   void Print1D(const std::string& path, const int32_t* counts, const double* sums, long long n_events, int ijk,
+                bool phys) const
+   {
+      if (ijk < 0 || ijk >= 3) return;
+      const int i1 = (ijk + 1) % 3, i2 = (ijk + 2) % 3;
+      std::ofstream f(path.c_str());
+      f << "# Total number of events: " << n_events << std::endl << std::endl;
+      f << std::setprecision(10);
+      int b[3];
+      for (b[ijk] = 0; b[ijk] < n_bins[ijk]; b[ijk]++) {
+         long n = 0;
+         double s[9] = {};
+         for (b[i1] = 0; b[i1] < n_bins[i1]; b[i1]++)
+            for (b[i2] = 0; b[i2] < n_bins[i2]; b[i2]++) {
+               const long k = Lin(b);
+               n += counts[k];
+               for (int w = 0; w < width; w++) s[w] += sums[k * width + w];
+            }
+         f << std::setw(20) << BinCent(ijk, b[ijk]) * (phys ? unit_val[ijk] : 1.0);
+         SumColumns(f, n, s, phys);
+         f << std::setw(20) << n << std::endl;
+      }
+   }
+
+   // Print2D: axes ijk1 and ijk2, the third collapsed; Print1D for equal axes
+   void Print2D(const std::string& path, const int32_t* counts, const double* sums, long long n_events, int ijk1,
+                int ijk2, bool phys) const
+   {
+      if (ijk1 < 0 || ijk1 >= 3 || ijk2 < 0 || ijk2 >= 3) return;
+      if (ijk1 == ijk2) {
+         Print1D(path, counts, sums, n_events, ijk1, phys);
+         return;
+      }
+      const int ijk = 3 - ijk1 - ijk2;
+      std::ofstream f(path.c_str());
+      f << "# Total number of events: " << n_events << std::endl << std::endl;
+      f << std::setprecision(10);
+      int b[3];
+      for (b[ijk1] = 0; b[ijk1] < n_bins[ijk1]; b[ijk1]++)
+         for (b[ijk2] = 0; b[ijk2] < n_bins[ijk2]; b[ijk2]++) {
+            long n = 0;
+            double s[9] = {};
+            for (b[ijk] = 0; b[ijk] < n_bins[ijk]; b[ijk]++) {
+               const long k = Lin(b);
+               n += counts[k];
+               for (int w = 0; w < width; w++) s[w] += sums[k * width + w];
+            }
+            f << std::setw(20) << BinCent(ijk1, b[ijk1]) * (phys ? unit_val[ijk1] : 1.0) << std::setw(20)
+              << BinCent(ijk2, b[ijk2]) * (phys ? unit_val[ijk2] : 1.0);
+            SumColumns(f, n, s, phys);
+            f << std::setw(20) << n << std::endl;
+         }
+   }
+
+   // PrintRecords with PrintWeight (src/distribution_templated.cc:643-682): three values, the weight(s)
+   void PrintRecords(const std::string& path, const double* values, const double* weights, size_t n, bool phys) const
+   {
+      std::ofstream f(path.c_str());
+      f << "# Total number of records: " << n << std::endl << std::endl;
+      for (size_t i = 0; i < n; i++) {
+         for (int j = 0; j < 3; j++) f << std::setw(20) << values[3 * i + j] * (phys ? unit_val[j] : 1.0);
+         for (int w = 0; w < width; w++) f << std::setw(20) << weights[i * width + w] * (phys ? unit_distro[w] : 1.0);
+         f << std::endl;
+      }
+   }
+};
+
 // ---- the simulation object -----------------------------------------------------------------------
 class SimulationGPU {
    spx_ctx_t ctx_ = nullptr;
@@ -244,6 +380,7 @@ public:
    {
       add(SPX_ROLE_DISTRIBUTION, p.kind, c, "AddDistribution");
       distro_names_.push_back(std::to_string(p.kind));
+      distro_blobs_.emplace_back(c.data(), c.data() + c.length());
    }
 
    // src/simulation.hh:96-97: one problem of n_traj trajectories (the batch sizes of the MPI farm
@@ -325,27 +462,64 @@ public:
       return k;
    }
 
-   // Bin index, count and mean weight per bin of one distribution of one problem (the columns of
-   // DistributionTemplated::Print1D, src/distribution_templated.cc:546-590, in code units).
-   void PrintDistro1D(int distro, int /*ijk*/, const std::string& file_name, bool /*phys_units*/, int problem = 0) const
+   // SimulationMaster::PrintDistro1D / PrintDistro2D / PrintRecords (src/simulation.cc:856-886): the
+   // distribution of one problem in the reference's text layout (DistroLayout).
+   void PrintDistro1D(int distro, int ijk, const std::string& file_name, bool phys_units, int problem = 0) const
    {
-      int64_t nb = 0;
-      int w = 0;
-      check(spx_get_distribution_info(ctx_, problem, distro, &nb, &w), "PrintDistro1D");
-      std::vector<int32_t> counts(nb);
-      std::vector<double> sums(nb * w);
+      std::vector<int32_t> counts;
+      std::vector<double> sums;
       int64_t nev = 0;
-      check(spx_get_distribution(ctx_, problem, distro, counts.data(), sums.data(), &nev), "PrintDistro1D");
-      FILE* f = std::fopen(file_name.c_str(), "w");
-      if (!f) throw std::runtime_error("cannot open " + file_name);
-      for (int64_t i = 0; i < nb; i++)
-         std::fprintf(f, "%8lld %12d %20.12e\n", (long long)i, counts[i], counts[i] ? sums[i * w] / counts[i] : 0.0);
-      std::fclose(f);
+      const DistroLayout L = histogram(distro, problem, counts, sums, nev, "PrintDistro1D");
+      L.Print1D(file_name, counts.data(), sums.data(), nev, ijk, phys_units);
+   }
+   void PrintDistro2D(int distro, int ijk1, int ijk2, const std::string& file_name, bool phys_units, int problem = 0) const
+   {
+      std::vector<int32_t> counts;
+      std::vector<double> sums;
+      int64_t nev = 0;
+      const DistroLayout L = histogram(distro, problem, counts, sums, nev, "PrintDistro2D");
+      L.Print2D(file_name, counts.data(), sums.data(), nev, ijk1, ijk2, phys_units);
+   }
+   // The device appends records in completion order, the reference in trajectory order.
+   void PrintRecords(int distro, const std::string& file_name, bool phys_units, int problem = 0) const
+   {
+      std::vector<double> values, weights;
+      const int64_t n = DistributionRecords(distro, values, weights, problem);
+      layout(distro, (int)(n ? weights.size() / n : width(distro, problem)), "PrintRecords")
+          .PrintRecords(file_name, values.data(), weights.data(), (size_t)n, phys_units);
    }
 
 private:
    int n_problems_ = 0;
    std::vector<int> restore_;
+   std::vector<std::vector<uint8_t>> distro_blobs_;
+
+   int width(int distro, int problem) const
+   {
+      int64_t nb = 0;
+      int w = 0;
+      check(spx_get_distribution_info(ctx_, problem, distro, &nb, &w), "spx_get_distribution_info");
+      return w;
+   }
+   DistroLayout layout(int distro, int w, const char* what) const
+   {
+      DistroLayout L;
+      if (distro < 0 || distro >= (int)distro_blobs_.size() ||
+          !L.Read(distro_blobs_[distro].data(), distro_blobs_[distro].size(), w))
+         throw std::runtime_error(std::string(what) + ": not a distribution of this simulation");
+      return L;
+   }
+   DistroLayout histogram(int distro, int problem, std::vector<int32_t>& counts, std::vector<double>& sums, int64_t& nev,
+                          const char* what) const
+   {
+      int64_t nb = 0;
+      int w = 0;
+      check(spx_get_distribution_info(ctx_, problem, distro, &nb, &w), what);
+      counts.assign((size_t)nb, 0);
+      sums.assign((size_t)nb * w, 0.0);
+      check(spx_get_distribution(ctx_, problem, distro, counts.data(), sums.data(), &nev), what);
+      return layout(distro, w, what);
+   }
 };
 
 }  // namespace spx

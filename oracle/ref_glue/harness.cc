@@ -19,7 +19,7 @@
  *   per distribution: u32 n_bins, u32 width, i32 counts[n_bins], f64 sums[n_bins*width],
  *                     i32 n_events
  * With a third argument, each distribution is also written by its own Dump() to
- * <dump_prefix><index>.out.
+ * <dump_prefix><index>.out, and by its Print1D, Print2D and PrintRecords.
  */
 #include <chrono>
 #include <cstdio>
@@ -305,9 +305,22 @@ int main(int argc, char** argv)
          Put<int32_t>(out, distros[d]->NEvents());
       }
       std::fclose(out);
-      // the reference's own dump files, named as its simulation names them (src/simulation.cc:790-793)
+      // the reference's own dump files, named as its simulation names them (src/simulation.cc:790-793),
+      // and its text output of each distribution: Print1D of every axis, Print2D of every pair, PrintRecords,
+      // each in code and in physical units (<prefix><d>.p1d<k>[u], .p2d<k1><k2>[u], .prec[u])
       if (argc > 3)
-         for (size_t d = 0; d < distros.size(); d++) distros[d]->Dump(std::string(argv[3]) + std::to_string(d) + ".out");
+         for (size_t d = 0; d < distros.size(); d++) {
+            const std::string base = std::string(argv[3]) + std::to_string(d);
+            distros[d]->Dump(base + ".out");
+            for (int u = 0; u < 2; u++) {
+               const std::string us = u ? "u" : "";
+               for (int k = 0; k < 3; k++) distros[d]->Print1D(k, base + ".p1d" + std::to_string(k) + us, u);
+               for (int k1 = 0; k1 < 3; k1++)
+                  for (int k2 = k1 + 1; k2 < 3; k2++)
+                     distros[d]->Print2D(k1, k2, base + ".p2d" + std::to_string(k1) + std::to_string(k2) + us, u);
+               distros[d]->PrintRecords(base + ".prec" + us, u);
+            }
+         }
       std::fprintf(stderr, "harness: %u trajectories, %llu steps, %.3f s\n", n_traj,
                    (unsigned long long)total_steps, secs);
    }

@@ -2,7 +2,7 @@
 
 The method names and argument meanings are those of SimulationWorker (src/simulation.hh:93-138):
 Add{Background,Diffusion,Source,Boundary,Initial,Distribution}(prototype, container), SetTasks,
-MainLoop, PrintDistro1D, RestoreDistro, DistroFileName, GetTrajectoryName. Instead of an MPI farm
+MainLoop, PrintDistro1D, PrintDistro2D, PrintRecords, RestoreDistro, DistroFileName, GetTrajectoryName. Instead of an MPI farm
 the trajectories run in one device launch; SetTasks may be called several times to batch many
 problems, each optionally replacing plugins of the base set (``AddProblem``).
 
@@ -15,7 +15,7 @@ import struct
 
 import numpy as np
 
-from . import capi
+from . import capi, distro_print
 from . import plugins as P
 from .datacontainer import DataContainer
 from .problem import TRAJ_NAMES, Problem
@@ -31,6 +31,10 @@ class SimulationGPU:
         for k, v in (options or {}).items():
             self.ctx.set_option(k, v)
         self._distro_names: list[str] = []
+        # each distribution's parameter container, and per problem the ones AddProblem replaced (the
+        # text output reads the binning from them)
+        self._distro_blobs: list[bytes] = []
+        self._problem_distro_blobs: list[dict[int, bytes]] = []
         self._file_prefix = ""
         self._restore: set[int] = set()
         self._n_problems = 0
@@ -43,6 +47,7 @@ class SimulationGPU:
         self.ctx.add_plugin(role, proto.kind, container.data(), container.size())
         if role == P.ROLE_DISTRIBUTION:
             self._distro_names.append(proto.name)
+            self._distro_blobs.append(container.data())
 
     def AddBackground(self, proto, container, fname_pattern_in: str = ""):  # noqa: N802
         self._add(P.ROLE_BACKGROUND, proto, container)
@@ -72,15 +77,20 @@ class SimulationGPU:
         """One problem of n_traj trajectories (batch sizes belong to the MPI farm and are ignored)."""
         self.ctx.add_problem(n_traj, seed)
         self._n_problems += 1
+        self._problem_distro_blobs.append({})
 
     def AddProblem(self, n_traj: int, seed: int, overrides=()):  # noqa: N802
         """A further problem: ``overrides`` is a list of (role, slot, prototype, DataContainer)."""
         blob = bytearray()
+        replaced = {}
         for role, slot, proto, c in overrides:
             data = c.data()
             blob += struct.pack("<5I", role, slot, proto.kind, c.size(), len(data)) + data
+            if role == P.ROLE_DISTRIBUTION:
+                replaced[slot] = data
         self.ctx.add_problem(n_traj, seed, bytes(blob))
         self._n_problems += 1
+        self._problem_distro_blobs.append(replaced)
 
     def MainLoop(self, tuning: capi.Tuning | None = None) -> capi.Stats:  # noqa: N802
         """Restore the distributions flagged by RestoreDistro, run every problem's trajectories, and,
@@ -126,15 +136,32 @@ class SimulationGPU:
     def distribution(self, distro: int, problem: int = 0):
         return self.ctx.distribution(problem, distro)
 
+    def _distro_header(self, distro: int, problem: int) -> distro_print.DistroHeader:
+        blob = self._problem_distro_blobs[problem].get(distro, self._distro_blobs[distro]) \
+            if problem < len(self._problem_distro_blobs) else self._distro_blobs[distro]
+        _, width = self.ctx.distribution_info(problem, distro)
+        return distro_print.DistroHeader.from_container(blob, width)
+
     def PrintDistro1D(self, distro: int, ijk: int, file_name: str, phys_units: bool = False, problem: int = 0) -> None:  # noqa: N802
-        """Write bin index, count and mean weight per bin along axis ``ijk`` (summed over the others),
-        the columns of DistributionTemplated::Print1D (src/distribution_templated.cc:546-590) in
-        code units."""
-        counts, sums, _ = self.distribution(distro, problem)
-        nb, _ = self.ctx.distribution_info(problem, distro)
-        with open(file_name, "w") as f:
-            for i, (c, s) in enumerate(zip(counts, sums[:, 0])):
-                f.write(f"{i:8d} {c:12d} {s / c if c else 0.0:20.12e}\n")
+        """The distribution along axis ``ijk``, the other two collapsed, in the text layout of
+        DistributionTemplated::Print1D (SimulationMaster::PrintDistro1D, src/simulation.cc:856-859)."""
+        counts, sums, n_events = self.distribution(distro, problem)
+        distro_print.print_1d(file_name, self._distro_header(distro, problem), counts, sums, n_events, ijk, phys_units)
+
+    def PrintDistro2D(self, distro: int, ijk1: int, ijk2: int, file_name: str, phys_units: bool = False,  # noqa: N802
+                      problem: int = 0) -> None:
+        """The distribution over axes ``ijk1`` and ``ijk2``, the third collapsed, in the text layout of
+        DistributionTemplated::Print2D (SimulationMaster::PrintDistro2D, src/simulation.cc:871-874)."""
+        counts, sums, n_events = self.distribution(distro, problem)
+        distro_print.print_2d(file_name, self._distro_header(distro, problem), counts, sums, n_events, ijk1, ijk2,
+                              phys_units)
+
+    def PrintRecords(self, distro: int, file_name: str, phys_units: bool = False, problem: int = 0) -> None:  # noqa: N802
+        """The records of a distribution that keeps them, in the text layout of
+        DistributionTemplated::PrintRecords (SimulationMaster::PrintRecords, src/simulation.cc:883-886).
+        The device appends records in completion order; the reference in trajectory order."""
+        values, weights, _ = self.ctx.distribution_records(problem, distro)
+        distro_print.print_records(file_name, self._distro_header(distro, problem), values, weights, phys_units)
 
     def close(self) -> None:
         self.ctx.close()
@@ -183,9 +210,11 @@ def open_problems(problems: list[Problem] | Problem, precision: int = capi.SPX_F
     for e in base.plugins:
         if e.plugin.role == P.ROLE_DISTRIBUTION:
             sim._distro_names.append(e.plugin.name)
+            sim._distro_blobs.append(e.blob)
     for p in problems:
         sim.ctx.add_problem(p.n_traj, p.seed, _diff_overrides(base, p))
         sim._n_problems += 1
+        sim._problem_distro_blobs.append({k: e.blob for k, e in enumerate(p.distributions())})
     return sim
 
 

@@ -12,6 +12,7 @@ including where the sources are not.
     python tests/golden/make_golden.py NAME...  # rewrites the named fixtures only
     python tests/golden/make_golden.py --dumps  # rewrites tests/golden/*.distro<d>.out
     python tests/golden/make_golden.py --grid   # rewrites tests/golden/grid_blocks_ref.npz
+    python tests/golden/make_golden.py --prints # rewrites tests/golden/distro_prints_ref.npz
 
 The second form keeps the reference's own distribution dump files (DistributionTemplated::Dump)
 of the fixtures whose distributions have at most DUMP_MAX_BINS bins: the pins of the dump format.
@@ -238,6 +239,33 @@ def write_dumps():
                 print(f"{name}.distro{d}.out: {len(data)} bytes")
 
 
+PRINT_KINDS = [f"p1d{k}{u}" for u in ("", "u") for k in range(3)] + \
+    [f"p2d{a}{b}{u}" for u in ("", "u") for a, b in ((0, 1), (0, 2), (1, 2))] + ["prec", "precu"]
+
+
+def write_prints():
+    """The reference's text output of the same distributions (Print1D of every axis, Print2D of every
+    pair, PrintRecords; code and physical units), as oracle/_ref's harness writes it beside the dumps,
+    into one compressed archive: distro_prints_ref.npz, key <case>.distro<d>.<kind>."""
+    import tempfile
+
+    import oracle_tools as ot
+    out = {}
+    for name, pb in cases():
+        with tempfile.TemporaryDirectory() as td:
+            pre = os.path.join(td, "distro")
+            ref = ot.run_reference(pb, dump_prefix=pre)
+            for d, (counts, _, _) in enumerate(ref.distros):
+                if len(counts) > DUMP_MAX_BINS:
+                    continue
+                for kind in PRINT_KINDS:
+                    with open(f"{pre}{d}.{kind}", "rb") as f:
+                        out[f"{name}.distro{d}.{kind}"] = np.frombuffer(f.read(), dtype=np.uint8)
+    path = os.path.join(HERE, "distro_prints_ref.npz")
+    np.savez_compressed(path, **out)
+    print(f"distro_prints_ref: {len(out)} files, {os.path.getsize(path)} bytes")
+
+
 def write_grid():
     """Fields and gradients of the reference's Cartesian data server (oracle/_ref/ref_grid0) at the
     probe points of tests/test_oracle_grid_blocks.py, with the grid they were computed on."""
@@ -265,6 +293,9 @@ def main():
         return
     if "--grid" in args:
         write_grid()
+        return
+    if "--prints" in args:
+        write_prints()
         return
     import oracle_tools as ot
     for name, pb in cases():

@@ -188,8 +188,10 @@ GOLDEN_DIR = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 
 def golden_names():
-    # trajectory fixtures (the grid fixture holds fields at points, test_oracle_grid_blocks.py)
-    return sorted(f[:-4] for f in os.listdir(GOLDEN_DIR) if f.endswith(".npz") and not f.startswith("grid_"))
+    # trajectory fixtures (the grid fixture holds fields at points, test_oracle_grid_blocks.py; the
+    # print fixture the reference's text output of distributions, test_distro_print.py)
+    return sorted(f[:-4] for f in os.listdir(GOLDEN_DIR)
+                  if f.endswith(".npz") and not f.startswith(("grid_", "distro_prints_")))
 
 
 def load_golden(name: str):
