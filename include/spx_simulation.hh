@@ -198,6 +198,34 @@ SPX_PROTOTYPE(DistributionAnisotropyLISM, DistributionBase, 11)  // Lorentz traj
 SPX_PROTOTYPE(DistributionTimeMu, DistributionBase, 20)  // extension: no reference class
 #undef SPX_PROTOTYPE
 
+// ---- the data files of the Cartesian server -------------------------------------------------------
+// What BackgroundServerCartesian's server reads for the file-name pattern it is given: the reader's blocks
+// (4^3 zones of six fluid-unit numbers each, blocks x fastest) from <pattern>.out, and the header from the
+// same name with its last four characters replaced by ".info": blocks per axis, domain minimum and
+// maximum, variables per zone (ServerCartesianBack::ServerStart, src/server_cartesian.cc:931-933;
+// ReadCartesianHeader and ReadCartesianData, src/reader_cartesian.cc:30-133).
+struct CartesianData {
+   int32_t n_blocks[3] = {0, 0, 0};
+   double domain_min[3] = {0, 0, 0}, domain_max[3] = {0, 0, 0};
+   std::vector<double> values;
+
+   // false on a missing or short file, or a header that does not give six variables per zone
+   bool Read(const std::string& data_file)
+   {
+      if (data_file.size() < 4) return false;
+      std::ifstream header((data_file.substr(0, data_file.size() - 4) + ".info").c_str());
+      int nvar = 0;
+      header >> n_blocks[0] >> n_blocks[1] >> n_blocks[2] >> domain_min[0] >> domain_min[1] >> domain_min[2] >>
+          domain_max[0] >> domain_max[1] >> domain_max[2] >> nvar;
+      if (!header || nvar != 6 || n_blocks[0] < 1 || n_blocks[1] < 1 || n_blocks[2] < 1) return false;
+      const size_t n = (size_t)n_blocks[0] * n_blocks[1] * n_blocks[2] * 64 * 6;
+      values.assign(n, 0.0);
+      std::ifstream data(data_file.c_str(), std::ios::binary);
+      data.read(reinterpret_cast<char*>(values.data()), (std::streamsize)(n * sizeof(double)));
+      return (bool)data;
+   }
+};
+
 // ---- text output of a distribution ---------------------------------------------------------------
 // DistributionTemplated::Print1D, Print2D and PrintRecords (src/distribution_templated.cc:472-686),
 // written from a distribution's parameter container, histogram and records. The binning is
@@ -363,9 +391,24 @@ public:
    spx_ctx_t context(void) const { return ctx_; }
    void SetOption(int option, double value) { check(spx_set_option(ctx_, option, value), "spx_set_option"); }
 
-   // src/simulation.hh:105-123
-   void AddBackground(const BackgroundBase& p, const DataContainer& c, const std::string& = "")
-   { add(SPX_ROLE_BACKGROUND, p.kind, c, "AddBackground"); }
+   // src/simulation.hh:105-123. With a file-name pattern a BackgroundServerCartesian reads its data as the
+   // reference's server does (CartesianData); ghost_cells stands for the build's SERVER_NUM_GHOST_CELLS.
+   void AddBackground(const BackgroundBase& p, const DataContainer& c, const std::string& fname_pattern = "",
+                      int ghost_cells = 0)
+   {
+      add(SPX_ROLE_BACKGROUND, p.kind, c, "AddBackground");
+      if (!fname_pattern.empty() && p.kind == BackgroundServerCartesian().kind) {
+         CartesianData d;
+         if (!d.Read(fname_pattern + ".out")) throw std::runtime_error("AddBackground: cannot read " + fname_pattern + ".out");
+         SetBackgroundBlocks(d.n_blocks, d.domain_min, d.domain_max, ghost_cells, d.values.data());
+      }
+   }
+   // The reader's blocks of a BackgroundServerCartesian background (spx_set_background_blocks).
+   void SetBackgroundBlocks(const int32_t n_blocks[3], const double domain_min[3], const double domain_max[3],
+                            int ghost_cells, const double* values)
+   {
+      check(spx_set_background_blocks(ctx_, n_blocks, domain_min, domain_max, ghost_cells, values), "SetBackgroundBlocks");
+   }
    // The block of a BackgroundServerCartesian background (six values per node: U, B; x fastest),
    // in place of the data files the reference's server reads.
    void SetBackgroundGrid(const int64_t n[3], const double cent_min[3], const double zone_length[3], const double* values)

@@ -77,8 +77,9 @@ class BlockGrid:
 
     @classmethod
     def read(cls, dat_path: str, ghost_cells: int = 0) -> "BlockGrid":
-        """The reader's pair of files: the binary block data ``name.dat`` and its text header
-        ``name.info`` (blocks per axis, domain minimum, domain maximum, variables per zone)."""
+        """The reader's pair of files: the binary block data ``name.dat`` (the server reads
+        ``<pattern>.out``) and its text header ``name.info``, the data file's name with its last four
+        characters replaced (blocks per axis, domain minimum, domain maximum, variables per zone)."""
         import numpy as np
         with open(dat_path[:-4] + ".info") as f:
             tok = f.read().split()

@@ -49,8 +49,16 @@ class SimulationGPU:
             self._distro_names.append(proto.name)
             self._distro_blobs.append(container.data())
 
-    def AddBackground(self, proto, container, fname_pattern_in: str = ""):  # noqa: N802
+    def AddBackground(self, proto, container, fname_pattern_in: str = "", ghost_cells: int = 0):  # noqa: N802
+        """With a file-name pattern, a BackgroundServerCartesian reads its data as the reference's server
+        does: the reader's blocks from <pattern>.out and their header from <pattern>.info
+        (ServerCartesianBack::ServerStart, src/server_cartesian.cc:931-933, and ReadCartesianHeader,
+        src/reader_cartesian.cc:36). ``ghost_cells`` stands for the build's SERVER_NUM_GHOST_CELLS."""
         self._add(P.ROLE_BACKGROUND, proto, container)
+        if fname_pattern_in and proto.name == "BackgroundServerCartesian":
+            from .problem import BlockGrid
+            g = BlockGrid.read(fname_pattern_in + ".out", ghost_cells)
+            self.ctx.set_background_blocks(g.n_blocks, g.domain_min, g.domain_max, g.ghost_cells, g.values)
 
     def SetBackgroundGrid(self, grid) -> None:  # noqa: N802
         """The block of a BackgroundServerCartesian background (a problem.Grid); takes the place of

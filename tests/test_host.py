@@ -208,3 +208,57 @@ def test_cpp_host_mirror_has_every_plugin_class():
     for num, name in TRAJ_NAMES.items():
         assert re.search(rf"#define SPX_TRAJ_\w+ {num}\b", hdr), num
         assert f'return "{name}";' in src, name
+
+
+def test_server_data_files_read_by_both_mirrors(tmp_path):
+    """AddBackground(BackgroundServerCartesian(), container, pattern) reads <pattern>.out and
+    <pattern>.info as the reference's server does: the C++ mirror's CartesianData and the Python
+    mirror's BlockGrid.read give the blocks the files hold, and the Python mirror hands them to
+    spx_set_background_blocks."""
+    import shutil
+    import subprocess
+    import numpy as np
+    from spectrum_gb300.datacontainer import DataContainer as DC
+    from spectrum_gb300.plugins import BackgroundServerCartesian
+    from spectrum_gb300.problem import BlockGrid
+    from spectrum_gb300.simulation import SimulationGPU
+    rng = np.random.default_rng(5)
+    g = BlockGrid((2, 3, 1), (-1.5, -0.25, 0.1), (2.0, 3.0, 0.7), rng.normal(size=(6, 64, 6)), 0)
+    pattern = str(tmp_path / "parker_2_3_1")
+    g.write(pattern + ".out")
+
+    calls = []
+
+    class Ctx:
+        def add_plugin(self, *a):
+            pass
+
+        def set_background_blocks(self, *a):
+            calls.append(a)
+
+    sim = SimulationGPU.__new__(SimulationGPU)
+    sim.ctx = Ctx()
+    sim._distro_names, sim._distro_blobs = [], []
+    sim.AddBackground(BackgroundServerCartesian(), DC().double(0.0), pattern, ghost_cells=1)
+    nb, lo, hi, ghost, vals = calls[0]
+    assert tuple(nb) == g.n_blocks and tuple(lo) == g.domain_min and tuple(hi) == g.domain_max and ghost == 1
+    assert np.array_equal(vals, g.values)
+
+    gxx = shutil.which("g++")
+    if gxx is None:
+        pytest.skip("no g++")
+    src = tmp_path / "rd.cc"
+    src.write_text('#include <cstdio>\n#include "spx_simulation.hh"\n'
+                   'int main(int, char** argv) { spx::CartesianData d; if (!d.Read(argv[1])) return 3;\n'
+                   '  FILE* f = std::fopen(argv[2], "wb"); std::fwrite(d.n_blocks, 4, 3, f);\n'
+                   '  std::fwrite(d.domain_min, 8, 3, f); std::fwrite(d.domain_max, 8, 3, f);\n'
+                   '  std::fwrite(d.values.data(), 8, d.values.size(), f); std::fclose(f); return 0; }\n')
+    exe = str(tmp_path / "rd")
+    subprocess.run([gxx, "-std=c++17", "-I", os.path.join(ROOT, "include"), str(src), "-o", exe], check=True)
+    subprocess.run([exe, pattern + ".out", str(tmp_path / "o.bin")], check=True)
+    raw = open(tmp_path / "o.bin", "rb").read()
+    assert np.array_equal(np.frombuffer(raw[:12], "<i4"), g.n_blocks)
+    assert np.array_equal(np.frombuffer(raw[12:36], "<f8"), g.domain_min)
+    assert np.array_equal(np.frombuffer(raw[36:60], "<f8"), g.domain_max)
+    assert np.array_equal(np.frombuffer(raw[60:], "<f8").reshape(g.values.shape), g.values)
+    assert subprocess.run([exe, str(tmp_path / "missing.out"), str(tmp_path / "x")]).returncode == 3
