@@ -101,7 +101,7 @@ extern "C" {
                                        autotuner's timing samples do: a steady-state throughput sample with no drain
                                        of the queue; trajectories stopped by the cap are neither finished nor binned */
 /* plugin kinds: see spectrum_gb300/plugins.py; e.g. background 1 uniform, 3 smooth shock,
- * 4 dipole, 5 solar wind; diffusion 5 full constant, 8 rigidity/field power law; boundary
+ * 4 dipole, 5 solar wind, 7 discontinuity, 8 smooth discontinuity; diffusion 5 full constant, 8 rigidity/field power law; boundary
  * 1 time expire, 10 plane absorb, 14 sphere absorb, 30 momentum inject; distribution 2 position
  * uniform, 5 kinetic-energy power-law spectrum. */
 
